@@ -1,0 +1,168 @@
+/*
+ * nr.h -- C ABI of the GB300 two-terminal network reliability engine.
+ *
+ * The engine computes R(G; s, t), the probability that terminal t can be
+ * reached from terminal s when every edge works independently with its own
+ * probability, by the path-decomposition (factoring) method of
+ * fmalazemi/relaibilityGPU.  It returns the same result block as the
+ * reference's `network_reliability` program (workingPad/main.cu:1037-1056):
+ * R, R + ESP, ESP, the truncation bound, paths enumerated, nodes processed,
+ * kernel iterations and the largest queue.
+ *
+ * The reference has no library interface: its only caller is its own
+ * command-line driver (workingPad/main.cu:795-1072).  Each entry point below
+ * names the reference code it stands in for.  Plain C types only; no CUDA or
+ * torch type appears in a signature.
+ *
+ * Status codes: every entry point returns NR_OK (0) or a negative NR_ERR_*;
+ * nothing calls exit() (the reference exits on errors, common.h:39-46,
+ * graph.h:49-69).  Calls on one nr_context are not re-entrant; separate
+ * contexts may be used from separate threads.
+ */
+#ifndef NR_H
+#define NR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NR_ABI_VERSION 1
+
+/* status codes */
+enum {
+    NR_OK              = 0,
+    NR_ERR_INVALID     = -1,   /* bad argument (terminal out of range, null pointer, ...) */
+    NR_ERR_IO          = -2,   /* graph file missing or unreadable */
+    NR_ERR_PARSE       = -3,   /* malformed graph file */
+    NR_ERR_UNSUPPORTED = -4,   /* graph outside the engine's limits */
+    NR_ERR_CUDA        = -5,   /* CUDA runtime error (no device, launch failure, ...) */
+    NR_ERR_NOMEM       = -6,   /* device or host allocation failed */
+    NR_ERR_TIMEOUT     = -7,   /* a bounded device-side wait gave up */
+    NR_ERR_INTERNAL    = -8    /* a device-side consistency check failed */
+};
+
+/* edge states in a subproblem mask: 2 bits per edge id, edge e at word e/16,
+ * bits 2*(e%16)..+1 (workingPad/common.h:22-24). */
+enum { NR_EDGE_DOWN = 0, NR_EDGE_UP = 1, NR_EDGE_UNKNOWN = 3 };
+
+/* Graph in the reference loader's host form (workingPad/graph.h:12-27):
+ * CSR arcs in adjacency-list order, an edge id per arc, a probability per
+ * edge id.  Undirected graphs list every edge in both endpoint lists with
+ * the same id.  The caller owns all arrays. */
+typedef struct nr_graph {
+    int32_t        n_nodes;
+    int32_t        n_edges;     /* distinct edge ids 0..n_edges-1 */
+    int32_t        n_arcs;      /* CSR entries */
+    const int32_t *row_ptr;     /* [n_nodes + 1] */
+    const int32_t *col_idx;     /* [n_arcs] */
+    const int32_t *edge_id;     /* [n_arcs] */
+    const double  *edge_p;      /* [n_edges], FP64 */
+} nr_graph;
+
+/* queue order */
+enum {
+    NR_ORDER_AUTO    = 0,   /* waves for exhaustive runs, max-mass buckets when a target width is set */
+    NR_ORDER_WAVES   = 1,   /* breadth-first waves, as the reference's ping-pong queue (main.cu:963-1008) */
+    NR_ORDER_MAXMASS = 2,   /* bucketed max-mass priority queue */
+    NR_ORDER_LEARNED = 3    /* bucket key and branch order from the learned scorer (never mass) */
+};
+
+typedef struct nr_options {
+    double   truncation_eps;  /* popped mass below eps goes to ESP (main.cu:537-543); 0 = off.
+                                 The reference CLI default is 1e-15. */
+    double   target_width;    /* stop once ESP + queued mass <= target; 0 = run to empty queue */
+    int32_t  order;           /* NR_ORDER_* */
+    int32_t  bucket_shift;    /* max-mass order: 2^shift buckets per factor of two in mass */
+    int32_t  n_buckets;       /* max-mass order: bucket count; the last takes all smaller masses */
+    int32_t  device;          /* CUDA device ordinal */
+    int32_t  blocks_per_sm;   /* 0 = occupancy maximum */
+    int32_t  warps_per_block; /* 0 = engine default */
+    double   timeout_ms;      /* device-side waits give up after this long without progress; 0 = 60 s */
+    int32_t  verbose;         /* 1: print the reference's preamble lines on stdout */
+    int32_t  reserved[7];
+} nr_options;
+
+typedef struct nr_result {
+    double   R;                 /* reliability found: sum of all-up path masses */
+    double   R_plus_esp;        /* upper bound */
+    double   esp;               /* ESP: eps-truncated + spilled + still-queued mass */
+    double   trunc_bound;       /* esp / R when R > 0 (main.cu:1047-1048) */
+    uint64_t paths;             /* all-up leaves + queue-overflow spills (main.cu:251,262) */
+    uint64_t nodes;             /* subproblems popped, dead ends and truncated ones included (main.cu:533) */
+    uint64_t leaves;
+    uint64_t dead_ends;
+    uint64_t truncated;
+    uint64_t spilled;
+    uint64_t queued;            /* subproblems left in the queue when a target width stopped the run */
+    int32_t  iterations;        /* waves (kernel iterations in the reference) */
+    int32_t  n_nodes;           /* echo of the graph */
+    int32_t  n_edges;
+    int32_t  src, dst;
+    int32_t  mask_words;
+    uint64_t max_queue_items;   /* largest wave */
+    double   max_queue_mb;      /* largest wave x bytes per queued subproblem */
+    double   ms;                /* device time of the solve (CUDA events) */
+    double   time_to_bound_ms;  /* device time until the target width was met (0 if no target) */
+    int32_t  engine;            /* which engine ran (NR_ENGINE_*) */
+    int32_t  grid_blocks;
+    int32_t  block_threads;
+    int32_t  item_bytes;        /* bytes per queued subproblem in HBM */
+    uint64_t capacity;          /* queue capacity actually used (items) */
+    uint64_t h2d_bytes;         /* host -> device bytes copied by this call */
+    uint64_t d2h_bytes;         /* device -> host bytes copied by this call */
+    int32_t  reserved[4];
+} nr_result;
+
+enum { NR_ENGINE_GRID = 1, NR_ENGINE_WARP = 2 };
+
+typedef struct nr_context nr_context;
+
+/* Defaults: eps 0 (exact), no target, NR_ORDER_AUTO, shift 2, 256 buckets, device 0. */
+void        nr_options_default(nr_options *opt);
+const char *nr_status_string(int status);
+int         nr_abi_version(void);
+
+/* Parse a reference graph file ("N E [U|D]" then N lines "deg (nbr p)*").
+ * Replaces graph_load (workingPad/graph.h:46-145) without its exit() paths;
+ * also accepts files whose header has no type character (the test_*.txt
+ * files).  Edge ids are first-seen (min,max) pairs (graph.h:77-90).
+ * Arrays are malloc'd into *out; release with nr_graph_free. */
+int  nr_graph_load(const char *path, nr_graph *out);
+void nr_graph_free(nr_graph *g);
+
+/* Initial mask of a graph: all UNKNOWN, p<=0 DOWN, p>=1 UP
+ * (workingPad/main.cu:717-748). words must hold ceil(2E/32) entries. */
+int  nr_initial_mask(const nr_graph *g, uint32_t *words, int n_words);
+
+/* Reusable device state (queue buffers, stream, events). */
+int  nr_context_create(int device, nr_context **out);
+void nr_context_destroy(nr_context *ctx);
+
+/* Solve one instance. capacity = queue capacity in subproblems per wave
+ * buffer (the reference's --queue_capacity, main.cu:781-782); 0 picks the
+ * reference default 1048576.  Replaces the body of main()
+ * (workingPad/main.cu:800-1056): graph_to_device, queue_pair_init, the wave
+ * loop over factoring_kernel, and the stats readback. opt may be NULL. */
+int  nr_reliability(const nr_graph *g, int src, int dst, uint64_t capacity,
+                    const nr_options *opt, nr_result *res);
+int  nr_reliability_ctx(nr_context *ctx, const nr_graph *g, int src, int dst, uint64_t capacity,
+                        const nr_options *opt, nr_result *res);
+
+/* Solve many instances in one persistent launch (no reference counterpart:
+ * the reference runs one graph per process). Instances that outgrow the
+ * per-warp queue are finished by the whole-GPU engine. */
+int  nr_reliability_batch(nr_context *ctx, int n_instances, const nr_graph *graphs,
+                          const int32_t *srcs, const int32_t *dsts, uint64_t capacity,
+                          const nr_options *opt, nr_result *results);
+
+/* The reference's result block (workingPad/main.cu:1037-1056) as text.
+ * Returns the number of characters written (snprintf semantics). */
+int  nr_format_result(const nr_result *res, char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NR_H */

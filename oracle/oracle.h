@@ -1,0 +1,110 @@
+/*
+ * oracle.h -- CPU oracle for two-terminal network reliability by path
+ * decomposition.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA engine, the
+ * C ABI in include/nr.h, the CLI) links or calls this code.  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the
+ * checker and as the timed CPU port of the reference algorithm.
+ *
+ * What it restates (paths relative to the fmalazemi/relaibilityGPU tree):
+ *   graph file + edge ids ..... workingPad/graph.h:46-145 (first-seen (min,max)
+ *                               pair order while scanning nodes in order)
+ *   initial mask .............. workingPad/main.cu:717-748
+ *   BFS, parent rule "level" .. workingPad/device_code.cuh:80-194 (bitmask
+ *                               frontier scanned in ascending node order, so
+ *                               parent[v] = smallest frontier node with a
+ *                               not-down arc to v)
+ *   BFS, parent rule "fifo" ... seq/seq.cpp:311-351 (FIFO queue, first
+ *                               discoverer, early exit at t)
+ *   branching ................. workingPad/main.cu:114-283 and
+ *                               seq/seq.cpp:539-578 (child k = first k-1
+ *                               UNKNOWN path edges up, k-th down, src side
+ *                               first; all-up mass -> R)
+ *   counts .................... workingPad/main.cu:533-534 (every pop is a
+ *                               node), :251 and :262 (overflow spills and
+ *                               leaves are paths); seq/seq.cpp:551-561
+ *                               (pre-push connectivity check)
+ *   eps truncation ............ workingPad/main.cu:537-543
+ *   max-mass order ............ seq/seq.cpp:49-197
+ *   brute force ............... 2^E state enumeration (definition of R)
+ *
+ * Masses are FP64 products in path order (not log sums) and every sum is
+ * compensated (two-sum), so R is accurate to ~1e-16 relative.
+ */
+#ifndef NR_ORACLE_H
+#define NR_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct og_graph {
+    int32_t n_nodes;
+    int32_t n_edges;
+    int32_t n_arcs;
+    const int32_t *row_ptr;   /* n_nodes + 1 */
+    const int32_t *col_idx;   /* n_arcs */
+    const int32_t *edge_id;   /* n_arcs */
+    const double  *edge_p;    /* n_edges */
+} og_graph;
+
+enum { OG_BFS_LEVEL = 0, OG_BFS_FIFO = 1 };
+enum { OG_ORDER_WAVES = 0, OG_ORDER_HEAP = 1, OG_ORDER_DFS = 2 };
+
+typedef struct og_opts {
+    int32_t  bfs_rule;      /* OG_BFS_LEVEL (GPU engine, main.cu) or OG_BFS_FIFO (seq.cpp) */
+    int32_t  precheck;      /* 1: drop disconnected children before queueing (seq.cpp) */
+    int32_t  order;         /* OG_ORDER_* */
+    int32_t  bucket_shift;  /* waves: 2^shift mass buckets per octave; < 0: one bucket */
+    int32_t  n_buckets;     /* waves: number of buckets (the last one takes all smaller masses) */
+    int32_t  threads;       /* waves: worker threads (>= 1) */
+    double   eps;           /* popped mass < eps goes to ESP unexpanded; 0 disables */
+    double   target_width;  /* waves/heap: stop once ESP + queued mass <= target; 0 disables */
+    uint64_t capacity;      /* queued-item limit, overflow spills to ESP; 0 = unlimited */
+    uint64_t max_nodes;     /* stop after about this many pops (timing samples); 0 = none */
+} og_opts;
+
+typedef struct og_result {
+    double   R;             /* reliability found (sum of all-up leaf masses) */
+    double   esp;           /* spilled + eps-truncated + still-queued mass */
+    double   esp_spilled;
+    double   esp_truncated;
+    double   queued_mass;
+    uint64_t paths;         /* leaves + overflow spills (main.cu:251,262) */
+    uint64_t nodes;         /* pops, including dead ends and truncated items */
+    uint64_t leaves;
+    uint64_t dead;          /* pops whose optimistic BFS fails */
+    uint64_t truncated;     /* pops below eps */
+    uint64_t spilled;       /* children that did not fit */
+    uint64_t pruned;        /* children dropped by the pre-push check */
+    uint64_t pushes;
+    uint64_t waves;
+    uint64_t max_wave;
+    uint64_t max_queued;
+    uint64_t queued;        /* items left in the queue at the end */
+    int32_t  status;        /* 0 done, 1 target width reached, 2 max_nodes reached, <0 error */
+    double   seconds;
+} og_result;
+
+/* Parse the reference graph file format: "N E [U|D]" then N lines "deg (nbr p)*".
+ * Arrays are malloc'd; release with og_free_graph. Returns 0 or a negative error. */
+int  og_load(const char *path, og_graph *g);
+void og_free_graph(og_graph *g);
+
+void og_default_opts(og_opts *o);
+int  og_run(const og_graph *g, int src, int dst, const og_opts *o, og_result *r);
+
+/* Exact R by enumerating the 2^k states of the k edges with 0 < p < 1.
+ * n_nodes <= 64, k <= 30. Returns a negative number on bad input. */
+double og_brute(const og_graph *g, int src, int dst);
+
+/* Bucket index used by the wave schedule (shared definition with the engine). */
+int og_bucket(double mass, int shift, int n_buckets);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

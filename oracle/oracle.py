@@ -1,0 +1,143 @@
+"""ctypes wrapper of the CPU oracle (oracle/pathdecomp.c).
+
+TEST INFRASTRUCTURE ONLY.  Imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, as the checker and the timed CPU port of the
+reference algorithm.  The engine never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+CLI = os.path.join(HERE, "og_cli")
+
+RULES = {"level": 0, "fifo": 1}
+ORDERS = {"waves": 0, "heap": 1, "dfs": 2}
+
+
+class OgGraph(C.Structure):
+    _fields_ = [("n_nodes", C.c_int32), ("n_edges", C.c_int32), ("n_arcs", C.c_int32),
+                ("row_ptr", C.POINTER(C.c_int32)), ("col_idx", C.POINTER(C.c_int32)),
+                ("edge_id", C.POINTER(C.c_int32)), ("edge_p", C.POINTER(C.c_double))]
+
+
+class OgOpts(C.Structure):
+    _fields_ = [("bfs_rule", C.c_int32), ("precheck", C.c_int32), ("order", C.c_int32),
+                ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("threads", C.c_int32),
+                ("eps", C.c_double), ("target_width", C.c_double), ("capacity", C.c_uint64),
+                ("max_nodes", C.c_uint64)]
+
+
+class OgResult(C.Structure):
+    _fields_ = [("R", C.c_double), ("esp", C.c_double), ("esp_spilled", C.c_double),
+                ("esp_truncated", C.c_double), ("queued_mass", C.c_double),
+                ("paths", C.c_uint64), ("nodes", C.c_uint64), ("leaves", C.c_uint64), ("dead", C.c_uint64),
+                ("truncated", C.c_uint64), ("spilled", C.c_uint64), ("pruned", C.c_uint64),
+                ("pushes", C.c_uint64), ("waves", C.c_uint64), ("max_wave", C.c_uint64),
+                ("max_queued", C.c_uint64), ("queued", C.c_uint64), ("status", C.c_int32),
+                ("seconds", C.c_double)]
+
+
+def build() -> None:
+    """Compile liboracle.so and og_cli with the oracle's Makefile."""
+    r = subprocess.run(["make", "-s", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        L.og_run.argtypes = [C.POINTER(OgGraph), C.c_int, C.c_int, C.POINTER(OgOpts), C.POINTER(OgResult)]
+        L.og_run.restype = C.c_int
+        L.og_brute.argtypes = [C.POINTER(OgGraph), C.c_int, C.c_int]
+        L.og_brute.restype = C.c_double
+        L.og_bucket.argtypes = [C.c_double, C.c_int, C.c_int]
+        L.og_bucket.restype = C.c_int
+        L.og_default_opts.argtypes = [C.POINTER(OgOpts)]
+        L.og_default_opts.restype = None
+        _lib = L
+    return _lib
+
+
+@dataclasses.dataclass
+class OracleResult:
+    R: float
+    esp: float
+    esp_spilled: float
+    esp_truncated: float
+    queued_mass: float
+    paths: int
+    nodes: int
+    leaves: int
+    dead: int
+    truncated: int
+    spilled: int
+    pruned: int
+    pushes: int
+    waves: int
+    max_wave: int
+    max_queued: int
+    queued: int
+    status: int
+    seconds: float
+
+
+class _View:
+    def __init__(self, g):
+        self.row = np.ascontiguousarray(g.row_ptr, dtype=np.int32)
+        self.col = np.ascontiguousarray(g.col_idx, dtype=np.int32)
+        self.eid = np.ascontiguousarray(g.edge_id, dtype=np.int32)
+        self.p = np.ascontiguousarray(g.edge_p, dtype=np.float64)
+        self.c = OgGraph(int(g.n_nodes), int(self.p.shape[0]), int(self.col.shape[0]),
+                         self.row.ctypes.data_as(C.POINTER(C.c_int32)),
+                         self.col.ctypes.data_as(C.POINTER(C.c_int32)),
+                         self.eid.ctypes.data_as(C.POINTER(C.c_int32)),
+                         self.p.ctypes.data_as(C.POINTER(C.c_double)))
+
+
+def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, order: str = "waves",
+        bucket_shift: int = -1, n_buckets: int = 1, threads: int = 1, eps: float = 0.0,
+        target_width: float = 0.0, capacity: int = 0, max_nodes: int = 0) -> OracleResult:
+    v = _View(g)
+    o = OgOpts()
+    lib().og_default_opts(C.byref(o))
+    o.bfs_rule = RULES[rule]
+    o.precheck = int(bool(precheck))
+    o.order = ORDERS[order]
+    o.bucket_shift = int(bucket_shift)
+    o.n_buckets = int(n_buckets)
+    o.threads = int(threads)
+    o.eps = float(eps)
+    o.target_width = float(target_width)
+    o.capacity = int(capacity)
+    o.max_nodes = int(max_nodes)
+    r = OgResult()
+    rc = lib().og_run(C.byref(v.c), int(src), int(dst), C.byref(o), C.byref(r))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the instance ({rc})")
+    return OracleResult(**{f: getattr(r, f) for f, _ in OgResult._fields_})
+
+
+def brute(g, src: int, dst: int) -> float:
+    v = _View(g)
+    r = lib().og_brute(C.byref(v.c), int(src), int(dst))
+    if r < 0:
+        raise ValueError("brute force limits: n_nodes <= 64 and at most 30 uncertain edges")
+    return r
+
+
+def bucket(mass: float, shift: int, n_buckets: int) -> int:
+    return lib().og_bucket(float(mass), int(shift), int(n_buckets))

@@ -1,0 +1,553 @@
+// nr_api.cu -- host side of the C ABI declared in include/nr.h.
+//
+// Replaces the reference driver (workingPad/main.cu:795-1072) and its graph
+// loader (workingPad/graph.h:46-178) with calls that return status codes.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "nr_internal.h"
+
+const void *nr_grid_kernel_ptr_g8(int w4);
+const void *nr_grid_kernel_ptr_g16(int w4);
+const void *nr_grid_kernel_ptr_g32(int w4);
+
+namespace {
+
+#define NR_CUDA_TRY(call)                                                     \
+    do {                                                                      \
+        cudaError_t _e = (call);                                              \
+        if (_e != cudaSuccess) {                                              \
+            nr_last_cuda_error(_e);                                           \
+            return NR_ERR_CUDA;                                               \
+        }                                                                     \
+    } while (0)
+
+thread_local char g_err[256];
+
+void nr_last_cuda_error(cudaError_t e)
+{
+    snprintf(g_err, sizeof(g_err), "%s", cudaGetErrorString(e));
+}
+
+struct KS {
+    double hi = 0, lo = 0;
+    void add(double x)
+    {
+        double t = hi + x;
+        double bp = t - hi;
+        lo += (hi - (t - bp)) + (x - bp);
+        hi = t;
+    }
+    void merge(double h, double l) { add(h); add(l); }
+    double val() const { return hi + lo; }
+};
+
+const void *grid_kernel(int G, int w4)
+{
+    switch (G) {
+    case 8: return nr_grid_kernel_ptr_g8(w4);
+    case 16: return nr_grid_kernel_ptr_g16(w4);
+    case 32: return nr_grid_kernel_ptr_g32(w4);
+    default: return nullptr;
+    }
+}
+
+int group_width(int n)
+{
+    if (n <= 8) return 8;
+    if (n <= 16) return 16;
+    return 32;
+}
+
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+}  // namespace
+
+struct nr_context {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    void *qbuf = nullptr;       // ping-pong wave buffers
+    size_t qbytes = 0;
+    void *sbuf = nullptr;       // blob, counters, barrier, status, partials
+    size_t sbytes = 0;
+    std::mutex mu;
+};
+
+static int ensure(void **buf, size_t *have, size_t need)
+{
+    if (*have >= need && *buf) return NR_OK;
+    if (*buf) cudaFree(*buf);
+    *buf = nullptr;
+    *have = 0;
+    cudaError_t e = cudaMalloc(buf, need);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *buf = nullptr;
+        return (e == cudaErrorMemoryAllocation) ? NR_ERR_NOMEM : NR_ERR_CUDA;
+    }
+    *have = need;
+    return NR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// validation and graph tables
+// ---------------------------------------------------------------------------
+static int validate(const nr_graph *g, int src, int dst)
+{
+    if (!g || g->n_nodes <= 0 || g->n_edges < 0 || g->n_arcs < 0 || !g->row_ptr) return NR_ERR_INVALID;
+    if (g->n_arcs > 0 && (!g->col_idx || !g->edge_id)) return NR_ERR_INVALID;
+    if (g->n_edges > 0 && !g->edge_p) return NR_ERR_INVALID;
+    if (src < 0 || dst < 0 || src >= g->n_nodes || dst >= g->n_nodes) return NR_ERR_INVALID;
+    if (g->row_ptr[0] != 0 || g->row_ptr[g->n_nodes] != g->n_arcs) return NR_ERR_INVALID;
+    for (int u = 0; u < g->n_nodes; ++u)
+        if (g->row_ptr[u + 1] < g->row_ptr[u]) return NR_ERR_INVALID;
+    for (int j = 0; j < g->n_arcs; ++j) {
+        if (g->col_idx[j] < 0 || g->col_idx[j] >= g->n_nodes) return NR_ERR_INVALID;
+        if (g->edge_id[j] < 0 || g->edge_id[j] >= g->n_edges) return NR_ERR_INVALID;
+    }
+    for (int e = 0; e < g->n_edges; ++e)
+        if (std::isnan(g->edge_p[e])) return NR_ERR_INVALID;
+    return NR_OK;
+}
+
+static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *sg, std::vector<unsigned char> *blob)
+{
+    const int n = g->n_nodes, E = g->n_edges;
+    const int W = std::max(1, (2 * E + 31) / 32);
+    sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst;
+    sg->n_in = g->n_arcs;
+    size_t off = 0;
+    sg->off_p = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
+    sg->off_q = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
+    sg->off_eid = (int)off; off = align16(off + sizeof(uint16_t) * 32 * 32);
+    sg->off_start = (int)off; off = align16(off + sizeof(int) * 33);
+    sg->off_list = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
+    sg->blob_bytes = (int)off;
+    blob->assign(off, 0);
+    double *p = reinterpret_cast<double *>(blob->data() + sg->off_p);
+    double *q = reinterpret_cast<double *>(blob->data() + sg->off_q);
+    uint16_t *eid = reinterpret_cast<uint16_t *>(blob->data() + sg->off_eid);
+    int *start = reinterpret_cast<int *>(blob->data() + sg->off_start);
+    uint32_t *list = reinterpret_cast<uint32_t *>(blob->data() + sg->off_list);
+    for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
+    for (int i = 0; i < 32 * 32; ++i) eid[i] = 0xffff;
+    // in-arcs grouped by head node; arc (u -> v) for every CSR entry of u
+    std::vector<int> cnt(n + 1, 0);
+    for (int u = 0; u < n; ++u)
+        for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) cnt[g->col_idx[j] + 1]++;
+    for (int v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
+    for (int v = 0; v <= n; ++v) start[v] = cnt[v];
+    std::vector<int> fill(n, 0);
+    for (int u = 0; u < n; ++u)
+        for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
+            const int v = g->col_idx[j], e = g->edge_id[j];
+            list[start[v] + fill[v]++] = ((uint32_t)e << 8) | (uint32_t)u;
+            if (eid[u * 32 + v] == 0xffff) eid[u * 32 + v] = (uint16_t)e;   // first arc u->v in CSR order
+        }
+}
+
+extern "C" int nr_initial_mask(const nr_graph *g, uint32_t *words, int n_words)
+{
+    if (!g || !words || g->n_edges < 0) return NR_ERR_INVALID;
+    const int W = std::max(1, (2 * g->n_edges + 31) / 32);
+    if (n_words < W) return NR_ERR_INVALID;
+    for (int i = 0; i < n_words; ++i) words[i] = 0;
+    for (int e = 0; e < g->n_edges; ++e) {
+        const double p = g->edge_p[e];
+        uint32_t st = (p <= 0.0) ? NR_EDGE_DOWN : (p >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN;
+        words[e >> 4] |= st << ((e & 15) * 2);
+    }
+    return NR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// public API
+// ---------------------------------------------------------------------------
+extern "C" void nr_options_default(nr_options *o)
+{
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->order = NR_ORDER_AUTO;
+    o->bucket_shift = 2;
+    o->n_buckets = 256;
+    o->device = 0;
+    o->timeout_ms = 60000.0;
+}
+
+extern "C" int nr_abi_version(void) { return NR_ABI_VERSION; }
+
+extern "C" const char *nr_status_string(int s)
+{
+    switch (s) {
+    case NR_OK: return "ok";
+    case NR_ERR_INVALID: return "invalid argument";
+    case NR_ERR_IO: return "cannot read graph file";
+    case NR_ERR_PARSE: return "malformed graph file";
+    case NR_ERR_UNSUPPORTED: return "graph outside engine limits";
+    case NR_ERR_CUDA: return g_err[0] ? g_err : "CUDA error";
+    case NR_ERR_NOMEM: return "out of memory";
+    case NR_ERR_TIMEOUT: return "device wait timed out";
+    case NR_ERR_INTERNAL: return "internal consistency check failed";
+    default: return "unknown status";
+    }
+}
+
+extern "C" int nr_context_create(int device, nr_context **out)
+{
+    if (!out) return NR_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    NR_CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return NR_ERR_INVALID;
+    NR_CUDA_TRY(cudaSetDevice(device));
+    nr_context *c = new nr_context();
+    c->device = device;
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e != cudaSuccess) {
+        nr_last_cuda_error(e);
+        nr_context_destroy(c);
+        return NR_ERR_CUDA;
+    }
+    c->sms = prop.multiProcessorCount;
+    *out = c;
+    return NR_OK;
+}
+
+extern "C" void nr_context_destroy(nr_context *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->qbuf) cudaFree(c->qbuf);
+    if (c->sbuf) cudaFree(c->sbuf);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap,
+                          const nr_options *o, nr_result *r)
+{
+    NrSmallGraph sg;
+    std::vector<unsigned char> blob;
+    build_small_blob(g, src, dst, &sg, &blob);
+    const int G = group_width(g->n_nodes);
+    const int W4 = sg.w4;
+    if (W4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
+    const void *kfn = grid_kernel(G, W4);
+    if (!kfn) return NR_ERR_UNSUPPORTED;
+
+    const int block = NR_BLOCK_THREADS;
+    const int warps = block / 32;
+    const size_t smem = (size_t)sg.blob_bytes + (size_t)warps * (32 / G) * 4 * W4 * sizeof(uint32_t);
+    NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int bps = 0;
+    NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
+    if (bps < 1) return NR_ERR_UNSUPPORTED;
+    if (o->blocks_per_sm > 0 && o->blocks_per_sm < bps) bps = o->blocks_per_sm;
+    const int grid = bps * c->sms;
+
+    const size_t item_bytes = (size_t)W4 * 16 + sizeof(double);
+    const size_t mask_bytes = align16((size_t)cap * W4 * 16);
+    const size_t mass_bytes = align16((size_t)cap * sizeof(double));
+    const size_t qneed = 2 * (mask_bytes + mass_bytes);
+    size_t free_b = 0, total_b = 0;
+    NR_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    if (qneed > c->qbytes && qneed > free_b + c->qbytes) return NR_ERR_NOMEM;
+    int rc = ensure(&c->qbuf, &c->qbytes, qneed);
+    if (rc) return rc;
+
+    const int max_waves = g->n_edges + 2;
+    size_t off = 0;
+    const size_t off_blob = off; off = align16(off + blob.size());
+    const size_t off_wc = off; off = align16(off + sizeof(unsigned long long) * (max_waves + 1));
+    const size_t off_bar = off; off = align16(off + 4 * sizeof(unsigned));
+    const size_t off_part = off; off = align16(off + sizeof(NrPartial) * grid);
+    rc = ensure(&c->sbuf, &c->sbytes, off);
+    if (rc) return rc;
+    unsigned char *sb = static_cast<unsigned char *>(c->sbuf);
+    unsigned char *qb = static_cast<unsigned char *>(c->qbuf);
+
+    NrGridParams P;
+    P.g = sg;
+    P.blob = sb + off_blob;
+    P.mask[0] = reinterpret_cast<uint4 *>(qb);
+    P.mass[0] = reinterpret_cast<double *>(qb + mask_bytes);
+    P.mask[1] = reinterpret_cast<uint4 *>(qb + mask_bytes + mass_bytes);
+    P.mass[1] = reinterpret_cast<double *>(qb + 2 * mask_bytes + mass_bytes);
+    P.capacity = cap;
+    P.wave_count = reinterpret_cast<unsigned long long *>(sb + off_wc);
+    P.max_waves = max_waves;
+    P.bar_count = reinterpret_cast<unsigned *>(sb + off_bar);
+    P.bar_gen = P.bar_count + 1;
+    P.status = reinterpret_cast<int *>(P.bar_count + 2);
+    P.partials = reinterpret_cast<NrPartial *>(sb + off_part);
+    P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
+    P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
+
+    // root subproblem: initial mask with mass 1 (main.cu:805-809)
+    std::vector<uint32_t> root(4 * W4, 0);
+    nr_initial_mask(g, root.data(), 4 * W4);
+    const double one = 1.0;
+    const unsigned long long one_u = 1;
+    cudaStream_t s = c->stream;
+    NR_CUDA_TRY(cudaMemcpyAsync(sb + off_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemsetAsync(sb + off_wc, 0, off_part - off_wc, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.wave_count, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.mask[0], root.data(), 16 * W4, cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.mass[0], &one, sizeof(one), cudaMemcpyHostToDevice, s));
+
+    void *args[] = {&P};
+    NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
+    NR_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(block), args, smem, s));
+    NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
+
+    std::vector<unsigned long long> wc(max_waves + 1);
+    std::vector<NrPartial> parts(grid);
+    int status = 0;
+    NR_CUDA_TRY(cudaMemcpyAsync(wc.data(), P.wave_count, sizeof(unsigned long long) * wc.size(),
+                                cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(parts.data(), P.partials, sizeof(NrPartial) * grid, cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(&status, P.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+
+    KS R, et, es;
+    unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0;
+    for (const NrPartial &p : parts) {
+        R.merge(p.R_hi, p.R_lo);
+        et.merge(p.et_hi, p.et_lo);
+        es.merge(p.es_hi, p.es_lo);
+        nodes += p.nodes; leaves += p.leaves; dead += p.dead; trunc += p.truncated; spilled += p.spilled;
+    }
+    int waves = 0;
+    unsigned long long maxw = 0;
+    for (int k = 0; k <= max_waves; ++k) {
+        unsigned long long n = std::min<unsigned long long>(wc[k], cap);
+        if (!n) break;
+        waves++;
+        maxw = std::max(maxw, n);
+    }
+    KS esp = et;
+    esp.merge(es.hi, es.lo);
+    r->R = R.val();
+    r->esp = esp.val();
+    r->R_plus_esp = r->R + r->esp;
+    r->trunc_bound = r->R > 0 ? r->esp / r->R : r->esp;
+    r->nodes = nodes; r->leaves = leaves; r->dead_ends = dead; r->truncated = trunc; r->spilled = spilled;
+    r->paths = leaves + spilled;
+    r->queued = 0;
+    r->iterations = waves;
+    r->max_queue_items = maxw;
+    r->item_bytes = (int)item_bytes;
+    r->max_queue_mb = (double)maxw * item_bytes / (1024.0 * 1024.0);
+    r->ms = ms;
+    r->time_to_bound_ms = 0;
+    r->engine = NR_ENGINE_GRID;
+    r->grid_blocks = grid;
+    r->block_threads = block;
+    r->capacity = cap;
+    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one);
+    r->d2h_bytes = sizeof(unsigned long long) * wc.size() + sizeof(NrPartial) * grid + sizeof(int);
+    if (status & NR_DEV_ERR_TIMEOUT) return NR_ERR_TIMEOUT;
+    if (status) return NR_ERR_INTERNAL;
+    return NR_OK;
+}
+
+extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int dst, uint64_t capacity,
+                                  const nr_options *opt, nr_result *res)
+{
+    if (!c || !res) return NR_ERR_INVALID;
+    memset(res, 0, sizeof(*res));
+    int rc = validate(g, src, dst);
+    if (rc) return rc;
+    nr_options o;
+    if (opt) o = *opt; else nr_options_default(&o);
+    res->n_nodes = g->n_nodes;
+    res->n_edges = g->n_edges;
+    res->src = src;
+    res->dst = dst;
+    res->mask_words = std::max(1, (2 * g->n_edges + 31) / 32);
+    if (capacity == 0) capacity = 1u << 20;   // reference default (common.h:33)
+    std::lock_guard<std::mutex> lock(c->mu);
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    if (g->n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
+    if (o.target_width > 0 || (o.order != NR_ORDER_AUTO && o.order != NR_ORDER_WAVES))
+        return NR_ERR_UNSUPPORTED;
+    return run_grid_small(c, g, src, dst, capacity, &o, res);
+}
+
+extern "C" int nr_reliability(const nr_graph *g, int src, int dst, uint64_t capacity, const nr_options *opt,
+                              nr_result *res)
+{
+    if (!res) return NR_ERR_INVALID;
+    memset(res, 0, sizeof(*res));
+    int rc = validate(g, src, dst);
+    if (rc) return rc;
+    nr_context *c = nullptr;
+    rc = nr_context_create(opt ? opt->device : 0, &c);
+    if (rc) return rc;
+    rc = nr_reliability_ctx(c, g, src, dst, capacity, opt, res);
+    nr_context_destroy(c);
+    return rc;
+}
+
+extern "C" int nr_reliability_batch(nr_context *, int, const nr_graph *, const int32_t *, const int32_t *,
+                                    uint64_t, const nr_options *, nr_result *)
+{
+    return NR_ERR_UNSUPPORTED;
+}
+
+// ---------------------------------------------------------------------------
+// graph file loader (workingPad/graph.h:46-145 semantics, status codes instead of exit)
+// ---------------------------------------------------------------------------
+namespace {
+struct Reader {
+    const char *p, *end;
+    bool skip()
+    {
+        while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r')) ++p;
+        return p < end;
+    }
+    bool integer(long *v)
+    {
+        if (!skip()) return false;
+        char *e;
+        long x = strtol(p, &e, 10);
+        if (e == p) return false;
+        p = e;
+        *v = x;
+        return true;
+    }
+    bool real(double *v)
+    {
+        if (!skip()) return false;
+        char *e;
+        double x = strtod(p, &e);
+        if (e == p) return false;
+        p = e;
+        *v = x;
+        return true;
+    }
+};
+}  // namespace
+
+extern "C" int nr_graph_load(const char *path, nr_graph *out)
+{
+    if (!path || !out) return NR_ERR_INVALID;
+    memset(out, 0, sizeof(*out));
+    FILE *f = fopen(path, "rb");
+    if (!f) return NR_ERR_IO;
+    std::string text;
+    char buf[65536];
+    size_t got;
+    while ((got = fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, got);
+    fclose(f);
+    Reader rd{text.data(), text.data() + text.size()};
+    long n = 0, efile = 0;
+    if (!rd.integer(&n) || !rd.integer(&efile) || n <= 0 || n > (1L << 24)) return NR_ERR_PARSE;
+    rd.skip();
+    if (rd.p < rd.end && isalpha((unsigned char)*rd.p)) ++rd.p;   // optional U / D
+    std::vector<int32_t> row(n + 1, 0), col;
+    std::vector<double> arc_p;
+    for (long u = 0; u < n; ++u) {
+        long deg;
+        if (!rd.integer(&deg) || deg < 0) return NR_ERR_PARSE;
+        for (long j = 0; j < deg; ++j) {
+            long v;
+            double p;
+            if (!rd.integer(&v) || !rd.real(&p) || v < 0 || v >= n) return NR_ERR_PARSE;
+            col.push_back((int32_t)v);
+            arc_p.push_back(p);
+        }
+        row[u + 1] = (int32_t)col.size();
+    }
+    std::map<std::pair<int32_t, int32_t>, int32_t> ids;
+    std::vector<int32_t> eid(col.size());
+    std::vector<double> ep;
+    for (long u = 0; u < n; ++u)
+        for (int32_t j = row[u]; j < row[u + 1]; ++j) {
+            std::pair<int32_t, int32_t> key(std::min<int32_t>((int32_t)u, col[j]), std::max<int32_t>((int32_t)u, col[j]));
+            auto it = ids.find(key);
+            if (it == ids.end()) {
+                it = ids.emplace(key, (int32_t)ep.size()).first;
+                ep.push_back(arc_p[j]);
+            }
+            eid[j] = it->second;
+        }
+    int32_t *r = (int32_t *)malloc(sizeof(int32_t) * (n + 1));
+    int32_t *c = (int32_t *)malloc(sizeof(int32_t) * std::max<size_t>(col.size(), 1));
+    int32_t *e = (int32_t *)malloc(sizeof(int32_t) * std::max<size_t>(col.size(), 1));
+    double *p = (double *)malloc(sizeof(double) * std::max<size_t>(ep.size(), 1));
+    if (!r || !c || !e || !p) {
+        free(r); free(c); free(e); free(p);
+        return NR_ERR_NOMEM;
+    }
+    memcpy(r, row.data(), sizeof(int32_t) * (n + 1));
+    if (!col.empty()) {
+        memcpy(c, col.data(), sizeof(int32_t) * col.size());
+        memcpy(e, eid.data(), sizeof(int32_t) * col.size());
+    }
+    if (!ep.empty()) memcpy(p, ep.data(), sizeof(double) * ep.size());
+    out->n_nodes = (int32_t)n;
+    out->n_edges = (int32_t)ep.size();
+    out->n_arcs = (int32_t)col.size();
+    out->row_ptr = r;
+    out->col_idx = c;
+    out->edge_id = e;
+    out->edge_p = p;
+    return NR_OK;
+}
+
+extern "C" void nr_graph_free(nr_graph *g)
+{
+    if (!g) return;
+    free((void *)g->row_ptr);
+    free((void *)g->col_idx);
+    free((void *)g->edge_id);
+    free((void *)g->edge_p);
+    memset(g, 0, sizeof(*g));
+}
+
+extern "C" int nr_format_result(const nr_result *r, char *buf, size_t len)
+{
+    if (!r) return NR_ERR_INVALID;
+    // line layout of workingPad/main.cu:1037-1056
+    return snprintf(buf, len,
+                    "\n"
+                    "============================================\n"
+                    "  Two-Terminal Network Reliability Results\n"
+                    "============================================\n"
+                    "Graph:            N = %d, E = %d\n"
+                    "Terminals:        src = %d, dst = %d\n"
+                    "--------------------------------------------\n"
+                    "Reliability:      R(G) = %.12f\n"
+                    "R + ESP:                 %.12f\n"
+                    "ESP (truncated):         %.6e\n"
+                    "Truncation bound:        %.6e\n"
+                    "--------------------------------------------\n"
+                    "Paths enumerated: %llu\n"
+                    "Nodes processed:  %llu\n"
+                    "Kernel iterations:%d\n"
+                    "Max queue RSS:    %.3f MB  (%llu items)\n"
+                    "Total time:       %.3f ms\n"
+                    "============================================\n",
+                    r->n_nodes, r->n_edges, r->src, r->dst, r->R, r->R_plus_esp, r->esp, r->trunc_bound,
+                    (unsigned long long)r->paths, (unsigned long long)r->nodes, r->iterations, r->max_queue_mb,
+                    (unsigned long long)r->max_queue_items, r->ms);
+}

@@ -1,0 +1,154 @@
+// nr_expand.cuh -- the per-subproblem step shared by the engines: optimistic
+// BFS over not-down arcs, path extraction, and the disjoint branches of the
+// path (child k = first k-1 UNKNOWN path edges up, k-th down; all-up -> R).
+//
+// Restates workingPad/device_code.cuh:80-194 (bfs_reachable) and
+// workingPad/main.cu:114-283 (path_edge_sweep_warp) with a different mapping:
+// a warp holds K = 32/G subproblems, G lanes each, lane v of a group owns
+// node v.  A node's not-down in-neighbours form one 32-bit row, so one BFS
+// level is one AND, one __ballot_sync and one __ffs per lane, and the parent
+// of v is the smallest frontier node with a not-down arc to v -- the rule
+// the reference kernel follows when one lane scans the frontier bitmask in
+// ascending order (device_code.cuh:141-171).  Masses are FP64 products in
+// path order (the reference uses float log sums, common.h:60).
+#pragma once
+
+#include "nr_device.cuh"
+
+// Shared-memory view of the staged graph tables.
+struct NrSmemGraph {
+    const double *p;
+    const double *q;
+    const uint16_t *eid;      // [32*32] arc (u -> v) -> edge id
+    const int *start;         // [n+1] in-arc ranges
+    const uint32_t *list;     // in-arcs of v: (eid << 8) | u
+};
+
+__device__ __forceinline__ NrSmemGraph nr_smem_graph(const unsigned char *s, const NrSmallGraph &g)
+{
+    NrSmemGraph v;
+    v.p = reinterpret_cast<const double *>(s + g.off_p);
+    v.q = reinterpret_cast<const double *>(s + g.off_q);
+    v.eid = reinterpret_cast<const uint16_t *>(s + g.off_eid);
+    v.start = reinterpret_cast<const int *>(s + g.off_start);
+    v.list = reinterpret_cast<const uint32_t *>(s + g.off_list);
+    return v;
+}
+
+struct NrLaneAcc {
+    NrKs R, et, es;
+    unsigned long long nodes, leaves, dead, trunc, spilled;
+};
+
+__device__ __forceinline__ void nr_acc_zero(NrLaneAcc &a)
+{
+    a.R.hi = a.R.lo = a.et.hi = a.et.lo = a.es.hi = a.es.lo = 0.0;
+    a.nodes = a.leaves = a.dead = a.trunc = a.spilled = 0;
+}
+
+// Expand the group's subproblem (mask words in smem at my_m, mass `mass`).
+// Every lane of the warp must call this (it uses full-warp shuffles/ballots).
+// On return, a lane with has_child holds one child: words w[] and mass cm.
+// Leaf mass, dead ends and truncation are accumulated on the group's lane 0.
+template <int G, int W4>
+__device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGraph &sg,
+                                          const uint32_t *my_m, bool valid, double mass, double eps,
+                                          bool &has_child, uint32_t (&w)[4 * W4], double &cm,
+                                          NrLaneAcc &acc)
+{
+    constexpr int NW = 4 * W4;
+    const int lane = threadIdx.x & 31;
+    const int v = lane & (G - 1);
+    const int gbase = lane & ~(G - 1);
+    const bool leader = (v == 0);
+    const int n = g.n, src = g.src, dst = g.dst;
+
+    has_child = false;
+    cm = 0.0;
+    if (valid && leader) acc.nodes++;
+    bool active = valid;
+    if (active && eps > 0.0 && mass < eps) {          // main.cu:537-543
+        if (leader) { acc.trunc++; nr_ks_add(acc.et, mass); }
+        active = false;
+    }
+
+    // not-down in-neighbour row of node v
+    uint32_t row = 0;
+    if (active && v < n) {
+        const int lo = sg.start[v], hi = sg.start[v + 1];
+        for (int j = lo; j < hi; ++j) {
+            const uint32_t ent = sg.list[j];
+            const int e = (int)(ent >> 8);
+            const uint32_t word = my_m[e >> 4];
+            row |= ((word >> ((e & 15) << 1)) & 1u) << (ent & 31u);
+        }
+    }
+
+    // level-synchronous BFS, one ballot per level for all groups of the warp
+    uint32_t F = 1u << src, vis = F;
+    int par = -1, level = 0;
+    bool found = active && (src == dst);
+    bool searching = active && !found;
+    while (__any_sync(NR_FULL, searching)) {
+        const uint32_t t = row & F;
+        const bool hit = searching && (v < n) && (t != 0u) && !((vis >> v) & 1u);
+        if (hit) par = __ffs(t) - 1;
+        const uint32_t b = __ballot_sync(NR_FULL, hit);
+        const uint32_t nf = (G == 32) ? b : ((b >> gbase) & ((1u << G) - 1u));
+        if (searching) {
+            vis |= nf;
+            F = nf;
+            ++level;
+            if ((vis >> dst) & 1u) { found = true; searching = false; }
+            else if (nf == 0u) searching = false;
+        }
+    }
+    if (active && !found && leader) acc.dead++;
+    const bool live = active && found;
+    const int L = live ? level : 0;                     // hops on the path
+
+    // walk dst -> src: lane h of the group receives hop h = (u, v)
+    int Lmax = L;
+    for (int off = 16; off > 0; off >>= 1) Lmax = max(Lmax, __shfl_xor_sync(NR_FULL, Lmax, off));
+    int hop_u = 0, hop_v = 0, cur = dst;
+    for (int s = Lmax - 1; s >= 0; --s) {
+        const int u = __shfl_sync(NR_FULL, par, gbase + (cur & (G - 1)));
+        if (s < L) {
+            if (v == s) { hop_u = u; hop_v = cur; }
+            cur = u;
+        }
+    }
+    int e_h = 0;
+    bool unk = false;
+    if (v < L) {
+        e_h = sg.eid[hop_u * 32 + hop_v];
+        unk = ((my_m[e_h >> 4] >> ((e_h & 15) << 1)) & 3u) == 3u;
+    }
+
+    // FP64 mass along the path, src side first (sequential, as the oracle)
+    double P = mass;
+    for (int h = 0; h < Lmax; ++h) {
+        const int e = __shfl_sync(NR_FULL, e_h, gbase + h);
+        const bool u = __shfl_sync(NR_FULL, unk, gbase + h);
+        if (h < L && u) {
+            if (v == h) { cm = __dmul_rn(P, sg.q[e]); has_child = true; }
+            P = __dmul_rn(P, sg.p[e]);
+        }
+    }
+    if (live && leader) { acc.leaves++; nr_ks_add(acc.R, P); }
+
+    // child of hop v: parent with earlier UNKNOWN hops up and hop v down
+#pragma unroll
+    for (int k = 0; k < NW; ++k) w[k] = my_m[k];
+    for (int j = 0; j < Lmax; ++j) {
+        const int e = __shfl_sync(NR_FULL, e_h, gbase + j);
+        const bool u = __shfl_sync(NR_FULL, unk, gbase + j);
+        if (has_child && u && j <= v) {
+            const int wi = e >> 4;
+            const uint32_t bits = (j < v ? 2u : 3u) << ((e & 15) << 1);
+#pragma unroll
+            for (int k = 0; k < NW; ++k)
+                if (k == wi) w[k] &= ~bits;
+        }
+    }
+}

@@ -1,0 +1,273 @@
+"""ctypes binding of the engine's C ABI (include/nr.h).
+
+This is the host-side mirror of the reference's `network_reliability`
+driver (workingPad/main.cu:795-1072): the same arguments (graph, src, dst,
+queue capacity, truncation eps) and the same result fields.  The CUDA
+library is required: if libnr.so is missing or cannot load, every call
+raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .graphs import Graph
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libnr.so")
+
+NR_OK = 0
+STATUS = {
+    0: "NR_OK", -1: "NR_ERR_INVALID", -2: "NR_ERR_IO", -3: "NR_ERR_PARSE", -4: "NR_ERR_UNSUPPORTED",
+    -5: "NR_ERR_CUDA", -6: "NR_ERR_NOMEM", -7: "NR_ERR_TIMEOUT", -8: "NR_ERR_INTERNAL",
+}
+ORDERS = {"auto": 0, "waves": 1, "maxmass": 2, "learned": 3}
+ENGINES = {1: "grid", 2: "warp"}
+
+
+class NrError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+
+
+class NrGraph(C.Structure):
+    _fields_ = [
+        ("n_nodes", C.c_int32), ("n_edges", C.c_int32), ("n_arcs", C.c_int32),
+        ("row_ptr", C.POINTER(C.c_int32)), ("col_idx", C.POINTER(C.c_int32)),
+        ("edge_id", C.POINTER(C.c_int32)), ("edge_p", C.POINTER(C.c_double)),
+    ]
+
+
+class NrOptions(C.Structure):
+    _fields_ = [
+        ("truncation_eps", C.c_double), ("target_width", C.c_double), ("order", C.c_int32),
+        ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("device", C.c_int32),
+        ("blocks_per_sm", C.c_int32), ("warps_per_block", C.c_int32), ("timeout_ms", C.c_double),
+        ("verbose", C.c_int32), ("reserved", C.c_int32 * 7),
+    ]
+
+
+class NrResult(C.Structure):
+    _fields_ = [
+        ("R", C.c_double), ("R_plus_esp", C.c_double), ("esp", C.c_double), ("trunc_bound", C.c_double),
+        ("paths", C.c_uint64), ("nodes", C.c_uint64), ("leaves", C.c_uint64), ("dead_ends", C.c_uint64),
+        ("truncated", C.c_uint64), ("spilled", C.c_uint64), ("queued", C.c_uint64),
+        ("iterations", C.c_int32), ("n_nodes", C.c_int32), ("n_edges", C.c_int32),
+        ("src", C.c_int32), ("dst", C.c_int32), ("mask_words", C.c_int32),
+        ("max_queue_items", C.c_uint64), ("max_queue_mb", C.c_double), ("ms", C.c_double),
+        ("time_to_bound_ms", C.c_double), ("engine", C.c_int32), ("grid_blocks", C.c_int32),
+        ("block_threads", C.c_int32), ("item_bytes", C.c_int32), ("capacity", C.c_uint64),
+        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("reserved", C.c_int32 * 4),
+    ]
+
+
+# every symbol include/nr.h declares
+EXPORTS = [
+    "nr_options_default", "nr_status_string", "nr_abi_version", "nr_graph_load", "nr_graph_free",
+    "nr_initial_mask", "nr_context_create", "nr_context_destroy", "nr_reliability", "nr_reliability_ctx",
+    "nr_reliability_batch", "nr_format_result",
+]
+
+_lib_handle: Optional[C.CDLL] = None
+
+
+def lib() -> C.CDLL:
+    """Load libnr.so (raises if it is missing; there is no fallback)."""
+    global _lib_handle
+    if _lib_handle is not None:
+        return _lib_handle
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with relaibilitygpu_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    L.nr_options_default.argtypes = [C.POINTER(NrOptions)]
+    L.nr_options_default.restype = None
+    L.nr_status_string.argtypes = [C.c_int]
+    L.nr_status_string.restype = C.c_char_p
+    L.nr_abi_version.restype = C.c_int
+    L.nr_graph_load.argtypes = [C.c_char_p, C.POINTER(NrGraph)]
+    L.nr_graph_load.restype = C.c_int
+    L.nr_graph_free.argtypes = [C.POINTER(NrGraph)]
+    L.nr_graph_free.restype = None
+    L.nr_initial_mask.argtypes = [C.POINTER(NrGraph), C.POINTER(C.c_uint32), C.c_int]
+    L.nr_initial_mask.restype = C.c_int
+    L.nr_context_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+    L.nr_context_create.restype = C.c_int
+    L.nr_context_destroy.argtypes = [C.c_void_p]
+    L.nr_context_destroy.restype = None
+    L.nr_reliability.argtypes = [C.POINTER(NrGraph), C.c_int, C.c_int, C.c_uint64, C.POINTER(NrOptions),
+                                 C.POINTER(NrResult)]
+    L.nr_reliability.restype = C.c_int
+    L.nr_reliability_ctx.argtypes = [C.c_void_p, C.POINTER(NrGraph), C.c_int, C.c_int, C.c_uint64,
+                                     C.POINTER(NrOptions), C.POINTER(NrResult)]
+    L.nr_reliability_ctx.restype = C.c_int
+    L.nr_reliability_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(NrGraph), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int32), C.c_uint64, C.POINTER(NrOptions),
+                                       C.POINTER(NrResult)]
+    L.nr_reliability_batch.restype = C.c_int
+    L.nr_format_result.argtypes = [C.POINTER(NrResult), C.c_char_p, C.c_size_t]
+    L.nr_format_result.restype = C.c_int
+    _lib_handle = L
+    return L
+
+
+@dataclasses.dataclass
+class Result:
+    R: float
+    R_plus_esp: float
+    esp: float
+    trunc_bound: float
+    paths: int
+    nodes: int
+    leaves: int
+    dead_ends: int
+    truncated: int
+    spilled: int
+    queued: int
+    iterations: int
+    n_nodes: int
+    n_edges: int
+    src: int
+    dst: int
+    mask_words: int
+    max_queue_items: int
+    max_queue_mb: float
+    ms: float
+    time_to_bound_ms: float
+    engine: str
+    grid_blocks: int
+    block_threads: int
+    item_bytes: int
+    capacity: int
+    h2d_bytes: int
+    d2h_bytes: int
+    _raw: NrResult = dataclasses.field(repr=False, default=None)
+
+    @staticmethod
+    def from_raw(r: NrResult) -> "Result":
+        kw = {f: getattr(r, f) for f, _ in NrResult._fields_ if f != "reserved"}
+        kw["engine"] = ENGINES.get(kw["engine"], str(kw["engine"]))
+        return Result(_raw=r, **kw)
+
+    def block(self) -> str:
+        """The reference's result block text (workingPad/main.cu:1037-1056)."""
+        buf = C.create_string_buffer(4096)
+        lib().nr_format_result(C.byref(self._raw), buf, len(buf))
+        return buf.value.decode()
+
+
+class _GraphView:
+    """Keeps the numpy arrays alive while C holds pointers into them."""
+
+    def __init__(self, g: Graph):
+        self.row = np.ascontiguousarray(g.row_ptr, dtype=np.int32)
+        self.col = np.ascontiguousarray(g.col_idx, dtype=np.int32)
+        self.eid = np.ascontiguousarray(g.edge_id, dtype=np.int32)
+        self.p = np.ascontiguousarray(g.edge_p, dtype=np.float64)
+        self.c = NrGraph(
+            int(g.n_nodes), int(self.p.shape[0]), int(self.col.shape[0]),
+            self.row.ctypes.data_as(C.POINTER(C.c_int32)), self.col.ctypes.data_as(C.POINTER(C.c_int32)),
+            self.eid.ctypes.data_as(C.POINTER(C.c_int32)), self.p.ctypes.data_as(C.POINTER(C.c_double)))
+
+
+def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto", bucket_shift: int = 2,
+                 n_buckets: int = 256, device: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0,
+                 timeout_ms: float = 60000.0) -> NrOptions:
+    o = NrOptions()
+    lib().nr_options_default(C.byref(o))
+    o.truncation_eps = float(eps)
+    o.target_width = float(target_width)
+    o.order = ORDERS[order] if isinstance(order, str) else int(order)
+    o.bucket_shift = int(bucket_shift)
+    o.n_buckets = int(n_buckets)
+    o.device = int(device)
+    o.blocks_per_sm = int(blocks_per_sm)
+    o.warps_per_block = int(warps_per_block)
+    o.timeout_ms = float(timeout_ms)
+    return o
+
+
+def _check(rc: int) -> None:
+    if rc != NR_OK:
+        raise NrError(rc, lib().nr_status_string(rc).decode())
+
+
+class Context:
+    """Reusable device state (queue buffers, stream); one call at a time."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().nr_context_create(int(device), C.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            lib().nr_context_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reliability(self, g: Graph, src: int, dst: int, capacity: int = 0, **opts) -> Result:
+        gv = _GraphView(g)
+        o = make_options(**opts)
+        r = NrResult()
+        _check(lib().nr_reliability_ctx(self.h, C.byref(gv.c), int(src), int(dst), int(capacity),
+                                        C.byref(o), C.byref(r)))
+        return Result.from_raw(r)
+
+    def reliability_batch(self, graphs: Sequence[Graph], srcs, dsts, capacity: int = 0, **opts):
+        views = [_GraphView(g) for g in graphs]
+        arr = (NrGraph * len(views))(*[v.c for v in views])
+        s = np.ascontiguousarray(srcs, dtype=np.int32)
+        d = np.ascontiguousarray(dsts, dtype=np.int32)
+        res = (NrResult * len(views))()
+        o = make_options(**opts)
+        _check(lib().nr_reliability_batch(self.h, len(views), arr, s.ctypes.data_as(C.POINTER(C.c_int32)),
+                                          d.ctypes.data_as(C.POINTER(C.c_int32)), int(capacity), C.byref(o),
+                                          res))
+        return [Result.from_raw(res[i]) for i in range(len(views))]
+
+
+def reliability(g: Graph, src: int, dst: int, capacity: int = 0, **opts) -> Result:
+    """One-shot solve through nr_reliability (creates and frees a context)."""
+    gv = _GraphView(g)
+    o = make_options(**opts)
+    r = NrResult()
+    _check(lib().nr_reliability(C.byref(gv.c), int(src), int(dst), int(capacity), C.byref(o), C.byref(r)))
+    return Result.from_raw(r)
+
+
+def load_graph_file(path: str) -> Graph:
+    """Parse a reference graph file through nr_graph_load."""
+    cg = NrGraph()
+    _check(lib().nr_graph_load(path.encode(), C.byref(cg)))
+    try:
+        n, na, ne = cg.n_nodes, cg.n_arcs, cg.n_edges
+        row = np.ctypeslib.as_array(cg.row_ptr, shape=(n + 1,)).copy()
+        col = np.ctypeslib.as_array(cg.col_idx, shape=(max(na, 1),))[:na].copy()
+        eid = np.ctypeslib.as_array(cg.edge_id, shape=(max(na, 1),))[:na].copy()
+        p = np.ctypeslib.as_array(cg.edge_p, shape=(max(ne, 1),))[:ne].copy()
+    finally:
+        lib().nr_graph_free(C.byref(cg))
+    return Graph(n, row, col, eid, p, name=path)
+
+
+def initial_mask(g: Graph) -> np.ndarray:
+    gv = _GraphView(g)
+    w = np.zeros(g.mask_words, dtype=np.uint32)
+    _check(lib().nr_initial_mask(C.byref(gv.c), w.ctypes.data_as(C.POINTER(C.c_uint32)), len(w)))
+    return w

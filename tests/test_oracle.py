@@ -1,0 +1,152 @@
+"""Pin the CPU oracle against the reference: published run logs, analytic
+values, brute force, and the reference's own seq.cpp / cpu_reference.cpp
+outputs (tests/golden/golden.json, made by tests/golden/make_golden.py)."""
+import pytest
+
+from conftest import rel_close
+
+SMALL_PUBLISHED = ["COMP8", "COMP8-03", "COMP9"]
+
+
+@pytest.mark.parametrize("name", SMALL_PUBLISHED)
+def test_published_counts_main_cu(golden, load_golden_graph, oracle, name):
+    """main.cu semantics: nodes include dead ends; waves and widest wave match the logs."""
+    d = golden["published"][name]
+    g = load_golden_graph(name)
+    r = oracle.run(g, d["src"], d["dst"], rule="level", order="waves")
+    assert r.paths == d["paths"]
+    assert r.nodes == d["nodes"]
+    assert r.waves == d["iterations"]
+    assert r.max_wave == d["max_queue_items"]
+    # COMP8-03's published FP64 value is a log-space sum (seq.cpp); the linear
+    # product agrees to ~4e-14 relative and brute force to ~1e-15
+    assert rel_close(r.R, d["R"], 1e-12)
+    assert r.esp == 0.0
+
+
+def test_published_k10_counts(golden, load_golden_graph, oracle):
+    d = golden["published"]["COMP10-05"]
+    g = load_golden_graph("COMP10-05")
+    r = oracle.run(g, 0, 9, rule="level", order="waves", threads=4)
+    assert (r.paths, r.nodes, r.waves, r.max_wave) == (d["paths"], d["nodes"], d["iterations"], d["max_queue_items"])
+    assert rel_close(r.R, d["R"], 1e-15)
+
+
+@pytest.mark.parametrize("name", SMALL_PUBLISHED)
+def test_seq_cpp_semantics(golden, load_golden_graph, oracle, name):
+    """seq.cpp semantics (FIFO parent, pre-push check): iterations = paths = published."""
+    d = golden["published"][name]
+    g = load_golden_graph(name)
+    r = oracle.run(g, d["src"], d["dst"], rule="fifo", precheck=True, order="heap")
+    assert r.nodes == d["paths"]
+    assert r.paths == d["paths"]
+
+
+def test_seq_ref_random_graphs(golden, load_golden_graph, oracle):
+    """The reference's seq.cpp built from source on seeded random graphs."""
+    seq = golden["seq_ref"]
+    assert len(seq) >= 20
+    for name, d in seq.items():
+        g = load_golden_graph(name)
+        r = oracle.run(g, d["src"], d["dst"], rule="fifo", precheck=True, order="heap")
+        assert r.nodes == d["iterations"], name
+        assert r.paths == d["paths"], name
+        assert rel_close(r.R, d["R"], 1e-12), (name, r.R, d["R"])
+
+
+def test_cpu_reference_tiny(golden, load_golden_graph, oracle):
+    """workingPad/cpu_reference.cpp reads p as float: agreement to float precision."""
+    for name, d in golden["cpu_reference"].items():
+        g = load_golden_graph(name)
+        r = oracle.run(g, d["src"], d["dst"])
+        assert abs(r.R - d["R"]) < 1e-6, name
+
+
+def test_analytic(golden, load_golden_graph, oracle):
+    for name, d in golden["analytic"].items():
+        g = load_golden_graph(name)
+        for rule in ("level", "fifo"):
+            r = oracle.run(g, d["src"], d["dst"], rule=rule)
+            assert rel_close(r.R, d["R"], 1e-14), (name, rule, r.R)
+
+
+def test_brute_force_agrees(golden, load_golden_graph, oracle):
+    names = [n for n in golden["files"] if n.startswith(("gnm", "grid", "kn", "test_", "cycle", "temp"))]
+    for name in names:
+        g = load_golden_graph(name)
+        f = golden["files"][name]
+        s, t = f.get("src", 0), f.get("dst", g.n_nodes - 1)
+        if name in golden["analytic"]:
+            s, t = golden["analytic"][name]["src"], golden["analytic"][name]["dst"]
+        if name == "test_kite":
+            s, t = 0, 4
+        b = oracle.brute(g, s, t)
+        for rule in ("level", "fifo"):
+            r = oracle.run(g, s, t, rule=rule)
+            assert rel_close(r.R, b, 1e-13), (name, rule, r.R, b)
+
+
+def test_grid4x4_config(oracle):
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.grid(4, 4, p=0.9)
+    b = oracle.brute(g, 0, 15)
+    r = oracle.run(g, 0, 15)
+    assert rel_close(r.R, b, 1e-14)
+    assert rel_close(b, 0.97504634957706637, 1e-14)
+
+
+def test_orders_agree_when_exhaustive(load_golden_graph, oracle):
+    g = load_golden_graph("COMP8")
+    base = oracle.run(g, 0, 7, order="waves")
+    for kw in (dict(order="heap"), dict(order="dfs"), dict(order="waves", bucket_shift=2, n_buckets=64),
+               dict(order="waves", threads=3)):
+        r = oracle.run(g, 0, 7, **kw)
+        assert (r.paths, r.nodes, r.leaves, r.dead) == (base.paths, base.nodes, base.leaves, base.dead), kw
+        assert rel_close(r.R, base.R, 1e-14)
+
+
+def test_truncation_brackets(golden, load_golden_graph, oracle):
+    """Truncated runs bracket the exhaustive value: R <= R_exact <= R + ESP."""
+    g = load_golden_graph("COMP9")
+    exact = oracle.run(g, 0, 8).R
+    for kw in (dict(eps=1e-6), dict(capacity=5000), dict(bucket_shift=2, n_buckets=128, target_width=1e-4),
+               dict(order="heap", capacity=300), dict(bucket_shift=1, n_buckets=64, target_width=1e-2)):
+        r = oracle.run(g, 0, 8, **kw)
+        assert r.R <= exact + 1e-15, kw
+        assert exact <= r.R + r.esp + 1e-15, kw
+        if kw.get("target_width"):
+            assert r.status == 1 and r.esp <= kw["target_width"]
+
+
+def test_k15_published_bracket(golden, load_golden_graph, oracle):
+    """A truncated K15 p=0.5 run overlaps the reference's truncated bracket."""
+    d = golden["published"]["COMP15-05_bracket"]
+    g = load_golden_graph("COMP15-05")
+    r = oracle.run(g, 0, 14, bucket_shift=2, n_buckets=256, target_width=2e-3, threads=4)
+    assert r.status == 1
+    assert r.R <= d["hi"] and d["lo"] <= r.R + r.esp
+
+
+def test_bucket_function(oracle):
+    assert oracle.bucket(1.0, 2, 256) == 0
+    assert oracle.bucket(0.5, 2, 256) == 4
+    assert oracle.bucket(0.75, 2, 256) == 2
+    assert oracle.bucket(1e-300, 2, 256) == 255
+    assert oracle.bucket(0.3, -1, 1) == 0
+    ms = [1.0, 0.9, 0.7, 0.5, 0.26, 0.01, 1e-5]
+    bs = [oracle.bucket(m, 3, 512) for m in ms]
+    assert bs == sorted(bs)
+
+
+def test_src_equals_dst(oracle):
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.complete(5, p=0.5)
+    r = oracle.run(g, 2, 2)
+    assert r.R == 1.0 and r.paths == 1 and r.nodes == 1
+
+
+def test_disconnected(oracle):
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.from_edges(4, [(0, 1), (2, 3)], [0.9, 0.9])
+    r = oracle.run(g, 0, 3)
+    assert r.R == 0.0 and r.nodes == 1 and r.dead == 1 and r.paths == 0
