@@ -2,22 +2,30 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
-A step is one solve of the workload through the C ABI.  `value` is
-subproblems (popped nodes) per second of device time, summed over ranks and
-divided by the slowest rank; the device time of each step is the kernel's
-CUDA-event time on the engine's own stream.  `e2e` is the same metric with
-wall-clock time around the public call (graph tables host->device, results
-device->host).  L2 is flushed (a 512 MB write) before every timed step.
+Workloads (all synthetic, seeded; numpy PCG64):
+  k15batch (default) -- the metric's configuration: K15 (N=15, E=105), src 0,
+      dst 14, edge p ~ U[0.9, 0.99] FP64, run in plain max-mass order until the
+      ESP width (ESP + queued mass) is <= 1e-6.  One instance needs only ~20-60
+      subproblems, so a step solves a batch of 4096 such instances (seeds
+      0..4095) in one launch; single-instance time-to-bound is reported beside it.
+  k10 -- K10 (N=10, E=45), p ~ U[0.5, 0.95], exhaustive (one solve per step).
 
---impl reference times the reference algorithm's CPU implementation on the
-host cores: the CPU port in oracle/ (the reference's own seq.cpp cannot be
-built on the GPU host, which has no reference tree), with every host thread.
-Multi-GPU runs are independent replicas (the decomposition shards, but each
-rank solves its own copy of the workload; no collective on the data path).
+`value` is subproblems (popped nodes, dead ends included) per second of
+device time: the engine's CUDA events on its own stream around the kernels,
+summed over ranks and divided by the slowest rank.  `e2e` is the same metric
+with wall-clock time around the public C call (graph tables host->device,
+results device->host).  L2 is flushed (a 512 MB write) before every step.
+
+--impl reference times the reference algorithm on the host cores: the CPU
+port in oracle/ (the reference's own seq/seq.cpp needs the reference tree,
+which the GPU host does not have), one instance per thread, every host
+thread.  Multi-GPU runs are independent replicas: each rank solves its own
+copy of the workload; no collective on the data path.
 """
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import json
 import os
 import statistics
@@ -32,6 +40,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 METRIC = "time to ESP<=1e-6 on K15, learned vs plain order (1 GB300); subproblems/sec"
 UNIT = "subproblems/sec"
+BATCH = 4096
 
 
 def peaks():
@@ -48,18 +57,23 @@ def peaks():
 # ---------------------------------------------------------------------------
 def workload(name: str):
     import relaibilitygpu_gb300 as nr
+    if name == "k15batch":
+        gs = [nr.complete(15, p_range=(0.9, 0.99), seed=s) for s in range(BATCH)]
+        return dict(kind="batch", graphs=gs, srcs=[0] * BATCH, dsts=[14] * BATCH, capacity=0,
+                    opts=dict(target_width=1e-6, bucket_shift=2, n_buckets=256),
+                    oracle=dict(bucket_shift=2, n_buckets=256, target_width=1e-6),
+                    name=f"K15 (N=15, E=105) src=0 dst=14 p~U[0.9,0.99] seeds 0..{BATCH - 1}, "
+                         f"max-mass order to ESP width<=1e-6, {BATCH} instances per step")
     if name == "k10":
         g = nr.complete(10, p_range=(0.5, 0.95), seed=2)
-        return dict(name="K10 (N=10, E=45) src=0 dst=9 p~U[0.5,0.95] seed 2, exhaustive",
-                    graph=g, src=0, dst=9, capacity=1 << 22, opts=dict(eps=0.0))
+        return dict(kind="single", graphs=[g], srcs=[0], dsts=[9], capacity=1 << 22, opts=dict(eps=0.0),
+                    oracle=dict(), name="K10 (N=10, E=45) src=0 dst=9 p~U[0.5,0.95] seed 2, exhaustive")
     raise SystemExit(f"unknown workload {name}")
 
 
-def algorithmic_bytes(n_edges: int, nodes: int, pushes: int) -> int:
-    """Each queued subproblem is written once and read once: S = 4*W + 8 bytes
-    (packed 2-bit mask words + FP64 mass)."""
-    W = max(1, (2 * n_edges + 31) // 32)
-    return (nodes + pushes) * (4 * W + 8)
+def item_bytes(n_edges: int) -> int:
+    """Algorithmic bytes of one queued subproblem: packed 2-bit mask words + FP64 mass."""
+    return 4 * max(1, (2 * n_edges + 31) // 32) + 8
 
 
 # ---------------------------------------------------------------------------
@@ -114,46 +128,73 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_port(w, threads: int, sample_note: str):
+# ---------------------------------------------------------------------------
+# CPU port (oracle/): instances in parallel, one per host thread
+# ---------------------------------------------------------------------------
+def cpu_solve_all(w, threads: int, reps: int = 1, _cache={}):
     import oracle as og
-    r = og.run(w["graph"], w["src"], w["dst"], threads=threads, eps=w["opts"].get("eps", 0.0))
-    return {"value": r.nodes / r.seconds, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": sample_note, "nodes": r.nodes, "seconds": r.seconds}
+    og.lib()
+    t0 = time.perf_counter()
+    nodes = 0
+    if w["kind"] == "single":
+        for _ in range(reps):
+            for g, s, d in zip(w["graphs"], w["srcs"], w["dsts"]):
+                nodes += og.run(g, s, d, threads=threads, **w["oracle"]).nodes
+    else:
+        key = id(w)
+        if key not in _cache:
+            _cache[key] = og.BatchArgs(w["graphs"], w["srcs"], w["dsts"])
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            res = og.run_batch(_cache[key], threads=threads, **w["oracle"])
+            nodes += sum(res[i].nodes for i in range(len(w["graphs"])))
+    secs = time.perf_counter() - t0
+    return nodes, secs, threads
+
+
+def cpu_baseline(w, threads: int):
+    # bounded sample: repeat the whole workload until about 2 s of host time has passed
+    nodes, secs, used = cpu_solve_all(w, threads, 1)
+    reps = max(1, min(50, int(2.0 / max(secs, 1e-3))))
+    if reps > 1:
+        nodes, secs, used = cpu_solve_all(w, threads, reps)
+    return {"value": nodes / secs, "unit": UNIT, "cores": used, "kind": "port",
+            "sample": f"{reps} x the full workload ({len(w['graphs'])} instance(s)), oracle/pathdecomp.c, "
+                      f"same schedule and stop rule, {used} host threads"}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    import oracle as og
-    og.lib()
     w = workload(args.workload)
     threads = os.cpu_count() or 1
-    vals = []
-    for i in range(args.warmup + args.steps):
-        r = og.run(w["graph"], w["src"], w["dst"], threads=threads, eps=w["opts"].get("eps", 0.0))
-        if i >= args.warmup:
-            vals.append((r.nodes, r.seconds))
-    nodes = sum(v[0] for v in vals)
-    secs = sum(v[1] for v in vals)
+    for _ in range(args.warmup):
+        cpu_solve_all(w, threads, 1)
+    nodes, secs = 0, 0.0
+    for _ in range(args.steps):
+        n, s, _ = cpu_solve_all(w, threads, 1)
+        nodes += n
+        secs += s
     value = nodes / secs
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "impl": "reference",
-            "config": {"workload": w["name"], "parallelism": "host threads"},
+            "config": {"workload": w["name"], "parallelism": f"{threads} host threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"full workload per step, oracle/pathdecomp.c waves schedule, {threads} threads"},
+                             "sample": f"full workload per step, oracle/pathdecomp.c, {threads} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="k10")
+    ap.add_argument("--workload", default="k15batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
 
@@ -162,8 +203,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
     if world > 1:
-        import torch.distributed as dist
         import torch
+        import torch.distributed as dist
         backend = "nccl" if args.impl == "ours" else "gloo"
         if backend == "nccl":
             torch.cuda.set_device(local)
@@ -183,36 +224,61 @@ def main():
     torch.cuda.set_device(local)
     w = workload(args.workload)
     ctx = nr.Context(local)
+    batch = nr.Batch(w["graphs"], w["srcs"], w["dsts"])
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
-    def step():
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        return ctx.reliability(w["graph"], w["src"], w["dst"], capacity=w["capacity"], **w["opts"])
+    def call():
+        if w["kind"] == "batch":
+            return ctx.run_batch(batch, capacity=w["capacity"], raw=True, **w["opts"])
+        return [ctx.reliability(w["graphs"][0], w["srcs"][0], w["dsts"][0], capacity=w["capacity"],
+                                **w["opts"])._raw]
 
     for _ in range(max(3, args.warmup)):
-        step()
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        call()
     sampler = ClockSampler(local)
     sampler.start()
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
-    dev_ms, wall_s, nodes, pushes = 0.0, 0.0, 0, 0
-    results = []
+    dev_ms, wall_s, nodes, abytes = 0.0, 0.0, 0, 0
+    per_step = []
     for _ in range(args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = ctx.reliability(w["graph"], w["src"], w["dst"], capacity=w["capacity"], **w["opts"])
+        res = call()
         wall_s += time.perf_counter() - t0
-        dev_ms += r.ms
-        nodes += r.nodes
-        pushes += r.nodes - 1 - r.truncated * 0   # every pop but the root was a push
-        results.append(r)
+        ms = res[0].ms
+        n_step = sum(r.nodes for r in res)
+        b_step = sum((r.nodes + max(0, r.nodes - 1 + r.queued)) * item_bytes(r.n_edges) for r in res)
+        dev_ms += ms
+        nodes += n_step
+        abytes += b_step
+        per_step.append((ms, n_step, b_step))
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
+    r0 = res[0]
+    h2d = sum(r.h2d_bytes for r in res)
+    d2h = sum(r.d2h_bytes for r in res)
+    stats = {"R": r0.R, "esp": r0.esp, "paths": int(r0.paths), "nodes": int(r0.nodes),
+             "iterations": int(r0.iterations), "engine": nr.engine.ENGINES.get(r0.engine, r0.engine),
+             "nodes_per_step": nodes // args.steps}
+
+    # single-instance time-to-bound (latency), plain max-mass order
+    ttb = None
+    if args.workload == "k15batch":
+        tk, tb = [], []
+        for s in range(16):
+            r = ctx.reliability(w["graphs"][s], 0, 14, **w["opts"])
+            tk.append(r.ms)
+            tb.append(r.time_to_bound_ms)
+        ttb = {"plain_kernel_us_median": 1e3 * statistics.median(tk),
+               "plain_in_kernel_us_median": 1e3 * statistics.median(tb), "learned": None,
+               "instances": 16}
 
     t_dev = dev_ms / 1e3
     if dist is not None:
@@ -225,36 +291,32 @@ def main():
     else:
         tot_nodes = float(nodes)
     if rank != 0:
+        ctx.close()
         if dist is not None:
             dist.destroy_process_group()
         return
-    r0 = results[0]
     peak, peak_kind = peaks()
-    bytes_per_step = algorithmic_bytes(r0.n_edges, r0.nodes, r0.nodes - 1)
-    achieved = bytes_per_step / (r0.ms / 1e3) / 1e9 if r0.ms > 0 else 0.0
-    ach = [algorithmic_bytes(r.n_edges, r.nodes, r.nodes - 1) / (r.ms / 1e3) / 1e9 for r in results]
-    achieved = statistics.mean(ach)
+    achieved = statistics.mean(b / (ms / 1e3) / 1e9 for ms, _, b in per_step)
     line = {
         "metric": METRIC, "value": tot_nodes / t_dev, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+        "warmup": max(3, args.warmup), "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": w["name"], "l2": "flushed (512 MB write) before every step",
-                   "parallelism": f"replicas x{world}", "engine": r0.engine, "grid": r0.grid_blocks,
-                   "block": r0.block_threads},
-        "result": {"R": r0.R, "esp": r0.esp, "paths": r0.paths, "nodes": r0.nodes, "iterations": r0.iterations,
-                   "max_queue_items": r0.max_queue_items},
+                   "parallelism": f"replicas x{world}", "engine": stats["engine"],
+                   "grid": int(r0.grid_blocks), "block": int(r0.block_threads)},
+        "result": stats,
+        "time_to_bound": ttb,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "note": f"algorithmic bytes (4W+8 per queued subproblem, read+write) / kernel time; "
-                             f"peak {peak_kind}"},
-        "e2e": {"value": tot_nodes / wall_s, "unit": UNIT, "h2d_bytes_per_step": r0.h2d_bytes,
-                "d2h_bytes_per_step": r0.d2h_bytes},
-        "gpu_launches": args.steps,
+                     "note": f"achieved = algorithmic bytes (4W+8 per queued subproblem, written once and "
+                             f"read once) / kernel time; peak {peak_kind} copy bandwidth"},
+        "e2e": {"value": tot_nodes / wall_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps * (len({(r.n_nodes, r.mask_words) for r in res}) if w["kind"] == "batch" else 1),
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        line["cpu_baseline"] = cpu_port(w, threads, f"one full solve of the workload, {threads} threads")
+        line["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
     print(json.dumps(line), flush=True)
     ctx.close()
     if dist is not None:

@@ -82,7 +82,11 @@ typedef struct nr_options {
     int32_t  warps_per_block; /* 0 = engine default */
     double   timeout_ms;      /* device-side waits give up after this long without progress; 0 = 60 s */
     int32_t  verbose;         /* 1: print the reference's preamble lines on stdout */
-    int32_t  reserved[7];
+    int32_t  pad0;
+    uint64_t max_nodes;       /* per-instance pop budget for the warp engine; truncated runs stop
+                                 there with a valid R <= true <= R + ESP bracket, exhaustive runs
+                                 hand the instance to the whole-GPU engine; 0 = engine default */
+    int32_t  reserved[4];
 } nr_options;
 
 typedef struct nr_result {
@@ -96,7 +100,7 @@ typedef struct nr_result {
     uint64_t dead_ends;
     uint64_t truncated;
     uint64_t spilled;
-    uint64_t queued;            /* subproblems left in the queue when a target width stopped the run */
+    uint64_t queued;            /* subproblems left in the queue when a target width or budget stopped the run */
     int32_t  iterations;        /* waves (kernel iterations in the reference) */
     int32_t  n_nodes;           /* echo of the graph */
     int32_t  n_edges;
@@ -113,7 +117,8 @@ typedef struct nr_result {
     uint64_t capacity;          /* queue capacity actually used (items) */
     uint64_t h2d_bytes;         /* host -> device bytes copied by this call */
     uint64_t d2h_bytes;         /* device -> host bytes copied by this call */
-    int32_t  reserved[4];
+    int32_t  stop;              /* 0 queue empty, 1 target width met, 3 pop budget reached */
+    int32_t  reserved[3];
 } nr_result;
 
 enum { NR_ENGINE_GRID = 1, NR_ENGINE_WARP = 2 };

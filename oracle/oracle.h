@@ -97,6 +97,11 @@ void og_free_graph(og_graph *g);
 void og_default_opts(og_opts *o);
 int  og_run(const og_graph *g, int src, int dst, const og_opts *o, og_result *r);
 
+/* Solve n instances, one per worker thread at a time (wave schedule, single-
+ * threaded per instance, storage reused across instances). */
+int  og_run_batch(int n, const og_graph *graphs, const int32_t *srcs, const int32_t *dsts,
+                  const og_opts *o, og_result *results, int threads);
+
 /* Exact R by enumerating the 2^k states of the k edges with 0 < p < 1.
  * n_nodes <= 64, k <= 30. Returns a negative number on bad input. */
 double og_brute(const og_graph *g, int src, int dst);

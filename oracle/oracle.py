@@ -66,6 +66,9 @@ def lib():
         L.og_brute.restype = C.c_double
         L.og_bucket.argtypes = [C.c_double, C.c_int, C.c_int]
         L.og_bucket.restype = C.c_int
+        L.og_run_batch.argtypes = [C.c_int, C.POINTER(OgGraph), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                   C.POINTER(OgOpts), C.POINTER(OgResult), C.c_int]
+        L.og_run_batch.restype = C.c_int
         L.og_default_opts.argtypes = [C.POINTER(OgOpts)]
         L.og_default_opts.restype = None
         _lib = L
@@ -106,6 +109,45 @@ class _View:
                          self.col.ctypes.data_as(C.POINTER(C.c_int32)),
                          self.eid.ctypes.data_as(C.POINTER(C.c_int32)),
                          self.p.ctypes.data_as(C.POINTER(C.c_double)))
+
+
+def _opts(rule="level", precheck=False, order="waves", bucket_shift=-1, n_buckets=1, threads=1, eps=0.0,
+          target_width=0.0, capacity=0, max_nodes=0) -> OgOpts:
+    o = OgOpts()
+    lib().og_default_opts(C.byref(o))
+    o.bfs_rule = RULES[rule]
+    o.precheck = int(bool(precheck))
+    o.order = ORDERS[order]
+    o.bucket_shift = int(bucket_shift)
+    o.n_buckets = int(n_buckets)
+    o.threads = int(threads)
+    o.eps = float(eps)
+    o.target_width = float(target_width)
+    o.capacity = int(capacity)
+    o.max_nodes = int(max_nodes)
+    return o
+
+
+class BatchArgs:
+    """Host arrays for og_run_batch, built once (keeps the numpy views alive)."""
+
+    def __init__(self, graphs, srcs, dsts):
+        self.views = [_View(g) for g in graphs]
+        self.n = len(self.views)
+        self.arr = (OgGraph * self.n)(*[v.c for v in self.views])
+        self.s = np.ascontiguousarray(srcs, dtype=np.int32)
+        self.d = np.ascontiguousarray(dsts, dtype=np.int32)
+        self.res = (OgResult * self.n)()
+
+
+def run_batch(batch: BatchArgs, threads: int = 1, **kw):
+    """Solve every instance (one worker thread per instance at a time); returns raw results."""
+    o = _opts(**kw)
+    rc = lib().og_run_batch(batch.n, batch.arr, batch.s.ctypes.data_as(C.POINTER(C.c_int32)),
+                            batch.d.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(o), batch.res, int(threads))
+    if rc != 0:
+        raise ValueError("oracle rejected the batch")
+    return batch.res
 
 
 def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, order: str = "waves",

@@ -663,6 +663,184 @@ static int run_serial(const og_graph *g, int src, int dst, const og_opts *o, con
     return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* single-thread wave schedule with reusable storage (batches)           */
+/* ------------------------------------------------------------------ */
+typedef struct og_arena {
+    xctx x;
+    int n_cap, w_cap, e_cap, nb_cap;
+    ivec *bk;
+    ivec cur;
+    double *q;
+    uint32_t *root;
+} og_arena;
+
+static void arena_free(og_arena *a)
+{
+    if (a->n_cap) x_free(&a->x);
+    for (int i = 0; i < a->nb_cap; i++) free(a->bk[i].d);
+    free(a->bk); free(a->cur.d); free(a->q); free(a->root);
+    memset(a, 0, sizeof(*a));
+}
+
+static void arena_fit(og_arena *a, const og_graph *g, int src, int dst, const og_opts *o, int nb)
+{
+    int W = (g->n_edges * 2 + 31) / 32;
+    if (W < 1) W = 1;
+    if (g->n_nodes > a->n_cap || W > a->w_cap) {
+        if (a->n_cap) x_free(&a->x);
+        og_graph big = *g;
+        og_opts oo = *o;
+        big.n_nodes = g->n_nodes > a->n_cap ? g->n_nodes : a->n_cap;
+        x_init(&a->x, &big, NULL, src, dst, &oo);
+        free(a->x.work); free(a->x.child);
+        int wc = W > a->w_cap ? W : a->w_cap;
+        a->x.work = (uint32_t *)malloc(wc * sizeof(uint32_t));
+        a->x.child = (uint32_t *)malloc(wc * sizeof(uint32_t));
+        a->n_cap = big.n_nodes;
+        a->w_cap = wc;
+    }
+    if (g->n_edges > a->e_cap) {
+        free(a->q); free(a->root);
+        a->e_cap = g->n_edges;
+        a->q = (double *)malloc((size_t)(a->e_cap > 0 ? a->e_cap : 1) * sizeof(double));
+        a->root = (uint32_t *)malloc((size_t)(a->w_cap > W ? a->w_cap : W) * sizeof(uint32_t));
+    }
+    if (nb > a->nb_cap) {
+        a->bk = (ivec *)realloc(a->bk, nb * sizeof(ivec));
+        memset(a->bk + a->nb_cap, 0, (nb - a->nb_cap) * sizeof(ivec));
+        a->nb_cap = nb;
+    }
+    /* point the context at this graph; scratch arrays are reused */
+    xctx *x = &a->x;
+    x->g = g; x->q = a->q; x->src = src; x->dst = dst; x->W = W;
+    x->rule = o->bfs_rule; x->precheck = o->precheck; x->eps = o->eps;
+    x->gen = 0;
+    memset(x->vis, 0, a->n_cap * sizeof(uint32_t));
+    x->R.hi = x->R.lo = x->esp_trunc.hi = x->esp_trunc.lo = x->esp_spill.hi = x->esp_spill.lo = 0;
+    x->nodes = x->leaves = x->dead = x->truncated = x->spilled = x->pruned = x->pushes = 0;
+}
+
+typedef struct { ivec *bk; int W, shift, nb; uint64_t capacity, queued; } st_sink;
+
+static int st_sink_fn(void *ud, const uint32_t *mask, double mass)
+{
+    st_sink *s = (st_sink *)ud;
+    if (s->capacity && s->queued >= s->capacity) return 1;
+    int b = og_bucket(mass, s->shift, s->nb);
+    if (iv_push(&s->bk[b], mask, mass, s->W)) return 1;
+    s->queued++;
+    return 0;
+}
+
+/* Same schedule as run_waves with one thread: children go straight into
+ * their buckets (the running wave was swapped out first). */
+static int run_waves_arena(og_arena *a, const og_graph *g, int src, int dst, const og_opts *o, og_result *r)
+{
+    int nb = (o->bucket_shift < 0) ? 1 : (o->n_buckets > 0 ? o->n_buckets : 1);
+    arena_fit(a, g, src, dst, o, nb);
+    xctx *x = &a->x;
+    int W = x->W;
+    for (int e = 0; e < g->n_edges; e++) a->q[e] = 1.0 - g->edge_p[e];
+    memset(a->root, 0, W * sizeof(uint32_t));
+    for (int e = 0; e < g->n_edges; e++) {
+        double p = g->edge_p[e];
+        if (p <= 0.0) { }
+        else if (p >= 1.0) a->root[e >> 4] |= 1u << ((e & 15) * 2);
+        else a->root[e >> 4] |= 3u << ((e & 15) * 2);
+    }
+    for (int i = 0; i < nb; i++) { a->bk[i].n = 0; a->bk[i].mass.hi = a->bk[i].mass.lo = 0; }
+    st_sink sk = { a->bk, W, o->bucket_shift, nb, o->capacity, 1 };
+    iv_push(&a->bk[og_bucket(1.0, o->bucket_shift, nb)], a->root, 1.0, W);
+    int status = 0;
+    uint64_t waves = 0, max_wave = 0, max_q = 1;
+    for (;;) {
+        int b = -1;
+        for (int i = 0; i < nb; i++) if (a->bk[i].n) { b = i; break; }
+        if (b < 0) break;
+        if (o->target_width > 0) {
+            ksum wdt = x->esp_trunc;
+            ks_merge(&wdt, &x->esp_spill);
+            for (int i = 0; i < nb; i++) ks_merge(&wdt, &a->bk[i].mass);
+            if (ks_val(&wdt) <= o->target_width) { status = 1; break; }
+        }
+        if (o->max_nodes && x->nodes >= o->max_nodes) { status = 2; break; }
+        ivec t = a->cur; a->cur = a->bk[b]; a->bk[b] = t;
+        a->bk[b].n = 0; a->bk[b].mass.hi = a->bk[b].mass.lo = 0;
+        waves++;
+        if (a->cur.n > max_wave) max_wave = a->cur.n;
+        for (size_t i = 0; i < a->cur.n; i++) {
+            x_expand(x, iv_rec(&a->cur, i, W), iv_mass(&a->cur, i, W), st_sink_fn, &sk);
+            sk.queued--;
+        }
+        if (sk.queued > max_q) max_q = sk.queued;
+    }
+    ksum qm = {0, 0};
+    uint64_t queued = 0;
+    for (int i = 0; i < nb; i++) { ks_merge(&qm, &a->bk[i].mass); queued += a->bk[i].n; }
+    memset(r, 0, sizeof(*r));
+    r->R = ks_val(&x->R);
+    r->esp_truncated = ks_val(&x->esp_trunc);
+    r->esp_spilled = ks_val(&x->esp_spill);
+    r->queued_mass = ks_val(&qm);
+    ksum e = x->esp_trunc; ks_merge(&e, &x->esp_spill); ks_merge(&e, &qm);
+    r->esp = ks_val(&e);
+    r->nodes = x->nodes; r->leaves = x->leaves; r->dead = x->dead; r->truncated = x->truncated;
+    r->spilled = x->spilled; r->pruned = x->pruned; r->pushes = x->pushes;
+    r->queued = queued; r->waves = waves; r->max_wave = max_wave; r->max_queued = max_q;
+    r->paths = r->leaves + r->spilled;
+    r->status = status;
+    return 0;
+}
+
+typedef struct {
+    int n;
+    const og_graph *graphs;
+    const int32_t *srcs, *dsts;
+    const og_opts *o;
+    og_result *res;
+    atomic_int next;
+} batch_job;
+
+static void *batch_thread(void *arg)
+{
+    batch_job *j = (batch_job *)arg;
+    og_arena a;
+    memset(&a, 0, sizeof(a));
+    for (;;) {
+        int i = atomic_fetch_add(&j->next, 1);
+        if (i >= j->n) break;
+        const og_graph *g = &j->graphs[i];
+        og_result *r = &j->res[i];
+        if (g->n_nodes <= 0 || j->srcs[i] < 0 || j->dsts[i] < 0 || j->srcs[i] >= g->n_nodes ||
+            j->dsts[i] >= g->n_nodes) {
+            memset(r, 0, sizeof(*r));
+            r->status = -1;
+            continue;
+        }
+        double t0 = now_s();
+        run_waves_arena(&a, g, j->srcs[i], j->dsts[i], j->o, r);
+        r->seconds = now_s() - t0;
+    }
+    arena_free(&a);
+    return NULL;
+}
+
+int og_run_batch(int n, const og_graph *graphs, const int32_t *srcs, const int32_t *dsts, const og_opts *o,
+                 og_result *res, int threads)
+{
+    if (n < 0 || (n > 0 && (!graphs || !srcs || !dsts || !res))) return -1;
+    if (threads < 1) threads = 1;
+    batch_job j = { n, graphs, srcs, dsts, o, res, 0 };
+    atomic_init(&j.next, 0);
+    pthread_t *t = (pthread_t *)calloc(threads, sizeof(pthread_t));
+    for (int i = 1; i < threads; i++) pthread_create(&t[i], NULL, batch_thread, &j);
+    batch_thread(&j);
+    for (int i = 1; i < threads; i++) pthread_join(t[i], NULL);
+    free(t);
+    return 0;
+}
+
 int og_run(const og_graph *g, int src, int dst, const og_opts *o, og_result *r)
 {
     memset(r, 0, sizeof(*r));
@@ -685,7 +863,12 @@ int og_run(const og_graph *g, int src, int dst, const og_opts *o, og_result *r)
         else root[e >> 4] |= 3u << ((e & 15) * 2);
     }
     int rc;
-    if (o->order == OG_ORDER_WAVES) rc = run_waves(g, src, dst, o, q, root, r);
+    if (o->order == OG_ORDER_WAVES && o->threads <= 1) {
+        og_arena a;
+        memset(&a, 0, sizeof(a));
+        rc = run_waves_arena(&a, g, src, dst, o, r);
+        arena_free(&a);
+    } else if (o->order == OG_ORDER_WAVES) rc = run_waves(g, src, dst, o, q, root, r);
     else rc = run_serial(g, src, dst, o, q, root, r);
     r->paths = r->leaves + r->spilled;
     r->seconds = now_s() - t0;

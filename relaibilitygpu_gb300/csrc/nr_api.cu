@@ -14,10 +14,14 @@
 #include <vector>
 
 #include "nr_internal.h"
+#include "nr_warp.cuh"
 
 const void *nr_grid_kernel_ptr_g8(int w4);
 const void *nr_grid_kernel_ptr_g16(int w4);
 const void *nr_grid_kernel_ptr_g32(int w4);
+const void *nr_warp_kernel_ptr_g8(int w4);
+const void *nr_warp_kernel_ptr_g16(int w4);
+const void *nr_warp_kernel_ptr_g32(int w4);
 
 namespace {
 
@@ -60,6 +64,16 @@ const void *grid_kernel(int G, int w4)
     }
 }
 
+const void *warp_kernel(int G, int w4)
+{
+    switch (G) {
+    case 8: return nr_warp_kernel_ptr_g8(w4);
+    case 16: return nr_warp_kernel_ptr_g16(w4);
+    case 32: return nr_warp_kernel_ptr_g32(w4);
+    default: return nullptr;
+    }
+}
+
 int group_width(int n)
 {
     if (n <= 8) return 8;
@@ -80,6 +94,10 @@ struct nr_context {
     size_t qbytes = 0;
     void *sbuf = nullptr;       // blob, counters, barrier, status, partials
     size_t sbytes = 0;
+    void *wslab = nullptr;      // warp engine: per-warp page slabs
+    size_t wslab_bytes = 0;
+    void *wbuf = nullptr;       // warp engine: blob, descriptors, outputs, counters
+    size_t wbuf_bytes = 0;
     std::mutex mu;
 };
 
@@ -120,27 +138,36 @@ static int validate(const nr_graph *g, int src, int dst)
     return NR_OK;
 }
 
-static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *sg, std::vector<unsigned char> *blob)
+static int group_width_of(int n) { return group_width(n); }
+
+// Graph tables of one instance for the small engines (layout in nr_internal.h).
+static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *sg, std::vector<unsigned char> *blob,
+                             size_t at = 0)
 {
     const int n = g->n_nodes, E = g->n_edges;
+    const int G = group_width_of(n);
     const int W = std::max(1, (2 * E + 31) / 32);
     sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst;
     sg->n_in = g->n_arcs;
     size_t off = 0;
     sg->off_p = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
     sg->off_q = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
-    sg->off_eid = (int)off; off = align16(off + sizeof(uint16_t) * 32 * 32);
-    sg->off_start = (int)off; off = align16(off + sizeof(int) * 33);
+    sg->off_eid = (int)off; off = align16(off + sizeof(uint16_t) * G * G);
+    sg->off_start = (int)off; off = align16(off + sizeof(int) * (n + 1));
     sg->off_list = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
+    sg->off_root = (int)off; off = align16(off + sizeof(uint32_t) * 4 * sg->w4);
     sg->blob_bytes = (int)off;
-    blob->assign(off, 0);
-    double *p = reinterpret_cast<double *>(blob->data() + sg->off_p);
-    double *q = reinterpret_cast<double *>(blob->data() + sg->off_q);
-    uint16_t *eid = reinterpret_cast<uint16_t *>(blob->data() + sg->off_eid);
-    int *start = reinterpret_cast<int *>(blob->data() + sg->off_start);
-    uint32_t *list = reinterpret_cast<uint32_t *>(blob->data() + sg->off_list);
+    sg->blob_off = (long long)at;
+    blob->resize(at + off, 0);
+    unsigned char *b = blob->data() + at;
+    double *p = reinterpret_cast<double *>(b + sg->off_p);
+    double *q = reinterpret_cast<double *>(b + sg->off_q);
+    uint16_t *eid = reinterpret_cast<uint16_t *>(b + sg->off_eid);
+    int *start = reinterpret_cast<int *>(b + sg->off_start);
+    uint32_t *list = reinterpret_cast<uint32_t *>(b + sg->off_list);
+    uint32_t *root = reinterpret_cast<uint32_t *>(b + sg->off_root);
     for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
-    for (int i = 0; i < 32 * 32; ++i) eid[i] = 0xffff;
+    for (int i = 0; i < G * G; ++i) eid[i] = 0xffff;
     // in-arcs grouped by head node; arc (u -> v) for every CSR entry of u
     std::vector<int> cnt(n + 1, 0);
     for (int u = 0; u < n; ++u)
@@ -152,8 +179,13 @@ static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *
         for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
             const int v = g->col_idx[j], e = g->edge_id[j];
             list[start[v] + fill[v]++] = ((uint32_t)e << 8) | (uint32_t)u;
-            if (eid[u * 32 + v] == 0xffff) eid[u * 32 + v] = (uint16_t)e;   // first arc u->v in CSR order
+            if (eid[u * G + v] == 0xffff) eid[u * G + v] = (uint16_t)e;   // first arc u->v in CSR order
         }
+    for (int e = 0; e < E; ++e) {
+        const double pe = g->edge_p[e];
+        const uint32_t st = (pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN;
+        root[e >> 4] |= st << ((e & 15) * 2);
+    }
 }
 
 extern "C" int nr_initial_mask(const nr_graph *g, uint32_t *words, int n_words)
@@ -233,6 +265,8 @@ extern "C" void nr_context_destroy(nr_context *c)
     cudaSetDevice(c->device);
     if (c->qbuf) cudaFree(c->qbuf);
     if (c->sbuf) cudaFree(c->sbuf);
+    if (c->wslab) cudaFree(c->wslab);
+    if (c->wbuf) cudaFree(c->wbuf);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -369,6 +403,190 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
     return NR_OK;
 }
 
+// ---------------------------------------------------------------------------
+// warp-per-instance engine (nr_warp.cuh)
+// ---------------------------------------------------------------------------
+struct WarpRunCfg {
+    int wave_mode, shift, n_buckets, pages, escalate;
+    double eps, target;
+    unsigned long long max_nodes;
+};
+
+static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhaustive)
+{
+    WarpRunCfg w;
+    w.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
+    w.target = o->target_width > 0 ? o->target_width : 0.0;
+    if (exhaustive) {
+        w.wave_mode = 0; w.shift = -1; w.n_buckets = 32; w.escalate = 1;
+        w.max_nodes = o->max_nodes ? o->max_nodes : (1ull << 21);
+    } else {
+        w.wave_mode = 1; w.shift = o->bucket_shift; w.escalate = 0; w.max_nodes = o->max_nodes;
+        int nb = o->n_buckets > 0 ? o->n_buckets : 256;
+        nb = std::min(1024, (nb + 31) / 32 * 32);
+        w.n_buckets = nb;
+    }
+    if (capacity == 0) w.pages = 512;
+    else w.pages = (int)std::min<uint64_t>(8192, std::max<uint64_t>(4, (capacity + NR_PAGE - 1) / NR_PAGE));
+    return w;
+}
+
+static void fill_from_warp(const NrWarpOut &w, const WarpRunCfg &cfg, int W4, nr_result *r)
+{
+    KS R, esp;
+    R.merge(w.R_hi, w.R_lo);
+    esp.merge(w.et_hi, w.et_lo);
+    esp.merge(w.es_hi, w.es_lo);
+    esp.merge(w.q_hi, w.q_lo);
+    r->R = R.val();
+    r->esp = esp.val();
+    if (r->esp < 0) r->esp = 0;   // queued-mass rounding can leave -1e-17 on an empty queue
+    r->R_plus_esp = r->R + r->esp;
+    r->trunc_bound = r->R > 0 ? r->esp / r->R : r->esp;
+    r->nodes = w.nodes; r->leaves = w.leaves; r->dead_ends = w.dead; r->truncated = w.trunc;
+    r->spilled = w.spilled; r->paths = w.leaves + w.spilled; r->queued = w.queued;
+    r->iterations = w.waves;
+    r->max_queue_items = w.max_wave;
+    r->item_bytes = 16 * W4 + 8;
+    r->max_queue_mb = (double)w.max_wave * r->item_bytes / (1024.0 * 1024.0);
+    r->time_to_bound_ms = w.t_ns / 1e6;
+    r->engine = NR_ENGINE_WARP;
+    r->stop = w.status;
+    r->capacity = (uint64_t)cfg.pages * NR_PAGE;
+}
+
+// Solve n instances with the warp engine; instances the engine hands over
+// (status 2) are left with engine = 0 for the caller.
+static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
+                          const WarpRunCfg &cfg, nr_result *res, std::vector<int> *handover)
+{
+    std::vector<unsigned char> blob;
+    std::vector<NrSmallGraph> desc(n);
+    std::map<std::pair<int, int>, std::vector<int>> classes;
+    for (int i = 0; i < n; ++i) {
+        build_small_blob(&gs[i], srcs[i], dsts[i], &desc[i], &blob, blob.size());
+        classes[{group_width(gs[i].n_nodes), desc[i].w4}].push_back(i);
+    }
+    // descriptors and ids in class order
+    std::vector<NrSmallGraph> dsorted;
+    std::vector<int> ids;
+    std::vector<std::pair<std::pair<int, int>, std::pair<int, int>>> spans;   // class -> [begin, count)
+    for (auto &kv : classes) {
+        spans.push_back({kv.first, {(int)ids.size(), (int)kv.second.size()}});
+        for (int i : kv.second) { dsorted.push_back(desc[i]); ids.push_back(i); }
+    }
+    const int nclass = (int)spans.size();
+    // launch geometry per class and slab size
+    const int block = NR_WARP_BLOCK, warps_pb = block / 32;
+    std::vector<int> grids(nclass);
+    std::vector<size_t> smems(nclass);
+    size_t slab_need = 0;
+    for (int k = 0; k < nclass; ++k) {
+        const int G = spans[k].first.first, W4 = spans[k].first.second;
+        if (W4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
+        const void *kfn = warp_kernel(G, W4);
+        if (!kfn) return NR_ERR_UNSUPPORTED;
+        const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfg.pages) * warps_pb;
+        NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int bps = 0;
+        NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
+        if (bps < 1) return NR_ERR_UNSUPPORTED;
+        const int cnt = spans[k].second.second;
+        const int grid = std::max(1, std::min(bps * c->sms, (cnt + warps_pb - 1) / warps_pb));
+        grids[k] = grid;
+        smems[k] = smem;
+        slab_need = std::max(slab_need, (size_t)grid * warps_pb * cfg.pages * NR_PAGE * (16 * (size_t)W4 + 8));
+    }
+    int rc = ensure(&c->wslab, &c->wslab_bytes, slab_need);
+    if (rc) return rc;
+    size_t off = 0;
+    const size_t off_blob = off; off = align16(off + blob.size());
+    const size_t off_desc = off; off = align16(off + sizeof(NrSmallGraph) * n);
+    const size_t off_ids = off; off = align16(off + sizeof(int) * n);
+    const size_t off_out = off; off = align16(off + sizeof(NrWarpOut) * n);
+    const size_t off_cnt = off; off = align16(off + sizeof(int) * nclass);
+    rc = ensure(&c->wbuf, &c->wbuf_bytes, off);
+    if (rc) return rc;
+    unsigned char *wb = static_cast<unsigned char *>(c->wbuf);
+    cudaStream_t s = c->stream;
+    NR_CUDA_TRY(cudaMemcpyAsync(wb + off_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(wb + off_desc, dsorted.data(), sizeof(NrSmallGraph) * n, cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(wb + off_ids, ids.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemsetAsync(wb + off_cnt, 0, sizeof(int) * nclass, s));
+    NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
+    for (int k = 0; k < nclass; ++k) {
+        const int G = spans[k].first.first, W4 = spans[k].first.second;
+        NrWarpParams P;
+        P.blob = wb + off_blob;
+        P.inst = reinterpret_cast<const NrSmallGraph *>(wb + off_desc) + spans[k].second.first;
+        P.inst_id = reinterpret_cast<const int *>(wb + off_ids) + spans[k].second.first;
+        P.n_inst = spans[k].second.second;
+        P.next_inst = reinterpret_cast<int *>(wb + off_cnt) + k;
+        P.slab_mask = static_cast<uint4 *>(c->wslab);
+        const size_t warps = (size_t)grids[k] * warps_pb;
+        P.slab_mass = reinterpret_cast<double *>(static_cast<unsigned char *>(c->wslab) +
+                                                 warps * cfg.pages * NR_PAGE * 16 * (size_t)W4);
+        P.pages = cfg.pages;
+        P.n_buckets = cfg.n_buckets;
+        P.shift = cfg.shift;
+        P.wave_mode = cfg.wave_mode;
+        P.escalate = cfg.escalate;
+        P.eps = cfg.eps;
+        P.target = cfg.target;
+        P.max_nodes = cfg.max_nodes;
+        P.out = reinterpret_cast<NrWarpOut *>(wb + off_out);
+        void *args[] = {&P};
+        NR_CUDA_TRY(cudaLaunchKernel(warp_kernel(G, W4), dim3(grids[k]), dim3(block), args, smems[k], s));
+    }
+    NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
+    std::vector<NrWarpOut> out(n);
+    NR_CUDA_TRY(cudaMemcpyAsync(out.data(), wb + off_out, sizeof(NrWarpOut) * n, cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    for (int i = 0; i < n; ++i) {
+        nr_result *r = &res[i];
+        r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
+        r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
+        if (out[i].status == 2) { handover->push_back(i); continue; }
+        fill_from_warp(out[i], cfg, desc[i].w4, r);
+        r->ms = ms;
+        r->grid_blocks = grids[0];
+        r->block_threads = block;
+        r->h2d_bytes = desc[i].blob_bytes + sizeof(NrSmallGraph) + sizeof(int);
+        r->d2h_bytes = sizeof(NrWarpOut);
+    }
+    return NR_OK;
+}
+
+extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs,
+                                    const int32_t *dsts, uint64_t capacity, const nr_options *opt,
+                                    nr_result *res)
+{
+    if (!c || n < 0 || (n > 0 && (!gs || !srcs || !dsts || !res))) return NR_ERR_INVALID;
+    if (n == 0) return NR_OK;
+    nr_options o;
+    if (opt) o = *opt; else nr_options_default(&o);
+    for (int i = 0; i < n; ++i) {
+        memset(&res[i], 0, sizeof(nr_result));
+        int rc = validate(&gs[i], srcs[i], dsts[i]);
+        if (rc) return rc;
+        if (gs[i].n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lock(c->mu);
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
+    const WarpRunCfg cfg = warp_cfg(&o, capacity, exhaustive);
+    std::vector<int> handover;
+    int rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover);
+    if (rc) return rc;
+    for (int i : handover) {
+        rc = run_grid_small(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, &res[i]);
+        if (rc) return rc;
+    }
+    return NR_OK;
+}
+
 extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int dst, uint64_t capacity,
                                   const nr_options *opt, nr_result *res)
 {
@@ -387,8 +605,15 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     std::lock_guard<std::mutex> lock(c->mu);
     NR_CUDA_TRY(cudaSetDevice(c->device));
     if (g->n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
-    if (o.target_width > 0 || (o.order != NR_ORDER_AUTO && o.order != NR_ORDER_WAVES))
-        return NR_ERR_UNSUPPORTED;
+    if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {
+        // bucketed max-mass order: one warp owns the instance (nr_warp.cuh)
+        const WarpRunCfg cfg = warp_cfg(&o, capacity, false);
+        std::vector<int> handover;
+        int rc = run_warp_batch(c, 1, g, &src, &dst, cfg, res, &handover);
+        if (rc) return rc;
+        if (!handover.empty()) return NR_ERR_INTERNAL;
+        return NR_OK;
+    }
     return run_grid_small(c, g, src, dst, capacity, &o, res);
 }
 
@@ -407,11 +632,6 @@ extern "C" int nr_reliability(const nr_graph *g, int src, int dst, uint64_t capa
     return rc;
 }
 
-extern "C" int nr_reliability_batch(nr_context *, int, const nr_graph *, const int32_t *, const int32_t *,
-                                    uint64_t, const nr_options *, nr_result *)
-{
-    return NR_ERR_UNSUPPORTED;
-}
 
 // ---------------------------------------------------------------------------
 // graph file loader (workingPad/graph.h:46-145 semantics, status codes instead of exit)

@@ -1,18 +1,20 @@
 // nr_engine_g32.cu -- kernels for graphs with up to 32 nodes (lane groups of 32).
 // One translation unit per group width keeps the build parallel.
 #include "nr_grid.cuh"
+#include "nr_warp.cuh"
 
-const void *nr_grid_kernel_ptr_g32(int w4)
-{
-    switch (w4) {
-    case 1: return (const void *)nr_grid_kernel<32, 1>;
-    case 2: return (const void *)nr_grid_kernel<32, 2>;
-    case 3: return (const void *)nr_grid_kernel<32, 3>;
-    case 4: return (const void *)nr_grid_kernel<32, 4>;
-    case 5: return (const void *)nr_grid_kernel<32, 5>;
-    case 6: return (const void *)nr_grid_kernel<32, 6>;
-    case 7: return (const void *)nr_grid_kernel<32, 7>;
-    case 8: return (const void *)nr_grid_kernel<32, 8>;
-    default: return nullptr;
+#define NR_W4_CASES(KERNEL)                              \
+    switch (w4) {                                        \
+    case 1: return (const void *)KERNEL<32, 1>;           \
+    case 2: return (const void *)KERNEL<32, 2>;           \
+    case 3: return (const void *)KERNEL<32, 3>;           \
+    case 4: return (const void *)KERNEL<32, 4>;           \
+    case 5: return (const void *)KERNEL<32, 5>;           \
+    case 6: return (const void *)KERNEL<32, 6>;           \
+    case 7: return (const void *)KERNEL<32, 7>;           \
+    case 8: return (const void *)KERNEL<32, 8>;           \
+    default: return nullptr;                             \
     }
-}
+
+const void *nr_grid_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_grid_kernel) }
+const void *nr_warp_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_warp_kernel) }

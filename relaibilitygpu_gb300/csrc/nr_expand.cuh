@@ -19,7 +19,7 @@
 struct NrSmemGraph {
     const double *p;
     const double *q;
-    const uint16_t *eid;      // [32*32] arc (u -> v) -> edge id
+    const uint16_t *eid;      // [G*G] arc (u -> v) -> edge id
     const int *start;         // [n+1] in-arc ranges
     const uint32_t *list;     // in-arcs of v: (eid << 8) | u
 };
@@ -121,7 +121,7 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
     int e_h = 0;
     bool unk = false;
     if (v < L) {
-        e_h = sg.eid[hop_u * 32 + hop_v];
+        e_h = sg.eid[hop_u * G + hop_v];
         unk = ((my_m[e_h >> 4] >> ((e_h & 15) << 1)) & 3u) == 3u;
     }
 

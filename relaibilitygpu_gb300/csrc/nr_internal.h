@@ -26,12 +26,14 @@ struct NrPartial {
     unsigned long long nodes, leaves, dead, truncated, spilled, pad;
 };
 
-// Graph tables staged into shared memory by every block (small engines).
-// Laid out in one device blob: p[E], q[E] (double), eid_tab[32*32] (u16),
-// in_start[33] (int), in_list[n_in] (u32 = eid << 8 | u).
+// Graph tables of one instance (small engines), laid out in one blob:
+// p[E], q[E] (double), eid_tab[G*G] (u16, arc u->v at u*G+v), in_start[n+1]
+// (int), in_list[n_in] (u32 = eid << 8 | u), root mask (4*w4 words).
+// Offsets are relative to blob_off; every section starts 16-byte aligned.
 struct NrSmallGraph {
     int n, e, w4, src, dst, n_in;
-    int off_p, off_q, off_eid, off_start, off_list, blob_bytes;
+    int off_p, off_q, off_eid, off_start, off_list, off_root, blob_bytes;
+    long long blob_off;
 };
 
 struct NrGridParams {

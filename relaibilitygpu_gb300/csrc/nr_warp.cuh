@@ -1,0 +1,312 @@
+// nr_warp.cuh -- warp-per-instance engine for batches and small truncated runs.
+//
+// The reference runs one graph per process through a host-driven wave loop
+// (workingPad/main.cu:963-1008).  Here each warp takes whole instances from
+// a device counter and solves them with a private queue:
+//   * subproblems live in the warp's own slab of HBM, in pages of 32 records
+//     (16-byte mask blocks + FP64 mass);
+//   * page chains are grouped into mass buckets (the bucketed max-mass
+//     priority queue); chain heads, page counts, a free-page stack and a
+//     bucket bitmap sit in the warp's shared memory, so queue bookkeeping
+//     needs no atomics and no global synchronisation;
+//   * wave mode (truncated runs): a wave takes the whole chain of the
+//     fullest non-empty bucket; children land in fresh chains, so the set of
+//     expanded subproblems, and the stop test between waves (ESP + queued
+//     mass <= target), match the oracle's wave schedule exactly;
+//   * page mode (exhaustive runs): one page at a time, depth-first, which
+//     keeps the live queue small; results do not depend on the order.
+// A warp that runs out of pages (or past max_nodes) either spills the child
+// mass into ESP, as the reference does when its queue is full
+// (main.cu:245-252), or marks the instance for the whole-GPU engine.
+#pragma once
+
+#include "nr_expand.cuh"
+
+#define NR_WARP_BLOCK 128
+#define NR_PAGE 32
+
+struct NrWarpOut {
+    double R_hi, R_lo, et_hi, et_lo, es_hi, es_lo, q_hi, q_lo;
+    unsigned long long nodes, leaves, dead, trunc, spilled, queued, max_wave;
+    long long t_ns;       // device time from instance start to stop (target met or queue empty)
+    int waves;
+    int status;           // 0 queue empty, 1 target width met, 2 handed over, 3 budget reached
+};
+
+struct NrWarpParams {
+    const unsigned char *blob;       // all instances' graph tables
+    const NrSmallGraph *inst;        // [n_inst] (this class only)
+    const int *inst_id;              // [n_inst] -> index into out
+    int n_inst;
+    int *next_inst;                  // work counter
+    uint4 *slab_mask;                // [warps][pages*32][w4]
+    double *slab_mass;               // [warps][pages*32]
+    int pages;                       // pages per warp
+    int n_buckets;                   // multiple of 32, <= 256
+    int shift;                       // bucket resolution (2^shift per octave); < 0 = one bucket
+    int wave_mode;                   // 1: whole-bucket waves; 0: one page at a time
+    int escalate;                    // 1: on overflow hand the instance to the grid engine
+    double eps;
+    double target;                   // stop once ESP + queued mass <= target (wave mode)
+    unsigned long long max_nodes;    // pop budget: page mode hands over, wave mode stops (0 = none)
+    NrWarpOut *out;
+};
+
+__device__ __forceinline__ int nr_bucket(double m, int shift, int nb)
+{
+    if (shift < 0 || nb <= 1) return 0;
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(m);
+    const long long key = (long long)(bits >> (52 - shift));
+    long long b = (1023LL << shift) - key;
+    b = b < 0 ? 0 : b;
+    b = b > nb - 1 ? nb - 1 : b;
+    return (int)b;
+}
+
+__device__ __forceinline__ NrKs nr_ks_warp_sum(NrKs s)
+{
+    for (int off = 16; off > 0; off >>= 1) {
+        NrKs o = nr_ks_shfl_down(s, off);
+        nr_ks_merge(s, o);
+    }
+    s.hi = __shfl_sync(NR_FULL, s.hi, 0);
+    s.lo = __shfl_sync(NR_FULL, s.lo, 0);
+    return s;
+}
+
+__device__ __forceinline__ unsigned long long nr_warp_sum_u64(unsigned long long x)
+{
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(NR_FULL, x, off);
+    return x;
+}
+
+// shared memory of one warp: staged items, bucket heads and bitmap, page metadata
+struct NrWarpShm {
+    uint32_t *masks;     // [K * 4 * W4]
+    short *heads;        // [n_buckets]
+    uint32_t *bitmap;    // [n_buckets / 32]
+    short *pnext;        // [pages]
+    unsigned char *pcnt; // [pages]
+    short *freel;        // [pages]
+};
+
+__host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets, int pages)
+{
+    size_t b = (size_t)K * 4 * W4 * 4;
+    b += (size_t)n_buckets * 2;
+    b = (b + 3) & ~size_t(3);
+    b += (size_t)(n_buckets / 32) * 4;
+    b += (size_t)pages * 2;
+    b += (size_t)pages;
+    b = (b + 1) & ~size_t(1);
+    b += (size_t)pages * 2;
+    return (b + 15) & ~size_t(15);
+}
+
+template <int G, int W4>
+__global__ void __launch_bounds__(NR_WARP_BLOCK) nr_warp_kernel(NrWarpParams P)
+{
+    constexpr int K = 32 / G;
+    constexpr int NW = 4 * W4;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int grp = lane / G, v = lane & (G - 1);
+    const bool leader = (v == 0);
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int NB = P.n_buckets, NP = P.pages;
+
+    NrWarpShm sh;
+    {
+        unsigned char *b = smem + (size_t)warp * nr_warp_shm_bytes(K, W4, NB, NP);
+        size_t o = 0;
+        sh.masks = reinterpret_cast<uint32_t *>(b + o); o += (size_t)K * NW * 4;
+        sh.heads = reinterpret_cast<short *>(b + o); o += (size_t)NB * 2; o = (o + 3) & ~size_t(3);
+        sh.bitmap = reinterpret_cast<uint32_t *>(b + o); o += (size_t)(NB / 32) * 4;
+        sh.pnext = reinterpret_cast<short *>(b + o); o += (size_t)NP * 2;
+        sh.pcnt = b + o; o += (size_t)NP; o = (o + 1) & ~size_t(1);
+        sh.freel = reinterpret_cast<short *>(b + o);
+    }
+    uint32_t *my_m = sh.masks + grp * NW;
+    const size_t gw = (size_t)blockIdx.x * (blockDim.x >> 5) + warp;
+    uint4 *sl_mask = P.slab_mask + gw * (size_t)NP * NR_PAGE * W4;
+    double *sl_mass = P.slab_mass + gw * (size_t)NP * NR_PAGE;
+
+    for (;;) {
+        int ii = 0;
+        if (lane == 0) ii = atomicAdd(P.next_inst, 1);
+        ii = __shfl_sync(NR_FULL, ii, 0);
+        if (ii >= P.n_inst) break;
+        const NrSmallGraph g = P.inst[ii];
+        const unsigned char *gb = P.blob + g.blob_off;
+        NrSmemGraph sg;
+        sg.p = reinterpret_cast<const double *>(gb + g.off_p);
+        sg.q = reinterpret_cast<const double *>(gb + g.off_q);
+        sg.eid = reinterpret_cast<const uint16_t *>(gb + g.off_eid);
+        sg.start = reinterpret_cast<const int *>(gb + g.off_start);
+        sg.list = reinterpret_cast<const uint32_t *>(gb + g.off_list);
+        const uint32_t *root = reinterpret_cast<const uint32_t *>(gb + g.off_root);
+        const long long t0 = nr_globaltimer();
+
+        // reset the private queue; the root is the only subproblem
+        for (int b = lane; b < NB; b += 32) sh.heads[b] = -1;
+        for (int b = lane; b < NB / 32; b += 32) sh.bitmap[b] = 0u;
+        for (int p = lane; p < NP; p += 32) { sh.freel[p] = (short)(NP - 1 - p); sh.pnext[p] = -1; sh.pcnt[p] = 0; }
+        int top = NP;
+        __syncwarp();
+        int rpg = 0;
+        if (lane == 0) {
+            const int rb = nr_bucket(1.0, P.shift, NB);
+            rpg = sh.freel[--top];
+            sh.heads[rb] = (short)rpg;
+            sh.pcnt[rpg] = 1;
+            sh.pnext[rpg] = -1;
+            sh.bitmap[rb >> 5] |= 1u << (rb & 31);
+        }
+        top = __shfl_sync(NR_FULL, top, 0);
+        rpg = __shfl_sync(NR_FULL, rpg, 0);
+        if (lane < W4)
+            sl_mask[((size_t)rpg * NR_PAGE) * W4 + lane] =
+                make_uint4(root[4 * lane], root[4 * lane + 1], root[4 * lane + 2], root[4 * lane + 3]);
+        if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
+        __syncwarp();
+
+        NrLaneAcc acc;
+        nr_acc_zero(acc);
+        NrKs qacc = {lane == 0 ? 1.0 : 0.0, 0.0};   // queued mass held by this lane's pushes/pops
+        long long qcount = (lane == 0) ? 1 : 0;
+        int waves = 0, status = 0;
+        unsigned long long max_wave = 0;
+        bool abandon = false;
+        long long t_stop = 0;
+
+        for (;;) {
+            if (P.wave_mode && P.target > 0.0) {
+                NrKs w = nr_ks_warp_sum(qacc);
+                NrKs a = nr_ks_warp_sum(acc.et), b = nr_ks_warp_sum(acc.es);
+                nr_ks_merge(w, a);
+                nr_ks_merge(w, b);
+                if (__dadd_rn(w.hi, w.lo) <= P.target) { status = 1; break; }
+            }
+            if (P.max_nodes && nr_warp_sum_u64(acc.nodes) >= P.max_nodes) {
+                if (P.wave_mode) { status = 3; } else { status = 2; abandon = true; }
+                break;
+            }
+            // fullest (lowest-index) non-empty bucket
+            const uint32_t wb = (lane < NB / 32) ? sh.bitmap[lane] : 0u;
+            const unsigned nz = __ballot_sync(NR_FULL, wb != 0u);
+            if (!nz) break;
+            const int wi = __ffs(nz) - 1;
+            const int bk = wi * 32 + __ffs(__shfl_sync(NR_FULL, wb, wi)) - 1;
+            int chain = 0;
+            if (lane == 0) {
+                chain = sh.heads[bk];
+                if (P.wave_mode) {
+                    sh.heads[bk] = -1;
+                    sh.bitmap[bk >> 5] &= ~(1u << (bk & 31));
+                } else {
+                    const int nx = sh.pnext[chain];
+                    sh.heads[bk] = (short)nx;
+                    sh.pnext[chain] = -1;
+                    if (nx < 0) sh.bitmap[bk >> 5] &= ~(1u << (bk & 31));
+                }
+            }
+            chain = __shfl_sync(NR_FULL, chain, 0);
+            __syncwarp();
+            ++waves;
+            unsigned long long wave_items = 0;
+            for (int pg = chain; pg >= 0 && !abandon;) {
+                const int cnt = sh.pcnt[pg];
+                const int nxt = sh.pnext[pg];
+                wave_items += cnt;
+                for (int i0 = 0; i0 < cnt; i0 += K) {
+                    const int idx = i0 + grp;
+                    const bool valid = idx < cnt;
+                    const size_t slot = (size_t)pg * NR_PAGE + idx;
+                    if (valid && v < W4) reinterpret_cast<uint4 *>(my_m)[v] = sl_mask[slot * W4 + v];
+                    const double mass = valid ? sl_mass[slot] : 0.0;
+                    if (valid && leader) { nr_ks_add(qacc, -mass); qcount--; }
+                    __syncwarp();
+
+                    bool has_child;
+                    uint32_t w[NW];
+                    double cm;
+                    nr_expand<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
+                    const int cb = has_child ? nr_bucket(cm, P.shift, NB) : 0;
+
+                    unsigned pend = __ballot_sync(NR_FULL, has_child);
+                    while (pend) {
+                        const int b = __shfl_sync(NR_FULL, cb, __ffs(pend) - 1);
+                        const unsigned m = __ballot_sync(NR_FULL, has_child && cb == b);
+                        const int n = __popc(m);
+                        int hA = -1, cA = 0, nA = 0, hB = -1;
+                        if (lane == 0) {
+                            const int h = sh.heads[b];
+                            const int c = (h >= 0) ? sh.pcnt[h] : NR_PAGE;
+                            nA = min(n, NR_PAGE - c);
+                            if (nA > 0) { hA = h; cA = c; sh.pcnt[h] = (unsigned char)(c + nA); }
+                            const int rest = n - nA;
+                            if (rest > 0 && top > 0) {
+                                hB = sh.freel[--top];
+                                sh.pnext[hB] = (short)h;
+                                sh.pcnt[hB] = (unsigned char)rest;
+                                sh.heads[b] = (short)hB;
+                                sh.bitmap[b >> 5] |= 1u << (b & 31);
+                            }
+                        }
+                        top = __shfl_sync(NR_FULL, top, 0);
+                        hA = __shfl_sync(NR_FULL, hA, 0);
+                        cA = __shfl_sync(NR_FULL, cA, 0);
+                        nA = __shfl_sync(NR_FULL, nA, 0);
+                        hB = __shfl_sync(NR_FULL, hB, 0);
+                        __syncwarp();
+                        if (has_child && cb == b) {
+                            const int r = __popc(m & lt_mask);
+                            const int s = (r < nA) ? hA * NR_PAGE + cA + r : (hB >= 0 ? hB * NR_PAGE + (r - nA) : -1);
+                            if (s >= 0) {
+                                uint4 *d = sl_mask + (size_t)s * W4;
+#pragma unroll
+                                for (int k = 0; k < W4; ++k)
+                                    d[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+                                sl_mass[s] = cm;
+                                nr_ks_add(qacc, cm);
+                                qcount++;
+                            } else if (P.escalate) {
+                                abandon = true;
+                            } else {                      // queue full: mass to ESP (main.cu:245-252)
+                                acc.spilled++;
+                                nr_ks_add(acc.es, cm);
+                            }
+                            has_child = false;
+                        }
+                        pend = __ballot_sync(NR_FULL, has_child);
+                    }
+                    abandon = __any_sync(NR_FULL, abandon);
+                    if (abandon) break;
+                }
+                if (lane == 0) sh.freel[top++] = (short)pg;
+                top = __shfl_sync(NR_FULL, top, 0);
+                __syncwarp();
+                pg = nxt;
+            }
+            if (abandon) { status = 2; break; }
+            if (wave_items > max_wave) max_wave = wave_items;
+        }
+        t_stop = nr_globaltimer() - t0;
+
+        NrKs R = nr_ks_warp_sum(acc.R), et = nr_ks_warp_sum(acc.et), es = nr_ks_warp_sum(acc.es);
+        NrKs qm = nr_ks_warp_sum(qacc);
+        const unsigned long long nodes = nr_warp_sum_u64(acc.nodes), leaves = nr_warp_sum_u64(acc.leaves);
+        const unsigned long long dead = nr_warp_sum_u64(acc.dead), trunc = nr_warp_sum_u64(acc.trunc);
+        const unsigned long long spilled = nr_warp_sum_u64(acc.spilled);
+        const unsigned long long queued = nr_warp_sum_u64((unsigned long long)qcount);
+        if (lane == 0) {
+            NrWarpOut o;
+            o.R_hi = R.hi; o.R_lo = R.lo; o.et_hi = et.hi; o.et_lo = et.lo; o.es_hi = es.hi; o.es_lo = es.lo;
+            o.q_hi = qm.hi; o.q_lo = qm.lo;
+            o.nodes = nodes; o.leaves = leaves; o.dead = dead; o.trunc = trunc; o.spilled = spilled;
+            o.queued = queued; o.max_wave = max_wave; o.t_ns = t_stop; o.waves = waves; o.status = status;
+            P.out[P.inst_id[ii]] = o;
+        }
+        __syncwarp();
+    }
+}

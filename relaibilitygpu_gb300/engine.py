@@ -48,7 +48,8 @@ class NrOptions(C.Structure):
         ("truncation_eps", C.c_double), ("target_width", C.c_double), ("order", C.c_int32),
         ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("device", C.c_int32),
         ("blocks_per_sm", C.c_int32), ("warps_per_block", C.c_int32), ("timeout_ms", C.c_double),
-        ("verbose", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("verbose", C.c_int32), ("pad0", C.c_int32), ("max_nodes", C.c_uint64),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -62,7 +63,7 @@ class NrResult(C.Structure):
         ("max_queue_items", C.c_uint64), ("max_queue_mb", C.c_double), ("ms", C.c_double),
         ("time_to_bound_ms", C.c_double), ("engine", C.c_int32), ("grid_blocks", C.c_int32),
         ("block_threads", C.c_int32), ("item_bytes", C.c_int32), ("capacity", C.c_uint64),
-        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("reserved", C.c_int32 * 4),
+        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("stop", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -145,6 +146,7 @@ class Result:
     capacity: int
     h2d_bytes: int
     d2h_bytes: int
+    stop: int
     _raw: NrResult = dataclasses.field(repr=False, default=None)
 
     @staticmethod
@@ -176,7 +178,7 @@ class _GraphView:
 
 def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto", bucket_shift: int = 2,
                  n_buckets: int = 256, device: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0,
-                 timeout_ms: float = 60000.0) -> NrOptions:
+                 timeout_ms: float = 60000.0, max_nodes: int = 0) -> NrOptions:
     o = NrOptions()
     lib().nr_options_default(C.byref(o))
     o.truncation_eps = float(eps)
@@ -188,6 +190,7 @@ def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto
     o.blocks_per_sm = int(blocks_per_sm)
     o.warps_per_block = int(warps_per_block)
     o.timeout_ms = float(timeout_ms)
+    o.max_nodes = int(max_nodes)
     return o
 
 
@@ -230,16 +233,29 @@ class Context:
         return Result.from_raw(r)
 
     def reliability_batch(self, graphs: Sequence[Graph], srcs, dsts, capacity: int = 0, **opts):
-        views = [_GraphView(g) for g in graphs]
-        arr = (NrGraph * len(views))(*[v.c for v in views])
-        s = np.ascontiguousarray(srcs, dtype=np.int32)
-        d = np.ascontiguousarray(dsts, dtype=np.int32)
-        res = (NrResult * len(views))()
+        return self.run_batch(Batch(graphs, srcs, dsts), capacity=capacity, **opts)
+
+    def run_batch(self, batch: "Batch", capacity: int = 0, raw: bool = False, **opts):
+        """Solve a prepared batch (host arrays marshalled once) with nr_reliability_batch."""
         o = make_options(**opts)
-        _check(lib().nr_reliability_batch(self.h, len(views), arr, s.ctypes.data_as(C.POINTER(C.c_int32)),
-                                          d.ctypes.data_as(C.POINTER(C.c_int32)), int(capacity), C.byref(o),
-                                          res))
-        return [Result.from_raw(res[i]) for i in range(len(views))]
+        _check(lib().nr_reliability_batch(self.h, batch.n, batch.arr, batch.s.ctypes.data_as(C.POINTER(C.c_int32)),
+                                          batch.d.ctypes.data_as(C.POINTER(C.c_int32)), int(capacity), C.byref(o),
+                                          batch.res))
+        if raw:
+            return batch.res
+        return [Result.from_raw(batch.res[i]) for i in range(batch.n)]
+
+
+class Batch:
+    """Host-side argument arrays of nr_reliability_batch, built once and reused."""
+
+    def __init__(self, graphs: Sequence[Graph], srcs, dsts):
+        self.views = [_GraphView(g) for g in graphs]
+        self.n = len(self.views)
+        self.arr = (NrGraph * self.n)(*[v.c for v in self.views])
+        self.s = np.ascontiguousarray(srcs, dtype=np.int32)
+        self.d = np.ascontiguousarray(dsts, dtype=np.int32)
+        self.res = (NrResult * self.n)()
 
 
 def reliability(g: Graph, src: int, dst: int, capacity: int = 0, **opts) -> Result:

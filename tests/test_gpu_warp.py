@@ -1,0 +1,149 @@
+"""Warp-per-instance engine (bucketed max-mass queue, batches) against the oracle.
+
+Truncated runs: the engine expands exactly the subproblems the oracle's wave
+schedule expands (same buckets, same waves, same stop wave), so counts are
+bit-exact and R, ESP agree to 1e-12.  Exhaustive batches: counts bit-exact,
+R within 1e-12 (order-independent)."""
+import numpy as np
+import pytest
+
+from conftest import rel_close
+
+pytestmark = pytest.mark.gpu
+
+R_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def ctx(engine_lib):
+    c = engine_lib.Context(0)
+    yield c
+    c.close()
+
+
+def check_wave_parity(r, o, esp_tol=1e-11):
+    assert r.nodes == o.nodes
+    assert r.leaves == o.leaves
+    assert r.dead_ends == o.dead
+    assert r.truncated == o.truncated
+    assert r.iterations == o.waves
+    assert r.max_queue_items == o.max_wave
+    assert r.queued == o.queued
+    assert rel_close(r.R, o.R, R_TOL), (r.R, o.R)
+    assert abs(r.esp - o.esp) <= esp_tol * max(o.esp, 1e-300) + 1e-18, (r.esp, o.esp)
+
+
+@pytest.mark.parametrize("target", [1e-3, 1e-6, 1e-9])
+def test_k15_target_width(ctx, oracle, target):
+    from relaibilitygpu_gb300 import graphs
+    for seed in range(4):
+        g = graphs.complete(15, p_range=(0.9, 0.99), seed=seed)
+        r = ctx.reliability(g, 0, 14, target_width=target, bucket_shift=2, n_buckets=256)
+        o = oracle.run(g, 0, 14, bucket_shift=2, n_buckets=256, target_width=target)
+        assert o.status == 1
+        check_wave_parity(r, o)
+        assert r.esp <= target
+        assert r.engine == "warp"
+
+
+@pytest.mark.parametrize("shift,nb", [(0, 64), (1, 128), (3, 512)])
+def test_bucket_resolutions(ctx, oracle, shift, nb):
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.complete(12, p_range=(0.7, 0.99), seed=5)
+    r = ctx.reliability(g, 0, 11, target_width=1e-7, bucket_shift=shift, n_buckets=nb)
+    o = oracle.run(g, 0, 11, bucket_shift=shift, n_buckets=nb, target_width=1e-7)
+    check_wave_parity(r, o)
+
+
+def test_maxmass_to_empty_queue_is_exact(ctx, oracle, load_golden_graph, golden):
+    """Max-mass order without a target runs to the empty queue: exhaustive result."""
+    g = load_golden_graph("COMP8")
+    r = ctx.reliability(g, 0, 7, order="maxmass", capacity=1 << 16)
+    o = oracle.run(g, 0, 7, bucket_shift=2, n_buckets=256)
+    check_wave_parity(r, o)
+    assert rel_close(r.R, golden["published"]["COMP8"]["R"], R_TOL)
+    assert r.paths == 26830 and r.nodes == 53660
+
+
+def test_k25_target(ctx, oracle):
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.complete(25, p_range=(0.9, 0.99), seed=1)
+    r = ctx.reliability(g, 0, 24, target_width=1e-5)
+    o = oracle.run(g, 0, 24, bucket_shift=2, n_buckets=256, target_width=1e-5)
+    check_wave_parity(r, o)
+
+
+def test_truncated_brackets_exact(ctx, oracle, load_golden_graph, golden):
+    g = load_golden_graph("COMP9")
+    exact = golden["published"]["COMP9"]["R"]
+    for t in (1e-2, 1e-4, 1e-6):
+        r = ctx.reliability(g, 0, 8, target_width=t, capacity=1 << 16)
+        assert r.R <= exact + 1e-15 <= r.R + r.esp + 2e-15
+        assert r.esp <= t
+
+
+def test_warp_overflow_spills_and_brackets(ctx, load_golden_graph, golden):
+    g = load_golden_graph("COMP9")
+    exact = golden["published"]["COMP9"]["R"]
+    r = ctx.reliability(g, 0, 8, order="maxmass", capacity=256)
+    assert r.spilled > 0
+    assert r.R <= exact + 1e-15 <= r.R + r.esp + 2e-15
+
+
+def test_batch_exhaustive_matches_oracle(ctx, oracle):
+    from relaibilitygpu_gb300 import graphs
+    gs = graphs.batch_instances(48, seed=11)
+    keep = []
+    for g in gs:
+        o = oracle.run(g, g.src, g.dst, max_nodes=200_000)
+        if o.status == 0:
+            keep.append((g, o))
+    assert len(keep) >= 20
+    res = ctx.reliability_batch([g for g, _ in keep], [g.src for g, _ in keep], [g.dst for g, _ in keep])
+    for (g, o), r in zip(keep, res):
+        assert r.paths == o.paths and r.nodes == o.nodes and r.leaves == o.leaves and r.dead_ends == o.dead
+        assert rel_close(r.R, o.R, R_TOL)
+        assert r.esp == 0.0
+
+
+def test_batch_handover_to_grid_engine(ctx, oracle, load_golden_graph, golden):
+    """An instance larger than the warp's budget is finished by the whole-GPU engine."""
+    big = load_golden_graph("COMP10-05")
+    small = load_golden_graph("COMP8")
+    res = ctx.reliability_batch([small, big, small], [0, 0, 0], [7, 9, 7])
+    assert res[0].engine == "warp" and res[2].engine == "warp"
+    assert res[1].engine == "grid"
+    assert res[1].paths == golden["published"]["COMP10-05"]["paths"]
+    assert res[1].nodes == golden["published"]["COMP10-05"]["nodes"]
+    for r in (res[0], res[2]):
+        assert r.paths == 26830 and r.nodes == 53660
+
+
+def test_batch_truncated_matches_oracle(ctx, oracle):
+    from relaibilitygpu_gb300 import graphs
+    gs = [graphs.complete(15, p_range=(0.9, 0.99), seed=100 + i) for i in range(64)]
+    res = ctx.reliability_batch(gs, [0] * len(gs), [14] * len(gs), target_width=1e-6)
+    for g, r in zip(gs, res):
+        o = oracle.run(g, 0, 14, bucket_shift=2, n_buckets=256, target_width=1e-6)
+        check_wave_parity(r, o)
+
+
+def test_batch_mixed_classes(ctx, oracle):
+    """Instances of several lane-group widths and mask sizes in one call."""
+    from relaibilitygpu_gb300 import graphs
+    rng = np.random.default_rng(3)
+    gs = []
+    for i in range(40):
+        n = int(rng.integers(4, 33))
+        m = int(min(n * (n - 1) // 2, n + rng.integers(0, 3 * n)))
+        gs.append(graphs.gnm(n, m, p_range=(0.85, 0.99), seed=500 + i))
+    res = ctx.reliability_batch(gs, [g.src for g in gs], [g.dst for g in gs], target_width=1e-5,
+                                max_nodes=100_000)
+    compared = 0
+    for g, r in zip(gs, res):
+        o = oracle.run(g, g.src, g.dst, bucket_shift=2, n_buckets=256, target_width=1e-5, max_nodes=20000)
+        if o.status == 2 or r.spilled or r.stop == 3:
+            continue      # larger than the quick-check budget or the warp's default pages
+        check_wave_parity(r, o)
+        compared += 1
+    assert compared >= 20

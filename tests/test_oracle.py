@@ -150,3 +150,20 @@ def test_disconnected(oracle):
     g = graphs.from_edges(4, [(0, 1), (2, 3)], [0.9, 0.9])
     r = oracle.run(g, 0, 3)
     assert r.R == 0.0 and r.nodes == 1 and r.dead == 1 and r.paths == 0
+
+
+def test_batch_runner_matches_single(oracle):
+    """og_run_batch (reused per-thread storage) gives the single-instance results."""
+    from relaibilitygpu_gb300 import graphs
+    gs = [graphs.complete(15, p_range=(0.9, 0.99), seed=s) for s in range(40)]
+    gs += [graphs.grid(3, 4, p_range=(0.5, 0.95), seed=s) for s in range(10)]
+    srcs = [0] * len(gs)
+    dsts = [g.n_nodes - 1 for g in gs]
+    kw = dict(bucket_shift=2, n_buckets=256, target_width=1e-6)
+    res = oracle.run_batch(oracle.BatchArgs(gs, srcs, dsts), threads=3, **kw)
+    for i, g in enumerate(gs):
+        o = oracle.run(g, srcs[i], dsts[i], **kw)
+        r = res[i]
+        assert (r.nodes, r.leaves, r.dead, r.waves, r.max_wave, r.queued) == (o.nodes, o.leaves, o.dead, o.waves,
+                                                                             o.max_wave, o.queued)
+        assert r.R == o.R and r.esp == o.esp
