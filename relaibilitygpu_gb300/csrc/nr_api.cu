@@ -437,10 +437,12 @@ static void fill_from_warp(const NrWarpOut &w, const WarpRunCfg &cfg, int W4, nr
     R.merge(w.R_hi, w.R_lo);
     esp.merge(w.et_hi, w.et_lo);
     esp.merge(w.es_hi, w.es_lo);
-    esp.merge(w.q_hi, w.q_lo);
+    // the queued mass is tracked by adding pushes and subtracting pops; an
+    // empty queue holds exactly nothing, whatever rounding residue is left
+    if (w.queued > 0) esp.merge(w.q_hi, w.q_lo);
     r->R = R.val();
     r->esp = esp.val();
-    if (r->esp < 0) r->esp = 0;   // queued-mass rounding can leave -1e-17 on an empty queue
+    if (r->esp < 0) r->esp = 0;
     r->R_plus_esp = r->R + r->esp;
     r->trunc_bound = r->R > 0 ? r->esp / r->R : r->esp;
     r->nodes = w.nodes; r->leaves = w.leaves; r->dead_ends = w.dead; r->truncated = w.trunc;
