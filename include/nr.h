@@ -163,6 +163,23 @@ int  nr_reliability_batch(nr_context *ctx, int n_instances, const nr_graph *grap
                           const int32_t *srcs, const int32_t *dsts, uint64_t capacity,
                           const nr_options *opt, nr_result *results);
 
+/* Solve one instance without allocating device memory (no counterpart in the
+ * reference, which allocates its queues with cudaMalloc on every run).
+ * For callers that cannot call cudaMalloc -- an application whose device
+ * memory belongs to its own allocator or pool, or a plugin that may not grow
+ * the process's device footprint -- the queue, graph tables and output live
+ * in one static device array of 4 MiB per GPU, held until the process exits.
+ * Limits: n_nodes <= 32 and graph tables that fit the array; larger inputs
+ * return NR_ERR_UNSUPPORTED.  The queue gets the rest of the array; when it
+ * is full, child mass is spilled into ESP (a valid bracket, as in the
+ * reference on queue overflow).  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  Calls share the array: they are serialised by a lock and each
+ * waits for its kernel, so anything else overlapping on the GPU that touched
+ * the array would race.  Runs on cudaStreamPerThread; res->ms is in-kernel
+ * device time.  capacity is not taken: the array sets it. */
+int  nr_reliability_noalloc(const nr_graph *g, int src, int dst, const nr_options *opt, nr_result *res);
+
 /* The reference's result block (workingPad/main.cu:1037-1056) as text.
  * Returns the number of characters written (snprintf semantics). */
 int  nr_format_result(const nr_result *res, char *buf, size_t len);

@@ -71,7 +71,7 @@ class NrResult(C.Structure):
 EXPORTS = [
     "nr_options_default", "nr_status_string", "nr_abi_version", "nr_graph_load", "nr_graph_free",
     "nr_initial_mask", "nr_context_create", "nr_context_destroy", "nr_reliability", "nr_reliability_ctx",
-    "nr_reliability_batch", "nr_format_result",
+    "nr_reliability_batch", "nr_format_result", "nr_reliability_noalloc",
 ]
 
 _lib_handle: Optional[C.CDLL] = None
@@ -110,6 +110,9 @@ def lib() -> C.CDLL:
                                        C.POINTER(C.c_int32), C.c_uint64, C.POINTER(NrOptions),
                                        C.POINTER(NrResult)]
     L.nr_reliability_batch.restype = C.c_int
+    L.nr_reliability_noalloc.argtypes = [C.POINTER(NrGraph), C.c_int, C.c_int, C.POINTER(NrOptions),
+                                         C.POINTER(NrResult)]
+    L.nr_reliability_noalloc.restype = C.c_int
     L.nr_format_result.argtypes = [C.POINTER(NrResult), C.c_char_p, C.c_size_t]
     L.nr_format_result.restype = C.c_int
     _lib_handle = L
@@ -264,6 +267,20 @@ def reliability(g: Graph, src: int, dst: int, capacity: int = 0, **opts) -> Resu
     o = make_options(**opts)
     r = NrResult()
     _check(lib().nr_reliability(C.byref(gv.c), int(src), int(dst), int(capacity), C.byref(o), C.byref(r)))
+    return Result.from_raw(r)
+
+
+def reliability_noalloc(g: Graph, src: int, dst: int, **opts) -> Result:
+    """Solve one instance through nr_reliability_noalloc: no device allocation.
+
+    For callers that cannot call cudaMalloc (their device memory belongs to
+    another allocator or pool).  The engine works inside a static 4 MiB device
+    array per GPU; graphs need n_nodes <= 32, and a full queue spills into ESP.
+    """
+    gv = _GraphView(g)
+    o = make_options(**opts)
+    r = NrResult()
+    _check(lib().nr_reliability_noalloc(C.byref(gv.c), int(src), int(dst), C.byref(o), C.byref(r)))
     return Result.from_raw(r)
 
 
