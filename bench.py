@@ -226,6 +226,13 @@ def main():
     ctx = nr.Context(local)
     batch = nr.Batch(w["graphs"], w["srcs"], w["dsts"])
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    tuned = None
+    if w["kind"] == "batch":
+        # autotuner (nr_autotune): bucket resolution, pages per warp, warps per block
+        tuned, tuned_ms = nr.autotune(ctx, batch, capacity=w["capacity"], **w["opts"])
+        w["opts"] = tuned
+        w["oracle"] = dict(bucket_shift=tuned["bucket_shift"], n_buckets=tuned["n_buckets"],
+                           target_width=tuned["target_width"])
 
     def call():
         if w["kind"] == "batch":
@@ -303,7 +310,10 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": w["name"], "l2": "flushed (512 MB write) before every step",
                    "parallelism": f"replicas x{world}", "engine": stats["engine"],
-                   "grid": int(r0.grid_blocks), "block": int(r0.block_threads)},
+                   "grid": int(r0.grid_blocks), "block": int(r0.block_threads),
+                   "autotuned": None if tuned is None else {k: tuned[k] for k in
+                                                             ("bucket_shift", "n_buckets", "warps_per_block",
+                                                              "pages_per_warp")}},
         "result": stats,
         "time_to_bound": ttb,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

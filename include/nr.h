@@ -86,7 +86,9 @@ typedef struct nr_options {
     uint64_t max_nodes;       /* per-instance pop budget for the warp engine; truncated runs stop
                                  there with a valid R <= true <= R + ESP bracket, exhaustive runs
                                  hand the instance to the whole-GPU engine; 0 = engine default */
-    int32_t  reserved[4];
+    int32_t  pages_per_warp;  /* warp engine: queue pages of 32 subproblems per warp when capacity is 0
+                                 (0 = 512) */
+    int32_t  reserved[3];
 } nr_options;
 
 typedef struct nr_result {
@@ -162,6 +164,17 @@ int  nr_reliability_ctx(nr_context *ctx, const nr_graph *g, int src, int dst, ui
 int  nr_reliability_batch(nr_context *ctx, int n_instances, const nr_graph *graphs,
                           const int32_t *srcs, const int32_t *dsts, uint64_t capacity,
                           const nr_options *opt, nr_result *results);
+
+/* Autotuner for batches (no reference counterpart).  Times the warp engine on
+ * up to 4096 instances of the batch for each candidate setting -- bucket
+ * resolution (bucket_shift 0..2, the bucket count), pages per warp (64 or 512,
+ * how much of the queue a warp holds) and warps per block (2, 4, 8) -- and
+ * writes the fastest into *best (based on *opt), with its device time in
+ * *best_ms.  Every candidate returns a valid result; the choice changes time
+ * and, for truncated runs, where the stop falls. */
+int  nr_autotune(nr_context *ctx, int n_instances, const nr_graph *graphs, const int32_t *srcs,
+                 const int32_t *dsts, uint64_t capacity, const nr_options *opt, nr_options *best,
+                 double *best_ms);
 
 /* Solve one instance without allocating device memory (no counterpart in the
  * reference, which allocates its queues with cudaMalloc on every run).

@@ -17,20 +17,89 @@
 #include <time.h>
 
 /* ------------------------------------------------------------------ */
-/* compensated (two-sum) accumulator                                   */
+/* exact sums: 192-bit unsigned fixed point, value = A / 2^190            */
+/* (the same number format as the engine's device sums; any order of the */
+/* additions gives the same integer, so results compare bit for bit)     */
 /* ------------------------------------------------------------------ */
-typedef struct { double hi, lo; } ksum;
+#define FIX_FRAC 190
+typedef struct { uint64_t w[3]; } ksum;
 
+static inline ksum fix_of(double m)
+{
+    ksum r = {{0, 0, 0}};
+    uint64_t bits;
+    memcpy(&bits, &m, 8);
+    int ex = (int)((bits >> 52) & 0x7ff);
+    uint64_t M = bits & 0xfffffffffffffull;
+    int e;
+    if (ex == 0) e = -1074;
+    else { M |= 1ull << 52; e = ex - 1075; }
+    if (!M) return r;
+    int s = e + FIX_FRAC;
+    if (s >= 0) {
+        int k = s >> 6, b = s & 63;
+        uint64_t lo = M << b, hi = b ? (M >> (64 - b)) : 0;
+        r.w[k] = lo;
+        if (k + 1 < 3) r.w[k + 1] = hi;
+    } else if (-s < 64) {
+        r.w[0] = M >> (-s);
+    }
+    return r;
+}
+static inline void ks_merge(ksum *a, const ksum *b)
+{
+    unsigned __int128 c = 0;
+    for (int i = 0; i < 3; i++) {
+        c += (unsigned __int128)a->w[i] + b->w[i];
+        a->w[i] = (uint64_t)c;
+        c >>= 64;
+    }
+}
+static inline void ks_sub(ksum *a, const ksum *b)
+{
+    uint64_t borrow = 0;
+    for (int i = 0; i < 3; i++) {
+        uint64_t x = a->w[i], y = b->w[i];
+        uint64_t d = x - y - borrow;
+        borrow = (x < y) || (x - y < borrow);
+        a->w[i] = d;
+    }
+}
 static inline void ks_add(ksum *s, double x)
 {
-    double t = s->hi + x;
-    double bp = t - s->hi;
-    double err = (s->hi - (t - bp)) + (x - bp);
-    s->hi = t;
-    s->lo += err;
+    if (x < 0) { ksum t = fix_of(-x); ks_sub(s, &t); }
+    else { ksum t = fix_of(x); ks_merge(s, &t); }
 }
-static inline void ks_merge(ksum *s, const ksum *o) { ks_add(s, o->hi); ks_add(s, o->lo); }
-static inline double ks_val(const ksum *s) { return s->hi + s->lo; }
+static inline int ks_le(const ksum *a, const ksum *b)
+{
+    for (int i = 2; i >= 0; i--) if (a->w[i] != b->w[i]) return a->w[i] < b->w[i];
+    return 1;
+}
+/* round to nearest, ties to even */
+static double ks_val(const ksum *a)
+{
+    int i = 2;
+    while (i >= 0 && a->w[i] == 0) i--;
+    if (i < 0) return 0.0;
+    int t = 64 * i + 63 - __builtin_clzll(a->w[i]);
+    uint64_t x;
+    int sticky = 0;
+    if (t >= 63) {
+        int lo = t - 63, k = lo >> 6, b = lo & 63;
+        x = a->w[k] >> b;
+        if (b && k + 1 < 3) x |= a->w[k + 1] << (64 - b);
+        if (b) sticky = (a->w[k] & ((1ull << b) - 1)) != 0;
+        for (int j = 0; j < k; j++) sticky |= a->w[j] != 0;
+    } else {
+        x = a->w[0] << (63 - t);
+    }
+    uint64_t mant = x >> 11, rem = x & 0x7ff;
+    if (rem > 0x400 || (rem == 0x400 && (sticky || (mant & 1)))) {
+        mant++;
+        if (mant >> 53) { mant >>= 1; t++; }
+    }
+    return ldexp((double)mant, t - 52 - FIX_FRAC);
+}
 
 static double now_s(void)
 {
@@ -474,14 +543,15 @@ static int run_waves(const og_graph *g, int src, int dst, const og_opts *o, cons
         if (b < 0) break;
         /* stop test between waves: ESP so far + queued mass */
         if (o->target_width > 0) {
-            ksum wdt = {0, 0};
+            ksum wdt = {{0, 0, 0}};
             for (int i = 0; i < T; i++) { ks_merge(&wdt, &s.th[i].x.esp_trunc); ks_merge(&wdt, &s.th[i].x.esp_spill); }
             for (int i = 0; i < nb; i++) ks_merge(&wdt, &bk[i].mass);
-            if (ks_val(&wdt) <= o->target_width) { status = 1; break; }
+            ksum tgt = fix_of(o->target_width);
+            if (ks_le(&wdt, &tgt)) { status = 1; break; }
         }
         if (o->max_nodes && total_nodes(&s) >= o->max_nodes) { status = 2; break; }
         /* take the whole bucket as this wave */
-        ivec t = cur; cur = bk[b]; bk[b] = t; bk[b].n = 0; bk[b].mass.hi = bk[b].mass.lo = 0;
+        ivec t = cur; cur = bk[b]; bk[b] = t; bk[b].n = 0; memset(&bk[b].mass, 0, sizeof(ksum));
         waves++;
         if (cur.n > max_wave) max_wave = cur.n;
         s.wave = &cur;
@@ -505,7 +575,7 @@ static int run_waves(const og_graph *g, int src, int dst, const og_opts *o, cons
                     memcpy(&mm, rr + W, sizeof(double));
                     iv_push(&bk[k], rr, mm, W);
                 }
-                src_v->n = 0; src_v->mass.hi = src_v->mass.lo = 0;
+                src_v->n = 0; memset(&src_v->mass, 0, sizeof(ksum));
             }
         }
         uint64_t qn = atomic_load(&s.queued);
@@ -519,7 +589,7 @@ static int run_waves(const og_graph *g, int src, int dst, const og_opts *o, cons
         pthread_barrier_destroy(&s.bar_end);
         free(tids);
     }
-    ksum R = {0, 0}, et = {0, 0}, es = {0, 0}, qm = {0, 0};
+    ksum R = {{0, 0, 0}}, et = {{0, 0, 0}}, es = {{0, 0, 0}}, qm = {{0, 0, 0}};
     uint64_t queued = 0;
     for (int i = 0; i < nb; i++) { ks_merge(&qm, &bk[i].mass); queued += bk[i].n; free(bk[i].d); }
     for (int i = 0; i < T; i++) {
@@ -637,17 +707,16 @@ static int run_serial(const og_graph *g, int src, int dst, const og_opts *o, con
     while (h.n) {
         if (o->target_width > 0 && h.heap) {
             ksum w = x.esp_trunc; ks_merge(&w, &x.esp_spill);
-            ksum qm = {0, 0};
-            for (size_t i = 0; i < h.n; i++) ks_add(&qm, h.key[i]);
-            ks_merge(&w, &qm);
-            if (ks_val(&w) <= o->target_width) { status = 1; break; }
+            ks_merge(&w, &h.mass);
+            ksum tgt = fix_of(o->target_width);
+            if (ks_le(&w, &tgt)) { status = 1; break; }
         }
         if (o->max_nodes && x.nodes >= o->max_nodes) { status = 2; break; }
         double mass = hq_pop(&h, m);
         x_expand(&x, m, mass, hq_sink, &h);
         if (h.n > max_q) max_q = h.n;
     }
-    ksum qm = {0, 0};
+    ksum qm = {{0, 0, 0}};
     for (size_t i = 0; i < h.n; i++) ks_add(&qm, h.key[i]);
     r->R = ks_val(&x.R);
     r->esp_truncated = ks_val(&x.esp_trunc);
@@ -717,7 +786,7 @@ static void arena_fit(og_arena *a, const og_graph *g, int src, int dst, const og
     x->rule = o->bfs_rule; x->precheck = o->precheck; x->eps = o->eps;
     x->gen = 0;
     memset(x->vis, 0, a->n_cap * sizeof(uint32_t));
-    x->R.hi = x->R.lo = x->esp_trunc.hi = x->esp_trunc.lo = x->esp_spill.hi = x->esp_spill.lo = 0;
+    memset(&x->R, 0, sizeof(ksum)); memset(&x->esp_trunc, 0, sizeof(ksum)); memset(&x->esp_spill, 0, sizeof(ksum));
     x->nodes = x->leaves = x->dead = x->truncated = x->spilled = x->pruned = x->pushes = 0;
 }
 
@@ -749,7 +818,7 @@ static int run_waves_arena(og_arena *a, const og_graph *g, int src, int dst, con
         else if (p >= 1.0) a->root[e >> 4] |= 1u << ((e & 15) * 2);
         else a->root[e >> 4] |= 3u << ((e & 15) * 2);
     }
-    for (int i = 0; i < nb; i++) { a->bk[i].n = 0; a->bk[i].mass.hi = a->bk[i].mass.lo = 0; }
+    for (int i = 0; i < nb; i++) { a->bk[i].n = 0; memset(&a->bk[i].mass, 0, sizeof(ksum)); }
     st_sink sk = { a->bk, W, o->bucket_shift, nb, o->capacity, 1 };
     iv_push(&a->bk[og_bucket(1.0, o->bucket_shift, nb)], a->root, 1.0, W);
     int status = 0;
@@ -762,11 +831,12 @@ static int run_waves_arena(og_arena *a, const og_graph *g, int src, int dst, con
             ksum wdt = x->esp_trunc;
             ks_merge(&wdt, &x->esp_spill);
             for (int i = 0; i < nb; i++) ks_merge(&wdt, &a->bk[i].mass);
-            if (ks_val(&wdt) <= o->target_width) { status = 1; break; }
+            ksum tgt = fix_of(o->target_width);
+            if (ks_le(&wdt, &tgt)) { status = 1; break; }
         }
         if (o->max_nodes && x->nodes >= o->max_nodes) { status = 2; break; }
         ivec t = a->cur; a->cur = a->bk[b]; a->bk[b] = t;
-        a->bk[b].n = 0; a->bk[b].mass.hi = a->bk[b].mass.lo = 0;
+        a->bk[b].n = 0; memset(&a->bk[b].mass, 0, sizeof(ksum));
         waves++;
         if (a->cur.n > max_wave) max_wave = a->cur.n;
         for (size_t i = 0; i < a->cur.n; i++) {
@@ -775,7 +845,7 @@ static int run_waves_arena(og_arena *a, const og_graph *g, int src, int dst, con
         }
         if (sk.queued > max_q) max_q = sk.queued;
     }
-    ksum qm = {0, 0};
+    ksum qm = {{0, 0, 0}};
     uint64_t queued = 0;
     for (int i = 0; i < nb; i++) { ks_merge(&qm, &a->bk[i].mass); queued += a->bk[i].n; }
     memset(r, 0, sizeof(*r));
@@ -928,7 +998,7 @@ double og_brute(const og_graph *g, int src, int dst)
     for (int i = 0; i < na; i++) vlist[vstart[arc_var[i]] + fill[arc_var[i]]++] = i;
     uint64_t adj[64];
     memcpy(adj, base, sizeof(adj));
-    ksum R = {0, 0};
+    ksum R = {{0, 0, 0}};
     uint64_t gray = 0;
     uint64_t total = (uint64_t)1 << k;
     for (uint64_t it = 0; it < total; it++) {

@@ -4,16 +4,22 @@
 // loader (workingPad/graph.h:46-178) with calls that return status codes.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "nr_internal.h"
+#include "nr_device.cuh"
 #include "nr_warp.cuh"
 
 const void *nr_grid_kernel_ptr_g8(int w4);
@@ -40,19 +46,6 @@ void nr_last_cuda_error(cudaError_t e)
 {
     snprintf(g_err, sizeof(g_err), "%s", cudaGetErrorString(e));
 }
-
-struct KS {
-    double hi = 0, lo = 0;
-    void add(double x)
-    {
-        double t = hi + x;
-        double bp = t - hi;
-        lo += (hi - (t - bp)) + (x - bp);
-        hi = t;
-    }
-    void merge(double h, double l) { add(h); add(l); }
-    double val() const { return hi + lo; }
-};
 
 const void *grid_kernel(int G, int w4)
 {
@@ -85,6 +78,109 @@ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 }  // namespace
 
+// Correctly rounded (to nearest, ties to even) value of a 192-bit fixed-point sum.
+double nr_fix_to_double_host(const NrFix &a)
+{
+    const unsigned long long w[3] = {a.w0, a.w1, a.w2};
+    int i = 2;
+    while (i >= 0 && w[i] == 0ull) --i;
+    if (i < 0) return 0.0;
+    const int t = 64 * i + 63 - __builtin_clzll(w[i]);   // top set bit
+    unsigned long long x;
+    bool sticky = false;
+    if (t >= 63) {
+        const int lo = t - 63, k = lo >> 6, b = lo & 63;
+        x = w[k] >> b;
+        if (b && k + 1 < 3) x |= w[k + 1] << (64 - b);
+        if (b) sticky = (w[k] & ((1ull << b) - 1ull)) != 0ull;
+        for (int j = 0; j < k; ++j) sticky = sticky || w[j] != 0ull;
+    } else {
+        x = w[0] << (63 - t);
+    }
+    unsigned long long mant = x >> 11;
+    const unsigned long long rem = x & 0x7ffull;
+    int top = t;
+    if (rem > 0x400ull || (rem == 0x400ull && (sticky || (mant & 1ull)))) {
+        ++mant;
+        if (mant >> 53) { mant >>= 1; ++top; }
+    }
+    return std::ldexp((double)mant, top - 52 - NR_FIX_FRAC);
+}
+
+NrFix nr_fix_from_double_host(double m) { return nr_fix_of(m); }
+void nr_fix_add_host(NrFix &a, const NrFix &b) { nr_fix_add(a, b); }
+
+// Worker threads kept by a context for the host side of batch calls (table
+// building and validation), so a call does not pay for thread creation.
+class NrPool {
+public:
+    explicit NrPool(int workers)
+    {
+        for (int i = 0; i < workers; ++i) th_.emplace_back([this] { loop(); });
+    }
+    ~NrPool()
+    {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    int size() const { return (int)th_.size() + 1; }
+    // run fn(i) for i in [0, n) on the workers and the calling thread
+    void run(int n, const std::function<void(int)> &fn)
+    {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            fn_ = &fn;
+            n_ = n;
+            next_.store(0);
+            busy_ = (int)th_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> l(mu_);
+        done_.wait(l, [this] { return busy_ == 0; });
+        fn_ = nullptr;
+    }
+
+private:
+    void work()
+    {
+        for (;;) {
+            const int b = next_.fetch_add(32);
+            if (b >= n_) break;
+            const int e = std::min(n_, b + 32);
+            for (int i = b; i < e; ++i) (*fn_)(i);
+        }
+    }
+    void loop()
+    {
+        unsigned long long seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> l(mu_);
+                cv_.wait(l, [&] { return quit_ || gen_ != seen; });
+                if (quit_) return;
+                seen = gen_;
+            }
+            work();
+            std::lock_guard<std::mutex> l(mu_);
+            if (--busy_ == 0) done_.notify_one();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)> *fn_ = nullptr;
+    int n_ = 0, busy_ = 0;
+    std::atomic<int> next_{0};
+    unsigned long long gen_ = 0;
+    bool quit_ = false;
+};
+
 struct nr_context {
     int device = 0;
     int sms = 0;
@@ -98,7 +194,25 @@ struct nr_context {
     size_t wslab_bytes = 0;
     void *wbuf = nullptr;       // warp engine: blob, descriptors, outputs, counters
     size_t wbuf_bytes = 0;
+    void *hbuf = nullptr;       // pinned host staging for the warp engine's uploads and results
+    size_t hbuf_bytes = 0;
+    std::map<std::pair<const void *, size_t>, int> occupancy;   // (kernel, smem) -> blocks per SM
+    std::unique_ptr<NrPool> pool;   // host worker threads, created by the first large batch
     std::mutex mu;
+
+    // run fn(i) for i in [0, n): serially for small n, else on the worker pool
+    void parallel_for(int n, int min_per_thread, const std::function<void(int)> &fn)
+    {
+        if (n < 2 * min_per_thread) {
+            for (int i = 0; i < n; ++i) fn(i);
+            return;
+        }
+        if (!pool) {
+            const int hw = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 32u));
+            pool.reset(new NrPool(hw - 1));
+        }
+        pool->run(n, fn);
+    }
 };
 
 static int ensure(void **buf, size_t *have, size_t need)
@@ -140,9 +254,9 @@ static int validate(const nr_graph *g, int src, int dst)
 
 static int group_width_of(int n) { return group_width(n); }
 
-// Graph tables of one instance for the small engines (layout in nr_internal.h).
-static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *sg, std::vector<unsigned char> *blob,
-                             size_t at = 0)
+// Graph tables of one instance for the small engines (layout in nr_internal.h):
+// small_layout sets the sizes and offsets, small_fill writes the tables.
+static size_t small_layout(const nr_graph *g, int src, int dst, NrSmallGraph *sg)
 {
     const int n = g->n_nodes, E = g->n_edges;
     const int G = group_width_of(n);
@@ -157,9 +271,15 @@ static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *
     sg->off_list = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
     sg->off_root = (int)off; off = align16(off + sizeof(uint32_t) * 4 * sg->w4);
     sg->blob_bytes = (int)off;
-    sg->blob_off = (long long)at;
-    blob->resize(at + off, 0);
-    unsigned char *b = blob->data() + at;
+    sg->blob_off = 0;
+    return off;
+}
+
+static void small_fill(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)
+{
+    const int n = g->n_nodes, E = g->n_edges;
+    const int G = group_width_of(n);
+    memset(b, 0, sg->blob_bytes);
     double *p = reinterpret_cast<double *>(b + sg->off_p);
     double *q = reinterpret_cast<double *>(b + sg->off_q);
     uint16_t *eid = reinterpret_cast<uint16_t *>(b + sg->off_eid);
@@ -169,12 +289,12 @@ static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *
     for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
     for (int i = 0; i < G * G; ++i) eid[i] = 0xffff;
     // in-arcs grouped by head node; arc (u -> v) for every CSR entry of u
-    std::vector<int> cnt(n + 1, 0);
+    int cnt[NR_SMALL_MAX_N + 1] = {0};
     for (int u = 0; u < n; ++u)
         for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) cnt[g->col_idx[j] + 1]++;
     for (int v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
     for (int v = 0; v <= n; ++v) start[v] = cnt[v];
-    std::vector<int> fill(n, 0);
+    int fill[NR_SMALL_MAX_N] = {0};
     for (int u = 0; u < n; ++u)
         for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
             const int v = g->col_idx[j], e = g->edge_id[j];
@@ -186,6 +306,13 @@ static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *
         const uint32_t st = (pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN;
         root[e >> 4] |= st << ((e & 15) * 2);
     }
+}
+
+static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *sg, std::vector<unsigned char> *blob)
+{
+    const size_t bytes = small_layout(g, src, dst, sg);
+    blob->assign(bytes, 0);
+    small_fill(g, sg, blob->data());
 }
 
 extern "C" int nr_initial_mask(const nr_graph *g, uint32_t *words, int n_words)
@@ -267,6 +394,7 @@ extern "C" void nr_context_destroy(nr_context *c)
     if (c->sbuf) cudaFree(c->sbuf);
     if (c->wslab) cudaFree(c->wslab);
     if (c->wbuf) cudaFree(c->wbuf);
+    if (c->hbuf) cudaFreeHost(c->hbuf);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -361,12 +489,12 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
     float ms = 0.f;
     NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
 
-    KS R, et, es;
+    NrFix R = nr_fix_zero(), esp = nr_fix_zero();
     unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0;
-    for (const NrPartial &p : parts) {
-        R.merge(p.R_hi, p.R_lo);
-        et.merge(p.et_hi, p.et_lo);
-        es.merge(p.es_hi, p.es_lo);
+    for (const NrPartial &p : parts) {          // exact: the order of the additions does not matter
+        nr_fix_add(R, p.R);
+        nr_fix_add(esp, p.et);
+        nr_fix_add(esp, p.es);
         nodes += p.nodes; leaves += p.leaves; dead += p.dead; trunc += p.truncated; spilled += p.spilled;
     }
     int waves = 0;
@@ -377,10 +505,8 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
         waves++;
         maxw = std::max(maxw, n);
     }
-    KS esp = et;
-    esp.merge(es.hi, es.lo);
-    r->R = R.val();
-    r->esp = esp.val();
+    r->R = nr_fix_to_double_host(R);
+    r->esp = nr_fix_to_double_host(esp);
     r->R_plus_esp = r->R + r->esp;
     r->trunc_bound = r->R > 0 ? r->esp / r->R : r->esp;
     r->nodes = nodes; r->leaves = leaves; r->dead_ends = dead; r->truncated = trunc; r->spilled = spilled;
@@ -407,7 +533,7 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
 // warp-per-instance engine (nr_warp.cuh)
 // ---------------------------------------------------------------------------
 struct WarpRunCfg {
-    int wave_mode, shift, n_buckets, pages, escalate;
+    int wave_mode, shift, n_buckets, pages, escalate, warps_per_block;
     double eps, target;
     unsigned long long max_nodes;
 };
@@ -426,23 +552,20 @@ static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhausti
         nb = std::min(1024, (nb + 31) / 32 * 32);
         w.n_buckets = nb;
     }
-    if (capacity == 0) w.pages = 512;
+    w.warps_per_block = (o->warps_per_block >= 1 && o->warps_per_block <= NR_WARP_BLOCK_MAX / 32)
+                            ? o->warps_per_block : NR_WARP_BLOCK / 32;
+    if (capacity == 0) w.pages = o->pages_per_warp > 0 ? std::min(8192, std::max(4, o->pages_per_warp)) : 512;
     else w.pages = (int)std::min<uint64_t>(8192, std::max<uint64_t>(4, (capacity + NR_PAGE - 1) / NR_PAGE));
     return w;
 }
 
 static void fill_from_warp(const NrWarpOut &w, const WarpRunCfg &cfg, int W4, nr_result *r)
 {
-    KS R, esp;
-    R.merge(w.R_hi, w.R_lo);
-    esp.merge(w.et_hi, w.et_lo);
-    esp.merge(w.es_hi, w.es_lo);
-    // the queued mass is tracked by adding pushes and subtracting pops; an
-    // empty queue holds exactly nothing, whatever rounding residue is left
-    if (w.queued > 0) esp.merge(w.q_hi, w.q_lo);
-    r->R = R.val();
-    r->esp = esp.val();
-    if (r->esp < 0) r->esp = 0;
+    NrFix esp = w.et;
+    nr_fix_add(esp, w.es);
+    nr_fix_add(esp, w.q);          // exact pushes - pops: zero on an empty queue
+    r->R = nr_fix_to_double_host(w.R);
+    r->esp = nr_fix_to_double_host(esp);
     r->R_plus_esp = r->R + r->esp;
     r->trunc_bound = r->R > 0 ? r->esp / r->R : r->esp;
     r->nodes = w.nodes; r->leaves = w.leaves; r->dead_ends = w.dead; r->truncated = w.trunc;
@@ -459,70 +582,113 @@ static void fill_from_warp(const NrWarpOut &w, const WarpRunCfg &cfg, int W4, nr
 
 // Solve n instances with the warp engine; instances the engine hands over
 // (status 2) are left with engine = 0 for the caller.
+static int ensure_host(void **buf, size_t *have, size_t need)
+{
+    if (*have >= need && *buf) return NR_OK;
+    if (*buf) cudaFreeHost(*buf);
+    *buf = nullptr;
+    *have = 0;
+    if (cudaMallocHost(buf, need) != cudaSuccess) {
+        cudaGetLastError();
+        *buf = nullptr;
+        return NR_ERR_NOMEM;
+    }
+    *have = need;
+    return NR_OK;
+}
+
+// Solve n instances with the warp engine; instances the engine hands over
+// (status 2) are listed in *handover for the caller.  Host work per call:
+// one layout pass, a parallel table fill into pinned staging memory, one
+// upload, one launch per (group width, mask width) class, one download.
 static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
                           const WarpRunCfg &cfg, nr_result *res, std::vector<int> *handover)
 {
-    std::vector<unsigned char> blob;
+    // layout and class of every instance (class = group width x mask blocks)
     std::vector<NrSmallGraph> desc(n);
-    std::map<std::pair<int, int>, std::vector<int>> classes;
+    std::vector<int> cls(n);
+    int class_count[3 * NR_MAX_W4] = {0};
+    size_t blob_bytes = 0;
     for (int i = 0; i < n; ++i) {
-        build_small_blob(&gs[i], srcs[i], dsts[i], &desc[i], &blob, blob.size());
-        classes[{group_width(gs[i].n_nodes), desc[i].w4}].push_back(i);
+        const size_t b = small_layout(&gs[i], srcs[i], dsts[i], &desc[i]);
+        desc[i].blob_off = (long long)blob_bytes;
+        blob_bytes += b;
+        if (desc[i].w4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
+        const int G = group_width(gs[i].n_nodes);
+        cls[i] = (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + desc[i].w4 - 1;
+        class_count[cls[i]]++;
     }
-    // descriptors and ids in class order
-    std::vector<NrSmallGraph> dsorted;
-    std::vector<int> ids;
-    std::vector<std::pair<std::pair<int, int>, std::pair<int, int>>> spans;   // class -> [begin, count)
-    for (auto &kv : classes) {
-        spans.push_back({kv.first, {(int)ids.size(), (int)kv.second.size()}});
-        for (int i : kv.second) { dsorted.push_back(desc[i]); ids.push_back(i); }
+    int class_begin[3 * NR_MAX_W4 + 1] = {0};
+    for (int k = 0; k < 3 * NR_MAX_W4; ++k) class_begin[k + 1] = class_begin[k] + class_count[k];
+    // pinned staging: [tables | descriptors (class order) | ids (class order)] then [outputs]
+    size_t off = 0;
+    const size_t off_blob = off; off = align16(off + blob_bytes);
+    const size_t off_desc = off; off = align16(off + sizeof(NrSmallGraph) * n);
+    const size_t off_ids = off; off = align16(off + sizeof(int) * n);
+    const size_t up_bytes = off;
+    const size_t off_out = off; off = align16(off + sizeof(NrWarpOut) * n);
+    const size_t off_cnt = off; off = align16(off + sizeof(int) * 3 * NR_MAX_W4);
+    int rc = ensure_host(&c->hbuf, &c->hbuf_bytes, off);
+    if (rc) return rc;
+    rc = ensure(&c->wbuf, &c->wbuf_bytes, off);
+    if (rc) return rc;
+    unsigned char *hb = static_cast<unsigned char *>(c->hbuf);
+    NrSmallGraph *hdesc = reinterpret_cast<NrSmallGraph *>(hb + off_desc);
+    int *hids = reinterpret_cast<int *>(hb + off_ids);
+    {
+        int fill[3 * NR_MAX_W4];
+        for (int k = 0; k < 3 * NR_MAX_W4; ++k) fill[k] = class_begin[k];
+        for (int i = 0; i < n; ++i) {
+            const int slot = fill[cls[i]]++;
+            hdesc[slot] = desc[i];
+            hids[slot] = i;
+        }
     }
-    const int nclass = (int)spans.size();
-    // launch geometry per class and slab size
-    const int block = NR_WARP_BLOCK, warps_pb = block / 32;
-    std::vector<int> grids(nclass);
-    std::vector<size_t> smems(nclass);
+    c->parallel_for(n, 128, [&](int i) { small_fill(&gs[i], &desc[i], hb + off_blob + desc[i].blob_off); });
+
+    // launch geometry per class (occupancy cached per kernel and shared-memory size)
+    const int warps_pb = cfg.warps_per_block, block = 32 * warps_pb;
+    int grids[3 * NR_MAX_W4] = {0};
+    size_t smems[3 * NR_MAX_W4] = {0};
     size_t slab_need = 0;
-    for (int k = 0; k < nclass; ++k) {
-        const int G = spans[k].first.first, W4 = spans[k].first.second;
-        if (W4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
+    for (int k = 0; k < 3 * NR_MAX_W4; ++k) {
+        if (!class_count[k]) continue;
+        const int G = 8 << (k / NR_MAX_W4), W4 = k % NR_MAX_W4 + 1;
         const void *kfn = warp_kernel(G, W4);
         if (!kfn) return NR_ERR_UNSUPPORTED;
         const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfg.pages) * warps_pb;
-        NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int bps = 0;
-        NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
+        auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
+        int bps;
+        if (it == c->occupancy.end()) {
+            NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
+            c->occupancy[{kfn, smem * 64 + warps_pb}] = bps;
+        } else {
+            bps = it->second;
+        }
         if (bps < 1) return NR_ERR_UNSUPPORTED;
-        const int cnt = spans[k].second.second;
-        const int grid = std::max(1, std::min(bps * c->sms, (cnt + warps_pb - 1) / warps_pb));
+        const int grid = std::max(1, std::min(bps * c->sms, (class_count[k] + warps_pb - 1) / warps_pb));
         grids[k] = grid;
         smems[k] = smem;
         slab_need = std::max(slab_need, (size_t)grid * warps_pb * cfg.pages * NR_PAGE * (16 * (size_t)W4 + 8));
     }
-    int rc = ensure(&c->wslab, &c->wslab_bytes, slab_need);
-    if (rc) return rc;
-    size_t off = 0;
-    const size_t off_blob = off; off = align16(off + blob.size());
-    const size_t off_desc = off; off = align16(off + sizeof(NrSmallGraph) * n);
-    const size_t off_ids = off; off = align16(off + sizeof(int) * n);
-    const size_t off_out = off; off = align16(off + sizeof(NrWarpOut) * n);
-    const size_t off_cnt = off; off = align16(off + sizeof(int) * nclass);
-    rc = ensure(&c->wbuf, &c->wbuf_bytes, off);
+    rc = ensure(&c->wslab, &c->wslab_bytes, slab_need);
     if (rc) return rc;
     unsigned char *wb = static_cast<unsigned char *>(c->wbuf);
     cudaStream_t s = c->stream;
-    NR_CUDA_TRY(cudaMemcpyAsync(wb + off_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemcpyAsync(wb + off_desc, dsorted.data(), sizeof(NrSmallGraph) * n, cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemcpyAsync(wb + off_ids, ids.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemsetAsync(wb + off_cnt, 0, sizeof(int) * nclass, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, up_bytes, cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemsetAsync(wb + off_cnt, 0, sizeof(int) * 3 * NR_MAX_W4, s));
     NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
-    for (int k = 0; k < nclass; ++k) {
-        const int G = spans[k].first.first, W4 = spans[k].first.second;
+    int first_grid = 0;
+    for (int k = 0; k < 3 * NR_MAX_W4; ++k) {
+        if (!class_count[k]) continue;
+        const int G = 8 << (k / NR_MAX_W4), W4 = k % NR_MAX_W4 + 1;
+        if (!first_grid) first_grid = grids[k];
         NrWarpParams P;
         P.blob = wb + off_blob;
-        P.inst = reinterpret_cast<const NrSmallGraph *>(wb + off_desc) + spans[k].second.first;
-        P.inst_id = reinterpret_cast<const int *>(wb + off_ids) + spans[k].second.first;
-        P.n_inst = spans[k].second.second;
+        P.inst = reinterpret_cast<const NrSmallGraph *>(wb + off_desc) + class_begin[k];
+        P.inst_id = reinterpret_cast<const int *>(wb + off_ids) + class_begin[k];
+        P.n_inst = class_count[k];
         P.next_inst = reinterpret_cast<int *>(wb + off_cnt) + k;
         P.slab_mask = static_cast<uint4 *>(c->wslab);
         const size_t warps = (size_t)grids[k] * warps_pb;
@@ -535,14 +701,18 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         P.escalate = cfg.escalate;
         P.eps = cfg.eps;
         P.target = cfg.target;
+        P.target_fix = nr_fix_of(cfg.target);
         P.max_nodes = cfg.max_nodes;
         P.out = reinterpret_cast<NrWarpOut *>(wb + off_out);
         void *args[] = {&P};
+        // the dynamic shared-memory limit is per-kernel state that another setting may have lowered
+        NR_CUDA_TRY(cudaFuncSetAttribute(warp_kernel(G, W4), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smems[k]));
         NR_CUDA_TRY(cudaLaunchKernel(warp_kernel(G, W4), dim3(grids[k]), dim3(block), args, smems[k], s));
     }
     NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
-    std::vector<NrWarpOut> out(n);
-    NR_CUDA_TRY(cudaMemcpyAsync(out.data(), wb + off_out, sizeof(NrWarpOut) * n, cudaMemcpyDeviceToHost, s));
+    NrWarpOut *hout = reinterpret_cast<NrWarpOut *>(hb + off_out);
+    NR_CUDA_TRY(cudaMemcpyAsync(hout, wb + off_out, sizeof(NrWarpOut) * n, cudaMemcpyDeviceToHost, s));
     NR_CUDA_TRY(cudaStreamSynchronize(s));
     float ms = 0.f;
     NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
@@ -550,10 +720,10 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         nr_result *r = &res[i];
         r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
-        if (out[i].status == 2) { handover->push_back(i); continue; }
-        fill_from_warp(out[i], cfg, desc[i].w4, r);
+        if (hout[i].status == 2) { handover->push_back(i); continue; }
+        fill_from_warp(hout[i], cfg, desc[i].w4, r);
         r->ms = ms;
-        r->grid_blocks = grids[0];
+        r->grid_blocks = first_grid;
         r->block_threads = block;
         r->h2d_bytes = desc[i].blob_bytes + sizeof(NrSmallGraph) + sizeof(int);
         r->d2h_bytes = sizeof(NrWarpOut);
@@ -569,13 +739,15 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
     if (n == 0) return NR_OK;
     nr_options o;
     if (opt) o = *opt; else nr_options_default(&o);
-    for (int i = 0; i < n; ++i) {
+    std::lock_guard<std::mutex> lock(c->mu);
+    std::atomic<int> bad(NR_OK);
+    c->parallel_for(n, 256, [&](int i) {
         memset(&res[i], 0, sizeof(nr_result));
         int rc = validate(&gs[i], srcs[i], dsts[i]);
-        if (rc) return rc;
-        if (gs[i].n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
-    }
-    std::lock_guard<std::mutex> lock(c->mu);
+        if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) rc = NR_ERR_UNSUPPORTED;
+        if (rc) bad.store(rc);
+    });
+    if (bad.load() != NR_OK) return bad.load();
     NR_CUDA_TRY(cudaSetDevice(c->device));
     const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
     const WarpRunCfg cfg = warp_cfg(&o, capacity, exhaustive);
@@ -586,6 +758,64 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
         rc = run_grid_small(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, &res[i]);
         if (rc) return rc;
     }
+    return NR_OK;
+}
+
+// Autotuner: time candidate warp-engine settings on (a sample of) the batch
+// and return the fastest.  Candidates: bucket resolution (2^shift buckets per
+// octave, shift 0..2, the "bucket count"), pages per warp (the pop chunk:
+// how much of a bucket a warp holds and takes at a time), and warps per
+// block.  Every candidate gives a valid result (exact counts for exhaustive
+// runs; for truncated runs a bracket whose width meets the target); the
+// choice only changes time, and for truncated runs where the stop falls.
+extern "C" int nr_autotune(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
+                           uint64_t capacity, const nr_options *opt, nr_options *best, double *best_ms)
+{
+    if (!c || n <= 0 || !gs || !srcs || !dsts || !best) return NR_ERR_INVALID;
+    nr_options base;
+    if (opt) base = *opt; else nr_options_default(&base);
+    const int sample = std::min(n, 4096);
+    std::vector<nr_result> res(sample);
+    const bool exhaustive = !(base.target_width > 0) && base.order != NR_ORDER_MAXMASS &&
+                            base.order != NR_ORDER_LEARNED;
+    const int shifts_t[] = {0, 1, 2};
+    const int shifts_e[] = {base.bucket_shift};
+    const int *shifts = exhaustive ? shifts_e : shifts_t;
+    const int n_shift = exhaustive ? 1 : 3;
+    const uint64_t pages_c[] = {64, 512};
+    const int wpb_c[] = {2, 4, 8};
+    double best_t = 1e300;
+    nr_options pick = base;
+    for (int si = 0; si < n_shift; ++si)
+        for (uint64_t pg : pages_c)
+            for (int wpb : wpb_c) {
+                nr_options o = base;
+                o.bucket_shift = shifts[si];
+                o.n_buckets = 64 << std::max(0, shifts[si]);
+                o.warps_per_block = wpb;
+                const uint64_t cap = capacity ? std::min<uint64_t>(capacity, pg * NR_PAGE) : pg * NR_PAGE;
+                double t = 1e300;
+                for (int rep = 0; rep < 3; ++rep) {
+                    int rc = nr_reliability_batch(c, sample, gs, srcs, dsts, cap, &o, res.data());
+                    if (rc) return rc;
+                    double ms = 0;
+                    bool warp_only = true;
+                    for (int i = 0; i < sample; ++i) {
+                        if (res[i].engine != NR_ENGINE_WARP) warp_only = false;
+                        ms = std::max(ms, res[i].ms);
+                    }
+                    if (!warp_only) ms = 1e300;      // a hand-over costs a full extra solve
+                    t = std::min(t, ms);
+                }
+                if (t < best_t) {
+                    best_t = t;
+                    pick = o;
+                    pick.max_nodes = base.max_nodes;
+                    if (!capacity) pick.pages_per_warp = (int32_t)pg;
+                }
+            }
+    *best = pick;
+    if (best_ms) *best_ms = best_t;
     return NR_OK;
 }
 

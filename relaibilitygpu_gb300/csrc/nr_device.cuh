@@ -1,31 +1,105 @@
 // nr_device.cuh -- device helpers shared by the engine kernels.
 #pragma once
 
+#include <string.h>
+
 #include "nr_internal.h"
 
 #define NR_FULL 0xffffffffu
 
-__device__ __forceinline__ void nr_ks_add(NrKs &s, double x)
+__host__ __device__ __forceinline__ NrFix nr_fix_zero()
 {
-    double t = __dadd_rn(s.hi, x);
-    double bp = __dadd_rn(t, -s.hi);
-    double err = __dadd_rn(__dadd_rn(s.hi, -__dadd_rn(t, -bp)), __dadd_rn(x, -bp));
-    s.hi = t;
-    s.lo = __dadd_rn(s.lo, err);
+    NrFix r;
+    r.w0 = r.w1 = r.w2 = 0ull;
+    return r;
 }
 
-__device__ __forceinline__ void nr_ks_merge(NrKs &s, const NrKs &o)
+// exact value of a non-negative finite double, as a 192-bit fixed-point number
+__host__ __device__ __forceinline__ NrFix nr_fix_of(double m)
 {
-    nr_ks_add(s, o.hi);
-    nr_ks_add(s, o.lo);
+    unsigned long long bits;
+#ifdef __CUDA_ARCH__
+    bits = (unsigned long long)__double_as_longlong(m);
+#else
+    memcpy(&bits, &m, 8);
+#endif
+    NrFix r = nr_fix_zero();
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    unsigned long long M = bits & 0xfffffffffffffull;
+    int e;
+    if (ex == 0) {
+        e = -1074;
+    } else {
+        M |= 1ull << 52;
+        e = ex - 1075;
+    }
+    if (M == 0ull) return r;
+    const int s = e + NR_FIX_FRAC;
+    if (s >= 0) {
+        const int k = s >> 6, b = s & 63;
+        const unsigned long long lo = M << b;
+        const unsigned long long hi = b ? (M >> (64 - b)) : 0ull;
+        if (k == 0) { r.w0 = lo; r.w1 = hi; }
+        else if (k == 1) { r.w1 = lo; r.w2 = hi; }
+        else if (k == 2) { r.w2 = lo; }
+    } else if (-s < 64) {
+        r.w0 = M >> (-s);
+    }
+    return r;
 }
 
-__device__ __forceinline__ NrKs nr_ks_shfl_down(const NrKs &s, int off)
+__host__ __device__ __forceinline__ void nr_fix_add(NrFix &a, const NrFix &b)
 {
-    NrKs o;
-    o.hi = __shfl_down_sync(NR_FULL, s.hi, off);
-    o.lo = __shfl_down_sync(NR_FULL, s.lo, off);
+    const unsigned long long w0 = a.w0 + b.w0;
+    const unsigned long long c0 = w0 < a.w0;
+    const unsigned long long t1 = a.w1 + b.w1;
+    unsigned long long c1 = t1 < a.w1;
+    const unsigned long long w1 = t1 + c0;
+    c1 += w1 < t1;
+    a.w2 = a.w2 + b.w2 + c1;
+    a.w1 = w1;
+    a.w0 = w0;
+}
+
+__host__ __device__ __forceinline__ void nr_fix_sub(NrFix &a, const NrFix &b)
+{
+    const unsigned long long w0 = a.w0 - b.w0;
+    const unsigned long long b0 = a.w0 < b.w0;
+    const unsigned long long t1 = a.w1 - b.w1;
+    unsigned long long b1 = a.w1 < b.w1;
+    const unsigned long long w1 = t1 - b0;
+    b1 += t1 < b0;
+    a.w2 = a.w2 - b.w2 - b1;
+    a.w1 = w1;
+    a.w0 = w0;
+}
+
+__host__ __device__ __forceinline__ bool nr_fix_le(const NrFix &a, const NrFix &b)
+{
+    if (a.w2 != b.w2) return a.w2 < b.w2;
+    if (a.w1 != b.w1) return a.w1 < b.w1;
+    return a.w0 <= b.w0;
+}
+
+__device__ __forceinline__ void nr_fix_add_mass(NrFix &a, double m) { nr_fix_add(a, nr_fix_of(m)); }
+
+__device__ __forceinline__ NrFix nr_fix_shfl_xor(const NrFix &a, int off)
+{
+    NrFix o;
+    o.w0 = __shfl_xor_sync(NR_FULL, a.w0, off);
+    o.w1 = __shfl_xor_sync(NR_FULL, a.w1, off);
+    o.w2 = __shfl_xor_sync(NR_FULL, a.w2, off);
     return o;
+}
+
+// exact warp total, returned on every lane
+__device__ __forceinline__ NrFix nr_fix_warp_sum(NrFix a)
+{
+    for (int off = 16; off > 0; off >>= 1) {
+        const NrFix o = nr_fix_shfl_xor(a, off);
+        nr_fix_add(a, o);
+    }
+    return a;
 }
 
 __device__ __forceinline__ long long nr_globaltimer()
@@ -80,43 +154,40 @@ __device__ __forceinline__ bool nr_grid_sync(unsigned *count, unsigned *gen, int
 }
 
 // Block reduction of the per-lane sums and counters into one NrPartial.
-__device__ __forceinline__ void nr_block_partial(NrPartial *out, NrKs R, NrKs et, NrKs es,
+__device__ __forceinline__ void nr_block_partial(NrPartial *out, NrFix R, NrFix et, NrFix es,
                                                  unsigned long long nodes, unsigned long long leaves,
                                                  unsigned long long dead, unsigned long long trunc,
                                                  unsigned long long spilled)
 {
-    __shared__ NrKs s_ks[NR_BLOCK_THREADS / 32][3];
+    __shared__ NrFix s_fx[NR_BLOCK_THREADS / 32][3];
     __shared__ unsigned long long s_c[NR_BLOCK_THREADS / 32][5];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    R = nr_fix_warp_sum(R);
+    et = nr_fix_warp_sum(et);
+    es = nr_fix_warp_sum(es);
     for (int off = 16; off > 0; off >>= 1) {
-        NrKs a = nr_ks_shfl_down(R, off), b = nr_ks_shfl_down(et, off), c = nr_ks_shfl_down(es, off);
-        nr_ks_merge(R, a);
-        nr_ks_merge(et, b);
-        nr_ks_merge(es, c);
-        nodes += __shfl_down_sync(NR_FULL, nodes, off);
-        leaves += __shfl_down_sync(NR_FULL, leaves, off);
-        dead += __shfl_down_sync(NR_FULL, dead, off);
-        trunc += __shfl_down_sync(NR_FULL, trunc, off);
-        spilled += __shfl_down_sync(NR_FULL, spilled, off);
+        nodes += __shfl_xor_sync(NR_FULL, nodes, off);
+        leaves += __shfl_xor_sync(NR_FULL, leaves, off);
+        dead += __shfl_xor_sync(NR_FULL, dead, off);
+        trunc += __shfl_xor_sync(NR_FULL, trunc, off);
+        spilled += __shfl_xor_sync(NR_FULL, spilled, off);
     }
     if (lane == 0) {
-        s_ks[warp][0] = R; s_ks[warp][1] = et; s_ks[warp][2] = es;
+        s_fx[warp][0] = R; s_fx[warp][1] = et; s_fx[warp][2] = es;
         s_c[warp][0] = nodes; s_c[warp][1] = leaves; s_c[warp][2] = dead;
         s_c[warp][3] = trunc; s_c[warp][4] = spilled;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        NrKs r = {0, 0}, a = {0, 0}, b = {0, 0};
+        NrFix r = nr_fix_zero(), a = nr_fix_zero(), b = nr_fix_zero();
         unsigned long long c[5] = {0, 0, 0, 0, 0};
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-            nr_ks_merge(r, s_ks[w][0]);
-            nr_ks_merge(a, s_ks[w][1]);
-            nr_ks_merge(b, s_ks[w][2]);
+            nr_fix_add(r, s_fx[w][0]);
+            nr_fix_add(a, s_fx[w][1]);
+            nr_fix_add(b, s_fx[w][2]);
             for (int k = 0; k < 5; ++k) c[k] += s_c[w][k];
         }
-        out->R_hi = r.hi; out->R_lo = r.lo;
-        out->et_hi = a.hi; out->et_lo = a.lo;
-        out->es_hi = b.hi; out->es_lo = b.lo;
+        out->R = r; out->et = a; out->es = b;
         out->nodes = c[0]; out->leaves = c[1]; out->dead = c[2];
         out->truncated = c[3]; out->spilled = c[4]; out->pad = 0;
     }

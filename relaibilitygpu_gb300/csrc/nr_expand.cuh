@@ -36,13 +36,13 @@ __device__ __forceinline__ NrSmemGraph nr_smem_graph(const unsigned char *s, con
 }
 
 struct NrLaneAcc {
-    NrKs R, et, es;
+    NrFix R, et, es;
     unsigned long long nodes, leaves, dead, trunc, spilled;
 };
 
 __device__ __forceinline__ void nr_acc_zero(NrLaneAcc &a)
 {
-    a.R.hi = a.R.lo = a.et.hi = a.et.lo = a.es.hi = a.es.lo = 0.0;
+    a.R = a.et = a.es = nr_fix_zero();
     a.nodes = a.leaves = a.dead = a.trunc = a.spilled = 0;
 }
 
@@ -68,7 +68,7 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
     if (valid && leader) acc.nodes++;
     bool active = valid;
     if (active && eps > 0.0 && mass < eps) {          // main.cu:537-543
-        if (leader) { acc.trunc++; nr_ks_add(acc.et, mass); }
+        if (leader) { acc.trunc++; nr_fix_add_mass(acc.et, mass); }
         active = false;
     }
 
@@ -135,7 +135,7 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
             P = __dmul_rn(P, sg.p[e]);
         }
     }
-    if (live && leader) { acc.leaves++; nr_ks_add(acc.R, P); }
+    if (live && leader) { acc.leaves++; nr_fix_add_mass(acc.R, P); }
 
     // child of hop v: parent with earlier UNKNOWN hops up and hop v down
 #pragma unroll

@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_kernel(NrGridParams 
                         __stcg(out_mass + slot, cm);
                     } else {                       // queue full: mass to ESP (main.cu:245-252)
                         acc.spilled++;
-                        nr_ks_add(acc.es, cm);
+                        nr_fix_add_mass(acc.es, cm);
                     }
                 }
             }

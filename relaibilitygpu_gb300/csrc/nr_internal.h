@@ -17,12 +17,21 @@
 #define NR_DEV_ERR_BOUNDS 2
 #define NR_DEV_ERR_WAVES 4
 
-// Per-block result partials written at kernel exit (no single-address atomics
-// on the sums; the host merges them with two-sum in block order).
+// Exact mass sums: a 192-bit unsigned integer A standing for A / 2^190.
+// Adding an FP64 mass places its 53-bit significand exactly (masses down to
+// 2^-137 are exact; smaller ones are truncated by less than 2^-190), so sums
+// do not depend on the order of the additions and subtraction is exact too.
+#define NR_FIX_FRAC 190
+struct NrFix {
+    unsigned long long w0, w1, w2;
+};
+
+// Per-block result partials written at kernel exit (no single-address atomics;
+// the host adds them).
 struct NrPartial {
-    double R_hi, R_lo;          // all-up leaf mass
-    double et_hi, et_lo;        // eps-truncated mass
-    double es_hi, es_lo;        // spilled mass
+    NrFix R;                    // all-up leaf mass
+    NrFix et;                   // eps-truncated mass
+    NrFix es;                   // spilled mass
     unsigned long long nodes, leaves, dead, truncated, spilled, pad;
 };
 
@@ -52,10 +61,10 @@ struct NrGridParams {
     long long timeout_ns;
 };
 
-// compensated summation, kept free of contraction by the _rn intrinsics
-struct NrKs {
-    double hi, lo;
-};
+// host helpers for NrFix (nr_api.cu)
+NrFix nr_fix_from_double_host(double m);
+double nr_fix_to_double_host(const NrFix &a);
+void nr_fix_add_host(NrFix &a, const NrFix &b);
 
 // host-side helpers implemented in nr_engine_*.cu
 int nr_launch_grid_small(int G, const NrGridParams &p, int grid, int block, size_t smem,

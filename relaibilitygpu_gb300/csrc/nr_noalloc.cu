@@ -102,18 +102,6 @@ size_t noalloc_tables(const nr_graph *g, int src, int dst, int G, NrSmallGraph *
     return off;
 }
 
-double ks2(double a_hi, double a_lo, double b_hi, double b_lo, double c_hi, double c_lo, bool with_c)
-{
-    double parts[6] = {a_hi, a_lo, b_hi, b_lo, c_hi, c_lo};
-    double hi = 0, lo = 0;
-    for (int i = 0; i < (with_c ? 6 : 4); ++i) {
-        const double x = parts[i], t = hi + x, bp = t - hi;
-        lo += (hi - (t - bp)) + (x - bp);
-        hi = t;
-    }
-    return hi + lo;
-}
-
 }  // namespace
 
 extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const nr_options *opt, nr_result *res)
@@ -183,6 +171,7 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     P.escalate = 0;
     P.eps = o.truncation_eps > 0 ? o.truncation_eps : 0.0;
     P.target = o.target_width > 0 ? o.target_width : 0.0;
+    P.target_fix = nr_fix_of(P.target);
     if (exhaustive) {
         P.wave_mode = 0; P.shift = -1; P.n_buckets = 32; P.max_nodes = o.max_nodes;
     } else {
@@ -209,9 +198,11 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
 
     res->n_nodes = g->n_nodes; res->n_edges = g->n_edges; res->src = src; res->dst = dst;
     res->mask_words = std::max(1, (2 * g->n_edges + 31) / 32);
-    res->R = ks2(out.R_hi, out.R_lo, 0, 0, 0, 0, false);
-    double esp = ks2(out.et_hi, out.et_lo, out.es_hi, out.es_lo, out.q_hi, out.q_lo, out.queued > 0);
-    res->esp = esp < 0 ? 0 : esp;
+    NrFix esp = out.et;
+    nr_fix_add_host(esp, out.es);
+    nr_fix_add_host(esp, out.q);
+    res->R = nr_fix_to_double_host(out.R);
+    res->esp = nr_fix_to_double_host(esp);
     res->R_plus_esp = res->R + res->esp;
     res->trunc_bound = res->R > 0 ? res->esp / res->R : res->esp;
     res->nodes = out.nodes; res->leaves = out.leaves; res->dead_ends = out.dead; res->truncated = out.trunc;

@@ -22,11 +22,12 @@
 
 #include "nr_expand.cuh"
 
-#define NR_WARP_BLOCK 128
+#define NR_WARP_BLOCK 128        // default block: 4 warps
+#define NR_WARP_BLOCK_MAX 256    // largest block the warp kernels are compiled for
 #define NR_PAGE 32
 
 struct NrWarpOut {
-    double R_hi, R_lo, et_hi, et_lo, es_hi, es_lo, q_hi, q_lo;
+    NrFix R, et, es, q;   // exact sums: leaves, eps-truncated, spilled, still queued
     unsigned long long nodes, leaves, dead, trunc, spilled, queued, max_wave;
     long long t_ns;       // device time from instance start to stop (target met or queue empty)
     int waves;
@@ -47,7 +48,8 @@ struct NrWarpParams {
     int wave_mode;                   // 1: whole-bucket waves; 0: one page at a time
     int escalate;                    // 1: on overflow hand the instance to the grid engine
     double eps;
-    double target;                   // stop once ESP + queued mass <= target (wave mode)
+    double target;                   // stop once ESP + queued mass <= target (wave mode); 0 = off
+    NrFix target_fix;                // the same target as an exact fixed-point number
     unsigned long long max_nodes;    // pop budget: page mode hands over, wave mode stops (0 = none)
     NrWarpOut *out;
 };
@@ -61,17 +63,6 @@ __device__ __forceinline__ int nr_bucket(double m, int shift, int nb)
     b = b < 0 ? 0 : b;
     b = b > nb - 1 ? nb - 1 : b;
     return (int)b;
-}
-
-__device__ __forceinline__ NrKs nr_ks_warp_sum(NrKs s)
-{
-    for (int off = 16; off > 0; off >>= 1) {
-        NrKs o = nr_ks_shfl_down(s, off);
-        nr_ks_merge(s, o);
-    }
-    s.hi = __shfl_sync(NR_FULL, s.hi, 0);
-    s.lo = __shfl_sync(NR_FULL, s.lo, 0);
-    return s;
 }
 
 __device__ __forceinline__ unsigned long long nr_warp_sum_u64(unsigned long long x)
@@ -104,7 +95,7 @@ __host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets
 }
 
 template <int G, int W4>
-__global__ void __launch_bounds__(NR_WARP_BLOCK) nr_warp_kernel(NrWarpParams P)
+__global__ void __launch_bounds__(NR_WARP_BLOCK_MAX) nr_warp_kernel(NrWarpParams P)
 {
     constexpr int K = 32 / G;
     constexpr int NW = 4 * W4;
@@ -172,7 +163,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK) nr_warp_kernel(NrWarpParams P)
 
         NrLaneAcc acc;
         nr_acc_zero(acc);
-        NrKs qacc = {lane == 0 ? 1.0 : 0.0, 0.0};   // queued mass held by this lane's pushes/pops
+        NrFix qacc = (lane == 0) ? nr_fix_of(1.0) : nr_fix_zero();   // queued mass: this lane's pushes - pops
         long long qcount = (lane == 0) ? 1 : 0;
         int waves = 0, status = 0;
         unsigned long long max_wave = 0;
@@ -180,12 +171,12 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK) nr_warp_kernel(NrWarpParams P)
         long long t_stop = 0;
 
         for (;;) {
-            if (P.wave_mode && P.target > 0.0) {
-                NrKs w = nr_ks_warp_sum(qacc);
-                NrKs a = nr_ks_warp_sum(acc.et), b = nr_ks_warp_sum(acc.es);
-                nr_ks_merge(w, a);
-                nr_ks_merge(w, b);
-                if (__dadd_rn(w.hi, w.lo) <= P.target) { status = 1; break; }
+            if (P.wave_mode && P.target > 0.0) {     // exact: ESP + queued mass <= target
+                NrFix w = qacc;
+                nr_fix_add(w, acc.et);
+                nr_fix_add(w, acc.es);
+                w = nr_fix_warp_sum(w);
+                if (nr_fix_le(w, P.target_fix)) { status = 1; break; }
             }
             if (P.max_nodes && nr_warp_sum_u64(acc.nodes) >= P.max_nodes) {
                 if (P.wave_mode) { status = 3; } else { status = 2; abandon = true; }
@@ -224,7 +215,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK) nr_warp_kernel(NrWarpParams P)
                     const size_t slot = (size_t)pg * NR_PAGE + idx;
                     if (valid && v < W4) reinterpret_cast<uint4 *>(my_m)[v] = sl_mask[slot * W4 + v];
                     const double mass = valid ? sl_mass[slot] : 0.0;
-                    if (valid && leader) { nr_ks_add(qacc, -mass); qcount--; }
+                    if (valid && leader) { nr_fix_sub(qacc, nr_fix_of(mass)); qcount--; }
                     __syncwarp();
 
                     bool has_child;
@@ -268,13 +259,13 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK) nr_warp_kernel(NrWarpParams P)
                                 for (int k = 0; k < W4; ++k)
                                     d[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
                                 sl_mass[s] = cm;
-                                nr_ks_add(qacc, cm);
+                                nr_fix_add_mass(qacc, cm);
                                 qcount++;
                             } else if (P.escalate) {
                                 abandon = true;
                             } else {                      // queue full: mass to ESP (main.cu:245-252)
                                 acc.spilled++;
-                                nr_ks_add(acc.es, cm);
+                                nr_fix_add_mass(acc.es, cm);
                             }
                             has_child = false;
                         }
@@ -293,16 +284,15 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK) nr_warp_kernel(NrWarpParams P)
         }
         t_stop = nr_globaltimer() - t0;
 
-        NrKs R = nr_ks_warp_sum(acc.R), et = nr_ks_warp_sum(acc.et), es = nr_ks_warp_sum(acc.es);
-        NrKs qm = nr_ks_warp_sum(qacc);
+        const NrFix R = nr_fix_warp_sum(acc.R), et = nr_fix_warp_sum(acc.et), es = nr_fix_warp_sum(acc.es);
+        const NrFix qm = nr_fix_warp_sum(qacc);
         const unsigned long long nodes = nr_warp_sum_u64(acc.nodes), leaves = nr_warp_sum_u64(acc.leaves);
         const unsigned long long dead = nr_warp_sum_u64(acc.dead), trunc = nr_warp_sum_u64(acc.trunc);
         const unsigned long long spilled = nr_warp_sum_u64(acc.spilled);
         const unsigned long long queued = nr_warp_sum_u64((unsigned long long)qcount);
         if (lane == 0) {
             NrWarpOut o;
-            o.R_hi = R.hi; o.R_lo = R.lo; o.et_hi = et.hi; o.et_lo = et.lo; o.es_hi = es.hi; o.es_lo = es.lo;
-            o.q_hi = qm.hi; o.q_lo = qm.lo;
+            o.R = R; o.et = et; o.es = es; o.q = qm;
             o.nodes = nodes; o.leaves = leaves; o.dead = dead; o.trunc = trunc; o.spilled = spilled;
             o.queued = queued; o.max_wave = max_wave; o.t_ns = t_stop; o.waves = waves; o.status = status;
             P.out[P.inst_id[ii]] = o;

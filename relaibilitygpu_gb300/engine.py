@@ -49,7 +49,7 @@ class NrOptions(C.Structure):
         ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("device", C.c_int32),
         ("blocks_per_sm", C.c_int32), ("warps_per_block", C.c_int32), ("timeout_ms", C.c_double),
         ("verbose", C.c_int32), ("pad0", C.c_int32), ("max_nodes", C.c_uint64),
-        ("reserved", C.c_int32 * 4),
+        ("pages_per_warp", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -71,7 +71,7 @@ class NrResult(C.Structure):
 EXPORTS = [
     "nr_options_default", "nr_status_string", "nr_abi_version", "nr_graph_load", "nr_graph_free",
     "nr_initial_mask", "nr_context_create", "nr_context_destroy", "nr_reliability", "nr_reliability_ctx",
-    "nr_reliability_batch", "nr_format_result", "nr_reliability_noalloc",
+    "nr_reliability_batch", "nr_format_result", "nr_reliability_noalloc", "nr_autotune",
 ]
 
 _lib_handle: Optional[C.CDLL] = None
@@ -113,6 +113,9 @@ def lib() -> C.CDLL:
     L.nr_reliability_noalloc.argtypes = [C.POINTER(NrGraph), C.c_int, C.c_int, C.POINTER(NrOptions),
                                          C.POINTER(NrResult)]
     L.nr_reliability_noalloc.restype = C.c_int
+    L.nr_autotune.argtypes = [C.c_void_p, C.c_int, C.POINTER(NrGraph), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                              C.c_uint64, C.POINTER(NrOptions), C.POINTER(NrOptions), C.POINTER(C.c_double)]
+    L.nr_autotune.restype = C.c_int
     L.nr_format_result.argtypes = [C.POINTER(NrResult), C.c_char_p, C.c_size_t]
     L.nr_format_result.restype = C.c_int
     _lib_handle = L
@@ -181,7 +184,7 @@ class _GraphView:
 
 def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto", bucket_shift: int = 2,
                  n_buckets: int = 256, device: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0,
-                 timeout_ms: float = 60000.0, max_nodes: int = 0) -> NrOptions:
+                 timeout_ms: float = 60000.0, max_nodes: int = 0, pages_per_warp: int = 0) -> NrOptions:
     o = NrOptions()
     lib().nr_options_default(C.byref(o))
     o.truncation_eps = float(eps)
@@ -194,7 +197,17 @@ def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto
     o.warps_per_block = int(warps_per_block)
     o.timeout_ms = float(timeout_ms)
     o.max_nodes = int(max_nodes)
+    o.pages_per_warp = int(pages_per_warp)
     return o
+
+
+def options_dict(o: NrOptions) -> dict:
+    """Keyword arguments of make_options that reproduce an NrOptions."""
+    inv = {v: k for k, v in ORDERS.items()}
+    return dict(eps=o.truncation_eps, target_width=o.target_width, order=inv.get(o.order, "auto"),
+                bucket_shift=o.bucket_shift, n_buckets=o.n_buckets, device=o.device,
+                blocks_per_sm=o.blocks_per_sm, warps_per_block=o.warps_per_block, timeout_ms=o.timeout_ms,
+                max_nodes=o.max_nodes, pages_per_warp=o.pages_per_warp)
 
 
 def _check(rc: int) -> None:
@@ -247,6 +260,17 @@ class Context:
         if raw:
             return batch.res
         return [Result.from_raw(batch.res[i]) for i in range(batch.n)]
+
+
+def autotune(ctx: "Context", batch: "Batch", capacity: int = 0, **opts):
+    """Pick warp-engine settings for a batch with nr_autotune; returns (options dict, device ms)."""
+    o = make_options(**opts)
+    best = NrOptions()
+    ms = C.c_double()
+    _check(lib().nr_autotune(ctx.h, batch.n, batch.arr, batch.s.ctypes.data_as(C.POINTER(C.c_int32)),
+                             batch.d.ctypes.data_as(C.POINTER(C.c_int32)), int(capacity), C.byref(o),
+                             C.byref(best), C.byref(ms)))
+    return options_dict(best), ms.value
 
 
 class Batch:

@@ -103,3 +103,19 @@ def test_status_strings(engine_lib):
     L = engine_lib.lib()
     for code in range(0, -9, -1):
         assert L.nr_status_string(code)
+
+
+def test_batch_validation_on_host_pool(engine_lib):
+    """Large batches validate on the context's worker threads; a bad instance is reported."""
+    import torch
+    from relaibilitygpu_gb300 import graphs
+    if torch.cuda.is_available():
+        pytest.skip("checks the no-GPU path")
+    try:
+        ctx = engine_lib.Context(0)
+    except engine_lib.NrError as e:
+        assert e.status in (-5, -1)      # no device here: context creation reports it
+        return
+    gs = [graphs.complete(6, p=0.5) for _ in range(2000)]
+    with pytest.raises(engine_lib.NrError):
+        ctx.reliability_batch(gs, [0] * 2000, [9] * 2000)

@@ -1,8 +1,9 @@
 """GPU engine against the oracle and the reference's published results, through the C ABI.
 
 Bars: counts (paths, nodes, leaves, dead ends, waves, widest wave) bit-exact;
-R within 1e-12 relative of the oracle and of brute force (FP64 products in
-the same path order; only the summation order differs)."""
+R and ESP bit-exact against the oracle (FP64 path-order products, summed
+exactly in 192-bit fixed point on both sides); R within 1e-12 relative of
+brute force and of the reference's published values."""
 import numpy as np
 import pytest
 
@@ -28,7 +29,8 @@ def check_exact(r, o):
     assert r.truncated == o.truncated
     assert r.iterations == o.waves
     assert r.max_queue_items == o.max_wave
-    assert rel_close(r.R, o.R, R_TOL), (r.R, o.R)
+    assert r.R == o.R, (r.R, o.R)
+    assert r.esp == o.esp, (r.esp, o.esp)
 
 
 @pytest.mark.parametrize("name", ["COMP8", "COMP8-03", "COMP9"])
@@ -103,7 +105,7 @@ def test_eps_truncation_matches_oracle(ctx, load_golden_graph, oracle):
         r = ctx.reliability(g, 0, 8, capacity=1 << 22, eps=eps)
         o = oracle.run(g, 0, 8, eps=eps)
         check_exact(r, o)
-        assert rel_close(r.esp, o.esp_truncated, 1e-12)
+        assert r.esp == o.esp_truncated
 
 
 def test_overflow_spills_and_brackets(ctx, golden, load_golden_graph):
