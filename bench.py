@@ -231,7 +231,8 @@ def main():
         # autotuner (nr_autotune): bucket resolution, pages per warp, warps per block
         tuned, tuned_ms = nr.autotune(ctx, batch, capacity=w["capacity"], **w["opts"])
         w["opts"] = tuned
-        w["oracle"] = dict(bucket_shift=tuned["bucket_shift"], n_buckets=tuned["n_buckets"],
+        w["oracle"] = dict(bucket_shift=tuned["bucket_shift"],
+                           n_buckets=tuned["n_buckets"] if tuned["bucket_shift"] >= 0 else 1,
                            target_width=tuned["target_width"])
 
     def call():
@@ -288,15 +289,10 @@ def main():
                "instances": 16}
 
     t_dev = dev_ms / 1e3
-    if dist is not None:
-        t = torch.tensor([t_dev, wall_s, float(nodes)], dtype=torch.float64, device=f"cuda:{local}")
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        tsum = t.clone()
-        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
-        t_dev, wall_s, tot_nodes = float(tmax[0]), float(tmax[1]), float(tsum[2])
-    else:
-        tot_nodes = float(nodes)
+    # replicas: units add up over ranks, the slowest rank sets the time (no data-path collective)
+    from relaibilitygpu_gb300 import replicas
+    tot = replicas.reduce_totals({"nodes": float(nodes), "t_dev_max": t_dev, "wall_max": wall_s})
+    tot_nodes, t_dev, wall_s = tot["nodes"], tot["t_dev_max"], tot["wall_max"]
     if rank != 0:
         ctx.close()
         if dist is not None:

@@ -75,7 +75,8 @@ typedef struct nr_options {
                                  The reference CLI default is 1e-15. */
     double   target_width;    /* stop once ESP + queued mass <= target; 0 = run to empty queue */
     int32_t  order;           /* NR_ORDER_* */
-    int32_t  bucket_shift;    /* max-mass order: 2^shift buckets per factor of two in mass */
+    int32_t  bucket_shift;    /* max-mass order: 2^shift buckets per factor of two in mass; -1 = one
+                                 bucket (breadth-first waves, still stopped by target_width) */
     int32_t  n_buckets;       /* max-mass order: bucket count; the last takes all smaller masses */
     int32_t  device;          /* CUDA device ordinal */
     int32_t  blocks_per_sm;   /* 0 = occupancy maximum */
@@ -167,7 +168,7 @@ int  nr_reliability_batch(nr_context *ctx, int n_instances, const nr_graph *grap
 
 /* Autotuner for batches (no reference counterpart).  Times the warp engine on
  * up to 4096 instances of the batch for each candidate setting -- bucket
- * resolution (bucket_shift 0..2, the bucket count), pages per warp (64 or 512,
+ * resolution (bucket_shift -1..2, where -1 is one bucket: breadth-first waves), pages per warp (64 or 512,
  * how much of the queue a warp holds) and warps per block (2, 4, 8) -- and
  * writes the fastest into *best (based on *opt), with its device time in
  * *best_ms.  Every candidate returns a valid result; the choice changes time

@@ -763,7 +763,7 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
 
 // Autotuner: time candidate warp-engine settings on (a sample of) the batch
 // and return the fastest.  Candidates: bucket resolution (2^shift buckets per
-// octave, shift 0..2, the "bucket count"), pages per warp (the pop chunk:
+// octave, shift 0..2, or one bucket = breadth-first waves; the "bucket count"), pages per warp (the pop chunk:
 // how much of a bucket a warp holds and takes at a time), and warps per
 // block.  Every candidate gives a valid result (exact counts for exhaustive
 // runs; for truncated runs a bracket whose width meets the target); the
@@ -778,10 +778,10 @@ extern "C" int nr_autotune(nr_context *c, int n, const nr_graph *gs, const int32
     std::vector<nr_result> res(sample);
     const bool exhaustive = !(base.target_width > 0) && base.order != NR_ORDER_MAXMASS &&
                             base.order != NR_ORDER_LEARNED;
-    const int shifts_t[] = {0, 1, 2};
+    const int shifts_t[] = {-1, 0, 1, 2};   // -1: one bucket, i.e. breadth-first waves
     const int shifts_e[] = {base.bucket_shift};
     const int *shifts = exhaustive ? shifts_e : shifts_t;
-    const int n_shift = exhaustive ? 1 : 3;
+    const int n_shift = exhaustive ? 1 : 4;
     const uint64_t pages_c[] = {64, 512};
     const int wpb_c[] = {2, 4, 8};
     double best_t = 1e300;

@@ -46,12 +46,12 @@ def test_k15_target_width(ctx, oracle, target):
         assert r.engine == "warp"
 
 
-@pytest.mark.parametrize("shift,nb", [(0, 64), (1, 128), (3, 512)])
+@pytest.mark.parametrize("shift,nb", [(-1, 64), (0, 64), (1, 128), (3, 512)])
 def test_bucket_resolutions(ctx, oracle, shift, nb):
     from relaibilitygpu_gb300 import graphs
     g = graphs.complete(12, p_range=(0.7, 0.99), seed=5)
     r = ctx.reliability(g, 0, 11, target_width=1e-7, bucket_shift=shift, n_buckets=nb)
-    o = oracle.run(g, 0, 11, bucket_shift=shift, n_buckets=nb, target_width=1e-7)
+    o = oracle.run(g, 0, 11, bucket_shift=shift, n_buckets=nb if shift >= 0 else 1, target_width=1e-7)
     check_wave_parity(r, o)
 
 
@@ -159,12 +159,12 @@ def test_autotune_picks_valid_settings(ctx, oracle):
     b = nr.Batch(gs, [0] * len(gs), [14] * len(gs))
     best, ms = nr.autotune(ctx, b, target_width=1e-6)
     assert ms > 0
-    assert best["bucket_shift"] in (0, 1, 2) and best["warps_per_block"] in (2, 4, 8)
+    assert best["bucket_shift"] in (-1, 0, 1, 2) and best["warps_per_block"] in (2, 4, 8)
     assert best["pages_per_warp"] in (64, 512)
     res = ctx.run_batch(b, **best)
     for g, r in zip(gs[:32], res[:32]):
-        o = oracle.run(g, 0, 14, bucket_shift=best["bucket_shift"], n_buckets=best["n_buckets"],
-                       target_width=1e-6)
+        o = oracle.run(g, 0, 14, bucket_shift=best["bucket_shift"],
+                       n_buckets=best["n_buckets"] if best["bucket_shift"] >= 0 else 1, target_width=1e-6)
         check_wave_parity(r, o)
 
 
