@@ -24,7 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I" + INCLUDE, "-I" + CSRC]
 
-CU_SOURCES = ["nr_api.cu", "nr_engine_g8.cu", "nr_engine_g16.cu", "nr_engine_g32.cu", "nr_noalloc.cu"]
+CU_SOURCES = ["nr_api.cu", "nr_engine_g8.cu", "nr_engine_g16.cu", "nr_engine_g32.cu", "nr_engine_wide.cu",
+              "nr_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -21,10 +21,12 @@
 #include "nr_internal.h"
 #include "nr_device.cuh"
 #include "nr_warp.cuh"
+#include "nr_wide.cuh"
 
 const void *nr_grid_kernel_ptr_g8(int w4);
 const void *nr_grid_kernel_ptr_g16(int w4);
 const void *nr_grid_kernel_ptr_g32(int w4);
+const void *nr_grid_wide_kernel_ptr(int w4);
 const void *nr_warp_kernel_ptr_g8(int w4);
 const void *nr_warp_kernel_ptr_g16(int w4);
 const void *nr_warp_kernel_ptr_g32(int w4);
@@ -530,6 +532,147 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
 }
 
 // ---------------------------------------------------------------------------
+// whole-GPU engine for 33..1024 nodes (nr_wide.cuh)
+// ---------------------------------------------------------------------------
+static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg, std::vector<unsigned char> *blob)
+{
+    const int n = g->n_nodes, E = g->n_edges;
+    const int W = std::max(1, (2 * E + 31) / 32);
+    wg->n = n; wg->e = E; wg->w4 = (W + 3) / 4; wg->src = src; wg->dst = dst; wg->n_arcs = g->n_arcs;
+    wg->nwd = (n + 31) / 32;
+    size_t off = 0;
+    wg->off_p = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
+    wg->off_q = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
+    wg->off_row = (int)off; off = align16(off + sizeof(int) * (n + 1));
+    wg->off_arc = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
+    wg->blob_bytes = (int)off;
+    blob->assign(off, 0);
+    double *p = reinterpret_cast<double *>(blob->data() + wg->off_p);
+    double *q = reinterpret_cast<double *>(blob->data() + wg->off_q);
+    int *row = reinterpret_cast<int *>(blob->data() + wg->off_row);
+    uint32_t *arc = reinterpret_cast<uint32_t *>(blob->data() + wg->off_arc);
+    for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
+    for (int u = 0; u <= n; ++u) row[u] = g->row_ptr[u];
+    for (int j = 0; j < g->n_arcs; ++j) arc[j] = ((uint32_t)g->edge_id[j] << 10) | (uint32_t)g->col_idx[j];
+}
+
+static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
+                         nr_result *r)
+{
+    if (g->n_nodes > NR_WIDE_MAX_N || g->n_edges > 65535) return NR_ERR_UNSUPPORTED;
+    NrWideGraph wg;
+    std::vector<unsigned char> blob;
+    build_wide_blob(g, src, dst, &wg, &blob);
+    const int W4 = wg.w4;
+    if (W4 > NR_WIDE_MAX_W4) return NR_ERR_UNSUPPORTED;
+    const void *kfn = nr_grid_wide_kernel_ptr(W4);
+    if (!kfn) return NR_ERR_UNSUPPORTED;
+    const int block = NR_WIDE_BLOCK;
+    const size_t smem = (size_t)wg.blob_bytes + (block / 32) * nr_wide_warp_shm(wg.n, W4);
+    NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int bps = 0;
+    NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
+    if (bps < 1) return NR_ERR_UNSUPPORTED;
+    if (o->blocks_per_sm > 0 && o->blocks_per_sm < bps) bps = o->blocks_per_sm;
+    const int grid = bps * c->sms;
+    const size_t item_bytes = (size_t)W4 * 16 + sizeof(double);
+    const size_t mask_bytes = align16((size_t)cap * W4 * 16);
+    const size_t mass_bytes = align16((size_t)cap * sizeof(double));
+    const size_t qneed = 2 * (mask_bytes + mass_bytes);
+    size_t free_b = 0, total_b = 0;
+    NR_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    if (qneed > c->qbytes && qneed > free_b + c->qbytes) return NR_ERR_NOMEM;
+    int rc = ensure(&c->qbuf, &c->qbytes, qneed);
+    if (rc) return rc;
+    const int max_waves = g->n_edges + 2;
+    size_t off = 0;
+    const size_t off_blob = off; off = align16(off + blob.size());
+    const size_t off_wc = off; off = align16(off + sizeof(unsigned long long) * (max_waves + 1));
+    const size_t off_bar = off; off = align16(off + 4 * sizeof(unsigned));
+    const size_t off_part = off; off = align16(off + sizeof(NrPartial) * grid);
+    rc = ensure(&c->sbuf, &c->sbytes, off);
+    if (rc) return rc;
+    unsigned char *sb = static_cast<unsigned char *>(c->sbuf);
+    unsigned char *qb = static_cast<unsigned char *>(c->qbuf);
+    NrGridWideParams P;
+    P.g = wg;
+    P.blob = sb + off_blob;
+    P.mask[0] = reinterpret_cast<uint4 *>(qb);
+    P.mass[0] = reinterpret_cast<double *>(qb + mask_bytes);
+    P.mask[1] = reinterpret_cast<uint4 *>(qb + mask_bytes + mass_bytes);
+    P.mass[1] = reinterpret_cast<double *>(qb + 2 * mask_bytes + mass_bytes);
+    P.capacity = cap;
+    P.wave_count = reinterpret_cast<unsigned long long *>(sb + off_wc);
+    P.max_waves = max_waves;
+    P.bar_count = reinterpret_cast<unsigned *>(sb + off_bar);
+    P.bar_gen = P.bar_count + 1;
+    P.status = reinterpret_cast<int *>(P.bar_count + 2);
+    P.partials = reinterpret_cast<NrPartial *>(sb + off_part);
+    P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
+    P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
+    std::vector<uint32_t> root(4 * W4, 0);
+    nr_initial_mask(g, root.data(), 4 * W4);
+    const double one = 1.0;
+    const unsigned long long one_u = 1;
+    cudaStream_t s = c->stream;
+    NR_CUDA_TRY(cudaMemcpyAsync(sb + off_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemsetAsync(sb + off_wc, 0, off_part - off_wc, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.wave_count, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.mask[0], root.data(), 16 * W4, cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.mass[0], &one, sizeof(one), cudaMemcpyHostToDevice, s));
+    void *args[] = {&P};
+    NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
+    NR_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(block), args, smem, s));
+    NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
+    std::vector<unsigned long long> wc(max_waves + 1);
+    std::vector<NrPartial> parts(grid);
+    int status = 0;
+    NR_CUDA_TRY(cudaMemcpyAsync(wc.data(), P.wave_count, sizeof(unsigned long long) * wc.size(),
+                                cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(parts.data(), P.partials, sizeof(NrPartial) * grid, cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(&status, P.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    NrFix R = nr_fix_zero(), esp = nr_fix_zero();
+    unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0;
+    for (const NrPartial &pp : parts) {
+        nr_fix_add(R, pp.R);
+        nr_fix_add(esp, pp.et);
+        nr_fix_add(esp, pp.es);
+        nodes += pp.nodes; leaves += pp.leaves; dead += pp.dead; trunc += pp.truncated; spilled += pp.spilled;
+    }
+    int waves = 0;
+    unsigned long long maxw = 0;
+    for (int k = 0; k <= max_waves; ++k) {
+        const unsigned long long nn = std::min<unsigned long long>(wc[k], cap);
+        if (!nn) break;
+        waves++;
+        maxw = std::max(maxw, nn);
+    }
+    r->R = nr_fix_to_double_host(R);
+    r->esp = nr_fix_to_double_host(esp);
+    r->R_plus_esp = r->R + r->esp;
+    r->trunc_bound = r->R > 0 ? r->esp / r->R : r->esp;
+    r->nodes = nodes; r->leaves = leaves; r->dead_ends = dead; r->truncated = trunc; r->spilled = spilled;
+    r->paths = leaves + spilled;
+    r->iterations = waves;
+    r->max_queue_items = maxw;
+    r->item_bytes = (int)item_bytes;
+    r->max_queue_mb = (double)maxw * item_bytes / (1024.0 * 1024.0);
+    r->ms = ms;
+    r->engine = NR_ENGINE_GRID;
+    r->grid_blocks = grid;
+    r->block_threads = block;
+    r->capacity = cap;
+    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one);
+    r->d2h_bytes = sizeof(unsigned long long) * wc.size() + sizeof(NrPartial) * grid + sizeof(int);
+    if (status & NR_DEV_ERR_TIMEOUT) return NR_ERR_TIMEOUT;
+    if (status) return NR_ERR_INTERNAL;
+    return NR_OK;
+}
+
+// ---------------------------------------------------------------------------
 // warp-per-instance engine (nr_warp.cuh)
 // ---------------------------------------------------------------------------
 struct WarpRunCfg {
@@ -836,7 +979,12 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     if (capacity == 0) capacity = 1u << 20;   // reference default (common.h:33)
     std::lock_guard<std::mutex> lock(c->mu);
     NR_CUDA_TRY(cudaSetDevice(c->device));
-    if (g->n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
+    if (g->n_nodes > NR_SMALL_MAX_N) {
+        // 33..1024 nodes: whole-GPU wave engine (max-mass order and target widths are n <= 32 only)
+        if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED)
+            return NR_ERR_UNSUPPORTED;
+        return run_grid_wide(c, g, src, dst, capacity, &o, res);
+    }
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {
         // bucketed max-mass order: one warp owns the instance (nr_warp.cuh)
         const WarpRunCfg cfg = warp_cfg(&o, capacity, false);

@@ -63,7 +63,8 @@ def complete_graphs():
     for name, n, p, path in [("COMP8", 8, 0.5, "workingPad/COMP8.txt"), ("COMP8-03", 8, 0.3, "workingPad/COMP8-03.txt"),
                              ("COMP9", 9, 0.5, "workingPad/COMP9.txt"), ("COMP10-05", 10, 0.5, "workingPad/COMP10-05.txt"),
                              ("COMP15-05", 15, 0.5, "workingPad/COMP15-05.txt"),
-                             ("COMP25-05", 25, 0.5, "workingPad/COMP25-05.txt")]:
+                             ("COMP25-05", 25, 0.5, "workingPad/COMP25-05.txt"),
+                             ("COMP40", 40, 0.1, "workingPad/COMP40.txt")]:
         g = G.complete(n, p=p)
         g.name = name
         out[name] = (g, path, "U")

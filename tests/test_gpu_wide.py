@@ -1,0 +1,74 @@
+"""Whole-GPU engine for 33..1024 nodes (nr_wide.cuh) against the oracle.
+
+Same bars as the small engines: counts, waves and widest wave bit-exact; R and
+ESP (exact fixed-point sums) equal to the oracle's."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(engine_lib):
+    c = engine_lib.Context(0)
+    yield c
+    c.close()
+
+
+def check(r, o):
+    assert (r.paths, r.nodes, r.leaves, r.dead_ends, r.truncated, r.spilled) == \
+        (o.paths, o.nodes, o.leaves, o.dead, o.truncated, o.spilled)
+    assert (r.iterations, r.max_queue_items) == (o.waves, o.max_wave)
+    assert r.R == o.R, (r.R, o.R)
+    assert r.esp == o.esp, (r.esp, o.esp)
+
+
+CASES = [
+    ("K40 p=0.5", lambda G: (G.complete(40, p=0.5), 0, 39), 1e-5),
+    ("K40 p=0.1 (COMP40)", lambda G: (G.complete(40, p=0.1), 0, 39), 1e-4),
+    ("K40 p~U[0.9,0.99]", lambda G: (G.complete(40, p_range=(0.9, 0.99), seed=1), 0, 39), 1e-10),
+    ("rgg 200/600", lambda G: (lambda g: (g, g.src, g.dst))(G.rgg(200, 600, p_range=(0.9, 0.99), seed=7)), 1e-5),
+    ("rgg 100/250", lambda G: (lambda g: (g, g.src, g.dst))(G.rgg(100, 250, p_range=(0.9, 0.99), seed=3)), 1e-6),
+    ("gnm 50/120", lambda G: (lambda g: (g, g.src, g.dst))(G.gnm(50, 120, p_range=(0.5, 0.95), seed=4)), 1e-9),
+    ("grid 6x7", lambda G: (G.grid(6, 7, p_range=(0.8, 0.99), seed=2), 0, 41), 1e-7),
+    ("gnm 300/1000", lambda G: (lambda g: (g, g.src, g.dst))(G.gnm(300, 1000, p_range=(0.85, 0.99), seed=9)), 1e-5),
+    ("path 1000", lambda G: (G.from_edges(1000, [(i, i + 1) for i in range(999)], [0.999] * 999), 0, 999), 0.0),
+]
+
+
+@pytest.mark.parametrize("name,make,eps", CASES, ids=[c[0] for c in CASES])
+def test_wide_matches_oracle(ctx, oracle, name, make, eps):
+    from relaibilitygpu_gb300 import graphs
+    g, s, t = make(graphs)
+    o = oracle.run(g, s, t, eps=eps, max_nodes=20_000_000)
+    assert o.status == 0
+    r = ctx.reliability(g, s, t, capacity=1 << 22, eps=eps)
+    assert r.engine == "grid"
+    check(r, o)
+
+
+def test_wide_long_path_exact():
+    """A 999-hop path: no 32-node cap (the reference truncates at 32, main.cu:152)."""
+    import relaibilitygpu_gb300 as nr
+    g = nr.from_edges(1000, [(i, i + 1) for i in range(999)], [0.999] * 999)
+    r = nr.reliability(g, 0, 999)
+    prod = 1.0
+    for _ in range(999):
+        prod *= 0.999
+    assert r.R == prod and r.paths == 1 and r.nodes == 1000 and r.dead_ends == 999
+
+
+def test_wide_overflow_brackets(ctx, oracle):
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.complete(40, p=0.5)
+    exact = oracle.run(g, 0, 39, eps=1e-6)
+    r = ctx.reliability(g, 0, 39, capacity=500, eps=1e-6)
+    assert r.spilled > 0
+    assert r.R <= exact.R + 1e-15 and exact.R + exact.esp <= r.R + r.esp + 1e-12
+
+
+def test_wide_rejects_too_many_edges(ctx, engine_lib):
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.complete(47, p=0.5)     # 1081 edges: masks above 64 words
+    with pytest.raises(engine_lib.NrError) as e:
+        ctx.reliability(g, 0, 46)
+    assert e.value.status == -4
