@@ -64,6 +64,13 @@ def workload(name: str):
                     oracle=dict(bucket_shift=2, n_buckets=256, target_width=1e-6),
                     name=f"K15 (N=15, E=105) src=0 dst=14 p~U[0.9,0.99] seeds 0..{BATCH - 1}, "
                          f"max-mass order to ESP width<=1e-6, {BATCH} instances per step")
+    if name in ("k15p05", "k25p05"):
+        n = 15 if name == "k15p05" else 25
+        g = nr.complete(n, p=0.5)
+        return dict(kind="single", graphs=[g], srcs=[0], dsts=[n - 1], capacity=77410924,
+                    opts=dict(eps=1e-15), oracle=dict(eps=1e-15, max_nodes=20_000_000),
+                    name=f"K{n} p=0.5 (COMP{n}-05.txt) src=0 dst={n - 1}, breadth-first waves, queue capacity "
+                         f"77,410,924 per wave buffer, truncation eps 1e-15 (the reference's own published run)")
     if name == "k10":
         g = nr.complete(10, p_range=(0.5, 0.95), seed=2)
         return dict(kind="single", graphs=[g], srcs=[0], dsts=[9], capacity=1 << 22, opts=dict(eps=0.0),
@@ -196,6 +203,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="k15batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batch workloads: use the stored tuned settings instead of running nr_autotune")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -227,7 +236,12 @@ def main():
     batch = nr.Batch(w["graphs"], w["srcs"], w["dsts"])
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     tuned = None
-    if w["kind"] == "batch":
+    if w["kind"] == "batch" and args.no_autotune:
+        tuned = dict(nr.options_dict(nr.make_options(**w["opts"])), bucket_shift=0, n_buckets=64,
+                     warps_per_block=2, pages_per_warp=64)
+        w["opts"] = tuned
+        w["oracle"] = dict(bucket_shift=0, n_buckets=64, target_width=tuned["target_width"])
+    elif w["kind"] == "batch":
         # autotuner (nr_autotune): bucket resolution, pages per warp, warps per block
         tuned, tuned_ms = nr.autotune(ctx, batch, capacity=w["capacity"], **w["opts"])
         w["opts"] = tuned
@@ -276,17 +290,37 @@ def main():
              "iterations": int(r0.iterations), "engine": nr.engine.ENGINES.get(r0.engine, r0.engine),
              "nodes_per_step": nodes // args.steps}
 
-    # single-instance time-to-bound (latency), plain max-mass order
+    # single-instance time-to-bound (latency): plain max-mass order vs the learned order
     ttb = None
     if args.workload == "k15batch":
-        tk, tb = [], []
-        for s in range(16):
-            r = ctx.reliability(w["graphs"][s], 0, 14, **w["opts"])
-            tk.append(r.ms)
-            tb.append(r.time_to_bound_ms)
-        ttb = {"plain_kernel_us_median": 1e3 * statistics.median(tk),
-               "plain_in_kernel_us_median": 1e3 * statistics.median(tb), "learned": None,
-               "instances": 16}
+        from relaibilitygpu_gb300 import learned as LR
+
+        def latency(order, **kw):
+            tk, tb, nd = [], [], []
+            for s in range(16):
+                r = ctx.reliability(w["graphs"][s], 0, 14, order=order,
+                                    **{k: v for k, v in w["opts"].items() if k != "order"}, **kw)
+                tk.append(r.ms)
+                tb.append(r.time_to_bound_ms)
+                nd.append(r.nodes)
+            return {"kernel_us_median": 1e3 * statistics.median(tk),
+                    "in_kernel_us_median": 1e3 * statistics.median(tb),
+                    "nodes_mean": statistics.mean(nd)}
+
+        ttb = {"plain": latency("maxmass"), "learned": None, "instances": 16}
+        if os.path.exists(LR.DEFAULT_MODEL):
+            LR.set_model(ctx, LR.load())
+            ttb["learned"] = latency("learned")
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            lres = ctx.run_batch(batch, capacity=w["capacity"], raw=True,
+                                 **{**w["opts"], "order": "learned"})
+            lnodes = sum(lres[i].nodes for i in range(len(w["graphs"])))
+            ttb["learned_batch"] = {"ms": lres[0].ms, "nodes": lnodes,
+                                    "subproblems_per_sec": lnodes / (lres[0].ms / 1e3)}
+            ttb["plain_batch"] = {"ms": res[0].ms, "nodes": int(sum(r.nodes for r in res))}
+        else:
+            ttb["learned"] = "no model file (python -m relaibilitygpu_gb300.learned train)"
 
     t_dev = dev_ms / 1e3
     # replicas: units add up over ranks, the slowest rank sets the time (no data-path collective)

@@ -177,6 +177,33 @@ int  nr_autotune(nr_context *ctx, int n_instances, const nr_graph *graphs, const
                  const int32_t *dsts, uint64_t capacity, const nr_options *opt, nr_options *best,
                  double *best_ms);
 
+/* ---- learned scorer (no reference counterpart) ------------------------------
+ * An MLP 16 -> 128 -> 128 -> 128 -> 1 (ReLU, sigmoid) estimating a
+ * subproblem's residual reliability from mask features.  NR_ORDER_LEARNED
+ * queues a child in the bucket of (mass x estimate) instead of mass; masses,
+ * R and ESP never depend on it.  Parameters are nr_mlp_param_count() FP32
+ * values: W1[128][16] b1[128] W2[128][128] b2[128] W3[128][128] b3[128]
+ * w4[128] b4. */
+int  nr_mlp_param_count(void);
+int  nr_mlp_init(float *params, uint64_t seed);               /* He-uniform, seeded */
+/* One forward + backward pass over (X[n][16], y[n]) on the GPU: mean binary
+ * cross-entropy in *loss and the gradient (same layout as params) in grads. */
+int  nr_mlp_grad(int device, const float *params, const float *X, const float *y, int n, float *loss, float *grads);
+/* Adam on the GPU (FP32); params in: initial values, out: trained values. */
+int  nr_mlp_train(int device, float *params, const float *X, const float *y, int n, int epochs, int batch,
+                  float lr, float weight_decay, uint64_t seed, float *loss_per_epoch);
+/* Batched inference on tensor cores (BF16 weights, FP32 accumulation). */
+int  nr_mlp_infer(int device, const float *params, const float *X, int n, float *y);
+/* Install parameters on a context for NR_ORDER_LEARNED. */
+int  nr_context_set_model(nr_context *ctx, const float *params);
+/* Run a batch like nr_reliability_batch and record every child the warp
+ * engine queues (16 features, 32 mask words, mass, instance index), up to
+ * max_items; training data for the scorer. */
+int  nr_collect_children(nr_context *ctx, int n_instances, const nr_graph *graphs, const int32_t *srcs,
+                         const int32_t *dsts, uint64_t capacity, const nr_options *opt, uint64_t max_items,
+                         float *feat, uint32_t *masks, double *mass, int32_t *inst, uint64_t *count,
+                         nr_result *results);
+
 /* Solve one instance without allocating device memory (no counterpart in the
  * reference, which allocates its queues with cudaMalloc on every run).
  * For callers that cannot call cudaMalloc -- an application whose device

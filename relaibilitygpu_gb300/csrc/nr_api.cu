@@ -22,6 +22,7 @@
 #include "nr_device.cuh"
 #include "nr_warp.cuh"
 #include "nr_wide.cuh"
+#include "nr_mlp.cuh"
 
 const void *nr_grid_kernel_ptr_g8(int w4);
 const void *nr_grid_kernel_ptr_g16(int w4);
@@ -30,6 +31,10 @@ const void *nr_grid_wide_kernel_ptr(int w4);
 const void *nr_warp_kernel_ptr_g8(int w4);
 const void *nr_warp_kernel_ptr_g16(int w4);
 const void *nr_warp_kernel_ptr_g32(int w4);
+const void *nr_warp_learn_kernel_ptr_g8(int w4);
+const void *nr_warp_learn_kernel_ptr_g16(int w4);
+const void *nr_warp_learn_kernel_ptr_g32(int w4);
+int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
 
 namespace {
 
@@ -59,12 +64,12 @@ const void *grid_kernel(int G, int w4)
     }
 }
 
-const void *warp_kernel(int G, int w4)
+const void *warp_kernel(int G, int w4, bool learn = false)
 {
     switch (G) {
-    case 8: return nr_warp_kernel_ptr_g8(w4);
-    case 16: return nr_warp_kernel_ptr_g16(w4);
-    case 32: return nr_warp_kernel_ptr_g32(w4);
+    case 8: return learn ? nr_warp_learn_kernel_ptr_g8(w4) : nr_warp_kernel_ptr_g8(w4);
+    case 16: return learn ? nr_warp_learn_kernel_ptr_g16(w4) : nr_warp_kernel_ptr_g16(w4);
+    case 32: return learn ? nr_warp_learn_kernel_ptr_g32(w4) : nr_warp_kernel_ptr_g32(w4);
     default: return nullptr;
     }
 }
@@ -200,6 +205,9 @@ struct nr_context {
     size_t hbuf_bytes = 0;
     std::map<std::pair<const void *, size_t>, int> occupancy;   // (kernel, smem) -> blocks per SM
     std::unique_ptr<NrPool> pool;   // host worker threads, created by the first large batch
+    void *model = nullptr;          // learned scorer: FP32 parameters and their BF16 copy
+    NrMlpDev mlp{};
+    bool has_model = false;
     std::mutex mu;
 
     // run fn(i) for i in [0, n): serially for small n, else on the worker pool
@@ -397,6 +405,7 @@ extern "C" void nr_context_destroy(nr_context *c)
     if (c->wslab) cudaFree(c->wslab);
     if (c->wbuf) cudaFree(c->wbuf);
     if (c->hbuf) cudaFreeHost(c->hbuf);
+    if (c->model) cudaFree(c->model);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -675,8 +684,20 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
 // ---------------------------------------------------------------------------
 // warp-per-instance engine (nr_warp.cuh)
 // ---------------------------------------------------------------------------
+struct WarpDump {
+    float *feat;                     // device buffers (nullptr: no dump)
+    uint32_t *mask;
+    double *mass;
+    int *inst;
+    unsigned long long *count;
+    unsigned long long cap;
+    int stride;
+};
+
 struct WarpRunCfg {
     int wave_mode, shift, n_buckets, pages, escalate, warps_per_block;
+    int learned = 0;
+    const WarpDump *dump = nullptr;
     double eps, target;
     unsigned long long max_nodes;
 };
@@ -691,6 +712,7 @@ static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhausti
         w.max_nodes = o->max_nodes ? o->max_nodes : (1ull << 21);
     } else {
         w.wave_mode = 1; w.shift = o->bucket_shift; w.escalate = 0; w.max_nodes = o->max_nodes;
+        w.learned = (o->order == NR_ORDER_LEARNED);
         int nb = o->n_buckets > 0 ? o->n_buckets : 256;
         nb = std::min(1024, (nb + 31) / 32 * 32);
         w.n_buckets = nb;
@@ -797,9 +819,10 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
     for (int k = 0; k < 3 * NR_MAX_W4; ++k) {
         if (!class_count[k]) continue;
         const int G = 8 << (k / NR_MAX_W4), W4 = k % NR_MAX_W4 + 1;
-        const void *kfn = warp_kernel(G, W4);
+        const bool learn = cfg.learned || cfg.dump;
+        const void *kfn = warp_kernel(G, W4, learn);
         if (!kfn) return NR_ERR_UNSUPPORTED;
-        const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfg.pages) * warps_pb;
+        const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfg.pages, learn) * warps_pb;
         auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
         int bps;
         if (it == c->occupancy.end()) {
@@ -847,11 +870,20 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         P.target_fix = nr_fix_of(cfg.target);
         P.max_nodes = cfg.max_nodes;
         P.out = reinterpret_cast<NrWarpOut *>(wb + off_out);
+        P.learned = cfg.learned;
+        P.mlp = c->mlp;
+        P.dump_feat = cfg.dump ? cfg.dump->feat : nullptr;
+        P.dump_mask = cfg.dump ? cfg.dump->mask : nullptr;
+        P.dump_mass = cfg.dump ? cfg.dump->mass : nullptr;
+        P.dump_inst = cfg.dump ? cfg.dump->inst : nullptr;
+        P.dump_count = cfg.dump ? cfg.dump->count : nullptr;
+        P.dump_cap = cfg.dump ? cfg.dump->cap : 0;
+        P.dump_stride = cfg.dump ? cfg.dump->stride : 0;
+        const void *kfn = warp_kernel(G, W4, cfg.learned || cfg.dump);
         void *args[] = {&P};
         // the dynamic shared-memory limit is per-kernel state that another setting may have lowered
-        NR_CUDA_TRY(cudaFuncSetAttribute(warp_kernel(G, W4), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smems[k]));
-        NR_CUDA_TRY(cudaLaunchKernel(warp_kernel(G, W4), dim3(grids[k]), dim3(block), args, smems[k], s));
+        NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smems[k]));
+        NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[k]), dim3(block), args, smems[k], s));
     }
     NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
     NrWarpOut *hout = reinterpret_cast<NrWarpOut *>(hb + off_out);
@@ -893,6 +925,7 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
     if (bad.load() != NR_OK) return bad.load();
     NR_CUDA_TRY(cudaSetDevice(c->device));
     const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
+    if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
     const WarpRunCfg cfg = warp_cfg(&o, capacity, exhaustive);
     std::vector<int> handover;
     int rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover);
@@ -962,6 +995,83 @@ extern "C" int nr_autotune(nr_context *c, int n, const nr_graph *gs, const int32
     return NR_OK;
 }
 
+// Install the learned scorer's parameters (flat FP32, nr_mlp_param_count()
+// floats) on the context; NR_ORDER_LEARNED calls use its BF16 copy.
+extern "C" int nr_context_set_model(nr_context *c, const float *params)
+{
+    if (!c || !params) return NR_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(c->mu);
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    int rc = nr_mlp_upload(params, &c->model, &c->mlp, c->stream);
+    if (rc) return rc;
+    NR_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->has_model = true;
+    return NR_OK;
+}
+
+// Solve a batch with the warp engine (options as nr_reliability_batch) and
+// record every child it queues: features (16 floats), mask words (stride 32),
+// mass and instance index, up to max_items.  *count receives how many were
+// recorded (children past max_items are not recorded).  Training data for the
+// learned scorer.
+extern "C" int nr_collect_children(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs,
+                                   const int32_t *dsts, uint64_t capacity, const nr_options *opt,
+                                   uint64_t max_items, float *feat, uint32_t *masks, double *mass, int32_t *inst,
+                                   uint64_t *count, nr_result *res)
+{
+    if (!c || n <= 0 || !gs || !srcs || !dsts || !feat || !masks || !mass || !inst || !count || !res)
+        return NR_ERR_INVALID;
+    nr_options o;
+    if (opt) o = *opt; else nr_options_default(&o);
+    for (int i = 0; i < n; ++i) {
+        memset(&res[i], 0, sizeof(nr_result));
+        int rc = validate(&gs[i], srcs[i], dsts[i]);
+        if (rc) return rc;
+        if (gs[i].n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lock(c->mu);
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
+    const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
+    WarpRunCfg cfg = warp_cfg(&o, capacity, exhaustive);
+    cfg.escalate = 0;                 // collect from whatever the warp engine reaches
+    const int stride = 32;
+    unsigned char *buf = nullptr;
+    const size_t bytes = max_items * (NR_FEAT * sizeof(float) + stride * sizeof(uint32_t) + sizeof(double) +
+                                      sizeof(int)) + 64;
+    if (cudaMalloc(&buf, bytes) != cudaSuccess) { cudaGetLastError(); return NR_ERR_NOMEM; }
+    WarpDump d;
+    d.count = reinterpret_cast<unsigned long long *>(buf);
+    d.feat = reinterpret_cast<float *>(buf + 64);
+    d.mask = reinterpret_cast<uint32_t *>(d.feat + max_items * NR_FEAT);
+    d.mass = reinterpret_cast<double *>(d.mask + max_items * stride);
+    d.inst = reinterpret_cast<int *>(d.mass + max_items);
+    d.cap = max_items;
+    d.stride = stride;
+    cfg.dump = &d;
+    int rc = NR_OK;
+    unsigned long long got = 0;
+    if (cudaMemsetAsync(buf, 0, 64, c->stream) != cudaSuccess) rc = NR_ERR_CUDA;
+    std::vector<int> handover;
+    if (!rc) rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover);
+    if (!rc) {
+        cudaStream_t s = c->stream;
+        cudaMemcpyAsync(&got, d.count, sizeof(got), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        const unsigned long long k = std::min<unsigned long long>(got, max_items);
+        if (k) {
+            cudaMemcpyAsync(feat, d.feat, k * NR_FEAT * sizeof(float), cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(masks, d.mask, k * stride * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(mass, d.mass, k * sizeof(double), cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(inst, d.inst, k * sizeof(int), cudaMemcpyDeviceToHost, s);
+        }
+        if (cudaStreamSynchronize(s) != cudaSuccess) { cudaGetLastError(); rc = NR_ERR_CUDA; }
+        *count = k;
+    }
+    cudaFree(buf);
+    return rc;
+}
+
 extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int dst, uint64_t capacity,
                                   const nr_options *opt, nr_result *res)
 {
@@ -986,7 +1096,8 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
         return run_grid_wide(c, g, src, dst, capacity, &o, res);
     }
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {
-        // bucketed max-mass order: one warp owns the instance (nr_warp.cuh)
+        // bucketed max-mass (or learned) order: one warp owns the instance (nr_warp.cuh)
+        if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
         const WarpRunCfg cfg = warp_cfg(&o, capacity, false);
         std::vector<int> handover;
         int rc = run_warp_batch(c, 1, g, &src, &dst, cfg, res, &handover);

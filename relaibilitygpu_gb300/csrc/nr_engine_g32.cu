@@ -3,18 +3,19 @@
 #include "nr_grid.cuh"
 #include "nr_warp.cuh"
 
-#define NR_W4_CASES(KERNEL)                              \
+#define NR_W4_CASES(KERNEL, ...)                         \
     switch (w4) {                                        \
-    case 1: return (const void *)KERNEL<32, 1>;           \
-    case 2: return (const void *)KERNEL<32, 2>;           \
-    case 3: return (const void *)KERNEL<32, 3>;           \
-    case 4: return (const void *)KERNEL<32, 4>;           \
-    case 5: return (const void *)KERNEL<32, 5>;           \
-    case 6: return (const void *)KERNEL<32, 6>;           \
-    case 7: return (const void *)KERNEL<32, 7>;           \
-    case 8: return (const void *)KERNEL<32, 8>;           \
+    case 1: return (const void *)KERNEL<32, 1 __VA_ARGS__>;   \
+    case 2: return (const void *)KERNEL<32, 2 __VA_ARGS__>;   \
+    case 3: return (const void *)KERNEL<32, 3 __VA_ARGS__>;   \
+    case 4: return (const void *)KERNEL<32, 4 __VA_ARGS__>;   \
+    case 5: return (const void *)KERNEL<32, 5 __VA_ARGS__>;   \
+    case 6: return (const void *)KERNEL<32, 6 __VA_ARGS__>;   \
+    case 7: return (const void *)KERNEL<32, 7 __VA_ARGS__>;   \
+    case 8: return (const void *)KERNEL<32, 8 __VA_ARGS__>;   \
     default: return nullptr;                             \
     }
 
 const void *nr_grid_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_grid_kernel) }
 const void *nr_warp_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_warp_kernel) }
+const void *nr_warp_learn_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_warp_kernel, , true) }

@@ -50,11 +50,50 @@ __device__ __forceinline__ void nr_acc_zero(NrLaneAcc &a)
 // Every lane of the warp must call this (it uses full-warp shuffles/ballots).
 // On return, a lane with has_child holds one child: words w[] and mass cm.
 // Leaf mass, dead ends and truncation are accumulated on the group's lane 0.
-template <int G, int W4>
+#define NR_FEAT 16
+
+// Features of the child a lane holds, for the learned scorer (nr_mlp.cuh):
+//   0 log2(child mass)/64     1-3 UNKNOWN/up/down edge fractions
+//   4 parent path length / n  5 position of the down edge on the path
+//   6 p of the down edge      7-9 not-down degree of src, dst, and their min
+//                             (a cut-size estimate), over n-1
+//   10 log2(parent mass)/64   11 n/64  12 E/512  13-14 zero  15 one
+template <int W4>
+__device__ __forceinline__ void nr_child_features(float (&f)[NR_FEAT], const uint32_t (&w)[4 * W4], double cm,
+                                                  double mass, int L, int h, double pe, int deg_s, int deg_d,
+                                                  int n, int E)
+{
+    int unk = 0, up = 0;
+#pragma unroll
+    for (int k = 0; k < 4 * W4; ++k) {
+        const uint32_t lo = w[k] & 0x55555555u, hi = (w[k] >> 1) & 0x55555555u;
+        unk += __popc(lo & hi);
+        up += __popc(lo & ~hi);
+    }
+    const float inv_e = E > 0 ? 1.f / (float)E : 0.f, inv_n1 = n > 1 ? 1.f / (float)(n - 1) : 0.f;
+    f[0] = cm > 0.0 ? log2f((float)cm) * (1.f / 64.f) : -16.f;
+    f[1] = unk * inv_e;
+    f[2] = up * inv_e;
+    f[3] = (E - unk - up) * inv_e;
+    f[4] = n > 0 ? (float)L / (float)n : 0.f;
+    f[5] = L > 0 ? (float)(h + 1) / (float)L : 0.f;
+    f[6] = (float)pe;
+    f[7] = deg_s * inv_n1;
+    f[8] = deg_d * inv_n1;
+    f[9] = min(deg_s, deg_d) * inv_n1;
+    f[10] = mass > 0.0 ? log2f((float)mass) * (1.f / 64.f) : -16.f;
+    f[11] = n * (1.f / 64.f);
+    f[12] = E * (1.f / 512.f);
+    f[13] = 0.f;
+    f[14] = 0.f;
+    f[15] = 1.f;
+}
+
+template <int G, int W4, bool FEAT = false>
 __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGraph &sg,
                                           const uint32_t *my_m, bool valid, double mass, double eps,
                                           bool &has_child, uint32_t (&w)[4 * W4], double &cm,
-                                          NrLaneAcc &acc)
+                                          NrLaneAcc &acc, float (*feat)[NR_FEAT] = nullptr)
 {
     constexpr int NW = 4 * W4;
     const int lane = threadIdx.x & 31;
@@ -76,11 +115,18 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
     uint32_t row = 0;
     if (active && v < n) {
         const int lo = sg.start[v], hi = sg.start[v + 1];
-        for (int j = lo; j < hi; ++j) {
-            const uint32_t ent = sg.list[j];
-            const int e = (int)(ent >> 8);
-            const uint32_t word = my_m[e >> 4];
-            row |= ((word >> ((e & 15) << 1)) & 1u) << (ent & 31u);
+        int j = lo;
+        for (; j + 4 <= hi; j += 4) {          // four independent in-arcs per trip
+            const uint32_t a0 = sg.list[j], a1 = sg.list[j + 1], a2 = sg.list[j + 2], a3 = sg.list[j + 3];
+            const uint32_t m0 = my_m[a0 >> 12], m1 = my_m[a1 >> 12], m2 = my_m[a2 >> 12], m3 = my_m[a3 >> 12];
+            row |= ((m0 >> ((a0 >> 7) & 30u)) & 1u) << (a0 & 31u);
+            row |= ((m1 >> ((a1 >> 7) & 30u)) & 1u) << (a1 & 31u);
+            row |= ((m2 >> ((a2 >> 7) & 30u)) & 1u) << (a2 & 31u);
+            row |= ((m3 >> ((a3 >> 7) & 30u)) & 1u) << (a3 & 31u);
+        }
+        for (; j < hi; ++j) {
+            const uint32_t a = sg.list[j];
+            row |= ((my_m[a >> 12] >> ((a >> 7) & 30u)) & 1u) << (a & 31u);
         }
     }
 
@@ -149,6 +195,16 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
 #pragma unroll
             for (int k = 0; k < NW; ++k)
                 if (k == wi) w[k] &= ~bits;
+        }
+    }
+    if constexpr (FEAT) {
+        // not-down degrees of src and dst in the child (the parent's rows minus the down edge)
+        const uint32_t rs = __shfl_sync(NR_FULL, row, gbase + src);
+        const uint32_t rd = __shfl_sync(NR_FULL, row, gbase + dst);
+        if (has_child) {
+            const int ds = __popc(rs) - ((hop_u == src || hop_v == src) ? 1 : 0);
+            const int dd = __popc(rd) - ((hop_u == dst || hop_v == dst) ? 1 : 0);
+            nr_child_features<W4>(*feat, w, cm, mass, L, v, sg.p[e_h], ds, dd, n, g.e);
         }
     }
 }

@@ -21,6 +21,7 @@
 #pragma once
 
 #include "nr_expand.cuh"
+#include "nr_mlp.cuh"
 
 #define NR_WARP_BLOCK 128        // default block: 4 warps
 #define NR_WARP_BLOCK_MAX 256    // largest block the warp kernels are compiled for
@@ -52,6 +53,16 @@ struct NrWarpParams {
     NrFix target_fix;                // the same target as an exact fixed-point number
     unsigned long long max_nodes;    // pop budget: page mode hands over, wave mode stops (0 = none)
     NrWarpOut *out;
+    // learned variant only (nr_warp_kernel<G, W4, true>)
+    int learned;                     // 1: bucket key = child mass x scorer output
+    NrMlpDev mlp;
+    float *dump_feat;                // optional: every child's features ...
+    uint32_t *dump_mask;             // ... mask words (dump_stride words each) ...
+    double *dump_mass;               // ... mass ...
+    int *dump_inst;                  // ... and instance index
+    unsigned long long *dump_count;
+    unsigned long long dump_cap;
+    int dump_stride;
 };
 
 __device__ __forceinline__ int nr_bucket(double m, int shift, int nb)
@@ -81,9 +92,10 @@ struct NrWarpShm {
     short *freel;        // [pages]
 };
 
-__host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets, int pages)
+__host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets, int pages, bool learn = false)
 {
-    size_t b = (size_t)K * 4 * W4 * 4;
+    size_t b = learn ? (size_t)(NR_MLP_WARP_WORDS + 16) * 4 : 0;   // scorer scratch + outputs
+    b += (size_t)K * 4 * W4 * 4;
     b += (size_t)n_buckets * 2;
     b = (b + 3) & ~size_t(3);
     b += (size_t)(n_buckets / 32) * 4;
@@ -94,7 +106,7 @@ __host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets
     return (b + 15) & ~size_t(15);
 }
 
-template <int G, int W4>
+template <int G, int W4, bool LEARN = false>
 __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX) nr_warp_kernel(NrWarpParams P)
 {
     constexpr int K = 32 / G;
@@ -107,9 +119,16 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX) nr_warp_kernel(NrWarpParams
     const int NB = P.n_buckets, NP = P.pages;
 
     NrWarpShm sh;
+    uint32_t *mlp_scratch = nullptr;
+    float *mlp_y = nullptr;
     {
-        unsigned char *b = smem + (size_t)warp * nr_warp_shm_bytes(K, W4, NB, NP);
+        unsigned char *b = smem + (size_t)warp * nr_warp_shm_bytes(K, W4, NB, NP, LEARN);
         size_t o = 0;
+        if (LEARN) {
+            mlp_scratch = reinterpret_cast<uint32_t *>(b);
+            mlp_y = reinterpret_cast<float *>(b + (size_t)NR_MLP_WARP_WORDS * 4);
+            o = (size_t)(NR_MLP_WARP_WORDS + 16) * 4;
+        }
         sh.masks = reinterpret_cast<uint32_t *>(b + o); o += (size_t)K * NW * 4;
         sh.heads = reinterpret_cast<short *>(b + o); o += (size_t)NB * 2; o = (o + 3) & ~size_t(3);
         sh.bitmap = reinterpret_cast<uint32_t *>(b + o); o += (size_t)(NB / 32) * 4;
@@ -221,8 +240,38 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX) nr_warp_kernel(NrWarpParams
                     bool has_child;
                     uint32_t w[NW];
                     double cm;
-                    nr_expand<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
-                    const int cb = has_child ? nr_bucket(cm, P.shift, NB) : 0;
+                    float feat[NR_FEAT];
+                    nr_expand<G, W4, LEARN>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc,
+                                            LEARN ? &feat : nullptr);
+                    double key = cm;
+                    if constexpr (LEARN) {
+                        const unsigned cbm = __ballot_sync(NR_FULL, has_child);
+                        if (P.dump_feat && has_child) {     // training data: the child as it is queued
+                            const unsigned long long d = atomicAdd(P.dump_count, 1ull);
+                            if (d < P.dump_cap) {
+#pragma unroll
+                                for (int k = 0; k < NR_FEAT; ++k) P.dump_feat[d * NR_FEAT + k] = feat[k];
+#pragma unroll
+                                for (int k = 0; k < NW; ++k) P.dump_mask[d * P.dump_stride + k] = w[k];
+                                P.dump_mass[d] = cm;
+                                P.dump_inst[d] = P.inst_id[ii];
+                            }
+                        }
+                        if (P.learned && cbm) {             // score this step's children, 16 per tile
+                            const int nch = __popc(cbm), rank = __popc(cbm & lt_mask);
+                            for (int t = 0; t * 16 < nch; ++t) {
+                                if (has_child && rank / 16 == t) {
+#pragma unroll
+                                    for (int k = 0; k < NR_FEAT / 2; ++k)
+                                        mlp_scratch[(rank % 16) * 8 + k] = nr_pack_bf16(feat[2 * k], feat[2 * k + 1]);
+                                }
+                                nr_mlp_warp_infer(P.mlp, mlp_scratch, mlp_y);
+                                if (has_child && rank / 16 == t) key = cm * (double)mlp_y[rank % 16];
+                                __syncwarp();
+                            }
+                        }
+                    }
+                    const int cb = has_child ? nr_bucket(key, P.shift, NB) : 0;
 
                     unsigned pend = __ballot_sync(NR_FULL, has_child);
                     while (pend) {

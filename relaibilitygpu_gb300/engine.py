@@ -72,6 +72,8 @@ EXPORTS = [
     "nr_options_default", "nr_status_string", "nr_abi_version", "nr_graph_load", "nr_graph_free",
     "nr_initial_mask", "nr_context_create", "nr_context_destroy", "nr_reliability", "nr_reliability_ctx",
     "nr_reliability_batch", "nr_format_result", "nr_reliability_noalloc", "nr_autotune",
+    "nr_mlp_param_count", "nr_mlp_init", "nr_mlp_grad", "nr_mlp_train", "nr_mlp_infer", "nr_context_set_model",
+    "nr_collect_children",
 ]
 
 _lib_handle: Optional[C.CDLL] = None
@@ -116,6 +118,23 @@ def lib() -> C.CDLL:
     L.nr_autotune.argtypes = [C.c_void_p, C.c_int, C.POINTER(NrGraph), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                               C.c_uint64, C.POINTER(NrOptions), C.POINTER(NrOptions), C.POINTER(C.c_double)]
     L.nr_autotune.restype = C.c_int
+    fp = C.POINTER(C.c_float)
+    L.nr_mlp_param_count.restype = C.c_int
+    L.nr_mlp_init.argtypes = [fp, C.c_uint64]
+    L.nr_mlp_init.restype = C.c_int
+    L.nr_mlp_grad.argtypes = [C.c_int, fp, fp, fp, C.c_int, fp, fp]
+    L.nr_mlp_grad.restype = C.c_int
+    L.nr_mlp_train.argtypes = [C.c_int, fp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint64, fp]
+    L.nr_mlp_train.restype = C.c_int
+    L.nr_mlp_infer.argtypes = [C.c_int, fp, fp, C.c_int, fp]
+    L.nr_mlp_infer.restype = C.c_int
+    L.nr_context_set_model.argtypes = [C.c_void_p, fp]
+    L.nr_context_set_model.restype = C.c_int
+    L.nr_collect_children.argtypes = [C.c_void_p, C.c_int, C.POINTER(NrGraph), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int32), C.c_uint64, C.POINTER(NrOptions), C.c_uint64, fp,
+                                      C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_uint64), C.POINTER(NrResult)]
+    L.nr_collect_children.restype = C.c_int
     L.nr_format_result.argtypes = [C.POINTER(NrResult), C.c_char_p, C.c_size_t]
     L.nr_format_result.restype = C.c_int
     _lib_handle = L

@@ -1,0 +1,84 @@
+"""The learned scorer on the GPU: gradients, inference, training, and its use as a
+queue priority (which must leave R and ESP exact and rigorous)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def L(engine_lib):
+    from relaibilitygpu_gb300 import learned
+    return learned
+
+
+def test_gradients_match_fp64_reference(L):
+    rng = np.random.default_rng(5)
+    p = L.init_params(7)
+    X = rng.random((300, 16)).astype(np.float32)
+    y = rng.random(300).astype(np.float32)
+    loss, g = L.gpu_grad(p, X, y)
+    rloss, rg = L.ref_grad(p, X, y)
+    assert abs(loss - rloss) <= 1e-5 * max(1.0, abs(rloss))
+    rel = np.abs(g - rg) / (np.abs(rg) + 1e-6 * np.abs(rg).max())
+    assert np.median(rel) < 1e-4
+    assert np.max(np.abs(g - rg)) <= 2e-4 * np.abs(rg).max()
+
+
+def test_tensor_core_inference_matches_bf16_reference(L):
+    rng = np.random.default_rng(6)
+    p = L.init_params(9) * 0.6
+    X = rng.random((1000, 16)).astype(np.float32)
+    y = L.gpu_infer(p, X)
+    ref = L.ref_forward(p, X, bf16=True)
+    assert np.max(np.abs(y - ref)) < 5e-3
+    assert np.max(np.abs(y - L.ref_forward(p, X))) < 5e-2
+
+
+def test_training_reduces_loss(L):
+    rng = np.random.default_rng(1)
+    X = rng.random((4096, 16)).astype(np.float32)
+    y = (1 / (1 + np.exp(-(X[:, 0] * 4 - 2 + X[:, 3])))).astype(np.float32)
+    p0 = L.init_params(2)
+    p, losses = L.gpu_train(p0, X, y, epochs=15, batch=256, lr=2e-3, seed=4)
+    assert losses[-1] < losses[0]
+    l0, _ = L.ref_grad(p0, X, y)
+    l1, _ = L.ref_grad(p, X, y)
+    assert l1 < l0
+
+
+def test_collect_and_label_children(L, engine_lib, oracle):
+    from relaibilitygpu_gb300 import graphs
+    gs = [graphs.complete(8, p_range=(0.5, 0.95), seed=s) for s in range(4)]
+    with engine_lib.Context(0) as ctx:
+        feat, masks, mass, inst = L.collect(ctx, gs, [0] * 4, [7] * 4, 4000, order="maxmass")
+        assert len(feat) > 100 and np.all((inst >= 0) & (inst < 4))
+        assert np.all(feat[:, 15] == 1.0) and np.all((feat[:, 1] >= 0) & (feat[:, 1] <= 1))
+        lab = L.label(ctx, gs, [0] * 4, [7] * 4, masks[:200], inst[:200], exact=True)
+    for k in range(0, 200, 17):
+        sub = L.subproblem_graph(gs[inst[k]], masks[k])
+        assert lab[k] == oracle.run(sub, 0, 7).R
+
+
+def test_learned_order_is_exact_and_rigorous(L, engine_lib, oracle, golden, load_golden_graph):
+    """Any scorer only changes the order: exhaustive results equal the plain ones, and truncated
+    results keep R <= exact <= R + ESP with ESP <= target."""
+    p = L.init_params(11)
+    with engine_lib.Context(0) as ctx:
+        L.set_model(ctx, p)
+        g = load_golden_graph("COMP8")
+        r = ctx.reliability(g, 0, 7, order="learned", capacity=1 << 16)
+        assert r.paths == 26830 and r.nodes == 53660 and r.R == oracle.run(g, 0, 7).R
+        g9 = load_golden_graph("COMP9")
+        exact = golden["published"]["COMP9"]["R"]
+        for t in (1e-3, 1e-5):
+            r = ctx.reliability(g9, 0, 8, order="learned", target_width=t, capacity=1 << 18)
+            assert r.stop == 1 and r.esp <= t
+            assert r.R <= exact + 1e-15 <= r.R + r.esp + 2e-15
+
+
+def test_learned_order_needs_a_model(engine_lib):
+    from relaibilitygpu_gb300 import graphs
+    with engine_lib.Context(0) as ctx:
+        with pytest.raises(engine_lib.NrError):
+            ctx.reliability(graphs.complete(6, p=0.5), 0, 5, order="learned")
