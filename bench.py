@@ -295,11 +295,15 @@ def main():
     if args.workload == "k15batch":
         from relaibilitygpu_gb300 import learned as LR
 
+        # the order comparison runs at one bucket resolution (one bucket per factor of two), since
+        # with a single bucket (breadth-first waves) there is nothing for a priority to reorder
+        cmp_opts = {k: v for k, v in w["opts"].items() if k not in ("order", "bucket_shift", "n_buckets")}
+        cmp_opts.update(bucket_shift=0, n_buckets=64)
+
         def latency(order, **kw):
             tk, tb, nd = [], [], []
             for s in range(16):
-                r = ctx.reliability(w["graphs"][s], 0, 14, order=order,
-                                    **{k: v for k, v in w["opts"].items() if k != "order"}, **kw)
+                r = ctx.reliability(w["graphs"][s], 0, 14, order=order, **{**cmp_opts, **kw})
                 tk.append(r.ms)
                 tb.append(r.time_to_bound_ms)
                 nd.append(r.nodes)
@@ -307,19 +311,24 @@ def main():
                     "in_kernel_us_median": 1e3 * statistics.median(tb),
                     "nodes_mean": statistics.mean(nd)}
 
-        ttb = {"plain": latency("maxmass"), "learned": None, "instances": 16}
-        if os.path.exists(LR.DEFAULT_MODEL):
-            LR.set_model(ctx, LR.load())
-            ttb["learned"] = latency("learned")
+        def batch_run(order):
             flush.fill_(1.0)
             torch.cuda.synchronize()
-            lres = ctx.run_batch(batch, capacity=w["capacity"], raw=True,
-                                 **{**w["opts"], "order": "learned"})
-            lnodes = sum(lres[i].nodes for i in range(len(w["graphs"])))
-            ttb["learned_batch"] = {"ms": lres[0].ms, "nodes": lnodes,
-                                    "subproblems_per_sec": lnodes / (lres[0].ms / 1e3)}
-            ttb["plain_batch"] = {"ms": res[0].ms, "nodes": int(sum(r.nodes for r in res))}
-        else:
+            rr = ctx.run_batch(batch, capacity=w["capacity"], raw=True, order=order, **cmp_opts)
+            nn = sum(rr[i].nodes for i in range(len(w["graphs"])))
+            return {"ms": rr[0].ms, "nodes": nn, "subproblems_per_sec": nn / (rr[0].ms / 1e3)}
+
+        try:
+            ttb = {"plain": latency("maxmass"), "learned": None, "instances": 16,
+                   "breadth_first": latency("maxmass", bucket_shift=-1),
+                   "plain_batch": batch_run("maxmass")}
+        except Exception as exc:                     # keep the bench line; report the failure
+            ttb = {"plain": f"failed: {exc}", "learned": None, "instances": 16}
+        if os.path.exists(LR.DEFAULT_MODEL) and isinstance(ttb["plain"], dict):
+            LR.set_model(ctx, LR.load())
+            ttb["learned"] = latency("learned")
+            ttb["learned_batch"] = batch_run("learned")
+        elif not os.path.exists(LR.DEFAULT_MODEL):
             ttb["learned"] = "no model file (python -m relaibilitygpu_gb300.learned train)"
 
     t_dev = dev_ms / 1e3

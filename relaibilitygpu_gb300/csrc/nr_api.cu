@@ -42,16 +42,17 @@ namespace {
     do {                                                                      \
         cudaError_t _e = (call);                                              \
         if (_e != cudaSuccess) {                                              \
-            nr_last_cuda_error(_e);                                           \
+            nr_last_cuda_error(_e, __LINE__, #call);                          \
             return NR_ERR_CUDA;                                               \
         }                                                                     \
     } while (0)
 
 thread_local char g_err[256];
 
-void nr_last_cuda_error(cudaError_t e)
+// keep the failing call and its line for nr_status_string
+void nr_last_cuda_error(cudaError_t e, int line, const char *what)
 {
-    snprintf(g_err, sizeof(g_err), "%s", cudaGetErrorString(e));
+    snprintf(g_err, sizeof(g_err), "%s (nr_api.cu:%d %.120s)", cudaGetErrorString(e), line, what);
 }
 
 const void *grid_kernel(int G, int w4)
@@ -205,6 +206,7 @@ struct nr_context {
     size_t hbuf_bytes = 0;
     std::map<std::pair<const void *, size_t>, int> occupancy;   // (kernel, smem) -> blocks per SM
     std::unique_ptr<NrPool> pool;   // host worker threads, created by the first large batch
+    int smem_optin = 0;             // largest dynamic shared memory a block may opt in to
     void *model = nullptr;          // learned scorer: FP32 parameters and their BF16 copy
     NrMlpDev mlp{};
     bool has_model = false;
@@ -387,7 +389,7 @@ extern "C" int nr_context_create(int device, nr_context **out)
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e != cudaSuccess) {
-        nr_last_cuda_error(e);
+        nr_last_cuda_error(e, __LINE__, "context set-up");
         nr_context_destroy(c);
         return NR_ERR_CUDA;
     }
@@ -813,6 +815,17 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
 
     // launch geometry per class (occupancy cached per kernel and shared-memory size)
     const int warps_pb = cfg.warps_per_block, block = 32 * warps_pb;
+    if (!c->smem_optin) {
+        int v = 0;
+        NR_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+        c->smem_optin = v;
+    }
+    // pages per warp: as asked, but no more than the block's shared memory can index
+    WarpRunCfg cfgv = cfg;
+    while (cfgv.pages > 4 &&
+           nr_warp_shm_bytes(4, NR_MAX_W4, cfgv.n_buckets, cfgv.pages, true) * warps_pb > (size_t)c->smem_optin)
+        cfgv.pages /= 2;
+    const WarpRunCfg &cfgp = cfgv;
     int grids[3 * NR_MAX_W4] = {0};
     size_t smems[3 * NR_MAX_W4] = {0};
     size_t slab_need = 0;
@@ -822,7 +835,7 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         const bool learn = cfg.learned || cfg.dump;
         const void *kfn = warp_kernel(G, W4, learn);
         if (!kfn) return NR_ERR_UNSUPPORTED;
-        const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfg.pages, learn) * warps_pb;
+        const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn) * warps_pb;
         auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
         int bps;
         if (it == c->occupancy.end()) {
@@ -836,7 +849,7 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         const int grid = std::max(1, std::min(bps * c->sms, (class_count[k] + warps_pb - 1) / warps_pb));
         grids[k] = grid;
         smems[k] = smem;
-        slab_need = std::max(slab_need, (size_t)grid * warps_pb * cfg.pages * NR_PAGE * (16 * (size_t)W4 + 8));
+        slab_need = std::max(slab_need, (size_t)grid * warps_pb * cfgp.pages * NR_PAGE * (16 * (size_t)W4 + 8));
     }
     rc = ensure(&c->wslab, &c->wslab_bytes, slab_need);
     if (rc) return rc;
@@ -859,8 +872,8 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         P.slab_mask = static_cast<uint4 *>(c->wslab);
         const size_t warps = (size_t)grids[k] * warps_pb;
         P.slab_mass = reinterpret_cast<double *>(static_cast<unsigned char *>(c->wslab) +
-                                                 warps * cfg.pages * NR_PAGE * 16 * (size_t)W4);
-        P.pages = cfg.pages;
+                                                 warps * cfgp.pages * NR_PAGE * 16 * (size_t)W4);
+        P.pages = cfgp.pages;
         P.n_buckets = cfg.n_buckets;
         P.shift = cfg.shift;
         P.wave_mode = cfg.wave_mode;
@@ -896,7 +909,7 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
         if (hout[i].status == 2) { handover->push_back(i); continue; }
-        fill_from_warp(hout[i], cfg, desc[i].w4, r);
+        fill_from_warp(hout[i], cfgp, desc[i].w4, r);
         r->ms = ms;
         r->grid_blocks = first_grid;
         r->block_threads = block;
@@ -1086,14 +1099,13 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     res->src = src;
     res->dst = dst;
     res->mask_words = std::max(1, (2 * g->n_edges + 31) / 32);
-    if (capacity == 0) capacity = 1u << 20;   // reference default (common.h:33)
     std::lock_guard<std::mutex> lock(c->mu);
     NR_CUDA_TRY(cudaSetDevice(c->device));
     if (g->n_nodes > NR_SMALL_MAX_N) {
         // 33..1024 nodes: whole-GPU wave engine (max-mass order and target widths are n <= 32 only)
         if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED)
             return NR_ERR_UNSUPPORTED;
-        return run_grid_wide(c, g, src, dst, capacity, &o, res);
+        return run_grid_wide(c, g, src, dst, capacity ? capacity : (1u << 20), &o, res);
     }
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {
         // bucketed max-mass (or learned) order: one warp owns the instance (nr_warp.cuh)
@@ -1105,7 +1117,8 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
         if (!handover.empty()) return NR_ERR_INTERNAL;
         return NR_OK;
     }
-    return run_grid_small(c, g, src, dst, capacity, &o, res);
+    // the wave engine's queue: the reference default capacity (common.h:33) when none is given
+    return run_grid_small(c, g, src, dst, capacity ? capacity : (1u << 20), &o, res);
 }
 
 extern "C" int nr_reliability(const nr_graph *g, int src, int dst, uint64_t capacity, const nr_options *opt,

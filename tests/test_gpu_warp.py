@@ -186,3 +186,16 @@ def test_large_batch_host_pool(ctx, oracle):
                                 n_buckets=128)
     for i in range(0, 3000, 97):
         check_wave_parity(res[i], oracle.run(gs[i], 0, 8, bucket_shift=1, n_buckets=128, target_width=1e-6))
+
+
+@pytest.mark.parametrize("wpb", [1, 4, 8])
+def test_single_instance_any_block_size(ctx, oracle, wpb):
+    """Single-instance calls with no capacity use the warp engine's own page default, for every block size."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.complete(15, p_range=(0.9, 0.99), seed=44)
+    for shift in (-1, 0):
+        r = ctx.reliability(g, 0, 14, target_width=1e-6, bucket_shift=shift, n_buckets=64, warps_per_block=wpb)
+        o = oracle.run(g, 0, 14, bucket_shift=shift, n_buckets=64 if shift >= 0 else 1, target_width=1e-6)
+        check_wave_parity(r, o)
+    r = ctx.reliability(g, 0, 14, target_width=1e-6, warps_per_block=wpb, pages_per_warp=8192)
+    assert r.stop == 1
