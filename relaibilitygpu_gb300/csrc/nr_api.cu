@@ -3,8 +3,11 @@
 // Replaces the reference driver (workingPad/main.cu:795-1072) and its graph
 // loader (workingPad/graph.h:46-178) with calls that return status codes.
 
+#include <sched.h>
+
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -84,6 +87,32 @@ int group_width(int n)
 
 size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
+// NR_PROFILE=1 in the environment: host phase timings of batch calls on stderr
+struct PhaseClock {
+    bool on;
+    std::chrono::steady_clock::time_point t0, last;
+    char buf[512];
+    int len = 0;
+    PhaseClock() : on(getenv("NR_PROFILE") != nullptr)
+    {
+        t0 = last = std::chrono::steady_clock::now();
+        buf[0] = 0;
+    }
+    void mark(const char *name)
+    {
+        if (!on) return;
+        const auto t = std::chrono::steady_clock::now();
+        len += snprintf(buf + len, sizeof(buf) - len, " %s=%.1fus", name,
+                        std::chrono::duration<double, std::micro>(t - last).count());
+        last = t;
+    }
+    ~PhaseClock()
+    {
+        if (on) fprintf(stderr, "[nr profile]%s total=%.1fus\n", buf,
+                        std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count());
+    }
+};
+
 }  // namespace
 
 // Correctly rounded (to nearest, ties to even) value of a 192-bit fixed-point sum.
@@ -119,74 +148,126 @@ NrFix nr_fix_from_double_host(double m) { return nr_fix_of(m); }
 void nr_fix_add_host(NrFix &a, const NrFix &b) { nr_fix_add(a, b); }
 
 // Worker threads kept by a context for the host side of batch calls (table
-// building and validation), so a call does not pay for thread creation.
+// building and validation), so a call does not pay for thread creation.  A
+// batch call runs several short jobs back to back: between jobs the workers
+// (and the caller waiting for a job's end) poll for up to kSpin before they
+// block, so a job does not wait for threads to be woken from sleep.
 class NrPool {
 public:
     explicit NrPool(int workers)
     {
-        for (int i = 0; i < workers; ++i) th_.emplace_back([this] { loop(); });
+        for (int i = 0; i < workers; ++i) th_.emplace_back([this, i] { loop(i); });
     }
     ~NrPool()
     {
         {
             std::lock_guard<std::mutex> l(mu_);
             quit_ = true;
+            gen_.fetch_add(1, std::memory_order_release);
         }
         cv_.notify_all();
         for (auto &t : th_) t.join();
     }
     int size() const { return (int)th_.size() + 1; }
-    // run fn(i) for i in [0, n) on the workers and the calling thread
-    void run(int n, const std::function<void(int)> &fn)
+    // run fn(i) for i in [0, n) on the calling thread and `helpers` workers; the
+    // threads take `grain` consecutive indices at a time
+    void run(int n, int helpers, int grain, const std::function<void(int)> &fn)
     {
+        helpers = std::max(0, std::min(helpers, (int)th_.size()));
+        if (helpers == 0) {
+            for (int i = 0; i < n; ++i) fn(i);
+            return;
+        }
         {
             std::lock_guard<std::mutex> l(mu_);
             fn_ = &fn;
             n_ = n;
-            next_.store(0);
-            busy_ = (int)th_.size();
-            ++gen_;
+            grain_ = std::max(1, grain);
+            helpers_ = helpers;
+            next_.store(0, std::memory_order_relaxed);
+            busy_.store(helpers, std::memory_order_relaxed);
+            gen_.fetch_add(1, std::memory_order_release);
         }
         cv_.notify_all();
         work();
-        std::unique_lock<std::mutex> l(mu_);
-        done_.wait(l, [this] { return busy_ == 0; });
+        const auto t0 = std::chrono::steady_clock::now();
+        while (busy_.load(std::memory_order_acquire) != 0) {
+            if (std::chrono::steady_clock::now() - t0 > kSpin) {
+                std::unique_lock<std::mutex> l(mu_);
+                done_.wait(l, [this] { return busy_.load(std::memory_order_acquire) == 0; });
+                break;
+            }
+            std::this_thread::yield();
+        }
+        std::lock_guard<std::mutex> l(mu_);
         fn_ = nullptr;
     }
 
 private:
+    static constexpr std::chrono::microseconds kSpin{300};
     void work()
     {
         for (;;) {
-            const int b = next_.fetch_add(32);
+            const int b = next_.fetch_add(grain_);
             if (b >= n_) break;
-            const int e = std::min(n_, b + 32);
+            const int e = std::min(n_, b + grain_);
             for (int i = b; i < e; ++i) (*fn_)(i);
         }
     }
-    void loop()
+    void loop(int id)
     {
         unsigned long long seen = 0;
         for (;;) {
+            const auto t0 = std::chrono::steady_clock::now();
+            while (gen_.load(std::memory_order_acquire) == seen &&
+                   std::chrono::steady_clock::now() - t0 < kSpin)
+                std::this_thread::yield();
+            int helpers;
             {
                 std::unique_lock<std::mutex> l(mu_);
-                cv_.wait(l, [&] { return quit_ || gen_ != seen; });
+                cv_.wait(l, [&] { return gen_.load(std::memory_order_relaxed) != seen; });
                 if (quit_) return;
-                seen = gen_;
+                seen = gen_.load(std::memory_order_relaxed);
+                helpers = helpers_;
             }
+            if (id >= helpers) continue;       // not a helper of this job
             work();
-            std::lock_guard<std::mutex> l(mu_);
-            if (--busy_ == 0) done_.notify_one();
+            if (busy_.fetch_sub(1, std::memory_order_acq_rel) == 1) {
+                std::lock_guard<std::mutex> l(mu_);
+                done_.notify_one();
+            }
         }
     }
     std::vector<std::thread> th_;
     std::mutex mu_;
     std::condition_variable cv_, done_;
     const std::function<void(int)> *fn_ = nullptr;
-    int n_ = 0, busy_ = 0;
-    std::atomic<int> next_{0};
-    unsigned long long gen_ = 0;
+    int n_ = 0, grain_ = 1, helpers_ = 0;
+    std::atomic<int> next_{0}, busy_{0};
+    std::atomic<unsigned long long> gen_{0};
     bool quit_ = false;
+};
+
+// One host block of a batch call (a contiguous instance range): table bytes,
+// instances per class, and where its tables and descriptors go.
+#define NR_HOST_BLOCKS 64
+struct NrHostBlock {
+    size_t bytes;               // tables of the block's instances (16-byte multiples)
+    long long last_owner_rel;   // offset in the block of its last structural part, -1 if none
+    size_t base;                // offset of the block's tables in the staging buffer
+    long long struct_in;        // struct_off of the last structural part before the block
+    int cnt[3 * NR_MAX_W4];     // instances per class
+    int cbase[3 * NR_MAX_W4];   // instances of each class in earlier blocks
+};
+
+// Host-side per-instance tables of a batch call, kept by the context so their
+// memory is reused from call to call.
+struct NrBatchScratch {
+    std::vector<NrSmallGraph> desc;
+    std::vector<int> cls;
+    std::vector<unsigned char> same_prev;
+    std::vector<size_t> inst_b, struct_b;
+    std::vector<NrHostBlock> blk;
 };
 
 struct nr_context {
@@ -206,13 +287,15 @@ struct nr_context {
     size_t hbuf_bytes = 0;
     std::map<std::pair<const void *, size_t>, int> occupancy;   // (kernel, smem) -> blocks per SM
     std::unique_ptr<NrPool> pool;   // host worker threads, created by the first large batch
+    NrBatchScratch scratch;         // per-instance host tables of the last batch call (reused)
     int smem_optin = 0;             // largest dynamic shared memory a block may opt in to
     void *model = nullptr;          // learned scorer: FP32 parameters and their BF16 copy
     NrMlpDev mlp{};
     bool has_model = false;
     std::mutex mu;
 
-    // run fn(i) for i in [0, n): serially for small n, else on the worker pool
+    // run fn(i) for i in [0, n): serially when n < 2 * min_per_thread, else on the
+    // worker pool with at most one thread per min_per_thread indices
     void parallel_for(int n, int min_per_thread, const std::function<void(int)> &fn)
     {
         if (n < 2 * min_per_thread) {
@@ -220,10 +303,16 @@ struct nr_context {
             return;
         }
         if (!pool) {
-            const int hw = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 32u));
+            // the CPUs this process may run on (a container can get fewer than the machine has)
+            cpu_set_t set;
+            int hw = 0;
+            if (sched_getaffinity(0, sizeof(set), &set) == 0) hw = CPU_COUNT(&set);
+            if (hw <= 0) hw = (int)std::thread::hardware_concurrency();
+            hw = std::max(1, std::min(hw, 32));
             pool.reset(new NrPool(hw - 1));
         }
-        pool->run(n, fn);
+        const int threads = std::min(pool->size(), (n + min_per_thread - 1) / min_per_thread);
+        pool->run(n, threads - 1, std::max(1, std::min(32, n / (8 * threads))), fn);
     }
 };
 
@@ -266,39 +355,43 @@ static int validate(const nr_graph *g, int src, int dst)
 
 static int group_width_of(int n) { return group_width(n); }
 
-// Graph tables of one instance for the small engines (layout in nr_internal.h):
-// small_layout sets the sizes and offsets, small_fill writes the tables.
-static size_t small_layout(const nr_graph *g, int src, int dst, NrSmallGraph *sg)
+// Graph tables of one instance for the small engines (layout in nr_internal.h).
+// Per-instance part: the offset of p from its own base.
+static size_t small_inst_layout(const nr_graph *g, int src, int dst, NrSmallGraph *sg)
 {
     const int n = g->n_nodes, E = g->n_edges;
-    const int G = group_width_of(n);
     const int W = std::max(1, (2 * E + 31) / 32);
     sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst;
     sg->n_in = g->n_arcs;
     size_t off = 0;
     sg->off_p = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
-    sg->off_q = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
-    sg->off_eid = (int)off; off = align16(off + sizeof(uint16_t) * G * G);
-    sg->off_start = (int)off; off = align16(off + sizeof(int) * (n + 1));
-    sg->off_list = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
-    sg->off_root = (int)off; off = align16(off + sizeof(uint32_t) * 4 * sg->w4);
-    sg->blob_bytes = (int)off;
-    sg->blob_off = 0;
     return off;
 }
 
-static void small_fill(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)
+// Structural part: offsets of the edge-id table and in-arc lists from base `at`.
+static size_t small_struct_layout(const nr_graph *g, NrSmallGraph *sg, size_t at)
 {
-    const int n = g->n_nodes, E = g->n_edges;
-    const int G = group_width_of(n);
-    memset(b, 0, sg->blob_bytes);
+    const int n = g->n_nodes, G = group_width_of(n);
+    size_t off = at;
+    sg->off_eid = (int)off; off = align16(off + sizeof(uint16_t) * G * G);
+    sg->off_start = (int)off; off = align16(off + sizeof(int) * (n + 1));
+    sg->off_list = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
+    return off - at;
+}
+
+static void small_fill_inst(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)
+{
+    const int E = g->n_edges;
     double *p = reinterpret_cast<double *>(b + sg->off_p);
-    double *q = reinterpret_cast<double *>(b + sg->off_q);
+    memcpy(p, g->edge_p, sizeof(double) * E);
+}
+
+static void small_fill_struct(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)
+{
+    const int n = g->n_nodes, G = group_width_of(n);
     uint16_t *eid = reinterpret_cast<uint16_t *>(b + sg->off_eid);
     int *start = reinterpret_cast<int *>(b + sg->off_start);
     uint32_t *list = reinterpret_cast<uint32_t *>(b + sg->off_list);
-    uint32_t *root = reinterpret_cast<uint32_t *>(b + sg->off_root);
-    for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
     for (int i = 0; i < G * G; ++i) eid[i] = 0xffff;
     // in-arcs grouped by head node; arc (u -> v) for every CSR entry of u
     int cnt[NR_SMALL_MAX_N + 1] = {0};
@@ -313,11 +406,33 @@ static void small_fill(const nr_graph *g, const NrSmallGraph *sg, unsigned char 
             list[start[v] + fill[v]++] = ((uint32_t)e << 8) | (uint32_t)u;
             if (eid[u * G + v] == 0xffff) eid[u * G + v] = (uint16_t)e;   // first arc u->v in CSR order
         }
-    for (int e = 0; e < E; ++e) {
-        const double pe = g->edge_p[e];
-        const uint32_t st = (pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN;
-        root[e >> 4] |= st << ((e & 15) * 2);
-    }
+}
+
+// Both parts in one blob (whole-GPU engine): struct_off == blob_off.
+static size_t small_layout(const nr_graph *g, int src, int dst, NrSmallGraph *sg)
+{
+    const size_t a = small_inst_layout(g, src, dst, sg);
+    const size_t b = small_struct_layout(g, sg, a);
+    sg->blob_bytes = (int)(a + b);
+    sg->blob_off = 0;
+    sg->struct_off = 0;
+    return a + b;
+}
+
+static void small_fill(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)
+{
+    small_fill_inst(g, sg, b);
+    small_fill_struct(g, sg, b);
+}
+
+// Same topology (CSR and edge ids) as another graph?
+static bool same_topology(const nr_graph *a, const nr_graph *b)
+{
+    if (a->n_nodes != b->n_nodes || a->n_arcs != b->n_arcs || a->n_edges != b->n_edges) return false;
+    const size_t na = (size_t)a->n_arcs;
+    return (a->row_ptr == b->row_ptr || !memcmp(a->row_ptr, b->row_ptr, sizeof(int32_t) * (a->n_nodes + 1))) &&
+           (a->col_idx == b->col_idx || !memcmp(a->col_idx, b->col_idx, sizeof(int32_t) * na)) &&
+           (a->edge_id == b->edge_id || !memcmp(a->edge_id, b->edge_id, sizeof(int32_t) * na));
 }
 
 static void build_small_blob(const nr_graph *g, int src, int dst, NrSmallGraph *sg, std::vector<unsigned char> *blob)
@@ -771,30 +886,70 @@ static int ensure_host(void **buf, size_t *have, size_t need)
 static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
                           const WarpRunCfg &cfg, nr_result *res, std::vector<int> *handover)
 {
-    // layout and class of every instance (class = group width x mask blocks)
-    std::vector<NrSmallGraph> desc(n);
-    std::vector<int> cls(n);
-    int class_count[3 * NR_MAX_W4] = {0};
-    size_t blob_bytes = 0;
-    for (int i = 0; i < n; ++i) {
-        const size_t b = small_layout(&gs[i], srcs[i], dsts[i], &desc[i]);
-        desc[i].blob_off = (long long)blob_bytes;
-        blob_bytes += b;
-        if (desc[i].w4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
-        const int G = group_width(gs[i].n_nodes);
-        cls[i] = (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + desc[i].w4 - 1;
-        class_count[cls[i]]++;
+    PhaseClock pc;
+    constexpr int NCLS = 3 * NR_MAX_W4;      // class = lane-group width x mask blocks
+    NrBatchScratch &S = c->scratch;          // kept by the context: no page faults on every call
+    S.desc.resize(n);
+    S.cls.resize(n);
+    S.same_prev.resize(n);
+    S.inst_b.resize(n);
+    S.struct_b.resize(n);
+    NrSmallGraph *desc = S.desc.data();
+    // Host blocks: contiguous instance ranges, one task of the worker pool each.  Two
+    // parallel passes (sizes, then offsets and tables) around a serial prefix over blocks.
+    const int B = std::max(1, std::min(NR_HOST_BLOCKS, n / 128));
+    S.blk.resize(B);
+    auto blk_begin = [&](int b) { return (int)((long long)n * b / B); };
+    std::atomic<int> too_wide(0);
+    c->parallel_for(B, 1, [&](int b) {
+        NrHostBlock &k = S.blk[b];
+        size_t rel = 0;
+        k.last_owner_rel = -1;
+        for (int j = 0; j < NCLS; ++j) k.cnt[j] = 0;
+        for (int i = blk_begin(b), e = blk_begin(b + 1); i < e; ++i) {
+            // consecutive instances with the same topology share one structural part
+            const bool same = i > 0 && same_topology(&gs[i], &gs[i - 1]);
+            const size_t ib = small_inst_layout(&gs[i], srcs[i], dsts[i], &desc[i]);
+            const size_t sb = small_struct_layout(&gs[i], &desc[i], 0);   // offsets relative to struct_off
+            S.same_prev[i] = same;
+            S.inst_b[i] = ib;
+            S.struct_b[i] = same ? 0 : sb;
+            rel += ib;
+            if (!same) { k.last_owner_rel = (long long)rel; rel += sb; }
+            if (desc[i].w4 > NR_MAX_W4) { too_wide.store(1); S.cls[i] = 0; continue; }
+            const int G = group_width(gs[i].n_nodes);
+            S.cls[i] = (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + desc[i].w4 - 1;
+            k.cnt[S.cls[i]]++;
+        }
+        k.bytes = rel;
+    });
+    if (too_wide.load()) return NR_ERR_UNSUPPORTED;
+    pc.mark("sizes");
+
+    // staging (the same offsets in pinned host memory and on the device):
+    //   [work counters | tables (instance order) | descriptors (class order) | ids] then [outputs]
+    size_t off = align16(sizeof(int) * NCLS);
+    const size_t off_cnt = 0;
+    long long owner_struct = -1;              // struct_off of the last structural part so far
+    int class_count[NCLS] = {0};
+    for (int b = 0; b < B; ++b) {
+        NrHostBlock &k = S.blk[b];
+        k.base = off;
+        k.struct_in = owner_struct;
+        if (k.last_owner_rel >= 0) owner_struct = (long long)off + k.last_owner_rel;
+        off += k.bytes;
+        for (int j = 0; j < NCLS; ++j) {
+            k.cbase[j] = class_count[j];
+            class_count[j] += k.cnt[j];
+        }
     }
-    int class_begin[3 * NR_MAX_W4 + 1] = {0};
-    for (int k = 0; k < 3 * NR_MAX_W4; ++k) class_begin[k + 1] = class_begin[k] + class_count[k];
-    // pinned staging: [tables | descriptors (class order) | ids (class order)] then [outputs]
-    size_t off = 0;
-    const size_t off_blob = off; off = align16(off + blob_bytes);
+    int class_begin[NCLS + 1] = {0};
+    for (int j = 0; j < NCLS; ++j) class_begin[j + 1] = class_begin[j] + class_count[j];
+    off = align16(off);
     const size_t off_desc = off; off = align16(off + sizeof(NrSmallGraph) * n);
     const size_t off_ids = off; off = align16(off + sizeof(int) * n);
     const size_t up_bytes = off;
     const size_t off_out = off; off = align16(off + sizeof(NrWarpOut) * n);
-    const size_t off_cnt = off; off = align16(off + sizeof(int) * 3 * NR_MAX_W4);
     int rc = ensure_host(&c->hbuf, &c->hbuf_bytes, off);
     if (rc) return rc;
     rc = ensure(&c->wbuf, &c->wbuf_bytes, off);
@@ -802,16 +957,33 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
     unsigned char *hb = static_cast<unsigned char *>(c->hbuf);
     NrSmallGraph *hdesc = reinterpret_cast<NrSmallGraph *>(hb + off_desc);
     int *hids = reinterpret_cast<int *>(hb + off_ids);
-    {
-        int fill[3 * NR_MAX_W4];
-        for (int k = 0; k < 3 * NR_MAX_W4; ++k) fill[k] = class_begin[k];
-        for (int i = 0; i < n; ++i) {
-            const int slot = fill[cls[i]]++;
-            hdesc[slot] = desc[i];
+    memset(hb + off_cnt, 0, sizeof(int) * NCLS);
+    c->parallel_for(B, 1, [&](int b) {
+        const NrHostBlock &k = S.blk[b];
+        size_t at = k.base;
+        long long rep = k.struct_in;
+        int fill[NCLS];
+        for (int j = 0; j < NCLS; ++j) fill[j] = class_begin[j] + k.cbase[j];
+        for (int i = blk_begin(b), e = blk_begin(b + 1); i < e; ++i) {
+            NrSmallGraph &d = desc[i];
+            d.blob_off = (long long)at;
+            at += S.inst_b[i];
+            if (!S.same_prev[i]) {
+                d.struct_off = (long long)at;
+                rep = d.struct_off;
+                at += S.struct_b[i];
+                small_fill_struct(&gs[i], &d, hb + d.struct_off);
+            } else {
+                d.struct_off = rep;               // instance 0 always owns one, so rep >= 0 here
+            }
+            d.blob_bytes = (int)(S.inst_b[i] + S.struct_b[i]);
+            small_fill_inst(&gs[i], &d, hb + d.blob_off);
+            const int slot = fill[S.cls[i]]++;
+            hdesc[slot] = d;
             hids[slot] = i;
         }
-    }
-    c->parallel_for(n, 128, [&](int i) { small_fill(&gs[i], &desc[i], hb + off_blob + desc[i].blob_off); });
+    });
+    pc.mark("tables");
 
     // launch geometry per class (occupancy cached per kernel and shared-memory size)
     const int warps_pb = cfg.warps_per_block, block = 32 * warps_pb;
@@ -821,18 +993,17 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         c->smem_optin = v;
     }
     // pages per warp: as asked, but no more than the block's shared memory can index
-    WarpRunCfg cfgv = cfg;
-    while (cfgv.pages > 4 &&
-           nr_warp_shm_bytes(4, NR_MAX_W4, cfgv.n_buckets, cfgv.pages, true) * warps_pb > (size_t)c->smem_optin)
-        cfgv.pages /= 2;
-    const WarpRunCfg &cfgp = cfgv;
-    int grids[3 * NR_MAX_W4] = {0};
-    size_t smems[3 * NR_MAX_W4] = {0};
+    WarpRunCfg cfgp = cfg;
+    while (cfgp.pages > 4 &&
+           nr_warp_shm_bytes(4, NR_MAX_W4, cfgp.n_buckets, cfgp.pages, true) * warps_pb > (size_t)c->smem_optin)
+        cfgp.pages /= 2;
+    const bool learn = cfg.learned || cfg.dump;
+    int grids[NCLS] = {0};
+    size_t smems[NCLS] = {0};
     size_t slab_need = 0;
-    for (int k = 0; k < 3 * NR_MAX_W4; ++k) {
-        if (!class_count[k]) continue;
-        const int G = 8 << (k / NR_MAX_W4), W4 = k % NR_MAX_W4 + 1;
-        const bool learn = cfg.learned || cfg.dump;
+    for (int j = 0; j < NCLS; ++j) {
+        if (!class_count[j]) continue;
+        const int G = 8 << (j / NR_MAX_W4), W4 = j % NR_MAX_W4 + 1;
         const void *kfn = warp_kernel(G, W4, learn);
         if (!kfn) return NR_ERR_UNSUPPORTED;
         const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn) * warps_pb;
@@ -846,31 +1017,30 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
             bps = it->second;
         }
         if (bps < 1) return NR_ERR_UNSUPPORTED;
-        const int grid = std::max(1, std::min(bps * c->sms, (class_count[k] + warps_pb - 1) / warps_pb));
-        grids[k] = grid;
-        smems[k] = smem;
-        slab_need = std::max(slab_need, (size_t)grid * warps_pb * cfgp.pages * NR_PAGE * (16 * (size_t)W4 + 8));
+        grids[j] = std::max(1, std::min(bps * c->sms, (class_count[j] + warps_pb - 1) / warps_pb));
+        smems[j] = smem;
+        slab_need = std::max(slab_need, (size_t)grids[j] * warps_pb * cfgp.pages * NR_PAGE * (16 * (size_t)W4 + 8));
     }
     rc = ensure(&c->wslab, &c->wslab_bytes, slab_need);
     if (rc) return rc;
     unsigned char *wb = static_cast<unsigned char *>(c->wbuf);
     cudaStream_t s = c->stream;
+    pc.mark("geometry");
     NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, up_bytes, cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemsetAsync(wb + off_cnt, 0, sizeof(int) * 3 * NR_MAX_W4, s));
     NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
     int first_grid = 0;
-    for (int k = 0; k < 3 * NR_MAX_W4; ++k) {
-        if (!class_count[k]) continue;
-        const int G = 8 << (k / NR_MAX_W4), W4 = k % NR_MAX_W4 + 1;
-        if (!first_grid) first_grid = grids[k];
+    for (int j = 0; j < NCLS; ++j) {
+        if (!class_count[j]) continue;
+        const int G = 8 << (j / NR_MAX_W4), W4 = j % NR_MAX_W4 + 1;
+        if (!first_grid) first_grid = grids[j];
         NrWarpParams P;
-        P.blob = wb + off_blob;
-        P.inst = reinterpret_cast<const NrSmallGraph *>(wb + off_desc) + class_begin[k];
-        P.inst_id = reinterpret_cast<const int *>(wb + off_ids) + class_begin[k];
-        P.n_inst = class_count[k];
-        P.next_inst = reinterpret_cast<int *>(wb + off_cnt) + k;
+        P.blob = wb;
+        P.inst = reinterpret_cast<const NrSmallGraph *>(wb + off_desc) + class_begin[j];
+        P.inst_id = reinterpret_cast<const int *>(wb + off_ids) + class_begin[j];
+        P.n_inst = class_count[j];
+        P.next_inst = reinterpret_cast<int *>(wb + off_cnt) + j;
         P.slab_mask = static_cast<uint4 *>(c->wslab);
-        const size_t warps = (size_t)grids[k] * warps_pb;
+        const size_t warps = (size_t)grids[j] * warps_pb;
         P.slab_mass = reinterpret_cast<double *>(static_cast<unsigned char *>(c->wslab) +
                                                  warps * cfgp.pages * NR_PAGE * 16 * (size_t)W4);
         P.pages = cfgp.pages;
@@ -892,30 +1062,37 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         P.dump_count = cfg.dump ? cfg.dump->count : nullptr;
         P.dump_cap = cfg.dump ? cfg.dump->cap : 0;
         P.dump_stride = cfg.dump ? cfg.dump->stride : 0;
-        const void *kfn = warp_kernel(G, W4, cfg.learned || cfg.dump);
+        const void *kfn = warp_kernel(G, W4, learn);
         void *args[] = {&P};
         // the dynamic shared-memory limit is per-kernel state that another setting may have lowered
-        NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smems[k]));
-        NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[k]), dim3(block), args, smems[k], s));
+        NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smems[j]));
+        NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[j]), dim3(block), args, smems[j], s));
     }
     NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
     NrWarpOut *hout = reinterpret_cast<NrWarpOut *>(hb + off_out);
     NR_CUDA_TRY(cudaMemcpyAsync(hout, wb + off_out, sizeof(NrWarpOut) * n, cudaMemcpyDeviceToHost, s));
+    pc.mark("enqueue");
     NR_CUDA_TRY(cudaStreamSynchronize(s));
+    pc.mark("device");
     float ms = 0.f;
     NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-    for (int i = 0; i < n; ++i) {
+    std::atomic<int> n_hand(0);
+    c->parallel_for(n, 512, [&](int i) {
         nr_result *r = &res[i];
         r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
-        if (hout[i].status == 2) { handover->push_back(i); continue; }
+        if (hout[i].status == 2) { n_hand.fetch_add(1); return; }
         fill_from_warp(hout[i], cfgp, desc[i].w4, r);
         r->ms = ms;
         r->grid_blocks = first_grid;
         r->block_threads = block;
         r->h2d_bytes = desc[i].blob_bytes + sizeof(NrSmallGraph) + sizeof(int);
         r->d2h_bytes = sizeof(NrWarpOut);
-    }
+    });
+    if (n_hand.load())
+        for (int i = 0; i < n; ++i)
+            if (hout[i].status == 2) handover->push_back(i);
+    pc.mark("results");
     return NR_OK;
 }
 

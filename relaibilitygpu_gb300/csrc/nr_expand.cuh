@@ -15,10 +15,10 @@
 
 #include "nr_device.cuh"
 
-// Shared-memory view of the staged graph tables.
+// View of an instance's graph tables (shared or global memory).  The down
+// probability of edge e is 1 - p[e], rounded as the host's double subtraction.
 struct NrSmemGraph {
     const double *p;
-    const double *q;
     const uint16_t *eid;      // [G*G] arc (u -> v) -> edge id
     const int *start;         // [n+1] in-arc ranges
     const uint32_t *list;     // in-arcs of v: (eid << 8) | u
@@ -28,7 +28,6 @@ __device__ __forceinline__ NrSmemGraph nr_smem_graph(const unsigned char *s, con
 {
     NrSmemGraph v;
     v.p = reinterpret_cast<const double *>(s + g.off_p);
-    v.q = reinterpret_cast<const double *>(s + g.off_q);
     v.eid = reinterpret_cast<const uint16_t *>(s + g.off_eid);
     v.start = reinterpret_cast<const int *>(s + g.off_start);
     v.list = reinterpret_cast<const uint32_t *>(s + g.off_list);
@@ -177,7 +176,7 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
         const int e = __shfl_sync(NR_FULL, e_h, gbase + h);
         const bool u = __shfl_sync(NR_FULL, unk, gbase + h);
         if (h < L && u) {
-            if (v == h) { cm = __dmul_rn(P, sg.q[e]); has_child = true; }
+            if (v == h) { cm = __dmul_rn(P, __dsub_rn(1.0, sg.p[e])); has_child = true; }
             P = __dmul_rn(P, sg.p[e]);
         }
     }

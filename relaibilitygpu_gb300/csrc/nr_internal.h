@@ -35,14 +35,18 @@ struct NrPartial {
     unsigned long long nodes, leaves, dead, truncated, spilled, pad;
 };
 
-// Graph tables of one instance (small engines), laid out in one blob:
-// p[E], q[E] (double), eid_tab[G*G] (u16, arc u->v at u*G+v), in_start[n+1]
-// (int), in_list[n_in] (u32 = eid << 8 | u), root mask (4*w4 words).
-// Offsets are relative to blob_off; every section starts 16-byte aligned.
+// Graph tables of one instance (small engines) in two parts:
+//   per instance, at blob_off:   p[E] (double); the root mask is derived from p on the device;
+//   per topology, at struct_off: eid_tab[G*G] (u16, arc u->v at u*G+v),
+//                                in_start[n+1] (int), in_list[n_in] (u32 = eid << 8 | u).
+// Instances with the same topology share one structural part.  When both parts
+// are one blob, struct_off == blob_off.  Every section starts 16-byte aligned;
+// blob_bytes is the size of the instance's own part(s).
 struct NrSmallGraph {
     int n, e, w4, src, dst, n_in;
-    int off_p, off_q, off_eid, off_start, off_list, off_root, blob_bytes;
+    int off_p, off_eid, off_start, off_list, blob_bytes;
     long long blob_off;
+    long long struct_off;
 };
 
 struct NrGridParams {

@@ -64,23 +64,20 @@ size_t noalloc_tables(const nr_graph *g, int src, int dst, int G, NrSmallGraph *
     sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst; sg->n_in = g->n_arcs;
     size_t off = 0;
     sg->off_p = (int)off; off = a16(off + sizeof(double) * std::max(E, 1));
-    sg->off_q = (int)off; off = a16(off + sizeof(double) * std::max(E, 1));
     sg->off_eid = (int)off; off = a16(off + sizeof(uint16_t) * G * G);
     sg->off_start = (int)off; off = a16(off + sizeof(int) * (n + 1));
     sg->off_list = (int)off; off = a16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
-    sg->off_root = (int)off; off = a16(off + sizeof(uint32_t) * 4 * sg->w4);
     sg->blob_bytes = (int)off;
     sg->blob_off = 0;
+    sg->struct_off = 0;
     if (off > NR_NOALLOC_BLOB_MAX) return 0;
     unsigned char *b = g_noalloc_blob;
     memset(b, 0, off);
     double *p = reinterpret_cast<double *>(b + sg->off_p);
-    double *q = reinterpret_cast<double *>(b + sg->off_q);
     uint16_t *eid = reinterpret_cast<uint16_t *>(b + sg->off_eid);
     int *start = reinterpret_cast<int *>(b + sg->off_start);
     uint32_t *list = reinterpret_cast<uint32_t *>(b + sg->off_list);
-    uint32_t *root = reinterpret_cast<uint32_t *>(b + sg->off_root);
-    for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
+    for (int e = 0; e < E; ++e) p[e] = g->edge_p[e];
     for (int i = 0; i < G * G; ++i) eid[i] = 0xffff;
     int cnt[NR_SMALL_MAX_N + 1] = {0};
     for (int u = 0; u < n; ++u)
@@ -94,11 +91,6 @@ size_t noalloc_tables(const nr_graph *g, int src, int dst, int G, NrSmallGraph *
             list[start[v] + fill[v]++] = ((uint32_t)e << 8) | (uint32_t)u;
             if (eid[u * G + v] == 0xffff) eid[u * G + v] = (uint16_t)e;
         }
-    for (int e = 0; e < E; ++e) {
-        const double pe = g->edge_p[e];
-        const uint32_t st = (pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN;
-        root[e >> 4] |= st << ((e & 15) * 2);
-    }
     return off;
 }
 

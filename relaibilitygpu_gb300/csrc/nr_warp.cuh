@@ -25,6 +25,9 @@
 
 #define NR_WARP_BLOCK 128        // default block: 4 warps
 #define NR_WARP_BLOCK_MAX 256    // largest block the warp kernels are compiled for
+#ifndef NR_WARP_MIN_BLOCKS
+#define NR_WARP_MIN_BLOCKS 1     // resident 256-thread blocks per SM the register budget must allow
+#endif
 #define NR_PAGE 32
 
 struct NrWarpOut {
@@ -107,7 +110,7 @@ __host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets
 }
 
 template <int G, int W4, bool LEARN = false>
-__global__ void __launch_bounds__(NR_WARP_BLOCK_MAX) nr_warp_kernel(NrWarpParams P)
+__global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, NR_WARP_MIN_BLOCKS) nr_warp_kernel(NrWarpParams P)
 {
     constexpr int K = 32 / G;
     constexpr int NW = 4 * W4;
@@ -147,14 +150,13 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX) nr_warp_kernel(NrWarpParams
         ii = __shfl_sync(NR_FULL, ii, 0);
         if (ii >= P.n_inst) break;
         const NrSmallGraph g = P.inst[ii];
-        const unsigned char *gb = P.blob + g.blob_off;
+        const unsigned char *gb = P.blob + g.blob_off;         // this instance's p
+        const unsigned char *gs = P.blob + g.struct_off;       // its topology's tables (maybe shared)
         NrSmemGraph sg;
         sg.p = reinterpret_cast<const double *>(gb + g.off_p);
-        sg.q = reinterpret_cast<const double *>(gb + g.off_q);
-        sg.eid = reinterpret_cast<const uint16_t *>(gb + g.off_eid);
-        sg.start = reinterpret_cast<const int *>(gb + g.off_start);
-        sg.list = reinterpret_cast<const uint32_t *>(gb + g.off_list);
-        const uint32_t *root = reinterpret_cast<const uint32_t *>(gb + g.off_root);
+        sg.eid = reinterpret_cast<const uint16_t *>(gs + g.off_eid);
+        sg.start = reinterpret_cast<const int *>(gs + g.off_start);
+        sg.list = reinterpret_cast<const uint32_t *>(gs + g.off_list);
         const long long t0 = nr_globaltimer();
 
         // reset the private queue; the root is the only subproblem
@@ -174,9 +176,25 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX) nr_warp_kernel(NrWarpParams
         }
         top = __shfl_sync(NR_FULL, top, 0);
         rpg = __shfl_sync(NR_FULL, rpg, 0);
-        if (lane < W4)
-            sl_mask[((size_t)rpg * NR_PAGE) * W4 + lane] =
-                make_uint4(root[4 * lane], root[4 * lane + 1], root[4 * lane + 2], root[4 * lane + 3]);
+        {
+            // root record from p: p <= 0 down, p >= 1 up, else unknown (main.cu:717-748);
+            // 16 edges a word, each half-warp ORs one word together
+            uint32_t *rw = reinterpret_cast<uint32_t *>(sl_mask + (size_t)rpg * NR_PAGE * W4);
+            for (int e0 = 0; e0 < 64 * W4; e0 += 32) {
+                const int e = e0 + lane;
+                uint32_t v = 0u;
+                if (e < g.e) {
+                    const double pe = sg.p[e];
+                    v = (uint32_t)((pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN)
+                        << ((e & 15) << 1);
+                }
+                v |= __shfl_xor_sync(NR_FULL, v, 8);
+                v |= __shfl_xor_sync(NR_FULL, v, 4);
+                v |= __shfl_xor_sync(NR_FULL, v, 2);
+                v |= __shfl_xor_sync(NR_FULL, v, 1);
+                if ((lane & 15) == 0) rw[(e0 >> 4) + (lane >> 4)] = v;
+            }
+        }
         if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
         __syncwarp();
 

@@ -188,13 +188,23 @@ class Result:
 
 
 class _GraphView:
-    """Keeps the numpy arrays alive while C holds pointers into them."""
+    """Keeps the numpy arrays alive while C holds pointers into them.
 
-    def __init__(self, g: Graph):
+    `shared` maps a topology (node count and the CSR / edge-id bytes) to the
+    structural arrays of the first view that had it: views of graphs with the
+    same topology then hand the engine the same pointers, and the batch entry
+    point keeps one copy of the structural tables for each run of them
+    without comparing the arrays."""
+
+    def __init__(self, g: Graph, shared: Optional[dict] = None):
         self.row = np.ascontiguousarray(g.row_ptr, dtype=np.int32)
         self.col = np.ascontiguousarray(g.col_idx, dtype=np.int32)
         self.eid = np.ascontiguousarray(g.edge_id, dtype=np.int32)
         self.p = np.ascontiguousarray(g.edge_p, dtype=np.float64)
+        if shared is not None:
+            key = (int(g.n_nodes), self.row.tobytes(), self.col.tobytes(), self.eid.tobytes())
+            first = shared.setdefault(key, (self.row, self.col, self.eid))
+            self.row, self.col, self.eid = first
         self.c = NrGraph(
             int(g.n_nodes), int(self.p.shape[0]), int(self.col.shape[0]),
             self.row.ctypes.data_as(C.POINTER(C.c_int32)), self.col.ctypes.data_as(C.POINTER(C.c_int32)),
@@ -296,7 +306,8 @@ class Batch:
     """Host-side argument arrays of nr_reliability_batch, built once and reused."""
 
     def __init__(self, graphs: Sequence[Graph], srcs, dsts):
-        self.views = [_GraphView(g) for g in graphs]
+        shared: dict = {}
+        self.views = [_GraphView(g, shared) for g in graphs]
         self.n = len(self.views)
         self.arr = (NrGraph * self.n)(*[v.c for v in self.views])
         self.s = np.ascontiguousarray(srcs, dtype=np.int32)
