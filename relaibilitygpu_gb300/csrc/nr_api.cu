@@ -716,6 +716,8 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     const size_t off_wc = off; off = align16(off + sizeof(unsigned long long) * (max_waves + 1));
     const size_t off_bar = off; off = align16(off + 4 * sizeof(unsigned));
     const size_t off_part = off; off = align16(off + sizeof(NrPartial) * grid);
+    const size_t off_wpart = off; off = align16(off + sizeof(NrFix) * 2 * grid);
+    const size_t off_stop = off; off = align16(off + sizeof(int));
     rc = ensure(&c->sbuf, &c->sbytes, off);
     if (rc) return rc;
     unsigned char *sb = static_cast<unsigned char *>(c->sbuf);
@@ -736,6 +738,11 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     P.partials = reinterpret_cast<NrPartial *>(sb + off_part);
     P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
+    P.target_on = o->target_width > 0 ? 1 : 0;
+    P.target_fix = nr_fix_of(o->target_width > 0 ? o->target_width : 0.0);
+    P.wpart = reinterpret_cast<NrFix *>(sb + off_wpart);
+    P.stop_wave = reinterpret_cast<int *>(sb + off_stop);
+    const int minus_one = -1;
     std::vector<uint32_t> root(4 * W4, 0);
     nr_initial_mask(g, root.data(), 4 * W4);
     const double one = 1.0;
@@ -746,6 +753,7 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     NR_CUDA_TRY(cudaMemcpyAsync(P.wave_count, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaMemcpyAsync(P.mask[0], root.data(), 16 * W4, cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaMemcpyAsync(P.mass[0], &one, sizeof(one), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.stop_wave, &minus_one, sizeof(int), cudaMemcpyHostToDevice, s));
     void *args[] = {&P};
     NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
     NR_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(block), args, smem, s));
@@ -757,6 +765,8 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
                                 cudaMemcpyDeviceToHost, s));
     NR_CUDA_TRY(cudaMemcpyAsync(parts.data(), P.partials, sizeof(NrPartial) * grid, cudaMemcpyDeviceToHost, s));
     NR_CUDA_TRY(cudaMemcpyAsync(&status, P.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int stop_wave = -1;
+    NR_CUDA_TRY(cudaMemcpyAsync(&stop_wave, P.stop_wave, sizeof(int), cudaMemcpyDeviceToHost, s));
     NR_CUDA_TRY(cudaStreamSynchronize(s));
     float ms = 0.f;
     NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
@@ -766,33 +776,40 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
         nr_fix_add(R, pp.R);
         nr_fix_add(esp, pp.et);
         nr_fix_add(esp, pp.es);
+        nr_fix_add(esp, pp.q);      // still queued at a target stop
         nodes += pp.nodes; leaves += pp.leaves; dead += pp.dead; trunc += pp.truncated; spilled += pp.spilled;
     }
+    // waves run (a target stop leaves wave stop_wave queued, not run)
     int waves = 0;
-    unsigned long long maxw = 0;
-    for (int k = 0; k <= max_waves; ++k) {
+    unsigned long long maxw = 0, queued = 0;
+    const int last = stop_wave >= 0 ? stop_wave : max_waves + 1;
+    for (int k = 0; k <= max_waves && k < last; ++k) {
         const unsigned long long nn = std::min<unsigned long long>(wc[k], cap);
         if (!nn) break;
         waves++;
         maxw = std::max(maxw, nn);
     }
+    if (stop_wave >= 0) queued = std::min<unsigned long long>(wc[stop_wave], cap);
     r->R = nr_fix_to_double_host(R);
     r->esp = nr_fix_to_double_host(esp);
     r->R_plus_esp = r->R + r->esp;
     r->trunc_bound = r->R > 0 ? r->esp / r->R : r->esp;
     r->nodes = nodes; r->leaves = leaves; r->dead_ends = dead; r->truncated = trunc; r->spilled = spilled;
     r->paths = leaves + spilled;
+    r->queued = queued;
+    r->stop = stop_wave >= 0 ? 1 : 0;
     r->iterations = waves;
     r->max_queue_items = maxw;
     r->item_bytes = (int)item_bytes;
     r->max_queue_mb = (double)maxw * item_bytes / (1024.0 * 1024.0);
     r->ms = ms;
+    if (stop_wave >= 0) r->time_to_bound_ms = ms;
     r->engine = NR_ENGINE_GRID;
     r->grid_blocks = grid;
     r->block_threads = block;
     r->capacity = cap;
-    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one);
-    r->d2h_bytes = sizeof(unsigned long long) * wc.size() + sizeof(NrPartial) * grid + sizeof(int);
+    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one) + sizeof(int);
+    r->d2h_bytes = sizeof(unsigned long long) * wc.size() + sizeof(NrPartial) * grid + 2 * sizeof(int);
     if (status & NR_DEV_ERR_TIMEOUT) return NR_ERR_TIMEOUT;
     if (status) return NR_ERR_INTERNAL;
     return NR_OK;
@@ -1105,23 +1122,56 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
     nr_options o;
     if (opt) o = *opt; else nr_options_default(&o);
     std::lock_guard<std::mutex> lock(c->mu);
-    std::atomic<int> bad(NR_OK);
+    std::atomic<int> bad(NR_OK), n_wide(0);
+    const bool wave_order = o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
     c->parallel_for(n, 256, [&](int i) {
         memset(&res[i], 0, sizeof(nr_result));
         int rc = validate(&gs[i], srcs[i], dsts[i]);
-        if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) rc = NR_ERR_UNSUPPORTED;
+        if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) {
+            if (!wave_order) rc = NR_ERR_UNSUPPORTED;    // max-mass and learned orders: n <= 32 only
+            n_wide.fetch_add(1);
+        }
         if (rc) bad.store(rc);
     });
     if (bad.load() != NR_OK) return bad.load();
     NR_CUDA_TRY(cudaSetDevice(c->device));
-    const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
+    const bool exhaustive = !(o.target_width > 0) && wave_order;
     if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
     const WarpRunCfg cfg = warp_cfg(&o, capacity, exhaustive);
-    std::vector<int> handover;
-    int rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover);
-    if (rc) return rc;
+    // graphs of up to 32 nodes run together on the warp engine; larger ones one at a time on
+    // the whole-GPU wave engine, as do warp-engine instances that outgrow a warp's budget
+    std::vector<int> small_idx, wide_idx, handover;
+    int rc;
+    if (n_wide.load() == 0) {
+        rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover);
+        if (rc) return rc;
+    } else {
+        for (int i = 0; i < n; ++i) (gs[i].n_nodes > NR_SMALL_MAX_N ? wide_idx : small_idx).push_back(i);
+        if (!small_idx.empty()) {
+            const int m = (int)small_idx.size();
+            std::vector<nr_graph> sg(m);
+            std::vector<int32_t> ss(m), sd(m);
+            std::vector<nr_result> sr(m);
+            for (int k = 0; k < m; ++k) {
+                sg[k] = gs[small_idx[k]]; ss[k] = srcs[small_idx[k]]; sd[k] = dsts[small_idx[k]];
+                sr[k] = res[small_idx[k]];
+            }
+            std::vector<int> hk;
+            rc = run_warp_batch(c, m, sg.data(), ss.data(), sd.data(), cfg, sr.data(), &hk);
+            if (rc) return rc;
+            for (int k = 0; k < m; ++k) res[small_idx[k]] = sr[k];
+            for (int k : hk) handover.push_back(small_idx[k]);
+        }
+    }
     for (int i : handover) {
         rc = run_grid_small(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, &res[i]);
+        if (rc) return rc;
+    }
+    for (int i : wide_idx) {
+        nr_result *r = &res[i];
+        r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
+        r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
+        rc = run_grid_wide(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, r);
         if (rc) return rc;
     }
     return NR_OK;
@@ -1279,9 +1329,9 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     std::lock_guard<std::mutex> lock(c->mu);
     NR_CUDA_TRY(cudaSetDevice(c->device));
     if (g->n_nodes > NR_SMALL_MAX_N) {
-        // 33..1024 nodes: whole-GPU wave engine (max-mass order and target widths are n <= 32 only)
-        if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED)
-            return NR_ERR_UNSUPPORTED;
+        // 33..1024 nodes: whole-GPU wave engine, breadth-first waves (a target width stops it
+        // between waves); the max-mass and learned orders are n <= 32 only
+        if (o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
         return run_grid_wide(c, g, src, dst, capacity ? capacity : (1u << 20), &o, res);
     }
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {

@@ -154,17 +154,18 @@ __device__ __forceinline__ bool nr_grid_sync(unsigned *count, unsigned *gen, int
 }
 
 // Block reduction of the per-lane sums and counters into one NrPartial.
-__device__ __forceinline__ void nr_block_partial(NrPartial *out, NrFix R, NrFix et, NrFix es,
+__device__ __forceinline__ void nr_block_partial(NrPartial *out, NrFix R, NrFix et, NrFix es, NrFix q,
                                                  unsigned long long nodes, unsigned long long leaves,
                                                  unsigned long long dead, unsigned long long trunc,
                                                  unsigned long long spilled)
 {
-    __shared__ NrFix s_fx[NR_BLOCK_THREADS / 32][3];
+    __shared__ NrFix s_fx[NR_BLOCK_THREADS / 32][4];
     __shared__ unsigned long long s_c[NR_BLOCK_THREADS / 32][5];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     R = nr_fix_warp_sum(R);
     et = nr_fix_warp_sum(et);
     es = nr_fix_warp_sum(es);
+    q = nr_fix_warp_sum(q);
     for (int off = 16; off > 0; off >>= 1) {
         nodes += __shfl_xor_sync(NR_FULL, nodes, off);
         leaves += __shfl_xor_sync(NR_FULL, leaves, off);
@@ -173,24 +174,40 @@ __device__ __forceinline__ void nr_block_partial(NrPartial *out, NrFix R, NrFix 
         spilled += __shfl_xor_sync(NR_FULL, spilled, off);
     }
     if (lane == 0) {
-        s_fx[warp][0] = R; s_fx[warp][1] = et; s_fx[warp][2] = es;
+        s_fx[warp][0] = R; s_fx[warp][1] = et; s_fx[warp][2] = es; s_fx[warp][3] = q;
         s_c[warp][0] = nodes; s_c[warp][1] = leaves; s_c[warp][2] = dead;
         s_c[warp][3] = trunc; s_c[warp][4] = spilled;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        NrFix r = nr_fix_zero(), a = nr_fix_zero(), b = nr_fix_zero();
+        NrFix r = nr_fix_zero(), a = nr_fix_zero(), b = nr_fix_zero(), qq = nr_fix_zero();
         unsigned long long c[5] = {0, 0, 0, 0, 0};
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
             nr_fix_add(r, s_fx[w][0]);
             nr_fix_add(a, s_fx[w][1]);
             nr_fix_add(b, s_fx[w][2]);
+            nr_fix_add(qq, s_fx[w][3]);
             for (int k = 0; k < 5; ++k) c[k] += s_c[w][k];
         }
-        out->R = r; out->et = a; out->es = b;
+        out->R = r; out->et = a; out->es = b; out->q = qq;
         out->nodes = c[0]; out->leaves = c[1]; out->dead = c[2];
         out->truncated = c[3]; out->spilled = c[4]; out->pad = 0;
     }
+}
+
+// Sum of one NrFix per thread over the block, returned on every thread (exact,
+// so every block that sums the same values gets the same bits).
+__device__ __forceinline__ NrFix nr_block_fix_sum(NrFix v)
+{
+    __shared__ NrFix s_w[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+    v = nr_fix_warp_sum(v);
+    __syncthreads();                       // s_w may still be read by an earlier call
+    if (lane == 0) s_w[warp] = v;
+    __syncthreads();
+    NrFix t = nr_fix_zero();
+    for (int w = 0; w < nw; ++w) nr_fix_add(t, s_w[w]);
+    return t;
 }
 
 // Stage the graph tables into shared memory (16-byte copies; blob_bytes is a multiple of 16).

@@ -86,6 +86,6 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_kernel(NrGridParams 
             *(volatile unsigned long long *)&P.wave_count[wave + 1] != 0)
             atomicOr(P.status, NR_DEV_ERR_WAVES);
     }
-    nr_block_partial(P.partials + blockIdx.x, acc.R, acc.et, acc.es, acc.nodes, acc.leaves, acc.dead,
+    nr_block_partial(P.partials + blockIdx.x, acc.R, acc.et, acc.es, nr_fix_zero(), acc.nodes, acc.leaves, acc.dead,
                      acc.trunc, acc.spilled);
 }

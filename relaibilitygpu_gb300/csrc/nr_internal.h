@@ -32,6 +32,7 @@ struct NrPartial {
     NrFix R;                    // all-up leaf mass
     NrFix et;                   // eps-truncated mass
     NrFix es;                   // spilled mass
+    NrFix q;                    // mass still queued when a target width stopped the run
     unsigned long long nodes, leaves, dead, truncated, spilled, pad;
 };
 

@@ -12,6 +12,13 @@
 // emitted in hop order with the lanes owning mask words, so every child
 // record is written with coalesced stores.  Waves, the grid barrier, the
 // wave counters and the block partials work as in nr_grid.cuh.
+//
+// With a target width the run stops before the first wave at which
+// ESP + queued mass <= target (the oracle's wave schedule with one bucket):
+// at the end of a wave every block writes its exact share of that width
+// (its ESP so far plus the mass it pushed) to one of two alternating slots,
+// and after the grid barrier every block adds all shares and takes the same
+// decision.  The pushed mass of the last wave run is the queued mass at the stop.
 #pragma once
 
 #include "nr_expand.cuh"
@@ -41,6 +48,10 @@ struct NrGridWideParams {
     NrPartial *partials;
     double eps;
     long long timeout_ns;
+    int target_on;              // stop at ESP + queued <= target_fix
+    NrFix target_fix;
+    NrFix *wpart;               // [2][gridDim.x] per-block width shares, alternating slots
+    int *stop_wave;             // waves run before the target stop, or -1
 };
 
 // per-warp shared memory: mask words, frontier / next / visited bitmasks,
@@ -79,12 +90,36 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
     const unsigned long long cap = P.capacity;
 
     NrFix R = nr_fix_zero(), et = nr_fix_zero(), es = nr_fix_zero();
+    // lane 0: mass this warp queued in the last wave run (the root counts as queued by
+    // block 0's first warp, for a stop before the first wave)
+    NrFix pushed = (blockIdx.x == 0 && threadIdx.x == 0) ? nr_fix_of(1.0) : nr_fix_zero();
     unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0;
 
     for (int wave = 0; wave < P.max_waves; ++wave) {
         unsigned long long n_in = *(volatile unsigned long long *)&P.wave_count[wave];
         if (n_in > cap) n_in = cap;
         if (n_in == 0) break;
+        if (P.target_on) {
+            NrFix width = nr_fix_zero();
+            if (wave == 0) {
+                width = nr_fix_of(1.0);                         // the root alone is queued
+            } else {
+                const NrFix *slot = P.wpart + (size_t)((wave - 1) & 1) * gridDim.x;
+                for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+                    NrFix v;                                    // written by other blocks: read from L2
+                    v.w0 = __ldcg(&slot[b].w0);
+                    v.w1 = __ldcg(&slot[b].w1);
+                    v.w2 = __ldcg(&slot[b].w2);
+                    nr_fix_add(width, v);
+                }
+                width = nr_block_fix_sum(width);
+            }
+            if (nr_fix_le(width, P.target_fix)) {
+                if (threadIdx.x == 0 && blockIdx.x == 0) *P.stop_wave = wave;
+                break;
+            }
+            pushed = nr_fix_zero();
+        }
         const uint4 *in_mask = P.mask[wave & 1];
         const double *in_mass = P.mass[wave & 1];
         uint4 *out_mask = P.mask[(wave + 1) & 1];
@@ -197,7 +232,10 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
                     uint32_t *dstw = reinterpret_cast<uint32_t *>(out_mask + slot * W4);
                     if (lane < NW) __stcg(dstw + lane, (lane == wi) ? (w0 & ~(3u << sh)) : w0);
                     if (lane + 32 < NW) __stcg(dstw + lane + 32, (lane + 32 == wi) ? (w1 & ~(3u << sh)) : w1);
-                    if (lane == 0) __stcg(out_mass + slot, cm);
+                    if (lane == 0) {
+                        __stcg(out_mass + slot, cm);
+                        if (P.target_on) nr_fix_add_mass(pushed, cm);
+                    }
                 } else if (lane == 0) {                             // queue full (main.cu:245-252)
                     spilled++;
                     nr_fix_add_mass(es, cm);
@@ -210,10 +248,27 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
             if (lane == 0) { leaves++; nr_fix_add_mass(R, Pm); }
             __syncwarp();
         }
+        if (P.target_on) {
+            // this block's share of the width after the wave: ESP so far + mass it queued
+            NrFix share = nr_fix_zero();
+            if (lane == 0) {
+                share = et;
+                nr_fix_add(share, es);
+                nr_fix_add(share, pushed);
+            }
+            share = nr_block_fix_sum(share);
+            if (threadIdx.x == 0) {
+                NrFix *dst = P.wpart + (size_t)(wave & 1) * gridDim.x + blockIdx.x;
+                __stcg(&dst->w0, share.w0);
+                __stcg(&dst->w1, share.w1);
+                __stcg(&dst->w2, share.w2);
+            }
+        }
         if (!nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns)) break;
         if (wave + 1 == P.max_waves && threadIdx.x == 0 && blockIdx.x == 0 &&
             *(volatile unsigned long long *)&P.wave_count[wave + 1] != 0)
             atomicOr(P.status, NR_DEV_ERR_WAVES);
     }
-    nr_block_partial(P.partials + blockIdx.x, R, et, es, nodes, leaves, dead, trunc, spilled);
+    nr_block_partial(P.partials + blockIdx.x, R, et, es, P.target_on ? pushed : nr_fix_zero(), nodes, leaves,
+                     dead, trunc, spilled);
 }

@@ -72,3 +72,61 @@ def test_wide_rejects_too_many_edges(ctx, engine_lib):
     with pytest.raises(engine_lib.NrError) as e:
         ctx.reliability(g, 0, 46)
     assert e.value.status == -4
+
+
+TARGET_CASES = [
+    ("rgg 200/600 to 1e-2", lambda G: (lambda g: (g, g.src, g.dst))(G.rgg(200, 600, p_range=(0.9, 0.99), seed=7)),
+     1e-2),
+    ("rgg 100/250 to 1e-3", lambda G: (lambda g: (g, g.src, g.dst))(G.rgg(100, 250, p_range=(0.9, 0.99), seed=3)),
+     1e-3),
+    ("rgg 60/150 to 1e-6", lambda G: (lambda g: (g, g.src, g.dst))(G.rgg(60, 150, p_range=(0.9, 0.99), seed=11)),
+     1e-6),
+    ("K40 p~U[0.9,0.99] to 1e-9", lambda G: (G.complete(40, p_range=(0.9, 0.99), seed=1), 0, 39), 1e-9),
+    ("grid 6x6 to 1e-3", lambda G: (G.grid(6, 6, p_range=(0.8, 0.99), seed=5), 0, 35), 1e-3),
+    ("target above 1: root only", lambda G: (G.complete(40, p=0.5), 0, 39), 2.0),
+]
+
+
+@pytest.mark.parametrize("name,make,target", TARGET_CASES, ids=[c[0] for c in TARGET_CASES])
+def test_wide_target_width_matches_oracle(ctx, oracle, name, make, target):
+    """Truncated runs: breadth-first waves stopped once ESP + queued mass <= target, as the
+    oracle's wave schedule with one bucket -- same waves, counts, queue and exact sums."""
+    from relaibilitygpu_gb300 import graphs
+    g, s, t = make(graphs)
+    o = oracle.run(g, s, t, target_width=target, threads=4)
+    assert o.status in (0, 1)
+    r = ctx.reliability(g, s, t, capacity=1 << 23, target_width=target)
+    assert r.engine == "grid"
+    check(r, o)
+    assert (r.queued, r.stop) == (o.queued, o.status)
+    assert r.esp <= target or o.status == 0
+
+
+def test_batch_routes_large_graphs_to_wide_engine(ctx, oracle):
+    """Batches mix graphs above 32 nodes (whole-GPU engine, one at a time) with small ones
+    (warp engine, all together); with one bucket both follow the oracle's wave schedule."""
+    from relaibilitygpu_gb300 import graphs
+    gs = []
+    for i in range(24):
+        if i % 6 == 0:
+            gs.append(graphs.grid(6, 6, p_range=(0.8, 0.99), seed=60 + i))
+        elif i % 6 == 3:
+            gs.append(graphs.rgg(60, 150, p_range=(0.9, 0.99), seed=60 + i))
+        else:
+            gs.append(graphs.gnm(8 + i % 12, 20 + i, p_range=(0.8, 0.99), seed=60 + i))
+    res = ctx.reliability_batch(gs, [g.src for g in gs], [g.dst for g in gs], capacity=1 << 16,
+                                target_width=1e-3, bucket_shift=-1)
+    for g, r in zip(gs, res):
+        o = oracle.run(g, g.src, g.dst, target_width=1e-3)
+        assert r.engine == ("grid" if g.n_nodes > 32 else "warp")
+        assert (r.n_nodes, r.src, r.dst) == (g.n_nodes, g.src, g.dst)
+        check(r, o)
+        assert r.queued == o.queued
+
+
+def test_batch_large_graph_needs_wave_order(ctx, engine_lib):
+    from relaibilitygpu_gb300 import graphs
+    gs = [graphs.complete(8, p=0.9), graphs.grid(6, 6, p=0.9)]
+    with pytest.raises(engine_lib.NrError) as e:
+        ctx.reliability_batch(gs, [0, 0], [7, 35], target_width=1e-6, order="maxmass")
+    assert e.value.status == -4
