@@ -31,6 +31,7 @@ const void *nr_grid_kernel_ptr_g8(int w4);
 const void *nr_grid_kernel_ptr_g16(int w4);
 const void *nr_grid_kernel_ptr_g32(int w4);
 const void *nr_grid_wide_kernel_ptr(int w4);
+const void *nr_bucket_wide_kernel_ptr(int w4);
 const void *nr_warp_kernel_ptr_g8(int w4);
 const void *nr_warp_kernel_ptr_g16(int w4);
 const void *nr_warp_kernel_ptr_g32(int w4);
@@ -716,8 +717,8 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     const size_t off_wc = off; off = align16(off + sizeof(unsigned long long) * (max_waves + 1));
     const size_t off_bar = off; off = align16(off + 4 * sizeof(unsigned));
     const size_t off_part = off; off = align16(off + sizeof(NrPartial) * grid);
-    const size_t off_wpart = off; off = align16(off + sizeof(NrFix) * 2 * grid);
-    const size_t off_stop = off; off = align16(off + sizeof(int));
+    const size_t off_wpart = off; off = align16(off + sizeof(NrWideShare) * 2 * grid);
+    const size_t off_stop = off; off = align16(off + 2 * sizeof(int));
     rc = ensure(&c->sbuf, &c->sbytes, off);
     if (rc) return rc;
     unsigned char *sb = static_cast<unsigned char *>(c->sbuf);
@@ -740,9 +741,10 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
     P.target_on = o->target_width > 0 ? 1 : 0;
     P.target_fix = nr_fix_of(o->target_width > 0 ? o->target_width : 0.0);
-    P.wpart = reinterpret_cast<NrFix *>(sb + off_wpart);
+    P.max_nodes = o->max_nodes;
+    P.wpart = reinterpret_cast<NrWideShare *>(sb + off_wpart);
     P.stop_wave = reinterpret_cast<int *>(sb + off_stop);
-    const int minus_one = -1;
+    const int stop_init[2] = {-1, 0};
     std::vector<uint32_t> root(4 * W4, 0);
     nr_initial_mask(g, root.data(), 4 * W4);
     const double one = 1.0;
@@ -753,7 +755,7 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     NR_CUDA_TRY(cudaMemcpyAsync(P.wave_count, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaMemcpyAsync(P.mask[0], root.data(), 16 * W4, cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaMemcpyAsync(P.mass[0], &one, sizeof(one), cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemcpyAsync(P.stop_wave, &minus_one, sizeof(int), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.stop_wave, stop_init, sizeof(stop_init), cudaMemcpyHostToDevice, s));
     void *args[] = {&P};
     NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
     NR_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(block), args, smem, s));
@@ -765,8 +767,8 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
                                 cudaMemcpyDeviceToHost, s));
     NR_CUDA_TRY(cudaMemcpyAsync(parts.data(), P.partials, sizeof(NrPartial) * grid, cudaMemcpyDeviceToHost, s));
     NR_CUDA_TRY(cudaMemcpyAsync(&status, P.status, sizeof(int), cudaMemcpyDeviceToHost, s));
-    int stop_wave = -1;
-    NR_CUDA_TRY(cudaMemcpyAsync(&stop_wave, P.stop_wave, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int stop_out[2] = {-1, 0};
+    NR_CUDA_TRY(cudaMemcpyAsync(stop_out, P.stop_wave, sizeof(stop_out), cudaMemcpyDeviceToHost, s));
     NR_CUDA_TRY(cudaStreamSynchronize(s));
     float ms = 0.f;
     NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
@@ -779,7 +781,8 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
         nr_fix_add(esp, pp.q);      // still queued at a target stop
         nodes += pp.nodes; leaves += pp.leaves; dead += pp.dead; trunc += pp.truncated; spilled += pp.spilled;
     }
-    // waves run (a target stop leaves wave stop_wave queued, not run)
+    // waves run (a stop leaves wave stop_wave queued, not run)
+    const int stop_wave = stop_out[0];
     int waves = 0;
     unsigned long long maxw = 0, queued = 0;
     const int last = stop_wave >= 0 ? stop_wave : max_waves + 1;
@@ -797,22 +800,175 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     r->nodes = nodes; r->leaves = leaves; r->dead_ends = dead; r->truncated = trunc; r->spilled = spilled;
     r->paths = leaves + spilled;
     r->queued = queued;
-    r->stop = stop_wave >= 0 ? 1 : 0;
+    r->stop = stop_wave >= 0 ? stop_out[1] : 0;
     r->iterations = waves;
     r->max_queue_items = maxw;
     r->item_bytes = (int)item_bytes;
     r->max_queue_mb = (double)maxw * item_bytes / (1024.0 * 1024.0);
     r->ms = ms;
-    if (stop_wave >= 0) r->time_to_bound_ms = ms;
+    if (stop_wave >= 0 && stop_out[1] == 1) r->time_to_bound_ms = ms;
     r->engine = NR_ENGINE_GRID;
     r->grid_blocks = grid;
     r->block_threads = block;
     r->capacity = cap;
-    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one) + sizeof(int);
-    r->d2h_bytes = sizeof(unsigned long long) * wc.size() + sizeof(NrPartial) * grid + 2 * sizeof(int);
+    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one) + sizeof(stop_init);
+    r->d2h_bytes = sizeof(unsigned long long) * wc.size() + sizeof(NrPartial) * grid + 3 * sizeof(int);
     if (status & NR_DEV_ERR_TIMEOUT) return NR_ERR_TIMEOUT;
     if (status) return NR_ERR_INTERNAL;
     return NR_OK;
+}
+
+// Whole-GPU bucketed max-mass queue (nr_bucket_wide_kernel) over an arena of
+// `cap` slots: 2^shift buckets per factor of two in mass, nb buckets.
+static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
+                           nr_result *r)
+{
+    if (g->n_nodes > NR_WIDE_MAX_N || g->n_edges > 65535) return NR_ERR_UNSUPPORTED;
+    cap = std::max<uint64_t>(64, std::min<uint64_t>(cap, 0xffffffffull));   // slot ids are 32-bit
+    const int nb = std::max(1, std::min(NR_WIDE_MAX_NB, o->n_buckets > 0 ? (int)o->n_buckets : NR_WIDE_MAX_NB));
+    NrWideGraph wg;
+    std::vector<unsigned char> blob;
+    build_wide_blob(g, src, dst, &wg, &blob);
+    const int W4 = wg.w4;
+    if (W4 > NR_WIDE_MAX_W4) return NR_ERR_UNSUPPORTED;
+    const void *kfn = nr_bucket_wide_kernel_ptr(W4);
+    if (!kfn) return NR_ERR_UNSUPPORTED;
+    const int block = NR_WIDE_BLOCK;
+    const size_t smem = (size_t)wg.blob_bytes + (block / 32) * nr_wide_warp_shm(wg.n, W4);
+    NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int bps = 0;
+    NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
+    if (bps < 1) return NR_ERR_UNSUPPORTED;
+    if (o->blocks_per_sm > 0 && o->blocks_per_sm < bps) bps = o->blocks_per_sm;
+    const int grid = bps * c->sms;
+    const size_t item_bytes = (size_t)W4 * 16 + sizeof(double) + 1;
+    // arena: masks, masses, bucket bytes, wave list
+    const size_t mask_bytes = align16((size_t)cap * W4 * 16);
+    const size_t mass_bytes = align16((size_t)cap * sizeof(double));
+    const size_t key_bytes = align16((size_t)cap);
+    const size_t list_bytes = align16((size_t)cap * sizeof(unsigned));
+    const size_t qneed = mask_bytes + mass_bytes + key_bytes + list_bytes;
+    size_t free_b = 0, total_b = 0;
+    NR_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    if (qneed > c->qbytes && qneed > free_b + c->qbytes) return NR_ERR_NOMEM;
+    int rc = ensure(&c->qbuf, &c->qbytes, qneed);
+    if (rc) return rc;
+    size_t off = 0;
+    const size_t off_blob = off; off = align16(off + blob.size());
+    const size_t off_zero = off;                                   // zeroed from here on
+    const size_t off_top = off; off = align16(off + sizeof(unsigned long long));
+    const size_t off_bc = off; off = align16(off + sizeof(unsigned long long) * nb);
+    const size_t off_wl = off; off = align16(off + sizeof(unsigned long long) * 2);
+    const size_t off_cc = off; off = align16(off + sizeof(unsigned long long) * 2 * grid);
+    const size_t off_bar = off; off = align16(off + 4 * sizeof(unsigned));
+    const size_t off_part = off; off = align16(off + sizeof(NrPartial) * grid);
+    const size_t off_wpart = off; off = align16(off + sizeof(NrWideShare) * 2 * grid);
+    const size_t off_info = off; off = align16(off + 3 * sizeof(int));
+    const size_t off_stats = off; off = align16(off + 2 * sizeof(unsigned long long));
+    rc = ensure(&c->sbuf, &c->sbytes, off);
+    if (rc) return rc;
+    unsigned char *sb = static_cast<unsigned char *>(c->sbuf);
+    unsigned char *qb = static_cast<unsigned char *>(c->qbuf);
+    NrBucketWideParams P;
+    P.g = wg;
+    P.blob = sb + off_blob;
+    P.mask = reinterpret_cast<uint4 *>(qb);
+    P.mass = reinterpret_cast<double *>(qb + mask_bytes);
+    P.key = qb + mask_bytes + mass_bytes;
+    P.list = reinterpret_cast<unsigned *>(qb + mask_bytes + mass_bytes + key_bytes);
+    P.capacity = cap;
+    P.top = reinterpret_cast<unsigned long long *>(sb + off_top);
+    P.bcount = reinterpret_cast<unsigned long long *>(sb + off_bc);
+    P.wave_len = reinterpret_cast<unsigned long long *>(sb + off_wl);
+    P.ccount = reinterpret_cast<unsigned long long *>(sb + off_cc);
+    P.shift = std::max(0, (int)o->bucket_shift);
+    P.nb = nb;
+    P.max_waves = 1 << 30;
+    P.bar_count = reinterpret_cast<unsigned *>(sb + off_bar);
+    P.bar_gen = P.bar_count + 1;
+    P.status = reinterpret_cast<int *>(P.bar_count + 2);
+    P.partials = reinterpret_cast<NrPartial *>(sb + off_part);
+    P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
+    P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
+    P.target_on = o->target_width > 0 ? 1 : 0;
+    P.target_fix = nr_fix_of(o->target_width > 0 ? o->target_width : 0.0);
+    P.max_nodes = o->max_nodes;
+    P.wpart = reinterpret_cast<NrWideShare *>(sb + off_wpart);
+    P.stop_info = reinterpret_cast<int *>(sb + off_info);
+    P.stats = reinterpret_cast<unsigned long long *>(sb + off_stats);
+    // the root: initial mask with mass 1 (main.cu:805-809) in slot 0, bucket 0 (mass 1 is the top bucket)
+    std::vector<uint32_t> root(4 * W4, 0);
+    nr_initial_mask(g, root.data(), 4 * W4);
+    const double one = 1.0;
+    const unsigned long long one_u = 1;
+    const unsigned char bucket0 = 0;
+    cudaStream_t s = c->stream;
+    NR_CUDA_TRY(cudaMemcpyAsync(sb + off_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemsetAsync(sb + off_zero, 0, off - off_zero, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.top, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.bcount, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.mask, root.data(), 16 * W4, cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.mass, &one, sizeof(one), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.key, &bucket0, 1, cudaMemcpyHostToDevice, s));
+    void *args[] = {&P};
+    NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
+    NR_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(block), args, smem, s));
+    NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
+    std::vector<NrPartial> parts(grid);
+    int status = 0, info[3] = {0, 0, 0};
+    unsigned long long stats[2] = {0, 0};
+    NR_CUDA_TRY(cudaMemcpyAsync(parts.data(), P.partials, sizeof(NrPartial) * grid, cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(&status, P.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(info, P.stop_info, sizeof(info), cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(stats, P.stats, sizeof(stats), cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    NrFix R = nr_fix_zero(), esp = nr_fix_zero();
+    unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0;
+    for (const NrPartial &pp : parts) {          // exact: the order of the additions does not matter
+        nr_fix_add(R, pp.R);
+        nr_fix_add(esp, pp.et);
+        nr_fix_add(esp, pp.es);
+        nr_fix_add(esp, pp.q);                   // still queued
+        nodes += pp.nodes; leaves += pp.leaves; dead += pp.dead; trunc += pp.truncated; spilled += pp.spilled;
+    }
+    r->R = nr_fix_to_double_host(R);
+    r->esp = nr_fix_to_double_host(esp);
+    r->R_plus_esp = r->R + r->esp;
+    r->trunc_bound = r->R > 0 ? r->esp / r->R : r->esp;
+    r->nodes = nodes; r->leaves = leaves; r->dead_ends = dead; r->truncated = trunc; r->spilled = spilled;
+    r->paths = leaves + spilled;
+    r->queued = stats[1];
+    r->stop = info[1];
+    r->iterations = info[0];
+    r->max_queue_items = stats[0];
+    r->item_bytes = (int)item_bytes;
+    r->max_queue_mb = (double)stats[0] * item_bytes / (1024.0 * 1024.0);
+    r->ms = ms;
+    if (info[1] == 1) r->time_to_bound_ms = ms;
+    r->engine = NR_ENGINE_GRID;
+    r->grid_blocks = grid;
+    r->block_threads = block;
+    r->capacity = cap;
+    r->h2d_bytes = blob.size() + 2 * sizeof(one_u) + 16 * W4 + sizeof(one) + 1;
+    r->d2h_bytes = sizeof(NrPartial) * grid + sizeof(int) + sizeof(info) + sizeof(stats);
+    if (status & NR_DEV_ERR_TIMEOUT) return NR_ERR_TIMEOUT;
+    if (status) return NR_ERR_INTERNAL;
+    return NR_OK;
+}
+
+// 33..1024 nodes: the bucketed max-mass queue for the max-mass order (and for a target width
+// in the default order) with a bucket shift >= 0, else breadth-first waves.  The learned
+// order is n <= 32 only.
+static int run_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t capacity, const nr_options *o,
+                    nr_result *r)
+{
+    if (o->order == NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
+    const bool buckets = o->bucket_shift >= 0 &&
+                         (o->order == NR_ORDER_MAXMASS || (o->order == NR_ORDER_AUTO && o->target_width > 0));
+    if (buckets) return run_bucket_wide(c, g, src, dst, capacity ? capacity : (1u << 22), o, r);
+    return run_grid_wide(c, g, src, dst, capacity ? capacity : (1u << 20), o, r);
 }
 
 // ---------------------------------------------------------------------------
@@ -1128,7 +1284,7 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
         memset(&res[i], 0, sizeof(nr_result));
         int rc = validate(&gs[i], srcs[i], dsts[i]);
         if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) {
-            if (!wave_order) rc = NR_ERR_UNSUPPORTED;    // max-mass and learned orders: n <= 32 only
+            if (o.order == NR_ORDER_LEARNED) rc = NR_ERR_UNSUPPORTED;    // learned order: n <= 32 only
             n_wide.fetch_add(1);
         }
         if (rc) bad.store(rc);
@@ -1171,7 +1327,7 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
         nr_result *r = &res[i];
         r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
-        rc = run_grid_wide(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, r);
+        rc = run_wide(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, r);
         if (rc) return rc;
     }
     return NR_OK;
@@ -1328,12 +1484,7 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     res->mask_words = std::max(1, (2 * g->n_edges + 31) / 32);
     std::lock_guard<std::mutex> lock(c->mu);
     NR_CUDA_TRY(cudaSetDevice(c->device));
-    if (g->n_nodes > NR_SMALL_MAX_N) {
-        // 33..1024 nodes: whole-GPU wave engine, breadth-first waves (a target width stops it
-        // between waves); the max-mass and learned orders are n <= 32 only
-        if (o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
-        return run_grid_wide(c, g, src, dst, capacity ? capacity : (1u << 20), &o, res);
-    }
+    if (g->n_nodes > NR_SMALL_MAX_N) return run_wide(c, g, src, dst, capacity, &o, res);
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {
         // bucketed max-mass (or learned) order: one warp owns the instance (nr_warp.cuh)
         if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;

@@ -210,6 +210,19 @@ __device__ __forceinline__ NrFix nr_block_fix_sum(NrFix v)
     return t;
 }
 
+// Bucket of a mass: 2^shift buckets per factor of two, highest masses first;
+// the last bucket takes every smaller mass.  Shift < 0 or one bucket: 0.
+__device__ __forceinline__ int nr_bucket(double m, int shift, int nb)
+{
+    if (shift < 0 || nb <= 1) return 0;
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(m);
+    const long long key = (long long)(bits >> (52 - shift));
+    long long b = (1023LL << shift) - key;
+    b = b < 0 ? 0 : b;
+    b = b > nb - 1 ? nb - 1 : b;
+    return (int)b;
+}
+
 // Stage the graph tables into shared memory (16-byte copies; blob_bytes is a multiple of 16).
 __device__ __forceinline__ void nr_stage_blob(unsigned char *dst, const unsigned char *src, int bytes)
 {

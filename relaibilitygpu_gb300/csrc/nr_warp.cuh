@@ -68,17 +68,6 @@ struct NrWarpParams {
     int dump_stride;
 };
 
-__device__ __forceinline__ int nr_bucket(double m, int shift, int nb)
-{
-    if (shift < 0 || nb <= 1) return 0;
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(m);
-    const long long key = (long long)(bits >> (52 - shift));
-    long long b = (1023LL << shift) - key;
-    b = b < 0 ? 0 : b;
-    b = b > nb - 1 ? nb - 1 : b;
-    return (int)b;
-}
-
 __device__ __forceinline__ unsigned long long nr_warp_sum_u64(unsigned long long x)
 {
     for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(NR_FULL, x, off);

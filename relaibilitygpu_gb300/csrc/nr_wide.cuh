@@ -10,15 +10,25 @@
 // (workingPad/device_code.cuh:165-170).  There is no path-length cap (the
 // reference stops at 32 nodes, workingPad/main.cu:152).  Children are
 // emitted in hop order with the lanes owning mask words, so every child
-// record is written with coalesced stores.  Waves, the grid barrier, the
-// wave counters and the block partials work as in nr_grid.cuh.
+// record is written with coalesced stores.
 //
-// With a target width the run stops before the first wave at which
-// ESP + queued mass <= target (the oracle's wave schedule with one bucket):
-// at the end of a wave every block writes its exact share of that width
-// (its ESP so far plus the mass it pushed) to one of two alternating slots,
-// and after the grid barrier every block adds all shares and takes the same
-// decision.  The pushed mass of the last wave run is the queued mass at the stop.
+// Two schedules share that step (nr_wide_step):
+//  * nr_grid_wide_kernel -- breadth-first waves in ping-pong buffers, as the
+//    reference's host loop (main.cu:963-1008), with the grid barrier, wave
+//    counters and block partials of nr_grid.cuh;
+//  * nr_bucket_wide_kernel -- the bucketed max-mass queue: records live in
+//    one HBM arena with a bucket byte each (2^shift buckets per factor of two
+//    in mass); every wave takes the whole highest non-empty bucket (a scan of
+//    the bucket bytes gathers its slots) and children are appended to the
+//    arena.  Slots freed by earlier waves are reclaimed by an in-place
+//    compaction once they are a large part of the used arena.
+//
+// A target width stops either schedule before the first wave at which
+// ESP + queued mass <= target (the oracle's wave schedule): at the end of a
+// wave every block writes its exact share of that width (its ESP so far plus
+// the mass it queued minus the mass it popped) to one of two alternating
+// slots, and after the grid barrier every block adds all shares and takes the
+// same decision.  The shares also carry node counts, for a node budget.
 #pragma once
 
 #include "nr_expand.cuh"
@@ -26,12 +36,21 @@
 #define NR_WIDE_MAX_N 1024
 #define NR_WIDE_MAX_W4 16
 #define NR_WIDE_BLOCK 128
+#define NR_WIDE_MAX_NB 255      // bucket schedule: bucket ids fit a byte
+#define NR_WIDE_FREE 0xffu      // bucket byte of a free arena slot
 
 // Graph tables of one wide instance: p[E], q[E] (double), row_ptr[n+1] (int),
 // arcs[n_arcs] (u32 = eid << 10 | head).  Offsets from the blob start, 16-byte aligned.
 struct NrWideGraph {
     int n, e, w4, src, dst, n_arcs, nwd;
     int off_p, off_q, off_row, off_arc, blob_bytes;
+};
+
+// A block's share of the stop test, written at the end of each wave.
+struct NrWideShare {
+    NrFix width;                // ESP so far + (mass queued - mass popped)
+    unsigned long long nodes;   // subproblems popped so far
+    unsigned long long pad;
 };
 
 struct NrGridWideParams {
@@ -48,10 +67,38 @@ struct NrGridWideParams {
     NrPartial *partials;
     double eps;
     long long timeout_ns;
-    int target_on;              // stop at ESP + queued <= target_fix
+    int target_on;                  // stop at ESP + queued <= target_fix
     NrFix target_fix;
-    NrFix *wpart;               // [2][gridDim.x] per-block width shares, alternating slots
-    int *stop_wave;             // waves run before the target stop, or -1
+    unsigned long long max_nodes;   // stop once this many subproblems were popped (0 = no budget)
+    NrWideShare *wpart;             // [2][gridDim.x] per-block shares, alternating slots
+    int *stop_wave;                 // [0] waves run before a stop (or -1), [1] stop reason
+};
+
+struct NrBucketWideParams {
+    NrWideGraph g;
+    const unsigned char *blob;
+    uint4 *mask;                    // arena [capacity][w4]
+    double *mass;                   // arena [capacity]
+    unsigned char *key;             // arena [capacity]: bucket, or NR_WIDE_FREE
+    unsigned *list;                 // [capacity]: slots of the running wave; compaction scratch
+    unsigned long long capacity;
+    unsigned long long *top;        // arena slots handed out (slots >= capacity were spilled)
+    unsigned long long *bcount;     // [nb] records per bucket
+    unsigned long long *wave_len;   // [2] gathered slots, alternating
+    unsigned long long *ccount;     // [2][gridDim.x] compaction counts
+    int shift, nb, max_waves;
+    unsigned *bar_count;
+    unsigned *bar_gen;
+    int *status;
+    NrPartial *partials;
+    double eps;
+    long long timeout_ns;
+    int target_on;
+    NrFix target_fix;
+    unsigned long long max_nodes;
+    NrWideShare *wpart;
+    int *stop_info;                 // [0] waves run, [1] stop reason (0 empty, 1 target, 3 budget), [2] compactions
+    unsigned long long *stats;      // [0] widest wave, [1] records queued at the end
 };
 
 // per-warp shared memory: mask words, frontier / next / visited bitmasks,
@@ -62,213 +109,490 @@ __host__ __device__ inline size_t nr_wide_warp_shm(int n, int w4)
     return ((((size_t)4 * w4 + 3 * 32 + 3 * (size_t)n) * 4) + 15) & ~(size_t)15;
 }
 
+// Where a step's children go.
+struct NrWideOut {
+    uint4 *mask;
+    double *mass;
+    unsigned char *key;              // bucket schedule: bucket byte of each record, else nullptr
+    unsigned long long *count;       // slots handed out so far; slots >= cap spill
+    unsigned long long cap;
+    int shift, nb;
+    unsigned *hist;                  // bucket schedule: this block's new records per bucket (shared memory)
+};
+
+// Lane-0 accumulators of a warp.
+struct NrWideAcc {
+    NrFix R, et, es;
+    NrFix net;                       // mass queued minus mass popped
+    unsigned long long nodes, leaves, dead, trunc, spilled;
+};
+
+struct NrWideView {
+    const double *p, *q;
+    const int *row;
+    const uint32_t *arc;
+    uint32_t *m, *F, *NF, *VIS, *par, *list, *hops;
+};
+
+template <int W4>
+__device__ __forceinline__ NrWideView nr_wide_view(unsigned char *smem, const NrWideGraph &g)
+{
+    constexpr int NW = 4 * W4;
+    NrWideView v;
+    v.p = reinterpret_cast<const double *>(smem + g.off_p);
+    v.q = reinterpret_cast<const double *>(smem + g.off_q);
+    v.row = reinterpret_cast<const int *>(smem + g.off_row);
+    v.arc = reinterpret_cast<const uint32_t *>(smem + g.off_arc);
+    const int warp = threadIdx.x >> 5;
+    uint32_t *ws = reinterpret_cast<uint32_t *>(smem + g.blob_bytes + (size_t)warp * nr_wide_warp_shm(g.n, W4));
+    v.m = ws;                        // [NW] mask words of the current subproblem
+    v.F = v.m + NW;                  // [32] frontier
+    v.NF = v.F + 32;                 // [32] next frontier
+    v.VIS = v.NF + 32;               // [32] visited
+    v.par = v.VIS + 32;              // [n] (parent << 16) | edge
+    v.list = v.par + g.n;            // [n] frontier nodes
+    v.hops = v.list + g.n;           // [n] path edges, dst side first
+    return v;
+}
+
+// Pop of one subproblem whose mask words are in v.m: count it, truncate it
+// below eps, else BFS, and on a path emit the branches and the all-up leaf.
+// All 32 lanes call it; the accumulators live on lane 0.
+template <int W4>
+__device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideView &v, double mass, double eps,
+                                             const NrWideOut &O, NrWideAcc &A)
+{
+    constexpr int NW = 4 * W4;
+    const int lane = threadIdx.x & 31;
+    const int n = g.n, nwd = g.nwd, src = g.src, dst = g.dst;
+    uint32_t *m = v.m, *F = v.F, *NF = v.NF, *VIS = v.VIS, *par = v.par, *list = v.list, *hops = v.hops;
+    if (lane == 0) {
+        A.nodes++;
+        nr_fix_sub(A.net, nr_fix_of(mass));
+    }
+    __syncwarp();
+    if (eps > 0.0 && mass < eps) {          // main.cu:537-543
+        if (lane == 0) { A.trunc++; nr_fix_add_mass(A.et, mass); }
+        __syncwarp();
+        return;
+    }
+    // ---- BFS from src over not-down arcs ----
+    for (int i = lane; i < nwd; i += 32) {
+        VIS[i] = 0u;
+        F[i] = 0u;
+    }
+    for (int i = lane; i < n; i += 32) par[i] = 0xffffffffu;
+    __syncwarp();
+    if (lane == 0) {
+        VIS[src >> 5] = 1u << (src & 31);
+        F[src >> 5] = 1u << (src & 31);
+    }
+    __syncwarp();
+    bool found = (src == dst);
+    int L = 0;
+    while (!found) {
+        // compact the frontier into list[]
+        const uint32_t fw = (lane < nwd) ? F[lane] : 0u;
+        const int cnt = __popc(fw);
+        int pre = cnt;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int t = __shfl_up_sync(NR_FULL, pre, off);
+            if (lane >= off) pre += t;
+        }
+        const int total = __shfl_sync(NR_FULL, pre, 31);
+        if (total == 0) break;
+        int o = pre - cnt;
+        for (uint32_t b = fw; b; b &= b - 1) list[o++] = (uint32_t)(lane * 32 + __ffs(b) - 1);
+        for (int i = lane; i < nwd; i += 32) NF[i] = 0u;
+        __syncwarp();
+        for (int i = lane; i < total; i += 32) {
+            const uint32_t u = list[i];
+            for (int j = v.row[u]; j < v.row[u + 1]; ++j) {
+                const uint32_t a = v.arc[j];
+                const uint32_t w = a & 1023u, e = a >> 10;
+                if (((m[e >> 4] >> ((e & 15) << 1)) & 1u) && !((VIS[w >> 5] >> (w & 31)) & 1u)) {
+                    atomicOr(&NF[w >> 5], 1u << (w & 31));
+                    atomicMin(&par[w], (u << 16) | e);
+                }
+            }
+        }
+        __syncwarp();
+        bool any = false;
+        for (int i = lane; i < nwd; i += 32) {
+            const uint32_t nf = NF[i];
+            VIS[i] |= nf;
+            F[i] = nf;
+            any = any || nf != 0u;
+        }
+        __syncwarp();
+        ++L;
+        found = (VIS[dst >> 5] >> (dst & 31)) & 1u;
+        if (!__any_sync(NR_FULL, any)) break;
+    }
+    if (!found) {
+        if (lane == 0) A.dead++;
+        __syncwarp();
+        return;
+    }
+    // ---- path: hops[] from dst back to src (L hops) ----
+    if (lane == 0) {
+        int w = dst, h = 0;
+        while (w != src && h < n) {
+            const uint32_t pe = par[w];
+            hops[h++] = pe & 0xffffu;
+            w = (int)(pe >> 16);
+        }
+        L = h;
+    }
+    L = __shfl_sync(NR_FULL, L, 0);
+    __syncwarp();
+    // number of UNKNOWN hops -> one slot range for all children
+    int unk = 0;
+    for (int h = lane; h < L; h += 32) {
+        const uint32_t e = hops[h];
+        unk += ((m[e >> 4] >> ((e & 15) << 1)) & 3u) == 3u;
+    }
+    for (int off = 16; off > 0; off >>= 1) unk += __shfl_xor_sync(NR_FULL, unk, off);
+    unsigned long long base = 0;
+    if (lane == 0 && unk > 0) base = atomicAdd(O.count, (unsigned long long)unk);
+    base = __shfl_sync(NR_FULL, base, 0);
+    // children in hop order, src side first; lanes own mask words
+    uint32_t w0 = (lane < NW) ? m[lane] : 0u;
+    uint32_t w1 = (lane + 32 < NW) ? m[lane + 32] : 0u;
+    double Pm = mass;
+    int k = 0;
+    for (int h = L - 1; h >= 0; --h) {
+        const uint32_t e = hops[h];
+        const int sh = (int)(e & 15u) << 1;
+        const int wi = (int)(e >> 4);
+        if (((m[wi] >> sh) & 3u) != 3u) continue;          // only UNKNOWN hops branch
+        const unsigned long long slot = base + (unsigned long long)k;
+        const double cm = __dmul_rn(Pm, v.q[e]);
+        if (slot < O.cap) {
+            uint32_t *dstw = reinterpret_cast<uint32_t *>(O.mask + slot * W4);
+            if (lane < NW) __stcg(dstw + lane, (lane == wi) ? (w0 & ~(3u << sh)) : w0);
+            if (lane + 32 < NW) __stcg(dstw + lane + 32, (lane + 32 == wi) ? (w1 & ~(3u << sh)) : w1);
+            if (lane == 0) {
+                __stcg(O.mass + slot, cm);
+                nr_fix_add_mass(A.net, cm);
+                if (O.key) {
+                    const int b = nr_bucket(cm, O.shift, O.nb);
+                    __stcg(O.key + slot, (unsigned char)b);
+                    atomicAdd(&O.hist[b], 1u);
+                }
+            }
+        } else if (lane == 0) {                             // queue full (main.cu:245-252)
+            A.spilled++;
+            nr_fix_add_mass(A.es, cm);
+        }
+        if (lane == wi) w0 &= ~(2u << sh);                  // this hop is up in later children
+        if (lane + 32 == wi) w1 &= ~(2u << sh);
+        Pm = __dmul_rn(Pm, v.p[e]);
+        ++k;
+    }
+    if (lane == 0) { A.leaves++; nr_fix_add_mass(A.R, Pm); }
+    __syncwarp();
+}
+
+__device__ __forceinline__ void nr_wide_acc_init(NrWideAcc &A)
+{
+    A.R = A.et = A.es = nr_fix_zero();
+    // the root is queued before the first wave: block 0's first lane holds its mass
+    A.net = (blockIdx.x == 0 && threadIdx.x == 0) ? nr_fix_of(1.0) : nr_fix_zero();
+    A.nodes = A.leaves = A.dead = A.trunc = A.spilled = 0;
+}
+
+// Sum over the block of a per-thread count, on every thread.
+__device__ __forceinline__ unsigned long long nr_block_u64_sum(unsigned long long x)
+{
+    __shared__ unsigned long long s_x[32];
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(NR_FULL, x, off);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_x[threadIdx.x >> 5] = x;
+    __syncthreads();
+    unsigned long long t = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += s_x[i];
+    return t;
+}
+
+// This block's share of the stop test after a wave (all threads call it).
+__device__ __forceinline__ void nr_wide_write_share(NrWideShare *slot, const NrWideAcc &A)
+{
+    NrFix w = nr_fix_zero();
+    unsigned long long nodes = 0;
+    if ((threadIdx.x & 31) == 0) {
+        w = A.et;
+        nr_fix_add(w, A.es);
+        nr_fix_add(w, A.net);
+        nodes = A.nodes;
+    }
+    w = nr_block_fix_sum(w);
+    nodes = nr_block_u64_sum(nodes);
+    if (threadIdx.x == 0) {
+        NrWideShare *d = slot + blockIdx.x;
+        __stcg(&d->width.w0, w.w0);
+        __stcg(&d->width.w1, w.w1);
+        __stcg(&d->width.w2, w.w2);
+        __stcg(&d->nodes, nodes);
+    }
+}
+
+// Stop test before a wave from the shares of the last one (every block gets
+// the same answer): 0 go on, 1 target width met, 3 node budget reached.
+__device__ __forceinline__ int nr_wide_stop_test(const NrWideShare *slot, bool first, int target_on,
+                                                 const NrFix &target_fix, unsigned long long max_nodes)
+{
+    if (!target_on && !max_nodes) return 0;
+    NrFix width = nr_fix_zero();
+    unsigned long long nodes = 0;
+    if (first) {
+        if (threadIdx.x == 0) width = nr_fix_of(1.0);      // the root alone is queued
+    } else {
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+            NrFix v;                                       // written by other blocks: read from L2
+            v.w0 = __ldcg(&slot[b].width.w0);
+            v.w1 = __ldcg(&slot[b].width.w1);
+            v.w2 = __ldcg(&slot[b].width.w2);
+            nr_fix_add(width, v);
+            nodes += __ldcg(&slot[b].nodes);
+        }
+    }
+    width = nr_block_fix_sum(width);
+    nodes = nr_block_u64_sum(nodes);
+    if (target_on && nr_fix_le(width, target_fix)) return 1;
+    if (max_nodes && nodes >= max_nodes) return 3;
+    return 0;
+}
+
 template <int W4>
 __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideParams P)
 {
-    constexpr int NW = 4 * W4;
     extern __shared__ __align__(16) unsigned char smem[];
     const NrWideGraph g = P.g;
     nr_stage_blob(smem, P.blob, g.blob_bytes);
     __syncthreads();
-    const double *p = reinterpret_cast<const double *>(smem + g.off_p);
-    const double *q = reinterpret_cast<const double *>(smem + g.off_q);
-    const int *row = reinterpret_cast<const int *>(smem + g.off_row);
-    const uint32_t *arc = reinterpret_cast<const uint32_t *>(smem + g.off_arc);
-
+    const NrWideView v = nr_wide_view<W4>(smem, g);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t *ws = reinterpret_cast<uint32_t *>(smem + g.blob_bytes + (size_t)warp * nr_wide_warp_shm(g.n, W4));
-    uint32_t *m = ws;                       // [NW] mask words of the current subproblem
-    uint32_t *F = m + NW;                   // [32] frontier
-    uint32_t *NF = F + 32;                  // [32] next frontier
-    uint32_t *VIS = NF + 32;                // [32] visited
-    uint32_t *par = VIS + 32;               // [n] (parent << 16) | edge
-    uint32_t *list = par + g.n;             // [n] frontier nodes
-    uint32_t *hops = list + g.n;            // [n] path edges, dst side first
-    const int n = g.n, nwd = g.nwd, src = g.src, dst = g.dst;
     const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const unsigned long long TW = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long cap = P.capacity;
-
-    NrFix R = nr_fix_zero(), et = nr_fix_zero(), es = nr_fix_zero();
-    // lane 0: mass this warp queued in the last wave run (the root counts as queued by
-    // block 0's first warp, for a stop before the first wave)
-    NrFix pushed = (blockIdx.x == 0 && threadIdx.x == 0) ? nr_fix_of(1.0) : nr_fix_zero();
-    unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0;
+    NrWideAcc A;
+    nr_wide_acc_init(A);
 
     for (int wave = 0; wave < P.max_waves; ++wave) {
         unsigned long long n_in = *(volatile unsigned long long *)&P.wave_count[wave];
         if (n_in > cap) n_in = cap;
         if (n_in == 0) break;
-        if (P.target_on) {
-            NrFix width = nr_fix_zero();
-            if (wave == 0) {
-                width = nr_fix_of(1.0);                         // the root alone is queued
-            } else {
-                const NrFix *slot = P.wpart + (size_t)((wave - 1) & 1) * gridDim.x;
-                for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-                    NrFix v;                                    // written by other blocks: read from L2
-                    v.w0 = __ldcg(&slot[b].w0);
-                    v.w1 = __ldcg(&slot[b].w1);
-                    v.w2 = __ldcg(&slot[b].w2);
-                    nr_fix_add(width, v);
-                }
-                width = nr_block_fix_sum(width);
-            }
-            if (nr_fix_le(width, P.target_fix)) {
-                if (threadIdx.x == 0 && blockIdx.x == 0) *P.stop_wave = wave;
-                break;
-            }
-            pushed = nr_fix_zero();
+        const int stop = nr_wide_stop_test(P.wpart + (size_t)((wave + 1) & 1) * gridDim.x, wave == 0,
+                                           P.target_on, P.target_fix, P.max_nodes);
+        if (stop) {
+            if (threadIdx.x == 0 && blockIdx.x == 0) { P.stop_wave[0] = wave; P.stop_wave[1] = stop; }
+            break;
         }
         const uint4 *in_mask = P.mask[wave & 1];
         const double *in_mass = P.mass[wave & 1];
-        uint4 *out_mask = P.mask[(wave + 1) & 1];
-        double *out_mass = P.mass[(wave + 1) & 1];
-        unsigned long long *out_count = &P.wave_count[wave + 1];
-
+        NrWideOut O;
+        O.mask = P.mask[(wave + 1) & 1];
+        O.mass = P.mass[(wave + 1) & 1];
+        O.key = nullptr;
+        O.count = &P.wave_count[wave + 1];
+        O.cap = cap;
+        O.shift = 0;
+        O.nb = 1;
+        O.hist = nullptr;
         for (unsigned long long idx = gw; idx < n_in; idx += TW) {
-            if (lane < W4) reinterpret_cast<uint4 *>(m)[lane] = __ldcg(in_mask + idx * W4 + lane);
+            if (lane < W4) reinterpret_cast<uint4 *>(v.m)[lane] = __ldcg(in_mask + idx * W4 + lane);
             const double mass = __ldcg(in_mass + idx);
-            if (lane == 0) nodes++;
             __syncwarp();
-            if (P.eps > 0.0 && mass < P.eps) {          // main.cu:537-543
-                if (lane == 0) { trunc++; nr_fix_add_mass(et, mass); }
-                __syncwarp();
-                continue;
-            }
-            // ---- BFS from src over not-down arcs ----
-            for (int i = lane; i < nwd; i += 32) {
-                VIS[i] = 0u;
-                F[i] = 0u;
-            }
-            for (int i = lane; i < n; i += 32) par[i] = 0xffffffffu;
-            __syncwarp();
-            if (lane == 0) {
-                VIS[src >> 5] = 1u << (src & 31);
-                F[src >> 5] = 1u << (src & 31);
-            }
-            __syncwarp();
-            bool found = (src == dst);
-            int L = 0;
-            while (!found) {
-                // compact the frontier into list[]
-                const uint32_t fw = (lane < nwd) ? F[lane] : 0u;
-                const int cnt = __popc(fw);
-                int pre = cnt;
-                for (int off = 1; off < 32; off <<= 1) {
-                    const int t = __shfl_up_sync(NR_FULL, pre, off);
-                    if (lane >= off) pre += t;
-                }
-                const int total = __shfl_sync(NR_FULL, pre, 31);
-                if (total == 0) break;
-                int o = pre - cnt;
-                for (uint32_t b = fw; b; b &= b - 1) list[o++] = (uint32_t)(lane * 32 + __ffs(b) - 1);
-                for (int i = lane; i < nwd; i += 32) NF[i] = 0u;
-                __syncwarp();
-                for (int i = lane; i < total; i += 32) {
-                    const uint32_t u = list[i];
-                    for (int j = row[u]; j < row[u + 1]; ++j) {
-                        const uint32_t a = arc[j];
-                        const uint32_t v = a & 1023u, e = a >> 10;
-                        if (((m[e >> 4] >> ((e & 15) << 1)) & 1u) && !((VIS[v >> 5] >> (v & 31)) & 1u)) {
-                            atomicOr(&NF[v >> 5], 1u << (v & 31));
-                            atomicMin(&par[v], (u << 16) | e);
-                        }
-                    }
-                }
-                __syncwarp();
-                bool any = false;
-                for (int i = lane; i < nwd; i += 32) {
-                    const uint32_t nf = NF[i];
-                    VIS[i] |= nf;
-                    F[i] = nf;
-                    any = any || nf != 0u;
-                }
-                __syncwarp();
-                ++L;
-                found = (VIS[dst >> 5] >> (dst & 31)) & 1u;
-                if (!__any_sync(NR_FULL, any)) break;
-            }
-            if (!found) {
-                if (lane == 0) dead++;
-                __syncwarp();
-                continue;
-            }
-            // ---- path: hops[] from dst back to src (L hops) ----
-            if (lane == 0) {
-                int v = dst, h = 0;
-                while (v != src && h < n) {
-                    const uint32_t pe = par[v];
-                    hops[h++] = pe & 0xffffu;
-                    v = (int)(pe >> 16);
-                }
-                L = h;
-            }
-            L = __shfl_sync(NR_FULL, L, 0);
-            __syncwarp();
-            // number of UNKNOWN hops -> one slot range for all children
-            int unk = 0;
-            for (int h = lane; h < L; h += 32) {
-                const uint32_t e = hops[h];
-                unk += ((m[e >> 4] >> ((e & 15) << 1)) & 3u) == 3u;
-            }
-            for (int off = 16; off > 0; off >>= 1) unk += __shfl_xor_sync(NR_FULL, unk, off);
-            unsigned long long base = 0;
-            if (lane == 0 && unk > 0) base = atomicAdd(out_count, (unsigned long long)unk);
-            base = __shfl_sync(NR_FULL, base, 0);
-            // children in hop order, src side first; lanes own mask words
-            uint32_t w0 = (lane < NW) ? m[lane] : 0u;
-            uint32_t w1 = (lane + 32 < NW) ? m[lane + 32] : 0u;
-            double Pm = mass;
-            int k = 0;
-            for (int h = L - 1; h >= 0; --h) {
-                const uint32_t e = hops[h];
-                const int sh = (int)(e & 15u) << 1;
-                const int wi = (int)(e >> 4);
-                if (((m[wi] >> sh) & 3u) != 3u) continue;          // only UNKNOWN hops branch
-                const unsigned long long slot = base + (unsigned long long)k;
-                const double cm = __dmul_rn(Pm, q[e]);
-                if (slot < cap) {
-                    uint32_t *dstw = reinterpret_cast<uint32_t *>(out_mask + slot * W4);
-                    if (lane < NW) __stcg(dstw + lane, (lane == wi) ? (w0 & ~(3u << sh)) : w0);
-                    if (lane + 32 < NW) __stcg(dstw + lane + 32, (lane + 32 == wi) ? (w1 & ~(3u << sh)) : w1);
-                    if (lane == 0) {
-                        __stcg(out_mass + slot, cm);
-                        if (P.target_on) nr_fix_add_mass(pushed, cm);
-                    }
-                } else if (lane == 0) {                             // queue full (main.cu:245-252)
-                    spilled++;
-                    nr_fix_add_mass(es, cm);
-                }
-                if (lane == wi) w0 &= ~(2u << sh);                  // this hop is up in later children
-                if (lane + 32 == wi) w1 &= ~(2u << sh);
-                Pm = __dmul_rn(Pm, p[e]);
-                ++k;
-            }
-            if (lane == 0) { leaves++; nr_fix_add_mass(R, Pm); }
-            __syncwarp();
+            nr_wide_step<W4>(g, v, mass, P.eps, O, A);
         }
-        if (P.target_on) {
-            // this block's share of the width after the wave: ESP so far + mass it queued
-            NrFix share = nr_fix_zero();
-            if (lane == 0) {
-                share = et;
-                nr_fix_add(share, es);
-                nr_fix_add(share, pushed);
-            }
-            share = nr_block_fix_sum(share);
-            if (threadIdx.x == 0) {
-                NrFix *dst = P.wpart + (size_t)(wave & 1) * gridDim.x + blockIdx.x;
-                __stcg(&dst->w0, share.w0);
-                __stcg(&dst->w1, share.w1);
-                __stcg(&dst->w2, share.w2);
-            }
-        }
+        if (P.target_on || P.max_nodes) nr_wide_write_share(P.wpart + (size_t)(wave & 1) * gridDim.x, A);
         if (!nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns)) break;
         if (wave + 1 == P.max_waves && threadIdx.x == 0 && blockIdx.x == 0 &&
             *(volatile unsigned long long *)&P.wave_count[wave + 1] != 0)
             atomicOr(P.status, NR_DEV_ERR_WAVES);
     }
-    nr_block_partial(P.partials + blockIdx.x, R, et, es, P.target_on ? pushed : nr_fix_zero(), nodes, leaves,
-                     dead, trunc, spilled);
+    nr_block_partial(P.partials + blockIdx.x, A.R, A.et, A.es, A.net, A.nodes, A.leaves, A.dead, A.trunc,
+                     A.spilled);
+}
+
+// Records queued in all buckets and the highest non-empty bucket (every block
+// reads the same counters after a grid barrier and gets the same answer).
+__device__ __forceinline__ void nr_bucket_select(const unsigned long long *bcount, int nb, int *b_out,
+                                                 unsigned long long *live_out)
+{
+    __shared__ int s_b[32];
+    int bmin = 1 << 30;
+    unsigned long long c = 0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const unsigned long long x = __ldcg(bcount + b);
+        c += x;
+        if (x && b < bmin) bmin = b;
+    }
+    for (int off = 16; off > 0; off >>= 1) bmin = min(bmin, __shfl_xor_sync(NR_FULL, bmin, off));
+    *live_out = nr_block_u64_sum(c);        // (its barriers also order s_b's reuse)
+    if ((threadIdx.x & 31) == 0) s_b[threadIdx.x >> 5] = bmin;
+    __syncthreads();
+    int bb = 1 << 30;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) bb = min(bb, s_b[i]);
+    *b_out = bb;
+}
+
+// In-place compaction of the arena's first `used` slots: the `live` records
+// end up in slots [0, live).  Free slots below `live` are paired, in slot
+// order, with records at or above it (there are as many of each).  Three
+// grid barriers; false if one of them failed.
+template <int W4>
+__device__ __forceinline__ bool nr_bucket_compact(const NrBucketWideParams &P, unsigned long long used,
+                                                  unsigned long long live)
+{
+    __shared__ unsigned long long s_h[NR_WIDE_BLOCK / 32], s_l[NR_WIDE_BLOCK / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    // block b owns slots [b * chunk, (b + 1) * chunk), each warp a contiguous part of them
+    const unsigned long long chunk = ((used + gridDim.x - 1) / gridDim.x + 31) & ~31ull;
+    const unsigned long long sub = ((chunk + nwarp - 1) / nwarp + 31) & ~31ull;
+    const unsigned long long c0 = (unsigned long long)blockIdx.x * chunk;
+    const unsigned long long c1 = min(used, c0 + chunk);
+    const unsigned long long w0 = c0 + (unsigned long long)warp * sub;
+    const unsigned long long w1 = min(c1, w0 + sub);
+    const unsigned long long iters = (w1 > w0) ? (w1 - w0 + 31) / 32 : 0;
+    unsigned long long nh = 0, nl = 0;      // free slots below live, records at or above it
+    for (unsigned long long it = 0; it < iters; ++it) {
+        const unsigned long long s = w0 + it * 32 + lane;
+        const unsigned k = (s < w1) ? __ldcg(P.key + s) : NR_WIDE_FREE;
+        nh += __popc(__ballot_sync(NR_FULL, s < w1 && s < live && k == NR_WIDE_FREE));
+        nl += __popc(__ballot_sync(NR_FULL, s < w1 && s >= live && k != NR_WIDE_FREE));
+    }
+    if (lane == 0) { s_h[warp] = nh; s_l[warp] = nl; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long th = 0, tl = 0;
+        for (int i = 0; i < nwarp; ++i) { th += s_h[i]; tl += s_l[i]; }
+        __stcg(P.ccount + blockIdx.x, th);
+        __stcg(P.ccount + gridDim.x + blockIdx.x, tl);
+    }
+    if (!nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns)) return false;
+    // global ranks: earlier blocks, then earlier warps of this block, then earlier lanes
+    unsigned long long rh = 0, rl = 0, moved = 0;
+    for (unsigned b = 0; b < gridDim.x; ++b) {
+        const unsigned long long h = __ldcg(P.ccount + b);
+        if (b < blockIdx.x) { rh += h; rl += __ldcg(P.ccount + gridDim.x + b); }
+        moved += h;
+    }
+    for (int i = 0; i < warp; ++i) { rh += s_h[i]; rl += s_l[i]; }
+    unsigned *hole = P.list, *from = P.list + P.capacity / 2;
+    for (unsigned long long it = 0; it < iters; ++it) {
+        const unsigned long long s = w0 + it * 32 + lane;
+        const unsigned k = (s < w1) ? __ldcg(P.key + s) : NR_WIDE_FREE;
+        const unsigned mh = __ballot_sync(NR_FULL, s < w1 && s < live && k == NR_WIDE_FREE);
+        const unsigned ml = __ballot_sync(NR_FULL, s < w1 && s >= live && k != NR_WIDE_FREE);
+        const unsigned below = (1u << lane) - 1u;
+        if ((mh >> lane) & 1u) __stcg(hole + rh + __popc(mh & below), (unsigned)s);
+        if ((ml >> lane) & 1u) __stcg(from + rl + __popc(ml & below), (unsigned)s);
+        rh += __popc(mh);
+        rl += __popc(ml);
+    }
+    if (!nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns)) return false;
+    // one warp per moved record; sources (>= live) and destinations (< live) never overlap
+    const unsigned long long gw = (unsigned long long)blockIdx.x * nwarp + warp;
+    const unsigned long long TW = (unsigned long long)gridDim.x * nwarp;
+    for (unsigned long long r = gw; r < moved; r += TW) {
+        const unsigned long long d = __ldcg(hole + r), s = __ldcg(from + r);
+        if (lane < W4) __stcg(P.mask + d * W4 + lane, __ldcg(P.mask + s * W4 + lane));
+        if (lane == 0) {
+            __stcg(P.mass + d, __ldcg(P.mass + s));
+            __stcg(P.key + d, __ldcg(P.key + s));
+        }
+    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *P.top = live;
+        P.stop_info[2]++;
+    }
+    return nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns);
+}
+
+template <int W4>
+__global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketWideParams P)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ unsigned s_hist[NR_WIDE_MAX_NB + 1];
+    const NrWideGraph g = P.g;
+    nr_stage_blob(smem, P.blob, g.blob_bytes);
+    __syncthreads();
+    const NrWideView v = nr_wide_view<W4>(smem, g);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    const unsigned long long TW = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long cap = P.capacity;
+    NrWideAcc A;
+    nr_wide_acc_init(A);
+    NrWideOut O;
+    O.mask = P.mask;
+    O.mass = P.mass;
+    O.key = P.key;
+    O.count = P.top;
+    O.cap = cap;
+    O.shift = P.shift;
+    O.nb = P.nb;
+    O.hist = s_hist;
+    int stop = 0, wave = 0;
+    unsigned long long live = 0;
+    for (; wave < P.max_waves; ++wave) {
+        int bsel;
+        nr_bucket_select(P.bcount, P.nb, &bsel, &live);
+        if (live == 0) break;                               // queue empty
+        stop = nr_wide_stop_test(P.wpart + (size_t)((wave + 1) & 1) * gridDim.x, wave == 0, P.target_on,
+                                 P.target_fix, P.max_nodes);
+        if (stop) break;
+        // reclaim freed slots once they are a large part of the used arena
+        unsigned long long used = min(__ldcg(P.top), cap);
+        if (used > live && ((used > cap / 2 && used - live >= used / 4) || used > cap - cap / 8)) {
+            if (!nr_bucket_compact<W4>(P, used, live)) break;
+            used = live;
+        }
+        // gather the slots of bucket bsel: the whole bucket is this wave
+        unsigned long long *wl = P.wave_len + (wave & 1);
+        for (unsigned long long s0 = gw * 32; s0 < used; s0 += TW * 32) {
+            const unsigned long long s = s0 + lane;
+            const bool hit = s < used && __ldcg(P.key + s) == (unsigned char)bsel;
+            const unsigned mk = __ballot_sync(NR_FULL, hit);
+            if (!mk) continue;
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(wl, (unsigned long long)__popc(mk));
+            base = __shfl_sync(NR_FULL, base, 0);
+            if (hit) {
+                __stcg(P.list + base + __popc(mk & ((1u << lane) - 1u)), (unsigned)s);
+                __stcg(P.key + s, (unsigned char)NR_WIDE_FREE);
+            }
+        }
+        for (int b = threadIdx.x; b < P.nb; b += blockDim.x) s_hist[b] = 0u;
+        if (!nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns)) break;
+        // run the wave; children go to the end of the arena
+        const unsigned long long n_in = __ldcg(wl);
+        if (threadIdx.x == 0 && blockIdx.x == 0) {
+            atomicAdd(P.bcount + bsel, (unsigned long long)0 - n_in);
+            P.wave_len[(wave + 1) & 1] = 0;
+            if (n_in > P.stats[0]) P.stats[0] = n_in;
+        }
+        for (unsigned long long idx = gw; idx < n_in; idx += TW) {
+            const unsigned long long s = __ldcg(P.list + idx);
+            if (lane < W4) reinterpret_cast<uint4 *>(v.m)[lane] = __ldcg(P.mask + s * W4 + lane);
+            const double mass = __ldcg(P.mass + s);
+            __syncwarp();
+            nr_wide_step<W4>(g, v, mass, P.eps, O, A);
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < P.nb; b += blockDim.x)
+            if (s_hist[b]) atomicAdd(P.bcount + b, (unsigned long long)s_hist[b]);
+        nr_wide_write_share(P.wpart + (size_t)(wave & 1) * gridDim.x, A);
+        if (!nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns)) break;
+    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (wave == P.max_waves) atomicOr(P.status, NR_DEV_ERR_WAVES);
+        P.stop_info[0] = wave;
+        P.stop_info[1] = stop;
+        P.stats[1] = live;
+    }
+    nr_block_partial(P.partials + blockIdx.x, A.R, A.et, A.es, A.net, A.nodes, A.leaves, A.dead, A.trunc,
+                     A.spilled);
 }

@@ -95,7 +95,7 @@ def test_wide_target_width_matches_oracle(ctx, oracle, name, make, target):
     g, s, t = make(graphs)
     o = oracle.run(g, s, t, target_width=target, threads=4)
     assert o.status in (0, 1)
-    r = ctx.reliability(g, s, t, capacity=1 << 23, target_width=target)
+    r = ctx.reliability(g, s, t, capacity=1 << 23, target_width=target, bucket_shift=-1)
     assert r.engine == "grid"
     check(r, o)
     assert (r.queued, r.stop) == (o.queued, o.status)
@@ -124,9 +124,72 @@ def test_batch_routes_large_graphs_to_wide_engine(ctx, oracle):
         assert r.queued == o.queued
 
 
-def test_batch_large_graph_needs_wave_order(ctx, engine_lib):
+def test_batch_large_graph_learned_order_unsupported(ctx, engine_lib):
     from relaibilitygpu_gb300 import graphs
     gs = [graphs.complete(8, p=0.9), graphs.grid(6, 6, p=0.9)]
     with pytest.raises(engine_lib.NrError) as e:
-        ctx.reliability_batch(gs, [0, 0], [7, 35], target_width=1e-6, order="maxmass")
-    assert e.value.status == -4
+        ctx.reliability_batch(gs, [0, 0], [7, 35], target_width=1e-6, order="learned")
+    assert e.value.status in (-1, -4)
+
+
+BUCKET_CASES = [
+    ("K40 p~U[0.9,0.99] to 1e-9", lambda G: (G.complete(40, p_range=(0.9, 0.99), seed=1), 0, 39), 1e-9, 2, 1 << 20),
+    ("rgg 60/150 to 1e-7", lambda G: (lambda g: (g, g.src, g.dst))(G.rgg(60, 150, p_range=(0.9, 0.99), seed=11)),
+     1e-7, 2, 1 << 22),
+    ("rgg 100/250 to 1e-4", lambda G: (lambda g: (g, g.src, g.dst))(G.rgg(100, 250, p_range=(0.9, 0.99), seed=3)),
+     1e-4, 2, 1 << 24),
+    ("gnm 40/52 exhaustive", lambda G: (lambda g: (g, g.src, g.dst))(G.gnm(40, 52, p_range=(0.5, 0.95), seed=9)),
+     0.0, 2, 1 << 20),
+    ("gnm 36/45 exhaustive, one bucket per octave", lambda G: (lambda g: (g, g.src, g.dst))(
+        G.gnm(36, 45, p_range=(0.5, 0.95), seed=8)), 0.0, 0, 1 << 20),
+]
+
+
+@pytest.mark.parametrize("name,make,target,shift,cap", BUCKET_CASES, ids=[c[0] for c in BUCKET_CASES])
+def test_bucket_queue_matches_oracle(ctx, oracle, name, make, target, shift, cap):
+    """The whole-GPU bucketed max-mass queue: each wave is the whole highest bucket, as the
+    oracle's bucketed wave schedule -- same waves, widest wave, counts, queue and exact sums."""
+    from relaibilitygpu_gb300 import graphs
+    g, s, t = make(graphs)
+    o = oracle.run(g, s, t, target_width=target, bucket_shift=shift, n_buckets=255, threads=4)
+    assert o.status in (0, 1)
+    r = ctx.reliability(g, s, t, capacity=cap, target_width=target, order="maxmass", bucket_shift=shift,
+                        n_buckets=255)
+    assert r.engine == "grid"
+    check(r, o)
+    assert (r.queued, r.stop) == (o.queued, o.status)
+
+
+def test_bucket_queue_reclaims_freed_slots(ctx, oracle):
+    """2.09M records are pushed over the run, at most 1.38M at a time: an arena of 1.8M slots
+    holds the run only if the slots of popped records are reused (no spill, exact match)."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.rgg(60, 150, p_range=(0.9, 0.99), seed=11)
+    o = oracle.run(g, g.src, g.dst, target_width=1e-7, bucket_shift=2, n_buckets=255, threads=4)
+    assert o.pushes > 1_800_000 > o.max_queued
+    r = ctx.reliability(g, g.src, g.dst, capacity=1_800_000, target_width=1e-7, order="maxmass", bucket_shift=2,
+                        n_buckets=255)
+    assert r.spilled == 0
+    check(r, o)
+
+
+def test_bucket_queue_overflow_brackets(ctx, oracle):
+    """A full arena spills children into ESP: R <= true <= R + ESP still holds."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.gnm(40, 52, p_range=(0.5, 0.95), seed=9)
+    exact = oracle.run(g, g.src, g.dst)
+    r = ctx.reliability(g, g.src, g.dst, capacity=2000, order="maxmass", bucket_shift=2, n_buckets=255)
+    assert r.spilled > 0
+    assert r.R <= exact.R + 1e-15 and exact.R <= r.R + r.esp + 1e-12
+
+
+def test_bucket_queue_node_budget(ctx, oracle):
+    """A node budget stops between waves with a valid bracket (stop reason 3)."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.rgg(100, 250, p_range=(0.9, 0.99), seed=3)
+    r = ctx.reliability(g, g.src, g.dst, capacity=1 << 23, target_width=1e-9, order="maxmass", bucket_shift=2,
+                        n_buckets=255, max_nodes=200_000)
+    assert r.stop == 3 and r.nodes >= 200_000
+    o = oracle.run(g, g.src, g.dst, target_width=1e-9, bucket_shift=2, n_buckets=255, threads=4,
+                   max_nodes=200_000)
+    check(r, o)
