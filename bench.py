@@ -9,6 +9,13 @@ Workloads (all synthetic, seeded; numpy PCG64):
       subproblems, so a step solves a batch of 4096 such instances (seeds
       0..4095) in one launch; single-instance time-to-bound is reported beside it.
   k10 -- K10 (N=10, E=45), p ~ U[0.5, 0.95], exhaustive (one solve per step).
+  k15p05, k25p05 -- the reference's own published K15 / K25 p=0.5 runs
+      (breadth-first waves, 77,410,924-slot wave buffers, eps 1e-15).
+  rgg200 -- random geometric graph N=200, E=600 (unit square, terminals the
+      farthest pair), p ~ U[0.9, 0.99]: the whole-GPU bucketed max-mass queue
+      aiming at ESP width <= 1e-5, stopped at a budget of 20M subproblems per
+      step (the bound is far beyond one GPU's queue memory; the line reports
+      the R <= true <= R + ESP bracket reached).
 
 `value` is subproblems (popped nodes, dead ends included) per second of
 device time: the engine's CUDA events on its own stream around the kernels,
@@ -71,6 +78,15 @@ def workload(name: str):
                     opts=dict(eps=1e-15), oracle=dict(eps=1e-15, max_nodes=20_000_000),
                     name=f"K{n} p=0.5 (COMP{n}-05.txt) src=0 dst={n - 1}, breadth-first waves, queue capacity "
                          f"77,410,924 per wave buffer, truncation eps 1e-15 (the reference's own published run)")
+    if name == "rgg200":
+        g = nr.rgg(200, 600, p_range=(0.9, 0.99), seed=7)
+        opts = dict(target_width=1e-5, order="maxmass", bucket_shift=2, n_buckets=255, max_nodes=20_000_000,
+                    timeout_ms=120000.0)
+        return dict(kind="single", graphs=[g], srcs=[g.src], dsts=[g.dst], capacity=1 << 28, opts=opts,
+                    oracle=dict(target_width=1e-5, bucket_shift=2, n_buckets=255, max_nodes=1_000_000),
+                    name=f"RGG N=200 E={g.n_edges} (unit square, seed 7) src={g.src} dst={g.dst} (farthest pair) "
+                         f"p~U[0.9,0.99], bucketed max-mass order (4 buckets per octave) toward ESP width <=1e-5, "
+                         f"20M-subproblem budget per step, 2^28-slot arena")
     if name == "k10":
         g = nr.complete(10, p_range=(0.5, 0.95), seed=2)
         return dict(kind="single", graphs=[g], srcs=[0], dsts=[9], capacity=1 << 22, opts=dict(eps=0.0),
@@ -203,6 +219,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="k15batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="k15batch: skip the plain / learned / breadth-first order comparison")
     ap.add_argument("--no-autotune", action="store_true",
                     help="batch workloads: use the stored tuned settings instead of running nr_autotune")
     args = ap.parse_args()
@@ -286,13 +304,14 @@ def main():
     r0 = res[0]
     h2d = sum(r.h2d_bytes for r in res)
     d2h = sum(r.d2h_bytes for r in res)
-    stats = {"R": r0.R, "esp": r0.esp, "paths": int(r0.paths), "nodes": int(r0.nodes),
-             "iterations": int(r0.iterations), "engine": nr.engine.ENGINES.get(r0.engine, r0.engine),
-             "nodes_per_step": nodes // args.steps}
+    stats = {"R": r0.R, "R_plus_esp": r0.R_plus_esp, "esp": r0.esp, "paths": int(r0.paths), "nodes": int(r0.nodes),
+             "iterations": int(r0.iterations), "queued": int(r0.queued), "spilled": int(r0.spilled),
+             "stop": {0: "queue empty", 1: "target width met", 3: "node budget"}.get(int(r0.stop), int(r0.stop)),
+             "engine": nr.engine.ENGINES.get(r0.engine, r0.engine), "nodes_per_step": nodes // args.steps}
 
     # single-instance time-to-bound (latency): plain max-mass order vs the learned order
     ttb = None
-    if args.workload == "k15batch":
+    if args.workload == "k15batch" and not args.no_compare:
         from relaibilitygpu_gb300 import learned as LR
 
         # the order comparison runs at one bucket resolution (one bucket per factor of two), since

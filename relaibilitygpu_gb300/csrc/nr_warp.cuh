@@ -26,7 +26,7 @@
 #define NR_WARP_BLOCK 128        // default block: 4 warps
 #define NR_WARP_BLOCK_MAX 256    // largest block the warp kernels are compiled for
 #ifndef NR_WARP_MIN_BLOCKS
-#define NR_WARP_MIN_BLOCKS 1     // resident 256-thread blocks per SM the register budget must allow
+#define NR_WARP_MIN_BLOCKS 3     // resident 256-thread blocks per SM the register budget must allow
 #endif
 #define NR_PAGE 32
 
@@ -86,7 +86,8 @@ struct NrWarpShm {
 
 __host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets, int pages, bool learn = false)
 {
-    size_t b = learn ? (size_t)(NR_MLP_WARP_WORDS + 16) * 4 : 0;   // scorer scratch + outputs
+    size_t b = 32 * sizeof(NrLaneAcc);                             // per-lane sums and counters
+    b += learn ? (size_t)(NR_MLP_WARP_WORDS + 16) * 4 : 0;         // scorer scratch + outputs
     b += (size_t)K * 4 * W4 * 4;
     b += (size_t)n_buckets * 2;
     b = (b + 3) & ~size_t(3);
@@ -98,8 +99,14 @@ __host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets
     return (b + 15) & ~size_t(15);
 }
 
+// The per-lane sums and counters (updated a few times per subproblem) live in
+// shared memory, which keeps the plain kernel for masks of up to 4 blocks at 80
+// registers without spills: three 256-thread blocks, 24 warps, per SM.  Wider
+// masks hold more words per lane (two blocks per SM), and the scorer's kernel
+// needs its registers for the MLP.
 template <int G, int W4, bool LEARN = false>
-__global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, NR_WARP_MIN_BLOCKS) nr_warp_kernel(NrWarpParams P)
+__global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_WARP_MIN_BLOCKS : 2))
+    nr_warp_kernel(NrWarpParams P)
 {
     constexpr int K = 32 / G;
     constexpr int NW = 4 * W4;
@@ -113,8 +120,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, NR_WARP_MIN_BLOCKS) nr_warp
     NrWarpShm sh;
     uint32_t *mlp_scratch = nullptr;
     float *mlp_y = nullptr;
+    NrLaneAcc *acc_base;
     {
         unsigned char *b = smem + (size_t)warp * nr_warp_shm_bytes(K, W4, NB, NP, LEARN);
+        acc_base = reinterpret_cast<NrLaneAcc *>(b);
+        b += 32 * sizeof(NrLaneAcc);
         size_t o = 0;
         if (LEARN) {
             mlp_scratch = reinterpret_cast<uint32_t *>(b);
@@ -187,7 +197,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, NR_WARP_MIN_BLOCKS) nr_warp
         if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
         __syncwarp();
 
-        NrLaneAcc acc;
+        NrLaneAcc &acc = acc_base[lane];
         nr_acc_zero(acc);
         NrFix qacc = (lane == 0) ? nr_fix_of(1.0) : nr_fix_zero();   // queued mass: this lane's pushes - pops
         long long qcount = (lane == 0) ? 1 : 0;
