@@ -116,6 +116,22 @@ struct PhaseClock {
 
 }  // namespace
 
+// Dynamic shared-memory limit of a kernel on a device: the attribute is
+// per-function state, so every setter in the library goes through here and
+// the attribute is set only when it differs from the value last set.
+cudaError_t nr_smem_limit(int device, const void *kfn, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> last;
+    std::lock_guard<std::mutex> l(mu);
+    auto it = last.find({device, kfn});
+    if (it != last.end() && it->second == bytes) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) last[{device, kfn}] = bytes;
+    else last.erase({device, kfn});
+    return e;
+}
+
 // Correctly rounded (to nearest, ties to even) value of a 192-bit fixed-point sum.
 double nr_fix_to_double_host(const NrFix &a)
 {
@@ -150,9 +166,16 @@ void nr_fix_add_host(NrFix &a, const NrFix &b) { nr_fix_add(a, b); }
 
 // Worker threads kept by a context for the host side of batch calls (table
 // building and validation), so a call does not pay for thread creation.  A
-// batch call runs several short jobs back to back: between jobs the workers
-// (and the caller waiting for a job's end) poll for up to kSpin before they
-// block, so a job does not wait for threads to be woken from sleep.
+// batch call runs several short jobs back to back, and batch calls often follow
+// one another: between jobs the workers (and the caller waiting for a job's
+// end) poll, yielding the core, for up to kSpin before they block, so a job
+// rarely waits for threads to be woken from sleep.
+#ifndef NR_POOL_MAX
+#define NR_POOL_MAX 32          // host threads of a batch call at most (the caller's included)
+#endif
+#ifndef NR_POOL_SPIN_US
+#define NR_POOL_SPIN_US 2000    // idle workers poll this long before they sleep
+#endif
 class NrPool {
 public:
     explicit NrPool(int workers)
@@ -205,7 +228,7 @@ public:
     }
 
 private:
-    static constexpr std::chrono::microseconds kSpin{300};
+    static constexpr std::chrono::microseconds kSpin{NR_POOL_SPIN_US};
     void work()
     {
         for (;;) {
@@ -271,6 +294,41 @@ struct NrBatchScratch {
     std::vector<NrHostBlock> blk;
 };
 
+struct WarpDump;
+struct WarpRunCfg {
+    int wave_mode, shift, n_buckets, pages, escalate, warps_per_block;
+    int learned = 0;
+    const WarpDump *dump = nullptr;
+    double eps, target;
+    unsigned long long max_nodes;
+};
+
+// A warp-engine batch in flight: its stream, staging, device tables and page
+// slabs.  (Splitting a batch over two slots, so the host builds one part's
+// tables while the other part runs, measured slower on 4096 K15 instances:
+// the host passes are dominated by fixed costs and two concurrent launches
+// lengthen the device span.)
+#define NR_SLOTS 1
+struct NrSlot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;   // around the part's kernels
+    void *hbuf = nullptr;       // pinned host staging for the uploads and results
+    size_t hbuf_bytes = 0;
+    void *wbuf = nullptr;       // device: counters, tables, descriptors, ids, outputs
+    size_t wbuf_bytes = 0;
+    void *wslab = nullptr;      // device: per-warp page slabs
+    size_t wslab_bytes = 0;
+    NrBatchScratch scratch;     // per-instance host tables (reused from call to call)
+    // the part queued by warp_submit, for warp_finish
+    int n = 0;
+    const nr_graph *gs = nullptr;
+    const int32_t *srcs = nullptr, *dsts = nullptr;
+    nr_result *res = nullptr;
+    WarpRunCfg cfgp{};
+    size_t off_out = 0;
+    int first_grid = 0, block = 0;
+};
+
 struct nr_context {
     int device = 0;
     int sms = 0;
@@ -280,15 +338,9 @@ struct nr_context {
     size_t qbytes = 0;
     void *sbuf = nullptr;       // blob, counters, barrier, status, partials
     size_t sbytes = 0;
-    void *wslab = nullptr;      // warp engine: per-warp page slabs
-    size_t wslab_bytes = 0;
-    void *wbuf = nullptr;       // warp engine: blob, descriptors, outputs, counters
-    size_t wbuf_bytes = 0;
-    void *hbuf = nullptr;       // pinned host staging for the warp engine's uploads and results
-    size_t hbuf_bytes = 0;
+    NrSlot slot[NR_SLOTS];      // warp engine: one per part of a batch in flight
     std::map<std::pair<const void *, size_t>, int> occupancy;   // (kernel, smem) -> blocks per SM
     std::unique_ptr<NrPool> pool;   // host worker threads, created by the first large batch
-    NrBatchScratch scratch;         // per-instance host tables of the last batch call (reused)
     int smem_optin = 0;             // largest dynamic shared memory a block may opt in to
     void *model = nullptr;          // learned scorer: FP32 parameters and their BF16 copy
     NrMlpDev mlp{};
@@ -309,7 +361,7 @@ struct nr_context {
             int hw = 0;
             if (sched_getaffinity(0, sizeof(set), &set) == 0) hw = CPU_COUNT(&set);
             if (hw <= 0) hw = (int)std::thread::hardware_concurrency();
-            hw = std::max(1, std::min(hw, 32));
+            hw = std::max(1, std::min(hw, NR_POOL_MAX));
             pool.reset(new NrPool(hw - 1));
         }
         const int threads = std::min(pool->size(), (n + min_per_thread - 1) / min_per_thread);
@@ -336,12 +388,26 @@ static int ensure(void **buf, size_t *have, size_t need)
 // ---------------------------------------------------------------------------
 // validation and graph tables
 // ---------------------------------------------------------------------------
-static int validate(const nr_graph *g, int src, int dst)
+// Checks of one instance that read no array: sizes, pointers, terminals.
+static int validate_shape(const nr_graph *g, int src, int dst)
 {
     if (!g || g->n_nodes <= 0 || g->n_edges < 0 || g->n_arcs < 0 || !g->row_ptr) return NR_ERR_INVALID;
     if (g->n_arcs > 0 && (!g->col_idx || !g->edge_id)) return NR_ERR_INVALID;
     if (g->n_edges > 0 && !g->edge_p) return NR_ERR_INVALID;
     if (src < 0 || dst < 0 || src >= g->n_nodes || dst >= g->n_nodes) return NR_ERR_INVALID;
+    return NR_OK;
+}
+
+static int validate_probabilities(const nr_graph *g)
+{
+    for (int e = 0; e < g->n_edges; ++e)
+        if (std::isnan(g->edge_p[e])) return NR_ERR_INVALID;
+    return NR_OK;
+}
+
+// The CSR arrays: row offsets, heads and edge ids in range.
+static int validate_structure(const nr_graph *g)
+{
     if (g->row_ptr[0] != 0 || g->row_ptr[g->n_nodes] != g->n_arcs) return NR_ERR_INVALID;
     for (int u = 0; u < g->n_nodes; ++u)
         if (g->row_ptr[u + 1] < g->row_ptr[u]) return NR_ERR_INVALID;
@@ -349,9 +415,22 @@ static int validate(const nr_graph *g, int src, int dst)
         if (g->col_idx[j] < 0 || g->col_idx[j] >= g->n_nodes) return NR_ERR_INVALID;
         if (g->edge_id[j] < 0 || g->edge_id[j] >= g->n_edges) return NR_ERR_INVALID;
     }
-    for (int e = 0; e < g->n_edges; ++e)
-        if (std::isnan(g->edge_p[e])) return NR_ERR_INVALID;
     return NR_OK;
+}
+
+// Same sizes and the same CSR arrays (pointers) as another graph.
+static bool same_structure_arrays(const nr_graph *a, const nr_graph *b)
+{
+    return a->n_nodes == b->n_nodes && a->n_arcs == b->n_arcs && a->n_edges == b->n_edges &&
+           a->row_ptr == b->row_ptr && a->col_idx == b->col_idx && a->edge_id == b->edge_id;
+}
+
+static int validate(const nr_graph *g, int src, int dst)
+{
+    int rc = validate_shape(g, src, dst);
+    if (!rc) rc = validate_probabilities(g);
+    if (!rc) rc = validate_structure(g);
+    return rc;
 }
 
 static int group_width_of(int n) { return group_width(n); }
@@ -380,11 +459,18 @@ static size_t small_struct_layout(const nr_graph *g, NrSmallGraph *sg, size_t at
     return off - at;
 }
 
-static void small_fill_inst(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)
+// Copies p; false if one of them is NaN.
+static bool small_fill_inst(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)
 {
     const int E = g->n_edges;
     double *p = reinterpret_cast<double *>(b + sg->off_p);
-    memcpy(p, g->edge_p, sizeof(double) * E);
+    bool ok = true;
+    for (int e = 0; e < E; ++e) {
+        const double x = g->edge_p[e];
+        ok = ok && !std::isnan(x);
+        p[e] = x;
+    }
+    return ok;
 }
 
 static void small_fill_struct(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)
@@ -520,9 +606,14 @@ extern "C" void nr_context_destroy(nr_context *c)
     cudaSetDevice(c->device);
     if (c->qbuf) cudaFree(c->qbuf);
     if (c->sbuf) cudaFree(c->sbuf);
-    if (c->wslab) cudaFree(c->wslab);
-    if (c->wbuf) cudaFree(c->wbuf);
-    if (c->hbuf) cudaFreeHost(c->hbuf);
+    for (NrSlot &sl : c->slot) {
+        if (sl.wslab) cudaFree(sl.wslab);
+        if (sl.wbuf) cudaFree(sl.wbuf);
+        if (sl.hbuf) cudaFreeHost(sl.hbuf);
+        if (sl.ev0) cudaEventDestroy(sl.ev0);
+        if (sl.ev1) cudaEventDestroy(sl.ev1);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
     if (c->model) cudaFree(c->model);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -545,7 +636,7 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
     const int block = NR_BLOCK_THREADS;
     const int warps = block / 32;
     const size_t smem = (size_t)sg.blob_bytes + (size_t)warps * (32 / G) * 4 * W4 * sizeof(uint32_t);
-    NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
     int bps = 0;
     NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
     if (bps < 1) return NR_ERR_UNSUPPORTED;
@@ -696,7 +787,7 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     if (!kfn) return NR_ERR_UNSUPPORTED;
     const int block = NR_WIDE_BLOCK;
     const size_t smem = (size_t)wg.blob_bytes + (block / 32) * nr_wide_warp_shm(wg.n, W4);
-    NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
     int bps = 0;
     NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
     if (bps < 1) return NR_ERR_UNSUPPORTED;
@@ -835,7 +926,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     if (!kfn) return NR_ERR_UNSUPPORTED;
     const int block = NR_WIDE_BLOCK;
     const size_t smem = (size_t)wg.blob_bytes + (block / 32) * nr_wide_warp_shm(wg.n, W4);
-    NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
     int bps = 0;
     NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
     if (bps < 1) return NR_ERR_UNSUPPORTED;
@@ -984,13 +1075,6 @@ struct WarpDump {
     int stride;
 };
 
-struct WarpRunCfg {
-    int wave_mode, shift, n_buckets, pages, escalate, warps_per_block;
-    int learned = 0;
-    const WarpDump *dump = nullptr;
-    double eps, target;
-    unsigned long long max_nodes;
-};
 
 static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhaustive)
 {
@@ -1056,12 +1140,29 @@ static int ensure_host(void **buf, size_t *have, size_t need)
 // (status 2) are listed in *handover for the caller.  Host work per call:
 // one layout pass, a parallel table fill into pinned staging memory, one
 // upload, one launch per (group width, mask width) class, one download.
-static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
-                          const WarpRunCfg &cfg, nr_result *res, std::vector<int> *handover)
+static int slot_ready(NrSlot &sl)
 {
-    PhaseClock pc;
+    if (sl.stream) return NR_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&sl.ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&sl.ev1);
+    if (e != cudaSuccess) {
+        nr_last_cuda_error(e, __LINE__, "batch stream set-up");
+        return NR_ERR_CUDA;
+    }
+    return NR_OK;
+}
+
+// Build the tables of instances [0, n) of gs on the host and queue their
+// upload, the kernels and the read-back of the outputs on slot `sl`.  `base`
+// is the index of gs[0] in the caller's batch (for collected children).
+static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_graph *gs, const int32_t *srcs,
+                       const int32_t *dsts, const WarpRunCfg &cfg, nr_result *res, PhaseClock &pc)
+{
     constexpr int NCLS = 3 * NR_MAX_W4;      // class = lane-group width x mask blocks
-    NrBatchScratch &S = c->scratch;          // kept by the context: no page faults on every call
+    int rc0 = slot_ready(sl);
+    if (rc0) return rc0;
+    NrBatchScratch &S = sl.scratch;          // kept by the slot: no page faults on every call
     S.desc.resize(n);
     S.cls.resize(n);
     S.same_prev.resize(n);
@@ -1123,14 +1224,15 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
     const size_t off_ids = off; off = align16(off + sizeof(int) * n);
     const size_t up_bytes = off;
     const size_t off_out = off; off = align16(off + sizeof(NrWarpOut) * n);
-    int rc = ensure_host(&c->hbuf, &c->hbuf_bytes, off);
+    int rc = ensure_host(&sl.hbuf, &sl.hbuf_bytes, off);
     if (rc) return rc;
-    rc = ensure(&c->wbuf, &c->wbuf_bytes, off);
+    rc = ensure(&sl.wbuf, &sl.wbuf_bytes, off);
     if (rc) return rc;
-    unsigned char *hb = static_cast<unsigned char *>(c->hbuf);
+    unsigned char *hb = static_cast<unsigned char *>(sl.hbuf);
     NrSmallGraph *hdesc = reinterpret_cast<NrSmallGraph *>(hb + off_desc);
     int *hids = reinterpret_cast<int *>(hb + off_ids);
     memset(hb + off_cnt, 0, sizeof(int) * NCLS);
+    std::atomic<int> bad_p(0);            // a NaN probability
     c->parallel_for(B, 1, [&](int b) {
         const NrHostBlock &k = S.blk[b];
         size_t at = k.base;
@@ -1150,12 +1252,13 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
                 d.struct_off = rep;               // instance 0 always owns one, so rep >= 0 here
             }
             d.blob_bytes = (int)(S.inst_b[i] + S.struct_b[i]);
-            small_fill_inst(&gs[i], &d, hb + d.blob_off);
+            if (!small_fill_inst(&gs[i], &d, hb + d.blob_off)) bad_p.store(1);
             const int slot = fill[S.cls[i]]++;
             hdesc[slot] = d;
             hids[slot] = i;
         }
     });
+    if (bad_p.load()) return NR_ERR_INVALID;
     pc.mark("tables");
 
     // launch geometry per class (occupancy cached per kernel and shared-memory size)
@@ -1183,7 +1286,7 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
         int bps;
         if (it == c->occupancy.end()) {
-            NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
             NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
             c->occupancy[{kfn, smem * 64 + warps_pb}] = bps;
         } else {
@@ -1194,13 +1297,13 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         smems[j] = smem;
         slab_need = std::max(slab_need, (size_t)grids[j] * warps_pb * cfgp.pages * NR_PAGE * (16 * (size_t)W4 + 8));
     }
-    rc = ensure(&c->wslab, &c->wslab_bytes, slab_need);
+    rc = ensure(&sl.wslab, &sl.wslab_bytes, slab_need);
     if (rc) return rc;
-    unsigned char *wb = static_cast<unsigned char *>(c->wbuf);
-    cudaStream_t s = c->stream;
+    unsigned char *wb = static_cast<unsigned char *>(sl.wbuf);
+    cudaStream_t s = sl.stream;
     pc.mark("geometry");
     NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, up_bytes, cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
+    NR_CUDA_TRY(cudaEventRecord(sl.ev0, s));
     int first_grid = 0;
     for (int j = 0; j < NCLS; ++j) {
         if (!class_count[j]) continue;
@@ -1212,9 +1315,9 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         P.inst_id = reinterpret_cast<const int *>(wb + off_ids) + class_begin[j];
         P.n_inst = class_count[j];
         P.next_inst = reinterpret_cast<int *>(wb + off_cnt) + j;
-        P.slab_mask = static_cast<uint4 *>(c->wslab);
+        P.slab_mask = static_cast<uint4 *>(sl.wslab);
         const size_t warps = (size_t)grids[j] * warps_pb;
-        P.slab_mass = reinterpret_cast<double *>(static_cast<unsigned char *>(c->wslab) +
+        P.slab_mass = reinterpret_cast<double *>(static_cast<unsigned char *>(sl.wslab) +
                                                  warps * cfgp.pages * NR_PAGE * 16 * (size_t)W4);
         P.pages = cfgp.pages;
         P.n_buckets = cfg.n_buckets;
@@ -1235,38 +1338,64 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
         P.dump_count = cfg.dump ? cfg.dump->count : nullptr;
         P.dump_cap = cfg.dump ? cfg.dump->cap : 0;
         P.dump_stride = cfg.dump ? cfg.dump->stride : 0;
+        P.inst_base = base;
         const void *kfn = warp_kernel(G, W4, learn);
         void *args[] = {&P};
-        // the dynamic shared-memory limit is per-kernel state that another setting may have lowered
-        NR_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smems[j]));
+        NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smems[j]));
         NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[j]), dim3(block), args, smems[j], s));
     }
-    NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
+    NR_CUDA_TRY(cudaEventRecord(sl.ev1, s));
     NrWarpOut *hout = reinterpret_cast<NrWarpOut *>(hb + off_out);
     NR_CUDA_TRY(cudaMemcpyAsync(hout, wb + off_out, sizeof(NrWarpOut) * n, cudaMemcpyDeviceToHost, s));
+    sl.n = n; sl.gs = gs; sl.srcs = srcs; sl.dsts = dsts; sl.res = res;
+    sl.cfgp = cfgp; sl.off_out = off_out; sl.first_grid = first_grid; sl.block = block;
     pc.mark("enqueue");
-    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    return NR_OK;
+}
+
+// Wait for the part queued on slot `sl` and fill its results; instances the
+// warp engine handed over are appended to `handover` (plus `base`).
+static int warp_finish(nr_context *c, NrSlot &sl, int base, std::vector<int> *handover, PhaseClock &pc)
+{
+    NR_CUDA_TRY(cudaStreamSynchronize(sl.stream));
     pc.mark("device");
     float ms = 0.f;
-    NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    NR_CUDA_TRY(cudaEventElapsedTime(&ms, sl.ev0, sl.ev1));
+    const int n = sl.n;
+    const nr_graph *gs = sl.gs;
+    const NrSmallGraph *desc = sl.scratch.desc.data();
+    const NrWarpOut *hout = reinterpret_cast<const NrWarpOut *>(static_cast<unsigned char *>(sl.hbuf) + sl.off_out);
     std::atomic<int> n_hand(0);
-    c->parallel_for(n, 512, [&](int i) {
-        nr_result *r = &res[i];
-        r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
+    c->parallel_for(n, 256, [&](int i) {
+        nr_result *r = &sl.res[i];
+        memset(r, 0, sizeof(*r));
+        r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = sl.srcs[i]; r->dst = sl.dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
         if (hout[i].status == 2) { n_hand.fetch_add(1); return; }
-        fill_from_warp(hout[i], cfgp, desc[i].w4, r);
+        fill_from_warp(hout[i], sl.cfgp, desc[i].w4, r);
         r->ms = ms;
-        r->grid_blocks = first_grid;
-        r->block_threads = block;
+        r->grid_blocks = sl.first_grid;
+        r->block_threads = sl.block;
         r->h2d_bytes = desc[i].blob_bytes + sizeof(NrSmallGraph) + sizeof(int);
         r->d2h_bytes = sizeof(NrWarpOut);
     });
     if (n_hand.load())
         for (int i = 0; i < n; ++i)
-            if (hout[i].status == 2) handover->push_back(i);
+            if (hout[i].status == 2) handover->push_back(base + i);
     pc.mark("results");
     return NR_OK;
+}
+
+// Warp engine over instances [0, n) on slot 0.
+static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
+                          const WarpRunCfg &cfg, nr_result *res, std::vector<int> *handover,
+                          PhaseClock *clock = nullptr)
+{
+    PhaseClock local;
+    PhaseClock &pc = clock ? *clock : local;
+    int rc = warp_submit(c, c->slot[0], 0, n, gs, srcs, dsts, cfg, res, pc);
+    if (rc) return rc;
+    return warp_finish(c, c->slot[0], 0, handover, pc);
 }
 
 extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs,
@@ -1278,11 +1407,16 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
     nr_options o;
     if (opt) o = *opt; else nr_options_default(&o);
     std::lock_guard<std::mutex> lock(c->mu);
+    PhaseClock pc;
     std::atomic<int> bad(NR_OK), n_wide(0);
     const bool wave_order = o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
+    // shapes here; CSR arrays shared with the previous instance are checked once (there, or
+    // the batch fails there); probabilities where the tables are built (the warp engine) or
+    // below (larger graphs)
     c->parallel_for(n, 256, [&](int i) {
-        memset(&res[i], 0, sizeof(nr_result));
-        int rc = validate(&gs[i], srcs[i], dsts[i]);
+        int rc = validate_shape(&gs[i], srcs[i], dsts[i]);
+        if (!rc && !(i > 0 && same_structure_arrays(&gs[i], &gs[i - 1]))) rc = validate_structure(&gs[i]);
+        if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) rc = validate_probabilities(&gs[i]);
         if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) {
             if (o.order == NR_ORDER_LEARNED) rc = NR_ERR_UNSUPPORTED;    // learned order: n <= 32 only
             n_wide.fetch_add(1);
@@ -1290,6 +1424,7 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
         if (rc) bad.store(rc);
     });
     if (bad.load() != NR_OK) return bad.load();
+    pc.mark("validate");
     NR_CUDA_TRY(cudaSetDevice(c->device));
     const bool exhaustive = !(o.target_width > 0) && wave_order;
     if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
@@ -1299,7 +1434,7 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
     std::vector<int> small_idx, wide_idx, handover;
     int rc;
     if (n_wide.load() == 0) {
-        rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover);
+        rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover, &pc);
         if (rc) return rc;
     } else {
         for (int i = 0; i < n; ++i) (gs[i].n_nodes > NR_SMALL_MAX_N ? wide_idx : small_idx).push_back(i);
@@ -1325,6 +1460,7 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
     }
     for (int i : wide_idx) {
         nr_result *r = &res[i];
+        memset(r, 0, sizeof(*r));
         r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
         rc = run_wide(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, r);
@@ -1447,7 +1583,9 @@ extern "C" int nr_collect_children(nr_context *c, int n, const nr_graph *gs, con
     cfg.dump = &d;
     int rc = NR_OK;
     unsigned long long got = 0;
-    if (cudaMemsetAsync(buf, 0, 64, c->stream) != cudaSuccess) rc = NR_ERR_CUDA;
+    // the counter must be zero before the batch's own streams start
+    if (cudaMemsetAsync(buf, 0, 64, c->stream) != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
+        rc = NR_ERR_CUDA;
     std::vector<int> handover;
     if (!rc) rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover);
     if (!rc) {

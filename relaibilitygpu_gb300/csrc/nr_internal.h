@@ -75,3 +75,7 @@ void nr_fix_add_host(NrFix &a, const NrFix &b);
 int nr_launch_grid_small(int G, const NrGridParams &p, int grid, int block, size_t smem,
                          cudaStream_t stream);
 int nr_grid_small_occupancy(int G, int w4, int block, size_t smem, int *blocks_per_sm);
+
+// Sets a kernel's dynamic shared-memory limit on a device when it differs from
+// the value last set through this function (nr_api.cu).
+cudaError_t nr_smem_limit(int device, const void *kfn, size_t bytes);

@@ -172,12 +172,15 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
         P.max_nodes = o.max_nodes;
     }
     P.out = reinterpret_cast<NrWarpOut *>(base + off_out);
+    P.learned = 0;
+    P.dump_feat = nullptr; P.dump_mask = nullptr; P.dump_mass = nullptr; P.dump_inst = nullptr;
+    P.dump_count = nullptr; P.dump_cap = 0; P.dump_stride = 0; P.inst_base = 0;
 
     const size_t smem = nr_warp_shm_bytes(32 / G, sg.w4, P.n_buckets, pages);
     cudaStream_t s = cudaStreamPerThread;
     const int zero = 0;
     NrWarpOut out;
-    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = nr_smem_limit(dev, kfn, smem);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base, g_noalloc_blob, blob, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + off_desc, &sg, sizeof(sg), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + off_id, &zero, sizeof(int), cudaMemcpyHostToDevice, s);

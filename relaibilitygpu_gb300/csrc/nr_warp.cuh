@@ -66,6 +66,7 @@ struct NrWarpParams {
     unsigned long long *dump_count;
     unsigned long long dump_cap;
     int dump_stride;
+    int inst_base;                   // index of this launch's instance 0 in the caller's batch
 };
 
 __device__ __forceinline__ unsigned long long nr_warp_sum_u64(unsigned long long x)
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
 #pragma unroll
                                 for (int k = 0; k < NW; ++k) P.dump_mask[d * P.dump_stride + k] = w[k];
                                 P.dump_mass[d] = cm;
-                                P.dump_inst[d] = P.inst_id[ii];
+                                P.dump_inst[d] = P.inst_base + P.inst_id[ii];
                             }
                         }
                         if (P.learned && cbm) {             // score this step's children, 16 per tile

@@ -199,3 +199,27 @@ def test_single_instance_any_block_size(ctx, oracle, wpb):
         check_wave_parity(r, o)
     r = ctx.reliability(g, 0, 14, target_width=1e-6, warps_per_block=wpb, pages_per_warp=8192)
     assert r.stop == 1
+
+
+def test_batch_rejects_bad_instances(ctx, engine_lib):
+    """Invalid probabilities, terminals or CSR arrays anywhere in a batch fail the whole call."""
+    from relaibilitygpu_gb300 import graphs
+    gs = [graphs.complete(9, p_range=(0.6, 0.99), seed=i) for i in range(600)]
+    bad = graphs.complete(9, p_range=(0.6, 0.99), seed=7)
+    bad.edge_p = bad.edge_p.copy()
+    bad.edge_p[5] = float("nan")
+    with pytest.raises(engine_lib.NrError) as e:
+        ctx.reliability_batch(gs[:300] + [bad] + gs[300:], [0] * 601, [8] * 601, target_width=1e-6)
+    assert e.value.status == -1
+    with pytest.raises(engine_lib.NrError) as e:
+        ctx.reliability_batch(gs, [0] * 599 + [9], [8] * 600, target_width=1e-6)
+    assert e.value.status == -1
+    broken = graphs.complete(9, p=0.9)
+    broken.col_idx = broken.col_idx.copy()
+    broken.col_idx[3] = 42
+    with pytest.raises(engine_lib.NrError) as e:
+        ctx.reliability_batch(gs[:10] + [broken], [0] * 11, [8] * 11)
+    assert e.value.status == -1
+    # the context stays usable
+    r = ctx.reliability_batch(gs[:4], [0] * 4, [8] * 4, target_width=1e-6)
+    assert all(x.stop == 1 for x in r)
