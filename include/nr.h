@@ -166,6 +166,23 @@ int  nr_reliability_batch(nr_context *ctx, int n_instances, const nr_graph *grap
                           const int32_t *srcs, const int32_t *dsts, uint64_t capacity,
                           const nr_options *opt, nr_result *results);
 
+/* Asynchronous batches (no reference counterpart): nr_reliability_batch in
+ * two halves, so the host builds one batch's tables while the GPU runs the
+ * one before.  nr_batch_submit checks the batch, builds its tables and queues
+ * the upload, the kernels and the read-back on one of the context's two batch
+ * slots, and returns a ticket; nr_batch_wait(ticket) finishes that batch and
+ * fills `results` (as given to the submit) exactly as nr_reliability_batch
+ * would.  Slots alternate: a submit whose slot still holds an unfinished batch
+ * finishes it first (a later wait on its ticket returns its status).  graphs,
+ * srcs, dsts and results must stay valid and unchanged until the wait returns.
+ * `after_stream` (a cudaStream_t, or NULL): the batch's upload starts after the
+ * work already queued on that stream.  A batch with a graph above 32 nodes
+ * runs to completion inside the submit. */
+int  nr_batch_submit(nr_context *ctx, int n_instances, const nr_graph *graphs, const int32_t *srcs,
+                     const int32_t *dsts, uint64_t capacity, const nr_options *opt, nr_result *results,
+                     void *after_stream, int64_t *ticket);
+int  nr_batch_wait(nr_context *ctx, int64_t ticket);
+
 /* Autotuner for batches (no reference counterpart).  Times the warp engine on
  * up to 4096 instances of the batch for each candidate setting -- bucket
  * resolution (bucket_shift -1..2, where -1 is one bucket: breadth-first waves), pages per warp (64 or 512,

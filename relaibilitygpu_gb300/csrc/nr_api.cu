@@ -304,11 +304,11 @@ struct WarpRunCfg {
 };
 
 // A warp-engine batch in flight: its stream, staging, device tables and page
-// slabs.  (Splitting a batch over two slots, so the host builds one part's
-// tables while the other part runs, measured slower on 4096 K15 instances:
-// the host passes are dominated by fixed costs and two concurrent launches
-// lengthen the device span.)
-#define NR_SLOTS 1
+// slabs.  A context has two, used in turn by nr_batch_submit, so one batch's
+// tables are built on the host while the batch before runs.  (Splitting one
+// batch over both slots measured slower on 4096 K15 instances: the host passes
+// are dominated by fixed costs and two concurrent launches lengthen the span.)
+#define NR_SLOTS 2
 struct NrSlot {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;   // around the part's kernels
@@ -327,6 +327,11 @@ struct NrSlot {
     WarpRunCfg cfgp{};
     size_t off_out = 0;
     int first_grid = 0, block = 0;
+    // asynchronous batches: the ticket queued here and what its wait needs
+    int64_t ticket = 0;
+    bool pending = false;
+    uint64_t capacity = 0;
+    nr_options opt{};
 };
 
 struct nr_context {
@@ -341,6 +346,9 @@ struct nr_context {
     NrSlot slot[NR_SLOTS];      // warp engine: one per part of a batch in flight
     std::map<std::pair<const void *, size_t>, int> occupancy;   // (kernel, smem) -> blocks per SM
     std::unique_ptr<NrPool> pool;   // host worker threads, created by the first large batch
+    int64_t next_ticket = 1;        // asynchronous batches
+    std::map<int64_t, int> done_rc; // status of batches finished before their wait
+    cudaEvent_t ev_after = nullptr; // orders a batch after a caller's stream
     int smem_optin = 0;             // largest dynamic shared memory a block may opt in to
     void *model = nullptr;          // learned scorer: FP32 parameters and their BF16 copy
     NrMlpDev mlp{};
@@ -607,6 +615,7 @@ extern "C" void nr_context_destroy(nr_context *c)
     if (c->qbuf) cudaFree(c->qbuf);
     if (c->sbuf) cudaFree(c->sbuf);
     for (NrSlot &sl : c->slot) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);   // a batch submitted and never waited for
         if (sl.wslab) cudaFree(sl.wslab);
         if (sl.wbuf) cudaFree(sl.wbuf);
         if (sl.hbuf) cudaFreeHost(sl.hbuf);
@@ -617,6 +626,7 @@ extern "C" void nr_context_destroy(nr_context *c)
     if (c->model) cudaFree(c->model);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev_after) cudaEventDestroy(c->ev_after);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1157,7 +1167,8 @@ static int slot_ready(NrSlot &sl)
 // upload, the kernels and the read-back of the outputs on slot `sl`.  `base`
 // is the index of gs[0] in the caller's batch (for collected children).
 static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_graph *gs, const int32_t *srcs,
-                       const int32_t *dsts, const WarpRunCfg &cfg, nr_result *res, PhaseClock &pc)
+                       const int32_t *dsts, const WarpRunCfg &cfg, nr_result *res, PhaseClock &pc,
+                       cudaStream_t after = nullptr)
 {
     constexpr int NCLS = 3 * NR_MAX_W4;      // class = lane-group width x mask blocks
     int rc0 = slot_ready(sl);
@@ -1302,6 +1313,11 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     unsigned char *wb = static_cast<unsigned char *>(sl.wbuf);
     cudaStream_t s = sl.stream;
     pc.mark("geometry");
+    if (after) {                          // the upload waits for the caller's stream
+        if (!c->ev_after) NR_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_after, cudaEventDisableTiming));
+        NR_CUDA_TRY(cudaEventRecord(c->ev_after, after));
+        NR_CUDA_TRY(cudaStreamWaitEvent(s, c->ev_after, 0));
+    }
     NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, up_bytes, cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaEventRecord(sl.ev0, s));
     int first_grid = 0;
@@ -1398,66 +1414,71 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
     return warp_finish(c, c->slot[0], 0, handover, pc);
 }
 
-extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs,
-                                    const int32_t *dsts, uint64_t capacity, const nr_options *opt,
-                                    nr_result *res)
+// Checks of a batch: shapes, CSR arrays (once per run of instances sharing them),
+// probabilities of graphs above 32 nodes (the warp engine checks its own while
+// copying them).  *n_wide = graphs above 32 nodes.
+static int batch_validate(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
+                          const nr_options &o, int *n_wide)
 {
-    if (!c || n < 0 || (n > 0 && (!gs || !srcs || !dsts || !res))) return NR_ERR_INVALID;
-    if (n == 0) return NR_OK;
-    nr_options o;
-    if (opt) o = *opt; else nr_options_default(&o);
-    std::lock_guard<std::mutex> lock(c->mu);
-    PhaseClock pc;
-    std::atomic<int> bad(NR_OK), n_wide(0);
-    const bool wave_order = o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
-    // shapes here; CSR arrays shared with the previous instance are checked once (there, or
-    // the batch fails there); probabilities where the tables are built (the warp engine) or
-    // below (larger graphs)
+    std::atomic<int> bad(NR_OK), wide(0);
     c->parallel_for(n, 256, [&](int i) {
         int rc = validate_shape(&gs[i], srcs[i], dsts[i]);
         if (!rc && !(i > 0 && same_structure_arrays(&gs[i], &gs[i - 1]))) rc = validate_structure(&gs[i]);
-        if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) rc = validate_probabilities(&gs[i]);
         if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) {
-            if (o.order == NR_ORDER_LEARNED) rc = NR_ERR_UNSUPPORTED;    // learned order: n <= 32 only
-            n_wide.fetch_add(1);
+            rc = validate_probabilities(&gs[i]);
+            if (!rc && o.order == NR_ORDER_LEARNED) rc = NR_ERR_UNSUPPORTED;    // learned order: n <= 32 only
+            wide.fetch_add(1);
         }
         if (rc) bad.store(rc);
     });
+    *n_wide = wide.load();
     if (bad.load() != NR_OK) return bad.load();
-    pc.mark("validate");
-    NR_CUDA_TRY(cudaSetDevice(c->device));
-    const bool exhaustive = !(o.target_width > 0) && wave_order;
     if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
-    const WarpRunCfg cfg = warp_cfg(&o, capacity, exhaustive);
-    // graphs of up to 32 nodes run together on the warp engine; larger ones one at a time on
-    // the whole-GPU wave engine, as do warp-engine instances that outgrow a warp's budget
-    std::vector<int> small_idx, wide_idx, handover;
-    int rc;
-    if (n_wide.load() == 0) {
-        rc = run_warp_batch(c, n, gs, srcs, dsts, cfg, res, &handover, &pc);
-        if (rc) return rc;
-    } else {
-        for (int i = 0; i < n; ++i) (gs[i].n_nodes > NR_SMALL_MAX_N ? wide_idx : small_idx).push_back(i);
-        if (!small_idx.empty()) {
-            const int m = (int)small_idx.size();
-            std::vector<nr_graph> sg(m);
-            std::vector<int32_t> ss(m), sd(m);
-            std::vector<nr_result> sr(m);
-            for (int k = 0; k < m; ++k) {
-                sg[k] = gs[small_idx[k]]; ss[k] = srcs[small_idx[k]]; sd[k] = dsts[small_idx[k]];
-                sr[k] = res[small_idx[k]];
-            }
-            std::vector<int> hk;
-            rc = run_warp_batch(c, m, sg.data(), ss.data(), sd.data(), cfg, sr.data(), &hk);
-            if (rc) return rc;
-            for (int k = 0; k < m; ++k) res[small_idx[k]] = sr[k];
-            for (int k : hk) handover.push_back(small_idx[k]);
-        }
-    }
+    return NR_OK;
+}
+
+static WarpRunCfg batch_cfg(const nr_options &o, uint64_t capacity)
+{
+    const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
+    return warp_cfg(&o, capacity, exhaustive);
+}
+
+// Instances the warp engine handed over (exhaustive runs that outgrew a warp's
+// budget) finish on the whole-GPU engine.
+static int run_handover(nr_context *c, const std::vector<int> &handover, const nr_graph *gs, const int32_t *srcs,
+                        const int32_t *dsts, uint64_t capacity, const nr_options &o, nr_result *res)
+{
     for (int i : handover) {
-        rc = run_grid_small(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, &res[i]);
+        const int rc = run_grid_small(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, &res[i]);
         if (rc) return rc;
     }
+    return NR_OK;
+}
+
+// A batch with graphs above 32 nodes, start to end: graphs of up to 32 nodes run
+// together on the warp engine, larger ones one at a time on the whole-GPU engine.
+static int run_mixed_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
+                           uint64_t capacity, const nr_options &o, nr_result *res)
+{
+    std::vector<int> small_idx, wide_idx, handover;
+    for (int i = 0; i < n; ++i) (gs[i].n_nodes > NR_SMALL_MAX_N ? wide_idx : small_idx).push_back(i);
+    int rc;
+    if (!small_idx.empty()) {
+        const int m = (int)small_idx.size();
+        std::vector<nr_graph> sg(m);
+        std::vector<int32_t> ss(m), sd(m);
+        std::vector<nr_result> sr(m);
+        for (int k = 0; k < m; ++k) {
+            sg[k] = gs[small_idx[k]]; ss[k] = srcs[small_idx[k]]; sd[k] = dsts[small_idx[k]];
+        }
+        std::vector<int> hk;
+        rc = run_warp_batch(c, m, sg.data(), ss.data(), sd.data(), batch_cfg(o, capacity), sr.data(), &hk);
+        if (rc) return rc;
+        for (int k = 0; k < m; ++k) res[small_idx[k]] = sr[k];
+        for (int k : hk) handover.push_back(small_idx[k]);
+    }
+    rc = run_handover(c, handover, gs, srcs, dsts, capacity, o, res);
+    if (rc) return rc;
     for (int i : wide_idx) {
         nr_result *r = &res[i];
         memset(r, 0, sizeof(*r));
@@ -1467,6 +1488,97 @@ extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, co
         if (rc) return rc;
     }
     return NR_OK;
+}
+
+// Finish the batch queued on a slot: results, then handed-over instances.
+static int slot_finish(nr_context *c, NrSlot &sl)
+{
+    PhaseClock pc;
+    std::vector<int> handover;
+    sl.pending = false;
+    int rc = warp_finish(c, sl, 0, &handover, pc);
+    if (!rc) rc = run_handover(c, handover, sl.gs, sl.srcs, sl.dsts, sl.capacity, sl.opt, sl.res);
+    return rc;
+}
+
+// Finish every batch still in flight (before work that uses slot 0 or swaps the model);
+// their statuses wait for their tickets.
+static void drain(nr_context *c)
+{
+    for (NrSlot &sl : c->slot)
+        if (sl.pending) c->done_rc[sl.ticket] = slot_finish(c, sl);
+}
+
+static void record_done(nr_context *c, int64_t ticket, int rc)
+{
+    c->done_rc[ticket] = rc;
+    while (c->done_rc.size() > 64) c->done_rc.erase(c->done_rc.begin());    // waits never made
+}
+
+extern "C" int nr_batch_submit(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
+                               uint64_t capacity, const nr_options *opt, nr_result *res, void *after_stream,
+                               int64_t *ticket)
+{
+    if (!c || !ticket || n < 0 || (n > 0 && (!gs || !srcs || !dsts || !res))) return NR_ERR_INVALID;
+    nr_options o;
+    if (opt) o = *opt; else nr_options_default(&o);
+    std::lock_guard<std::mutex> lock(c->mu);
+    const int64_t t = c->next_ticket++;
+    *ticket = t;
+    if (n == 0) { record_done(c, t, NR_OK); return NR_OK; }
+    PhaseClock pc;
+    int n_wide = 0;
+    int rc = batch_validate(c, n, gs, srcs, dsts, o, &n_wide);
+    if (rc) { record_done(c, t, rc); return rc; }
+    pc.mark("validate");
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    if (n_wide) {                             // larger graphs: the whole batch now
+        drain(c);
+        rc = run_mixed_batch(c, n, gs, srcs, dsts, capacity, o, res);
+        record_done(c, t, rc);
+        return rc;
+    }
+    NrSlot &sl = c->slot[(t - 1) % NR_SLOTS];
+    if (sl.pending) record_done(c, sl.ticket, slot_finish(c, sl));
+    rc = warp_submit(c, sl, 0, n, gs, srcs, dsts, batch_cfg(o, capacity), res, pc,
+                     static_cast<cudaStream_t>(after_stream));
+    if (rc) {
+        cudaStreamSynchronize(sl.stream);
+        record_done(c, t, rc);
+        return rc;
+    }
+    sl.ticket = t;
+    sl.pending = true;
+    sl.capacity = capacity;
+    sl.opt = o;
+    return NR_OK;
+}
+
+extern "C" int nr_batch_wait(nr_context *c, int64_t ticket)
+{
+    if (!c) return NR_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(c->mu);
+    for (NrSlot &sl : c->slot)
+        if (sl.pending && sl.ticket == ticket) {
+            NR_CUDA_TRY(cudaSetDevice(c->device));
+            return slot_finish(c, sl);
+        }
+    auto it = c->done_rc.find(ticket);
+    if (it == c->done_rc.end()) return NR_ERR_INVALID;
+    const int rc = it->second;
+    c->done_rc.erase(it);
+    return rc;
+}
+
+extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs,
+                                    const int32_t *dsts, uint64_t capacity, const nr_options *opt,
+                                    nr_result *res)
+{
+    if (!c || n < 0 || (n > 0 && (!gs || !srcs || !dsts || !res))) return NR_ERR_INVALID;
+    int64_t t = 0;
+    const int rc = nr_batch_submit(c, n, gs, srcs, dsts, capacity, opt, res, nullptr, &t);
+    const int rw = nr_batch_wait(c, t);
+    return rc ? rc : rw;
 }
 
 // Autotuner: time candidate warp-engine settings on (a sample of) the batch
@@ -1533,6 +1645,7 @@ extern "C" int nr_context_set_model(nr_context *c, const float *params)
 {
     if (!c || !params) return NR_ERR_INVALID;
     std::lock_guard<std::mutex> lock(c->mu);
+    drain(c);                          // finish batches in flight: slot 0 and the model are used here
     NR_CUDA_TRY(cudaSetDevice(c->device));
     int rc = nr_mlp_upload(params, &c->model, &c->mlp, c->stream);
     if (rc) return rc;
@@ -1562,6 +1675,7 @@ extern "C" int nr_collect_children(nr_context *c, int n, const nr_graph *gs, con
         if (gs[i].n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
     }
     std::lock_guard<std::mutex> lock(c->mu);
+    drain(c);                          // finish batches in flight: slot 0 and the model are used here
     NR_CUDA_TRY(cudaSetDevice(c->device));
     if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
     const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
@@ -1621,6 +1735,7 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     res->dst = dst;
     res->mask_words = std::max(1, (2 * g->n_edges + 31) / 32);
     std::lock_guard<std::mutex> lock(c->mu);
+    drain(c);                          // finish batches in flight: slot 0 and the model are used here
     NR_CUDA_TRY(cudaSetDevice(c->device));
     if (g->n_nodes > NR_SMALL_MAX_N) return run_wide(c, g, src, dst, capacity, &o, res);
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {

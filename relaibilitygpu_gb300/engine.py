@@ -71,7 +71,7 @@ class NrResult(C.Structure):
 EXPORTS = [
     "nr_options_default", "nr_status_string", "nr_abi_version", "nr_graph_load", "nr_graph_free",
     "nr_initial_mask", "nr_context_create", "nr_context_destroy", "nr_reliability", "nr_reliability_ctx",
-    "nr_reliability_batch", "nr_format_result", "nr_reliability_noalloc", "nr_autotune",
+    "nr_reliability_batch", "nr_batch_submit", "nr_batch_wait", "nr_format_result", "nr_reliability_noalloc", "nr_autotune",
     "nr_mlp_param_count", "nr_mlp_init", "nr_mlp_grad", "nr_mlp_train", "nr_mlp_infer", "nr_context_set_model",
     "nr_collect_children",
 ]
@@ -112,6 +112,12 @@ def lib() -> C.CDLL:
                                        C.POINTER(C.c_int32), C.c_uint64, C.POINTER(NrOptions),
                                        C.POINTER(NrResult)]
     L.nr_reliability_batch.restype = C.c_int
+    L.nr_batch_submit.argtypes = [C.c_void_p, C.c_int, C.POINTER(NrGraph), C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int32), C.c_uint64, C.POINTER(NrOptions), C.POINTER(NrResult),
+                                  C.c_void_p, C.POINTER(C.c_int64)]
+    L.nr_batch_submit.restype = C.c_int
+    L.nr_batch_wait.argtypes = [C.c_void_p, C.c_int64]
+    L.nr_batch_wait.restype = C.c_int
     L.nr_reliability_noalloc.argtypes = [C.POINTER(NrGraph), C.c_int, C.c_int, C.POINTER(NrOptions),
                                          C.POINTER(NrResult)]
     L.nr_reliability_noalloc.restype = C.c_int
@@ -279,6 +285,26 @@ class Context:
 
     def reliability_batch(self, graphs: Sequence[Graph], srcs, dsts, capacity: int = 0, **opts):
         return self.run_batch(Batch(graphs, srcs, dsts), capacity=capacity, **opts)
+
+    def submit(self, batch: "Batch", capacity: int = 0, after_stream: int = 0, **opts) -> int:
+        """Queue a prepared batch with nr_batch_submit and return its ticket.
+
+        The batch's tables are built before this returns; the GPU work runs
+        while the caller goes on (for example to submit the next batch).
+        `after_stream` is a raw cudaStream_t (e.g. torch's
+        `torch.cuda.current_stream().cuda_stream`): the upload starts after the
+        work already queued there.  The batch's results are valid after
+        wait(ticket); do not resubmit the same Batch object before that."""
+        o = make_options(**opts)
+        t = C.c_int64()
+        _check(lib().nr_batch_submit(self.h, batch.n, batch.arr, batch.s.ctypes.data_as(C.POINTER(C.c_int32)),
+                                     batch.d.ctypes.data_as(C.POINTER(C.c_int32)), int(capacity), C.byref(o),
+                                     batch.res, C.c_void_p(after_stream or None), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int) -> None:
+        """Finish a submitted batch (nr_batch_wait): its Batch.res is filled."""
+        _check(lib().nr_batch_wait(self.h, int(ticket)))
 
     def run_batch(self, batch: "Batch", capacity: int = 0, raw: bool = False, **opts):
         """Solve a prepared batch (host arrays marshalled once) with nr_reliability_batch."""

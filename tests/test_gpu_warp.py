@@ -223,3 +223,44 @@ def test_batch_rejects_bad_instances(ctx, engine_lib):
     # the context stays usable
     r = ctx.reliability_batch(gs[:4], [0] * 4, [8] * 4, target_width=1e-6)
     assert all(x.stop == 1 for x in r)
+
+
+def test_async_batches_match_sync(ctx, oracle):
+    """nr_batch_submit / nr_batch_wait: three batches in flight on two slots (the third submit
+    finishes the first), waits in any order, results identical to the synchronous call."""
+    from relaibilitygpu_gb300 import graphs
+    import relaibilitygpu_gb300 as nr
+    sets = [[graphs.complete(12, p_range=(0.85, 0.99), seed=1000 * k + i) for i in range(700)] for k in range(3)]
+    opts = dict(target_width=1e-6, bucket_shift=1, n_buckets=128)
+    ref = [ctx.reliability_batch(gs, [0] * 700, [11] * 700, **opts) for gs in sets]
+    batches = [nr.Batch(gs, [0] * 700, [11] * 700) for gs in sets]
+    tickets = [ctx.submit(b, **opts) for b in batches]
+    for t in (tickets[2], tickets[0], tickets[1]):
+        ctx.wait(t)
+    for b, rr in zip(batches, ref):
+        got = [nr.Result.from_raw(b.res[i]) for i in range(b.n)]
+        for a, r in zip(got, rr):
+            assert (a.R, a.esp, a.nodes, a.paths, a.iterations, a.queued) == (r.R, r.esp, r.nodes, r.paths,
+                                                                               r.iterations, r.queued)
+    check_wave_parity(nr.Result.from_raw(batches[1].res[5]),
+                      oracle.run(sets[1][5], 0, 11, bucket_shift=1, n_buckets=128, target_width=1e-6))
+    with pytest.raises(nr.NrError):
+        ctx.wait(tickets[0])                  # already waited for
+
+
+def test_async_batch_ordering_and_drain(ctx):
+    """The upload waits for the caller's stream; a synchronous call in between finishes the
+    batch in flight first, and its wait still succeeds."""
+    torch = pytest.importorskip("torch")
+    from relaibilitygpu_gb300 import graphs
+    import relaibilitygpu_gb300 as nr
+    gs = [graphs.complete(10, p_range=(0.8, 0.99), seed=i) for i in range(300)]
+    b = nr.Batch(gs, [0] * 300, [9] * 300)
+    ref = ctx.reliability_batch(gs, [0] * 300, [9] * 300, target_width=1e-7)
+    buf = torch.empty(64 << 20, dtype=torch.float32, device="cuda:0")
+    buf.fill_(1.0)                               # queued on torch's stream, ahead of the upload
+    t = ctx.submit(b, target_width=1e-7, after_stream=torch.cuda.current_stream().cuda_stream)
+    single = ctx.reliability(gs[3], 0, 9, target_width=1e-7)
+    ctx.wait(t)
+    assert single.R == ref[3].R
+    assert [b.res[i].R for i in range(300)] == [r.R for r in ref]
