@@ -94,6 +94,11 @@ def workload(name: str):
     raise SystemExit(f"unknown workload {name}")
 
 
+# DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu capture of the same
+# workload (the launch summaries are kept under profiles/).
+TRAFFIC = {"k15batch": 4.690e6, "k10": 136.8e6}
+
+
 def item_bytes(n_edges: int) -> int:
     """Algorithmic bytes of one queued subproblem: packed 2-bit mask words + FP64 mass."""
     return 4 * max(1, (2 * n_edges + 31) // 32) + 8
@@ -408,9 +413,11 @@ def main():
         "result": stats,
         "time_to_bound": ttb,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": TRAFFIC.get(args.workload),
                      "note": f"achieved = algorithmic bytes (4W+8 per queued subproblem, written once and "
-                             f"read once) / kernel time; peak {peak_kind} copy bandwidth"},
+                             f"read once) / kernel time; peak {peak_kind} copy bandwidth; traffic = DRAM "
+                             f"bytes read + written per launch in one ncu capture (profiles/), the queue "
+                             f"itself stays in L2"},
         "e2e": ({"value": tot["pipe_nodes"] / tot["pipe_wall_max"], "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                  "d2h_bytes_per_step": int(d2h),
                  "api": "nr_batch_submit / nr_batch_wait, two batches in flight; L2 flushed before every step's "
