@@ -82,3 +82,43 @@ def test_learned_order_needs_a_model(engine_lib):
     with engine_lib.Context(0) as ctx:
         with pytest.raises(engine_lib.NrError):
             ctx.reliability(graphs.complete(6, p=0.5), 0, 5, order="learned")
+
+
+@pytest.mark.parametrize("family", ["k15_u90_99_1e-6", "k10_u50_95_1e-4"])
+def test_trained_scorer_gain_over_plain_order(L, engine_lib, family, capsys):
+    """What the shipped scorer gains over the plain max-mass order, on held-out seeds of the two
+    training families: subproblems popped until ESP + queued <= target, summed over 128
+    instances, at one bucket per factor of two (the resolution where a priority can reorder).
+
+    Measured on a GB300: K15 p~U[0.9,0.99] to 1e-6, 3,795 subproblems either way (ratio 1.000);
+    K10 p~U[0.5,0.95] to 1e-4, 139,252 plain against 178,874 learned (ratio 1.285, a loss).  On
+    these families max-mass is already about the best one-step order (an exact-residual key,
+    computed by brute force on the CPU, does not beat it either), so the scorer gains nothing and
+    its inference makes each pop slower.  The test pins the exactness and rigour of both runs and
+    bounds the loss (at most 1.5x the subproblems); the printed line is the measurement."""
+    import os
+    if not os.path.exists(L.DEFAULT_MODEL):
+        pytest.skip("no trained scorer")
+    from relaibilitygpu_gb300 import graphs
+    if family.startswith("k15"):
+        gs = [graphs.complete(15, p_range=(0.9, 0.99), seed=50_000 + s) for s in range(128)]
+        target = 1e-6
+    else:
+        gs = [graphs.complete(10, p_range=(0.5, 0.95), seed=60_000 + s) for s in range(128)]
+        target = 1e-4
+    srcs, dsts = [0] * len(gs), [g.n_nodes - 1 for g in gs]
+    opts = dict(target_width=target, bucket_shift=0, n_buckets=64, capacity=1 << 16)
+    with engine_lib.Context(0) as ctx:
+        plain = ctx.reliability_batch(gs, srcs, dsts, order="maxmass", **opts)
+        L.set_model(ctx, L.load())
+        learned = ctx.reliability_batch(gs, srcs, dsts, order="learned", **opts)
+    for a, b in zip(plain, learned):
+        assert a.stop == 1 and b.stop == 1 and a.esp <= target and b.esp <= target
+        # both bracket the same exact value: the intervals overlap
+        assert max(a.R, b.R) <= min(a.R + a.esp, b.R + b.esp) + 1e-15
+    n_plain = sum(r.nodes for r in plain)
+    n_learned = sum(r.nodes for r in learned)
+    with capsys.disabled():
+        print(f"\n[{family}] subproblems to the bound over {len(gs)} instances: plain {n_plain}, "
+              f"learned {n_learned} (ratio {n_learned / n_plain:.3f})")
+    assert n_learned <= 1.5 * n_plain
