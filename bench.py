@@ -372,10 +372,24 @@ def main():
             nn = sum(rr[i].nodes for i in range(len(w["graphs"])))
             return {"ms": rr[0].ms, "nodes": nn, "subproblems_per_sec": nn / (rr[0].ms / 1e3)}
 
+        def per_graph_launches():
+            # the same 4096 instances one call (one launch) each, with the batch's tuned settings
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            nn, dev = 0, 0.0
+            for g, s_, d_ in zip(w["graphs"], w["srcs"], w["dsts"]):
+                r = ctx.reliability(g, s_, d_, capacity=w["capacity"], **w["opts"])
+                nn += r.nodes
+                dev += r.ms
+            wall = time.perf_counter() - t0
+            return {"launches": len(w["graphs"]), "wall_ms": 1e3 * wall, "device_ms_sum": dev,
+                    "subproblems_per_sec_wall": nn / wall, "subproblems_per_sec_device": nn / (dev / 1e3)}
+
         try:
             ttb = {"plain": latency("maxmass"), "learned": None, "instances": 16,
                    "breadth_first": latency("maxmass", bucket_shift=-1),
-                   "plain_batch": batch_run("maxmass")}
+                   "plain_batch": batch_run("maxmass"),
+                   "per_graph_launches": per_graph_launches()}
         except Exception as exc:                     # keep the bench line; report the failure
             ttb = {"plain": f"failed: {exc}", "learned": None, "instances": 16}
         if os.path.exists(LR.DEFAULT_MODEL) and isinstance(ttb["plain"], dict):
