@@ -70,6 +70,14 @@ enum {
     NR_ORDER_LEARNED = 3    /* bucket key and branch order from the learned scorer (never mass) */
 };
 
+/* branching of a subproblem whose optimistic BFS finds a path */
+enum {
+    NR_BRANCH_PATH = 0,     /* one disjoint child per UNKNOWN path edge (main.cu:114-283, the default) */
+    NR_BRANCH_FORK = 1      /* a path of up edges puts the mass in R; else fork on the optimistic path's
+                               UNKNOWN edge with the largest p, down and up (main.cu:303-430 with
+                               :550-565, FORK_BEST_EDGE); not with NR_ORDER_LEARNED */
+};
+
 typedef struct nr_options {
     double   truncation_eps;  /* popped mass below eps goes to ESP (main.cu:537-543); 0 = off.
                                  The reference CLI default is 1e-15. */
@@ -89,7 +97,8 @@ typedef struct nr_options {
                                  hand the instance to the whole-GPU engine; 0 = engine default */
     int32_t  pages_per_warp;  /* warp engine: queue pages of 32 subproblems per warp when capacity is 0
                                  (0 = 512) */
-    int32_t  reserved[3];
+    int32_t  branching;       /* NR_BRANCH_* */
+    int32_t  reserved[2];
 } nr_options;
 
 typedef struct nr_result {

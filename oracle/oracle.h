@@ -21,6 +21,12 @@
  *                               seq/seq.cpp:539-578 (child k = first k-1
  *                               UNKNOWN path edges up, k-th down, src side
  *                               first; all-up mass -> R)
+ *   fork branching ............ workingPad/main.cu:303-430 with :550-565
+ *                               (FORK_BEST_EDGE) and seq/seq_best.cpp:358-389:
+ *                               a path of up edges puts the whole mass in R;
+ *                               else the UNKNOWN edge of the optimistic path
+ *                               with the largest p (ties: the one nearest
+ *                               dst) gives two children, down and up
  *   counts .................... workingPad/main.cu:533-534 (every pop is a
  *                               node), :251 and :262 (overflow spills and
  *                               leaves are paths); seq/seq.cpp:551-561
@@ -53,6 +59,7 @@ typedef struct og_graph {
 
 enum { OG_BFS_LEVEL = 0, OG_BFS_FIFO = 1 };
 enum { OG_ORDER_WAVES = 0, OG_ORDER_HEAP = 1, OG_ORDER_DFS = 2 };
+enum { OG_BRANCH_PATH = 0, OG_BRANCH_FORK = 1 };
 
 typedef struct og_opts {
     int32_t  bfs_rule;      /* OG_BFS_LEVEL (GPU engine, main.cu) or OG_BFS_FIFO (seq.cpp) */
@@ -65,6 +72,8 @@ typedef struct og_opts {
     double   target_width;  /* waves/heap: stop once ESP + queued mass <= target; 0 disables */
     uint64_t capacity;      /* queued-item limit, overflow spills to ESP; 0 = unlimited */
     uint64_t max_nodes;     /* stop after about this many pops (timing samples); 0 = none */
+    int32_t  branching;     /* OG_BRANCH_PATH (disjoint path children) or OG_BRANCH_FORK */
+    int32_t  pad0;
 } og_opts;
 
 typedef struct og_result {

@@ -27,11 +27,14 @@ class OgGraph(C.Structure):
                 ("edge_id", C.POINTER(C.c_int32)), ("edge_p", C.POINTER(C.c_double))]
 
 
+BRANCHING = {"path": 0, "fork": 1}
+
+
 class OgOpts(C.Structure):
     _fields_ = [("bfs_rule", C.c_int32), ("precheck", C.c_int32), ("order", C.c_int32),
                 ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("threads", C.c_int32),
                 ("eps", C.c_double), ("target_width", C.c_double), ("capacity", C.c_uint64),
-                ("max_nodes", C.c_uint64)]
+                ("max_nodes", C.c_uint64), ("branching", C.c_int32), ("pad0", C.c_int32)]
 
 
 class OgResult(C.Structure):
@@ -112,7 +115,7 @@ class _View:
 
 
 def _opts(rule="level", precheck=False, order="waves", bucket_shift=-1, n_buckets=1, threads=1, eps=0.0,
-          target_width=0.0, capacity=0, max_nodes=0) -> OgOpts:
+          target_width=0.0, capacity=0, max_nodes=0, branching="path") -> OgOpts:
     o = OgOpts()
     lib().og_default_opts(C.byref(o))
     o.bfs_rule = RULES[rule]
@@ -125,6 +128,7 @@ def _opts(rule="level", precheck=False, order="waves", bucket_shift=-1, n_bucket
     o.target_width = float(target_width)
     o.capacity = int(capacity)
     o.max_nodes = int(max_nodes)
+    o.branching = BRANCHING[branching]
     return o
 
 
@@ -152,7 +156,7 @@ def run_batch(batch: BatchArgs, threads: int = 1, **kw):
 
 def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, order: str = "waves",
         bucket_shift: int = -1, n_buckets: int = 1, threads: int = 1, eps: float = 0.0,
-        target_width: float = 0.0, capacity: int = 0, max_nodes: int = 0) -> OracleResult:
+        target_width: float = 0.0, capacity: int = 0, max_nodes: int = 0, branching: str = "path") -> OracleResult:
     v = _View(g)
     o = OgOpts()
     lib().og_default_opts(C.byref(o))
@@ -166,6 +170,7 @@ def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, orde
     o.target_width = float(target_width)
     o.capacity = int(capacity)
     o.max_nodes = int(max_nodes)
+    o.branching = BRANCHING[branching]
     r = OgResult()
     rc = lib().og_run(C.byref(v.c), int(src), int(dst), C.byref(o), C.byref(r))
     if rc != 0:

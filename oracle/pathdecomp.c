@@ -256,7 +256,7 @@ void og_default_opts(og_opts *o)
 typedef struct {
     const og_graph *g;
     const double *q;
-    int src, dst, W, rule, precheck;
+    int src, dst, W, rule, precheck, branching;
     double eps;
     /* BFS scratch */
     uint32_t gen;
@@ -275,7 +275,7 @@ static void x_init(xctx *x, const og_graph *g, const double *q, int src, int dst
     x->g = g; x->q = q; x->src = src; x->dst = dst;
     x->W = (g->n_edges * 2 + 31) / 32;
     if (x->W < 1) x->W = 1;
-    x->rule = o->bfs_rule; x->precheck = o->precheck; x->eps = o->eps;
+    x->rule = o->bfs_rule; x->precheck = o->precheck; x->eps = o->eps; x->branching = o->branching;
     x->vis = (uint32_t *)calloc(n, sizeof(uint32_t));
     x->par_e = (int32_t *)malloc(n * sizeof(int32_t));
     x->par_v = (int32_t *)malloc(n * sizeof(int32_t));
@@ -307,7 +307,16 @@ static void sort_small(int32_t *a, int n)
  * with one lane per word), so the parent is the smallest frontier node.
  * FIFO rule: seq/seq.cpp:311-351. Both stop when dst is first discovered,
  * which fixes parent[dst] the same way as finishing the level would. */
-static int x_bfs(xctx *x, const uint32_t *m)
+static int x_bfs_states(xctx *x, const uint32_t *m, int up_only);
+static int x_bfs(xctx *x, const uint32_t *m) { return x_bfs_states(x, m, 0); }
+
+/* arc usable by the search: not down, or (up_only) up */
+static inline int usable(const uint32_t *m, int e, int up_only)
+{
+    return up_only ? st_get(m, e) == 1 : notdown(m, e);
+}
+
+static int x_bfs_states(xctx *x, const uint32_t *m, int up_only)
 {
     const og_graph *g = x->g;
     int src = x->src, dst = x->dst;
@@ -322,7 +331,7 @@ static int x_bfs(xctx *x, const uint32_t *m)
             int u = x->cur[head++];
             for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; j++) {
                 int v = g->col_idx[j], e = g->edge_id[j];
-                if (x->vis[v] != gen && notdown(m, e)) {
+                if (x->vis[v] != gen && usable(m, e, up_only)) {
                     x->vis[v] = gen; x->par_v[v] = u; x->par_e[v] = e;
                     x->cur[tail++] = v;
                     if (v == dst) return 1;
@@ -339,7 +348,7 @@ static int x_bfs(xctx *x, const uint32_t *m)
             int u = x->cur[i];
             for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; j++) {
                 int v = g->col_idx[j], e = g->edge_id[j];
-                if (x->vis[v] != gen && notdown(m, e)) {
+                if (x->vis[v] != gen && usable(m, e, up_only)) {
                     x->vis[v] = gen; x->par_v[v] = u; x->par_e[v] = e;
                     x->nxt[nn++] = v;
                     if (v == dst) return 1;
@@ -358,6 +367,45 @@ typedef int (*sink_fn)(void *ud, const uint32_t *mask, double mass);
 
 /* Expand one popped subproblem: workingPad/main.cu:504-628 with the sweep of
  * :114-283, FP64 products in path order, src-side hop first. */
+/* Fork branching (main.cu:303-430, :550-565): a path of up edges means the
+ * subproblem is connected, so its whole mass goes to R; else the optimistic
+ * path's UNKNOWN edge with the largest p (ties: nearest dst, as the
+ * reference's dst-first scan with a strict comparison keeps) gives two
+ * children, that edge down (mass x q) and up (mass x p), queued in that order. */
+static void x_fork(xctx *x, const uint32_t *m, double mass, sink_fn sink, void *ud)
+{
+    if (x_bfs_states(x, m, 1)) {
+        x->leaves++;
+        ks_add(&x->R, mass);
+        return;
+    }
+    if (!x_bfs(x, m)) { x->dead++; return; }
+    const double *p = x->g->edge_p;
+    int best = -1;
+    double bp = -1.0;
+    for (int v = x->dst; v != x->src; v = x->par_v[v]) {      /* dst side first */
+        int e = x->par_e[v];
+        if (st_get(m, e) == 3 && p[e] > bp) { bp = p[e]; best = e; }
+    }
+    if (best < 0) {            /* cannot happen: no path of up edges exists */
+        x->leaves++;
+        ks_add(&x->R, mass);
+        return;
+    }
+    for (int k = 0; k < 2; k++) {
+        memcpy(x->child, m, x->W * sizeof(uint32_t));
+        double cm;
+        if (k == 0) { set_down(x->child, best); cm = mass * x->q[best]; }
+        else { set_up(x->child, best); cm = mass * p[best]; }
+        if (sink(ud, x->child, cm)) {
+            x->spilled++;
+            ks_add(&x->esp_spill, cm);
+        } else {
+            x->pushes++;
+        }
+    }
+}
+
 static void x_expand(xctx *x, const uint32_t *m, double mass, sink_fn sink, void *ud)
 {
     x->nodes++;
@@ -366,6 +414,7 @@ static void x_expand(xctx *x, const uint32_t *m, double mass, sink_fn sink, void
         ks_add(&x->esp_trunc, mass);
         return;
     }
+    if (x->branching == OG_BRANCH_FORK) { x_fork(x, m, mass, sink, ud); return; }
     if (!x_bfs(x, m)) { x->dead++; return; }
     /* path hops in src -> dst order */
     int L = 0;

@@ -36,6 +36,9 @@ const void *nr_warp_kernel_ptr_g8(int w4);
 const void *nr_warp_kernel_ptr_g16(int w4);
 const void *nr_warp_kernel_ptr_g32(int w4);
 const void *nr_warp_learn_kernel_ptr_g8(int w4);
+const void *nr_warp_fork_kernel_ptr_g8(int w4);
+const void *nr_warp_fork_kernel_ptr_g16(int w4);
+const void *nr_warp_fork_kernel_ptr_g32(int w4);
 const void *nr_warp_learn_kernel_ptr_g16(int w4);
 const void *nr_warp_learn_kernel_ptr_g32(int w4);
 int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
@@ -69,12 +72,15 @@ const void *grid_kernel(int G, int w4)
     }
 }
 
-const void *warp_kernel(int G, int w4, bool learn = false)
+const void *warp_kernel(int G, int w4, bool learn = false, bool fork = false)
 {
     switch (G) {
-    case 8: return learn ? nr_warp_learn_kernel_ptr_g8(w4) : nr_warp_kernel_ptr_g8(w4);
-    case 16: return learn ? nr_warp_learn_kernel_ptr_g16(w4) : nr_warp_kernel_ptr_g16(w4);
-    case 32: return learn ? nr_warp_learn_kernel_ptr_g32(w4) : nr_warp_kernel_ptr_g32(w4);
+    case 8: return learn ? nr_warp_learn_kernel_ptr_g8(w4) : fork ? nr_warp_fork_kernel_ptr_g8(w4)
+                                                                 : nr_warp_kernel_ptr_g8(w4);
+    case 16: return learn ? nr_warp_learn_kernel_ptr_g16(w4) : fork ? nr_warp_fork_kernel_ptr_g16(w4)
+                                                                   : nr_warp_kernel_ptr_g16(w4);
+    case 32: return learn ? nr_warp_learn_kernel_ptr_g32(w4) : fork ? nr_warp_fork_kernel_ptr_g32(w4)
+                                                                   : nr_warp_kernel_ptr_g32(w4);
     default: return nullptr;
     }
 }
@@ -297,6 +303,7 @@ struct NrBatchScratch {
 struct WarpDump;
 struct WarpRunCfg {
     int wave_mode, shift, n_buckets, pages, escalate, warps_per_block;
+    int fork = 0;
     int learned = 0;
     const WarpDump *dump = nullptr;
     double eps, target;
@@ -690,6 +697,7 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
     P.partials = reinterpret_cast<NrPartial *>(sb + off_part);
     P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
+    P.fork = (o->branching == NR_BRANCH_FORK);
 
     // root subproblem: initial mask with mass 1 (main.cu:805-809)
     std::vector<uint32_t> root(4 * W4, 0);
@@ -840,6 +848,7 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     P.partials = reinterpret_cast<NrPartial *>(sb + off_part);
     P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
+    P.fork = (o->branching == NR_BRANCH_FORK);
     P.target_on = o->target_width > 0 ? 1 : 0;
     P.target_fix = nr_fix_of(o->target_width > 0 ? o->target_width : 0.0);
     P.max_nodes = o->max_nodes;
@@ -991,6 +1000,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     P.partials = reinterpret_cast<NrPartial *>(sb + off_part);
     P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
+    P.fork = (o->branching == NR_BRANCH_FORK);
     P.target_on = o->target_width > 0 ? 1 : 0;
     P.target_fix = nr_fix_of(o->target_width > 0 ? o->target_width : 0.0);
     P.max_nodes = o->max_nodes;
@@ -1101,6 +1111,7 @@ static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhausti
         nb = std::min(1024, (nb + 31) / 32 * 32);
         w.n_buckets = nb;
     }
+    w.fork = (o->branching == NR_BRANCH_FORK);
     w.warps_per_block = (o->warps_per_block >= 1 && o->warps_per_block <= NR_WARP_BLOCK_MAX / 32)
                             ? o->warps_per_block : NR_WARP_BLOCK / 32;
     if (capacity == 0) w.pages = o->pages_per_warp > 0 ? std::min(8192, std::max(4, o->pages_per_warp)) : 512;
@@ -1291,7 +1302,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     for (int j = 0; j < NCLS; ++j) {
         if (!class_count[j]) continue;
         const int G = 8 << (j / NR_MAX_W4), W4 = j % NR_MAX_W4 + 1;
-        const void *kfn = warp_kernel(G, W4, learn);
+        const void *kfn = warp_kernel(G, W4, learn, cfg.fork != 0);
         if (!kfn) return NR_ERR_UNSUPPORTED;
         const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn) * warps_pb;
         auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
@@ -1355,7 +1366,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.dump_cap = cfg.dump ? cfg.dump->cap : 0;
         P.dump_stride = cfg.dump ? cfg.dump->stride : 0;
         P.inst_base = base;
-        const void *kfn = warp_kernel(G, W4, learn);
+        P.fork = cfg.fork;
+        const void *kfn = warp_kernel(G, W4, learn, cfg.fork != 0);
         void *args[] = {&P};
         NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smems[j]));
         NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[j]), dim3(block), args, smems[j], s));
@@ -1434,6 +1446,8 @@ static int batch_validate(nr_context *c, int n, const nr_graph *gs, const int32_
     *n_wide = wide.load();
     if (bad.load() != NR_OK) return bad.load();
     if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
+    if (o.order == NR_ORDER_LEARNED && o.branching == NR_BRANCH_FORK) return NR_ERR_UNSUPPORTED;
+    if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
     return NR_OK;
 }
 
@@ -1678,6 +1692,7 @@ extern "C" int nr_collect_children(nr_context *c, int n, const nr_graph *gs, con
     drain(c);                          // finish batches in flight: slot 0 and the model are used here
     NR_CUDA_TRY(cudaSetDevice(c->device));
     if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
+    if (o.branching != NR_BRANCH_PATH) return NR_ERR_UNSUPPORTED;    // features describe path children
     const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
     WarpRunCfg cfg = warp_cfg(&o, capacity, exhaustive);
     cfg.escalate = 0;                 // collect from whatever the warp engine reaches
@@ -1737,6 +1752,8 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     std::lock_guard<std::mutex> lock(c->mu);
     drain(c);                          // finish batches in flight: slot 0 and the model are used here
     NR_CUDA_TRY(cudaSetDevice(c->device));
+    if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
+    if (o.branching == NR_BRANCH_FORK && o.order == NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
     if (g->n_nodes > NR_SMALL_MAX_N) return run_wide(c, g, src, dst, capacity, &o, res);
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {
         // bucketed max-mass (or learned) order: one warp owns the instance (nr_warp.cuh)

@@ -3,7 +3,9 @@
 //
 //   network_reliability <graph_file> <src> <dst> [--truncation_eps f]
 //       [--queue_capacity n] [--thresh_high f] [--thresh_low f]
-//       [--target_width f] [--order auto|waves|maxmass|learned] [--device d]
+//       [--target_width f] [--order auto|waves|maxmass|learned] [--fork] [--device d]
+//
+// --fork selects the reference's FORK_BEST_EDGE branching (main.cu:21, :550-565).
 //
 // --thresh_high / --thresh_low are accepted and ignored, as in the reference
 // (parsed at main.cu:783-786, never used).  Unknown flags are ignored too.
@@ -26,6 +28,7 @@ static void usage(const char *prog)
             "  --thresh_low  <float>      Low-priority  log-prob threshold\n"
             "  --target_width <float>     Stop once ESP + queued mass <= target (default: off)\n"
             "  --order <auto|waves|maxmass|learned>\n"
+            "  --fork                     Fork on the most reliable path edge (FORK_BEST_EDGE)\n"
             "  --device <int>             CUDA device (default 0)\n",
             prog, 1 << 20);
 }
@@ -51,6 +54,7 @@ int main(int argc, char **argv)
         else if (!strcmp(argv[i], "--thresh_low") && has) ++i;
         else if (!strcmp(argv[i], "--target_width") && has) opt.target_width = atof(argv[++i]);
         else if (!strcmp(argv[i], "--device") && has) opt.device = atoi(argv[++i]);
+        else if (!strcmp(argv[i], "--fork")) opt.branching = NR_BRANCH_FORK;
         else if (!strcmp(argv[i], "--order") && has) {
             const char *o = argv[++i];
             opt.order = !strcmp(o, "waves") ? NR_ORDER_WAVES

@@ -207,3 +207,130 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
         }
     }
 }
+
+// Level-synchronous BFS of every group of the warp over the in-neighbour rows
+// `row` (lane v: the nodes u with a usable arc u -> v); one ballot per level.
+// Returns whether dst was reached; par = the smallest frontier node with a
+// usable arc to v (lane v), level = hops of the shortest path.  All 32 lanes
+// call it; groups with search == false take part without searching.
+template <int G>
+__device__ __forceinline__ bool nr_group_bfs(uint32_t row, bool search, int n, int src, int dst, int &par, int &level)
+{
+    const int lane = threadIdx.x & 31;
+    const int v = lane & (G - 1);
+    const int gbase = lane & ~(G - 1);
+    uint32_t F = 1u << src, vis = F;
+    par = -1;
+    level = 0;
+    bool found = search && (src == dst);
+    bool searching = search && !found;
+    while (__any_sync(NR_FULL, searching)) {
+        const uint32_t t = row & F;
+        const bool hit = searching && (v < n) && (t != 0u) && !((vis >> v) & 1u);
+        if (hit) par = __ffs(t) - 1;
+        const uint32_t b = __ballot_sync(NR_FULL, hit);
+        const uint32_t nf = (G == 32) ? b : ((b >> gbase) & ((1u << G) - 1u));
+        if (searching) {
+            vis |= nf;
+            F = nf;
+            ++level;
+            if ((vis >> dst) & 1u) { found = true; searching = false; }
+            else if (nf == 0u) searching = false;
+        }
+    }
+    return found;
+}
+
+// Fork branching (workingPad/main.cu:303-430 with :550-565, FORK_BEST_EDGE):
+// a path of up edges means the subproblem is connected, so its whole mass goes
+// to R; else the optimistic path's UNKNOWN edge with the largest p (ties: the
+// one nearest dst, which the reference's dst-first scan with a strict
+// comparison keeps) gives two children: that edge down (held by the lane of its
+// hop) and up (held by lane L of the group, L = hops on the path < G).
+template <int G, int W4>
+__device__ __forceinline__ void nr_expand_fork(const NrSmallGraph &g, const NrSmemGraph &sg,
+                                               const uint32_t *my_m, bool valid, double mass, double eps,
+                                               bool &has_child, uint32_t (&w)[4 * W4], double &cm,
+                                               NrLaneAcc &acc)
+{
+    constexpr int NW = 4 * W4;
+    const int lane = threadIdx.x & 31;
+    const int v = lane & (G - 1);
+    const int gbase = lane & ~(G - 1);
+    const bool leader = (v == 0);
+    const int n = g.n, src = g.src, dst = g.dst;
+
+    has_child = false;
+    cm = 0.0;
+    if (valid && leader) acc.nodes++;
+    bool active = valid;
+    if (active && eps > 0.0 && mass < eps) {          // main.cu:537-543
+        if (leader) { acc.trunc++; nr_fix_add_mass(acc.et, mass); }
+        active = false;
+    }
+    // not-down and up in-neighbour rows of node v
+    uint32_t row = 0, row_up = 0;
+    if (active && v < n) {
+        for (int j = sg.start[v]; j < sg.start[v + 1]; ++j) {
+            const uint32_t a = sg.list[j];
+            const uint32_t st = (my_m[a >> 12] >> ((a >> 7) & 30u)) & 3u;
+            row |= (st & 1u) << (a & 31u);
+            row_up |= (uint32_t)(st == 1u) << (a & 31u);
+        }
+    }
+    int par, level;
+    const bool connected = nr_group_bfs<G>(row_up, active, n, src, dst, par, level);
+    if (active && connected && leader) { acc.leaves++; nr_fix_add_mass(acc.R, mass); }
+    const bool go = active && !connected;
+    const bool found = nr_group_bfs<G>(row, go, n, src, dst, par, level);
+    if (go && !found && leader) acc.dead++;
+    const bool live = go && found;
+    const int L = live ? level : 0;
+
+    // walk dst -> src: lane h of the group receives hop h = (u, v); hop L-1 is at dst
+    int Lmax = L;
+    for (int off = 16; off > 0; off >>= 1) Lmax = max(Lmax, __shfl_xor_sync(NR_FULL, Lmax, off));
+    int hop_u = 0, hop_v = 0, cur = dst;
+    for (int s = Lmax - 1; s >= 0; --s) {
+        const int u = __shfl_sync(NR_FULL, par, gbase + (cur & (G - 1)));
+        if (s < L) {
+            if (v == s) { hop_u = u; hop_v = cur; }
+            cur = u;
+        }
+    }
+    int e_h = 0;
+    bool unk = false;
+    if (v < L) {
+        e_h = sg.eid[hop_u * G + hop_v];
+        unk = ((my_m[e_h >> 4] >> ((e_h & 15) << 1)) & 3u) == 3u;
+    }
+    // the pivot: largest p among the UNKNOWN hops, the highest hop index (nearest dst) on ties
+    const double mp = unk ? sg.p[e_h] : -1.0;
+    double best = mp;
+    for (int off = G / 2; off > 0; off >>= 1) best = fmax(best, __shfl_xor_sync(NR_FULL, best, off, G));
+    const unsigned cand = __ballot_sync(NR_FULL, unk && mp == best);
+    const unsigned gc = (G == 32) ? cand : ((cand >> gbase) & ((1u << G) - 1u));
+    const int hstar = gc ? 31 - __clz(gc) : 0;
+    const int estar = __shfl_sync(NR_FULL, e_h, gbase + hstar);
+    if (live && !gc && leader) { acc.leaves++; nr_fix_add_mass(acc.R, mass); }   // not reached: see above
+    if (live && gc && (v == hstar || v == L)) {
+        const bool down = (v == hstar);
+        const double pe = sg.p[estar];
+        cm = down ? __dmul_rn(mass, __dsub_rn(1.0, pe)) : __dmul_rn(mass, pe);
+        const int wi = estar >> 4;
+        const uint32_t clear = (down ? 3u : 2u) << ((estar & 15) << 1);
+#pragma unroll
+        for (int k = 0; k < NW; ++k) w[k] = (k == wi) ? (my_m[k] & ~clear) : my_m[k];
+        has_child = true;
+    }
+}
+
+// The same as an out-of-line call, for kernels that branch on fork at run time:
+// the plain path keeps its own register allocation.
+template <int G, int W4>
+__device__ __noinline__ void nr_expand_fork_call(const NrSmallGraph &g, const NrSmemGraph &sg, const uint32_t *my_m,
+                                                 bool valid, double mass, double eps, bool &has_child,
+                                                 uint32_t (&w)[4 * W4], double &cm, NrLaneAcc &acc)
+{
+    nr_expand_fork<G, W4>(g, sg, my_m, valid, mass, eps, has_child, w, cm, acc);
+}

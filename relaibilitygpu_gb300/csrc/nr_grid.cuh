@@ -58,7 +58,10 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_kernel(NrGridParams 
             bool has_child;
             uint32_t w[NW];
             double cm;
-            nr_expand<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
+            if (P.fork)
+                nr_expand_fork_call<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
+            else
+                nr_expand<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
 
             const unsigned cb = __ballot_sync(NR_FULL, has_child);
             if (cb) {

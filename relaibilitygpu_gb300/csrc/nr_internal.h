@@ -64,6 +64,7 @@ struct NrGridParams {
     NrPartial *partials;              // [gridDim.x]
     double eps;
     long long timeout_ns;
+    int fork;                         // 1: fork branching on the most reliable path edge
 };
 
 // host helpers for NrFix (nr_api.cu)

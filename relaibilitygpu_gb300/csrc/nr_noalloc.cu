@@ -39,6 +39,9 @@
 const void *nr_warp_kernel_ptr_g8(int w4);
 const void *nr_warp_kernel_ptr_g16(int w4);
 const void *nr_warp_kernel_ptr_g32(int w4);
+const void *nr_warp_fork_kernel_ptr_g8(int w4);
+const void *nr_warp_fork_kernel_ptr_g16(int w4);
+const void *nr_warp_fork_kernel_ptr_g32(int w4);
 
 #define NR_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define NR_NOALLOC_MAX_DEVICES 64
@@ -132,8 +135,11 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     NrSmallGraph sg;
     const size_t blob = noalloc_tables(g, src, dst, G, &sg);
     if (!blob || sg.w4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
-    const void *kfn = G == 8 ? nr_warp_kernel_ptr_g8(sg.w4) : G == 16 ? nr_warp_kernel_ptr_g16(sg.w4)
-                                                                     : nr_warp_kernel_ptr_g32(sg.w4);
+    const bool fork = (o.branching == NR_BRANCH_FORK);
+    const void *kfn = fork ? (G == 8 ? nr_warp_fork_kernel_ptr_g8(sg.w4) : G == 16 ? nr_warp_fork_kernel_ptr_g16(sg.w4)
+                                                                              : nr_warp_fork_kernel_ptr_g32(sg.w4))
+                           : (G == 8 ? nr_warp_kernel_ptr_g8(sg.w4) : G == 16 ? nr_warp_kernel_ptr_g16(sg.w4)
+                                                                         : nr_warp_kernel_ptr_g32(sg.w4));
     if (!kfn) return NR_ERR_UNSUPPORTED;
 
     // array layout: tables | descriptor | id | counter | output | page masks | page masses
@@ -150,6 +156,7 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     const size_t off_mass = a256(off_mask + (size_t)pages * NR_PAGE * 16 * sg.w4);
     if (off_mass + (size_t)pages * NR_PAGE * sizeof(double) > NR_NOALLOC_SCRATCH_BYTES) return NR_ERR_UNSUPPORTED;
 
+    if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
     const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
     NrWarpParams P;
     P.blob = base;
@@ -173,6 +180,7 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     }
     P.out = reinterpret_cast<NrWarpOut *>(base + off_out);
     P.learned = 0;
+    P.fork = (o.branching == NR_BRANCH_FORK);
     P.dump_feat = nullptr; P.dump_mask = nullptr; P.dump_mass = nullptr; P.dump_inst = nullptr;
     P.dump_count = nullptr; P.dump_cap = 0; P.dump_stride = 0; P.inst_base = 0;
 

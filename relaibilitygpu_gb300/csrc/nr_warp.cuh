@@ -67,6 +67,7 @@ struct NrWarpParams {
     unsigned long long dump_cap;
     int dump_stride;
     int inst_base;                   // index of this launch's instance 0 in the caller's batch
+    int fork;                        // fork branching (informational: the FORK instantiation runs it)
 };
 
 __device__ __forceinline__ unsigned long long nr_warp_sum_u64(unsigned long long x)
@@ -105,7 +106,8 @@ __host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets
 // registers without spills: three 256-thread blocks, 24 warps, per SM.  Wider
 // masks hold more words per lane (two blocks per SM), and the scorer's kernel
 // needs its registers for the MLP.
-template <int G, int W4, bool LEARN = false>
+// FORK instantiates fork branching (nr_expand_fork) in place of path branching.
+template <int G, int W4, bool LEARN = false, bool FORK = false>
 __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_WARP_MIN_BLOCKS : 2))
     nr_warp_kernel(NrWarpParams P)
 {
@@ -259,8 +261,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
                     uint32_t w[NW];
                     double cm;
                     float feat[NR_FEAT];
-                    nr_expand<G, W4, LEARN>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc,
-                                            LEARN ? &feat : nullptr);
+                    if constexpr (FORK)
+                        nr_expand_fork<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
+                    else
+                        nr_expand<G, W4, LEARN>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc,
+                                                LEARN ? &feat : nullptr);
                     double key = cm;
                     if constexpr (LEARN) {
                         const unsigned cbm = __ballot_sync(NR_FULL, has_child);

@@ -72,6 +72,7 @@ struct NrGridWideParams {
     unsigned long long max_nodes;   // stop once this many subproblems were popped (0 = no budget)
     NrWideShare *wpart;             // [2][gridDim.x] per-block shares, alternating slots
     int *stop_wave;                 // [0] waves run before a stop (or -1), [1] stop reason
+    int fork;                       // 1: fork branching on the most reliable path edge
 };
 
 struct NrBucketWideParams {
@@ -99,6 +100,7 @@ struct NrBucketWideParams {
     NrWideShare *wpart;
     int *stop_info;                 // [0] waves run, [1] stop reason (0 empty, 1 target, 3 budget), [2] compactions
     unsigned long long *stats;      // [0] widest wave, [1] records queued at the end
+    int fork;                       // 1: fork branching on the most reliable path edge
 };
 
 // per-warp shared memory: mask words, frontier / next / visited bitmasks,
@@ -155,28 +157,16 @@ __device__ __forceinline__ NrWideView nr_wide_view(unsigned char *smem, const Nr
     return v;
 }
 
-// Pop of one subproblem whose mask words are in v.m: count it, truncate it
-// below eps, else BFS, and on a path emit the branches and the all-up leaf.
-// All 32 lanes call it; the accumulators live on lane 0.
-template <int W4>
-__device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideView &v, double mass, double eps,
-                                             const NrWideOut &O, NrWideAcc &A)
+// BFS of the warp from src over the arcs whose edge is not down (up_only:
+// up), with the parent rule above; true if dst is reached.  All 32 lanes call it.
+__device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideView &v, bool up_only)
 {
-    constexpr int NW = 4 * W4;
     const int lane = threadIdx.x & 31;
     const int n = g.n, nwd = g.nwd, src = g.src, dst = g.dst;
-    uint32_t *m = v.m, *F = v.F, *NF = v.NF, *VIS = v.VIS, *par = v.par, *list = v.list, *hops = v.hops;
-    if (lane == 0) {
-        A.nodes++;
-        nr_fix_sub(A.net, nr_fix_of(mass));
-    }
-    __syncwarp();
-    if (eps > 0.0 && mass < eps) {          // main.cu:537-543
-        if (lane == 0) { A.trunc++; nr_fix_add_mass(A.et, mass); }
-        __syncwarp();
-        return;
-    }
-    // ---- BFS from src over not-down arcs ----
+    const uint32_t *m = v.m;
+    uint32_t *F = v.F, *NF = v.NF, *VIS = v.VIS, *par = v.par, *list = v.list;
+    // usable state: 01 or 11 (bit 0 set), or exactly 01
+    const uint32_t want = up_only ? 1u : 1u, sel = up_only ? 3u : 1u;
     for (int i = lane; i < nwd; i += 32) {
         VIS[i] = 0u;
         F[i] = 0u;
@@ -189,7 +179,6 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
     }
     __syncwarp();
     bool found = (src == dst);
-    int L = 0;
     while (!found) {
         // compact the frontier into list[]
         const uint32_t fw = (lane < nwd) ? F[lane] : 0u;
@@ -210,7 +199,7 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
             for (int j = v.row[u]; j < v.row[u + 1]; ++j) {
                 const uint32_t a = v.arc[j];
                 const uint32_t w = a & 1023u, e = a >> 10;
-                if (((m[e >> 4] >> ((e & 15) << 1)) & 1u) && !((VIS[w >> 5] >> (w & 31)) & 1u)) {
+                if (((m[e >> 4] >> ((e & 15) << 1)) & sel) == want && !((VIS[w >> 5] >> (w & 31)) & 1u)) {
                     atomicOr(&NF[w >> 5], 1u << (w & 31));
                     atomicMin(&par[w], (u << 16) | e);
                 }
@@ -225,10 +214,71 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
             any = any || nf != 0u;
         }
         __syncwarp();
-        ++L;
         found = (VIS[dst >> 5] >> (dst & 31)) & 1u;
         if (!__any_sync(NR_FULL, any)) break;
     }
+    return found;
+}
+
+// Write one child record (mask = m with edge e's state bits cleared by `clear`)
+// at the next slot of O and count it; lanes own mask words.
+template <int W4>
+__device__ __forceinline__ void nr_wide_emit(const NrWideOut &O, NrWideAcc &A, const uint32_t *m,
+                                             unsigned long long slot, int e, uint32_t clear, double cm)
+{
+    constexpr int NW = 4 * W4;
+    const int lane = threadIdx.x & 31;
+    const int wi = e >> 4;
+    if (slot < O.cap) {
+        uint32_t *dstw = reinterpret_cast<uint32_t *>(O.mask + slot * W4);
+        if (lane < NW) __stcg(dstw + lane, (lane == wi) ? (m[lane] & ~clear) : m[lane]);
+        if (lane + 32 < NW) __stcg(dstw + lane + 32, (lane + 32 == wi) ? (m[lane + 32] & ~clear) : m[lane + 32]);
+        if (lane == 0) {
+            __stcg(O.mass + slot, cm);
+            nr_fix_add_mass(A.net, cm);
+            if (O.key) {
+                const int b = nr_bucket(cm, O.shift, O.nb);
+                __stcg(O.key + slot, (unsigned char)b);
+                atomicAdd(&O.hist[b], 1u);
+            }
+        }
+    } else if (lane == 0) {                                 // queue full (main.cu:245-252)
+        A.spilled++;
+        nr_fix_add_mass(A.es, cm);
+    }
+}
+
+// Pop of one subproblem whose mask words are in v.m: count it, truncate it
+// below eps, else BFS, and on a path emit the branches and the all-up leaf --
+// or, with fork branching (main.cu:303-430 with :550-565), put the whole mass
+// in R when a path of up edges exists, else fork on the optimistic path's
+// UNKNOWN edge with the largest p (ties: nearest dst): down child, then up.
+// All 32 lanes call it; the accumulators live on lane 0.
+template <int W4>
+__device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideView &v, double mass, double eps,
+                                             const NrWideOut &O, NrWideAcc &A, bool fork = false)
+{
+    constexpr int NW = 4 * W4;
+    const int lane = threadIdx.x & 31;
+    const int n = g.n, src = g.src, dst = g.dst;
+    uint32_t *m = v.m, *par = v.par, *hops = v.hops;
+    if (lane == 0) {
+        A.nodes++;
+        nr_fix_sub(A.net, nr_fix_of(mass));
+    }
+    __syncwarp();
+    if (eps > 0.0 && mass < eps) {          // main.cu:537-543
+        if (lane == 0) { A.trunc++; nr_fix_add_mass(A.et, mass); }
+        __syncwarp();
+        return;
+    }
+    if (fork && nr_wide_bfs(g, v, true)) {   // connected: the whole mass to R
+        if (lane == 0) { A.leaves++; nr_fix_add_mass(A.R, mass); }
+        __syncwarp();
+        return;
+    }
+    const bool found = nr_wide_bfs(g, v, false);
+    int L = 0;
     if (!found) {
         if (lane == 0) A.dead++;
         __syncwarp();
@@ -246,6 +296,37 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
     }
     L = __shfl_sync(NR_FULL, L, 0);
     __syncwarp();
+    if (fork) {
+        // the pivot: largest p among the UNKNOWN hops, the nearest dst (lowest index) on ties
+        double bp = -1.0;
+        int bh = 1 << 30;
+        for (int h = lane; h < L; h += 32) {
+            const uint32_t e = hops[h];
+            if (((m[e >> 4] >> ((e & 15) << 1)) & 3u) == 3u) {
+                const double pe = v.p[e];
+                if (pe > bp || (pe == bp && h < bh)) { bp = pe; bh = h; }
+            }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            const double op = __shfl_xor_sync(NR_FULL, bp, off);
+            const int oh = __shfl_xor_sync(NR_FULL, bh, off);
+            if (op > bp || (op == bp && oh < bh)) { bp = op; bh = oh; }
+        }
+        if (bp < 0.0) {                 // not reached: without a path of up edges one hop is UNKNOWN
+            if (lane == 0) { A.leaves++; nr_fix_add_mass(A.R, mass); }
+            __syncwarp();
+            return;
+        }
+        const int e = (int)hops[bh];
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(O.count, 2ull);
+        base = __shfl_sync(NR_FULL, base, 0);
+        const int sh = (e & 15) << 1;
+        nr_wide_emit<W4>(O, A, m, base, e, 3u << sh, __dmul_rn(mass, v.q[e]));        // down
+        nr_wide_emit<W4>(O, A, m, base + 1, e, 2u << sh, __dmul_rn(mass, v.p[e]));    // up
+        __syncwarp();
+        return;
+    }
     // number of UNKNOWN hops -> one slot range for all children
     int unk = 0;
     for (int h = lane; h < L; h += 32) {
@@ -404,7 +485,7 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
             if (lane < W4) reinterpret_cast<uint4 *>(v.m)[lane] = __ldcg(in_mask + idx * W4 + lane);
             const double mass = __ldcg(in_mass + idx);
             __syncwarp();
-            nr_wide_step<W4>(g, v, mass, P.eps, O, A);
+            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0);
         }
         if (P.target_on || P.max_nodes) nr_wide_write_share(P.wpart + (size_t)(wave & 1) * gridDim.x, A);
         if (!nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns)) break;
@@ -579,7 +660,7 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketW
             if (lane < W4) reinterpret_cast<uint4 *>(v.m)[lane] = __ldcg(P.mask + s * W4 + lane);
             const double mass = __ldcg(P.mass + s);
             __syncwarp();
-            nr_wide_step<W4>(g, v, mass, P.eps, O, A);
+            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0);
         }
         __syncthreads();
         for (int b = threadIdx.x; b < P.nb; b += blockDim.x)

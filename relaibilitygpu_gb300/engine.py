@@ -26,6 +26,7 @@ STATUS = {
     -5: "NR_ERR_CUDA", -6: "NR_ERR_NOMEM", -7: "NR_ERR_TIMEOUT", -8: "NR_ERR_INTERNAL",
 }
 ORDERS = {"auto": 0, "waves": 1, "maxmass": 2, "learned": 3}
+BRANCHING = {"path": 0, "fork": 1}
 ENGINES = {1: "grid", 2: "warp"}
 
 
@@ -49,7 +50,7 @@ class NrOptions(C.Structure):
         ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("device", C.c_int32),
         ("blocks_per_sm", C.c_int32), ("warps_per_block", C.c_int32), ("timeout_ms", C.c_double),
         ("verbose", C.c_int32), ("pad0", C.c_int32), ("max_nodes", C.c_uint64),
-        ("pages_per_warp", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("pages_per_warp", C.c_int32), ("branching", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -219,7 +220,7 @@ class _GraphView:
 
 def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto", bucket_shift: int = 2,
                  n_buckets: int = 256, device: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0,
-                 timeout_ms: float = 60000.0, max_nodes: int = 0, pages_per_warp: int = 0) -> NrOptions:
+                 timeout_ms: float = 60000.0, max_nodes: int = 0, pages_per_warp: int = 0, branching: str = "path") -> NrOptions:
     o = NrOptions()
     lib().nr_options_default(C.byref(o))
     o.truncation_eps = float(eps)
@@ -233,6 +234,7 @@ def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto
     o.timeout_ms = float(timeout_ms)
     o.max_nodes = int(max_nodes)
     o.pages_per_warp = int(pages_per_warp)
+    o.branching = BRANCHING[branching] if isinstance(branching, str) else int(branching)
     return o
 
 
@@ -242,7 +244,8 @@ def options_dict(o: NrOptions) -> dict:
     return dict(eps=o.truncation_eps, target_width=o.target_width, order=inv.get(o.order, "auto"),
                 bucket_shift=o.bucket_shift, n_buckets=o.n_buckets, device=o.device,
                 blocks_per_sm=o.blocks_per_sm, warps_per_block=o.warps_per_block, timeout_ms=o.timeout_ms,
-                max_nodes=o.max_nodes, pages_per_warp=o.pages_per_warp)
+                max_nodes=o.max_nodes, pages_per_warp=o.pages_per_warp,
+                branching={v: k for k, v in BRANCHING.items()}.get(o.branching, "path"))
 
 
 def _check(rc: int) -> None:

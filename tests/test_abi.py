@@ -119,3 +119,22 @@ def test_batch_validation_on_host_pool(engine_lib):
     gs = [graphs.complete(6, p=0.5) for _ in range(2000)]
     with pytest.raises(engine_lib.NrError):
         ctx.reliability_batch(gs, [0] * 2000, [9] * 2000)
+
+
+def test_cli_usage_and_errors_without_gpu(tmp_path):
+    """The program's argument and file errors need no GPU: usage on too few arguments, a message
+    and a non-zero exit on a missing or malformed file."""
+    import subprocess
+    import os
+    cli = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "relaibilitygpu_gb300",
+                       "network_reliability")
+    if not os.path.exists(cli):
+        pytest.skip("CLI not built")
+    r = subprocess.run([cli], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Usage" in r.stderr and "--fork" in r.stderr
+    r = subprocess.run([cli, str(tmp_path / "missing.txt"), "0", "1"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Cannot load" in r.stderr
+    bad = tmp_path / "bad.txt"
+    bad.write_text("3 4 U\n1 1\n")
+    r = subprocess.run([cli, str(bad), "0", "1"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Cannot load" in r.stderr

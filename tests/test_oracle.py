@@ -167,3 +167,38 @@ def test_batch_runner_matches_single(oracle):
         assert (r.nodes, r.leaves, r.dead, r.waves, r.max_wave, r.queued) == (o.nodes, o.leaves, o.dead, o.waves,
                                                                              o.max_wave, o.queued)
         assert r.R == o.R and r.esp == o.esp
+
+
+def test_fork_branching_is_exact(load_golden_graph, oracle):
+    """Fork branching (main.cu:303-430 with FORK_BEST_EDGE) is a different decomposition with the
+    same R: exhaustive runs agree with brute force; truncated runs bracket it."""
+    from relaibilitygpu_gb300 import graphs
+    cases = [(load_golden_graph("COMP8"), 0, 7), (load_golden_graph("test_kite"), 0, 4),
+             (graphs.grid(3, 4, p_range=(0.5, 0.95), seed=3), 0, 11),
+             (graphs.gnm(9, 16, p_range=(0.3, 0.95), seed=5), None, None)]
+    for g, s, t in cases:
+        s = g.src if s is None else s
+        t = g.dst if t is None else t
+        exact = oracle.brute(g, s, t)
+        for order, kw in (("waves", {}), ("waves", dict(bucket_shift=2, n_buckets=64)), ("heap", {})):
+            r = oracle.run(g, s, t, order=order, branching="fork", **kw)
+            assert r.status == 0 and r.esp == 0.0
+            assert abs(r.R - exact) <= 1e-13 * max(exact, 1e-300)
+            # every pop is a leaf, a dead end or a fork with two children, and every child is popped
+            assert r.paths == r.leaves and r.pushes % 2 == 0
+            assert r.nodes == r.leaves + r.dead + r.pushes // 2 == 1 + r.pushes
+        r = oracle.run(g, s, t, branching="fork", bucket_shift=1, n_buckets=64, target_width=1e-3)
+        assert r.R <= exact + 1e-15 <= r.R + r.esp + 1e-15 and r.esp <= 1e-3
+
+
+def test_fork_branching_counts_by_hand():
+    """A 3-edge path s-a-t plus the edge s-t: the fork picks the most reliable UNKNOWN edge of the
+    optimistic path s-t first (the direct edge), then the path s-a-t with its best edge."""
+    import oracle
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.from_edges(3, [(0, 1), (1, 2), (0, 2)], [0.9, 0.8, 0.7])
+    r = oracle.run(g, 0, 2, branching="fork")
+    # pops: root (s-t unknown -> fork on (0,2)); up child: connected leaf; down child: path 0-1-2,
+    # fork on (0,1) p=0.9: its down child is dead, its up child forks on (1,2): up leaf, down dead
+    assert (r.nodes, r.leaves, r.dead, r.pushes) == (7, 2, 2, 6)
+    assert abs(r.R - (0.7 + 0.3 * 0.9 * 0.8)) < 1e-15
