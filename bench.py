@@ -388,6 +388,7 @@ def main():
         try:
             ttb = {"plain": latency("maxmass"), "learned": None, "instances": 16,
                    "breadth_first": latency("maxmass", bucket_shift=-1),
+                   "fork_branching": latency("maxmass", branching="fork"),
                    "plain_batch": batch_run("maxmass"),
                    "per_graph_launches": per_graph_launches()}
         except Exception as exc:                     # keep the bench line; report the failure

@@ -166,7 +166,11 @@ int og_load(const char *path, og_graph *g)
     if (tok_long(&t, &n) || tok_long(&t, &efile) || n <= 0) { free(buf); return -3; }
     /* optional graph type character (U/D); files without one start the lists */
     tok_skip(&t);
-    if (t.p < t.end && ((*t.p >= 'A' && *t.p <= 'Z') || (*t.p >= 'a' && *t.p <= 'z'))) t.p++;
+    int directed = 0;
+    if (t.p < t.end && ((*t.p >= 'A' && *t.p <= 'Z') || (*t.p >= 'a' && *t.p <= 'z'))) {
+        directed = (*t.p == 'D' || *t.p == 'd');
+        t.p++;
+    }
 
     int32_t *row = (int32_t *)calloc(n + 1, sizeof(int32_t));
     size_t cap = 64, na = 0;
@@ -189,9 +193,17 @@ int og_load(const char *path, og_graph *g)
     }
     free(buf);
 
-    /* edge ids: first-seen (min,max) pair scanning nodes in order (graph.h:77-90) */
+    /* edge ids: first-seen (min,max) pair scanning nodes in order (graph.h:77-90);
+     * a directed graph gives every arc its own id in file order (seq/GraphRP.h:131-145) */
     int32_t *eid = (int32_t *)malloc((na ? na : 1) * sizeof(int32_t));
     double *ep = (double *)malloc((na ? na : 1) * sizeof(double));
+    if (directed) {
+        for (size_t j = 0; j < na; j++) { eid[j] = (int32_t)j; ep[j] = ap[j]; }
+        free(ap);
+        g->n_nodes = (int32_t)n; g->n_edges = (int32_t)na; g->n_arcs = (int32_t)na;
+        g->row_ptr = row; g->col_idx = col; g->edge_id = eid; g->edge_p = ep;
+        return 0;
+    }
     /* pair -> id via an open-addressing table keyed on (a,b) */
     size_t hcap = 16;
     while (hcap < 2 * na + 16) hcap <<= 1;

@@ -1834,7 +1834,11 @@ extern "C" int nr_graph_load(const char *path, nr_graph *out)
     long n = 0, efile = 0;
     if (!rd.integer(&n) || !rd.integer(&efile) || n <= 0 || n > (1L << 24)) return NR_ERR_PARSE;
     rd.skip();
-    if (rd.p < rd.end && isalpha((unsigned char)*rd.p)) ++rd.p;   // optional U / D
+    bool directed = false;
+    if (rd.p < rd.end && isalpha((unsigned char)*rd.p)) {        // optional U / D
+        directed = (*rd.p == 'D' || *rd.p == 'd');
+        ++rd.p;
+    }
     std::vector<int32_t> row(n + 1, 0), col;
     std::vector<double> arc_p;
     for (long u = 0; u < n; ++u) {
@@ -1849,10 +1853,16 @@ extern "C" int nr_graph_load(const char *path, nr_graph *out)
         }
         row[u + 1] = (int32_t)col.size();
     }
+    // edge ids: first-seen (min,max) pairs (graph.h:77-90); a directed graph gives every arc
+    // its own id in file order (seq/GraphRP.h:131-145: no merging of the two directions)
     std::map<std::pair<int32_t, int32_t>, int32_t> ids;
     std::vector<int32_t> eid(col.size());
     std::vector<double> ep;
-    for (long u = 0; u < n; ++u)
+    if (directed) {
+        for (size_t j = 0; j < col.size(); ++j) eid[j] = (int32_t)j;
+        ep = arc_p;
+    }
+    for (long u = 0; u < n && !directed; ++u)
         for (int32_t j = row[u]; j < row[u + 1]; ++j) {
             std::pair<int32_t, int32_t> key(std::min<int32_t>((int32_t)u, col[j]), std::max<int32_t>((int32_t)u, col[j]));
             auto it = ids.find(key);

@@ -63,8 +63,11 @@ class Graph:
         return [p if p is not None else (0, 0) for p in pairs]
 
 
-def from_adjacency(adj: Sequence[Sequence[Tuple[int, float]]], name: str = "") -> Graph:
-    """Build a Graph from adjacency lists ``adj[u] = [(v, p), ...]`` (graph.h:77-130)."""
+def from_adjacency(adj: Sequence[Sequence[Tuple[int, float]]], name: str = "", directed: bool = False) -> Graph:
+    """Build a Graph from adjacency lists ``adj[u] = [(v, p), ...]`` (graph.h:77-130).
+
+    Undirected: the two arcs of an edge share the id of the first-seen (min,max) pair.
+    Directed: every arc is its own edge, ids in list order (seq/GraphRP.h:131-145)."""
     n = len(adj)
     row = np.zeros(n + 1, dtype=np.int32)
     cols: List[int] = []
@@ -73,7 +76,7 @@ def from_adjacency(adj: Sequence[Sequence[Tuple[int, float]]], name: str = "") -
     ids = {}
     for u in range(n):
         for v, p in adj[u]:
-            key = (min(u, v), max(u, v))
+            key = (u, v, len(cols)) if directed else (min(u, v), max(u, v))
             if key not in ids:
                 ids[key] = len(probs)
                 probs.append(float(p))
@@ -106,7 +109,9 @@ def parse_graph_text(text: str, name: str = "") -> Graph:
         raise ValueError("graph header needs N and E")
     n = int(toks[0])
     pos = 2
+    directed = False
     if pos < len(toks) and toks[pos][:1].isalpha():
+        directed = toks[pos][:1] in "Dd"
         pos += 1
     adj: List[List[Tuple[int, float]]] = []
     for u in range(n):
@@ -122,7 +127,7 @@ def parse_graph_text(text: str, name: str = "") -> Graph:
                 raise ValueError(f"neighbour {v} of node {u} out of range")
             lst.append((v, p))
         adj.append(lst)
-    return from_adjacency(adj, name=name)
+    return from_adjacency(adj, name=name, directed=directed)
 
 
 def load_graph(path: str) -> Graph:
@@ -130,8 +135,17 @@ def load_graph(path: str) -> Graph:
         return parse_graph_text(f.read(), name=path)
 
 
+def from_arcs(n: int, arcs: Iterable[Tuple[int, int]], probs: Iterable[float], name: str = "") -> Graph:
+    """Directed graph: arc u -> v with its own probability (and edge id, in list order per node)."""
+    adj: List[List[Tuple[int, float]]] = [[] for _ in range(n)]
+    for (u, v), p in zip(arcs, probs):
+        adj[u].append((v, p))
+    return from_adjacency(adj, name=name, directed=True)
+
+
 def format_graph(g: Graph, type_char: str = "U") -> str:
-    """Reference file text; for 'U' the header E counts arcs (graph.h:93)."""
+    """Reference file text; the header E counts arcs (graph.h:93).  Write a directed graph
+    (every arc its own edge) with type_char 'D'."""
     lines = [f"{g.n_nodes} {g.n_arcs} {type_char}"]
     for u in range(g.n_nodes):
         lo, hi = int(g.row_ptr[u]), int(g.row_ptr[u + 1])

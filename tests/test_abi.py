@@ -138,3 +138,15 @@ def test_cli_usage_and_errors_without_gpu(tmp_path):
     bad.write_text("3 4 U\n1 1\n")
     r = subprocess.run([cli, str(bad), "0", "1"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "Cannot load" in r.stderr
+
+
+def test_loader_directed_graphs(engine_lib, tmp_path):
+    """nr_graph_load on a 'D' file: one edge per arc, ids in file order, as the Python parser."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.from_arcs(4, [(0, 1), (1, 0), (1, 2), (2, 3), (3, 1)], [0.9, 0.8, 0.7, 0.6, 0.5])
+    path = tmp_path / "d.txt"
+    path.write_text(graphs.format_graph(g, "D"))
+    c = engine_lib.load_graph_file(str(path))
+    assert (c.n_edges, c.n_arcs) == (5, 5)
+    assert np.array_equal(c.edge_id, g.edge_id) and np.array_equal(c.edge_p, g.edge_p)
+    assert np.array_equal(c.col_idx, g.col_idx) and np.array_equal(c.row_ptr, g.row_ptr)

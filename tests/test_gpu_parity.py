@@ -148,3 +148,30 @@ def test_one_shot_entry_point(engine_lib, load_golden_graph):
     g = load_golden_graph("test_bridge")
     r = engine_lib.reliability(g, 0, 3)
     assert rel_close(r.R, 0.835, 1e-14)
+
+
+def test_directed_graphs_all_engines(ctx, oracle):
+    """'D' graphs (every arc its own edge, searches follow arcs) on the whole-GPU wave engine,
+    the warp engine and the wide engines, against the oracle."""
+    from relaibilitygpu_gb300 import graphs
+    rng = np.random.default_rng(9)
+    compared = 0
+    for n in (8, 14, 20, 24, 48):
+        arcs = sorted({(int(a), int(b)) for a, b in rng.integers(0, n, size=(4 * n, 2)) if a != b})
+        g = graphs.from_arcs(n, arcs, rng.uniform(0.6, 0.97, size=len(arcs)))
+        s, t = 0, n - 1
+        o = oracle.run(g, s, t, max_nodes=3_000_000, threads=4)
+        if o.status == 0:
+            r = ctx.reliability(g, s, t, capacity=1 << 22)
+            check_exact(r, o)
+        for shift in (-1, 1):
+            nb = 64 if shift >= 0 else 1
+            o2 = oracle.run(g, s, t, target_width=1e-4, bucket_shift=shift, n_buckets=nb, threads=4)
+            r2 = ctx.reliability(g, s, t, capacity=1 << 22, target_width=1e-4, bucket_shift=shift, n_buckets=64,
+                                 order="maxmass")
+            if r2.spilled:
+                continue          # larger than one warp's queue: a valid bracket, not the oracle's run
+            assert (r2.nodes, r2.leaves, r2.dead_ends, r2.iterations) == (o2.nodes, o2.leaves, o2.dead, o2.waves)
+            assert r2.R == o2.R and r2.esp == o2.esp
+            compared += 1
+    assert compared >= 6

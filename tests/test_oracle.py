@@ -202,3 +202,27 @@ def test_fork_branching_counts_by_hand():
     # fork on (0,1) p=0.9: its down child is dead, its up child forks on (1,2): up leaf, down dead
     assert (r.nodes, r.leaves, r.dead, r.pushes) == (7, 2, 2, 6)
     assert abs(r.R - (0.7 + 0.3 * 0.9 * 0.8)) < 1e-15
+
+
+def test_directed_graphs(oracle, tmp_path):
+    """'D' files give every arc its own edge id (seq/GraphRP.h:131-145); searches follow arcs."""
+    import numpy as np
+    from relaibilitygpu_gb300 import graphs
+    # 0->1->2 with a back arc 2->1 and an arc 2->0 that cannot help a 0->2 path
+    g = graphs.from_arcs(3, [(0, 1), (1, 2), (2, 1), (2, 0)], [0.9, 0.8, 0.5, 0.7])
+    assert (g.n_edges, g.n_arcs) == (4, 4)
+    r = oracle.run(g, 0, 2)
+    assert abs(r.R - 0.9 * 0.8) < 1e-15 and abs(oracle.brute(g, 0, 2) - 0.72) < 1e-15
+    # the reverse direction needs 2->0 or 2->1->? : only 2->0
+    assert abs(oracle.run(g, 2, 0).R - 0.7) < 1e-15
+    text = graphs.format_graph(g, "D")
+    g2 = graphs.parse_graph_text(text)
+    assert np.array_equal(g2.edge_id, g.edge_id) and np.array_equal(g2.edge_p, g.edge_p)
+    assert abs(oracle.run(g2, 0, 2).R - 0.72) < 1e-15
+    # a random directed graph: the decomposition equals brute force, with both parent rules
+    rng = np.random.default_rng(3)
+    arcs = sorted({(int(a), int(b)) for a, b in rng.integers(0, 8, size=(30, 2)) if a != b})
+    dg = graphs.from_arcs(8, arcs, rng.uniform(0.4, 0.95, size=len(arcs)))
+    exact = oracle.brute(dg, 0, 7)
+    for rule in ("level", "fifo"):
+        assert abs(oracle.run(dg, 0, 7, rule=rule).R - exact) <= 1e-13
