@@ -50,6 +50,14 @@ __host__ __device__ __forceinline__ NrFix nr_fix_of(double m)
 
 __host__ __device__ __forceinline__ void nr_fix_add(NrFix &a, const NrFix &b)
 {
+#ifdef __CUDA_ARCH__
+    // one carry chain through the three words
+    asm("add.cc.u64 %0, %0, %3;\n\t"
+        "addc.cc.u64 %1, %1, %4;\n\t"
+        "addc.u64 %2, %2, %5;"
+        : "+l"(a.w0), "+l"(a.w1), "+l"(a.w2)
+        : "l"(b.w0), "l"(b.w1), "l"(b.w2));
+#else
     const unsigned long long w0 = a.w0 + b.w0;
     const unsigned long long c0 = w0 < a.w0;
     const unsigned long long t1 = a.w1 + b.w1;
@@ -59,10 +67,18 @@ __host__ __device__ __forceinline__ void nr_fix_add(NrFix &a, const NrFix &b)
     a.w2 = a.w2 + b.w2 + c1;
     a.w1 = w1;
     a.w0 = w0;
+#endif
 }
 
 __host__ __device__ __forceinline__ void nr_fix_sub(NrFix &a, const NrFix &b)
 {
+#ifdef __CUDA_ARCH__
+    asm("sub.cc.u64 %0, %0, %3;\n\t"
+        "subc.cc.u64 %1, %1, %4;\n\t"
+        "subc.u64 %2, %2, %5;"
+        : "+l"(a.w0), "+l"(a.w1), "+l"(a.w2)
+        : "l"(b.w0), "l"(b.w1), "l"(b.w2));
+#else
     const unsigned long long w0 = a.w0 - b.w0;
     const unsigned long long b0 = a.w0 < b.w0;
     const unsigned long long t1 = a.w1 - b.w1;
@@ -72,6 +88,7 @@ __host__ __device__ __forceinline__ void nr_fix_sub(NrFix &a, const NrFix &b)
     a.w2 = a.w2 - b.w2 - b1;
     a.w1 = w1;
     a.w0 = w0;
+#endif
 }
 
 __host__ __device__ __forceinline__ bool nr_fix_le(const NrFix &a, const NrFix &b)
