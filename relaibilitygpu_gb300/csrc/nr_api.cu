@@ -286,6 +286,8 @@ struct NrHostBlock {
     long long last_owner_rel;   // offset in the block of its last structural part, -1 if none
     size_t base;                // offset of the block's tables in the staging buffer
     long long struct_in;        // struct_off of the last structural part before the block
+    int last_rows;              // rows mode of the block's last structural part, -1 if none
+    int rows_in;                // rows mode of the last structural part before the block
     int cnt[3 * NR_MAX_W4];     // instances per class
     int cbase[3 * NR_MAX_W4];   // instances of each class in earlier blocks
 };
@@ -450,6 +452,41 @@ static int validate(const nr_graph *g, int src, int dst)
 
 static int group_width_of(int n) { return group_width(n); }
 
+// Whether the warp engine can carry not-down in-neighbour rows in its queue
+// records (a child's rows are its parent's less the arcs of its down edge):
+// 1 for an undirected simple graph (every edge id on exactly two arcs, u -> v and
+// v -> u), 2 for a directed simple graph (one arc per edge id), 0 otherwise
+// (self-loops, or one ordered pair with two edge ids); 0 makes it rebuild rows.
+static int rows_mode_of(const nr_graph *g)
+{
+    const int n = g->n_nodes, E = g->n_edges;
+    if (n > NR_SMALL_MAX_N) return 0;
+    static thread_local int pid[NR_SMALL_MAX_N][NR_SMALL_MAX_N];
+    for (int u = 0; u < n; ++u)
+        for (int v = 0; v < n; ++v) pid[u][v] = -1;
+    std::vector<int> cnt(std::max(E, 1), 0);
+    for (int u = 0; u < n; ++u)
+        for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
+            const int v = g->col_idx[j], e = g->edge_id[j];
+            if (v == u) return 0;
+            if (pid[u][v] != -1 && pid[u][v] != e) return 0;
+            if (pid[u][v] == e) return 0;                 // the same arc twice
+            pid[u][v] = e;
+            cnt[e]++;
+        }
+    bool all1 = true, all2 = true;
+    for (int e = 0; e < E; ++e) {
+        all1 = all1 && cnt[e] == 1;
+        all2 = all2 && cnt[e] == 2;
+    }
+    if (all1) return 2;
+    if (!all2) return 0;
+    for (int u = 0; u < n; ++u)
+        for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j)
+            if (pid[g->col_idx[j]][u] != g->edge_id[j]) return 0;   // the other arc is not v -> u
+    return 1;
+}
+
 // Graph tables of one instance for the small engines (layout in nr_internal.h).
 // Per-instance part: the offset of p from its own base.
 static size_t small_inst_layout(const nr_graph *g, int src, int dst, NrSmallGraph *sg)
@@ -458,6 +495,8 @@ static size_t small_inst_layout(const nr_graph *g, int src, int dst, NrSmallGrap
     const int W = std::max(1, (2 * E + 31) / 32);
     sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst;
     sg->n_in = g->n_arcs;
+    sg->rows = 0;
+    sg->pad0 = 0;
     size_t off = 0;
     sg->off_p = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
     return off;
@@ -1201,6 +1240,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         NrHostBlock &k = S.blk[b];
         size_t rel = 0;
         k.last_owner_rel = -1;
+        k.last_rows = -1;
         for (int j = 0; j < NCLS; ++j) k.cnt[j] = 0;
         for (int i = blk_begin(b), e = blk_begin(b + 1); i < e; ++i) {
             // consecutive instances with the same topology share one structural part
@@ -1211,7 +1251,12 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
             S.inst_b[i] = ib;
             S.struct_b[i] = same ? 0 : sb;
             rel += ib;
-            if (!same) { k.last_owner_rel = (long long)rel; rel += sb; }
+            if (!same) {
+                k.last_owner_rel = (long long)rel;
+                rel += sb;
+                desc[i].rows = rows_mode_of(&gs[i]);
+                k.last_rows = desc[i].rows;
+            }
             if (desc[i].w4 > NR_MAX_W4) { too_wide.store(1); S.cls[i] = 0; continue; }
             const int G = group_width(gs[i].n_nodes);
             S.cls[i] = (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + desc[i].w4 - 1;
@@ -1227,12 +1272,15 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     size_t off = align16(sizeof(int) * NCLS);
     const size_t off_cnt = 0;
     long long owner_struct = -1;              // struct_off of the last structural part so far
+    int owner_rows = 0;                       // and its rows mode
     int class_count[NCLS] = {0};
     for (int b = 0; b < B; ++b) {
         NrHostBlock &k = S.blk[b];
         k.base = off;
         k.struct_in = owner_struct;
+        k.rows_in = owner_rows;
         if (k.last_owner_rel >= 0) owner_struct = (long long)off + k.last_owner_rel;
+        if (k.last_rows >= 0) owner_rows = k.last_rows;
         off += k.bytes;
         for (int j = 0; j < NCLS; ++j) {
             k.cbase[j] = class_count[j];
@@ -1259,6 +1307,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         const NrHostBlock &k = S.blk[b];
         size_t at = k.base;
         long long rep = k.struct_in;
+        int rep_rows = k.rows_in;
         int fill[NCLS];
         for (int j = 0; j < NCLS; ++j) fill[j] = class_begin[j] + k.cbase[j];
         for (int i = blk_begin(b), e = blk_begin(b + 1); i < e; ++i) {
@@ -1268,10 +1317,12 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
             if (!S.same_prev[i]) {
                 d.struct_off = (long long)at;
                 rep = d.struct_off;
+                rep_rows = d.rows;
                 at += S.struct_b[i];
                 small_fill_struct(&gs[i], &d, hb + d.struct_off);
             } else {
                 d.struct_off = rep;               // instance 0 always owns one, so rep >= 0 here
+                d.rows = rep_rows;
             }
             d.blob_bytes = (int)(S.inst_b[i] + S.struct_b[i]);
             if (!small_fill_inst(&gs[i], &d, hb + d.blob_off)) bad_p.store(1);
@@ -1317,7 +1368,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         if (bps < 1) return NR_ERR_UNSUPPORTED;
         grids[j] = std::max(1, std::min(bps * c->sms, (class_count[j] + warps_pb - 1) / warps_pb));
         smems[j] = smem;
-        slab_need = std::max(slab_need, (size_t)grids[j] * warps_pb * cfgp.pages * NR_PAGE * (16 * (size_t)W4 + 8));
+        slab_need = std::max(slab_need, (size_t)grids[j] * warps_pb * cfgp.pages * NR_PAGE *
+                                            (16 * (size_t)W4 + 8 + 4 * (size_t)G));
     }
     rc = ensure(&sl.wslab, &sl.wslab_bytes, slab_need);
     if (rc) return rc;
@@ -1346,6 +1398,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         const size_t warps = (size_t)grids[j] * warps_pb;
         P.slab_mass = reinterpret_cast<double *>(static_cast<unsigned char *>(sl.wslab) +
                                                  warps * cfgp.pages * NR_PAGE * 16 * (size_t)W4);
+        P.slab_rows = reinterpret_cast<uint32_t *>(static_cast<unsigned char *>(sl.wslab) +
+                                                   warps * cfgp.pages * NR_PAGE * (16 * (size_t)W4 + 8));
         P.pages = cfgp.pages;
         P.n_buckets = cfg.n_buckets;
         P.shift = cfg.shift;

@@ -88,11 +88,44 @@ __device__ __forceinline__ void nr_child_features(float (&f)[NR_FEAT], const uin
     f[15] = 1.f;
 }
 
+// Rows carried in the queue records (the warp engine, simple graphs): the
+// subproblem's in-neighbour row of node v comes in, and the row used and the
+// down edge's endpoints of the lane's child go out, so the child's rows are the
+// parent's with that edge's arcs removed.
+struct NrRowIO {
+    bool have;          // row_in holds node v's not-down in-neighbour row
+    uint32_t row_in;
+    uint32_t row;       // out: the row used
+    int cu, cv;         // out: the lane's child's down hop (cu -> cv)
+};
+
+// not-down in-neighbour row of node v from its in-arc list and the mask
+__device__ __forceinline__ uint32_t nr_build_row(const NrSmemGraph &sg, const uint32_t *my_m, int v)
+{
+    uint32_t row = 0;
+    const int lo = sg.start[v], hi = sg.start[v + 1];
+    int j = lo;
+    for (; j + 4 <= hi; j += 4) {          // four independent in-arcs per trip
+        const uint32_t a0 = sg.list[j], a1 = sg.list[j + 1], a2 = sg.list[j + 2], a3 = sg.list[j + 3];
+        const uint32_t m0 = my_m[a0 >> 12], m1 = my_m[a1 >> 12], m2 = my_m[a2 >> 12], m3 = my_m[a3 >> 12];
+        row |= ((m0 >> ((a0 >> 7) & 30u)) & 1u) << (a0 & 31u);
+        row |= ((m1 >> ((a1 >> 7) & 30u)) & 1u) << (a1 & 31u);
+        row |= ((m2 >> ((a2 >> 7) & 30u)) & 1u) << (a2 & 31u);
+        row |= ((m3 >> ((a3 >> 7) & 30u)) & 1u) << (a3 & 31u);
+    }
+    for (; j < hi; ++j) {
+        const uint32_t a = sg.list[j];
+        row |= ((my_m[a >> 12] >> ((a >> 7) & 30u)) & 1u) << (a & 31u);
+    }
+    return row;
+}
+
 template <int G, int W4, bool FEAT = false>
 __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGraph &sg,
                                           const uint32_t *my_m, bool valid, double mass, double eps,
                                           bool &has_child, uint32_t (&w)[4 * W4], double &cm,
-                                          NrLaneAcc &acc, float (*feat)[NR_FEAT] = nullptr)
+                                          NrLaneAcc &acc, float (*feat)[NR_FEAT] = nullptr,
+                                          NrRowIO *rio = nullptr)
 {
     constexpr int NW = 4 * W4;
     const int lane = threadIdx.x & 31;
@@ -110,24 +143,10 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
         active = false;
     }
 
-    // not-down in-neighbour row of node v
+    // not-down in-neighbour row of node v (carried in, or built from the mask)
     uint32_t row = 0;
-    if (active && v < n) {
-        const int lo = sg.start[v], hi = sg.start[v + 1];
-        int j = lo;
-        for (; j + 4 <= hi; j += 4) {          // four independent in-arcs per trip
-            const uint32_t a0 = sg.list[j], a1 = sg.list[j + 1], a2 = sg.list[j + 2], a3 = sg.list[j + 3];
-            const uint32_t m0 = my_m[a0 >> 12], m1 = my_m[a1 >> 12], m2 = my_m[a2 >> 12], m3 = my_m[a3 >> 12];
-            row |= ((m0 >> ((a0 >> 7) & 30u)) & 1u) << (a0 & 31u);
-            row |= ((m1 >> ((a1 >> 7) & 30u)) & 1u) << (a1 & 31u);
-            row |= ((m2 >> ((a2 >> 7) & 30u)) & 1u) << (a2 & 31u);
-            row |= ((m3 >> ((a3 >> 7) & 30u)) & 1u) << (a3 & 31u);
-        }
-        for (; j < hi; ++j) {
-            const uint32_t a = sg.list[j];
-            row |= ((my_m[a >> 12] >> ((a >> 7) & 30u)) & 1u) << (a & 31u);
-        }
-    }
+    if (rio && rio->have) row = (active && v < n) ? rio->row_in : 0u;
+    else if (active && v < n) row = nr_build_row(sg, my_m, v);
 
     // level-synchronous BFS, one ballot per level for all groups of the warp
     uint32_t F = 1u << src, vis = F;
@@ -170,14 +189,16 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
         unk = ((my_m[e_h >> 4] >> ((e_h & 15) << 1)) & 3u) == 3u;
     }
 
-    // FP64 mass along the path, src side first (sequential, as the oracle)
+    // FP64 mass along the path, src side first (sequential, as the oracle); each hop lane
+    // loads its own p first, so the chain only waits on shuffles and multiplies
+    const double p_h = unk ? sg.p[e_h] : 1.0;
     double P = mass;
     for (int h = 0; h < Lmax; ++h) {
-        const int e = __shfl_sync(NR_FULL, e_h, gbase + h);
+        const double pe = __shfl_sync(NR_FULL, p_h, gbase + h);
         const bool u = __shfl_sync(NR_FULL, unk, gbase + h);
         if (h < L && u) {
-            if (v == h) { cm = __dmul_rn(P, __dsub_rn(1.0, sg.p[e])); has_child = true; }
-            P = __dmul_rn(P, sg.p[e]);
+            if (v == h) { cm = __dmul_rn(P, __dsub_rn(1.0, p_h)); has_child = true; }
+            P = __dmul_rn(P, pe);
         }
     }
     if (live && leader) { acc.leaves++; nr_fix_add_mass(acc.R, P); }
@@ -196,6 +217,7 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
                 if (k == wi) w[k] &= ~bits;
         }
     }
+    if (rio) { rio->row = row; rio->cu = hop_u; rio->cv = hop_v; }
     if constexpr (FEAT) {
         // not-down degrees of src and dst in the child (the parent's rows minus the down edge)
         const uint32_t rs = __shfl_sync(NR_FULL, row, gbase + src);

@@ -46,6 +46,9 @@ struct NrPartial {
 struct NrSmallGraph {
     int n, e, w4, src, dst, n_in;
     int off_p, off_eid, off_start, off_list, blob_bytes;
+    int rows;                   // rows carried in queue records: 0 no (rebuilt from the mask),
+                                // 1 undirected simple graph, 2 directed simple graph
+    int pad0;
     long long blob_off;
     long long struct_off;
 };

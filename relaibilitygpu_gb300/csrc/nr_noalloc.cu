@@ -65,6 +65,7 @@ size_t noalloc_tables(const nr_graph *g, int src, int dst, int G, NrSmallGraph *
     const int n = g->n_nodes, E = g->n_edges;
     const int W = std::max(1, (2 * E + 31) / 32);
     sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst; sg->n_in = g->n_arcs;
+    sg->rows = 0; sg->pad0 = 0;
     size_t off = 0;
     sg->off_p = (int)off; off = a16(off + sizeof(double) * std::max(E, 1));
     sg->off_eid = (int)off; off = a16(off + sizeof(uint16_t) * G * G);
@@ -166,6 +167,7 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     P.next_inst = reinterpret_cast<int *>(base + off_cnt);
     P.slab_mask = reinterpret_cast<uint4 *>(base + off_mask);
     P.slab_mass = reinterpret_cast<double *>(base + off_mass);
+    P.slab_rows = nullptr;            // rows are rebuilt from the masks (no room budgeted for them)
     P.pages = pages;
     P.escalate = 0;
     P.eps = o.truncation_eps > 0 ? o.truncation_eps : 0.0;

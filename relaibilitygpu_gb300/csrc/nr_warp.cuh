@@ -46,6 +46,7 @@ struct NrWarpParams {
     int *next_inst;                  // work counter
     uint4 *slab_mask;                // [warps][pages*32][w4]
     double *slab_mass;               // [warps][pages*32]
+    uint32_t *slab_rows;             // [warps][pages*32][G]: not-down in-neighbour rows (nullptr: none)
     int pages;                       // pages per warp
     int n_buckets;                   // multiple of 32, <= 256
     int shift;                       // bucket resolution (2^shift per octave); < 0 = one bucket
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
     const size_t gw = (size_t)blockIdx.x * (blockDim.x >> 5) + warp;
     uint4 *sl_mask = P.slab_mask + gw * (size_t)NP * NR_PAGE * W4;
     double *sl_mass = P.slab_mass + gw * (size_t)NP * NR_PAGE;
+    uint32_t *sl_rows = P.slab_rows ? P.slab_rows + gw * (size_t)NP * NR_PAGE * G : nullptr;
 
     for (;;) {
         int ii = 0;
@@ -159,6 +161,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
         sg.eid = reinterpret_cast<const uint16_t *>(gs + g.off_eid);
         sg.start = reinterpret_cast<const int *>(gs + g.off_start);
         sg.list = reinterpret_cast<const uint32_t *>(gs + g.off_list);
+        // rows travel with the records on simple graphs (the fork branching rebuilds its own)
+        const int rows_mode = (FORK || !sl_rows) ? 0 : g.rows;
         const long long t0 = nr_globaltimer();
 
         // reset the private queue; the root is the only subproblem
@@ -198,6 +202,16 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
             }
         }
         if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
+        if (rows_mode && grp == 0) {
+            // the root's rows: an arc u -> v is not down when p > 0 (its edge is up or unknown)
+            uint32_t r = 0;
+            if (v < g.n)
+                for (int j = sg.start[v]; j < sg.start[v + 1]; ++j) {
+                    const uint32_t a = sg.list[j];
+                    if (sg.p[a >> 8] > 0.0) r |= 1u << (a & 31u);
+                }
+            sl_rows[(size_t)rpg * NR_PAGE * G + v] = r;
+        }
         __syncwarp();
 
         NrLaneAcc &acc = acc_base[lane];
@@ -253,6 +267,9 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
                     const bool valid = idx < cnt;
                     const size_t slot = (size_t)pg * NR_PAGE + idx;
                     if (valid && v < W4) reinterpret_cast<uint4 *>(my_m)[v] = sl_mask[slot * W4 + v];
+                    NrRowIO rio;
+                    rio.have = rows_mode != 0;
+                    rio.row_in = (rows_mode && valid) ? sl_rows[slot * G + v] : 0u;
                     const double mass = valid ? sl_mass[slot] : 0.0;
                     if (valid && leader) { nr_fix_sub(qacc, nr_fix_of(mass)); qcount--; }
                     __syncwarp();
@@ -265,7 +282,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
                         nr_expand_fork<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
                     else
                         nr_expand<G, W4, LEARN>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc,
-                                                LEARN ? &feat : nullptr);
+                                                LEARN ? &feat : nullptr, &rio);
                     double key = cm;
                     if constexpr (LEARN) {
                         const unsigned cbm = __ballot_sync(NR_FULL, has_child);
@@ -322,9 +339,10 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
                         nA = __shfl_sync(NR_FULL, nA, 0);
                         hB = __shfl_sync(NR_FULL, hB, 0);
                         __syncwarp();
+                        int s = -1;                       // this lane's child's slot
                         if (has_child && cb == b) {
                             const int r = __popc(m & lt_mask);
-                            const int s = (r < nA) ? hA * NR_PAGE + cA + r : (hB >= 0 ? hB * NR_PAGE + (r - nA) : -1);
+                            s = (r < nA) ? hA * NR_PAGE + cA + r : (hB >= 0 ? hB * NR_PAGE + (r - nA) : -1);
                             if (s >= 0) {
                                 uint4 *d = sl_mask + (size_t)s * W4;
 #pragma unroll
@@ -340,6 +358,25 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
                                 nr_fix_add_mass(acc.es, cm);
                             }
                             has_child = false;
+                        }
+                        if (rows_mode) {
+                            // the children's rows: the parent's, less the arcs of the child's down
+                            // edge; one child of every group per step, lane v writes node v's row
+                            const int gb = lane & ~(G - 1);
+                            unsigned todo = (G == 32) ? m : ((m >> gb) & ((1u << G) - 1u));
+                            while (__any_sync(NR_FULL, todo != 0u)) {
+                                const int c = todo ? __ffs(todo) - 1 : 0;
+                                const int sc = __shfl_sync(NR_FULL, s, gb + c);
+                                const int cu = __shfl_sync(NR_FULL, rio.cu, gb + c);
+                                const int cv = __shfl_sync(NR_FULL, rio.cv, gb + c);
+                                if (todo && sc >= 0) {
+                                    uint32_t rr = rio.row;
+                                    if (v == cv) rr &= ~(1u << cu);
+                                    if (rows_mode == 1 && v == cu) rr &= ~(1u << cv);
+                                    sl_rows[(size_t)sc * G + v] = rr;
+                                }
+                                todo &= todo - 1u;
+                            }
                         }
                         pend = __ballot_sync(NR_FULL, has_child);
                     }
