@@ -28,6 +28,9 @@
 #include "nr_mlp.cuh"
 
 const void *nr_grid_kernel_ptr_g8(int w4);
+const void *nr_grid_fork_kernel_ptr_g8(int w4);
+const void *nr_grid_fork_kernel_ptr_g16(int w4);
+const void *nr_grid_fork_kernel_ptr_g32(int w4);
 const void *nr_grid_kernel_ptr_g16(int w4);
 const void *nr_grid_kernel_ptr_g32(int w4);
 const void *nr_grid_wide_kernel_ptr(int w4);
@@ -62,12 +65,12 @@ void nr_last_cuda_error(cudaError_t e, int line, const char *what)
     snprintf(g_err, sizeof(g_err), "%s (nr_api.cu:%d %.120s)", cudaGetErrorString(e), line, what);
 }
 
-const void *grid_kernel(int G, int w4)
+const void *grid_kernel(int G, int w4, bool fork = false)
 {
     switch (G) {
-    case 8: return nr_grid_kernel_ptr_g8(w4);
-    case 16: return nr_grid_kernel_ptr_g16(w4);
-    case 32: return nr_grid_kernel_ptr_g32(w4);
+    case 8: return fork ? nr_grid_fork_kernel_ptr_g8(w4) : nr_grid_kernel_ptr_g8(w4);
+    case 16: return fork ? nr_grid_fork_kernel_ptr_g16(w4) : nr_grid_kernel_ptr_g16(w4);
+    case 32: return fork ? nr_grid_fork_kernel_ptr_g32(w4) : nr_grid_kernel_ptr_g32(w4);
     default: return nullptr;
     }
 }
@@ -686,7 +689,7 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
     const int G = group_width(g->n_nodes);
     const int W4 = sg.w4;
     if (W4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
-    const void *kfn = grid_kernel(G, W4);
+    const void *kfn = grid_kernel(G, W4, o->branching == NR_BRANCH_FORK);
     if (!kfn) return NR_ERR_UNSUPPORTED;
 
     const int block = NR_BLOCK_THREADS;

@@ -17,6 +17,7 @@
     }
 
 const void *nr_grid_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_grid_kernel) }
+const void *nr_grid_fork_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_grid_kernel, , true) }
 const void *nr_warp_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_warp_kernel) }
 const void *nr_warp_learn_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_warp_kernel, , true) }
 const void *nr_warp_fork_kernel_ptr_g32(int w4) { NR_W4_CASES(nr_warp_kernel, , false, true) }

@@ -346,13 +346,3 @@ __device__ __forceinline__ void nr_expand_fork(const NrSmallGraph &g, const NrSm
         has_child = true;
     }
 }
-
-// The same as an out-of-line call, for kernels that branch on fork at run time:
-// the plain path keeps its own register allocation.
-template <int G, int W4>
-__device__ __noinline__ void nr_expand_fork_call(const NrSmallGraph &g, const NrSmemGraph &sg, const uint32_t *my_m,
-                                                 bool valid, double mass, double eps, bool &has_child,
-                                                 uint32_t (&w)[4 * W4], double &cm, NrLaneAcc &acc)
-{
-    nr_expand_fork<G, W4>(g, sg, my_m, valid, mass, eps, has_child, w, cm, acc);
-}

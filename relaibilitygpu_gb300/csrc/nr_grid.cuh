@@ -13,7 +13,8 @@
 
 #include "nr_expand.cuh"
 
-template <int G, int W4>
+// FORK instantiates fork branching (nr_expand_fork) in place of path branching.
+template <int G, int W4, bool FORK = false>
 __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_kernel(NrGridParams P)
 {
     constexpr int K = 32 / G;
@@ -58,8 +59,8 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_kernel(NrGridParams 
             bool has_child;
             uint32_t w[NW];
             double cm;
-            if (P.fork)
-                nr_expand_fork_call<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
+            if constexpr (FORK)
+                nr_expand_fork<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
             else
                 nr_expand<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
 
