@@ -192,6 +192,18 @@ int  nr_batch_submit(nr_context *ctx, int n_instances, const nr_graph *graphs, c
                      void *after_stream, int64_t *ticket);
 int  nr_batch_wait(nr_context *ctx, int64_t ticket);
 
+/* Checkpoint / resume (no reference counterpart) of a bucketed whole-GPU run (graphs above 32
+ * nodes, bucket_shift >= 0): after an nr_reliability_ctx call on the context that ran one (and
+ * before another whole-GPU run on it), nr_checkpoint_save writes the live queue records, the
+ * exact sums and the counts to a file.  nr_checkpoint_resume reloads them for the same graph,
+ * terminals, bucket resolution, eps and branching (checked against a fingerprint in the file)
+ * and continues the run with the given options -- typically a larger max_nodes or a target
+ * width -- as if it had never stopped: counts, sums and waves include the work before the
+ * checkpoint.  Host memory for the live records is needed on both sides. */
+int  nr_checkpoint_save(nr_context *ctx, const char *path);
+int  nr_checkpoint_resume(nr_context *ctx, const char *path, const nr_graph *graph, int src, int dst,
+                          uint64_t capacity, const nr_options *opt, nr_result *result);
+
 /* Autotuner for batches (no reference counterpart).  Times the warp engine on
  * up to 4096 instances of the batch for each candidate setting -- bucket
  * resolution (bucket_shift -1..2, where -1 is one bucket: breadth-first waves), pages per warp (64 or 512,

@@ -346,6 +346,29 @@ struct NrSlot {
     nr_options opt{};
 };
 
+// What a checkpoint of the last bucketed whole-GPU run needs (its queue stays in the
+// context's arena until another whole-GPU run reuses it).
+struct NrCkptState {
+    bool valid = false;
+    uint64_t fp = 0;                 // graph, terminals and options
+    int n = 0, E = 0, src = 0, dst = 0, W4 = 0;
+    NrFix R{}, et{}, es{}, net{};
+    unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0, max_wave = 0;
+    long long waves = 0;
+    unsigned long long cap = 0;      // arena slots
+    size_t mask_bytes = 0, mass_bytes = 0;
+    size_t off_top = 0;              // arena top in the control buffer
+};
+
+// A checkpoint to resume from: the live records and the sums and counts so far.
+struct NrResumeIn {
+    std::vector<unsigned char> masks;  // [live][W4 * 16]
+    std::vector<double> mass;          // [live]
+    NrFix R{}, et{}, es{}, net{};
+    unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0, max_wave = 0;
+    long long waves = 0;
+};
+
 struct nr_context {
     int device = 0;
     int sms = 0;
@@ -361,6 +384,7 @@ struct nr_context {
     int64_t next_ticket = 1;        // asynchronous batches
     std::map<int64_t, int> done_rc; // status of batches finished before their wait
     cudaEvent_t ev_after = nullptr; // orders a batch after a caller's stream
+    NrCkptState ckpt;               // the last bucketed whole-GPU run
     int smem_optin = 0;             // largest dynamic shared memory a block may opt in to
     void *model = nullptr;          // learned scorer: FP32 parameters and their BF16 copy
     NrMlpDev mlp{};
@@ -683,6 +707,7 @@ extern "C" void nr_context_destroy(nr_context *c)
 static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap,
                           const nr_options *o, nr_result *r)
 {
+    c->ckpt.valid = false;                 // the arena is about to be reused
     NrSmallGraph sg;
     std::vector<unsigned char> blob;
     build_small_blob(g, src, dst, &sg, &blob);
@@ -837,6 +862,7 @@ static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg
 static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
                          nr_result *r)
 {
+    c->ckpt.valid = false;                 // the arena is about to be reused
     if (g->n_nodes > NR_WIDE_MAX_N || g->n_edges > 65535) return NR_ERR_UNSUPPORTED;
     NrWideGraph wg;
     std::vector<unsigned char> blob;
@@ -970,13 +996,51 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     return NR_OK;
 }
 
+// Bucket of a mass on the host: the device's nr_bucket (integer operations on the bits).
+static int nr_bucket_host(double m, int shift, int nb)
+{
+    if (shift < 0 || nb <= 1) return 0;
+    unsigned long long bits;
+    memcpy(&bits, &m, 8);
+    long long b = (1023LL << shift) - (long long)(bits >> (52 - shift));
+    b = b < 0 ? 0 : b;
+    b = b > nb - 1 ? nb - 1 : b;
+    return (int)b;
+}
+
+// FNV-1a over everything a bucketed run's queue depends on: the graph, the
+// terminals, the bucket resolution, eps and the branching.
+static uint64_t nr_run_fingerprint(const nr_graph *g, int src, int dst, const nr_options *o)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void *p, size_t n) {
+        const unsigned char *b = static_cast<const unsigned char *>(p);
+        for (size_t i = 0; i < n; ++i) { h ^= b[i]; h *= 1099511628211ull; }
+    };
+    mix(&g->n_nodes, sizeof(int32_t)); mix(&g->n_edges, sizeof(int32_t)); mix(&g->n_arcs, sizeof(int32_t));
+    mix(g->row_ptr, sizeof(int32_t) * (g->n_nodes + 1));
+    mix(g->col_idx, sizeof(int32_t) * g->n_arcs);
+    mix(g->edge_id, sizeof(int32_t) * g->n_arcs);
+    mix(g->edge_p, sizeof(double) * g->n_edges);
+    const int32_t nb = std::max(1, std::min(NR_WIDE_MAX_NB, o->n_buckets > 0 ? (int)o->n_buckets : NR_WIDE_MAX_NB));
+    const int32_t v[5] = {src, dst, o->bucket_shift, nb, o->branching};
+    mix(v, sizeof(v));
+    const double eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
+    mix(&eps, sizeof(eps));
+    return h;
+}
+
 // Whole-GPU bucketed max-mass queue (nr_bucket_wide_kernel) over an arena of
 // `cap` slots: 2^shift buckets per factor of two in mass, nb buckets.
 static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
-                           nr_result *r)
+                           nr_result *r, const NrResumeIn *rin = nullptr)
 {
     if (g->n_nodes > NR_WIDE_MAX_N || g->n_edges > 65535) return NR_ERR_UNSUPPORTED;
-    cap = std::max<uint64_t>(64, std::min<uint64_t>(cap, 0xffffffffull));   // slot ids are 32-bit
+    c->ckpt.valid = false;
+    const uint64_t live_in = rin ? (uint64_t)rin->mass.size() : 0;
+    cap = std::max<uint64_t>(std::max<uint64_t>(64, 2 * live_in),
+                             std::min<uint64_t>(cap, 0xffffffffull));   // slot ids are 32-bit
+    if (cap > 0xffffffffull) return NR_ERR_UNSUPPORTED;
     const int nb = std::max(1, std::min(NR_WIDE_MAX_NB, o->n_buckets > 0 ? (int)o->n_buckets : NR_WIDE_MAX_NB));
     NrWideGraph wg;
     std::vector<unsigned char> blob;
@@ -1049,20 +1113,54 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     P.wpart = reinterpret_cast<NrWideShare *>(sb + off_wpart);
     P.stop_info = reinterpret_cast<int *>(sb + off_info);
     P.stats = reinterpret_cast<unsigned long long *>(sb + off_stats);
-    // the root: initial mask with mass 1 (main.cu:805-809) in slot 0, bucket 0 (mass 1 is the top bucket)
-    std::vector<uint32_t> root(4 * W4, 0);
-    nr_initial_mask(g, root.data(), 4 * W4);
-    const double one = 1.0;
-    const unsigned long long one_u = 1;
-    const unsigned char bucket0 = 0;
+    P.resume = rin ? 1 : 0;
+    P.init_R = P.init_et = P.init_es = P.init_net = nr_fix_zero();
+    P.init_nodes = P.init_leaves = P.init_dead = P.init_trunc = P.init_spilled = 0;
     cudaStream_t s = c->stream;
     NR_CUDA_TRY(cudaMemcpyAsync(sb + off_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaMemsetAsync(sb + off_zero, 0, off - off_zero, s));
-    NR_CUDA_TRY(cudaMemcpyAsync(P.top, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemcpyAsync(P.bcount, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemcpyAsync(P.mask, root.data(), 16 * W4, cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemcpyAsync(P.mass, &one, sizeof(one), cudaMemcpyHostToDevice, s));
-    NR_CUDA_TRY(cudaMemcpyAsync(P.key, &bucket0, 1, cudaMemcpyHostToDevice, s));
+    // host copies must outlive the asynchronous uploads: they live until the synchronise below
+    std::vector<unsigned char> keys;
+    std::vector<unsigned long long> bcnt;
+    NrWideShare share0{};
+    unsigned long long top0 = 1;
+    if (!rin) {
+        // the root: initial mask with mass 1 (main.cu:805-809) in slot 0, bucket 0 (mass 1 is the top bucket)
+        std::vector<uint32_t> root(4 * W4, 0);
+        nr_initial_mask(g, root.data(), 4 * W4);
+        keys.assign(1, 0);
+        bcnt.assign(1, 1);
+        NR_CUDA_TRY(cudaMemcpy(P.mask, root.data(), 16 * W4, cudaMemcpyHostToDevice));
+        const double one = 1.0;
+        NR_CUDA_TRY(cudaMemcpy(P.mass, &one, sizeof(one), cudaMemcpyHostToDevice));
+    } else {
+        // a checkpoint: its records in slots [0, live), their buckets and counts, block 0's sums
+        top0 = live_in;
+        keys.resize(live_in);
+        bcnt.assign(nb, 0);
+        for (uint64_t i = 0; i < live_in; ++i) {
+            keys[i] = (unsigned char)nr_bucket_host(rin->mass[i], P.shift, nb);
+            bcnt[keys[i]]++;
+        }
+        if (live_in) {
+            NR_CUDA_TRY(cudaMemcpy(P.mask, rin->masks.data(), (size_t)live_in * 16 * W4, cudaMemcpyHostToDevice));
+            NR_CUDA_TRY(cudaMemcpy(P.mass, rin->mass.data(), (size_t)live_in * sizeof(double),
+                                   cudaMemcpyHostToDevice));
+        }
+        P.init_R = rin->R; P.init_et = rin->et; P.init_es = rin->es; P.init_net = rin->net;
+        P.init_nodes = rin->nodes; P.init_leaves = rin->leaves; P.init_dead = rin->dead;
+        P.init_trunc = rin->trunc; P.init_spilled = rin->spilled;
+        // the shares the first stop test reads (slot 1): block 0 holds the whole width so far
+        share0.width = rin->et;
+        nr_fix_add(share0.width, rin->es);
+        nr_fix_add(share0.width, rin->net);
+        share0.nodes = rin->nodes;
+    }
+    NR_CUDA_TRY(cudaMemcpyAsync(P.top, &top0, sizeof(top0), cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaMemcpyAsync(P.bcount, bcnt.data(), sizeof(unsigned long long) * bcnt.size(),
+                                cudaMemcpyHostToDevice, s));
+    if (!keys.empty()) NR_CUDA_TRY(cudaMemcpyAsync(P.key, keys.data(), keys.size(), cudaMemcpyHostToDevice, s));
+    if (rin) NR_CUDA_TRY(cudaMemcpyAsync(P.wpart + grid, &share0, sizeof(share0), cudaMemcpyHostToDevice, s));
     void *args[] = {&P};
     NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
     NR_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(block), args, smem, s));
@@ -1077,14 +1175,33 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     NR_CUDA_TRY(cudaStreamSynchronize(s));
     float ms = 0.f;
     NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-    NrFix R = nr_fix_zero(), esp = nr_fix_zero();
+    NrFix R = nr_fix_zero(), esp = nr_fix_zero(), et = nr_fix_zero(), es = nr_fix_zero(), net = nr_fix_zero();
     unsigned long long nodes = 0, leaves = 0, dead = 0, trunc = 0, spilled = 0;
     for (const NrPartial &pp : parts) {          // exact: the order of the additions does not matter
         nr_fix_add(R, pp.R);
-        nr_fix_add(esp, pp.et);
-        nr_fix_add(esp, pp.es);
-        nr_fix_add(esp, pp.q);                   // still queued
+        nr_fix_add(et, pp.et);
+        nr_fix_add(es, pp.es);
+        nr_fix_add(net, pp.q);                   // still queued
         nodes += pp.nodes; leaves += pp.leaves; dead += pp.dead; trunc += pp.truncated; spilled += pp.spilled;
+    }
+    esp = et;
+    nr_fix_add(esp, es);
+    nr_fix_add(esp, net);
+    const long long waves_total = (rin ? rin->waves : 0) + info[0];
+    const unsigned long long maxw_total = std::max<unsigned long long>(rin ? rin->max_wave : 0, stats[0]);
+    if (!status && !(info[0] == P.max_waves)) {
+        NrCkptState &k = c->ckpt;
+        k.valid = true;
+        k.fp = nr_run_fingerprint(g, src, dst, o);
+        k.n = g->n_nodes; k.E = g->n_edges; k.src = src; k.dst = dst; k.W4 = W4;
+        k.R = R; k.et = et; k.es = es; k.net = net;
+        k.nodes = nodes; k.leaves = leaves; k.dead = dead; k.trunc = trunc; k.spilled = spilled;
+        k.max_wave = maxw_total;
+        k.waves = waves_total;
+        k.cap = cap;
+        k.mask_bytes = mask_bytes;
+        k.mass_bytes = mass_bytes;
+        k.off_top = off_top;
     }
     r->R = nr_fix_to_double_host(R);
     r->esp = nr_fix_to_double_host(esp);
@@ -1094,17 +1211,18 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     r->paths = leaves + spilled;
     r->queued = stats[1];
     r->stop = info[1];
-    r->iterations = info[0];
-    r->max_queue_items = stats[0];
+    r->iterations = (int)waves_total;
+    r->max_queue_items = maxw_total;
     r->item_bytes = (int)item_bytes;
-    r->max_queue_mb = (double)stats[0] * item_bytes / (1024.0 * 1024.0);
+    r->max_queue_mb = (double)maxw_total * item_bytes / (1024.0 * 1024.0);
     r->ms = ms;
     if (info[1] == 1) r->time_to_bound_ms = ms;
     r->engine = NR_ENGINE_GRID;
     r->grid_blocks = grid;
     r->block_threads = block;
     r->capacity = cap;
-    r->h2d_bytes = blob.size() + 2 * sizeof(one_u) + 16 * W4 + sizeof(one) + 1;
+    r->h2d_bytes = blob.size() + sizeof(top0) + sizeof(unsigned long long) * bcnt.size() + keys.size() +
+                   (rin ? live_in * (16 * W4 + sizeof(double)) + sizeof(share0) : 16 * W4 + sizeof(double));
     r->d2h_bytes = sizeof(NrPartial) * grid + sizeof(int) + sizeof(info) + sizeof(stats);
     if (status & NR_DEV_ERR_TIMEOUT) return NR_ERR_TIMEOUT;
     if (status) return NR_ERR_INTERNAL;
@@ -1824,6 +1942,103 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     }
     // the wave engine's queue: the reference default capacity (common.h:33) when none is given
     return run_grid_small(c, g, src, dst, capacity ? capacity : (1u << 20), &o, res);
+}
+
+// ---------------------------------------------------------------------------
+// checkpoint / resume of a bucketed whole-GPU run
+// file: "NRCKPT1" magic, run fingerprint, sizes, exact sums, counts, waves, then
+// the live records (mask words, FP64 mass) one after another
+// ---------------------------------------------------------------------------
+namespace {
+struct NrCkptHeader {
+    char magic[8];
+    uint64_t fp;
+    int32_t n, E, src, dst, W4, pad;
+    NrFix R, et, es, net;
+    uint64_t nodes, leaves, dead, trunc, spilled, max_wave;
+    int64_t waves;
+    uint64_t live;
+};
+const char kCkptMagic[8] = {'N', 'R', 'C', 'K', 'P', 'T', '1', 0};
+}  // namespace
+
+extern "C" int nr_checkpoint_save(nr_context *c, const char *path)
+{
+    if (!c || !path) return NR_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const NrCkptState &k = c->ckpt;
+    if (!k.valid) return NR_ERR_INVALID;
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    unsigned long long top = 0;
+    NR_CUDA_TRY(cudaMemcpy(&top, static_cast<unsigned char *>(c->sbuf) + k.off_top, sizeof(top),
+                           cudaMemcpyDeviceToHost));
+    const size_t used = (size_t)std::min<unsigned long long>(top, k.cap);
+    const size_t rec = 16 * (size_t)k.W4;
+    const unsigned char *qb = static_cast<const unsigned char *>(c->qbuf);
+    std::vector<unsigned char> keys(used), masks(used * rec);
+    std::vector<double> mass(used);
+    if (used) {
+        NR_CUDA_TRY(cudaMemcpy(keys.data(), qb + k.mask_bytes + k.mass_bytes, used, cudaMemcpyDeviceToHost));
+        NR_CUDA_TRY(cudaMemcpy(masks.data(), qb, used * rec, cudaMemcpyDeviceToHost));
+        NR_CUDA_TRY(cudaMemcpy(mass.data(), qb + k.mask_bytes, used * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    NrCkptHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, kCkptMagic, 8);
+    h.fp = k.fp;
+    h.n = k.n; h.E = k.E; h.src = k.src; h.dst = k.dst; h.W4 = k.W4;
+    h.R = k.R; h.et = k.et; h.es = k.es; h.net = k.net;
+    h.nodes = k.nodes; h.leaves = k.leaves; h.dead = k.dead; h.trunc = k.trunc; h.spilled = k.spilled;
+    h.max_wave = k.max_wave;
+    h.waves = k.waves;
+    for (size_t i = 0; i < used; ++i) h.live += (keys[i] != NR_WIDE_FREE);
+    FILE *f = fopen(path, "wb");
+    if (!f) return NR_ERR_IO;
+    bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+    for (size_t i = 0; i < used && ok; ++i) {
+        if (keys[i] == NR_WIDE_FREE) continue;
+        ok = fwrite(masks.data() + i * rec, 1, rec, f) == rec && fwrite(&mass[i], sizeof(double), 1, f) == 1;
+    }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? NR_OK : NR_ERR_IO;
+}
+
+extern "C" int nr_checkpoint_resume(nr_context *c, const char *path, const nr_graph *g, int src, int dst,
+                                    uint64_t capacity, const nr_options *opt, nr_result *res)
+{
+    if (!c || !path || !res) return NR_ERR_INVALID;
+    memset(res, 0, sizeof(*res));
+    int rc = validate(g, src, dst);
+    if (rc) return rc;
+    nr_options o;
+    if (opt) o = *opt; else nr_options_default(&o);
+    if (g->n_nodes <= NR_SMALL_MAX_N || o.bucket_shift < 0 || o.order == NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
+    if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
+    FILE *f = fopen(path, "rb");
+    if (!f) return NR_ERR_IO;
+    NrCkptHeader h;
+    NrResumeIn rin;
+    bool ok = fread(&h, sizeof(h), 1, f) == 1 && memcmp(h.magic, kCkptMagic, 8) == 0;
+    const int W4 = std::max(1, ((2 * g->n_edges + 31) / 32 + 3) / 4);
+    ok = ok && h.fp == nr_run_fingerprint(g, src, dst, &o) && h.W4 == W4 && h.live < (1ull << 32);
+    if (!ok) { fclose(f); return NR_ERR_INVALID; }
+    const size_t rec = 16 * (size_t)W4;
+    rin.masks.resize(h.live * rec);
+    rin.mass.resize(h.live);
+    for (uint64_t i = 0; i < h.live && ok; ++i)
+        ok = fread(rin.masks.data() + i * rec, 1, rec, f) == rec && fread(&rin.mass[i], sizeof(double), 1, f) == 1;
+    fclose(f);
+    if (!ok) return NR_ERR_PARSE;
+    rin.R = h.R; rin.et = h.et; rin.es = h.es; rin.net = h.net;
+    rin.nodes = h.nodes; rin.leaves = h.leaves; rin.dead = h.dead; rin.trunc = h.trunc; rin.spilled = h.spilled;
+    rin.max_wave = h.max_wave;
+    rin.waves = h.waves;
+    res->n_nodes = g->n_nodes; res->n_edges = g->n_edges; res->src = src; res->dst = dst;
+    res->mask_words = std::max(1, (2 * g->n_edges + 31) / 32);
+    std::lock_guard<std::mutex> lock(c->mu);
+    drain(c);
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    return run_bucket_wide(c, g, src, dst, capacity ? capacity : (1u << 22), &o, res, &rin);
 }
 
 extern "C" int nr_reliability(const nr_graph *g, int src, int dst, uint64_t capacity, const nr_options *opt,

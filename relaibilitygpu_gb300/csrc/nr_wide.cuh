@@ -101,6 +101,11 @@ struct NrBucketWideParams {
     int *stop_info;                 // [0] waves run, [1] stop reason (0 empty, 1 target, 3 budget), [2] compactions
     unsigned long long *stats;      // [0] widest wave, [1] records queued at the end
     int fork;                       // 1: fork branching on the most reliable path edge
+    // resume from a checkpoint: the arena holds its queue and block 0's first lane starts from
+    // its sums and counts (the stop test before the first wave sees them through the shares)
+    int resume;
+    NrFix init_R, init_et, init_es, init_net;
+    unsigned long long init_nodes, init_leaves, init_dead, init_trunc, init_spilled;
 };
 
 // per-warp shared memory: mask words, frontier / next / visited bitmasks,
@@ -607,6 +612,11 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketW
     const unsigned long long cap = P.capacity;
     NrWideAcc A;
     nr_wide_acc_init(A);
+    if (P.resume && blockIdx.x == 0 && threadIdx.x == 0) {
+        A.R = P.init_R; A.et = P.init_et; A.es = P.init_es; A.net = P.init_net;
+        A.nodes = P.init_nodes; A.leaves = P.init_leaves; A.dead = P.init_dead; A.trunc = P.init_trunc;
+        A.spilled = P.init_spilled;
+    }
     NrWideOut O;
     O.mask = P.mask;
     O.mass = P.mass;
@@ -622,8 +632,8 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketW
         int bsel;
         nr_bucket_select(P.bcount, P.nb, &bsel, &live);
         if (live == 0) break;                               // queue empty
-        stop = nr_wide_stop_test(P.wpart + (size_t)((wave + 1) & 1) * gridDim.x, wave == 0, P.target_on,
-                                 P.target_fix, P.max_nodes);
+        stop = nr_wide_stop_test(P.wpart + (size_t)((wave + 1) & 1) * gridDim.x, wave == 0 && !P.resume,
+                                 P.target_on, P.target_fix, P.max_nodes);
         if (stop) break;
         // reclaim freed slots once they are a large part of the used arena
         unsigned long long used = min(__ldcg(P.top), cap);

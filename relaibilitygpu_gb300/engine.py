@@ -74,7 +74,7 @@ EXPORTS = [
     "nr_initial_mask", "nr_context_create", "nr_context_destroy", "nr_reliability", "nr_reliability_ctx",
     "nr_reliability_batch", "nr_batch_submit", "nr_batch_wait", "nr_format_result", "nr_reliability_noalloc", "nr_autotune",
     "nr_mlp_param_count", "nr_mlp_init", "nr_mlp_grad", "nr_mlp_train", "nr_mlp_infer", "nr_context_set_model",
-    "nr_collect_children",
+    "nr_collect_children", "nr_checkpoint_save", "nr_checkpoint_resume",
 ]
 
 _lib_handle: Optional[C.CDLL] = None
@@ -142,6 +142,11 @@ def lib() -> C.CDLL:
                                       C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_uint64), C.POINTER(NrResult)]
     L.nr_collect_children.restype = C.c_int
+    L.nr_checkpoint_save.argtypes = [C.c_void_p, C.c_char_p]
+    L.nr_checkpoint_save.restype = C.c_int
+    L.nr_checkpoint_resume.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(NrGraph), C.c_int, C.c_int, C.c_uint64,
+                                       C.POINTER(NrOptions), C.POINTER(NrResult)]
+    L.nr_checkpoint_resume.restype = C.c_int
     L.nr_format_result.argtypes = [C.POINTER(NrResult), C.c_char_p, C.c_size_t]
     L.nr_format_result.restype = C.c_int
     _lib_handle = L
@@ -288,6 +293,19 @@ class Context:
 
     def reliability_batch(self, graphs: Sequence[Graph], srcs, dsts, capacity: int = 0, **opts):
         return self.run_batch(Batch(graphs, srcs, dsts), capacity=capacity, **opts)
+
+    def checkpoint_save(self, path: str) -> None:
+        """Write the last bucketed whole-GPU run's queue and sums (nr_checkpoint_save)."""
+        _check(lib().nr_checkpoint_save(self.h, path.encode()))
+
+    def checkpoint_resume(self, path: str, g: Graph, src: int, dst: int, capacity: int = 0, **opts) -> Result:
+        """Continue a checkpointed run (nr_checkpoint_resume) with these options."""
+        gv = _GraphView(g)
+        o = make_options(**opts)
+        r = NrResult()
+        _check(lib().nr_checkpoint_resume(self.h, path.encode(), C.byref(gv.c), int(src), int(dst), int(capacity),
+                                          C.byref(o), C.byref(r)))
+        return Result.from_raw(r)
 
     def submit(self, batch: "Batch", capacity: int = 0, after_stream: int = 0, **opts) -> int:
         """Queue a prepared batch with nr_batch_submit and return its ticket.

@@ -193,3 +193,35 @@ def test_bucket_queue_node_budget(ctx, oracle):
     o = oracle.run(g, g.src, g.dst, target_width=1e-9, bucket_shift=2, n_buckets=255, threads=4,
                    max_nodes=200_000)
     check(r, o)
+
+
+def test_checkpoint_resume_continues_the_same_run(ctx, engine_lib, tmp_path):
+    """A bucketed run stopped at a node budget, saved and resumed (twice) ends exactly where the
+    uninterrupted run ends: same waves, counts, queue and exact sums."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.rgg(60, 150, p_range=(0.9, 0.99), seed=11)
+    opts = dict(order="maxmass", bucket_shift=2, n_buckets=255, target_width=1e-7)
+    full = ctx.reliability(g, g.src, g.dst, capacity=1 << 22, **opts)
+    assert full.stop == 1
+    part = ctx.reliability(g, g.src, g.dst, capacity=1 << 22, max_nodes=150_000, **opts)
+    assert part.stop == 3 and part.nodes < full.nodes
+    p1 = str(tmp_path / "a.ckpt")
+    ctx.checkpoint_save(p1)
+    mid = ctx.checkpoint_resume(p1, g, g.src, g.dst, capacity=1 << 22, max_nodes=400_000, **opts)
+    assert mid.stop == 3 and part.nodes < mid.nodes < full.nodes
+    p2 = str(tmp_path / "b.ckpt")
+    ctx.checkpoint_save(p2)
+    end = ctx.checkpoint_resume(p2, g, g.src, g.dst, capacity=1 << 22, **opts)
+    for f in ("R", "esp", "nodes", "leaves", "dead_ends", "paths", "iterations", "max_queue_items", "queued", "stop"):
+        assert getattr(end, f) == getattr(full, f), f
+    # another graph, or other buckets, cannot resume this file
+    other = graphs.rgg(60, 150, p_range=(0.9, 0.99), seed=12)
+    with pytest.raises(engine_lib.NrError) as e:
+        ctx.checkpoint_resume(p2, other, other.src, other.dst, **opts)
+    assert e.value.status == -1
+    with pytest.raises(engine_lib.NrError):
+        ctx.checkpoint_resume(p2, g, g.src, g.dst, **dict(opts, bucket_shift=1))
+    # a run on another engine invalidates the saved state
+    ctx.reliability(graphs.complete(40, p=0.5), 0, 39, capacity=1 << 16, eps=1e-3)
+    with pytest.raises(engine_lib.NrError):
+        ctx.checkpoint_save(str(tmp_path / "c.ckpt"))
