@@ -192,6 +192,16 @@ int  nr_batch_submit(nr_context *ctx, int n_instances, const nr_graph *graphs, c
                      void *after_stream, int64_t *ticket);
 int  nr_batch_wait(nr_context *ctx, int64_t ticket);
 
+/* K-terminal reliability (the reference stubs a target set, parallel/Rel_16M.cu:43): the
+ * probability that every node of terminals[0..n_terminals) is connected to terminals[0].  The
+ * same disjoint decomposition runs over the BFS tree that joins every terminal to terminals[0]
+ * (the union of their parent paths), its UNKNOWN edges in BFS order (by depth, then node
+ * index); with two terminals it is the two-terminal run exactly.  Runs on the whole-GPU
+ * engines for any n <= 1024 (breadth-first waves, or the bucketed max-mass queue for
+ * NR_ORDER_MAXMASS and target widths); path branching only. */
+int  nr_reliability_kterminal(nr_context *ctx, const nr_graph *graph, const int32_t *terminals, int n_terminals,
+                              uint64_t capacity, const nr_options *opt, nr_result *result);
+
 /* Checkpoint / resume (no reference counterpart) of a bucketed whole-GPU run (graphs above 32
  * nodes, bucket_shift >= 0): after an nr_reliability_ctx call on the context that ran one (and
  * before another whole-GPU run on it), nr_checkpoint_save writes the live queue records, the

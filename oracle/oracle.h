@@ -21,6 +21,10 @@
  *                               seq/seq.cpp:539-578 (child k = first k-1
  *                               UNKNOWN path edges up, k-th down, src side
  *                               first; all-up mass -> R)
+ *   K-terminal ................ the same decomposition over the BFS tree that joins
+ *                               every terminal to src (the union of the parent
+ *                               paths), its edges in BFS order; the reference only
+ *                               stubs a target set (parallel/Rel_16M.cu:43)
  *   fork branching ............ workingPad/main.cu:303-430 with :550-565
  *                               (FORK_BEST_EDGE) and seq/seq_best.cpp:358-389:
  *                               a path of up edges puts the whole mass in R;
@@ -73,7 +77,8 @@ typedef struct og_opts {
     uint64_t capacity;      /* queued-item limit, overflow spills to ESP; 0 = unlimited */
     uint64_t max_nodes;     /* stop after about this many pops (timing samples); 0 = none */
     int32_t  branching;     /* OG_BRANCH_PATH (disjoint path children) or OG_BRANCH_FORK */
-    int32_t  pad0;
+    int32_t  n_terminals;   /* K-terminal: > 0 with `terminals` below; src is terminals[0] */
+    const int32_t *terminals;
 } og_opts;
 
 typedef struct og_result {
@@ -114,6 +119,9 @@ int  og_run_batch(int n, const og_graph *graphs, const int32_t *srcs, const int3
 /* Exact R by enumerating the 2^k states of the k edges with 0 < p < 1.
  * n_nodes <= 64, k <= 30. Returns a negative number on bad input. */
 double og_brute(const og_graph *g, int src, int dst);
+
+/* The same for K-terminal reliability: every node of `terminals` connected to terminals[0]. */
+double og_brute_k(const og_graph *g, const int32_t *terminals, int n_terminals);
 
 /* Bucket index used by the wave schedule (shared definition with the engine). */
 int og_bucket(double mass, int shift, int n_buckets);

@@ -34,7 +34,8 @@ class OgOpts(C.Structure):
     _fields_ = [("bfs_rule", C.c_int32), ("precheck", C.c_int32), ("order", C.c_int32),
                 ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("threads", C.c_int32),
                 ("eps", C.c_double), ("target_width", C.c_double), ("capacity", C.c_uint64),
-                ("max_nodes", C.c_uint64), ("branching", C.c_int32), ("pad0", C.c_int32)]
+                ("max_nodes", C.c_uint64), ("branching", C.c_int32), ("n_terminals", C.c_int32),
+                ("terminals", C.c_void_p)]
 
 
 class OgResult(C.Structure):
@@ -67,6 +68,8 @@ def lib():
         L.og_run.restype = C.c_int
         L.og_brute.argtypes = [C.POINTER(OgGraph), C.c_int, C.c_int]
         L.og_brute.restype = C.c_double
+        L.og_brute_k.argtypes = [C.POINTER(OgGraph), C.POINTER(C.c_int32), C.c_int]
+        L.og_brute_k.restype = C.c_double
         L.og_bucket.argtypes = [C.c_double, C.c_int, C.c_int]
         L.og_bucket.restype = C.c_int
         L.og_run_batch.argtypes = [C.c_int, C.POINTER(OgGraph), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
@@ -156,7 +159,10 @@ def run_batch(batch: BatchArgs, threads: int = 1, **kw):
 
 def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, order: str = "waves",
         bucket_shift: int = -1, n_buckets: int = 1, threads: int = 1, eps: float = 0.0,
-        target_width: float = 0.0, capacity: int = 0, max_nodes: int = 0, branching: str = "path") -> OracleResult:
+        target_width: float = 0.0, capacity: int = 0, max_nodes: int = 0, branching: str = "path",
+        terminals=None) -> OracleResult:
+    """terminals: K-terminal reliability of this node list (src and dst are then ignored;
+    terminals[0] is the search root)."""
     v = _View(g)
     o = OgOpts()
     lib().og_default_opts(C.byref(o))
@@ -171,11 +177,25 @@ def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, orde
     o.capacity = int(capacity)
     o.max_nodes = int(max_nodes)
     o.branching = BRANCHING[branching]
+    term = None
+    if terminals is not None:
+        term = np.ascontiguousarray(terminals, dtype=np.int32)
+        o.n_terminals = len(term)
+        o.terminals = term.ctypes.data
     r = OgResult()
     rc = lib().og_run(C.byref(v.c), int(src), int(dst), C.byref(o), C.byref(r))
     if rc != 0:
         raise ValueError(f"oracle rejected the instance ({rc})")
     return OracleResult(**{f: getattr(r, f) for f, _ in OgResult._fields_})
+
+
+def brute_k(g, terminals) -> float:
+    v = _View(g)
+    t = np.ascontiguousarray(terminals, dtype=np.int32)
+    r = lib().og_brute_k(C.byref(v.c), t.ctypes.data_as(C.POINTER(C.c_int32)), len(t))
+    if r < 0:
+        raise ValueError("brute force limits: n_nodes <= 64 and at most 30 uncertain edges")
+    return r
 
 
 def brute(g, src: int, dst: int) -> float:

@@ -269,6 +269,10 @@ typedef struct {
     const og_graph *g;
     const double *q;
     int src, dst, W, rule, precheck, branching;
+    int nk;                     /* K-terminal: terminals other than src (0: two-terminal) */
+    uint8_t *isterm;            /* [n] */
+    int32_t *order;             /* [n] BFS order of the last K-terminal search */
+    uint8_t *mark;              /* [n] */
     double eps;
     /* BFS scratch */
     uint32_t gen;
@@ -288,6 +292,15 @@ static void x_init(xctx *x, const og_graph *g, const double *q, int src, int dst
     x->W = (g->n_edges * 2 + 31) / 32;
     if (x->W < 1) x->W = 1;
     x->rule = o->bfs_rule; x->precheck = o->precheck; x->eps = o->eps; x->branching = o->branching;
+    x->isterm = (uint8_t *)calloc(n, 1);
+    x->order = (int32_t *)malloc((n + 1) * sizeof(int32_t));
+    x->mark = (uint8_t *)calloc(n, 1);
+    if (o->n_terminals > 0 && o->terminals) {
+        for (int i = 0; i < o->n_terminals; i++) {
+            int t = o->terminals[i];
+            if (t != src && t >= 0 && t < n && !x->isterm[t]) { x->isterm[t] = 1; x->nk++; }
+        }
+    }
     x->vis = (uint32_t *)calloc(n, sizeof(uint32_t));
     x->par_e = (int32_t *)malloc(n * sizeof(int32_t));
     x->par_v = (int32_t *)malloc(n * sizeof(int32_t));
@@ -300,6 +313,7 @@ static void x_init(xctx *x, const og_graph *g, const double *q, int src, int dst
 
 static void x_free(xctx *x)
 {
+    free(x->isterm); free(x->order); free(x->mark);
     free(x->vis); free(x->par_e); free(x->par_v); free(x->cur); free(x->nxt);
     free(x->path); free(x->work); free(x->child);
 }
@@ -374,6 +388,42 @@ static int x_bfs_states(xctx *x, const uint32_t *m, int up_only)
     return 0;
 }
 
+/* K-terminal search: level BFS from src over not-down arcs (parent = smallest
+ * frontier node, as x_bfs), whole levels, until every terminal is reached; the
+ * visit order (src, then each level in ascending node order) goes to x->order.
+ * Returns the number of nodes in x->order if all terminals were reached, else 0. */
+static int x_bfs_k(xctx *x, const uint32_t *m)
+{
+    const og_graph *g = x->g;
+    int src = x->src;
+    if (++x->gen == 0) { memset(x->vis, 0, g->n_nodes * sizeof(uint32_t)); x->gen = 1; }
+    uint32_t gen = x->gen;
+    x->vis[src] = gen;
+    int no = 0, found = 0;
+    x->order[no++] = src;
+    int nc = 1;
+    x->cur[0] = src;
+    while (nc && found < x->nk) {
+        int nn = 0;
+        for (int i = 0; i < nc; i++) {
+            int u = x->cur[i];
+            for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; j++) {
+                int v = g->col_idx[j], e = g->edge_id[j];
+                if (x->vis[v] != gen && notdown(m, e)) {
+                    x->vis[v] = gen; x->par_v[v] = u; x->par_e[v] = e;
+                    x->nxt[nn++] = v;
+                    if (x->isterm[v]) found++;
+                }
+            }
+        }
+        sort_small(x->nxt, nn);
+        for (int i = 0; i < nn; i++) x->order[no++] = x->nxt[i];
+        int32_t *t = x->cur; x->cur = x->nxt; x->nxt = t;
+        nc = nn;
+    }
+    return found == x->nk ? no : 0;
+}
+
 /* child sink: returns 0 if stored, 1 if it overflowed (counted by caller) */
 typedef int (*sink_fn)(void *ud, const uint32_t *mask, double mass);
 
@@ -427,11 +477,25 @@ static void x_expand(xctx *x, const uint32_t *m, double mass, sink_fn sink, void
         return;
     }
     if (x->branching == OG_BRANCH_FORK) { x_fork(x, m, mass, sink, ud); return; }
-    if (!x_bfs(x, m)) { x->dead++; return; }
-    /* path hops in src -> dst order */
     int L = 0;
-    for (int v = x->dst; v != x->src; v = x->par_v[v]) x->path[L++] = x->par_e[v];
-    for (int i = 0, j = L - 1; i < j; i++, j--) { int32_t t = x->path[i]; x->path[i] = x->path[j]; x->path[j] = t; }
+    if (x->nk) {
+        /* K-terminal: the tree joining every terminal to src, its edges in BFS order */
+        int no = x_bfs_k(x, m);
+        if (!no) { x->dead++; return; }
+        for (int i = 0; i < no; i++) x->mark[x->order[i]] = 0;
+        for (int i = 1; i < no; i++) {
+            int t = x->order[i];
+            if (!x->isterm[t]) continue;
+            for (int v = t; v != x->src && !x->mark[v]; v = x->par_v[v]) x->mark[v] = 1;
+        }
+        for (int i = 1; i < no; i++)
+            if (x->mark[x->order[i]]) x->path[L++] = x->par_e[x->order[i]];
+    } else {
+        if (!x_bfs(x, m)) { x->dead++; return; }
+        /* path hops in src -> dst order */
+        for (int v = x->dst; v != x->src; v = x->par_v[v]) x->path[L++] = x->par_e[v];
+        for (int i = 0, j = L - 1; i < j; i++, j--) { int32_t t = x->path[i]; x->path[i] = x->path[j]; x->path[j] = t; }
+    }
     const double *p = x->g->edge_p;
     memcpy(x->work, m, x->W * sizeof(uint32_t));
     double P = mass;
@@ -975,6 +1039,13 @@ int og_run_batch(int n, const og_graph *graphs, const int32_t *srcs, const int32
 int og_run(const og_graph *g, int src, int dst, const og_opts *o, og_result *r)
 {
     memset(r, 0, sizeof(*r));
+    if (o->n_terminals > 0) {                     /* K-terminal: src is terminals[0] */
+        if (!o->terminals) { r->status = -1; return -1; }
+        for (int i = 0; i < o->n_terminals; i++)
+            if (o->terminals[i] < 0 || o->terminals[i] >= g->n_nodes) { r->status = -1; return -1; }
+        src = o->terminals[0];
+        dst = o->terminals[o->n_terminals - 1];
+    }
     if (!g || g->n_nodes <= 0 || src < 0 || dst < 0 || src >= g->n_nodes || dst >= g->n_nodes) {
         r->status = -1;
         return -1;
@@ -994,7 +1065,7 @@ int og_run(const og_graph *g, int src, int dst, const og_opts *o, og_result *r)
         else root[e >> 4] |= 3u << ((e & 15) * 2);
     }
     int rc;
-    if (o->order == OG_ORDER_WAVES && o->threads <= 1) {
+    if (o->order == OG_ORDER_WAVES && o->threads <= 1 && o->n_terminals <= 0) {
         og_arena a;
         memset(&a, 0, sizeof(a));
         rc = run_waves_arena(&a, g, src, dst, o, r);
@@ -1010,11 +1081,34 @@ int og_run(const og_graph *g, int src, int dst, const og_opts *o, og_result *r)
 /* ------------------------------------------------------------------ */
 /* 2^k brute force over the edges with 0 < p < 1                       */
 /* ------------------------------------------------------------------ */
+static double brute_set(const og_graph *g, int src, uint64_t want);
+
 double og_brute(const og_graph *g, int src, int dst)
 {
-    int n = g->n_nodes, E = g->n_edges;
+    int n = g->n_nodes;
     if (n > 64 || src < 0 || dst < 0 || src >= n || dst >= n) return -1.0;
     if (src == dst) return 1.0;
+    return brute_set(g, src, 1ull << dst);
+}
+
+double og_brute_k(const og_graph *g, const int32_t *terminals, int n_terminals)
+{
+    int n = g->n_nodes;
+    if (n > 64 || n_terminals < 1) return -1.0;
+    uint64_t want = 0;
+    for (int i = 0; i < n_terminals; i++) {
+        if (terminals[i] < 0 || terminals[i] >= n) return -1.0;
+        want |= 1ull << terminals[i];
+    }
+    want &= ~(1ull << terminals[0]);
+    if (!want) return 1.0;
+    return brute_set(g, terminals[0], want);
+}
+
+/* probability that every node of `want` is reachable from src */
+static double brute_set(const og_graph *g, int src, uint64_t want)
+{
+    int n = g->n_nodes, E = g->n_edges;
     int *var = (int *)malloc((E ? E : 1) * sizeof(int));
     int k = 0;
     for (int e = 0; e < E; e++) if (g->edge_p[e] > 0.0 && g->edge_p[e] < 1.0) var[k++] = e;
@@ -1082,9 +1176,9 @@ double og_brute(const og_graph *g, int src, int dst)
             nf &= ~reach;
             reach |= nf;
             fr = nf;
-            if ((reach >> dst) & 1) break;
+            if ((reach & want) == want) break;
         }
-        if ((reach >> dst) & 1)
+        if ((reach & want) == want)
             ks_add(&R, tl[gray & (((uint64_t)1 << kl) - 1)] * th[gray >> kl]);
     }
     free(var); free(arcs); free(arc_var); free(vindex); free(tl); free(th);

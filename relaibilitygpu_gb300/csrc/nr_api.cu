@@ -837,7 +837,8 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
 // ---------------------------------------------------------------------------
 // whole-GPU engine for 33..1024 nodes (nr_wide.cuh)
 // ---------------------------------------------------------------------------
-static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg, std::vector<unsigned char> *blob)
+static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg, std::vector<unsigned char> *blob,
+                            const int32_t *terms = nullptr, int nt = 0)
 {
     const int n = g->n_nodes, E = g->n_edges;
     const int W = std::max(1, (2 * E + 31) / 32);
@@ -848,8 +849,18 @@ static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg
     wg->off_q = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
     wg->off_row = (int)off; off = align16(off + sizeof(int) * (n + 1));
     wg->off_arc = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
+    wg->off_kmask = (int)off; off = align16(off + sizeof(uint32_t) * wg->nwd);
     wg->blob_bytes = (int)off;
     blob->assign(off, 0);
+    // K-terminal: the terminals other than src
+    uint32_t *km = reinterpret_cast<uint32_t *>(blob->data() + wg->off_kmask);
+    wg->nk = 0;
+    for (int i = 0; i < nt; ++i) {
+        const int t = terms[i];
+        if (t == src || ((km[t >> 5] >> (t & 31)) & 1u)) continue;
+        km[t >> 5] |= 1u << (t & 31);
+        wg->nk++;
+    }
     double *p = reinterpret_cast<double *>(blob->data() + wg->off_p);
     double *q = reinterpret_cast<double *>(blob->data() + wg->off_q);
     int *row = reinterpret_cast<int *>(blob->data() + wg->off_row);
@@ -860,13 +871,13 @@ static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg
 }
 
 static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
-                         nr_result *r)
+                         nr_result *r, const int32_t *terms = nullptr, int nt = 0)
 {
     c->ckpt.valid = false;                 // the arena is about to be reused
     if (g->n_nodes > NR_WIDE_MAX_N || g->n_edges > 65535) return NR_ERR_UNSUPPORTED;
     NrWideGraph wg;
     std::vector<unsigned char> blob;
-    build_wide_blob(g, src, dst, &wg, &blob);
+    build_wide_blob(g, src, dst, &wg, &blob, terms, nt);
     const int W4 = wg.w4;
     if (W4 > NR_WIDE_MAX_W4) return NR_ERR_UNSUPPORTED;
     const void *kfn = nr_grid_wide_kernel_ptr(W4);
@@ -1033,7 +1044,8 @@ static uint64_t nr_run_fingerprint(const nr_graph *g, int src, int dst, const nr
 // Whole-GPU bucketed max-mass queue (nr_bucket_wide_kernel) over an arena of
 // `cap` slots: 2^shift buckets per factor of two in mass, nb buckets.
 static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
-                           nr_result *r, const NrResumeIn *rin = nullptr)
+                           nr_result *r, const NrResumeIn *rin = nullptr, const int32_t *terms = nullptr,
+                           int nt = 0)
 {
     if (g->n_nodes > NR_WIDE_MAX_N || g->n_edges > 65535) return NR_ERR_UNSUPPORTED;
     c->ckpt.valid = false;
@@ -1044,7 +1056,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     const int nb = std::max(1, std::min(NR_WIDE_MAX_NB, o->n_buckets > 0 ? (int)o->n_buckets : NR_WIDE_MAX_NB));
     NrWideGraph wg;
     std::vector<unsigned char> blob;
-    build_wide_blob(g, src, dst, &wg, &blob);
+    build_wide_blob(g, src, dst, &wg, &blob, terms, nt);
     const int W4 = wg.w4;
     if (W4 > NR_WIDE_MAX_W4) return NR_ERR_UNSUPPORTED;
     const void *kfn = nr_bucket_wide_kernel_ptr(W4);
@@ -1189,7 +1201,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     nr_fix_add(esp, net);
     const long long waves_total = (rin ? rin->waves : 0) + info[0];
     const unsigned long long maxw_total = std::max<unsigned long long>(rin ? rin->max_wave : 0, stats[0]);
-    if (!status && !(info[0] == P.max_waves)) {
+    if (!status && !(info[0] == P.max_waves) && wg.nk == 0) {   // K-terminal runs are not checkpointed
         NrCkptState &k = c->ckpt;
         k.valid = true;
         k.fp = nr_run_fingerprint(g, src, dst, o);
@@ -1233,13 +1245,13 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
 // in the default order) with a bucket shift >= 0, else breadth-first waves.  The learned
 // order is n <= 32 only.
 static int run_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t capacity, const nr_options *o,
-                    nr_result *r)
+                    nr_result *r, const int32_t *terms = nullptr, int nt = 0)
 {
     if (o->order == NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
     const bool buckets = o->bucket_shift >= 0 &&
                          (o->order == NR_ORDER_MAXMASS || (o->order == NR_ORDER_AUTO && o->target_width > 0));
-    if (buckets) return run_bucket_wide(c, g, src, dst, capacity ? capacity : (1u << 22), o, r);
-    return run_grid_wide(c, g, src, dst, capacity ? capacity : (1u << 20), o, r);
+    if (buckets) return run_bucket_wide(c, g, src, dst, capacity ? capacity : (1u << 22), o, r, nullptr, terms, nt);
+    return run_grid_wide(c, g, src, dst, capacity ? capacity : (1u << 20), o, r, terms, nt);
 }
 
 // ---------------------------------------------------------------------------
@@ -1942,6 +1954,31 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     }
     // the wave engine's queue: the reference default capacity (common.h:33) when none is given
     return run_grid_small(c, g, src, dst, capacity ? capacity : (1u << 20), &o, res);
+}
+
+extern "C" int nr_reliability_kterminal(nr_context *c, const nr_graph *g, const int32_t *terminals, int n_terminals,
+                                        uint64_t capacity, const nr_options *opt, nr_result *res)
+{
+    if (!c || !res || !terminals || n_terminals < 1) return NR_ERR_INVALID;
+    memset(res, 0, sizeof(*res));
+    const int src = terminals[0];
+    for (int i = 0; i < n_terminals; ++i) {
+        const int rc = validate(g, src, terminals[i]);
+        if (rc) return rc;
+    }
+    nr_options o;
+    if (opt) o = *opt; else nr_options_default(&o);
+    if (o.order == NR_ORDER_LEARNED || o.branching != NR_BRANCH_PATH) return NR_ERR_UNSUPPORTED;
+    res->n_nodes = g->n_nodes;
+    res->n_edges = g->n_edges;
+    res->src = src;
+    res->dst = terminals[n_terminals - 1];
+    res->mask_words = std::max(1, (2 * g->n_edges + 31) / 32);
+    std::lock_guard<std::mutex> lock(c->mu);
+    drain(c);
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    // one terminal besides src is the two-terminal problem on the same engine (dst = that terminal)
+    return run_wide(c, g, src, terminals[n_terminals - 1], capacity, &o, res, terminals, n_terminals);
 }
 
 // ---------------------------------------------------------------------------

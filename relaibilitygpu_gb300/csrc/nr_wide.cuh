@@ -44,6 +44,8 @@
 struct NrWideGraph {
     int n, e, w4, src, dst, n_arcs, nwd;
     int off_p, off_q, off_row, off_arc, blob_bytes;
+    int nk;                     // K-terminal: terminals other than src (0: two-terminal, dst)
+    int off_kmask;              // K-terminal: bitmask of the terminals, nwd words
 };
 
 // A block's share of the stop test, written at the end of each wave.
@@ -113,7 +115,7 @@ struct NrBucketWideParams {
 // warp's region starts with the mask, which is written with 16-byte stores.
 __host__ __device__ inline size_t nr_wide_warp_shm(int n, int w4)
 {
-    return ((((size_t)4 * w4 + 3 * 32 + 3 * (size_t)n) * 4) + 15) & ~(size_t)15;
+    return ((((size_t)4 * w4 + 3 * 32 + 4 * (size_t)n) * 4) + 15) & ~(size_t)15;
 }
 
 // Where a step's children go.
@@ -138,7 +140,8 @@ struct NrWideView {
     const double *p, *q;
     const int *row;
     const uint32_t *arc;
-    uint32_t *m, *F, *NF, *VIS, *par, *list, *hops;
+    const uint32_t *kmask;           // K-terminal terminals (nullptr: two-terminal)
+    uint32_t *m, *F, *NF, *VIS, *par, *list, *hops, *order;
 };
 
 template <int W4>
@@ -159,12 +162,15 @@ __device__ __forceinline__ NrWideView nr_wide_view(unsigned char *smem, const Nr
     v.par = v.VIS + 32;              // [n] (parent << 16) | edge
     v.list = v.par + g.n;            // [n] frontier nodes
     v.hops = v.list + g.n;           // [n] path edges, dst side first
+    v.order = v.hops + g.n;          // [n] K-terminal: visit order of the search
+    v.kmask = g.nk ? reinterpret_cast<const uint32_t *>(smem + g.off_kmask) : nullptr;
     return v;
 }
 
 // BFS of the warp from src over the arcs whose edge is not down (up_only:
 // up), with the parent rule above; true if dst is reached.  All 32 lanes call it.
-__device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideView &v, bool up_only)
+__device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideView &v, bool up_only,
+                                            int *n_order = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const int n = g.n, nwd = g.nwd, src = g.src, dst = g.dst;
@@ -183,7 +189,11 @@ __device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideVi
         F[src >> 5] = 1u << (src & 31);
     }
     __syncwarp();
-    bool found = (src == dst);
+    // K-terminal (n_order given): search until every terminal is reached, recording the
+    // visit order (src, then each level in ascending node order) in v.order
+    const bool kmode = n_order != nullptr;
+    int no = 0;
+    bool found = kmode ? (g.nk == 0) : (src == dst);
     while (!found) {
         // compact the frontier into list[]
         const uint32_t fw = (lane < nwd) ? F[lane] : 0u;
@@ -197,6 +207,11 @@ __device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideVi
         if (total == 0) break;
         int o = pre - cnt;
         for (uint32_t b = fw; b; b &= b - 1) list[o++] = (uint32_t)(lane * 32 + __ffs(b) - 1);
+        if (kmode) {
+            int oo = no + pre - cnt;
+            for (uint32_t b = fw; b; b &= b - 1) v.order[oo++] = (uint32_t)(lane * 32 + __ffs(b) - 1);
+            no += total;
+        }
         for (int i = lane; i < nwd; i += 32) NF[i] = 0u;
         __syncwarp();
         for (int i = lane; i < total; i += 32) {
@@ -219,9 +234,31 @@ __device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideVi
             any = any || nf != 0u;
         }
         __syncwarp();
-        found = (VIS[dst >> 5] >> (dst & 31)) & 1u;
+        if (kmode) {
+            bool all = true;
+            for (int i = lane; i < nwd; i += 32) all = all && ((VIS[i] & v.kmask[i]) == v.kmask[i]);
+            found = __all_sync(NR_FULL, all);
+        } else {
+            found = (VIS[dst >> 5] >> (dst & 31)) & 1u;
+        }
         if (!__any_sync(NR_FULL, any)) break;
     }
+    if (kmode && found) {
+        // the last level searched: the new frontier, appended in ascending node order
+        const uint32_t fw = (lane < nwd) ? F[lane] : 0u;
+        const int cnt = __popc(fw);
+        int pre = cnt;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int t = __shfl_up_sync(NR_FULL, pre, off);
+            if (lane >= off) pre += t;
+        }
+        const int total = __shfl_sync(NR_FULL, pre, 31);
+        int oo = no + pre - cnt;
+        for (uint32_t b = fw; b; b &= b - 1) v.order[oo++] = (uint32_t)(lane * 32 + __ffs(b) - 1);
+        no += total;
+        __syncwarp();
+    }
+    if (kmode) *n_order = no;
     return found;
 }
 
@@ -282,22 +319,44 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
         __syncwarp();
         return;
     }
-    const bool found = nr_wide_bfs(g, v, false);
+    int no = 0;
+    const bool found = nr_wide_bfs(g, v, false, g.nk ? &no : nullptr);
     int L = 0;
     if (!found) {
         if (lane == 0) A.dead++;
         __syncwarp();
         return;
     }
-    // ---- path: hops[] from dst back to src (L hops) ----
     if (lane == 0) {
-        int w = dst, h = 0;
-        while (w != src && h < n) {
-            const uint32_t pe = par[w];
-            hops[h++] = pe & 0xffffu;
-            w = (int)(pe >> 16);
+        if (g.nk) {
+            // K-terminal: the tree of the terminals' parent paths to src (marked in NF), its
+            // edges in visit order, stored last first as the path hops are (dst side first)
+            uint32_t *mk = v.NF;
+            for (int i = 0; i < g.nwd; ++i) mk[i] = 0u;
+            for (int i = 1; i < no; ++i) {
+                const int t = (int)v.order[i];
+                if (!((v.kmask[t >> 5] >> (t & 31)) & 1u)) continue;
+                for (int x = t; x != src && !((mk[x >> 5] >> (x & 31)) & 1u); x = (int)(par[x] >> 16))
+                    mk[x >> 5] |= 1u << (x & 31);
+            }
+            int cntm = 0;
+            for (int i = 1; i < no; ++i) cntm += (mk[v.order[i] >> 5] >> (v.order[i] & 31)) & 1u;
+            int j = 0;
+            for (int i = 1; i < no; ++i) {
+                const int x = (int)v.order[i];
+                if ((mk[x >> 5] >> (x & 31)) & 1u) hops[cntm - 1 - j++] = par[x] & 0xffffu;
+            }
+            L = cntm;
+        } else {
+            // ---- path: hops[] from dst back to src (L hops) ----
+            int x = dst, h = 0;
+            while (x != src && h < n) {
+                const uint32_t pe = par[x];
+                hops[h++] = pe & 0xffffu;
+                x = (int)(pe >> 16);
+            }
+            L = h;
         }
-        L = h;
     }
     L = __shfl_sync(NR_FULL, L, 0);
     __syncwarp();

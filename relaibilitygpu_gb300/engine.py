@@ -74,7 +74,7 @@ EXPORTS = [
     "nr_initial_mask", "nr_context_create", "nr_context_destroy", "nr_reliability", "nr_reliability_ctx",
     "nr_reliability_batch", "nr_batch_submit", "nr_batch_wait", "nr_format_result", "nr_reliability_noalloc", "nr_autotune",
     "nr_mlp_param_count", "nr_mlp_init", "nr_mlp_grad", "nr_mlp_train", "nr_mlp_infer", "nr_context_set_model",
-    "nr_collect_children", "nr_checkpoint_save", "nr_checkpoint_resume",
+    "nr_collect_children", "nr_checkpoint_save", "nr_checkpoint_resume", "nr_reliability_kterminal",
 ]
 
 _lib_handle: Optional[C.CDLL] = None
@@ -142,6 +142,9 @@ def lib() -> C.CDLL:
                                       C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_uint64), C.POINTER(NrResult)]
     L.nr_collect_children.restype = C.c_int
+    L.nr_reliability_kterminal.argtypes = [C.c_void_p, C.POINTER(NrGraph), C.POINTER(C.c_int32), C.c_int,
+                                           C.c_uint64, C.POINTER(NrOptions), C.POINTER(NrResult)]
+    L.nr_reliability_kterminal.restype = C.c_int
     L.nr_checkpoint_save.argtypes = [C.c_void_p, C.c_char_p]
     L.nr_checkpoint_save.restype = C.c_int
     L.nr_checkpoint_resume.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(NrGraph), C.c_int, C.c_int, C.c_uint64,
@@ -293,6 +296,16 @@ class Context:
 
     def reliability_batch(self, graphs: Sequence[Graph], srcs, dsts, capacity: int = 0, **opts):
         return self.run_batch(Batch(graphs, srcs, dsts), capacity=capacity, **opts)
+
+    def reliability_kterminal(self, g: Graph, terminals, capacity: int = 0, **opts) -> Result:
+        """K-terminal reliability of `terminals` (all joined to terminals[0]), nr_reliability_kterminal."""
+        gv = _GraphView(g)
+        t = np.ascontiguousarray(terminals, dtype=np.int32)
+        o = make_options(**opts)
+        r = NrResult()
+        _check(lib().nr_reliability_kterminal(self.h, C.byref(gv.c), t.ctypes.data_as(C.POINTER(C.c_int32)), len(t),
+                                              int(capacity), C.byref(o), C.byref(r)))
+        return Result.from_raw(r)
 
     def checkpoint_save(self, path: str) -> None:
         """Write the last bucketed whole-GPU run's queue and sums (nr_checkpoint_save)."""

@@ -225,3 +225,74 @@ def test_checkpoint_resume_continues_the_same_run(ctx, engine_lib, tmp_path):
     ctx.reliability(graphs.complete(40, p=0.5), 0, 39, capacity=1 << 16, eps=1e-3)
     with pytest.raises(engine_lib.NrError):
         ctx.checkpoint_save(str(tmp_path / "c.ckpt"))
+
+
+KT_CASES = [
+    ("K7 3 terminals", lambda G: G.complete(7, p_range=(0.5, 0.95), seed=2), [0, 3, 6]),
+    ("grid 3x4 4 terminals", lambda G: G.grid(3, 4, p_range=(0.6, 0.97), seed=4), [0, 5, 11, 3]),
+    ("gnm 9/15 root 2", lambda G: G.gnm(9, 15, p_range=(0.4, 0.95), seed=6), [2, 0, 8, 4, 7]),
+    ("directed 4-cycle", lambda G: G.from_arcs(4, [(0, 1), (1, 2), (2, 3), (3, 0), (0, 2)],
+                                               [0.9, 0.8, 0.7, 0.6, 0.5]), [0, 2, 3]),
+    ("repeated terminals", lambda G: G.grid(3, 3, p_range=(0.6, 0.97), seed=1), [4, 0, 8, 0, 8]),
+]
+
+
+@pytest.mark.parametrize("name,make,term", KT_CASES, ids=[c[0] for c in KT_CASES])
+def test_k_terminal_exact(ctx, oracle, name, make, term):
+    """K-terminal reliability (every terminal joined to terminals[0]) on the whole-GPU engine:
+    the oracle's waves, counts and exact sums, and brute force over the edge states."""
+    from relaibilitygpu_gb300 import graphs
+    g = make(graphs)
+    exact = oracle.brute_k(g, term)
+    o = oracle.run(g, 0, 0, terminals=term)
+    assert o.status == 0
+    r = ctx.reliability_kterminal(g, term, capacity=1 << 20)
+    assert r.engine == "grid" and (r.src, r.dst) == (term[0], term[-1])
+    check(r, o)
+    assert abs(r.R - exact) <= 1e-13
+
+
+KT_WIDE_CASES = [
+    ("K40 p=0.5, 4 terminals", lambda G: G.complete(40, p=0.5), [0, 13, 27, 39], dict(eps=1e-4)),
+    ("grid 6x7 corners", lambda G: G.grid(6, 7, p_range=(0.8, 0.99), seed=2), [0, 6, 35, 41], dict(eps=1e-7)),
+    ("rgg 100/250 to 1e-3, waves", lambda G: G.rgg(100, 250, p_range=(0.9, 0.99), seed=3), [0, 17, 55, 99],
+     dict(target_width=1e-3, bucket_shift=-1)),
+    ("rgg 60/150 to 1e-5, buckets", lambda G: G.rgg(60, 150, p_range=(0.9, 0.99), seed=11), [5, 20, 40, 59],
+     dict(target_width=1e-5, bucket_shift=2, n_buckets=255)),
+    ("gnm 40/52 exhaustive, buckets", lambda G: G.gnm(40, 52, p_range=(0.5, 0.95), seed=9), [0, 9, 19, 29, 39],
+     dict(bucket_shift=1, n_buckets=255, order="maxmass")),
+]
+
+
+@pytest.mark.parametrize("name,make,term,kw", KT_WIDE_CASES, ids=[c[0] for c in KT_WIDE_CASES])
+def test_k_terminal_matches_oracle(ctx, oracle, name, make, term, kw):
+    """Larger K-terminal runs, truncated (eps), target-stopped (waves or buckets) or exhaustive:
+    the same schedule, counts, queue and exact sums as the oracle."""
+    from relaibilitygpu_gb300 import graphs
+    g = make(graphs)
+    okw = {k: v for k, v in kw.items() if k != "order"}
+    o = oracle.run(g, 0, 0, terminals=term, threads=4, max_nodes=20_000_000, **okw)
+    assert o.status in (0, 1)
+    r = ctx.reliability_kterminal(g, term, capacity=1 << 22, **kw)
+    check(r, o)
+    assert (r.queued, r.stop) == (o.queued, o.status)
+
+
+def test_k_terminal_two_terminals_is_the_two_terminal_run(ctx, engine_lib):
+    """terminals [s, t] is the two-terminal problem on the same engine, bit for bit; terminals
+    [s] alone gives R = 1; fork branching and the learned order are refused."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.rgg(60, 150, p_range=(0.9, 0.99), seed=11)
+    for kw in (dict(eps=1e-6), dict(target_width=1e-6, bucket_shift=2, n_buckets=255, order="maxmass")):
+        a = ctx.reliability(g, g.src, g.dst, capacity=1 << 22, **kw)
+        b = ctx.reliability_kterminal(g, [g.src, g.dst], capacity=1 << 22, **kw)
+        for f in ("R", "esp", "nodes", "leaves", "dead_ends", "paths", "iterations", "max_queue_items", "queued"):
+            assert getattr(a, f) == getattr(b, f), (kw, f)
+    one = ctx.reliability_kterminal(g, [7])
+    assert one.R == 1.0 and one.esp == 0.0
+    for bad in (dict(branching="fork"), dict(order="learned")):
+        with pytest.raises(engine_lib.NrError) as e:
+            ctx.reliability_kterminal(g, [0, 5, 9], **bad)
+        assert e.value.status in (-1, -4)
+    with pytest.raises(engine_lib.NrError):
+        ctx.reliability_kterminal(g, [0, 60])

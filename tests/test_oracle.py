@@ -226,3 +226,26 @@ def test_directed_graphs(oracle, tmp_path):
     exact = oracle.brute(dg, 0, 7)
     for rule in ("level", "fifo"):
         assert abs(oracle.run(dg, 0, 7, rule=rule).R - exact) <= 1e-13
+
+
+def test_k_terminal_decomposition(load_golden_graph, oracle):
+    """K-terminal reliability (every terminal joined to terminals[0]) by the same disjoint
+    decomposition over the BFS tree: exact against brute force; two terminals give the
+    two-terminal run exactly; truncated runs bracket it."""
+    from relaibilitygpu_gb300 import graphs
+    g = load_golden_graph("COMP8")
+    two = oracle.run(g, 0, 7)
+    k2 = oracle.run(g, 0, 0, terminals=[0, 7])
+    assert (k2.R, k2.nodes, k2.paths, k2.waves) == (two.R, two.nodes, two.paths, two.waves)
+    cases = [(graphs.complete(7, p_range=(0.5, 0.95), seed=2), [0, 3, 6]),
+             (graphs.grid(3, 4, p_range=(0.6, 0.97), seed=4), [0, 5, 11, 3]),
+             (graphs.gnm(9, 15, p_range=(0.4, 0.95), seed=6), [2, 0, 8, 4, 7]),
+             (graphs.from_arcs(4, [(0, 1), (1, 2), (2, 3), (3, 0), (0, 2)], [0.9, 0.8, 0.7, 0.6, 0.5]), [0, 2, 3])]
+    for gg, term in cases:
+        exact = oracle.brute_k(gg, term)
+        for kw in ({}, dict(bucket_shift=1, n_buckets=64), dict(order="heap")):
+            r = oracle.run(gg, 0, 0, terminals=term, **kw)
+            assert r.status == 0 and abs(r.R - exact) <= 1e-13, (term, kw, r.R, exact)
+        t = oracle.run(gg, 0, 0, terminals=term, target_width=1e-3, bucket_shift=1, n_buckets=64)
+        assert t.R <= exact + 1e-15 <= t.R + t.esp + 1e-15
+    assert abs(oracle.brute_k(graphs.complete(5, p=0.5), [1]) - 1.0) < 1e-15   # one terminal
