@@ -70,6 +70,14 @@ enum {
     NR_ORDER_LEARNED = 3    /* bucket key and branch order from the learned scorer (never mass) */
 };
 
+/* kernel of the warp engine (batches and small truncated runs, n <= 32) */
+enum {
+    NR_SMALL_AUTO = 0,      /* one lane per subproblem where it applies (undirected simple graphs of
+                               <= 16 nodes, path branching, plain order), lane groups elsewhere */
+    NR_SMALL_GROUP = 1      /* a lane group (one lane per node) per subproblem for every instance */
+};
+enum { NR_KERNEL_GROUP = 1, NR_KERNEL_LANE = 2 };
+
 /* branching of a subproblem whose optimistic BFS finds a path */
 enum {
     NR_BRANCH_PATH = 0,     /* one disjoint child per UNKNOWN path edge (main.cu:114-283, the default) */
@@ -98,7 +106,8 @@ typedef struct nr_options {
     int32_t  pages_per_warp;  /* warp engine: queue pages of 32 subproblems per warp when capacity is 0
                                  (0 = 512) */
     int32_t  branching;       /* NR_BRANCH_* */
-    int32_t  reserved[2];
+    int32_t  small_kernel;    /* NR_SMALL_*: the warp engine's kernel */
+    int32_t  reserved[1];
 } nr_options;
 
 typedef struct nr_result {
@@ -130,7 +139,8 @@ typedef struct nr_result {
     uint64_t h2d_bytes;         /* host -> device bytes copied by this call */
     uint64_t d2h_bytes;         /* device -> host bytes copied by this call */
     int32_t  stop;              /* 0 queue empty, 1 target width met, 3 pop budget reached */
-    int32_t  reserved[3];
+    int32_t  kernel;            /* warp engine: NR_KERNEL_GROUP or NR_KERNEL_LANE; 0 otherwise */
+    int32_t  reserved[2];
 } nr_result;
 
 enum { NR_ENGINE_GRID = 1, NR_ENGINE_WARP = 2 };

@@ -24,6 +24,7 @@
 #include "nr_internal.h"
 #include "nr_device.cuh"
 #include "nr_warp.cuh"
+#include "nr_lane.cuh"
 #include "nr_wide.cuh"
 #include "nr_mlp.cuh"
 
@@ -44,6 +45,7 @@ const void *nr_warp_fork_kernel_ptr_g16(int w4);
 const void *nr_warp_fork_kernel_ptr_g32(int w4);
 const void *nr_warp_learn_kernel_ptr_g16(int w4);
 const void *nr_warp_learn_kernel_ptr_g32(int w4);
+const void *nr_lane_kernel_ptr(int w4);
 int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
 
 namespace {
@@ -58,6 +60,7 @@ namespace {
     } while (0)
 
 thread_local char g_err[256];
+thread_local char g_internal[128];      // which device-side check failed, when one says
 
 // keep the failing call and its line for nr_status_string
 void nr_last_cuda_error(cudaError_t e, int line, const char *what)
@@ -284,6 +287,10 @@ private:
 // One host block of a batch call (a contiguous instance range): table bytes,
 // instances per class, and where its tables and descriptors go.
 #define NR_HOST_BLOCKS 64
+// warp-engine kernel classes: lane-group width (8, 16, 32) x mask blocks, then the
+// one-lane-per-subproblem kernel x mask blocks
+#define NR_LANE_CLS0 (3 * NR_MAX_W4)
+#define NR_NCLS (NR_LANE_CLS0 + NR_LANE_MAX_W4)
 struct NrHostBlock {
     size_t bytes;               // tables of the block's instances (16-byte multiples)
     long long last_owner_rel;   // offset in the block of its last structural part, -1 if none
@@ -291,8 +298,8 @@ struct NrHostBlock {
     long long struct_in;        // struct_off of the last structural part before the block
     int last_rows;              // rows mode of the block's last structural part, -1 if none
     int rows_in;                // rows mode of the last structural part before the block
-    int cnt[3 * NR_MAX_W4];     // instances per class
-    int cbase[3 * NR_MAX_W4];   // instances of each class in earlier blocks
+    int cnt[NR_NCLS];           // instances per class
+    int cbase[NR_NCLS];         // instances of each class in earlier blocks
 };
 
 // Host-side per-instance tables of a batch call, kept by the context so their
@@ -310,6 +317,7 @@ struct WarpRunCfg {
     int wave_mode, shift, n_buckets, pages, escalate, warps_per_block;
     int fork = 0;
     int learned = 0;
+    int lane = 1;                 // one lane per subproblem where it applies
     const WarpDump *dump = nullptr;
     double eps, target;
     unsigned long long max_nodes;
@@ -651,7 +659,7 @@ extern "C" const char *nr_status_string(int s)
     case NR_ERR_CUDA: return g_err[0] ? g_err : "CUDA error";
     case NR_ERR_NOMEM: return "out of memory";
     case NR_ERR_TIMEOUT: return "device wait timed out";
-    case NR_ERR_INTERNAL: return "internal consistency check failed";
+    case NR_ERR_INTERNAL: return g_internal[0] ? g_internal : "internal consistency check failed";
     default: return "unknown status";
     }
 }
@@ -1284,6 +1292,7 @@ static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhausti
         w.n_buckets = nb;
     }
     w.fork = (o->branching == NR_BRANCH_FORK);
+    w.lane = (o->small_kernel != NR_SMALL_GROUP);
     w.warps_per_block = (o->warps_per_block >= 1 && o->warps_per_block <= NR_WARP_BLOCK_MAX / 32)
                             ? o->warps_per_block : NR_WARP_BLOCK / 32;
     if (capacity == 0) w.pages = o->pages_per_warp > 0 ? std::min(8192, std::max(4, o->pages_per_warp)) : 512;
@@ -1353,7 +1362,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
                        const int32_t *dsts, const WarpRunCfg &cfg, nr_result *res, PhaseClock &pc,
                        cudaStream_t after = nullptr)
 {
-    constexpr int NCLS = 3 * NR_MAX_W4;      // class = lane-group width x mask blocks
+    constexpr int NCLS = NR_NCLS;
+    const bool lane_ok = cfg.lane && !cfg.fork && !cfg.learned && !cfg.dump;
     int rc0 = slot_ready(sl);
     if (rc0) return rc0;
     NrBatchScratch &S = sl.scratch;          // kept by the slot: no page faults on every call
@@ -1375,6 +1385,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         k.last_owner_rel = -1;
         k.last_rows = -1;
         for (int j = 0; j < NCLS; ++j) k.cnt[j] = 0;
+        int cur_rows = -1;                    // rows mode of the current topology
         for (int i = blk_begin(b), e = blk_begin(b + 1); i < e; ++i) {
             // consecutive instances with the same topology share one structural part
             const bool same = i > 0 && same_topology(&gs[i], &gs[i - 1]);
@@ -1389,10 +1400,16 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
                 rel += sb;
                 desc[i].rows = rows_mode_of(&gs[i]);
                 k.last_rows = desc[i].rows;
+                cur_rows = desc[i].rows;
+            } else if (cur_rows < 0) {
+                cur_rows = rows_mode_of(&gs[i]);   // its owner is in an earlier block
             }
             if (desc[i].w4 > NR_MAX_W4) { too_wide.store(1); S.cls[i] = 0; continue; }
             const int G = group_width(gs[i].n_nodes);
-            S.cls[i] = (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + desc[i].w4 - 1;
+            if (lane_ok && gs[i].n_nodes <= NR_LANE_MAX_N && cur_rows == 1 && desc[i].w4 <= NR_LANE_MAX_W4)
+                S.cls[i] = NR_LANE_CLS0 + desc[i].w4 - 1;
+            else
+                S.cls[i] = (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + desc[i].w4 - 1;
             k.cnt[S.cls[i]]++;
         }
         k.bytes = rel;
@@ -1477,7 +1494,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     // pages per warp: as asked, but no more than the block's shared memory can index
     WarpRunCfg cfgp = cfg;
     while (cfgp.pages > 4 &&
-           nr_warp_shm_bytes(4, NR_MAX_W4, cfgp.n_buckets, cfgp.pages, true) * warps_pb > (size_t)c->smem_optin)
+           std::max(nr_warp_shm_bytes(4, NR_MAX_W4, cfgp.n_buckets, cfgp.pages, true),
+                    nr_lane_shm_bytes(cfgp.n_buckets, cfgp.pages)) * warps_pb > (size_t)c->smem_optin)
         cfgp.pages /= 2;
     const bool learn = cfg.learned || cfg.dump;
     int grids[NCLS] = {0};
@@ -1485,10 +1503,13 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     size_t slab_need = 0;
     for (int j = 0; j < NCLS; ++j) {
         if (!class_count[j]) continue;
-        const int G = 8 << (j / NR_MAX_W4), W4 = j % NR_MAX_W4 + 1;
-        const void *kfn = warp_kernel(G, W4, learn, cfg.fork != 0);
+        const bool lanek = j >= NR_LANE_CLS0;
+        const int G = lanek ? 0 : 8 << (j / NR_MAX_W4);
+        const int W4 = lanek ? j - NR_LANE_CLS0 + 1 : j % NR_MAX_W4 + 1;
+        const void *kfn = lanek ? nr_lane_kernel_ptr(W4) : warp_kernel(G, W4, learn, cfg.fork != 0);
         if (!kfn) return NR_ERR_UNSUPPORTED;
-        const size_t smem = nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn) * warps_pb;
+        const size_t smem = (lanek ? nr_lane_shm_bytes(cfg.n_buckets, cfgp.pages)
+                                   : nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn)) * warps_pb;
         auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
         int bps;
         if (it == c->occupancy.end()) {
@@ -1501,8 +1522,9 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         if (bps < 1) return NR_ERR_UNSUPPORTED;
         grids[j] = std::max(1, std::min(bps * c->sms, (class_count[j] + warps_pb - 1) / warps_pb));
         smems[j] = smem;
+        const size_t row_bytes = lanek ? 4 * (size_t)NR_LANE_ROW_WORDS : 4 * (size_t)G;
         slab_need = std::max(slab_need, (size_t)grids[j] * warps_pb * cfgp.pages * NR_PAGE *
-                                            (16 * (size_t)W4 + 8 + 4 * (size_t)G));
+                                            (16 * (size_t)W4 + 8 + row_bytes));
     }
     rc = ensure(&sl.wslab, &sl.wslab_bytes, slab_need);
     if (rc) return rc;
@@ -1519,7 +1541,9 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     int first_grid = 0;
     for (int j = 0; j < NCLS; ++j) {
         if (!class_count[j]) continue;
-        const int G = 8 << (j / NR_MAX_W4), W4 = j % NR_MAX_W4 + 1;
+        const bool lanek = j >= NR_LANE_CLS0;
+        const int G = lanek ? 0 : 8 << (j / NR_MAX_W4);
+        const int W4 = lanek ? j - NR_LANE_CLS0 + 1 : j % NR_MAX_W4 + 1;
         if (!first_grid) first_grid = grids[j];
         NrWarpParams P;
         P.blob = wb;
@@ -1554,7 +1578,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.dump_stride = cfg.dump ? cfg.dump->stride : 0;
         P.inst_base = base;
         P.fork = cfg.fork;
-        const void *kfn = warp_kernel(G, W4, learn, cfg.fork != 0);
+        const void *kfn = lanek ? nr_lane_kernel_ptr(W4) : warp_kernel(G, W4, learn, cfg.fork != 0);
         void *args[] = {&P};
         NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smems[j]));
         NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[j]), dim3(block), args, smems[j], s));
@@ -1580,20 +1604,31 @@ static int warp_finish(nr_context *c, NrSlot &sl, int base, std::vector<int> *ha
     const nr_graph *gs = sl.gs;
     const NrSmallGraph *desc = sl.scratch.desc.data();
     const NrWarpOut *hout = reinterpret_cast<const NrWarpOut *>(static_cast<unsigned char *>(sl.hbuf) + sl.off_out);
-    std::atomic<int> n_hand(0);
+    std::atomic<int> n_hand(0), n_check(0);
     c->parallel_for(n, 256, [&](int i) {
         nr_result *r = &sl.res[i];
         memset(r, 0, sizeof(*r));
         r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = sl.srcs[i]; r->dst = sl.dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
         if (hout[i].status == 2) { n_hand.fetch_add(1); return; }
+        if (hout[i].status == NR_LANE_STATUS_CHECK) { n_check.fetch_add(1); return; }
         fill_from_warp(hout[i], sl.cfgp, desc[i].w4, r);
+        r->kernel = sl.scratch.cls[i] >= NR_LANE_CLS0 ? NR_KERNEL_LANE : NR_KERNEL_GROUP;
         r->ms = ms;
         r->grid_blocks = sl.first_grid;
         r->block_threads = sl.block;
         r->h2d_bytes = desc[i].blob_bytes + sizeof(NrSmallGraph) + sizeof(int);
         r->d2h_bytes = sizeof(NrWarpOut);
     });
+    if (n_check.load()) {
+        for (int i = 0; i < n; ++i)
+            if (hout[i].status == NR_LANE_STATUS_CHECK) {
+                snprintf(g_internal, sizeof(g_internal), "lane kernel check %llu failed on instance %d",
+                         (unsigned long long)hout[i].max_wave, base + i);
+                break;
+            }
+        return NR_ERR_INTERNAL;
+    }
     if (n_hand.load())
         for (int i = 0; i < n; ++i)
             if (hout[i].status == 2) handover->push_back(base + i);

@@ -28,6 +28,8 @@ STATUS = {
 ORDERS = {"auto": 0, "waves": 1, "maxmass": 2, "learned": 3}
 BRANCHING = {"path": 0, "fork": 1}
 ENGINES = {1: "grid", 2: "warp"}
+KERNELS = {0: "", 1: "group", 2: "lane"}     # the warp engine's kernel
+SMALL_KERNELS = {"auto": 0, "group": 1}
 
 
 class NrError(RuntimeError):
@@ -50,7 +52,8 @@ class NrOptions(C.Structure):
         ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("device", C.c_int32),
         ("blocks_per_sm", C.c_int32), ("warps_per_block", C.c_int32), ("timeout_ms", C.c_double),
         ("verbose", C.c_int32), ("pad0", C.c_int32), ("max_nodes", C.c_uint64),
-        ("pages_per_warp", C.c_int32), ("branching", C.c_int32), ("reserved", C.c_int32 * 2),
+        ("pages_per_warp", C.c_int32), ("branching", C.c_int32), ("small_kernel", C.c_int32),
+        ("reserved", C.c_int32 * 1),
     ]
 
 
@@ -64,7 +67,8 @@ class NrResult(C.Structure):
         ("max_queue_items", C.c_uint64), ("max_queue_mb", C.c_double), ("ms", C.c_double),
         ("time_to_bound_ms", C.c_double), ("engine", C.c_int32), ("grid_blocks", C.c_int32),
         ("block_threads", C.c_int32), ("item_bytes", C.c_int32), ("capacity", C.c_uint64),
-        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("stop", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("stop", C.c_int32), ("kernel", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -187,12 +191,14 @@ class Result:
     h2d_bytes: int
     d2h_bytes: int
     stop: int
+    kernel: str = ""
     _raw: NrResult = dataclasses.field(repr=False, default=None)
 
     @staticmethod
     def from_raw(r: NrResult) -> "Result":
         kw = {f: getattr(r, f) for f, _ in NrResult._fields_ if f != "reserved"}
         kw["engine"] = ENGINES.get(kw["engine"], str(kw["engine"]))
+        kw["kernel"] = KERNELS.get(kw["kernel"], str(kw["kernel"]))
         return Result(_raw=r, **kw)
 
     def block(self) -> str:
@@ -228,7 +234,8 @@ class _GraphView:
 
 def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto", bucket_shift: int = 2,
                  n_buckets: int = 256, device: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0,
-                 timeout_ms: float = 60000.0, max_nodes: int = 0, pages_per_warp: int = 0, branching: str = "path") -> NrOptions:
+                 timeout_ms: float = 60000.0, max_nodes: int = 0, pages_per_warp: int = 0, branching: str = "path",
+                 small_kernel: str = "auto") -> NrOptions:
     o = NrOptions()
     lib().nr_options_default(C.byref(o))
     o.truncation_eps = float(eps)
@@ -243,6 +250,7 @@ def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto
     o.max_nodes = int(max_nodes)
     o.pages_per_warp = int(pages_per_warp)
     o.branching = BRANCHING[branching] if isinstance(branching, str) else int(branching)
+    o.small_kernel = SMALL_KERNELS[small_kernel] if isinstance(small_kernel, str) else int(small_kernel)
     return o
 
 
@@ -253,7 +261,8 @@ def options_dict(o: NrOptions) -> dict:
                 bucket_shift=o.bucket_shift, n_buckets=o.n_buckets, device=o.device,
                 blocks_per_sm=o.blocks_per_sm, warps_per_block=o.warps_per_block, timeout_ms=o.timeout_ms,
                 max_nodes=o.max_nodes, pages_per_warp=o.pages_per_warp,
-                branching={v: k for k, v in BRANCHING.items()}.get(o.branching, "path"))
+                branching={v: k for k, v in BRANCHING.items()}.get(o.branching, "path"),
+                small_kernel={v: k for k, v in SMALL_KERNELS.items()}.get(o.small_kernel, "auto"))
 
 
 def _check(rc: int) -> None:

@@ -1,0 +1,131 @@
+"""One-lane-per-subproblem warp kernel (nr_lane.cuh) against the oracle and the
+lane-group kernel (nr_warp.cuh).
+
+Truncated runs follow the oracle's wave schedule, so every count (waves, widest
+wave, nodes, leaves, dead ends, truncated, queued) is bit-exact and R and ESP
+(exact fixed-point sums) are equal.  Exhaustive batches run page by page; their
+totals do not depend on the order, so they equal the oracle's too."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("R", "esp", "nodes", "leaves", "dead_ends", "truncated", "spilled", "paths", "iterations",
+          "max_queue_items", "queued", "stop")
+
+
+@pytest.fixture(scope="module")
+def ctx(engine_lib):
+    c = engine_lib.Context(0)
+    yield c
+    c.close()
+
+
+def mixed_batch():
+    """Instances the lane kernel takes (undirected simple, n <= 16) and some it leaves to the
+    lane groups (n > 16, directed, parallel edges)."""
+    from relaibilitygpu_gb300 import graphs
+    gs, st = [], []
+    for s in range(48):
+        gs.append(graphs.complete(15, p_range=(0.9, 0.99), seed=s)); st.append((0, 14))
+    for s in range(8):
+        gs.append(graphs.complete(8, p_range=(0.5, 0.95), seed=100 + s)); st.append((0, 7))
+        gs.append(graphs.grid(3, 4, p_range=(0.6, 0.97), seed=200 + s)); st.append((0, 11))
+        gs.append(graphs.grid(4, 4, p_range=(0.7, 0.99), seed=300 + s)); st.append((0, 15))
+        g = graphs.gnm(12, 30, p_range=(0.8, 0.99), seed=400 + s); gs.append(g); st.append((g.src, g.dst))
+        gs.append(graphs.complete(20, p_range=(0.9, 0.99), seed=500 + s)); st.append((0, 19))
+    # edge cases: src == dst, an isolated dst, certain edges (p = 0 and p = 1), two nodes
+    gs.append(graphs.complete(6, p=0.7)); st.append((3, 3))
+    gs.append(graphs.from_edges(5, [(0, 1), (1, 2), (2, 0), (3, 1)], [0.9, 0.8, 0.7, 0.6])); st.append((0, 4))
+    gs.append(graphs.from_edges(6, [(0, 1), (1, 5), (0, 2), (2, 5), (1, 2), (0, 5)], [1.0, 0.9, 0.0, 0.8, 1.0, 0.5]))
+    st.append((0, 5))
+    gs.append(graphs.from_edges(2, [(0, 1)], [0.75])); st.append((0, 1))
+    # parallel edges and a directed graph: lane groups
+    gs.append(graphs.from_edges(4, [(0, 1), (0, 1), (1, 3), (0, 2), (2, 3)], [0.9, 0.8, 0.7, 0.6, 0.95]))
+    st.append((0, 3))
+    gs.append(graphs.from_arcs(6, [(0, 1), (1, 2), (2, 5), (0, 3), (3, 4), (4, 5), (1, 4), (4, 1)],
+                               [0.9, 0.8, 0.7, 0.85, 0.75, 0.95, 0.6, 0.65]))
+    st.append((0, 5))
+    return gs, [s for s, _ in st], [t for _, t in st]
+
+
+def lane_expected(g):
+    """n <= 16 and an undirected simple graph: every edge id on exactly the two arcs u -> v and
+    v -> u, no self-loop, no ordered pair twice."""
+    import numpy as np
+    if g.n_nodes > 16:
+        return False
+    tails = np.repeat(np.arange(g.n_nodes), np.diff(g.row_ptr))
+    arcs = list(zip(tails.tolist(), g.col_idx.tolist(), g.edge_id.tolist()))
+    if len({(u, v) for u, v, _ in arcs}) != len(arcs) or any(u == v for u, v, _ in arcs):
+        return False
+    by_id = {}
+    for u, v, e in arcs:
+        by_id.setdefault(e, []).append((u, v))
+    return len(by_id) == g.n_edges and all(len(a) == 2 and a[0] == a[1][::-1] for a in by_id.values())
+
+
+@pytest.mark.parametrize("target,shift", [(1e-6, -1), (1e-6, 0), (1e-9, 2), (1e-3, 1)])
+def test_lane_kernel_wave_schedule(ctx, oracle, target, shift):
+    """The largest queue of these runs is 27K records (oracle): 64K per warp never spills, and a
+    run that spilled more mass than its target could not meet it and would run on to the empty
+    queue."""
+    gs, srcs, dsts = mixed_batch()
+    nb = 64 << max(shift, 0)
+    lane = ctx.reliability_batch(gs, srcs, dsts, target_width=target, bucket_shift=shift, n_buckets=nb,
+                                 capacity=1 << 16)
+    group = ctx.reliability_batch(gs, srcs, dsts, target_width=target, bucket_shift=shift, n_buckets=nb,
+                                  capacity=1 << 16, small_kernel="group")
+    for i, (g, a, b) in enumerate(zip(gs, lane, group)):
+        assert a.engine == "warp" and b.engine == "warp" and a.spilled == 0
+        assert a.kernel == ("lane" if lane_expected(g) else "group"), i
+        assert b.kernel == "group"
+        for f in FIELDS:
+            assert getattr(a, f) == getattr(b, f), (i, f, getattr(a, f), getattr(b, f))
+        if i % 5 == 0 or i >= len(gs) - 6:
+            o = oracle.run(g, srcs[i], dsts[i], target_width=target, bucket_shift=shift,
+                           n_buckets=nb if shift >= 0 else 1)
+            assert (a.nodes, a.leaves, a.dead_ends, a.iterations, a.max_queue_items, a.queued) == \
+                (o.nodes, o.leaves, o.dead, o.waves, o.max_wave, o.queued), i
+            assert a.R == o.R and a.esp == o.esp, i
+
+
+def test_lane_kernel_exhaustive_pages_and_truncation(ctx, oracle):
+    """Exhaustive batches (page mode) and eps truncation: the oracle's totals and exact sums."""
+    from relaibilitygpu_gb300 import graphs
+    gs = [graphs.complete(8, p_range=(0.5, 0.95), seed=s) for s in range(6)] + \
+         [graphs.grid(3, 4, p_range=(0.6, 0.97), seed=s) for s in range(6)] + \
+         [graphs.complete(9, p=0.5), graphs.complete(9, p_range=(0.5, 0.95), seed=2)]
+    srcs = [0] * len(gs)
+    dsts = [g.n_nodes - 1 for g in gs]
+    for eps in (0.0, 1e-6):
+        res = ctx.reliability_batch(gs, srcs, dsts, eps=eps, capacity=1 << 16)
+        for g, s, t, r in zip(gs, srcs, dsts, res):
+            o = oracle.run(g, s, t, eps=eps)
+            assert r.kernel == "lane" and r.engine == "warp"
+            assert (r.nodes, r.leaves, r.dead_ends, r.truncated, r.paths) == \
+                (o.nodes, o.leaves, o.dead, o.truncated, o.paths)
+            assert r.R == o.R and r.esp == o.esp
+
+
+def test_lane_kernel_spills_budget_and_handover(ctx, oracle):
+    """A full queue spills into ESP (a bracket); a pop budget stops between waves like the
+    lane groups; an exhaustive instance larger than its warp's queue goes to the whole-GPU
+    engine and is still exact."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.complete(9, p_range=(0.6, 0.97), seed=5)
+    exact = oracle.run(g, 0, 8)
+    r = ctx.reliability(g, 0, 8, target_width=1e-14, bucket_shift=1, n_buckets=128, capacity=128)
+    assert r.kernel == "lane" and r.spilled > 0
+    assert r.R <= exact.R + 1e-15 and exact.R <= r.R + r.esp + 1e-12
+    k12 = graphs.complete(12, p_range=(0.7, 0.99), seed=5)
+    opts = dict(target_width=1e-12, bucket_shift=1, n_buckets=128, max_nodes=3000)
+    a = ctx.reliability(k12, 0, 11, **opts)
+    b = ctx.reliability(k12, 0, 11, small_kernel="group", **opts)
+    assert a.stop == 3 and a.kernel == "lane" and b.kernel == "group"
+    for f in FIELDS:
+        assert getattr(a, f) == getattr(b, f), f
+    big = graphs.complete(10, p=0.5)           # 14.9M subproblems: past the warp engine's budget
+    res = ctx.reliability_batch([big, g], [0, 0], [9, 8], capacity=256)
+    o = oracle.run(big, 0, 9, threads=8)
+    assert res[0].engine == "grid" and (res[0].nodes, res[0].paths, res[0].R) == (o.nodes, o.paths, o.R)
+    assert res[1].kernel == "lane" and res[1].R == exact.R and res[1].nodes == exact.nodes
