@@ -531,7 +531,7 @@ static size_t small_inst_layout(const nr_graph *g, int src, int dst, NrSmallGrap
     sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst;
     sg->n_in = g->n_arcs;
     sg->rows = 0;
-    sg->pad0 = 0;
+    sg->off_rows16 = 0;
     size_t off = 0;
     sg->off_p = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
     return off;
@@ -545,6 +545,7 @@ static size_t small_struct_layout(const nr_graph *g, NrSmallGraph *sg, size_t at
     sg->off_eid = (int)off; off = align16(off + sizeof(uint16_t) * G * G);
     sg->off_start = (int)off; off = align16(off + sizeof(int) * (n + 1));
     sg->off_list = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
+    sg->off_rows16 = (int)off; off = align16(off + sizeof(uint32_t) * 8);
     return off - at;
 }
 
@@ -582,6 +583,15 @@ static void small_fill_struct(const nr_graph *g, const NrSmallGraph *sg, unsigne
             list[start[v] + fill[v]++] = ((uint32_t)e << 8) | (uint32_t)u;
             if (eid[u * G + v] == 0xffff) eid[u * G + v] = (uint16_t)e;   // first arc u->v in CSR order
         }
+    // n <= 16: the rows of the lane kernel's root when no edge is certainly down
+    uint32_t *rows16 = reinterpret_cast<uint32_t *>(b + sg->off_rows16);
+    for (int k = 0; k < 8; ++k) rows16[k] = 0u;
+    if (n <= 16)
+        for (int u = 0; u < n; ++u)
+            for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
+                const int v = g->col_idx[j];
+                rows16[v >> 1] |= 1u << (u + ((v & 1) << 4));
+            }
 }
 
 // Both parts in one blob (whole-GPU engine): struct_off == blob_off.

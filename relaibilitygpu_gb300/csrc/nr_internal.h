@@ -48,7 +48,8 @@ struct NrSmallGraph {
     int off_p, off_eid, off_start, off_list, blob_bytes;
     int rows;                   // rows carried in queue records: 0 no (rebuilt from the mask),
                                 // 1 undirected simple graph, 2 directed simple graph
-    int pad0;
+    int off_rows16;             // n <= 16: every node's in-neighbour row (all arcs), 16 bits each,
+                                // two to a word (structural part; 0 when absent)
     long long blob_off;
     long long struct_off;
 };

@@ -16,8 +16,12 @@
 //   * the same parent rule as the lane-group engine (the smallest frontier node
 //     adjacent to a node discovers it), hence the same path and the same
 //     children (workingPad/main.cu:114-283), and the same FP64 products;
-//   * children are pushed one hop index at a time with warp-aggregated page
-//     allocation into the same bucketed page queue as nr_warp_kernel.
+//   * with one bucket (breadth-first waves, exhaustive pages) a warp-wide prefix
+//     over the lanes' child counts places every child of a step with one page
+//     allocation; with mass buckets, children are pushed one hop index at a
+//     time with warp-aggregated allocation per bucket;
+//   * the root's rows come from the topology's table when no edge is certainly
+//     down (the usual case), so an instance starts without a gather.
 // The queue (bucket chains, free-page stack, wave and page modes, spills and
 // hand-over) is the one nr_warp.cuh describes; a popped page is returned to the
 // free stack as soon as its records are loaded, so its step's children can
@@ -136,11 +140,14 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
             // root record from p: p <= 0 down, p >= 1 up, else unknown (main.cu:717-748);
             // 16 edges a word, each half-warp ORs one word together
             uint32_t *rw = reinterpret_cast<uint32_t *>(sl_mask + (size_t)rpg * NR_PAGE * W4);
+            bool down = false;
+#pragma unroll
             for (int e0 = 0; e0 < 64 * W4; e0 += 32) {
                 const int e = e0 + lane;
                 uint32_t v = 0u;
                 if (e < g.e) {
                     const double pe = pt[e];
+                    down = down || pe <= 0.0;
                     v = (uint32_t)((pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN)
                         << ((e & 15) << 1);
                 }
@@ -150,25 +157,43 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                 v |= __shfl_xor_sync(NR_FULL, v, 1);
                 if ((lane & 15) == 0) rw[(e0 >> 4) + (lane >> 4)] = v;
             }
-            // the root's rows: lane u gathers its not-down neighbours (p > 0); rows 2k and
-            // 2k+1 share word k
-            uint32_t r = 0;
-            if (lane < n)
-                for (int j = start[lane]; j < start[lane + 1]; ++j) {
-                    const uint32_t a = list[j];
-                    if (pt[a >> 8] > 0.0) r |= 1u << (a & 31u);
-                }
-            const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
-            if (lane < 2 * RW && !(lane & 1))
-                reinterpret_cast<uint32_t *>(sl_rows + (size_t)rpg * NR_PAGE * (RW / 4))[lane >> 1] = r | (hi << 16);
+            // the root's rows (rows 2k and 2k+1 share word k): the topology's when no edge is
+            // certainly down, else lane u gathers its not-down neighbours (p > 0)
+            uint32_t *rr = reinterpret_cast<uint32_t *>(sl_rows + (size_t)rpg * NR_PAGE * (RW / 4));
+            if (!__any_sync(NR_FULL, down)) {
+                if (lane < RW) rr[lane] = reinterpret_cast<const uint32_t *>(gs + g.off_rows16)[lane];
+            } else {
+                uint32_t r = 0;
+                if (lane < n)
+                    for (int j = start[lane]; j < start[lane + 1]; ++j) {
+                        const uint32_t a = list[j];
+                        if (pt[a >> 8] > 0.0) r |= 1u << (a & 31u);
+                    }
+                const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
+                if (lane < 2 * RW && !(lane & 1)) rr[lane >> 1] = r | (hi << 16);
+            }
         }
         if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
         __syncwarp();
 
         NrLaneAcc &acc = acc_base[lane];
         nr_acc_zero(acc);
-        NrFix qacc = (lane == 0) ? nr_fix_of(1.0) : nr_fix_zero();   // queued mass: this lane's pushes - pops
-        long long qcount = (lane == 0) ? 1 : 0;
+        // queued mass and count.  Mass buckets: this lane's pushes - pops.  One bucket: every
+        // queued record is on bucket 0's chain, so the stop test sums that chain instead
+        // (lane i takes record i of each page) and pushes and pops keep no account.
+        const bool one_bucket = P.shift < 0;
+        NrFix qacc = (lane == 0 && !one_bucket) ? nr_fix_of(1.0) : nr_fix_zero();
+        long long qcount = (lane == 0 && !one_bucket) ? 1 : 0;
+        auto chain_sum = [&]() {
+            if (!one_bucket) return;
+            qacc = nr_fix_zero();
+            qcount = 0;
+            for (int pg = sh.heads[0]; pg >= 0; pg = sh.pnext[pg])
+                if (lane < (int)sh.pcnt[pg]) {
+                    nr_fix_add_mass(qacc, sl_mass[(size_t)pg * NR_PAGE + lane]);
+                    qcount++;
+                }
+        };
         int waves = 0, status = 0;
         unsigned long long max_wave = 0;
         bool abandon = false;
@@ -177,6 +202,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
 
         for (;;) {
             if (P.wave_mode && P.target > 0.0) {     // exact: ESP + queued mass <= target
+                chain_sum();
                 NrFix w = qacc;
                 nr_fix_add(w, acc.et);
                 nr_fix_add(w, acc.es);
@@ -248,8 +274,10 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                 bool active = valid;
                 if (valid) {
                     acc.nodes++;
-                    nr_fix_sub(qacc, nr_fix_of(mass));
-                    qcount--;
+                    if (!one_bucket) {
+                        nr_fix_sub(qacc, nr_fix_of(mass));
+                        qcount--;
+                    }
                     if (use_eps && mass < P.eps) {         // main.cu:537-543
                         acc.trunc++;
                         nr_fix_add_mass(acc.et, mass);
@@ -286,7 +314,9 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                     }
                 }
                 // walk dst -> src: the parent of a node on level l+1 is the smallest node of
-                // frontier l adjacent to it; hop l = (u, x) with its edge id replaces frontier l
+                // frontier l adjacent to it; hop l = (u, x) with its edge id replaces frontier l.
+                // nch = the UNKNOWN hops: the lane's children
+                int nch = 0;
                 if (live && !bad) {
                     int x = dst;
                     for (int l = L - 1; l >= 0; --l) {
@@ -295,6 +325,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                         const uint32_t e = eid[u * es + x];
                         if ((int)e >= g.e) { bad = 4; break; }
                         my_hop[32 * l] = e | ((uint32_t)u << 16) | ((uint32_t)x << 24);
+                        nch += ((nr_pick(wc, (int)e >> 4) >> ((e & 15) << 1)) & 3u) == 3u;
                         x = u;
                     }
                 }
@@ -309,8 +340,102 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                 }
                 // the path src side first: child h = earlier UNKNOWN hops up, hop h down;
                 // FP64 masses in path order, as the lane-group engine and the oracle
-                const int Lmax = (int)__reduce_max_sync(NR_FULL, (unsigned)L);
                 double Pm = mass;
+                if (P.shift < 0) {
+                    // one bucket: every child of the step goes to the same chain, so one warp-wide
+                    // prefix over the lanes' child counts places them all (the head page's free
+                    // slots first, then fresh pages from the free stack)
+                    int pre = nch;
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const int t = __shfl_up_sync(NR_FULL, pre, off);
+                        if (lane >= off) pre += t;
+                    }
+                    const int total = __shfl_sync(NR_FULL, pre, 31);
+                    pre -= nch;
+                    int hA = -1, cA = 0, nA = 0, npg = 0;
+                    const int top0 = top;
+                    if (lane == 0 && total > 0) {
+                        const int hd = sh.heads[0];
+                        const int c = (hd >= 0) ? sh.pcnt[hd] : NR_PAGE;
+                        nA = min(total, NR_PAGE - c);
+                        if (nA > 0) { hA = hd; cA = c; sh.pcnt[hd] = (unsigned char)(c + nA); }
+                        const int rest = total - nA;
+                        npg = min((rest + NR_PAGE - 1) / NR_PAGE, top0);
+                        int prev = hd;
+                        for (int i = 0; i < npg; ++i) {       // fresh pages, the last one the new head
+                            const int pgi = sh.freel[top0 - 1 - i];
+                            sh.pnext[pgi] = (short)prev;
+                            sh.pcnt[pgi] = (unsigned char)min(NR_PAGE, rest - NR_PAGE * i);
+                            prev = pgi;
+                        }
+                        if (npg > 0) {
+                            sh.heads[0] = (short)prev;
+                            sh.bitmap[0] |= 1u;
+                        }
+                    }
+                    hA = __shfl_sync(NR_FULL, hA, 0);
+                    cA = __shfl_sync(NR_FULL, cA, 0);
+                    nA = __shfl_sync(NR_FULL, nA, 0);
+                    npg = __shfl_sync(NR_FULL, npg, 0);
+                    top = top0 - npg;
+                    __syncwarp();
+                    int q = pre;                            // this lane's next child index
+                    for (int h = 0; h < L; ++h) {
+                        const uint32_t hp = my_hop[32 * h];
+                        const int e = (int)(hp & 0xffffu);
+                        const int ew = e >> 4;
+                        const uint32_t wv = nr_pick(wc, ew);
+                        if (((wv >> ((e & 15) << 1)) & 3u) != 3u) continue;
+                        const int cu = (int)((hp >> 16) & 0xffu), cv = (int)(hp >> 24);
+                        const double pe = pt[e];
+                        const double cm = __dmul_rn(Pm, __dsub_rn(1.0, pe));
+                        Pm = __dmul_rn(Pm, pe);
+                        int s = -1;
+                        if (q < nA) {
+                            s = hA * NR_PAGE + cA + q;
+                        } else {
+                            const int r = q - nA;
+                            if ((r >> 5) < npg) s = sh.freel[top0 - 1 - (r >> 5)] * NR_PAGE + (r & 31);
+                        }
+                        ++q;
+                        if (s >= 0) {
+                            // the parent's words, then the one word that differs (this thread's
+                            // later store to the same address wins)
+                            uint4 *d = sl_mask + (size_t)s * W4;
+#pragma unroll
+                            for (int kk = 0; kk < W4; ++kk)
+                                d[kk] = make_uint4(wc[4 * kk], wc[4 * kk + 1], wc[4 * kk + 2], wc[4 * kk + 3]);
+                            reinterpret_cast<uint32_t *>(d)[ew] = wv & ~(3u << ((e & 15) << 1));
+                            // the child's rows: the parent's less the down edge cu - cv
+                            const int wu = cu >> 1, wv2 = cv >> 1;
+                            const uint32_t bu = 1u << (cv + ((cu & 1) << 4));
+                            const uint32_t bv = 1u << (cu + ((cv & 1) << 4));
+                            uint4 *dr = sl_rows + (size_t)s * (RW / 4);
+#pragma unroll
+                            for (int kk = 0; kk < RW / 4; ++kk)
+                                dr[kk] = make_uint4(rw[4 * kk], rw[4 * kk + 1], rw[4 * kk + 2], rw[4 * kk + 3]);
+                            uint32_t *drw = reinterpret_cast<uint32_t *>(dr);
+                            if (wu == wv2) {
+                                drw[wu] = my_rows[32 * wu] & ~(bu | bv);
+                            } else {
+                                drw[wu] = my_rows[32 * wu] & ~bu;
+                                drw[wv2] = my_rows[32 * wv2] & ~bv;
+                            }
+                            sl_mass[s] = cm;
+                        } else if (P.escalate) {
+                            abandon = true;
+                        } else {                          // queue full: mass to ESP (main.cu:245-252)
+                            acc.spilled++;
+                            nr_fix_add_mass(acc.es, cm);
+                        }
+#pragma unroll
+                        for (int kk = 0; kk < NW; ++kk)   // later children see hop h up
+                            if (kk == ew) wc[kk] &= ~(2u << ((e & 15) << 1));
+                    }
+                    abandon = __any_sync(NR_FULL, abandon);
+                }
+                const int Lmax = (P.shift < 0) ? 0 : (int)__reduce_max_sync(NR_FULL, (unsigned)L);
                 for (int h = 0; h < Lmax; ++h) {
                     bool has_child = false;
                     double cm = 0.0;
@@ -420,6 +545,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
             if (wave_items > max_wave) max_wave = wave_items;
         }
         const long long t_stop = nr_globaltimer() - t0;
+        chain_sum();                                // one bucket: what is left queued
 
         const NrFix R = nr_fix_warp_sum(acc.R), et = nr_fix_warp_sum(acc.et), es_ = nr_fix_warp_sum(acc.es);
         const NrFix qm = nr_fix_warp_sum(qacc);

@@ -124,8 +124,8 @@ def test_lane_kernel_spills_budget_and_handover(ctx, oracle):
     assert a.stop == 3 and a.kernel == "lane" and b.kernel == "group"
     for f in FIELDS:
         assert getattr(a, f) == getattr(b, f), f
-    big = graphs.complete(10, p=0.5)           # 14.9M subproblems: past the warp engine's budget
-    res = ctx.reliability_batch([big, g], [0, 0], [9, 8], capacity=256)
+    big = graphs.complete(10, p=0.5)           # 14.9M subproblems: past the warp engine's 2^21 budget
+    res = ctx.reliability_batch([big, g], [0, 0], [9, 8], capacity=1 << 12)
     o = oracle.run(big, 0, 9, threads=8)
     assert res[0].engine == "grid" and (res[0].nodes, res[0].paths, res[0].R) == (o.nodes, o.paths, o.R)
     assert res[1].kernel == "lane" and res[1].R == exact.R and res[1].nodes == exact.nodes
