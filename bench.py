@@ -96,7 +96,7 @@ def workload(name: str):
 
 # DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu capture of the same
 # workload (the launch summaries are kept under profiles/).
-TRAFFIC = {"k15batch": 5.024e6, "k10": 136.8e6}
+TRAFFIC = {"k15batch": 4.078e6, "k10": 136.8e6}
 
 
 def item_bytes(n_edges: int) -> int:
@@ -260,10 +260,11 @@ def main():
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     tuned = None
     if w["kind"] == "batch" and args.no_autotune:
-        tuned = dict(nr.options_dict(nr.make_options(**w["opts"])), bucket_shift=0, n_buckets=64,
-                     warps_per_block=2, pages_per_warp=64)
+        # the autotuner's choice on GB300 (breadth-first waves, 8 warps a block, 64 pages a warp)
+        tuned = dict(nr.options_dict(nr.make_options(**w["opts"])), bucket_shift=-1, n_buckets=64,
+                     warps_per_block=8, pages_per_warp=64)
         w["opts"] = tuned
-        w["oracle"] = dict(bucket_shift=0, n_buckets=64, target_width=tuned["target_width"])
+        w["oracle"] = dict(bucket_shift=-1, n_buckets=1, target_width=tuned["target_width"])
     elif w["kind"] == "batch":
         # autotuner (nr_autotune): bucket resolution, pages per warp, warps per block
         tuned, tuned_ms = nr.autotune(ctx, batch, capacity=w["capacity"], **w["opts"])
@@ -312,14 +313,21 @@ def main():
         batches = [batch, nr.Batch(w["graphs"], w["srcs"], w["dsts"])]
         fs = torch.cuda.Stream(device=f"cuda:{local}")
         # 192 MB (1.5x the 129 MB L2) evicts the previous steps' lines; a bigger write would only
-        # take HBM time from the step running beside it
-        flush_e2e = flush[: 192 * 1024 * 1024 // 4]
+        # take HBM time from the step running beside it.  The write is a cudaMemsetAsync on the
+        # flush stream, issued through the CUDA runtime that libnr.so links (a few microseconds of
+        # host time, where a torch fill under a stream context costs tens)
+        import ctypes
+        cudart = ctypes.CDLL("libcudart.so.13")
+        cudart.cudaMemsetAsync.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
+        cudart.cudaMemsetAsync.restype = ctypes.c_int
+        flush_args = (ctypes.c_void_p(flush.data_ptr()), 1, ctypes.c_size_t(192 * 1024 * 1024),
+                      ctypes.c_void_p(fs.cuda_stream))
 
         def pipelined(steps):
             pending = None
             for k in range(steps):
-                with torch.cuda.stream(fs):
-                    flush_e2e.fill_(1.0)
+                if cudart.cudaMemsetAsync(*flush_args) != 0:
+                    raise RuntimeError("cudaMemsetAsync (L2 flush) failed")
                 tk = ctx.submit(batches[k % 2], capacity=w["capacity"], after_stream=fs.cuda_stream, **w["opts"])
                 if pending is not None:
                     ctx.wait(pending)
@@ -345,7 +353,8 @@ def main():
     stats = {"R": r0.R, "R_plus_esp": r0.R_plus_esp, "esp": r0.esp, "paths": int(r0.paths), "nodes": int(r0.nodes),
              "iterations": int(r0.iterations), "queued": int(r0.queued), "spilled": int(r0.spilled),
              "stop": {0: "queue empty", 1: "target width met", 3: "node budget"}.get(int(r0.stop), int(r0.stop)),
-             "engine": nr.engine.ENGINES.get(r0.engine, r0.engine), "nodes_per_step": nodes // args.steps}
+             "engine": nr.engine.ENGINES.get(r0.engine, r0.engine),
+             "kernel": nr.engine.KERNELS.get(r0.kernel, r0.kernel), "nodes_per_step": nodes // args.steps}
 
     # single-instance time-to-bound (latency): plain max-mass order vs the learned order
     ttb = None
@@ -423,7 +432,7 @@ def main():
         "warmup": max(3, args.warmup), "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": w["name"], "l2": "flushed (512 MB write) before every step",
-                   "parallelism": f"replicas x{world}", "engine": stats["engine"],
+                   "parallelism": f"replicas x{world}", "engine": stats["engine"], "kernel": stats["kernel"],
                    "grid": int(r0.grid_blocks), "block": int(r0.block_threads),
                    "autotuned": None if tuned is None else {k: tuned[k] for k in
                                                              ("bucket_shift", "n_buckets", "warps_per_block",

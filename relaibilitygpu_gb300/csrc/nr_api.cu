@@ -170,7 +170,13 @@ double nr_fix_to_double_host(const NrFix &a)
         ++mant;
         if (mant >> 53) { mant >>= 1; ++top; }
     }
-    return std::ldexp((double)mant, top - 52 - NR_FIX_FRAC);
+    // mant in [2^52, 2^53): the value is mant * 2^(top - 52 - NR_FIX_FRAC), a normal double
+    // (top <= 191 and NR_FIX_FRAC = 190 keep the exponent well inside the normal range)
+    const unsigned long long bits = ((unsigned long long)(top - NR_FIX_FRAC + 1023) << 52) |
+                                    (mant & 0xfffffffffffffull);
+    double d;
+    memcpy(&d, &bits, sizeof d);
+    return d;
 }
 
 NrFix nr_fix_from_double_host(double m) { return nr_fix_of(m); }
@@ -199,7 +205,9 @@ public:
         {
             std::lock_guard<std::mutex> l(mu_);
             quit_ = true;
-            gen_.fetch_add(1, std::memory_order_release);
+            // a new job number with every slot taken: spinning workers stop and see quit_
+            const unsigned long long job = (state_.load(std::memory_order_relaxed) >> 32) + 1;
+            state_.store((job << 32) | 0xffffffffull, std::memory_order_release);
         }
         cv_.notify_all();
         for (auto &t : th_) t.join();
@@ -215,14 +223,16 @@ public:
             return;
         }
         {
+            // publish the job: its fields, then a new job number with no helper slot claimed
             std::lock_guard<std::mutex> l(mu_);
-            fn_ = &fn;
-            n_ = n;
-            grain_ = std::max(1, grain);
-            helpers_ = helpers;
+            fn_.store(&fn, std::memory_order_relaxed);
+            n_.store(n, std::memory_order_relaxed);
+            grain_.store(std::max(1, grain), std::memory_order_relaxed);
+            helpers_.store(helpers, std::memory_order_relaxed);
             next_.store(0, std::memory_order_relaxed);
             busy_.store(helpers, std::memory_order_relaxed);
-            gen_.fetch_add(1, std::memory_order_release);
+            const unsigned long long job = (state_.load(std::memory_order_relaxed) >> 32) + 1;
+            state_.store(job << 32, std::memory_order_release);
         }
         cv_.notify_all();
         work();
@@ -235,38 +245,57 @@ public:
             }
             std::this_thread::yield();
         }
-        std::lock_guard<std::mutex> l(mu_);
-        fn_ = nullptr;
+        fn_.store(nullptr, std::memory_order_relaxed);
     }
 
 private:
     static constexpr std::chrono::microseconds kSpin{NR_POOL_SPIN_US};
     void work()
     {
+        const int n = n_.load(std::memory_order_relaxed), grain = grain_.load(std::memory_order_relaxed);
+        const std::function<void(int)> &fn = *fn_.load(std::memory_order_relaxed);
         for (;;) {
-            const int b = next_.fetch_add(grain_);
-            if (b >= n_) break;
-            const int e = std::min(n_, b + grain_);
-            for (int i = b; i < e; ++i) (*fn_)(i);
+            const int b = next_.fetch_add(grain);
+            if (b >= n) break;
+            const int e = std::min(n, b + grain);
+            for (int i = b; i < e; ++i) fn(i);
         }
     }
-    void loop(int id)
+    // A worker joins a job by claiming one of its helper slots with a compare-and-swap
+    // on state_ (job number << 32 | slots claimed): no lock on the way in, and a claim
+    // can only succeed for the job it read, whose fields stay put until every claimed
+    // helper has finished.  The mutex is taken only to sleep.
+    void loop(int)
     {
-        unsigned long long seen = 0;
+        unsigned long long seen = 0;           // last job this worker has dealt with
         for (;;) {
-            const auto t0 = std::chrono::steady_clock::now();
-            while (gen_.load(std::memory_order_acquire) == seen &&
-                   std::chrono::steady_clock::now() - t0 < kSpin)
-                std::this_thread::yield();
-            int helpers;
-            {
-                std::unique_lock<std::mutex> l(mu_);
-                cv_.wait(l, [&] { return gen_.load(std::memory_order_relaxed) != seen; });
-                if (quit_) return;
-                seen = gen_.load(std::memory_order_relaxed);
-                helpers = helpers_;
+            unsigned long long s = state_.load(std::memory_order_acquire);
+            if ((s >> 32) == seen) {
+                const auto t0 = std::chrono::steady_clock::now();
+                while (((s = state_.load(std::memory_order_acquire)) >> 32) == seen &&
+                       std::chrono::steady_clock::now() - t0 < kSpin)
+                    std::this_thread::yield();
+                if ((s >> 32) == seen) {
+                    std::unique_lock<std::mutex> l(mu_);
+                    cv_.wait(l, [&] { return quit_ || (state_.load(std::memory_order_relaxed) >> 32) != seen; });
+                    if (quit_) return;
+                    continue;
+                }
             }
-            if (id >= helpers) continue;       // not a helper of this job
+            if (quit_.load(std::memory_order_acquire)) return;
+            bool joined = false;
+            while ((s >> 32) != seen) {
+                if ((unsigned)(s & 0xffffffffull) >= (unsigned)helpers_.load(std::memory_order_relaxed)) {
+                    seen = s >> 32;
+                    break;
+                }
+                if (state_.compare_exchange_weak(s, s + 1, std::memory_order_acq_rel, std::memory_order_acquire)) {
+                    seen = s >> 32;
+                    joined = true;
+                    break;
+                }
+            }
+            if (!joined) continue;
             work();
             if (busy_.fetch_sub(1, std::memory_order_acq_rel) == 1) {
                 std::lock_guard<std::mutex> l(mu_);
@@ -277,11 +306,13 @@ private:
     std::vector<std::thread> th_;
     std::mutex mu_;
     std::condition_variable cv_, done_;
-    const std::function<void(int)> *fn_ = nullptr;
-    int n_ = 0, grain_ = 1, helpers_ = 0;
+    // the job: written by the caller before it publishes a job number in state_; a worker
+    // reads them after its claim on state_ (an acquire) succeeded
+    std::atomic<const std::function<void(int)> *> fn_{nullptr};
+    std::atomic<int> n_{0}, grain_{1}, helpers_{0};
     std::atomic<int> next_{0}, busy_{0};
-    std::atomic<unsigned long long> gen_{0};
-    bool quit_ = false;
+    std::atomic<unsigned long long> state_{0};   // job number << 32 | helper slots claimed
+    std::atomic<bool> quit_{false};
 };
 
 // One host block of a batch call (a contiguous instance range): table bytes,
@@ -417,7 +448,9 @@ struct nr_context {
             pool.reset(new NrPool(hw - 1));
         }
         const int threads = std::min(pool->size(), (n + min_per_thread - 1) / min_per_thread);
-        pool->run(n, threads - 1, std::max(1, std::min(32, n / (8 * threads))), fn);
+        // about four grabs per thread: enough to even out uneven items, few enough that the
+        // shared counter is not the cost
+        pool->run(n, threads - 1, std::max(1, std::min(256, n / (4 * threads))), fn);
     }
 };
 
@@ -554,13 +587,10 @@ static bool small_fill_inst(const nr_graph *g, const NrSmallGraph *sg, unsigned 
 {
     const int E = g->n_edges;
     double *p = reinterpret_cast<double *>(b + sg->off_p);
-    bool ok = true;
-    for (int e = 0; e < E; ++e) {
-        const double x = g->edge_p[e];
-        ok = ok && !std::isnan(x);
-        p[e] = x;
-    }
-    return ok;
+    memcpy(p, g->edge_p, sizeof(double) * E);
+    int nan = 0;
+    for (int e = 0; e < E; ++e) nan |= p[e] != p[e];     // no early exit: the loop vectorizes
+    return nan == 0;
 }
 
 static void small_fill_struct(const nr_graph *g, const NrSmallGraph *sg, unsigned char *b)

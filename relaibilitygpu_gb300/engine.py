@@ -277,6 +277,7 @@ class Context:
         h = C.c_void_p()
         _check(lib().nr_context_create(int(device), C.byref(h)))
         self.h = h
+        self._opt_cache: dict = {}
 
     def close(self) -> None:
         if self.h:
@@ -338,12 +339,22 @@ class Context:
         `torch.cuda.current_stream().cuda_stream`): the upload starts after the
         work already queued there.  The batch's results are valid after
         wait(ticket); do not resubmit the same Batch object before that."""
-        o = make_options(**opts)
+        o = self._options(opts)
         t = C.c_int64()
-        _check(lib().nr_batch_submit(self.h, batch.n, batch.arr, batch.s.ctypes.data_as(C.POINTER(C.c_int32)),
-                                     batch.d.ctypes.data_as(C.POINTER(C.c_int32)), int(capacity), C.byref(o),
+        _check(lib().nr_batch_submit(self.h, batch.n, batch.arr, batch.sp, batch.dp, int(capacity), C.byref(o),
                                      batch.res, C.c_void_p(after_stream or None), C.byref(t)))
         return t.value
+
+    def _options(self, opts: dict) -> NrOptions:
+        """make_options(**opts), kept per keyword set: a stream of calls with the same options
+        (the batch loop of a service) does not rebuild the struct each time."""
+        key = tuple(sorted(opts.items()))
+        o = self._opt_cache.get(key)
+        if o is None:
+            if len(self._opt_cache) > 64:
+                self._opt_cache.clear()
+            o = self._opt_cache[key] = make_options(**opts)
+        return o
 
     def wait(self, ticket: int) -> None:
         """Finish a submitted batch (nr_batch_wait): its Batch.res is filled."""
@@ -351,9 +362,8 @@ class Context:
 
     def run_batch(self, batch: "Batch", capacity: int = 0, raw: bool = False, **opts):
         """Solve a prepared batch (host arrays marshalled once) with nr_reliability_batch."""
-        o = make_options(**opts)
-        _check(lib().nr_reliability_batch(self.h, batch.n, batch.arr, batch.s.ctypes.data_as(C.POINTER(C.c_int32)),
-                                          batch.d.ctypes.data_as(C.POINTER(C.c_int32)), int(capacity), C.byref(o),
+        o = self._options(opts)
+        _check(lib().nr_reliability_batch(self.h, batch.n, batch.arr, batch.sp, batch.dp, int(capacity), C.byref(o),
                                           batch.res))
         if raw:
             return batch.res
@@ -381,6 +391,8 @@ class Batch:
         self.arr = (NrGraph * self.n)(*[v.c for v in self.views])
         self.s = np.ascontiguousarray(srcs, dtype=np.int32)
         self.d = np.ascontiguousarray(dsts, dtype=np.int32)
+        self.sp = self.s.ctypes.data_as(C.POINTER(C.c_int32))     # converted once: each is ~5 us a call
+        self.dp = self.d.ctypes.data_as(C.POINTER(C.c_int32))
         self.res = (NrResult * self.n)()
 
 
