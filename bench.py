@@ -260,9 +260,9 @@ def main():
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     tuned = None
     if w["kind"] == "batch" and args.no_autotune:
-        # the autotuner's choice on GB300 (breadth-first waves, 8 warps a block, 64 pages a warp)
+        # the autotuner's choice on GB300 (breadth-first waves, 2 warps a block, 64 pages a warp)
         tuned = dict(nr.options_dict(nr.make_options(**w["opts"])), bucket_shift=-1, n_buckets=64,
-                     warps_per_block=8, pages_per_warp=64)
+                     warps_per_block=2, pages_per_warp=64)
         w["opts"] = tuned
         w["oracle"] = dict(bucket_shift=-1, n_buckets=1, target_width=tuned["target_width"])
     elif w["kind"] == "batch":

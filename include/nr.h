@@ -74,9 +74,11 @@ enum {
 enum {
     NR_SMALL_AUTO = 0,      /* one lane per subproblem where it applies (undirected simple graphs of
                                <= 16 nodes, path branching, plain order), lane groups elsewhere */
-    NR_SMALL_GROUP = 1      /* a lane group (one lane per node) per subproblem for every instance */
+    NR_SMALL_GROUP = 1,     /* a lane group (one lane per node) per subproblem for every instance */
+    NR_SMALL_LANE1 = 2      /* where one lane per subproblem applies, one instance per warp (with one
+                               bucket the default gives a warp two instances, interleaving their steps) */
 };
-enum { NR_KERNEL_GROUP = 1, NR_KERNEL_LANE = 2 };
+enum { NR_KERNEL_GROUP = 1, NR_KERNEL_LANE = 2, NR_KERNEL_LANE2 = 3 };
 
 /* branching of a subproblem whose optimistic BFS finds a path */
 enum {

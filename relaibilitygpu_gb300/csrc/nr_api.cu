@@ -24,7 +24,7 @@
 #include "nr_internal.h"
 #include "nr_device.cuh"
 #include "nr_warp.cuh"
-#include "nr_lane.cuh"
+#include "nr_lane2.cuh"
 #include "nr_wide.cuh"
 #include "nr_mlp.cuh"
 
@@ -46,6 +46,7 @@ const void *nr_warp_fork_kernel_ptr_g32(int w4);
 const void *nr_warp_learn_kernel_ptr_g16(int w4);
 const void *nr_warp_learn_kernel_ptr_g32(int w4);
 const void *nr_lane_kernel_ptr(int w4);
+const void *nr_lane2_kernel_ptr(int w4);
 int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
 
 namespace {
@@ -349,6 +350,7 @@ struct WarpRunCfg {
     int fork = 0;
     int learned = 0;
     int lane = 1;                 // one lane per subproblem where it applies
+    int lane2 = 1;                // ... with two instances per warp in breadth-first waves
     const WarpDump *dump = nullptr;
     double eps, target;
     unsigned long long max_nodes;
@@ -1333,6 +1335,7 @@ static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhausti
     }
     w.fork = (o->branching == NR_BRANCH_FORK);
     w.lane = (o->small_kernel != NR_SMALL_GROUP);
+    w.lane2 = (o->small_kernel == NR_SMALL_AUTO) && w.wave_mode && w.shift < 0;
     w.warps_per_block = (o->warps_per_block >= 1 && o->warps_per_block <= NR_WARP_BLOCK_MAX / 32)
                             ? o->warps_per_block : NR_WARP_BLOCK / 32;
     if (capacity == 0) w.pages = o->pages_per_warp > 0 ? std::min(8192, std::max(4, o->pages_per_warp)) : 512;
@@ -1534,8 +1537,9 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     // pages per warp: as asked, but no more than the block's shared memory can index
     WarpRunCfg cfgp = cfg;
     while (cfgp.pages > 4 &&
-           std::max(nr_warp_shm_bytes(4, NR_MAX_W4, cfgp.n_buckets, cfgp.pages, true),
-                    nr_lane_shm_bytes(cfgp.n_buckets, cfgp.pages)) * warps_pb > (size_t)c->smem_optin)
+           std::max(std::max(nr_warp_shm_bytes(4, NR_MAX_W4, cfgp.n_buckets, cfgp.pages, true),
+                             nr_lane_shm_bytes(cfgp.n_buckets, cfgp.pages)),
+                    nr_lane2_shm_bytes(cfgp.pages)) * warps_pb > (size_t)c->smem_optin)
         cfgp.pages /= 2;
     const bool learn = cfg.learned || cfg.dump;
     int grids[NCLS] = {0};
@@ -1546,10 +1550,13 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         const bool lanek = j >= NR_LANE_CLS0;
         const int G = lanek ? 0 : 8 << (j / NR_MAX_W4);
         const int W4 = lanek ? j - NR_LANE_CLS0 + 1 : j % NR_MAX_W4 + 1;
-        const void *kfn = lanek ? nr_lane_kernel_ptr(W4) : warp_kernel(G, W4, learn, cfg.fork != 0);
+        const bool two = lanek && cfg.lane2;
+        const void *kfn = lanek ? (two ? nr_lane2_kernel_ptr(W4) : nr_lane_kernel_ptr(W4))
+                                : warp_kernel(G, W4, learn, cfg.fork != 0);
         if (!kfn) return NR_ERR_UNSUPPORTED;
-        const size_t smem = (lanek ? nr_lane_shm_bytes(cfg.n_buckets, cfgp.pages)
-                                   : nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn)) * warps_pb;
+        const size_t smem = (two ? nr_lane2_shm_bytes(cfgp.pages)
+                                 : lanek ? nr_lane_shm_bytes(cfg.n_buckets, cfgp.pages)
+                                         : nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn)) * warps_pb;
         auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
         int bps;
         if (it == c->occupancy.end()) {
@@ -1560,7 +1567,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
             bps = it->second;
         }
         if (bps < 1) return NR_ERR_UNSUPPORTED;
-        grids[j] = std::max(1, std::min(bps * c->sms, (class_count[j] + warps_pb - 1) / warps_pb));
+        const int per_block = warps_pb * (two ? 2 : 1);      // instances a block starts with
+        grids[j] = std::max(1, std::min(bps * c->sms, (class_count[j] + per_block - 1) / per_block));
         smems[j] = smem;
         const size_t row_bytes = lanek ? 4 * (size_t)NR_LANE_ROW_WORDS : 4 * (size_t)G;
         slab_need = std::max(slab_need, (size_t)grids[j] * warps_pb * cfgp.pages * NR_PAGE *
@@ -1618,7 +1626,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.dump_stride = cfg.dump ? cfg.dump->stride : 0;
         P.inst_base = base;
         P.fork = cfg.fork;
-        const void *kfn = lanek ? nr_lane_kernel_ptr(W4) : warp_kernel(G, W4, learn, cfg.fork != 0);
+        const void *kfn = lanek ? (cfg.lane2 ? nr_lane2_kernel_ptr(W4) : nr_lane_kernel_ptr(W4))
+                                : warp_kernel(G, W4, learn, cfg.fork != 0);
         void *args[] = {&P};
         NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smems[j]));
         NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[j]), dim3(block), args, smems[j], s));
@@ -1653,7 +1662,8 @@ static int warp_finish(nr_context *c, NrSlot &sl, int base, std::vector<int> *ha
         if (hout[i].status == 2) { n_hand.fetch_add(1); return; }
         if (hout[i].status == NR_LANE_STATUS_CHECK) { n_check.fetch_add(1); return; }
         fill_from_warp(hout[i], sl.cfgp, desc[i].w4, r);
-        r->kernel = sl.scratch.cls[i] >= NR_LANE_CLS0 ? NR_KERNEL_LANE : NR_KERNEL_GROUP;
+        r->kernel = sl.scratch.cls[i] < NR_LANE_CLS0 ? NR_KERNEL_GROUP
+                    : sl.cfgp.lane2 ? NR_KERNEL_LANE2 : NR_KERNEL_LANE;
         r->ms = ms;
         r->grid_blocks = sl.first_grid;
         r->block_threads = sl.block;

@@ -1,0 +1,429 @@
+// nr_lane2.cuh -- the lane kernel with two instances per warp, for breadth-first waves
+// (one bucket) on undirected simple graphs of up to 16 nodes.
+//
+// nr_lane_kernel gives a warp one instance, and the first waves of an instance hold
+// 1, 1, 2, 4, ... records: most lanes idle while every step pays its full fixed work,
+// and a batch of a few thousand instances ends with a tail of warps on their last
+// instance.  Here a warp carries two instance slots.  A step takes the next page of
+// each slot's current wave when both fit in 32 lanes (else one of them, alternating):
+// lanes 0..cA-1 expand slot 0's records, the next cB lanes slot 1's.  Each slot keeps
+// its own wave structure -- its current wave's page chain, the chain its children go
+// to, its own stop test between its waves -- so each instance follows exactly the
+// schedule of the one-slot kernel and of the oracle; only the interleaving of the two
+// instances' steps is new.  The slots share the warp's page pool, each limited to half
+// of it, so a new instance always finds a page for its root.
+#pragma once
+
+#include "nr_lane.cuh"
+
+// warp-uniform state of one instance slot, in shared memory (written by lane 0)
+struct NrLaneSlot {
+    long long t0;
+    long long blob_off, struct_off;   // the instance's tables in P.blob
+    int ii;                 // instance (index into the class); -1 empty, -2 no instance left
+    int n, src, dst, ge;
+    int off_p, off_eid, off_rows16, off_start, off_list;
+    int head;               // the chain the current wave's children go to (the next wave)
+    int cur;                // next page of the current wave; -1: the wave is done
+    int waves, used;        // waves started; pages held (current wave + next wave)
+    unsigned wave_items, max_wave;
+    int pad[2];
+};
+
+__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages)
+{
+    size_t b = 2 * 32 * sizeof(NrLaneAcc);                   // per slot, per lane sums
+    b += (size_t)(NR_LANE_ROW_WORDS + NR_LANE_MAX_N) * 32 * 4;  // rows and hops, [word][lane]
+    b += 2 * sizeof(NrLaneSlot);
+    b += 16 * 4;                                             // the step's allocation, 8 ints a slot
+    b += (size_t)pages * 2;                                  // pnext
+    b += (size_t)pages;                                      // pcnt
+    b = (b + 1) & ~size_t(1);
+    b += (size_t)pages * 2;                                  // free stack
+    return (b + 15) & ~size_t(15);
+}
+
+template <int W4>
+__global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpParams P)
+{
+    constexpr int NW = 4 * W4;
+    constexpr int RW = NR_LANE_ROW_WORDS;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int NP = P.pages;
+    const int budget = max(1, NP / 2);        // pages one slot may hold
+
+    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP);
+    NrLaneAcc *accs = reinterpret_cast<NrLaneAcc *>(wbase);                      // [slot * 32 + lane]
+    uint32_t *my_rows = reinterpret_cast<uint32_t *>(wbase + 2 * 32 * sizeof(NrLaneAcc)) + lane;
+    uint32_t *my_hop = my_rows + RW * 32;
+    NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(wbase + 2 * 32 * sizeof(NrLaneAcc) +
+                                                       (size_t)(RW + NR_LANE_MAX_N) * 32 * 4);
+    int *alloc = reinterpret_cast<int *>(slots + 2);
+    short *pnext = reinterpret_cast<short *>(alloc + 16);
+    unsigned char *pcnt = reinterpret_cast<unsigned char *>(pnext + NP);
+    short *freel = reinterpret_cast<short *>(pcnt + ((NP + 1) & ~1));
+
+    const size_t gw = (size_t)blockIdx.x * (blockDim.x >> 5) + warp;
+    uint4 *sl_mask = P.slab_mask + gw * (size_t)NP * NR_PAGE * W4;
+    double *sl_mass = P.slab_mass + gw * (size_t)NP * NR_PAGE;
+    uint4 *sl_rows = reinterpret_cast<uint4 *>(P.slab_rows) + gw * (size_t)NP * NR_PAGE * (RW / 4);
+    const bool use_eps = P.eps > 0.0;
+
+    for (int p = lane; p < NP; p += 32) { freel[p] = (short)(NP - 1 - p); pnext[p] = -1; pcnt[p] = 0; }
+    if (lane < 2) { slots[lane].ii = -1; slots[lane].cur = -1; slots[lane].head = -1; }
+    int top = NP;
+    long long steps = 0;
+    __syncwarp();
+
+    // end slot s's instance: its sums and counts to P.out, its pages back to the stack
+    auto finish = [&](int s, int status, int check, const NrFix &qs, long long qn) {
+        NrLaneAcc &A = accs[s * 32 + lane];
+        const NrFix R = nr_fix_warp_sum(A.R), et = nr_fix_warp_sum(A.et), es_ = nr_fix_warp_sum(A.es);
+        const NrFix qm = nr_fix_warp_sum(qs);
+        const unsigned long long nodes = nr_warp_sum_u64(A.nodes), leaves = nr_warp_sum_u64(A.leaves);
+        const unsigned long long dead = nr_warp_sum_u64(A.dead), trunc = nr_warp_sum_u64(A.trunc);
+        const unsigned long long spilled = nr_warp_sum_u64(A.spilled);
+        const unsigned long long queued = nr_warp_sum_u64((unsigned long long)qn);
+        NrLaneSlot &S = slots[s];
+        if (lane == 0) {
+            NrWarpOut o;
+            o.R = R; o.et = et; o.es = es_; o.q = qm;
+            o.nodes = nodes; o.leaves = leaves; o.dead = dead; o.trunc = trunc; o.spilled = spilled;
+            o.queued = queued; o.t_ns = nr_globaltimer() - S.t0; o.waves = S.waves;
+            o.max_wave = check ? (unsigned long long)check : S.max_wave;
+            o.status = check ? NR_LANE_STATUS_CHECK : status;
+            P.out[P.inst_id[S.ii]] = o;
+            for (int c = 0; c < 2; ++c)                       // both of its chains
+                for (int pg = c ? S.head : S.cur; pg >= 0;) {
+                    const int nx = pnext[pg];
+                    pnext[pg] = -1;
+                    freel[top++] = (short)pg;
+                    pg = nx;
+                }
+            S.ii = -1; S.cur = -1; S.head = -1; S.used = 0;
+        }
+        top = __shfl_sync(NR_FULL, top, 0);
+        __syncwarp();
+    };
+
+    for (;;) {
+        // ---- slot upkeep: take instances, end waves, stop tests ----
+        for (int s = 0; s < 2; ++s) {
+            NrLaneSlot &S = slots[s];
+            if (S.ii == -1) {
+                int ii = 0;
+                if (lane == 0) ii = atomicAdd(P.next_inst, 1);
+                ii = __shfl_sync(NR_FULL, ii, 0);
+                if (ii >= P.n_inst) {
+                    if (lane == 0) S.ii = -2;
+                    __syncwarp();
+                    continue;
+                }
+                const NrSmallGraph g = P.inst[ii];
+                const unsigned char *gb = P.blob + g.blob_off;
+                const unsigned char *gs = P.blob + g.struct_off;
+                const double *pt = reinterpret_cast<const double *>(gb + g.off_p);
+                int rpg = 0;
+                if (lane == 0) {
+                    S.t0 = nr_globaltimer();
+                    S.ii = ii; S.blob_off = g.blob_off; S.struct_off = g.struct_off;
+                    S.n = g.n; S.src = g.src; S.dst = g.dst; S.ge = g.e;
+                    S.off_p = g.off_p; S.off_eid = g.off_eid; S.off_rows16 = g.off_rows16;
+                    S.off_start = g.off_start; S.off_list = g.off_list;
+                    S.waves = 0; S.wave_items = 0; S.max_wave = 0;
+                    rpg = freel[--top];                    // a slot holds <= NP/2 pages: one is free
+                    pcnt[rpg] = 1;
+                    pnext[rpg] = -1;
+                    S.head = rpg; S.cur = -1; S.used = 1;
+                }
+                top = __shfl_sync(NR_FULL, top, 0);
+                rpg = __shfl_sync(NR_FULL, rpg, 0);
+                {
+                    // root record, as nr_lane_kernel's
+                    uint32_t *rw = reinterpret_cast<uint32_t *>(sl_mask + (size_t)rpg * NR_PAGE * W4);
+                    bool down = false;
+#pragma unroll
+                    for (int e0 = 0; e0 < 64 * W4; e0 += 32) {
+                        const int e = e0 + lane;
+                        uint32_t v = 0u;
+                        if (e < g.e) {
+                            const double pe = pt[e];
+                            down = down || pe <= 0.0;
+                            v = (uint32_t)((pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN)
+                                << ((e & 15) << 1);
+                        }
+                        v |= __shfl_xor_sync(NR_FULL, v, 8);
+                        v |= __shfl_xor_sync(NR_FULL, v, 4);
+                        v |= __shfl_xor_sync(NR_FULL, v, 2);
+                        v |= __shfl_xor_sync(NR_FULL, v, 1);
+                        if ((lane & 15) == 0) rw[(e0 >> 4) + (lane >> 4)] = v;
+                    }
+                    uint32_t *rr = reinterpret_cast<uint32_t *>(sl_rows + (size_t)rpg * NR_PAGE * (RW / 4));
+                    if (!__any_sync(NR_FULL, down)) {
+                        if (lane < RW) rr[lane] = reinterpret_cast<const uint32_t *>(gs + g.off_rows16)[lane];
+                    } else {
+                        const int *start = reinterpret_cast<const int *>(gs + g.off_start);
+                        const uint32_t *list = reinterpret_cast<const uint32_t *>(gs + g.off_list);
+                        uint32_t r = 0;
+                        if (lane < g.n)
+                            for (int j = start[lane]; j < start[lane + 1]; ++j) {
+                                const uint32_t a = list[j];
+                                if (pt[a >> 8] > 0.0) r |= 1u << (a & 31u);
+                            }
+                        const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
+                        if (lane < 2 * RW && !(lane & 1)) rr[lane >> 1] = r | (hi << 16);
+                    }
+                }
+                if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
+                nr_acc_zero(accs[s * 32 + lane]);
+                __syncwarp();
+            }
+            if (S.ii < 0 || S.cur >= 0) continue;
+            // slot s's wave is done (or its first not begun): the stop tests, in the one-slot
+            // kernel's order (target width, node budget, empty queue)
+            if (lane == 0 && S.wave_items > S.max_wave) S.max_wave = S.wave_items;
+            NrFix qs = nr_fix_zero();
+            long long qn = 0;
+            for (int pg = S.head; pg >= 0; pg = pnext[pg])
+                if (lane < (int)pcnt[pg]) {
+                    nr_fix_add_mass(qs, sl_mass[(size_t)pg * NR_PAGE + lane]);
+                    qn++;
+                }
+            NrLaneAcc &A = accs[s * 32 + lane];
+            int st = -1;
+            if (P.target > 0.0) {
+                NrFix w = qs;
+                nr_fix_add(w, A.et);
+                nr_fix_add(w, A.es);
+                w = nr_fix_warp_sum(w);
+                if (nr_fix_le(w, P.target_fix)) st = 1;
+            }
+            if (st < 0 && P.max_nodes && nr_warp_sum_u64(A.nodes) >= P.max_nodes) st = 3;
+            if (st < 0 && S.head < 0) st = 0;
+            __syncwarp();
+            if (st >= 0) {
+                finish(s, st, 0, qs, qn);
+            } else {
+                if (lane == 0) { S.cur = S.head; S.head = -1; S.waves++; S.wave_items = 0; }
+                __syncwarp();
+            }
+        }
+        const int A0 = slots[0].ii >= 0 ? slots[0].cur : -1;
+        const int B0 = slots[1].ii >= 0 ? slots[1].cur : -1;
+        if (A0 < 0 && B0 < 0) {
+            if (slots[0].ii == -2 && slots[1].ii == -2) break;
+            continue;                               // the upkeep starts waves and instances
+        }
+
+        // ---- one step: the next page of each slot's wave, if both fit ----
+        const int cA = A0 >= 0 ? pcnt[A0] : 0, cB = B0 >= 0 ? pcnt[B0] : 0;
+        bool tA = A0 >= 0, tB = B0 >= 0;
+        if (tA && tB && cA + cB > NR_PAGE) {
+            if (steps & 1) tA = false; else tB = false;
+        }
+        const int offB = tA ? cA : 0;
+        int s = -1, pg = -1, idx = 0;
+        if (tA && lane < cA) { s = 0; pg = A0; idx = lane; }
+        else if (tB && lane >= offB && lane < offB + cB) { s = 1; pg = B0; idx = lane - offB; }
+        const bool valid = s >= 0;
+        const int sl = valid ? s : 0;
+        const size_t slot = (size_t)(valid ? pg : 0) * NR_PAGE + idx;
+        uint32_t wc[NW], rw[RW];
+        double mass = 0.0;
+        if (valid) {
+#pragma unroll
+            for (int k = 0; k < W4; ++k) {
+                const uint4 q = sl_mask[slot * W4 + k];
+                wc[4 * k] = q.x; wc[4 * k + 1] = q.y; wc[4 * k + 2] = q.z; wc[4 * k + 3] = q.w;
+            }
+#pragma unroll
+            for (int k = 0; k < RW / 4; ++k) {
+                const uint4 q = sl_rows[slot * (RW / 4) + k];
+                rw[4 * k] = q.x; rw[4 * k + 1] = q.y; rw[4 * k + 2] = q.z; rw[4 * k + 3] = q.w;
+            }
+            mass = sl_mass[slot];
+        } else {
+#pragma unroll
+            for (int k = 0; k < NW; ++k) wc[k] = 0u;
+#pragma unroll
+            for (int k = 0; k < RW; ++k) rw[k] = 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < RW; ++k) my_rows[32 * k] = rw[k];
+        __syncwarp();                               // every lane holds its record: the pages are free
+        if (lane == 0) {
+            if (tA) { slots[0].cur = pnext[A0]; slots[0].wave_items += cA; pnext[A0] = -1; freel[top++] = (short)A0; slots[0].used--; }
+            if (tB) { slots[1].cur = pnext[B0]; slots[1].wave_items += cB; pnext[B0] = -1; freel[top++] = (short)B0; slots[1].used--; }
+        }
+        top = __shfl_sync(NR_FULL, top, 0);
+        __syncwarp();
+
+        // the lane's instance
+        const NrLaneSlot &S = slots[sl];
+        const unsigned char *gs = P.blob + S.struct_off;
+        const double *pt = reinterpret_cast<const double *>(P.blob + S.blob_off + S.off_p);
+        const uint16_t *eid = reinterpret_cast<const uint16_t *>(gs + S.off_eid);
+        const int n = S.n, src = S.src, dst = S.dst, ge = S.ge;
+        const int es = n <= 8 ? 8 : 16;
+        NrLaneAcc &acc = accs[sl * 32 + lane];
+
+        bool active = valid;
+        if (valid) {
+            acc.nodes++;
+            if (use_eps && mass < P.eps) {          // main.cu:537-543
+                acc.trunc++;
+                nr_fix_add_mass(acc.et, mass);
+                active = false;
+            }
+        }
+        int L = 0;
+        bool live = false;
+        int bad = 0;
+        if (active) {
+            if (src == dst) {
+                live = true;
+            } else {
+                const uint32_t rd = nr_lane_row(my_rows, dst);
+                uint32_t F = 1u << src, vis = F;
+                for (;;) {
+                    if (L >= NR_LANE_MAX_N) { bad = 2; break; }
+                    my_hop[32 * L] = F;
+                    if (rd & F) { ++L; live = true; break; }
+                    uint32_t nf = 0u;
+                    for (uint32_t t = F; t; t &= t - 1u) nf |= nr_lane_row(my_rows, __ffs(t) - 1);
+                    nf &= ~vis;
+                    if (!nf) break;
+                    vis |= nf;
+                    F = nf;
+                    ++L;
+                }
+            }
+            if (!live) {
+                acc.dead++;
+                L = 0;
+            }
+        }
+        int nch = 0;
+        if (live && !bad) {
+            int x = dst;
+            for (int l = L - 1; l >= 0; --l) {
+                const int u = __ffs(nr_lane_row(my_rows, x) & my_hop[32 * l]) - 1;
+                if (u < 0 || u >= n) { bad = 3; break; }
+                const uint32_t e = eid[u * es + x];
+                if ((int)e >= ge) { bad = 4; break; }
+                my_hop[32 * l] = e | ((uint32_t)u << 16) | ((uint32_t)x << 24);
+                nch += ((nr_pick(wc, (int)e >> 4) >> ((e & 15) << 1)) & 3u) == 3u;
+                x = u;
+            }
+        }
+        if (++steps > NR_LANE_STEP_CAP) bad = 1;
+        {
+            const unsigned bm = __ballot_sync(NR_FULL, bad != 0);
+            if (bm) {                                   // an internal check failed: end both slots
+                const int check = __shfl_sync(NR_FULL, bad, __ffs(bm) - 1);
+                for (int t = 0; t < 2; ++t)
+                    if (slots[t].ii >= 0) finish(t, 0, check, nr_fix_zero(), 0);
+                continue;
+            }
+        }
+
+        // children: a prefix over the lanes (slot 0's lanes first) places each slot's children
+        // on that slot's next-wave chain, one allocation a slot
+        int pre = nch;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int t = __shfl_up_sync(NR_FULL, pre, off);
+            if (lane >= off) pre += t;
+        }
+        const int total = __shfl_sync(NR_FULL, pre, 31);
+        const int tot0 = tA ? __shfl_sync(NR_FULL, pre, cA - 1) : 0;
+        pre -= nch;
+        if (lane == 0) {
+            for (int t = 0; t < 2; ++t) {
+                NrLaneSlot &T = slots[t];
+                const int want = t ? total - tot0 : tot0;
+                int hA = -1, cA2 = 0, nA = 0, npg = 0;
+                const int top0 = top;
+                if (want > 0) {
+                    const int hd = T.head;
+                    const int c = (hd >= 0) ? pcnt[hd] : NR_PAGE;
+                    nA = min(want, NR_PAGE - c);
+                    if (nA > 0) { hA = hd; cA2 = c; pcnt[hd] = (unsigned char)(c + nA); }
+                    const int rest = want - nA;
+                    npg = min(min((rest + NR_PAGE - 1) / NR_PAGE, top0), max(0, budget - T.used));
+                    int prev = hd;
+                    for (int i = 0; i < npg; ++i) {
+                        const int pgi = freel[top0 - 1 - i];
+                        pnext[pgi] = (short)prev;
+                        pcnt[pgi] = (unsigned char)min(NR_PAGE, rest - NR_PAGE * i);
+                        prev = pgi;
+                    }
+                    if (npg > 0) { T.head = prev; T.used += npg; }
+                    top = top0 - npg;
+                }
+                alloc[8 * t] = hA; alloc[8 * t + 1] = cA2; alloc[8 * t + 2] = nA; alloc[8 * t + 3] = npg;
+                alloc[8 * t + 4] = top0;
+            }
+        }
+        top = __shfl_sync(NR_FULL, top, 0);
+        __syncwarp();
+        const int hA = alloc[8 * sl], cA2 = alloc[8 * sl + 1], nA = alloc[8 * sl + 2], npg = alloc[8 * sl + 3];
+        const int top0 = alloc[8 * sl + 4];
+        int q = pre - (sl == 1 ? tot0 : 0);         // this lane's first child, within its slot
+        double Pm = mass;
+        for (int h = 0; h < L; ++h) {
+            const uint32_t hp = my_hop[32 * h];
+            const int e = (int)(hp & 0xffffu);
+            const int ew = e >> 4;
+            const uint32_t wv = nr_pick(wc, ew);
+            if (((wv >> ((e & 15) << 1)) & 3u) != 3u) continue;
+            const int cu = (int)((hp >> 16) & 0xffu), cv = (int)(hp >> 24);
+            const double pe = pt[e];
+            const double cm = __dmul_rn(Pm, __dsub_rn(1.0, pe));
+            Pm = __dmul_rn(Pm, pe);
+            int sc = -1;
+            if (q < nA) {
+                sc = hA * NR_PAGE + cA2 + q;
+            } else {
+                const int r = q - nA;
+                if ((r >> 5) < npg) sc = freel[top0 - 1 - (r >> 5)] * NR_PAGE + (r & 31);
+            }
+            ++q;
+            if (sc >= 0) {
+                uint4 *d = sl_mask + (size_t)sc * W4;
+#pragma unroll
+                for (int kk = 0; kk < W4; ++kk)
+                    d[kk] = make_uint4(wc[4 * kk], wc[4 * kk + 1], wc[4 * kk + 2], wc[4 * kk + 3]);
+                reinterpret_cast<uint32_t *>(d)[ew] = wv & ~(3u << ((e & 15) << 1));
+                const int wu = cu >> 1, wv2 = cv >> 1;
+                const uint32_t bu = 1u << (cv + ((cu & 1) << 4));
+                const uint32_t bv = 1u << (cu + ((cv & 1) << 4));
+                uint4 *dr = sl_rows + (size_t)sc * (RW / 4);
+#pragma unroll
+                for (int kk = 0; kk < RW / 4; ++kk)
+                    dr[kk] = make_uint4(rw[4 * kk], rw[4 * kk + 1], rw[4 * kk + 2], rw[4 * kk + 3]);
+                uint32_t *drw = reinterpret_cast<uint32_t *>(dr);
+                if (wu == wv2) {
+                    drw[wu] = my_rows[32 * wu] & ~(bu | bv);
+                } else {
+                    drw[wu] = my_rows[32 * wu] & ~bu;
+                    drw[wv2] = my_rows[32 * wv2] & ~bv;
+                }
+                sl_mass[sc] = cm;
+            } else {                                  // the slot's pages are full: mass to ESP
+                acc.spilled++;
+                nr_fix_add_mass(acc.es, cm);
+            }
+#pragma unroll
+            for (int kk = 0; kk < NW; ++kk)            // later children see hop h up
+                if (kk == ew) wc[kk] &= ~(2u << ((e & 15) << 1));
+        }
+        if (live) {
+            acc.leaves++;
+            nr_fix_add_mass(acc.R, Pm);
+        }
+        __syncwarp();
+    }
+}

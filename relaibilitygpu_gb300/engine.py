@@ -28,8 +28,8 @@ STATUS = {
 ORDERS = {"auto": 0, "waves": 1, "maxmass": 2, "learned": 3}
 BRANCHING = {"path": 0, "fork": 1}
 ENGINES = {1: "grid", 2: "warp"}
-KERNELS = {0: "", 1: "group", 2: "lane"}     # the warp engine's kernel
-SMALL_KERNELS = {"auto": 0, "group": 1}
+KERNELS = {0: "", 1: "group", 2: "lane", 3: "lane2"}     # the warp engine's kernel
+SMALL_KERNELS = {"auto": 0, "group": 1, "lane1": 2}
 
 
 class NrError(RuntimeError):

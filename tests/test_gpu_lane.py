@@ -75,12 +75,17 @@ def test_lane_kernel_wave_schedule(ctx, oracle, target, shift):
                                  capacity=1 << 16)
     group = ctx.reliability_batch(gs, srcs, dsts, target_width=target, bucket_shift=shift, n_buckets=nb,
                                   capacity=1 << 16, small_kernel="group")
-    for i, (g, a, b) in enumerate(zip(gs, lane, group)):
+    # one bucket: two instances per warp by default; the one-instance lane kernel beside it
+    one = ctx.reliability_batch(gs, srcs, dsts, target_width=target, bucket_shift=shift, n_buckets=nb,
+                                capacity=1 << 16, small_kernel="lane1")
+    lane_name = "lane2" if shift < 0 else "lane"
+    for i, (g, a, b, c) in enumerate(zip(gs, lane, group, one)):
         assert a.engine == "warp" and b.engine == "warp" and a.spilled == 0
-        assert a.kernel == ("lane" if lane_expected(g) else "group"), i
-        assert b.kernel == "group"
+        assert a.kernel == (lane_name if lane_expected(g) else "group"), i
+        assert b.kernel == "group" and c.kernel == ("lane" if lane_expected(g) else "group")
         for f in FIELDS:
             assert getattr(a, f) == getattr(b, f), (i, f, getattr(a, f), getattr(b, f))
+            assert getattr(c, f) == getattr(b, f), (i, f, getattr(c, f), getattr(b, f))
         if i % 5 == 0 or i >= len(gs) - 6:
             o = oracle.run(g, srcs[i], dsts[i], target_width=target, bucket_shift=shift,
                            n_buckets=nb if shift >= 0 else 1)
