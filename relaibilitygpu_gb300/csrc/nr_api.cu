@@ -1421,7 +1421,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     const int B = std::max(1, std::min(NR_HOST_BLOCKS, n / 128));
     S.blk.resize(B);
     auto blk_begin = [&](int b) { return (int)((long long)n * b / B); };
-    std::atomic<int> too_wide(0);
+    std::atomic<int> too_wide(0), invalid(NR_OK);
     c->parallel_for(B, 1, [&](int b) {
         NrHostBlock &k = S.blk[b];
         size_t rel = 0;
@@ -1429,11 +1429,25 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         k.last_rows = -1;
         for (int j = 0; j < NCLS; ++j) k.cnt[j] = 0;
         int cur_rows = -1;                    // rows mode of the current topology
-        for (int i = blk_begin(b), e = blk_begin(b + 1); i < e; ++i) {
+        const int i0 = blk_begin(b);
+        for (int i = i0, e = blk_begin(b + 1); i < e; ++i) {
+            // validation (the shape of every instance; the arrays of the first of a run of
+            // instances sharing them, and of the block's first, whose run may start earlier)
+            int vr = validate_shape(&gs[i], srcs[i], dsts[i]);
+            const bool prev_ok = i > 0 && validate_shape(&gs[i - 1], srcs[i - 1], dsts[i - 1]) == NR_OK;
+            if (!vr && (i == i0 || !prev_ok || !same_structure_arrays(&gs[i], &gs[i - 1])))
+                vr = validate_structure(&gs[i]);
+            if (vr) { invalid.store(vr); S.cls[i] = 0; S.same_prev[i] = 0; S.inst_b[i] = 0; S.struct_b[i] = 0; continue; }
             // consecutive instances with the same topology share one structural part
-            const bool same = i > 0 && same_topology(&gs[i], &gs[i - 1]);
+            const bool same = prev_ok && same_topology(&gs[i], &gs[i - 1]);
             const size_t ib = small_inst_layout(&gs[i], srcs[i], dsts[i], &desc[i]);
-            const size_t sb = small_struct_layout(&gs[i], &desc[i], 0);   // offsets relative to struct_off
+            size_t sb = 0;                    // offsets relative to struct_off
+            if (same && i > i0) {
+                desc[i].off_eid = desc[i - 1].off_eid; desc[i].off_start = desc[i - 1].off_start;
+                desc[i].off_list = desc[i - 1].off_list; desc[i].off_rows16 = desc[i - 1].off_rows16;
+            } else {
+                sb = small_struct_layout(&gs[i], &desc[i], 0);
+            }
             S.same_prev[i] = same;
             S.inst_b[i] = ib;
             S.struct_b[i] = same ? 0 : sb;
@@ -1457,6 +1471,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         }
         k.bytes = rel;
     });
+    if (invalid.load() != NR_OK) return invalid.load();
     if (too_wide.load()) return NR_ERR_UNSUPPORTED;
     pc.mark("sizes");
 
@@ -1701,6 +1716,14 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
 // Checks of a batch: shapes, CSR arrays (once per run of instances sharing them),
 // probabilities of graphs above 32 nodes (the warp engine checks its own while
 // copying them).  *n_wide = graphs above 32 nodes.
+static int batch_options_ok(const nr_context *c, const nr_options &o)
+{
+    if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
+    if (o.order == NR_ORDER_LEARNED && o.branching == NR_BRANCH_FORK) return NR_ERR_UNSUPPORTED;
+    if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
+    return NR_OK;
+}
+
 static int batch_validate(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
                           const nr_options &o, int *n_wide)
 {
@@ -1717,10 +1740,7 @@ static int batch_validate(nr_context *c, int n, const nr_graph *gs, const int32_
     });
     *n_wide = wide.load();
     if (bad.load() != NR_OK) return bad.load();
-    if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
-    if (o.order == NR_ORDER_LEARNED && o.branching == NR_BRANCH_FORK) return NR_ERR_UNSUPPORTED;
-    if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
-    return NR_OK;
+    return batch_options_ok(c, o);
 }
 
 static WarpRunCfg batch_cfg(const nr_options &o, uint64_t capacity)
@@ -1813,8 +1833,12 @@ extern "C" int nr_batch_submit(nr_context *c, int n, const nr_graph *gs, const i
     *ticket = t;
     if (n == 0) { record_done(c, t, NR_OK); return NR_OK; }
     PhaseClock pc;
+    // graphs of up to 32 nodes only (the usual batch): the warp engine's first host pass
+    // validates them as it sizes their tables; else the whole batch is validated here first
+    bool any_wide = false;
+    for (int i = 0; i < n && !any_wide; ++i) any_wide = gs[i].n_nodes > NR_SMALL_MAX_N;
     int n_wide = 0;
-    int rc = batch_validate(c, n, gs, srcs, dsts, o, &n_wide);
+    int rc = any_wide ? batch_validate(c, n, gs, srcs, dsts, o, &n_wide) : batch_options_ok(c, o);
     if (rc) { record_done(c, t, rc); return rc; }
     pc.mark("validate");
     NR_CUDA_TRY(cudaSetDevice(c->device));
