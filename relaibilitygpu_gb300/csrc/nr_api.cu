@@ -206,9 +206,9 @@ public:
         {
             std::lock_guard<std::mutex> l(mu_);
             quit_ = true;
-            // a new job number with every slot taken: spinning workers stop and see quit_
+            // a new job number with no helper slot: spinning workers stop and see quit_
             const unsigned long long job = (state_.load(std::memory_order_relaxed) >> 32) + 1;
-            state_.store((job << 32) | 0xffffffffull, std::memory_order_release);
+            state_.store(job << 32, std::memory_order_release);
         }
         cv_.notify_all();
         for (auto &t : th_) t.join();
@@ -229,14 +229,14 @@ public:
             fn_.store(&fn, std::memory_order_relaxed);
             n_.store(n, std::memory_order_relaxed);
             grain_.store(std::max(1, grain), std::memory_order_relaxed);
-            helpers_.store(helpers, std::memory_order_relaxed);
             next_.store(0, std::memory_order_relaxed);
             busy_.store(helpers, std::memory_order_relaxed);
             const unsigned long long job = (state_.load(std::memory_order_relaxed) >> 32) + 1;
-            state_.store(job << 32, std::memory_order_release);
+            state_.store((job << 32) | ((unsigned long long)helpers << 16), std::memory_order_release);
         }
         cv_.notify_all();
         work();
+        for (int it = 0; it < kBusyPolls && busy_.load(std::memory_order_acquire) != 0; ++it) {}
         const auto t0 = std::chrono::steady_clock::now();
         while (busy_.load(std::memory_order_acquire) != 0) {
             if (std::chrono::steady_clock::now() - t0 > kSpin) {
@@ -251,6 +251,7 @@ public:
 
 private:
     static constexpr std::chrono::microseconds kSpin{NR_POOL_SPIN_US};
+    static constexpr int kBusyPolls = 20000;    // loads of the job word before yielding (tens of us)
     void work()
     {
         const int n = n_.load(std::memory_order_relaxed), grain = grain_.load(std::memory_order_relaxed);
@@ -263,9 +264,11 @@ private:
         }
     }
     // A worker joins a job by claiming one of its helper slots with a compare-and-swap
-    // on state_ (job number << 32 | slots claimed): no lock on the way in, and a claim
-    // can only succeed for the job it read, whose fields stay put until every claimed
-    // helper has finished.  The mutex is taken only to sleep.
+    // on state_ (job number << 32 | helper slots << 16 | slots claimed): no lock on the
+    // way in.  The slot count travels in the same word as the claims, so a worker that
+    // read an old job's word can only see it full (a job ends only after all its slots
+    // were claimed and their helpers finished) and can never claim into a job whose
+    // fields are being rewritten.  The mutex is taken only to sleep.
     void loop(int)
     {
         unsigned long long seen = 0;           // last job this worker has dealt with
@@ -273,6 +276,9 @@ private:
             unsigned long long s = state_.load(std::memory_order_acquire);
             if ((s >> 32) == seen) {
                 const auto t0 = std::chrono::steady_clock::now();
+                // poll the word itself for a few tens of microseconds (a new job is seen within
+                // a cache-line transfer), then yield the core between polls, then sleep
+                for (int it = 0; it < kBusyPolls && ((s = state_.load(std::memory_order_acquire)) >> 32) == seen; ++it) {}
                 while (((s = state_.load(std::memory_order_acquire)) >> 32) == seen &&
                        std::chrono::steady_clock::now() - t0 < kSpin)
                     std::this_thread::yield();
@@ -286,7 +292,7 @@ private:
             if (quit_.load(std::memory_order_acquire)) return;
             bool joined = false;
             while ((s >> 32) != seen) {
-                if ((unsigned)(s & 0xffffffffull) >= (unsigned)helpers_.load(std::memory_order_relaxed)) {
+                if ((s & 0xffffull) >= ((s >> 16) & 0xffffull)) {   // every slot of this job taken
                     seen = s >> 32;
                     break;
                 }
@@ -310,9 +316,9 @@ private:
     // the job: written by the caller before it publishes a job number in state_; a worker
     // reads them after its claim on state_ (an acquire) succeeded
     std::atomic<const std::function<void(int)> *> fn_{nullptr};
-    std::atomic<int> n_{0}, grain_{1}, helpers_{0};
+    std::atomic<int> n_{0}, grain_{1};
     std::atomic<int> next_{0}, busy_{0};
-    std::atomic<unsigned long long> state_{0};   // job number << 32 | helper slots claimed
+    std::atomic<unsigned long long> state_{0};   // job number << 32 | helper slots << 16 | claimed
     std::atomic<bool> quit_{false};
 };
 

@@ -134,3 +134,32 @@ def test_lane_kernel_spills_budget_and_handover(ctx, oracle):
     o = oracle.run(big, 0, 9, threads=8)
     assert res[0].engine == "grid" and (res[0].nodes, res[0].paths, res[0].R) == (o.nodes, o.paths, o.R)
     assert res[1].kernel == "lane" and res[1].R == exact.R and res[1].nodes == exact.nodes
+
+
+def test_two_slot_kernel_budget_spills_and_uneven_batches(ctx, oracle):
+    """Breadth-first waves (two instances a warp): a node budget stops each instance between its
+    waves exactly as the lane-group kernel does; a slot whose half of the pages is full spills into
+    ESP and the bracket holds; batches of 1, 2, 3 and 33 instances (empty slots, a warp with one
+    instance) give the oracle's results."""
+    from relaibilitygpu_gb300 import graphs
+    k12 = graphs.complete(12, p_range=(0.7, 0.99), seed=5)
+    opts = dict(target_width=1e-12, bucket_shift=-1, n_buckets=64, max_nodes=3000)
+    a = ctx.reliability(k12, 0, 11, **opts)
+    b = ctx.reliability(k12, 0, 11, small_kernel="group", **opts)
+    assert a.stop == 3 and a.kernel == "lane2" and b.kernel == "group"
+    for f in FIELDS:
+        assert getattr(a, f) == getattr(b, f), f
+    g = graphs.complete(9, p_range=(0.6, 0.97), seed=5)
+    exact = oracle.run(g, 0, 8)
+    r = ctx.reliability(g, 0, 8, target_width=1e-14, bucket_shift=-1, n_buckets=64, capacity=256)
+    assert r.kernel == "lane2" and r.spilled > 0
+    assert r.R <= exact.R + 1e-15 and exact.R <= r.R + r.esp + 1e-12
+    for m in (1, 2, 3, 33):
+        gs = [graphs.complete(8 + s % 6, p_range=(0.8, 0.99), seed=700 + s) for s in range(m)]
+        res = ctx.reliability_batch(gs, [0] * m, [x.n_nodes - 1 for x in gs], target_width=1e-7,
+                                    bucket_shift=-1, n_buckets=64, capacity=1 << 14)
+        for x, rr in zip(gs, res):
+            o = oracle.run(x, 0, x.n_nodes - 1, target_width=1e-7)
+            assert rr.kernel == "lane2" and rr.spilled == 0
+            assert (rr.nodes, rr.iterations, rr.max_queue_items, rr.queued) == (o.nodes, o.waves, o.max_wave, o.queued)
+            assert rr.R == o.R and rr.esp == o.esp
