@@ -109,7 +109,9 @@ typedef struct nr_options {
                                  (0 = 512) */
     int32_t  branching;       /* NR_BRANCH_* */
     int32_t  small_kernel;    /* NR_SMALL_*: the warp engine's kernel */
-    int32_t  reserved[1];
+    int32_t  lane_slots;      /* one lane per subproblem, one bucket: instances a warp carries (2 or 4;
+                                 0 = the default, 2: on 4096 K15 instances 4 slots leave too few warps
+                                 per SM to hide the steps' latency, 0.096 against 0.060 ms) */
 } nr_options;
 
 typedef struct nr_result {

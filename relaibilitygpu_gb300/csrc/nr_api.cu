@@ -46,7 +46,7 @@ const void *nr_warp_fork_kernel_ptr_g32(int w4);
 const void *nr_warp_learn_kernel_ptr_g16(int w4);
 const void *nr_warp_learn_kernel_ptr_g32(int w4);
 const void *nr_lane_kernel_ptr(int w4);
-const void *nr_lane2_kernel_ptr(int w4);
+const void *nr_lane2_kernel_ptr(int w4, int slots);
 int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
 
 namespace {
@@ -356,7 +356,8 @@ struct WarpRunCfg {
     int fork = 0;
     int learned = 0;
     int lane = 1;                 // one lane per subproblem where it applies
-    int lane2 = 1;                // ... with two instances per warp in breadth-first waves
+    int lane2 = 1;                // ... with several instances per warp in breadth-first waves
+    int lane_slots = 2;           // instances per warp then
     const WarpDump *dump = nullptr;
     double eps, target;
     unsigned long long max_nodes;
@@ -1342,6 +1343,7 @@ static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhausti
     w.fork = (o->branching == NR_BRANCH_FORK);
     w.lane = (o->small_kernel != NR_SMALL_GROUP);
     w.lane2 = (o->small_kernel == NR_SMALL_AUTO) && w.wave_mode && w.shift < 0;
+    w.lane_slots = (o->lane_slots == 4) ? 4 : 2;
     w.warps_per_block = (o->warps_per_block >= 1 && o->warps_per_block <= NR_WARP_BLOCK_MAX / 32)
                             ? o->warps_per_block : NR_WARP_BLOCK / 32;
     if (capacity == 0) w.pages = o->pages_per_warp > 0 ? std::min(8192, std::max(4, o->pages_per_warp)) : 512;
@@ -1560,7 +1562,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     while (cfgp.pages > 4 &&
            std::max(std::max(nr_warp_shm_bytes(4, NR_MAX_W4, cfgp.n_buckets, cfgp.pages, true),
                              nr_lane_shm_bytes(cfgp.n_buckets, cfgp.pages)),
-                    nr_lane2_shm_bytes(cfgp.pages)) * warps_pb > (size_t)c->smem_optin)
+                    nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots)) * warps_pb > (size_t)c->smem_optin)
         cfgp.pages /= 2;
     const bool learn = cfg.learned || cfg.dump;
     int grids[NCLS] = {0};
@@ -1572,10 +1574,10 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         const int G = lanek ? 0 : 8 << (j / NR_MAX_W4);
         const int W4 = lanek ? j - NR_LANE_CLS0 + 1 : j % NR_MAX_W4 + 1;
         const bool two = lanek && cfg.lane2;
-        const void *kfn = lanek ? (two ? nr_lane2_kernel_ptr(W4) : nr_lane_kernel_ptr(W4))
+        const void *kfn = lanek ? (two ? nr_lane2_kernel_ptr(W4, cfg.lane_slots) : nr_lane_kernel_ptr(W4))
                                 : warp_kernel(G, W4, learn, cfg.fork != 0);
         if (!kfn) return NR_ERR_UNSUPPORTED;
-        const size_t smem = (two ? nr_lane2_shm_bytes(cfgp.pages)
+        const size_t smem = (two ? nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots)
                                  : lanek ? nr_lane_shm_bytes(cfg.n_buckets, cfgp.pages)
                                          : nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn)) * warps_pb;
         auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
@@ -1588,7 +1590,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
             bps = it->second;
         }
         if (bps < 1) return NR_ERR_UNSUPPORTED;
-        const int per_block = warps_pb * (two ? 2 : 1);      // instances a block starts with
+        const int per_block = warps_pb * (two ? cfg.lane_slots : 1);   // instances a block starts with
         grids[j] = std::max(1, std::min(bps * c->sms, (class_count[j] + per_block - 1) / per_block));
         smems[j] = smem;
         const size_t row_bytes = lanek ? 4 * (size_t)NR_LANE_ROW_WORDS : 4 * (size_t)G;
@@ -1647,7 +1649,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.dump_stride = cfg.dump ? cfg.dump->stride : 0;
         P.inst_base = base;
         P.fork = cfg.fork;
-        const void *kfn = lanek ? (cfg.lane2 ? nr_lane2_kernel_ptr(W4) : nr_lane_kernel_ptr(W4))
+        const void *kfn = lanek ? (cfg.lane2 ? nr_lane2_kernel_ptr(W4, cfg.lane_slots) : nr_lane_kernel_ptr(W4))
                                 : warp_kernel(G, W4, learn, cfg.fork != 0);
         void *args[] = {&P};
         NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smems[j]));

@@ -11,11 +11,14 @@ const void *nr_lane_kernel_ptr(int w4)
     }
 }
 
-const void *nr_lane2_kernel_ptr(int w4)
+const void *nr_lane2_kernel_ptr(int w4, int slots)
 {
-    switch (w4) {
-    case 1: return (const void *)nr_lane2_kernel<1>;
-    case 2: return (const void *)nr_lane2_kernel<2>;
-    default: return nullptr;
+    if (slots == 2) {
+        if (w4 == 1) return (const void *)nr_lane2_kernel<1, 2>;
+        if (w4 == 2) return (const void *)nr_lane2_kernel<2, 2>;
+    } else if (slots == 4) {
+        if (w4 == 1) return (const void *)nr_lane2_kernel<1, 4>;
+        if (w4 == 2) return (const void *)nr_lane2_kernel<2, 4>;
     }
+    return nullptr;
 }

@@ -1,16 +1,16 @@
-// nr_lane2.cuh -- the lane kernel with two instances per warp, for breadth-first waves
-// (one bucket) on undirected simple graphs of up to 16 nodes.
+// nr_lane2.cuh -- the lane kernel with several instances per warp (NS = 2 or 4), for
+// breadth-first waves (one bucket) on undirected simple graphs of up to 16 nodes.
 //
 // nr_lane_kernel gives a warp one instance, and the first waves of an instance hold
 // 1, 1, 2, 4, ... records: most lanes idle while every step pays its full fixed work,
 // and a batch of a few thousand instances ends with a tail of warps on their last
-// instance.  Here a warp carries two instance slots.  A step takes the next page of
-// each slot's current wave when both fit in 32 lanes (else one of them, alternating):
-// lanes 0..cA-1 expand slot 0's records, the next cB lanes slot 1's.  Each slot keeps
+// instance.  Here a warp carries NS instance slots.  A step takes the next page of as
+// many slots' current waves as fit in 32 lanes, starting from a slot that rotates step
+// by step; each taken page gets a contiguous range of lanes.  Each slot keeps
 // its own wave structure -- its current wave's page chain, the chain its children go
 // to, its own stop test between its waves -- so each instance follows exactly the
 // schedule of the one-slot kernel and of the oracle; only the interleaving of the two
-// instances' steps is new.  The slots share the warp's page pool, each limited to half
+// instances' steps is new.  The slots share the warp's page pool, each limited to 1/NS
 // of it, so a new instance always finds a page for its root.
 #pragma once
 
@@ -30,12 +30,12 @@ struct NrLaneSlot {
     int pad[2];
 };
 
-__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages)
+__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots)
 {
-    size_t b = 2 * 32 * sizeof(NrLaneAcc);                   // per slot, per lane sums
+    size_t b = (size_t)slots * 32 * sizeof(NrLaneAcc);       // per slot, per lane sums
     b += (size_t)(NR_LANE_ROW_WORDS + NR_LANE_MAX_N) * 32 * 4;  // rows and hops, [word][lane]
-    b += 2 * sizeof(NrLaneSlot);
-    b += 16 * 4;                                             // the step's allocation, 8 ints a slot
+    b += (size_t)slots * sizeof(NrLaneSlot);
+    b += (size_t)slots * 8 * 4;                              // the step's allocation, 8 ints a slot
     b += (size_t)pages * 2;                                  // pnext
     b += (size_t)pages;                                      // pcnt
     b = (b + 1) & ~size_t(1);
@@ -43,25 +43,24 @@ __host__ __device__ inline size_t nr_lane2_shm_bytes(int pages)
     return (b + 15) & ~size_t(15);
 }
 
-template <int W4>
+template <int W4, int NS>
 __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpParams P)
 {
     constexpr int NW = 4 * W4;
     constexpr int RW = NR_LANE_ROW_WORDS;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned lt_mask = (1u << lane) - 1u;
     const int NP = P.pages;
-    const int budget = max(1, NP / 2);        // pages one slot may hold
+    const int budget = max(1, NP / NS);       // pages one slot may hold
 
-    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP);
+    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP, NS);
     NrLaneAcc *accs = reinterpret_cast<NrLaneAcc *>(wbase);                      // [slot * 32 + lane]
-    uint32_t *my_rows = reinterpret_cast<uint32_t *>(wbase + 2 * 32 * sizeof(NrLaneAcc)) + lane;
+    uint32_t *my_rows = reinterpret_cast<uint32_t *>(wbase + NS * 32 * sizeof(NrLaneAcc)) + lane;
     uint32_t *my_hop = my_rows + RW * 32;
-    NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(wbase + 2 * 32 * sizeof(NrLaneAcc) +
+    NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(wbase + NS * 32 * sizeof(NrLaneAcc) +
                                                        (size_t)(RW + NR_LANE_MAX_N) * 32 * 4);
-    int *alloc = reinterpret_cast<int *>(slots + 2);
-    short *pnext = reinterpret_cast<short *>(alloc + 16);
+    int *alloc = reinterpret_cast<int *>(slots + NS);
+    short *pnext = reinterpret_cast<short *>(alloc + 8 * NS);
     unsigned char *pcnt = reinterpret_cast<unsigned char *>(pnext + NP);
     short *freel = reinterpret_cast<short *>(pcnt + ((NP + 1) & ~1));
 
@@ -72,7 +71,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     const bool use_eps = P.eps > 0.0;
 
     for (int p = lane; p < NP; p += 32) { freel[p] = (short)(NP - 1 - p); pnext[p] = -1; pcnt[p] = 0; }
-    if (lane < 2) { slots[lane].ii = -1; slots[lane].cur = -1; slots[lane].head = -1; }
+    if (lane < NS) { slots[lane].ii = -1; slots[lane].cur = -1; slots[lane].head = -1; }
     int top = NP;
     long long steps = 0;
     __syncwarp();
@@ -110,7 +109,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
 
     for (;;) {
         // ---- slot upkeep: take instances, end waves, stop tests ----
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < NS; ++s) {
             NrLaneSlot &S = slots[s];
             if (S.ii == -1) {
                 int ii = 0;
@@ -210,23 +209,29 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 __syncwarp();
             }
         }
-        const int A0 = slots[0].ii >= 0 ? slots[0].cur : -1;
-        const int B0 = slots[1].ii >= 0 ? slots[1].cur : -1;
-        if (A0 < 0 && B0 < 0) {
-            if (slots[0].ii == -2 && slots[1].ii == -2) break;
-            continue;                               // the upkeep starts waves and instances
+        // ---- one step: the next page of as many slots' waves as fit in 32 lanes, starting
+        // from a slot that rotates step by step (so no slot waits for long) ----
+        int tpg[NS], toff[NS], tcnt[NS];          // per slot: page taken (-1 none), first lane, records
+        int used_lanes = 0;
+        bool all_done = true;
+#pragma unroll
+        for (int t = 0; t < NS; ++t) { tpg[t] = -1; toff[t] = 0; tcnt[t] = 0; all_done = all_done && slots[t].ii == -2; }
+        if (all_done) break;
+#pragma unroll
+        for (int k2 = 0; k2 < NS; ++k2) {
+            const int t = (int)((steps + k2) % NS);
+            const int cp = slots[t].ii >= 0 ? slots[t].cur : -1;
+            if (cp < 0) continue;
+            const int c = pcnt[cp];
+            if (used_lanes + c > NR_PAGE) continue;
+            tpg[t] = cp; toff[t] = used_lanes; tcnt[t] = c;
+            used_lanes += c;
         }
-
-        // ---- one step: the next page of each slot's wave, if both fit ----
-        const int cA = A0 >= 0 ? pcnt[A0] : 0, cB = B0 >= 0 ? pcnt[B0] : 0;
-        bool tA = A0 >= 0, tB = B0 >= 0;
-        if (tA && tB && cA + cB > NR_PAGE) {
-            if (steps & 1) tA = false; else tB = false;
-        }
-        const int offB = tA ? cA : 0;
+        if (used_lanes == 0) continue;              // the upkeep starts waves and instances
         int s = -1, pg = -1, idx = 0;
-        if (tA && lane < cA) { s = 0; pg = A0; idx = lane; }
-        else if (tB && lane >= offB && lane < offB + cB) { s = 1; pg = B0; idx = lane - offB; }
+#pragma unroll
+        for (int t = 0; t < NS; ++t)
+            if (tpg[t] >= 0 && lane >= toff[t] && lane < toff[t] + tcnt[t]) { s = t; pg = tpg[t]; idx = lane - toff[t]; }
         const bool valid = s >= 0;
         const int sl = valid ? s : 0;
         const size_t slot = (size_t)(valid ? pg : 0) * NR_PAGE + idx;
@@ -254,8 +259,13 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         for (int k = 0; k < RW; ++k) my_rows[32 * k] = rw[k];
         __syncwarp();                               // every lane holds its record: the pages are free
         if (lane == 0) {
-            if (tA) { slots[0].cur = pnext[A0]; slots[0].wave_items += cA; pnext[A0] = -1; freel[top++] = (short)A0; slots[0].used--; }
-            if (tB) { slots[1].cur = pnext[B0]; slots[1].wave_items += cB; pnext[B0] = -1; freel[top++] = (short)B0; slots[1].used--; }
+#pragma unroll
+            for (int t = 0; t < NS; ++t)
+                if (tpg[t] >= 0) {
+                    const int p0 = tpg[t];
+                    slots[t].cur = pnext[p0]; slots[t].wave_items += tcnt[t]; pnext[p0] = -1;
+                    freel[top++] = (short)p0; slots[t].used--;
+                }
         }
         top = __shfl_sync(NR_FULL, top, 0);
         __syncwarp();
@@ -323,7 +333,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             const unsigned bm = __ballot_sync(NR_FULL, bad != 0);
             if (bm) {                                   // an internal check failed: end both slots
                 const int check = __shfl_sync(NR_FULL, bad, __ffs(bm) - 1);
-                for (int t = 0; t < 2; ++t)
+                for (int t = 0; t < NS; ++t)
                     if (slots[t].ii >= 0) finish(t, 0, check, nr_fix_zero(), 0);
                 continue;
             }
@@ -337,13 +347,20 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             const int t = __shfl_up_sync(NR_FULL, pre, off);
             if (lane >= off) pre += t;
         }
-        const int total = __shfl_sync(NR_FULL, pre, 31);
-        const int tot0 = tA ? __shfl_sync(NR_FULL, pre, cA - 1) : 0;
+        // inclusive prefix before and at the end of each taken slot's lanes
+        int tbeg[NS], tend[NS];
+#pragma unroll
+        for (int t = 0; t < NS; ++t) {
+            const int e1 = __shfl_sync(NR_FULL, pre, tcnt[t] ? toff[t] + tcnt[t] - 1 : 0);
+            const int b1 = __shfl_sync(NR_FULL, pre, toff[t] > 0 ? toff[t] - 1 : 0);
+            tend[t] = tcnt[t] ? e1 : 0;
+            tbeg[t] = (tcnt[t] && toff[t] > 0) ? b1 : 0;
+        }
         pre -= nch;
         if (lane == 0) {
-            for (int t = 0; t < 2; ++t) {
+            for (int t = 0; t < NS; ++t) {
                 NrLaneSlot &T = slots[t];
-                const int want = t ? total - tot0 : tot0;
+                const int want = tend[t] - tbeg[t];
                 int hA = -1, cA2 = 0, nA = 0, npg = 0;
                 const int top0 = top;
                 if (want > 0) {
@@ -371,7 +388,10 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         __syncwarp();
         const int hA = alloc[8 * sl], cA2 = alloc[8 * sl + 1], nA = alloc[8 * sl + 2], npg = alloc[8 * sl + 3];
         const int top0 = alloc[8 * sl + 4];
-        int q = pre - (sl == 1 ? tot0 : 0);         // this lane's first child, within its slot
+        int q = pre;                                // this lane's first child, within its slot
+#pragma unroll
+        for (int t = 0; t < NS; ++t)
+            if (t == sl) q -= tbeg[t];
         double Pm = mass;
         for (int h = 0; h < L; ++h) {
             const uint32_t hp = my_hop[32 * h];

@@ -79,6 +79,13 @@ def test_lane_kernel_wave_schedule(ctx, oracle, target, shift):
     one = ctx.reliability_batch(gs, srcs, dsts, target_width=target, bucket_shift=shift, n_buckets=nb,
                                 capacity=1 << 16, small_kernel="lane1")
     lane_name = "lane2" if shift < 0 else "lane"
+    if shift < 0:                                 # four instances a warp instead of the default two
+        two = ctx.reliability_batch(gs, srcs, dsts, target_width=target, bucket_shift=shift, n_buckets=nb,
+                                    capacity=1 << 16, lane_slots=4)
+        for i, (a, d) in enumerate(zip(lane, two)):
+            assert a.kernel == d.kernel, i
+            for f in FIELDS:
+                assert getattr(a, f) == getattr(d, f), (i, f)
     for i, (g, a, b, c) in enumerate(zip(gs, lane, group, one)):
         assert a.engine == "warp" and b.engine == "warp" and a.spilled == 0
         assert a.kernel == (lane_name if lane_expected(g) else "group"), i
