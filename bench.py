@@ -323,12 +323,14 @@ def main():
         flush_args = (ctypes.c_void_p(flush.data_ptr()), 1, ctypes.c_size_t(192 * 1024 * 1024),
                       ctypes.c_void_p(fs.cuda_stream))
 
+        pipe_opts = nr.make_options(**w["opts"])
+
         def pipelined(steps):
             pending = None
             for k in range(steps):
                 if cudart.cudaMemsetAsync(*flush_args) != 0:
                     raise RuntimeError("cudaMemsetAsync (L2 flush) failed")
-                tk = ctx.submit(batches[k % 2], capacity=w["capacity"], after_stream=fs.cuda_stream, **w["opts"])
+                tk = ctx.submit(batches[k % 2], capacity=w["capacity"], after_stream=fs.cuda_stream, options=pipe_opts)
                 if pending is not None:
                     ctx.wait(pending)
                 pending = tk

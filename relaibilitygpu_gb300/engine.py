@@ -332,7 +332,8 @@ class Context:
                                           C.byref(o), C.byref(r)))
         return Result.from_raw(r)
 
-    def submit(self, batch: "Batch", capacity: int = 0, after_stream: int = 0, **opts) -> int:
+    def submit(self, batch: "Batch", capacity: int = 0, after_stream: int = 0, options: Optional[NrOptions] = None,
+               **opts) -> int:
         """Queue a prepared batch with nr_batch_submit and return its ticket.
 
         The batch's tables are built before this returns; the GPU work runs
@@ -340,8 +341,9 @@ class Context:
         `after_stream` is a raw cudaStream_t (e.g. torch's
         `torch.cuda.current_stream().cuda_stream`): the upload starts after the
         work already queued there.  The batch's results are valid after
-        wait(ticket); do not resubmit the same Batch object before that."""
-        o = self._options(opts)
+        wait(ticket); do not resubmit the same Batch object before that.  `options` (from
+        make_options) replaces the keyword options: a loop of calls then builds them once."""
+        o = options if options is not None else self._options(opts)
         t = C.c_int64()
         _check(lib().nr_batch_submit(self.h, batch.n, batch.arr, batch.sp, batch.dp, int(capacity), C.byref(o),
                                      batch.res, C.c_void_p(after_stream or None), C.byref(t)))
