@@ -353,6 +353,8 @@ def main():
         dist.barrier()
     clocks = sampler.stop()
     r0 = res[0]
+    # the batch's result array is reused by the comparison runs below: keep the timed run's figures
+    grid0, block0 = int(r0.grid_blocks), int(r0.block_threads)
     h2d = sum(r.h2d_bytes for r in res)
     d2h = sum(r.d2h_bytes for r in res)
     stats = {"R": r0.R, "R_plus_esp": r0.R_plus_esp, "esp": r0.esp, "paths": int(r0.paths), "nodes": int(r0.nodes),
@@ -438,7 +440,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": w["name"], "l2": "flushed (512 MB write) before every step",
                    "parallelism": f"replicas x{world}", "engine": stats["engine"], "kernel": stats["kernel"],
-                   "grid": int(r0.grid_blocks), "block": int(r0.block_threads),
+                   "grid": grid0, "block": block0,
                    "autotuned": None if tuned is None else {k: tuned[k] for k in
                                                              ("bucket_shift", "n_buckets", "warps_per_block",
                                                               "pages_per_warp")}},
