@@ -68,6 +68,131 @@ __device__ __forceinline__ uint32_t nr_pick(const uint32_t (&a)[N], int i)
     return r;
 }
 
+// The root record of an instance, at slot 0 of page rpg (all lanes): the mask from p (p <= 0
+// down, p >= 1 up, else unknown, main.cu:717-748; 16 edges a word, each half-warp ORs one word
+// together), the rows (rows 2k and 2k+1 share word k: the topology's table when no edge is
+// certainly down, else lane u gathers its not-down neighbours), mass 1.
+template <int W4>
+__device__ __forceinline__ void nr_lane_root(const NrSmallGraph &g, const unsigned char *gb, const unsigned char *gs,
+                                             uint4 *sl_mask, uint4 *sl_rows, double *sl_mass, int rpg)
+{
+    constexpr int RW = NR_LANE_ROW_WORDS;
+    const int lane = threadIdx.x & 31;
+    const double *pt = reinterpret_cast<const double *>(gb + g.off_p);
+    uint32_t *rw = reinterpret_cast<uint32_t *>(sl_mask + (size_t)rpg * NR_PAGE * W4);
+    bool down = false;
+#pragma unroll
+    for (int e0 = 0; e0 < 64 * W4; e0 += 32) {
+        const int e = e0 + lane;
+        uint32_t v = 0u;
+        if (e < g.e) {
+            const double pe = pt[e];
+            down = down || pe <= 0.0;
+            v = (uint32_t)((pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN)
+                << ((e & 15) << 1);
+        }
+        v |= __shfl_xor_sync(NR_FULL, v, 8);
+        v |= __shfl_xor_sync(NR_FULL, v, 4);
+        v |= __shfl_xor_sync(NR_FULL, v, 2);
+        v |= __shfl_xor_sync(NR_FULL, v, 1);
+        if ((lane & 15) == 0) rw[(e0 >> 4) + (lane >> 4)] = v;
+    }
+    uint32_t *rr = reinterpret_cast<uint32_t *>(sl_rows + (size_t)rpg * NR_PAGE * (RW / 4));
+    if (!__any_sync(NR_FULL, down)) {
+        if (lane < RW) rr[lane] = reinterpret_cast<const uint32_t *>(gs + g.off_rows16)[lane];
+    } else {
+        const int *start = reinterpret_cast<const int *>(gs + g.off_start);
+        const uint32_t *list = reinterpret_cast<const uint32_t *>(gs + g.off_list);
+        uint32_t r = 0;
+        if (lane < g.n)
+            for (int j = start[lane]; j < start[lane + 1]; ++j) {
+                const uint32_t a = list[j];
+                if (pt[a >> 8] > 0.0) r |= 1u << (a & 31u);
+            }
+        const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
+        if (lane < 2 * RW && !(lane & 1)) rr[lane >> 1] = r | (hi << 16);
+    }
+    if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
+}
+
+// One lane's path: BFS from src over the not-down rows (the frontier of level l goes to
+// my_hop[l]; dst is tested against the frontier first, so the level that reaches it is never
+// expanded), then the walk dst -> src (the parent of a node on level l+1 is the smallest node
+// of frontier l adjacent to it; hop l = (u, x) with its edge id replaces frontier l).  Returns
+// the hops L (0 for a dead end or an inactive lane); live = dst reached; nch = the UNKNOWN hops,
+// i.e. the lane's children; bad = a failed internal check (2 levels, 3 parent, 4 edge id).
+template <int NW>
+__device__ __forceinline__ int nr_lane_path(const uint32_t *my_rows, uint32_t *my_hop, const uint32_t (&wc)[NW],
+                                            const uint16_t *eid, int n, int ge, int src, int dst, bool active,
+                                            bool &live, int &nch, int &bad)
+{
+    const int es = n <= 8 ? 8 : 16;                 // edge-id table stride (the host's group width)
+    int L = 0;
+    live = false;
+    nch = 0;
+    bad = 0;
+    if (!active) return 0;
+    if (src == dst) { live = true; return 0; }
+    const uint32_t rd = nr_lane_row(my_rows, dst);
+    uint32_t F = 1u << src, vis = F;
+    for (;;) {                                      // every level adds a node: at most n - 1 levels
+        if (L >= NR_LANE_MAX_N) { bad = 2; return 0; }
+        my_hop[32 * L] = F;
+        if (rd & F) { ++L; live = true; break; }    // dst is on the next level
+        uint32_t nf = 0u;
+        for (uint32_t t = F; t; t &= t - 1u) nf |= nr_lane_row(my_rows, __ffs(t) - 1);
+        nf &= ~vis;
+        if (!nf) return 0;                          // a dead end has no path: no hops, no children
+        vis |= nf;
+        F = nf;
+        ++L;
+    }
+    int x = dst;
+    for (int l = L - 1; l >= 0; --l) {
+        const int u = __ffs(nr_lane_row(my_rows, x) & my_hop[32 * l]) - 1;
+        if (u < 0 || u >= n) { bad = 3; return 0; }
+        const uint32_t e = eid[u * es + x];
+        if ((int)e >= ge) { bad = 4; return 0; }
+        my_hop[32 * l] = e | ((uint32_t)u << 16) | ((uint32_t)x << 24);
+        nch += ((nr_pick(wc, (int)e >> 4) >> ((e & 15) << 1)) & 3u) == 3u;
+        x = u;
+    }
+    return L;
+}
+
+// Child record at slot s: the parent's mask blocks, then the one word that differs (hop edge e
+// down; this thread's later store to the same address wins); the parent's rows less the down
+// edge cu - cv; mass cm.  wv = the parent's (current) mask word of e.
+template <int W4>
+__device__ __forceinline__ void nr_lane_write_child(uint4 *sl_mask, uint4 *sl_rows, double *sl_mass, int s,
+                                                    const uint32_t (&wc)[4 * W4],
+                                                    const uint32_t (&rw)[NR_LANE_ROW_WORDS],
+                                                    const uint32_t *my_rows, int e, uint32_t wv, int cu, int cv,
+                                                    double cm)
+{
+    constexpr int RW = NR_LANE_ROW_WORDS;
+    uint4 *d = sl_mask + (size_t)s * W4;
+#pragma unroll
+    for (int kk = 0; kk < W4; ++kk)
+        d[kk] = make_uint4(wc[4 * kk], wc[4 * kk + 1], wc[4 * kk + 2], wc[4 * kk + 3]);
+    reinterpret_cast<uint32_t *>(d)[e >> 4] = wv & ~(3u << ((e & 15) << 1));
+    const int wu = cu >> 1, wv2 = cv >> 1;
+    const uint32_t bu = 1u << (cv + ((cu & 1) << 4));
+    const uint32_t bv = 1u << (cu + ((cv & 1) << 4));
+    uint4 *dr = sl_rows + (size_t)s * (RW / 4);
+#pragma unroll
+    for (int kk = 0; kk < RW / 4; ++kk)
+        dr[kk] = make_uint4(rw[4 * kk], rw[4 * kk + 1], rw[4 * kk + 2], rw[4 * kk + 3]);
+    uint32_t *drw = reinterpret_cast<uint32_t *>(dr);
+    if (wu == wv2) {
+        drw[wu] = my_rows[32 * wu] & ~(bu | bv);
+    } else {
+        drw[wu] = my_rows[32 * wu] & ~bu;
+        drw[wv2] = my_rows[32 * wv2] & ~bv;
+    }
+    sl_mass[s] = cm;
+}
+
 template <int W4>
 __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpParams P)
 {
@@ -113,10 +238,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
         const unsigned char *gs = P.blob + g.struct_off;
         const double *pt = reinterpret_cast<const double *>(gb + g.off_p);
         const uint16_t *eid = reinterpret_cast<const uint16_t *>(gs + g.off_eid);
-        const int *start = reinterpret_cast<const int *>(gs + g.off_start);
-        const uint32_t *list = reinterpret_cast<const uint32_t *>(gs + g.off_list);
         const int n = g.n, src = g.src, dst = g.dst;
-        const int es = n <= 8 ? 8 : 16;                 // edge-id table stride (the host's group width)
         const long long t0 = nr_globaltimer();
 
         // reset the private queue; the root is the only subproblem
@@ -136,44 +258,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
         }
         top = __shfl_sync(NR_FULL, top, 0);
         rpg = __shfl_sync(NR_FULL, rpg, 0);
-        {
-            // root record from p: p <= 0 down, p >= 1 up, else unknown (main.cu:717-748);
-            // 16 edges a word, each half-warp ORs one word together
-            uint32_t *rw = reinterpret_cast<uint32_t *>(sl_mask + (size_t)rpg * NR_PAGE * W4);
-            bool down = false;
-#pragma unroll
-            for (int e0 = 0; e0 < 64 * W4; e0 += 32) {
-                const int e = e0 + lane;
-                uint32_t v = 0u;
-                if (e < g.e) {
-                    const double pe = pt[e];
-                    down = down || pe <= 0.0;
-                    v = (uint32_t)((pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN)
-                        << ((e & 15) << 1);
-                }
-                v |= __shfl_xor_sync(NR_FULL, v, 8);
-                v |= __shfl_xor_sync(NR_FULL, v, 4);
-                v |= __shfl_xor_sync(NR_FULL, v, 2);
-                v |= __shfl_xor_sync(NR_FULL, v, 1);
-                if ((lane & 15) == 0) rw[(e0 >> 4) + (lane >> 4)] = v;
-            }
-            // the root's rows (rows 2k and 2k+1 share word k): the topology's when no edge is
-            // certainly down, else lane u gathers its not-down neighbours (p > 0)
-            uint32_t *rr = reinterpret_cast<uint32_t *>(sl_rows + (size_t)rpg * NR_PAGE * (RW / 4));
-            if (!__any_sync(NR_FULL, down)) {
-                if (lane < RW) rr[lane] = reinterpret_cast<const uint32_t *>(gs + g.off_rows16)[lane];
-            } else {
-                uint32_t r = 0;
-                if (lane < n)
-                    for (int j = start[lane]; j < start[lane + 1]; ++j) {
-                        const uint32_t a = list[j];
-                        if (pt[a >> 8] > 0.0) r |= 1u << (a & 31u);
-                    }
-                const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
-                if (lane < 2 * RW && !(lane & 1)) rr[lane >> 1] = r | (hi << 16);
-            }
-        }
-        if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
+        nr_lane_root<W4>(g, gb, gs, sl_mask, sl_rows, sl_mass, rpg);
         __syncwarp();
 
         NrLaneAcc &acc = acc_base[lane];
@@ -285,50 +370,10 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                     }
                 }
 
-                // BFS from src over the not-down rows; the frontier of level l goes to my_hop[l]
-                int L = 0;
-                bool live = false;
-                int bad = 0;
-                if (active) {
-                    if (src == dst) {
-                        live = true;
-                    } else {
-                        const uint32_t rd = nr_lane_row(my_rows, dst);
-                        uint32_t F = 1u << src, vis = F;
-                        for (;;) {                  // every level adds a node: at most n - 1 levels
-                            if (L >= NR_LANE_MAX_N) { bad = 2; break; }
-                            my_hop[32 * L] = F;
-                            if (rd & F) { ++L; live = true; break; }     // dst is on the next level
-                            uint32_t nf = 0u;
-                            for (uint32_t t = F; t; t &= t - 1u) nf |= nr_lane_row(my_rows, __ffs(t) - 1);
-                            nf &= ~vis;
-                            if (!nf) break;
-                            vis |= nf;
-                            F = nf;
-                            ++L;
-                        }
-                    }
-                    if (!live) {
-                        acc.dead++;
-                        L = 0;                      // a dead end has no path: no hops, no children
-                    }
-                }
-                // walk dst -> src: the parent of a node on level l+1 is the smallest node of
-                // frontier l adjacent to it; hop l = (u, x) with its edge id replaces frontier l.
-                // nch = the UNKNOWN hops: the lane's children
-                int nch = 0;
-                if (live && !bad) {
-                    int x = dst;
-                    for (int l = L - 1; l >= 0; --l) {
-                        const int u = __ffs(nr_lane_row(my_rows, x) & my_hop[32 * l]) - 1;
-                        if (u < 0 || u >= n) { bad = 3; break; }
-                        const uint32_t e = eid[u * es + x];
-                        if ((int)e >= g.e) { bad = 4; break; }
-                        my_hop[32 * l] = e | ((uint32_t)u << 16) | ((uint32_t)x << 24);
-                        nch += ((nr_pick(wc, (int)e >> 4) >> ((e & 15) << 1)) & 3u) == 3u;
-                        x = u;
-                    }
-                }
+                bool live;
+                int nch, bad;
+                const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, g.e, src, dst, active, live, nch, bad);
+                if (active && !live && !bad) acc.dead++;
 
                 {
                     const unsigned bm = __ballot_sync(NR_FULL, bad != 0);
@@ -400,29 +445,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                         }
                         ++q;
                         if (s >= 0) {
-                            // the parent's words, then the one word that differs (this thread's
-                            // later store to the same address wins)
-                            uint4 *d = sl_mask + (size_t)s * W4;
-#pragma unroll
-                            for (int kk = 0; kk < W4; ++kk)
-                                d[kk] = make_uint4(wc[4 * kk], wc[4 * kk + 1], wc[4 * kk + 2], wc[4 * kk + 3]);
-                            reinterpret_cast<uint32_t *>(d)[ew] = wv & ~(3u << ((e & 15) << 1));
-                            // the child's rows: the parent's less the down edge cu - cv
-                            const int wu = cu >> 1, wv2 = cv >> 1;
-                            const uint32_t bu = 1u << (cv + ((cu & 1) << 4));
-                            const uint32_t bv = 1u << (cu + ((cv & 1) << 4));
-                            uint4 *dr = sl_rows + (size_t)s * (RW / 4);
-#pragma unroll
-                            for (int kk = 0; kk < RW / 4; ++kk)
-                                dr[kk] = make_uint4(rw[4 * kk], rw[4 * kk + 1], rw[4 * kk + 2], rw[4 * kk + 3]);
-                            uint32_t *drw = reinterpret_cast<uint32_t *>(dr);
-                            if (wu == wv2) {
-                                drw[wu] = my_rows[32 * wu] & ~(bu | bv);
-                            } else {
-                                drw[wu] = my_rows[32 * wu] & ~bu;
-                                drw[wv2] = my_rows[32 * wv2] & ~bv;
-                            }
-                            sl_mass[s] = cm;
+                            nr_lane_write_child<W4>(sl_mask, sl_rows, sl_mass, s, wc, rw, my_rows, e, wv, cu, cv, cm);
                         } else if (P.escalate) {
                             abandon = true;
                         } else {                          // queue full: mass to ESP (main.cu:245-252)
@@ -440,12 +463,13 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                     bool has_child = false;
                     double cm = 0.0;
                     int e = 0, cu = 0, cv = 0;
+                    uint32_t wv = 0u;
                     if (h < L) {
                         const uint32_t hp = my_hop[32 * h];
                         e = (int)(hp & 0xffffu);
                         cu = (int)((hp >> 16) & 0xffu);
                         cv = (int)(hp >> 24);
-                        const uint32_t wv = nr_pick(wc, e >> 4);
+                        wv = nr_pick(wc, e >> 4);
                         if (((wv >> ((e & 15) << 1)) & 3u) == 3u) {
                             const double pe = pt[e];
                             cm = __dmul_rn(Pm, __dsub_rn(1.0, pe));
@@ -485,32 +509,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                             const int r = __popc(m & lt_mask);
                             const int s = (r < nA) ? hA * NR_PAGE + cA + r : (hB >= 0 ? hB * NR_PAGE + (r - nA) : -1);
                             if (s >= 0) {
-                                const int ew = e >> 4;
-                                const uint32_t ebits = 3u << ((e & 15) << 1);
-                                uint32_t cw[NW];
-#pragma unroll
-                                for (int k = 0; k < NW; ++k) cw[k] = (k == ew) ? (wc[k] & ~ebits) : wc[k];
-                                uint4 *d = sl_mask + (size_t)s * W4;
-#pragma unroll
-                                for (int k = 0; k < W4; ++k)
-                                    d[k] = make_uint4(cw[4 * k], cw[4 * k + 1], cw[4 * k + 2], cw[4 * k + 3]);
-                                // the child's rows: the parent's less the down edge cu - cv
-                                const int wu = cu >> 1, wv2 = cv >> 1;
-                                const uint32_t bu = 1u << (cv + ((cu & 1) << 4));
-                                const uint32_t bv = 1u << (cu + ((cv & 1) << 4));
-                                uint32_t cr[RW];
-#pragma unroll
-                                for (int k = 0; k < RW; ++k) {
-                                    uint32_t t = rw[k];
-                                    if (k == wu) t &= ~bu;
-                                    if (k == wv2) t &= ~bv;
-                                    cr[k] = t;
-                                }
-                                uint4 *dr = sl_rows + (size_t)s * (RW / 4);
-#pragma unroll
-                                for (int k = 0; k < RW / 4; ++k)
-                                    dr[k] = make_uint4(cr[4 * k], cr[4 * k + 1], cr[4 * k + 2], cr[4 * k + 3]);
-                                sl_mass[s] = cm;
+                                nr_lane_write_child<W4>(sl_mask, sl_rows, sl_mass, s, wc, rw, my_rows, e, wv, cu, cv, cm);
                                 nr_fix_add_mass(qacc, cm);
                                 qcount++;
                             } else if (P.escalate) {

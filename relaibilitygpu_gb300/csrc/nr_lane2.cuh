@@ -123,7 +123,6 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 const NrSmallGraph g = P.inst[ii];
                 const unsigned char *gb = P.blob + g.blob_off;
                 const unsigned char *gs = P.blob + g.struct_off;
-                const double *pt = reinterpret_cast<const double *>(gb + g.off_p);
                 int rpg = 0;
                 if (lane == 0) {
                     S.t0 = nr_globaltimer();
@@ -139,43 +138,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 }
                 top = __shfl_sync(NR_FULL, top, 0);
                 rpg = __shfl_sync(NR_FULL, rpg, 0);
-                {
-                    // root record, as nr_lane_kernel's
-                    uint32_t *rw = reinterpret_cast<uint32_t *>(sl_mask + (size_t)rpg * NR_PAGE * W4);
-                    bool down = false;
-#pragma unroll
-                    for (int e0 = 0; e0 < 64 * W4; e0 += 32) {
-                        const int e = e0 + lane;
-                        uint32_t v = 0u;
-                        if (e < g.e) {
-                            const double pe = pt[e];
-                            down = down || pe <= 0.0;
-                            v = (uint32_t)((pe <= 0.0) ? NR_EDGE_DOWN : (pe >= 1.0) ? NR_EDGE_UP : NR_EDGE_UNKNOWN)
-                                << ((e & 15) << 1);
-                        }
-                        v |= __shfl_xor_sync(NR_FULL, v, 8);
-                        v |= __shfl_xor_sync(NR_FULL, v, 4);
-                        v |= __shfl_xor_sync(NR_FULL, v, 2);
-                        v |= __shfl_xor_sync(NR_FULL, v, 1);
-                        if ((lane & 15) == 0) rw[(e0 >> 4) + (lane >> 4)] = v;
-                    }
-                    uint32_t *rr = reinterpret_cast<uint32_t *>(sl_rows + (size_t)rpg * NR_PAGE * (RW / 4));
-                    if (!__any_sync(NR_FULL, down)) {
-                        if (lane < RW) rr[lane] = reinterpret_cast<const uint32_t *>(gs + g.off_rows16)[lane];
-                    } else {
-                        const int *start = reinterpret_cast<const int *>(gs + g.off_start);
-                        const uint32_t *list = reinterpret_cast<const uint32_t *>(gs + g.off_list);
-                        uint32_t r = 0;
-                        if (lane < g.n)
-                            for (int j = start[lane]; j < start[lane + 1]; ++j) {
-                                const uint32_t a = list[j];
-                                if (pt[a >> 8] > 0.0) r |= 1u << (a & 31u);
-                            }
-                        const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
-                        if (lane < 2 * RW && !(lane & 1)) rr[lane >> 1] = r | (hi << 16);
-                    }
-                }
-                if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
+                nr_lane_root<W4>(g, gb, gs, sl_mask, sl_rows, sl_mass, rpg);
                 nr_acc_zero(accs[s * 32 + lane]);
                 __syncwarp();
             }
@@ -276,7 +239,6 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         const double *pt = reinterpret_cast<const double *>(P.blob + S.blob_off + S.off_p);
         const uint16_t *eid = reinterpret_cast<const uint16_t *>(gs + S.off_eid);
         const int n = S.n, src = S.src, dst = S.dst, ge = S.ge;
-        const int es = n <= 8 ? 8 : 16;
         NrLaneAcc &acc = accs[sl * 32 + lane];
 
         bool active = valid;
@@ -288,46 +250,10 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 active = false;
             }
         }
-        int L = 0;
-        bool live = false;
-        int bad = 0;
-        if (active) {
-            if (src == dst) {
-                live = true;
-            } else {
-                const uint32_t rd = nr_lane_row(my_rows, dst);
-                uint32_t F = 1u << src, vis = F;
-                for (;;) {
-                    if (L >= NR_LANE_MAX_N) { bad = 2; break; }
-                    my_hop[32 * L] = F;
-                    if (rd & F) { ++L; live = true; break; }
-                    uint32_t nf = 0u;
-                    for (uint32_t t = F; t; t &= t - 1u) nf |= nr_lane_row(my_rows, __ffs(t) - 1);
-                    nf &= ~vis;
-                    if (!nf) break;
-                    vis |= nf;
-                    F = nf;
-                    ++L;
-                }
-            }
-            if (!live) {
-                acc.dead++;
-                L = 0;
-            }
-        }
-        int nch = 0;
-        if (live && !bad) {
-            int x = dst;
-            for (int l = L - 1; l >= 0; --l) {
-                const int u = __ffs(nr_lane_row(my_rows, x) & my_hop[32 * l]) - 1;
-                if (u < 0 || u >= n) { bad = 3; break; }
-                const uint32_t e = eid[u * es + x];
-                if ((int)e >= ge) { bad = 4; break; }
-                my_hop[32 * l] = e | ((uint32_t)u << 16) | ((uint32_t)x << 24);
-                nch += ((nr_pick(wc, (int)e >> 4) >> ((e & 15) << 1)) & 3u) == 3u;
-                x = u;
-            }
-        }
+        bool live;
+        int nch, bad;
+        const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
+        if (active && !live && !bad) acc.dead++;
         if (++steps > NR_LANE_STEP_CAP) bad = 1;
         {
             const unsigned bm = __ballot_sync(NR_FULL, bad != 0);
@@ -412,26 +338,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             }
             ++q;
             if (sc >= 0) {
-                uint4 *d = sl_mask + (size_t)sc * W4;
-#pragma unroll
-                for (int kk = 0; kk < W4; ++kk)
-                    d[kk] = make_uint4(wc[4 * kk], wc[4 * kk + 1], wc[4 * kk + 2], wc[4 * kk + 3]);
-                reinterpret_cast<uint32_t *>(d)[ew] = wv & ~(3u << ((e & 15) << 1));
-                const int wu = cu >> 1, wv2 = cv >> 1;
-                const uint32_t bu = 1u << (cv + ((cu & 1) << 4));
-                const uint32_t bv = 1u << (cu + ((cv & 1) << 4));
-                uint4 *dr = sl_rows + (size_t)sc * (RW / 4);
-#pragma unroll
-                for (int kk = 0; kk < RW / 4; ++kk)
-                    dr[kk] = make_uint4(rw[4 * kk], rw[4 * kk + 1], rw[4 * kk + 2], rw[4 * kk + 3]);
-                uint32_t *drw = reinterpret_cast<uint32_t *>(dr);
-                if (wu == wv2) {
-                    drw[wu] = my_rows[32 * wu] & ~(bu | bv);
-                } else {
-                    drw[wu] = my_rows[32 * wu] & ~bu;
-                    drw[wv2] = my_rows[32 * wv2] & ~bv;
-                }
-                sl_mass[sc] = cm;
+                nr_lane_write_child<W4>(sl_mask, sl_rows, sl_mass, sc, wc, rw, my_rows, e, wv, cu, cv, cm);
             } else {                                  // the slot's pages are full: mass to ESP
                 acc.spilled++;
                 nr_fix_add_mass(acc.es, cm);
