@@ -191,10 +191,29 @@ def cpu_baseline(w, threads: int):
                       f"same schedule and stop rule, {used} host threads"}
 
 
+def stored_schedule(w):
+    """The oracle schedule of the autotuner's choice on GB300 for a batch workload: breadth-first
+    waves (one bucket) to the workload's target width."""
+    w["oracle"] = dict(bucket_shift=-1, n_buckets=1, target_width=w["opts"]["target_width"])
+
+
+def stored_tuning(w):
+    """A batch workload with the autotuner's choice on GB300 (breadth-first waves, 2 warps a block,
+    64 pages a warp): the options of --no-autotune, and the oracle schedule they correspond to."""
+    import relaibilitygpu_gb300 as nr
+    tuned = dict(nr.options_dict(nr.make_options(**w["opts"])), bucket_shift=-1, n_buckets=64,
+                 warps_per_block=2, pages_per_warp=64)
+    stored_schedule(w)
+    w["opts"] = tuned
+    return tuned
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     w = workload(args.workload)
+    if w["kind"] == "batch":
+        stored_schedule(w)                # the schedule our arm runs (and its CPU baseline times)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_solve_all(w, threads, 1)
@@ -260,11 +279,7 @@ def main():
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     tuned = None
     if w["kind"] == "batch" and args.no_autotune:
-        # the autotuner's choice on GB300 (breadth-first waves, 2 warps a block, 64 pages a warp)
-        tuned = dict(nr.options_dict(nr.make_options(**w["opts"])), bucket_shift=-1, n_buckets=64,
-                     warps_per_block=2, pages_per_warp=64)
-        w["opts"] = tuned
-        w["oracle"] = dict(bucket_shift=-1, n_buckets=1, target_width=tuned["target_width"])
+        tuned = stored_tuning(w)
     elif w["kind"] == "batch":
         # autotuner (nr_autotune): bucket resolution, pages per warp, warps per block
         tuned, tuned_ms = nr.autotune(ctx, batch, capacity=w["capacity"], **w["opts"])
