@@ -1275,7 +1275,7 @@ static int slot_ready(NrSlot &sl)
 // is the index of gs[0] in the caller's batch (for collected children).
 static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_graph *gs, const int32_t *srcs,
                        const int32_t *dsts, const WarpRunCfg &cfg, nr_result *res, PhaseClock &pc,
-                       cudaStream_t after = nullptr)
+                       cudaStream_t after = nullptr, bool uniform = false)
 {
     constexpr int NCLS = NR_NCLS;
     const bool lane_ok = cfg.lane && !cfg.fork && !cfg.learned && !cfg.dump;
@@ -1288,11 +1288,78 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     S.inst_b.resize(n);
     S.struct_b.resize(n);
     NrSmallGraph *desc = S.desc.data();
+    // staging (the same offsets in pinned host memory and on the device):
+    //   [work counters | tables (instance order) | descriptors (class order) | ids] then [outputs]
+    size_t off_desc = 0, off_ids = 0, up_bytes = 0, off_out = 0;
+    const size_t off_cnt = 0;
+    int class_count[NCLS] = {0};
+    int class_begin[NCLS + 1] = {0};
+    unsigned char *hb = nullptr;
+    NrSmallGraph *hdesc = nullptr;
+    int *hids = nullptr;
+    int rc = NR_OK;
+    const int B = std::max(1, std::min(NR_HOST_BLOCKS, n / 128));
+    auto blk_begin = [&](int b) { return (int)((long long)n * b / B); };
+    if (uniform) {
+        // one topology (the same CSR arrays) for every instance: every instance's tables have the
+        // same size, so the offsets are known without a sizes pass -- instance 0's p, the shared
+        // structural part, then the other instances' p -- and one parallel pass validates,
+        // describes and copies them.  One class, so class order is instance order.
+        int vr = validate_shape(&gs[0], srcs[0], dsts[0]);
+        if (!vr) vr = validate_structure(&gs[0]);
+        if (vr) return vr;
+        NrSmallGraph t;
+        const size_t ib = small_inst_layout(&gs[0], srcs[0], dsts[0], &t);
+        const size_t sb = small_struct_layout(&gs[0], &t, 0);
+        t.rows = rows_mode_of(&gs[0]);
+        if (t.w4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
+        const int G = group_width(gs[0].n_nodes);
+        const int cls = (lane_ok && gs[0].n_nodes <= NR_LANE_MAX_N && t.rows == 1 && t.w4 <= NR_LANE_MAX_W4)
+                            ? NR_LANE_CLS0 + t.w4 - 1
+                            : (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + t.w4 - 1;
+        size_t off = align16(sizeof(int) * NCLS);
+        const size_t tbase = off;
+        off = align16(off + (size_t)n * ib + sb);
+        class_count[cls] = n;
+        for (int j = 0; j < NCLS; ++j) class_begin[j + 1] = class_begin[j] + class_count[j];
+        off_desc = off; off = align16(off + sizeof(NrSmallGraph) * n);
+        off_ids = off; off = align16(off + sizeof(int) * n);
+        up_bytes = off;
+        off_out = off; off = align16(off + sizeof(NrWarpOut) * n);
+        rc = ensure_host(&sl.hbuf, &sl.hbuf_bytes, off);
+        if (rc) return rc;
+        rc = ensure(&sl.wbuf, &sl.wbuf_bytes, off);
+        if (rc) return rc;
+        hb = static_cast<unsigned char *>(sl.hbuf);
+        hdesc = reinterpret_cast<NrSmallGraph *>(hb + off_desc);
+        hids = reinterpret_cast<int *>(hb + off_ids);
+        memset(hb + off_cnt, 0, sizeof(int) * NCLS);
+        t.struct_off = (long long)(tbase + ib);
+        small_fill_struct(&gs[0], &t, hb + t.struct_off);
+        pc.mark("sizes");
+        std::atomic<int> bad(NR_OK);
+        c->parallel_for(B, 1, [&](int b) {
+            for (int i = blk_begin(b), e = blk_begin(b + 1); i < e; ++i) {
+                const int v = validate_shape(&gs[i], srcs[i], dsts[i]);
+                if (v) { bad.store(v); continue; }
+                NrSmallGraph d = t;
+                d.src = srcs[i];
+                d.dst = dsts[i];
+                d.blob_off = (long long)(tbase + (i == 0 ? 0 : ib + sb + (size_t)(i - 1) * ib));
+                d.blob_bytes = (int)(ib + (i == 0 ? sb : 0));
+                if (!small_fill_inst(&gs[i], &d, hb + d.blob_off)) bad.store(NR_ERR_INVALID);
+                desc[i] = d;
+                S.cls[i] = cls;
+                hdesc[i] = d;
+                hids[i] = i;
+            }
+        });
+        if (bad.load() != NR_OK) return bad.load();
+        pc.mark("tables");
+    } else {
     // Host blocks: contiguous instance ranges, one task of the worker pool each.  Two
     // parallel passes (sizes, then offsets and tables) around a serial prefix over blocks.
-    const int B = std::max(1, std::min(NR_HOST_BLOCKS, n / 128));
     S.blk.resize(B);
-    auto blk_begin = [&](int b) { return (int)((long long)n * b / B); };
     std::atomic<int> too_wide(0), invalid(NR_OK);
     c->parallel_for(B, 1, [&](int b) {
         NrHostBlock &k = S.blk[b];
@@ -1347,13 +1414,9 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     if (too_wide.load()) return NR_ERR_UNSUPPORTED;
     pc.mark("sizes");
 
-    // staging (the same offsets in pinned host memory and on the device):
-    //   [work counters | tables (instance order) | descriptors (class order) | ids] then [outputs]
     size_t off = align16(sizeof(int) * NCLS);
-    const size_t off_cnt = 0;
     long long owner_struct = -1;              // struct_off of the last structural part so far
     int owner_rows = 0;                       // and its rows mode
-    int class_count[NCLS] = {0};
     for (int b = 0; b < B; ++b) {
         NrHostBlock &k = S.blk[b];
         k.base = off;
@@ -1367,20 +1430,19 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
             class_count[j] += k.cnt[j];
         }
     }
-    int class_begin[NCLS + 1] = {0};
     for (int j = 0; j < NCLS; ++j) class_begin[j + 1] = class_begin[j] + class_count[j];
     off = align16(off);
-    const size_t off_desc = off; off = align16(off + sizeof(NrSmallGraph) * n);
-    const size_t off_ids = off; off = align16(off + sizeof(int) * n);
-    const size_t up_bytes = off;
-    const size_t off_out = off; off = align16(off + sizeof(NrWarpOut) * n);
-    int rc = ensure_host(&sl.hbuf, &sl.hbuf_bytes, off);
+    off_desc = off; off = align16(off + sizeof(NrSmallGraph) * n);
+    off_ids = off; off = align16(off + sizeof(int) * n);
+    up_bytes = off;
+    off_out = off; off = align16(off + sizeof(NrWarpOut) * n);
+    rc = ensure_host(&sl.hbuf, &sl.hbuf_bytes, off);
     if (rc) return rc;
     rc = ensure(&sl.wbuf, &sl.wbuf_bytes, off);
     if (rc) return rc;
-    unsigned char *hb = static_cast<unsigned char *>(sl.hbuf);
-    NrSmallGraph *hdesc = reinterpret_cast<NrSmallGraph *>(hb + off_desc);
-    int *hids = reinterpret_cast<int *>(hb + off_ids);
+    hb = static_cast<unsigned char *>(sl.hbuf);
+    hdesc = reinterpret_cast<NrSmallGraph *>(hb + off_desc);
+    hids = reinterpret_cast<int *>(hb + off_ids);
     memset(hb + off_cnt, 0, sizeof(int) * NCLS);
     std::atomic<int> bad_p(0);            // a NaN probability
     c->parallel_for(B, 1, [&](int b) {
@@ -1413,6 +1475,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     });
     if (bad_p.load()) return NR_ERR_INVALID;
     pc.mark("tables");
+    }
 
     // launch geometry per class (occupancy cached per kernel and shared-memory size)
     const int warps_pb = cfg.warps_per_block, block = 32 * warps_pb;
@@ -1707,8 +1770,11 @@ extern "C" int nr_batch_submit(nr_context *c, int n, const nr_graph *gs, const i
     PhaseClock pc;
     // graphs of up to 32 nodes only (the usual batch): the warp engine's first host pass
     // validates them as it sizes their tables; else the whole batch is validated here first
-    bool any_wide = false;
-    for (int i = 0; i < n && !any_wide; ++i) any_wide = gs[i].n_nodes > NR_SMALL_MAX_N;
+    bool any_wide = false, uniform = true;   // uniform: one topology (the same CSR arrays) throughout
+    for (int i = 0; i < n && !any_wide; ++i) {
+        any_wide = gs[i].n_nodes > NR_SMALL_MAX_N;
+        uniform = uniform && same_structure_arrays(&gs[i], &gs[0]);
+    }
     int n_wide = 0;
     int rc = any_wide ? batch_validate(c, n, gs, srcs, dsts, o, &n_wide) : batch_options_ok(c, o);
     if (rc) { record_done(c, t, rc); return rc; }
@@ -1723,7 +1789,7 @@ extern "C" int nr_batch_submit(nr_context *c, int n, const nr_graph *gs, const i
     NrSlot &sl = c->slot[(t - 1) % NR_SLOTS];
     if (sl.pending) record_done(c, sl.ticket, slot_finish(c, sl));
     rc = warp_submit(c, sl, 0, n, gs, srcs, dsts, batch_cfg(o, capacity), res, pc,
-                     static_cast<cudaStream_t>(after_stream));
+                     static_cast<cudaStream_t>(after_stream), uniform);
     if (rc) {
         cudaStreamSynchronize(sl.stream);
         record_done(c, t, rc);
