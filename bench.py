@@ -96,7 +96,7 @@ def workload(name: str):
 
 # DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu capture of the same
 # workload (the launch summaries are kept under profiles/).
-TRAFFIC = {"k15batch": 4.237e6, "k10": 136.8e6}
+TRAFFIC = {"k15batch": 4.194e6, "k10": 136.8e6}
 
 
 def item_bytes(n_edges: int) -> int:
