@@ -529,16 +529,17 @@ static void x_expand(xctx *x, const uint32_t *m, double mass, sink_fn sink, void
 /* ------------------------------------------------------------------ */
 typedef struct {
     uint32_t *d;      /* n * rec words */
-    size_t n, cap;
+    size_t n, cap;    /* cap counts words: a batch arena reuses one vector for records of any width */
     ksum mass;
 } ivec;
 
 static int iv_push(ivec *v, const uint32_t *m, double mass, int W)
 {
-    int rec = W + 2;
-    if (v->n == v->cap) {
-        size_t nc = v->cap ? v->cap * 2 : 256;
-        uint32_t *nd = (uint32_t *)realloc(v->d, nc * rec * sizeof(uint32_t));
+    const size_t rec = (size_t)W + 2;
+    if ((v->n + 1) * rec > v->cap) {
+        size_t nc = v->cap ? v->cap * 2 : 256 * rec;
+        while (nc < (v->n + 1) * rec) nc *= 2;
+        uint32_t *nd = (uint32_t *)realloc(v->d, nc * sizeof(uint32_t));
         if (!nd) return -1;
         v->d = nd; v->cap = nc;
     }

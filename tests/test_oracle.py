@@ -249,3 +249,22 @@ def test_k_terminal_decomposition(load_golden_graph, oracle):
         t = oracle.run(gg, 0, 0, terminals=term, target_width=1e-3, bucket_shift=1, n_buckets=64)
         assert t.R <= exact + 1e-15 <= t.R + t.esp + 1e-15
     assert abs(oracle.brute_k(graphs.complete(5, p=0.5), [1]) - 1.0) < 1e-15   # one terminal
+
+
+def test_batch_runner_mixed_mask_widths(oracle):
+    """og_run_batch keeps one set of queue vectors per thread for all its instances: records of a
+    wider mask after a narrower one must fit the storage (it counts words, not records), and every
+    instance equals its own og_run."""
+    from relaibilitygpu_gb300 import graphs
+    gs = [graphs.grid(4, 4, p_range=(0.6, 0.95), seed=1), graphs.complete(12, p_range=(0.5, 0.95), seed=2),
+          graphs.grid(3, 3, p=0.9), graphs.complete(14, p_range=(0.7, 0.99), seed=3)] * 2
+    srcs = [0] * len(gs)
+    dsts = [g.n_nodes - 1 for g in gs]
+    kw = dict(bucket_shift=-1, n_buckets=1, target_width=1e-7, max_nodes=400_000)
+    res = oracle.run_batch(oracle.BatchArgs(gs, srcs, dsts), threads=1, **kw)
+    assert max(res[i].max_wave for i in range(len(gs))) > 4096
+    for i, g in enumerate(gs):
+        o = oracle.run(g, srcs[i], dsts[i], **kw)
+        r = res[i]
+        assert (r.nodes, r.waves, r.max_wave, r.queued, r.R, r.esp) == (o.nodes, o.waves, o.max_wave, o.queued,
+                                                                         o.R, o.esp)
