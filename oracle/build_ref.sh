@@ -3,9 +3,11 @@
 # (test infrastructure: used to pin the oracle; never part of the product).
 #   seq_ref        <- seq/seq.cpp + seq/TYPES.h + seq/GraphRP.h (max-heap path decomposition)
 #   cpu_reference  <- workingPad/cpu_reference.cpp (single-edge factoring, float p)
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference_root]
+# The reference root is the argument, else $NR_REFERENCE_ROOT, else the
+# read-only mount of the build container this recipe was written for.
 set -e
-REF="${1:-/root/reference}"
+REF="${1:-${NR_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/seq/seq.cpp" ]; then

@@ -2,7 +2,7 @@
 
 Run here (where the reference tree is mounted), not on the GPU host:
 
-    python tests/golden/make_golden.py [reference_root]
+    python tests/golden/make_golden.py <reference_root>   (or NR_REFERENCE_ROOT=<root>)
 
 It writes
   graphs/*.txt   reference-format graph files produced by this repo's own
@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 
 from relaibilitygpu_gb300 import graphs as G  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NR_REFERENCE_ROOT", "")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref")
 
 
@@ -112,6 +112,8 @@ def run_cpu_reference(path: str, s: int, t: int):
 
 
 def main():
+    if not REF:
+        raise SystemExit("usage: make_golden.py <reference_root>  (or set NR_REFERENCE_ROOT)")
     gdir = os.path.join(HERE, "graphs")
     os.makedirs(gdir, exist_ok=True)
     have_ref = os.path.isdir(REF)
