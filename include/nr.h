@@ -65,7 +65,8 @@ typedef struct nr_graph {
 /* queue order */
 enum {
     NR_ORDER_AUTO    = 0,   /* waves for exhaustive runs, max-mass buckets when a target width is set */
-    NR_ORDER_WAVES   = 1,   /* breadth-first waves, as the reference's ping-pong queue (main.cu:963-1008) */
+    NR_ORDER_WAVES   = 1,   /* breadth-first waves, as the reference's ping-pong queue (main.cu:963-1008);
+                               with a target width, one bucket whatever bucket_shift says */
     NR_ORDER_MAXMASS = 2,   /* bucketed max-mass priority queue */
     NR_ORDER_LEARNED = 3    /* bucket key and branch order from the learned scorer (never mass) */
 };
@@ -101,7 +102,13 @@ typedef struct nr_options {
     int32_t  warps_per_block; /* 0 = engine default */
     double   timeout_ms;      /* device-side waits give up after this long without progress; 0 = 60 s */
     int32_t  verbose;         /* 1: print the reference's preamble lines on stdout */
-    int32_t  pad0;
+    int32_t  test_fault;      /* tests of the failure paths only; 0 = off (always, in use).
+                                 1: block 0 of the cooperative whole-GPU launch leaves before its
+                                 first grid barrier, so the other blocks' bounded waits run out
+                                 (NR_ERR_TIMEOUT after timeout_ms);
+                                 2: the lane kernels' step bound is one step, so their
+                                 self-check ends the instance (NR_ERR_INTERNAL).
+                                 Nothing faults: every wait and check returns a status. */
     uint64_t max_nodes;       /* per-instance pop budget for the warp engine; truncated runs stop
                                  there with a valid R <= true <= R + ESP bracket, exhaustive runs
                                  hand the instance to the whole-GPU engine; 0 = engine default */
@@ -230,10 +237,12 @@ int  nr_checkpoint_resume(nr_context *ctx, const char *path, const nr_graph *gra
 
 /* Autotuner for batches (no reference counterpart).  Times the warp engine on
  * up to 4096 instances of the batch for each candidate setting -- bucket
- * resolution (bucket_shift -1..2, where -1 is one bucket: breadth-first waves), pages per warp (64 or 512,
- * how much of the queue a warp holds) and warps per block (2, 4, 8) -- and
+ * resolution (bucket_shift -1..2, where -1 is one bucket: breadth-first waves), pages per warp (64, 512
+ * or 4096, how much of the queue a warp holds; never above capacity) and warps per block (2, 4, 8) -- and
  * writes the fastest into *best (based on *opt), with its device time in
- * *best_ms.  Every candidate returns a valid result; the choice changes time
+ * *best_ms.  The bucket resolution is searched only for opt->order ==
+ * NR_ORDER_AUTO with a target width: NR_ORDER_WAVES holds one bucket and
+ * NR_ORDER_MAXMASS / NR_ORDER_LEARNED hold opt's bucket_shift and n_buckets.  Every candidate returns a valid result; the choice changes time
  * and, for truncated runs, where the stop falls. */
 int  nr_autotune(nr_context *ctx, int n_instances, const nr_graph *graphs, const int32_t *srcs,
                  const int32_t *dsts, uint64_t capacity, const nr_options *opt, nr_options *best,
@@ -280,7 +289,11 @@ int  nr_collect_children(nr_context *ctx, int n_instances, const nr_graph *graph
  * capture.  Calls share the array: they are serialised by a lock and each
  * waits for its kernel, so anything else overlapping on the GPU that touched
  * the array would race.  Runs on cudaStreamPerThread; res->ms is in-kernel
- * device time.  capacity is not taken: the array sets it. */
+ * device time.  capacity is not taken: the array sets it.  One warp does the
+ * solve, so every run has a pop budget: opt->max_nodes, or 2^24 pops when it
+ * is 0; a run that reaches it returns NR_OK with res->stop = 3 and a valid
+ * bracket.  NaN probabilities return NR_ERR_INVALID.  The calling thread's
+ * current device is the same after the call as before it. */
 int  nr_reliability_noalloc(const nr_graph *g, int src, int dst, const nr_options *opt, nr_result *res);
 
 /* The reference's result block (workingPad/main.cu:1037-1056) as text.

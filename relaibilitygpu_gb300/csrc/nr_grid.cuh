@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_kernel(NrGridParams 
     nr_acc_zero(acc);
 
     for (int wave = 0; wave < P.max_waves; ++wave) {
+        if (P.test_fault == 1 && blockIdx.x == 0) break;   // tests: the others' barrier waits run out
         unsigned long long n_in = *(volatile unsigned long long *)&P.wave_count[wave];
         if (n_in > cap) n_in = cap;
         if (n_in == 0) break;

@@ -34,7 +34,7 @@
 #define NR_LANE_MAX_W4 2        // a simple graph on <= 16 nodes has <= 120 edges: 8 mask words
 #define NR_LANE_ROW_WORDS 8     // 16 rows of 16 bits, two to a word
 #define NR_LANE_STEP_CAP (1ll << 26)   // steps (pages) per instance: 2^31 subproblems
-#define NR_LANE_STATUS_CHECK 4  // an internal check failed (the host reports NR_ERR_INTERNAL)
+#define NR_LANE_STATUS_CHECK NR_WARP_STATUS_CHECK
 
 // shared memory of one warp
 __host__ __device__ inline size_t nr_lane_shm_bytes(int n_buckets, int pages)
@@ -227,6 +227,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
     double *sl_mass = P.slab_mass + gw * (size_t)NP * NR_PAGE;
     uint4 *sl_rows = reinterpret_cast<uint4 *>(P.slab_rows) + gw * (size_t)NP * NR_PAGE * (RW / 4);
     const bool use_eps = P.eps > 0.0;
+    const long long step_cap = P.step_cap > 0 ? P.step_cap : NR_LANE_STEP_CAP;
 
     for (;;) {
         int ii = 0;
@@ -267,27 +268,30 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
         // queued record is on bucket 0's chain, so the stop test sums that chain instead
         // (lane i takes record i of each page) and pushes and pops keep no account.
         const bool one_bucket = P.shift < 0;
+        int check = 0;                          // which internal check failed (0: none)
         NrFix qacc = (lane == 0 && !one_bucket) ? nr_fix_of(1.0) : nr_fix_zero();
         long long qcount = (lane == 0 && !one_bucket) ? 1 : 0;
         auto chain_sum = [&]() {
             if (!one_bucket) return;
             qacc = nr_fix_zero();
             qcount = 0;
-            for (int pg = sh.heads[0]; pg >= 0; pg = sh.pnext[pg])
+            int pg = sh.heads[0];
+            for (int k = 0; pg >= 0 && k < NP; pg = sh.pnext[pg], ++k)   // a chain holds <= NP pages
                 if (lane < (int)sh.pcnt[pg]) {
                     nr_fix_add_mass(qacc, sl_mass[(size_t)pg * NR_PAGE + lane]);
                     qcount++;
                 }
+            if (pg >= 0) check = 6;                  // longer than the pool: the chain is corrupt
         };
         int waves = 0, status = 0;
         unsigned long long max_wave = 0;
         bool abandon = false;
         long long steps = 0;
-        int check = 0;                          // which internal check failed (0: none)
 
         for (;;) {
             if (P.wave_mode && P.target > 0.0) {     // exact: ESP + queued mass <= target
                 chain_sum();
+                if (check) { status = NR_LANE_STATUS_CHECK; max_wave = (unsigned long long)check; break; }
                 NrFix w = qacc;
                 nr_fix_add(w, acc.et);
                 nr_fix_add(w, acc.es);
@@ -326,7 +330,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                 const int nxt = sh.pnext[pg];
                 wave_items += cnt;
                 // one step: lane i expands record i of the page
-                if (++steps > NR_LANE_STEP_CAP) { check = 1; abandon = true; break; }
+                if (++steps > step_cap) { check = 1; abandon = true; break; }
                 const bool valid = lane < cnt;
                 const size_t slot = (size_t)pg * NR_PAGE + lane;
                 uint32_t wc[NW], rw[RW];
@@ -545,6 +549,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
         }
         const long long t_stop = nr_globaltimer() - t0;
         chain_sum();                                // one bucket: what is left queued
+        if (check && status != NR_LANE_STATUS_CHECK) { status = NR_LANE_STATUS_CHECK; max_wave = (unsigned long long)check; }
 
         const NrFix R = nr_fix_warp_sum(acc.R), et = nr_fix_warp_sum(acc.et), es_ = nr_fix_warp_sum(acc.es);
         const NrFix qm = nr_fix_warp_sum(qacc);

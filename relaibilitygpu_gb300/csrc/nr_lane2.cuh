@@ -69,6 +69,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     double *sl_mass = P.slab_mass + gw * (size_t)NP * NR_PAGE;
     uint4 *sl_rows = reinterpret_cast<uint4 *>(P.slab_rows) + gw * (size_t)NP * NR_PAGE * (RW / 4);
     const bool use_eps = P.eps > 0.0;
+    const long long step_cap = P.step_cap > 0 ? P.step_cap : NR_LANE_STEP_CAP;
 
     for (int p = lane; p < NP; p += 32) { freel[p] = (short)(NP - 1 - p); pnext[p] = -1; pcnt[p] = 0; }
     if (lane < NS) { slots[lane].ii = -1; slots[lane].cur = -1; slots[lane].head = -1; }
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             o.status = check ? NR_LANE_STATUS_CHECK : status;
             P.out[P.inst_id[S.ii]] = o;
             for (int c = 0; c < 2; ++c)                       // both of its chains
-                for (int pg = c ? S.head : S.cur; pg >= 0;) {
+                for (int pg = c ? S.head : S.cur; pg >= 0 && top < NP;) {
                     const int nx = pnext[pg];
                     pnext[pg] = -1;
                     freel[top++] = (short)pg;
@@ -148,11 +149,16 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             if (lane == 0 && S.wave_items > S.max_wave) S.max_wave = S.wave_items;
             NrFix qs = nr_fix_zero();
             long long qn = 0;
-            for (int pg = S.head; pg >= 0; pg = pnext[pg])
+            int pg = S.head;
+            for (int k = 0; pg >= 0 && k < NP; pg = pnext[pg], ++k)   // a chain holds <= NP pages
                 if (lane < (int)pcnt[pg]) {
                     nr_fix_add_mass(qs, sl_mass[(size_t)pg * NR_PAGE + lane]);
                     qn++;
                 }
+            if (pg >= 0) {                           // longer than the pool: the chain is corrupt
+                finish(s, 0, 6, nr_fix_zero(), 0);
+                continue;
+            }
             NrLaneAcc &A = accs[s * 32 + lane];
             int st = -1;
             if (P.target > 0.0) {
@@ -175,7 +181,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         // ---- one step: the next page of as many slots' waves as fit in 32 lanes, starting
         // from a slot that rotates step by step (so no slot waits for long) ----
         int tpg[NS], toff[NS], tcnt[NS];          // per slot: page taken (-1 none), first lane, records
-        int used_lanes = 0;
+        int used_lanes = 0, empty_page = 0;
         bool all_done = true;
 #pragma unroll
         for (int t = 0; t < NS; ++t) { tpg[t] = -1; toff[t] = 0; tcnt[t] = 0; all_done = all_done && slots[t].ii == -2; }
@@ -186,9 +192,22 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             const int cp = slots[t].ii >= 0 ? slots[t].cur : -1;
             if (cp < 0) continue;
             const int c = pcnt[cp];
+            empty_page |= (c == 0);                 // a chain page holds >= 1 record: checked, not assumed
             if (used_lanes + c > NR_PAGE) continue;
             tpg[t] = cp; toff[t] = used_lanes; tcnt[t] = c;
             used_lanes += c;
+        }
+        // Every pass counts toward the step bound, an idle one too, so the loop ends whatever
+        // state the slots are in: past the bound (or on an empty chain page) the live slots end
+        // with a check status, and the instances still to come end the same way at their first
+        // pass.  (After the upkeep every live slot has a page of its current wave, so an idle
+        // pass only follows instances ending: the next upkeep takes new ones or leaves.)
+        if (++steps > step_cap || empty_page) {
+            const int check = empty_page ? 5 : 1;
+#pragma unroll 1
+            for (int t = 0; t < NS; ++t)
+                if (slots[t].ii >= 0) finish(t, 0, check, nr_fix_zero(), 0);
+            continue;
         }
         if (used_lanes == 0) continue;              // the upkeep starts waves and instances
         int s = -1, pg = -1, idx = 0;
@@ -254,7 +273,6 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         int nch, bad;
         const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
         if (active && !live && !bad) acc.dead++;
-        if (++steps > NR_LANE_STEP_CAP) bad = 1;
         {
             const unsigned bm = __ballot_sync(NR_FULL, bad != 0);
             if (bm) {                                   // an internal check failed: end both slots

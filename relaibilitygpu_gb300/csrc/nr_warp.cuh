@@ -29,6 +29,7 @@
 #define NR_WARP_MIN_BLOCKS 3     // resident 256-thread blocks per SM the register budget must allow
 #endif
 #define NR_PAGE 32
+#define NR_WARP_STATUS_CHECK 4   // an internal check failed; max_wave holds which (host: NR_ERR_INTERNAL)
 
 struct NrWarpOut {
     NrFix R, et, es, q;   // exact sums: leaves, eps-truncated, spilled, still queued
@@ -69,6 +70,8 @@ struct NrWarpParams {
     int dump_stride;
     int inst_base;                   // index of this launch's instance 0 in the caller's batch
     int fork;                        // fork branching (informational: the FORK instantiation runs it)
+    long long step_cap;              // lane kernels: steps before the self-check ends an instance
+                                     // (0: NR_LANE_STEP_CAP; the failure-path tests set 1)
 };
 
 __device__ __forceinline__ unsigned long long nr_warp_sum_u64(unsigned long long x)
@@ -258,7 +261,9 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
             __syncwarp();
             ++waves;
             unsigned long long wave_items = 0;
+            int walked = 0;                          // pages of this chain so far: at most NP
             for (int pg = chain; pg >= 0 && !abandon;) {
+                if (++walked > NP) break;            // longer than the pool: the chain is corrupt
                 const int cnt = sh.pcnt[pg];
                 const int nxt = sh.pnext[pg];
                 wave_items += cnt;
@@ -388,6 +393,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
                 __syncwarp();
                 pg = nxt;
             }
+            if (walked > NP) { status = NR_WARP_STATUS_CHECK; max_wave = 6; break; }
             if (abandon) { status = 2; break; }
             if (wave_items > max_wave) max_wave = wave_items;
         }

@@ -51,7 +51,7 @@ class NrOptions(C.Structure):
         ("truncation_eps", C.c_double), ("target_width", C.c_double), ("order", C.c_int32),
         ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("device", C.c_int32),
         ("blocks_per_sm", C.c_int32), ("warps_per_block", C.c_int32), ("timeout_ms", C.c_double),
-        ("verbose", C.c_int32), ("pad0", C.c_int32), ("max_nodes", C.c_uint64),
+        ("verbose", C.c_int32), ("test_fault", C.c_int32), ("max_nodes", C.c_uint64),
         ("pages_per_warp", C.c_int32), ("branching", C.c_int32), ("small_kernel", C.c_int32),
         ("lane_slots", C.c_int32),
     ]
@@ -235,7 +235,7 @@ class _GraphView:
 def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto", bucket_shift: int = 2,
                  n_buckets: int = 256, device: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0,
                  timeout_ms: float = 60000.0, max_nodes: int = 0, pages_per_warp: int = 0, branching: str = "path",
-                 small_kernel: str = "auto", lane_slots: int = 0) -> NrOptions:
+                 small_kernel: str = "auto", lane_slots: int = 0, test_fault: int = 0) -> NrOptions:
     o = NrOptions()
     lib().nr_options_default(C.byref(o))
     o.truncation_eps = float(eps)
@@ -252,6 +252,7 @@ def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto
     o.branching = BRANCHING[branching] if isinstance(branching, str) else int(branching)
     o.small_kernel = SMALL_KERNELS[small_kernel] if isinstance(small_kernel, str) else int(small_kernel)
     o.lane_slots = int(lane_slots)
+    o.test_fault = int(test_fault)
     return o
 
 
@@ -264,7 +265,7 @@ def options_dict(o: NrOptions) -> dict:
                 max_nodes=o.max_nodes, pages_per_warp=o.pages_per_warp,
                 branching={v: k for k, v in BRANCHING.items()}.get(o.branching, "path"),
                 small_kernel={v: k for k, v in SMALL_KERNELS.items()}.get(o.small_kernel, "auto"),
-                lane_slots=o.lane_slots)
+                lane_slots=o.lane_slots, test_fault=o.test_fault)
 
 
 def _check(rc: int) -> None:
