@@ -28,8 +28,14 @@
 //     kernel, but work that overlaps with a call on the GPU and touches the
 //     array (another process cannot: it has its own copy) would race;
 //   * it runs on cudaStreamPerThread and reports the in-kernel device time
-//     (globaltimer) as ms, because timing events are created resources.
+//     (globaltimer) as ms, because timing events are created resources;
+//   * one warp does the whole solve, so every run has a pop budget: max_nodes,
+//     or NR_NOALLOC_DEFAULT_BUDGET (2^24 pops, enough for exhaustive K10) when it
+//     is 0.  A run that reaches it stops with stop = 3 and a valid
+//     R <= true <= R + ESP bracket (the mass still queued is part of ESP);
+//   * the caller's current device is restored before the call returns.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -46,6 +52,7 @@ const void *nr_warp_fork_kernel_ptr_g32(int w4);
 #define NR_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define NR_NOALLOC_MAX_DEVICES 64
 #define NR_NOALLOC_BLOB_MAX (32u << 10)
+#define NR_NOALLOC_DEFAULT_BUDGET (1ull << 24)
 
 static __device__ __align__(256) unsigned char nr_noalloc_scratch[NR_NOALLOC_SCRATCH_BYTES];
 
@@ -56,6 +63,13 @@ unsigned char *g_noalloc_addr[NR_NOALLOC_MAX_DEVICES];
 unsigned char g_noalloc_blob[NR_NOALLOC_BLOB_MAX];   // host staging for the graph tables
 
 size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// Puts the calling thread's current device back when the call returns.
+struct DeviceRestore {
+    int prev = -1;
+    DeviceRestore() { if (cudaGetDevice(&prev) != cudaSuccess) { cudaGetLastError(); prev = -1; } }
+    ~DeviceRestore() { if (prev >= 0) cudaSetDevice(prev); }
+};
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Graph tables in the layout of NrSmallGraph (nr_internal.h), written into
@@ -114,13 +128,18 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     for (int j = 0; j < g->n_arcs; ++j)
         if (g->col_idx[j] < 0 || g->col_idx[j] >= g->n_nodes || g->edge_id[j] < 0 || g->edge_id[j] >= g->n_edges)
             return NR_ERR_INVALID;
+    for (int e = 0; e < g->n_edges; ++e)        // a NaN p would feed NaN masses into the exact sums
+        if (std::isnan(g->edge_p[e])) return NR_ERR_INVALID;
     if (g->n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
     nr_options o;
     if (opt) o = *opt; else nr_options_default(&o);
     const int dev = o.device;
     if (dev < 0 || dev >= NR_NOALLOC_MAX_DEVICES) return NR_ERR_INVALID;
 
+    if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
+
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    DeviceRestore restore;
     if (cudaSetDevice(dev) != cudaSuccess) { cudaGetLastError(); return NR_ERR_CUDA; }
     if (!g_noalloc_addr[dev]) {     // set-up, once per device, with the device current
         void *p = nullptr;
@@ -157,7 +176,6 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     const size_t off_mass = a256(off_mask + (size_t)pages * NR_PAGE * 16 * sg.w4);
     if (off_mass + (size_t)pages * NR_PAGE * sizeof(double) > NR_NOALLOC_SCRATCH_BYTES) return NR_ERR_UNSUPPORTED;
 
-    if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
     const bool exhaustive = !(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED;
     NrWarpParams P;
     P.blob = base;
@@ -173,18 +191,22 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     P.eps = o.truncation_eps > 0 ? o.truncation_eps : 0.0;
     P.target = o.target_width > 0 ? o.target_width : 0.0;
     P.target_fix = nr_fix_of(P.target);
+    // Exhaustive runs take one page at a time (depth first: the queue stays small); the others
+    // run the wave schedule of their order.  Both stop at the budget with their queue intact.
+    const unsigned long long budget = o.max_nodes ? o.max_nodes : NR_NOALLOC_DEFAULT_BUDGET;
     if (exhaustive) {
-        P.wave_mode = 0; P.shift = -1; P.n_buckets = 32; P.max_nodes = o.max_nodes;
+        P.wave_mode = 0; P.shift = -1; P.n_buckets = 32; P.max_nodes = budget;
     } else {
         P.wave_mode = 1; P.shift = o.bucket_shift;
         P.n_buckets = std::min(1024, ((o.n_buckets > 0 ? o.n_buckets : 256) + 31) / 32 * 32);
-        P.max_nodes = o.max_nodes;
+        P.max_nodes = budget;
     }
     P.out = reinterpret_cast<NrWarpOut *>(base + off_out);
     P.learned = 0;
     P.fork = (o.branching == NR_BRANCH_FORK);
     P.dump_feat = nullptr; P.dump_mask = nullptr; P.dump_mass = nullptr; P.dump_inst = nullptr;
     P.dump_count = nullptr; P.dump_cap = 0; P.dump_stride = 0; P.inst_base = 0;
+    P.step_cap = 0;
 
     const size_t smem = nr_warp_shm_bytes(32 / G, sg.w4, P.n_buckets, pages);
     cudaStream_t s = cudaStreamPerThread;
@@ -224,7 +246,9 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     res->capacity = (uint64_t)pages * NR_PAGE;
     res->h2d_bytes = blob + sizeof(sg) + sizeof(int);
     res->d2h_bytes = sizeof(out);
-    res->stop = out.status;
-    if (out.status == 2) return NR_ERR_INTERNAL;
+    // With no hand-over (escalate = 0) a page-mode stop (status 2) can only be the budget: the
+    // queued mass is still counted in ESP, so the bracket is valid, as for a wave-mode budget stop.
+    res->stop = (out.status == 2) ? 3 : out.status;
+    if (out.status < 0 || out.status > 3) return NR_ERR_INTERNAL;
     return NR_OK;
 }
