@@ -1,38 +1,45 @@
 """Benchmark of the GB300 reliability engine (one JSON line on rank 0).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--quick]
 
-Workloads (all synthetic, seeded; numpy PCG64):
-  k15batch (default) -- the metric's configuration: K15 (N=15, E=105), src 0,
-      dst 14, edge p ~ U[0.9, 0.99] FP64, run in plain max-mass order until the
-      ESP width (ESP + queued mass) is <= 1e-6.  One instance needs only ~20-60
-      subproblems, so a step solves a batch of 4096 such instances (seeds
-      0..4095) in one launch; single-instance time-to-bound is reported beside it.
-  k10 -- K10 (N=10, E=45), p ~ U[0.5, 0.95], exhaustive (one solve per step).
-  k15p05, k25p05 -- the reference's own published K15 / K25 p=0.5 runs
-      (breadth-first waves, 77,410,924-slot wave buffers, eps 1e-15).
-  rgg200 -- random geometric graph N=200, E=600 (unit square, terminals the
-      farthest pair), p ~ U[0.9, 0.99]: the whole-GPU bucketed max-mass queue
-      aiming at ESP width <= 1e-5, stopped at a budget of 20M subproblems per
-      step (the bound is far beyond one GPU's queue memory; the line reports
-      the R <= true <= R + ESP bracket reached).
+Headline (the metric's configuration): K15 (N=15, E=105), src 0, dst 14, edge
+p ~ U[0.9, 0.99] FP64, solved until the ESP width (ESP + queued mass) is <= 1e-6
+in breadth-first waves (one bucket; the stop test runs between waves).  One
+instance needs only ~20-60 subproblems, so a step solves 4096 seeded instances
+(seeds 0..4095) in one launch; the autotuner picks the launch geometry (warps
+per block, pages of queue per warp) with the schedule held.  Both arms run
+this schedule, so their `config` objects are identical.
 
 `value` is subproblems (popped nodes, dead ends included) per second of
-device time: the engine's CUDA events on its own stream around the kernels,
-summed over ranks and divided by the slowest rank.  `e2e` is the same metric
-with wall-clock time around the public C call (graph tables host->device,
-results device->host).  L2 is flushed (a 512 MB write) before every step.
+device time: CUDA events on the engine's own stream around its kernels, L2
+flushed (a 512 MB write) before every step.  `time_to_bound_ms` is the batch's
+device time per step (every instance reaches its bound inside it).  `e2e` is
+the same metric through the asynchronous public C API (nr_batch_submit /
+nr_batch_wait) with every step's tables uploaded from pinned host memory and
+its results read back.
+
+`configs` carries the other configurations, each with its own in-run parity
+check against the oracle (oracle/, the CPU restatement of the reference):
+  grid4x4   -- 4x4 grid, p = 0.9, exhaustive; R against 2^24 brute force
+  k10       -- K10, p ~ U[0.5, 0.95], exhaustive; against the single-thread oracle
+  uneven    -- 4096 uneven instances (G(n,m) n~U{8..20}, grids 3x3..6x6), p ~ U[0.8, 0.99],
+               each to ESP width <= 1e-6 or 16,384 subproblems; autotuned batched launch
+               against per-graph launches, device and e2e
+  k25       -- K25, p ~ U[0.9, 0.99], to ESP width <= 1e-5: plain vs learned order
+  rgg200    -- random geometric graph N=200, E=600: the bucketed whole-GPU queue toward
+               1e-5, the bracket at a 20M-subproblem budget
+(--quick skips them.)
 
 --impl reference times the reference algorithm on the host cores: the CPU
 port in oracle/ (the reference's own seq/seq.cpp needs the reference tree,
 which the GPU host does not have), one instance per thread, every host
-thread.  Multi-GPU runs are independent replicas: each rank solves its own
-copy of the workload; no collective on the data path.
+thread, on the same workload and schedule.  Multi-GPU runs are independent
+replicas: each rank solves its own copy of the workload; no collective on the
+data path.
 """
 from __future__ import annotations
 
 import argparse
-import concurrent.futures as cf
 import json
 import os
 import statistics
@@ -48,6 +55,8 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 METRIC = "time to ESP<=1e-6 on K15, learned vs plain order (1 GB300); subproblems/sec"
 UNIT = "subproblems/sec"
 BATCH = 4096
+K15_TARGET = 1e-6
+K15_SCHEDULE = "breadth-first waves (one bucket); stop test ESP + queued mass <= target between waves"
 
 
 def peaks():
@@ -59,49 +68,26 @@ def peaks():
         return 6800.0, "fallback"
 
 
-# ---------------------------------------------------------------------------
-# workloads
-# ---------------------------------------------------------------------------
-def workload(name: str):
+def k15_workload():
     import relaibilitygpu_gb300 as nr
-    if name == "k15batch":
-        gs = [nr.complete(15, p_range=(0.9, 0.99), seed=s) for s in range(BATCH)]
-        return dict(kind="batch", graphs=gs, srcs=[0] * BATCH, dsts=[14] * BATCH, capacity=0,
-                    opts=dict(target_width=1e-6, bucket_shift=2, n_buckets=256),
-                    oracle=dict(bucket_shift=2, n_buckets=256, target_width=1e-6),
-                    name=f"K15 (N=15, E=105) src=0 dst=14 p~U[0.9,0.99] seeds 0..{BATCH - 1}, "
-                         f"max-mass order to ESP width<=1e-6, {BATCH} instances per step")
-    if name in ("k15p05", "k25p05"):
-        n = 15 if name == "k15p05" else 25
-        g = nr.complete(n, p=0.5)
-        return dict(kind="single", graphs=[g], srcs=[0], dsts=[n - 1], capacity=77410924,
-                    opts=dict(eps=1e-15), oracle=dict(eps=1e-15, max_nodes=20_000_000),
-                    name=f"K{n} p=0.5 (COMP{n}-05.txt) src=0 dst={n - 1}, breadth-first waves, queue capacity "
-                         f"77,410,924 per wave buffer, truncation eps 1e-15 (the reference's own published run)")
-    if name == "rgg200":
-        g = nr.rgg(200, 600, p_range=(0.9, 0.99), seed=7)
-        opts = dict(target_width=1e-5, order="maxmass", bucket_shift=2, n_buckets=255, max_nodes=20_000_000,
-                    timeout_ms=120000.0)
-        return dict(kind="single", graphs=[g], srcs=[g.src], dsts=[g.dst], capacity=1 << 28, opts=opts,
-                    oracle=dict(target_width=1e-5, bucket_shift=2, n_buckets=255, max_nodes=1_000_000),
-                    name=f"RGG N=200 E={g.n_edges} (unit square, seed 7) src={g.src} dst={g.dst} (farthest pair) "
-                         f"p~U[0.9,0.99], bucketed max-mass order (4 buckets per octave) toward ESP width <=1e-5, "
-                         f"20M-subproblem budget per step, 2^28-slot arena")
-    if name == "k10":
-        g = nr.complete(10, p_range=(0.5, 0.95), seed=2)
-        return dict(kind="single", graphs=[g], srcs=[0], dsts=[9], capacity=1 << 22, opts=dict(eps=0.0),
-                    oracle=dict(), name="K10 (N=10, E=45) src=0 dst=9 p~U[0.5,0.95] seed 2, exhaustive")
-    raise SystemExit(f"unknown workload {name}")
-
-
-# DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu capture of the same
-# workload (the launch summaries are kept under profiles/).
-TRAFFIC = {"k15batch": 4.194e6, "k10": 136.8e6}
+    gs = [nr.complete(15, p_range=(0.9, 0.99), seed=s) for s in range(BATCH)]
+    return dict(graphs=gs, srcs=[0] * BATCH, dsts=[14] * BATCH,
+                opts=dict(target_width=K15_TARGET, order="waves", n_buckets=64),
+                oracle=dict(bucket_shift=-1, n_buckets=1, target_width=K15_TARGET),
+                config={"workload": f"K15 (N=15, E=105) src=0 dst=14 p~U[0.9,0.99] seeds 0..{BATCH - 1}, "
+                                    f"{BATCH} instances per step, each to ESP width<={K15_TARGET:g}",
+                        "schedule": K15_SCHEDULE, "instances": BATCH, "target_width": K15_TARGET,
+                        "l2": "flushed (512 MB write) before every step"})
 
 
 def item_bytes(n_edges: int) -> int:
     """Algorithmic bytes of one queued subproblem: packed 2-bit mask words + FP64 mass."""
     return 4 * max(1, (2 * n_edges + 31) // 32) + 8
+
+
+# DRAM bytes (read + written) per launch of the headline kernel from one ncu capture of the
+# same workload (summaries under profiles/)
+K15_TRAFFIC = 4.194e6
 
 
 # ---------------------------------------------------------------------------
@@ -159,79 +145,356 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU port (oracle/): instances in parallel, one per host thread
 # ---------------------------------------------------------------------------
-def cpu_solve_all(w, threads: int, reps: int = 1, _cache={}):
+_ORACLE_BATCH = {}
+
+
+def oracle_batch(w, threads: int, **kw):
+    """Solve every instance of a batch workload with the oracle; returns (results, seconds)."""
     import oracle as og
-    og.lib()
+    key = id(w)
+    if key not in _ORACLE_BATCH:
+        _ORACLE_BATCH[key] = og.BatchArgs(w["graphs"], w["srcs"], w["dsts"])
     t0 = time.perf_counter()
-    nodes = 0
-    if w["kind"] == "single":
-        for _ in range(reps):
-            for g, s, d in zip(w["graphs"], w["srcs"], w["dsts"]):
-                nodes += og.run(g, s, d, threads=threads, **w["oracle"]).nodes
-    else:
-        key = id(w)
-        if key not in _cache:
-            _cache[key] = og.BatchArgs(w["graphs"], w["srcs"], w["dsts"])
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            res = og.run_batch(_cache[key], threads=threads, **w["oracle"])
-            nodes += sum(res[i].nodes for i in range(len(w["graphs"])))
-    secs = time.perf_counter() - t0
-    return nodes, secs, threads
+    res = og.run_batch(_ORACLE_BATCH[key], threads=threads, **{**w["oracle"], **kw})
+    return res, time.perf_counter() - t0
 
 
 def cpu_baseline(w, threads: int):
-    # bounded sample: repeat the whole workload until about 2 s of host time has passed
-    nodes, secs, used = cpu_solve_all(w, threads, 1)
+    """Bounded sample: the whole batch, repeated until about 2 s of host time has passed."""
+    res, secs = oracle_batch(w, threads)
+    nodes = sum(res[i].nodes for i in range(len(w["graphs"])))
     reps = max(1, min(50, int(2.0 / max(secs, 1e-3))))
-    if reps > 1:
-        nodes, secs, used = cpu_solve_all(w, threads, reps)
-    return {"value": nodes / secs, "unit": UNIT, "cores": used, "kind": "port",
-            "sample": f"{reps} x the full workload ({len(w['graphs'])} instance(s)), oracle/pathdecomp.c, "
-                      f"same schedule and stop rule, {used} host threads"}
-
-
-def stored_schedule(w):
-    """The oracle schedule of the autotuner's choice on GB300 for a batch workload: breadth-first
-    waves (one bucket) to the workload's target width."""
-    w["oracle"] = dict(bucket_shift=-1, n_buckets=1, target_width=w["opts"]["target_width"])
-
-
-def stored_tuning(w):
-    """A batch workload with the autotuner's choice on GB300 (breadth-first waves, 2 warps a block,
-    64 pages a warp): the options of --no-autotune, and the oracle schedule they correspond to."""
-    import relaibilitygpu_gb300 as nr
-    tuned = dict(nr.options_dict(nr.make_options(**w["opts"])), bucket_shift=-1, n_buckets=64,
-                 warps_per_block=2, pages_per_warp=64)
-    stored_schedule(w)
-    w["opts"] = tuned
-    return tuned
+    total_n, total_s = nodes, secs
+    for _ in range(reps - 1):
+        _, s = oracle_batch(w, threads)
+        total_n += nodes
+        total_s += s
+    return {"value": total_n / total_s, "unit": UNIT, "cores": threads, "kind": "port",
+            "time_to_bound_ms": 1e3 * total_s / reps,
+            "sample": f"{reps} x the full workload ({len(w['graphs'])} instances), oracle/pathdecomp.c, "
+                      f"same schedule and stop rule, {threads} host threads"}
 
 
 def run_reference(args, rank, world):
+    """The reference algorithm (the oracle port) on every host thread, same workload and schedule."""
     if rank != 0:
         return
-    w = workload(args.workload)
-    if w["kind"] == "batch":
-        stored_schedule(w)                # the schedule our arm runs (and its CPU baseline times)
+    w = k15_workload()
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_solve_all(w, threads, 1)
+        oracle_batch(w, threads)
     nodes, secs = 0, 0.0
     for _ in range(args.steps):
-        n, s, _ = cpu_solve_all(w, threads, 1)
-        nodes += n
+        res, s = oracle_batch(w, threads)
+        nodes += sum(res[i].nodes for i in range(BATCH))
         secs += s
     value = nodes / secs
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "impl": "reference",
-            "config": {"workload": w["name"], "parallelism": f"{threads} host threads"},
+            "impl": "reference", "config": w["config"], "time_to_bound_ms": 1e3 * secs / args.steps,
+            "host_threads": threads,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"full workload per step, oracle/pathdecomp.c, {threads} threads"},
+                             "sample": f"the full workload per step, oracle/pathdecomp.c, {threads} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# helpers for the GPU arm
+# ---------------------------------------------------------------------------
+def parity_batch(res, w, idx, oracle_kw=None):
+    """Bit-exact comparison of batch results (raw NrResult array) with the oracle on instances idx:
+    subproblems, waves, widest wave, still queued, R and ESP.  Returns (checked, mismatches)."""
+    import oracle as og
+    bad = []
+    for i in idx:
+        r = res[i]
+        kw = dict(oracle_kw or w["oracle"])
+        if w["graphs"][i].n_nodes > 32:          # the whole-GPU bucket queue keeps at most 255 buckets
+            kw["n_buckets"] = min(255, kw.get("n_buckets", 1))
+        o = og.run(w["graphs"][i], w["srcs"][i], w["dsts"][i], **kw)
+        if (r.nodes, r.iterations, r.max_queue_items, r.queued) != (o.nodes, o.waves, o.max_wave, o.queued) \
+                or r.R != o.R or r.esp != o.esp:
+            bad.append(int(i))
+    return len(idx), bad
+
+
+class Flusher:
+    """L2 flush: a 512 MB write on the current stream before a timed step."""
+
+    def __init__(self, device):
+        import torch
+        self.buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+
+    def __call__(self):
+        import torch
+        self.buf.fill_(1.0)
+        torch.cuda.synchronize()
+
+
+def pipelined_e2e(ctx, w, capacity, opts, flush_buf, steps, device):
+    """Throughput through nr_batch_submit / nr_batch_wait, two batches in flight: every step uploads
+    its inputs from pinned memory and reads its results back; a 192 MB L2 flush (1.5x the L2) runs
+    on its own stream before each step's upload, which is ordered after it."""
+    import ctypes
+    import torch
+    import relaibilitygpu_gb300 as nr
+    batches = [nr.Batch(w["graphs"], w["srcs"], w["dsts"]), nr.Batch(w["graphs"], w["srcs"], w["dsts"])]
+    fs = torch.cuda.Stream(device=f"cuda:{device}")
+    cudart = ctypes.CDLL("libcudart.so.13")
+    cudart.cudaMemsetAsync.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
+    cudart.cudaMemsetAsync.restype = ctypes.c_int
+    flush_args = (ctypes.c_void_p(flush_buf.data_ptr()), 1, ctypes.c_size_t(192 * 1024 * 1024),
+                  ctypes.c_void_p(fs.cuda_stream))
+    o = nr.make_options(**opts)
+
+    def loop(k_steps):
+        pending = None
+        for k in range(k_steps):
+            if cudart.cudaMemsetAsync(*flush_args) != 0:
+                raise RuntimeError("cudaMemsetAsync (L2 flush) failed")
+            tk = ctx.submit(batches[k % 2], capacity=capacity, after_stream=fs.cuda_stream, options=o)
+            if pending is not None:
+                ctx.wait(pending)
+            pending = tk
+        ctx.wait(pending)
+
+    loop(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop(steps)
+    secs = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    per_batch = [sum(bb.res[i].nodes for i in range(bb.n)) for bb in batches]
+    nodes = sum(per_batch[k % 2] for k in range(steps))
+    h2d = sum(bb.res[i].h2d_bytes for bb in batches[:1] for i in range(bb.n))
+    d2h = sum(bb.res[i].d2h_bytes for bb in batches[:1] for i in range(bb.n))
+    return nodes, secs, h2d, d2h
+
+
+def median_us(xs):
+    return 1e3 * statistics.median(xs)
+
+
+# ---------------------------------------------------------------------------
+# the other configurations (each with in-run parity against the oracle)
+# ---------------------------------------------------------------------------
+def cfg_grid4x4(ctx, flush):
+    import oracle as og
+    import relaibilitygpu_gb300 as nr
+    g = nr.grid(4, 4, p=0.9)
+    ms = []
+    for k in range(6):
+        flush()
+        r = ctx.reliability(g, 0, 15)
+        if k >= 3:
+            ms.append(r.ms)
+    t0 = time.perf_counter()
+    brute = og.brute(g, 0, 15)
+    t_brute = time.perf_counter() - t0
+    o = og.run(g, 0, 15)
+    exact = (r.paths, r.nodes, r.iterations, r.max_queue_items) == (o.paths, o.nodes, o.waves, o.max_wave)
+    return {"workload": "4x4 grid (N=16, E=24) src=0 dst=15, p=0.9, exhaustive", "engine": r.engine,
+            "R": r.R, "paths": int(r.paths), "nodes": int(r.nodes), "waves": int(r.iterations),
+            "gpu_ms_median": statistics.median(ms), "subproblems_per_sec": r.nodes / (statistics.median(ms) / 1e3),
+            "parity": {"counts_bit_exact_vs_oracle": exact, "R_equal_oracle": r.R == o.R,
+                       "R_rel_err_vs_brute_force": abs(r.R - brute) / brute,
+                       "brute_force_R": brute, "brute_force_s": t_brute,
+                       "ok": exact and r.R == o.R and abs(r.R - brute) <= 1e-12 * brute}}
+
+
+def cfg_k10(ctx, flush):
+    import oracle as og
+    import relaibilitygpu_gb300 as nr
+    g = nr.complete(10, p_range=(0.5, 0.95), seed=2)
+    ms, walls = [], []
+    for k in range(8):
+        flush()
+        t0 = time.perf_counter()
+        r = ctx.reliability(g, 0, 9, capacity=1 << 22)
+        walls.append(time.perf_counter() - t0)
+        if k >= 3:
+            ms.append(r.ms)
+    t0 = time.perf_counter()
+    o = og.run(g, 0, 9, threads=1)
+    cpu_s = time.perf_counter() - t0
+    gpu_s = statistics.median(ms) / 1e3
+    wall_s = statistics.median(walls[3:])
+    exact = (r.paths, r.nodes, r.leaves, r.dead_ends, r.iterations, r.max_queue_items) == \
+        (o.paths, o.nodes, o.leaves, o.dead, o.waves, o.max_wave)
+    return {"workload": "K10 (N=10, E=45) src=0 dst=9 p~U[0.5,0.95] seed 2, exhaustive", "engine": r.engine,
+            "R": r.R, "paths": int(r.paths), "nodes": int(r.nodes), "waves": int(r.iterations),
+            "gpu_ms_median": 1e3 * gpu_s, "gpu_call_wall_ms_median": 1e3 * wall_s,
+            "subproblems_per_sec": r.nodes / gpu_s,
+            "cpu_single_thread_s": cpu_s, "cpu_subproblems_per_sec": o.nodes / cpu_s,
+            "speedup_vs_single_thread_oracle": cpu_s / gpu_s, "speedup_e2e": cpu_s / wall_s,
+            "gate_50x": cpu_s / gpu_s >= 50.0,
+            "parity": {"counts_bit_exact_vs_oracle": exact, "R_equal_oracle": r.R == o.R,
+                       "ok": exact and r.R == o.R}}
+
+
+UNEVEN_TARGET, UNEVEN_BUDGET = 1e-6, 16384
+
+
+def cfg_uneven(ctx, flush, device):
+    import relaibilitygpu_gb300 as nr
+    gs = nr.batch_instances(BATCH, seed=0)
+    w = dict(graphs=gs, srcs=[g.src for g in gs], dsts=[g.dst for g in gs])
+    batch = nr.Batch(w["graphs"], w["srcs"], w["dsts"])
+    base = dict(target_width=UNEVEN_TARGET, max_nodes=UNEVEN_BUDGET)
+    # graphs above 32 nodes (the 6x6 grids) run one at a time on the whole-GPU engine after the
+    # batched launch; the autotuner times the batched launch on the others
+    small = [i for i in range(BATCH) if gs[i].n_nodes <= 32]
+    wide = [i for i in range(BATCH) if gs[i].n_nodes > 32]
+    tb = nr.Batch([gs[i] for i in small], [w["srcs"][i] for i in small], [w["dsts"][i] for i in small])
+    t0 = time.perf_counter()
+    tuned, tuned_ms = nr.autotune(ctx, tb, capacity=0, **base)
+    t_tune = time.perf_counter() - t0
+    shift = tuned["bucket_shift"]
+    w["oracle"] = dict(bucket_shift=shift, n_buckets=tuned["n_buckets"] if shift >= 0 else 1,
+                       target_width=UNEVEN_TARGET, max_nodes=UNEVEN_BUDGET)
+    ms, ms_batched, ms_wide = [], [], []
+    for k in range(6):
+        flush()
+        res = ctx.run_batch(batch, capacity=0, raw=True, **tuned)
+        if k >= 2:
+            # the batched launch's time (shared by its instances) plus each whole-GPU run's
+            mb = res[small[0]].ms
+            mw = sum(res[i].ms for i in wide)
+            ms_batched.append(mb)
+            ms_wide.append(mw)
+            ms.append(mb + mw)
+    n_step = sum(res[i].nodes for i in range(BATCH))
+    n_small = sum(res[i].nodes for i in small)
+    spilled = [i for i in range(BATCH) if res[i].spilled]
+    kernels = {}
+    for i in range(BATCH):
+        kk = nr.engine.KERNELS.get(res[i].kernel, str(res[i].kernel)) or nr.engine.ENGINES.get(res[i].engine, "?")
+        kernels[kk] = kernels.get(kk, 0) + 1
+    stops = {}
+    for i in range(BATCH):
+        stops[int(res[i].stop)] = stops.get(int(res[i].stop), 0) + 1
+    # parity: every 16th instance that did not spill, bit for bit against the oracle's schedule
+    idx = [i for i in range(0, BATCH, 16) if not res[i].spilled]
+    checked, bad = parity_batch(res, w, idx)
+    dev_s = statistics.median(ms) / 1e3
+    # e2e through the asynchronous API (the general host path: 4096 different topologies)
+    e_nodes, e_secs, h2d, d2h = pipelined_e2e(ctx, w, 0, tuned, flush.buf, 10, device)
+    # per-graph launches against the batched launch, on the first 256 instances
+    first = small[:256]
+    sub = dict(graphs=[gs[i] for i in first], srcs=[w["srcs"][i] for i in first], dsts=[w["dsts"][i] for i in first])
+    sb = nr.Batch(sub["graphs"], sub["srcs"], sub["dsts"])
+    flush()
+    rb = ctx.run_batch(sb, capacity=0, raw=True, **tuned)
+    b_ms = rb[0].ms
+    t0 = time.perf_counter()
+    dev_sum, n_sub = 0.0, 0
+    for g, s_, d_ in zip(sub["graphs"], sub["srcs"], sub["dsts"]):
+        r1 = ctx.reliability(g, s_, d_, capacity=0, **tuned)
+        dev_sum += r1.ms
+        n_sub += r1.nodes
+    wall = time.perf_counter() - t0
+    # CPU: the oracle on every host thread, same schedule and stops
+    import oracle  # noqa: F401  (loaded by oracle_batch)
+    threads = os.cpu_count() or 1
+    _, cpu_s = oracle_batch(w, threads)
+    return {"workload": f"{BATCH} uneven instances (graphs.batch_instances seed 0: half connected G(n,m) "
+                        f"n~U{{8..20}} mean degree U[3,8], half grids 3x3..6x6), p~U[0.8,0.99], random distinct "
+                        f"terminals; each to ESP width<={UNEVEN_TARGET:g} or {UNEVEN_BUDGET} subproblems "
+                        f"(checked between waves), whichever first",
+            "substitution": "exhaustive runs of the 5x6 and 6x6 grids need > 2.7e8 subproblems each, so the mix "
+                            "runs to a target width with a per-instance budget",
+            "autotuned": {k: tuned[k] for k in ("bucket_shift", "n_buckets", "warps_per_block", "pages_per_warp")},
+            "autotune_s": t_tune, "kernels": kernels, "stops": {str(k): v for k, v in stops.items()},
+            "subproblems_per_step": n_step, "gpu_ms_median": 1e3 * dev_s,
+            "subproblems_per_sec": n_step / dev_s,
+            "batched_launch": {"instances": len(small), "ms_median": statistics.median(ms_batched),
+                               "subproblems": n_small,
+                               "subproblems_per_sec": n_small / (statistics.median(ms_batched) / 1e3)},
+            "whole_gpu_one_at_a_time": {"instances": len(wide), "ms_median_sum": statistics.median(ms_wide)},
+            "e2e": {"subproblems_per_sec": e_nodes / e_secs, "steps": 10, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "over_device": (e_nodes / e_secs) / (n_step / dev_s)},
+            "per_graph_launches": {"instances": "the first 256 of at most 32 nodes", "batched_launch_ms": b_ms, "wall_ms": 1e3 * wall,
+                                   "device_ms_sum": dev_sum, "batched_speedup_device": dev_sum / b_ms,
+                                   "batched_speedup_wall": 1e3 * wall / b_ms},
+            "cpu": {"threads": threads, "seconds": cpu_s, "subproblems_per_sec": n_step / cpu_s},
+            "spilled_instances": len(spilled),
+            "parity": {"checked": checked, "mismatches": bad, "ok": not bad}}
+
+
+def cfg_k25(ctx, flush):
+    import relaibilitygpu_gb300 as nr
+    from relaibilitygpu_gb300 import learned as LR
+    n_inst = 1024
+    gs = [nr.complete(25, p_range=(0.9, 0.99), seed=s) for s in range(n_inst)]
+    w = dict(graphs=gs, srcs=[0] * n_inst, dsts=[24] * n_inst)
+    batch = nr.Batch(gs, w["srcs"], w["dsts"])
+    out = {"workload": f"K25 (N=25, E=300) src=0 dst=24 p~U[0.9,0.99] seeds 0..{n_inst - 1}, "
+                       f"each to ESP width<=1e-5"}
+    orders = {"plain_maxmass": dict(order="maxmass", bucket_shift=0, n_buckets=64),
+              "breadth_first": dict(order="waves", n_buckets=64)}
+    have_model = os.path.exists(LR.DEFAULT_MODEL)
+    if have_model:
+        LR.set_model(ctx, LR.load())
+        orders["learned"] = dict(order="learned", bucket_shift=0, n_buckets=64)
+    for name, kw in orders.items():
+        lat, nodes = [], []
+        for s in range(16):
+            r = ctx.reliability(gs[s], 0, 24, target_width=1e-5, **kw)
+            lat.append(r.time_to_bound_ms)
+            nodes.append(r.nodes)
+        ms = []
+        for k in range(5):
+            flush()
+            res = ctx.run_batch(batch, raw=True, target_width=1e-5, **kw)
+            if k >= 2:
+                ms.append(res[0].ms)
+        n_b = sum(res[i].nodes for i in range(n_inst))
+        rec = {"single_in_kernel_us_median": median_us(lat), "single_nodes_mean": statistics.mean(nodes),
+               "batch_ms_median": statistics.median(ms), "batch_subproblems": n_b,
+               "batch_subproblems_per_sec": n_b / (statistics.median(ms) / 1e3)}
+        if name != "learned":
+            oracle_kw = dict(bucket_shift=kw.get("bucket_shift", -1) if kw["order"] != "waves" else -1,
+                             n_buckets=64 if kw["order"] != "waves" else 1, target_width=1e-5)
+            checked, bad = parity_batch(res, w, list(range(0, n_inst, 32)), oracle_kw)
+            rec["parity"] = {"checked": checked, "mismatches": bad, "ok": not bad}
+        out[name] = rec
+    if have_model:
+        out["learned_over_plain_batch_time"] = out["learned"]["batch_ms_median"] / out["plain_maxmass"]["batch_ms_median"]
+    return out
+
+
+def cfg_rgg200(ctx, flush):
+    import oracle as og
+    import relaibilitygpu_gb300 as nr
+    g = nr.rgg(200, 600, p_range=(0.9, 0.99), seed=7)
+    kw = dict(target_width=1e-5, order="maxmass", bucket_shift=2, n_buckets=255, timeout_ms=120000.0)
+    budget = 20_000_000
+    ms = []
+    for k in range(3):
+        flush()
+        r = ctx.reliability(g, g.src, g.dst, capacity=1 << 28, max_nodes=budget, **kw)
+        if k >= 1:
+            ms.append(r.ms)
+    # parity at a 1M budget against the oracle's bucketed schedule (all host threads)
+    small = 1_000_000
+    r1 = ctx.reliability(g, g.src, g.dst, capacity=1 << 28, max_nodes=small, **kw)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    o = og.run(g, g.src, g.dst, target_width=1e-5, bucket_shift=2, n_buckets=255, max_nodes=small, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    exact = (r1.nodes, r1.leaves, r1.dead_ends, r1.iterations, r1.queued) == \
+        (o.nodes, o.leaves, o.dead, o.waves, o.queued) and r1.R == o.R and r1.esp == o.esp
+    dev_s = statistics.median(ms) / 1e3
+    return {"workload": f"RGG N=200 E={g.n_edges} (unit square, seed 7) src={g.src} dst={g.dst} (farthest pair) "
+                        f"p~U[0.9,0.99], bucketed max-mass queue (4 buckets per octave) toward ESP width<=1e-5, "
+                        f"stopped at {budget:,} subproblems; 2^28-slot arena",
+            "engine": r.engine, "R": r.R, "R_plus_esp": r.R_plus_esp, "esp": r.esp, "nodes": int(r.nodes),
+            "waves": int(r.iterations), "stop": int(r.stop), "gpu_ms_median": 1e3 * dev_s,
+            "subproblems_per_sec": r.nodes / dev_s,
+            "cpu": {"threads": threads, "budget": small, "seconds": cpu_s, "subproblems_per_sec": o.nodes / cpu_s},
+            "parity": {"budget": small, "bit_exact_vs_oracle": exact, "ok": exact}}
 
 
 # ---------------------------------------------------------------------------
@@ -241,12 +504,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="k15batch")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-compare", action="store_true",
-                    help="k15batch: skip the plain / learned / breadth-first order comparison")
-    ap.add_argument("--no-autotune", action="store_true",
-                    help="batch workloads: use the stored tuned settings instead of running nr_autotune")
+    ap.add_argument("--quick", action="store_true", help="only the headline line (no configs, orders or CPU leg)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -273,175 +531,77 @@ def main():
     from relaibilitygpu_gb300 import build as nb
     nb.build()
     torch.cuda.set_device(local)
-    w = workload(args.workload)
+    w = k15_workload()
     ctx = nr.Context(local)
     batch = nr.Batch(w["graphs"], w["srcs"], w["dsts"])
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    tuned = None
-    if w["kind"] == "batch" and args.no_autotune:
-        tuned = stored_tuning(w)
-    elif w["kind"] == "batch":
-        # autotuner (nr_autotune): bucket resolution, pages per warp, warps per block
-        tuned, tuned_ms = nr.autotune(ctx, batch, capacity=w["capacity"], **w["opts"])
-        w["opts"] = tuned
-        w["oracle"] = dict(bucket_shift=tuned["bucket_shift"],
-                           n_buckets=tuned["n_buckets"] if tuned["bucket_shift"] >= 0 else 1,
-                           target_width=tuned["target_width"])
+    flush = Flusher(local)
+    # autotuner (nr_autotune): warps per block and pages per warp, the schedule held
+    tuned, tuned_ms = nr.autotune(ctx, batch, capacity=0, **w["opts"])
 
     def call():
-        if w["kind"] == "batch":
-            return ctx.run_batch(batch, capacity=w["capacity"], raw=True, **w["opts"])
-        return [ctx.reliability(w["graphs"][0], w["srcs"][0], w["dsts"][0], capacity=w["capacity"],
-                                **w["opts"])._raw]
+        return ctx.run_batch(batch, capacity=0, raw=True, **tuned)
 
     for _ in range(max(3, args.warmup)):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
+        flush()
         call()
     sampler = ClockSampler(local)
     sampler.start()
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
-    dev_ms, wall_s, nodes, abytes = 0.0, 0.0, 0, 0
+    dev_ms, wall_s, nodes = 0.0, 0.0, 0
     per_step = []
     for _ in range(args.steps):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
+        flush()
         t0 = time.perf_counter()
         res = call()
         wall_s += time.perf_counter() - t0
         ms = res[0].ms
-        n_step = sum(r.nodes for r in res)
-        b_step = sum((r.nodes + max(0, r.nodes - 1 + r.queued)) * item_bytes(r.n_edges) for r in res)
+        n_step = sum(res[i].nodes for i in range(BATCH))
+        b_step = sum((res[i].nodes + max(0, res[i].nodes - 1 + res[i].queued)) * item_bytes(res[i].n_edges)
+                     for i in range(BATCH))
         dev_ms += ms
         nodes += n_step
-        abytes += b_step
         per_step.append((ms, n_step, b_step))
     torch.cuda.synchronize()
-    # e2e through the asynchronous API: two batches in flight, so the host builds one step's
-    # tables while the GPU runs the step before.  Every step still uploads its inputs from
-    # pinned host memory and reads its results back; the L2 flush of each step runs on its
-    # own stream and the step's upload is ordered after it.
-    e2e_pipe = None
-    if w["kind"] == "batch":
-        batches = [batch, nr.Batch(w["graphs"], w["srcs"], w["dsts"])]
-        fs = torch.cuda.Stream(device=f"cuda:{local}")
-        # 192 MB (1.5x the 129 MB L2) evicts the previous steps' lines; a bigger write would only
-        # take HBM time from the step running beside it.  The write is a cudaMemsetAsync on the
-        # flush stream, issued through the CUDA runtime that libnr.so links (a few microseconds of
-        # host time, where a torch fill under a stream context costs tens)
-        import ctypes
-        cudart = ctypes.CDLL("libcudart.so.13")
-        cudart.cudaMemsetAsync.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
-        cudart.cudaMemsetAsync.restype = ctypes.c_int
-        flush_args = (ctypes.c_void_p(flush.data_ptr()), 1, ctypes.c_size_t(192 * 1024 * 1024),
-                      ctypes.c_void_p(fs.cuda_stream))
-
-        pipe_opts = nr.make_options(**w["opts"])
-
-        def pipelined(steps):
-            pending = None
-            for k in range(steps):
-                if cudart.cudaMemsetAsync(*flush_args) != 0:
-                    raise RuntimeError("cudaMemsetAsync (L2 flush) failed")
-                tk = ctx.submit(batches[k % 2], capacity=w["capacity"], after_stream=fs.cuda_stream, options=pipe_opts)
-                if pending is not None:
-                    ctx.wait(pending)
-                pending = tk
-            ctx.wait(pending)
-
-        pipelined(max(3, args.warmup))
-        torch.cuda.synchronize()
-        # a pipelined call stream is measured in its steady state: at least 50 steps, so the
-        # filling and draining of the two-batch pipeline are a small part of the time
-        e2e_steps = max(args.steps, 50)
-        t0 = time.perf_counter()
-        pipelined(e2e_steps)
-        t_pipe = time.perf_counter() - t0
-        torch.cuda.synchronize()
-        # every step solves the same instances: count the subproblems of each batch's last step
-        per_batch = [sum(bb.res[i].nodes for i in range(bb.n)) for bb in batches]
-        n_pipe = sum(per_batch[k % 2] for k in range(e2e_steps))
-        e2e_pipe = (n_pipe, t_pipe)
-    if dist is not None:
-        dist.barrier()
-    clocks = sampler.stop()
     r0 = res[0]
-    # the batch's result array is reused by the comparison runs below: keep the timed run's figures
-    grid0, block0 = int(r0.grid_blocks), int(r0.block_threads)
-    h2d = sum(r.h2d_bytes for r in res)
-    d2h = sum(r.d2h_bytes for r in res)
+    launch = {"engine": nr.engine.ENGINES.get(r0.engine, r0.engine),
+              "kernel": nr.engine.KERNELS.get(r0.kernel, r0.kernel), "grid": int(r0.grid_blocks),
+              "block": int(r0.block_threads),
+              "autotuned": {k: tuned[k] for k in ("warps_per_block", "pages_per_warp")}, "autotune_ms": tuned_ms}
     stats = {"R": r0.R, "R_plus_esp": r0.R_plus_esp, "esp": r0.esp, "paths": int(r0.paths), "nodes": int(r0.nodes),
              "iterations": int(r0.iterations), "queued": int(r0.queued), "spilled": int(r0.spilled),
              "stop": {0: "queue empty", 1: "target width met", 3: "node budget"}.get(int(r0.stop), int(r0.stop)),
-             "engine": nr.engine.ENGINES.get(r0.engine, r0.engine),
-             "kernel": nr.engine.KERNELS.get(r0.kernel, r0.kernel), "nodes_per_step": nodes // args.steps}
+             "nodes_per_step": nodes // args.steps}
+    h2d = sum(res[i].h2d_bytes for i in range(BATCH))
+    d2h = sum(res[i].d2h_bytes for i in range(BATCH))
+    checked, bad = parity_batch(res, w, list(range(0, BATCH, 64)))
+    parity = {"checked": checked, "mismatches": bad, "ok": not bad,
+              "what": "subproblems, waves, widest wave, queued, R and ESP bit-exact against the oracle"}
+    e2e_nodes, e2e_secs, _, _ = pipelined_e2e(ctx, w, 0, tuned, flush.buf, max(args.steps, 50), local)
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
 
-    # single-instance time-to-bound (latency): plain max-mass order vs the learned order
-    ttb = None
-    if args.workload == "k15batch" and not args.no_compare:
-        from relaibilitygpu_gb300 import learned as LR
-
-        # the order comparison runs at one bucket resolution (one bucket per factor of two), since
-        # with a single bucket (breadth-first waves) there is nothing for a priority to reorder
-        cmp_opts = {k: v for k, v in w["opts"].items() if k not in ("order", "bucket_shift", "n_buckets")}
-        cmp_opts.update(bucket_shift=0, n_buckets=64)
-
-        def latency(order, **kw):
-            tk, tb, nd = [], [], []
-            for s in range(16):
-                r = ctx.reliability(w["graphs"][s], 0, 14, order=order, **{**cmp_opts, **kw})
-                tk.append(r.ms)
-                tb.append(r.time_to_bound_ms)
-                nd.append(r.nodes)
-            return {"kernel_us_median": 1e3 * statistics.median(tk),
-                    "in_kernel_us_median": 1e3 * statistics.median(tb),
-                    "nodes_mean": statistics.mean(nd)}
-
-        def batch_run(order):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            rr = ctx.run_batch(batch, capacity=w["capacity"], raw=True, order=order, **cmp_opts)
-            nn = sum(rr[i].nodes for i in range(len(w["graphs"])))
-            return {"ms": rr[0].ms, "nodes": nn, "subproblems_per_sec": nn / (rr[0].ms / 1e3)}
-
-        def per_graph_launches():
-            # the same 4096 instances one call (one launch) each, with the batch's tuned settings
-            torch.cuda.synchronize()
+    orders, configs = None, None
+    if not args.quick:
+        orders = k15_orders(ctx, w, batch, tuned, flush)
+        configs = {}
+        for name, fn in (("grid4x4", lambda: cfg_grid4x4(ctx, flush)), ("k10", lambda: cfg_k10(ctx, flush)),
+                         ("uneven", lambda: cfg_uneven(ctx, flush, local)), ("k25", lambda: cfg_k25(ctx, flush)),
+                         ("rgg200", lambda: cfg_rgg200(ctx, flush))):
             t0 = time.perf_counter()
-            nn, dev = 0, 0.0
-            for g, s_, d_ in zip(w["graphs"], w["srcs"], w["dsts"]):
-                r = ctx.reliability(g, s_, d_, capacity=w["capacity"], **w["opts"])
-                nn += r.nodes
-                dev += r.ms
-            wall = time.perf_counter() - t0
-            return {"launches": len(w["graphs"]), "wall_ms": 1e3 * wall, "device_ms_sum": dev,
-                    "subproblems_per_sec_wall": nn / wall, "subproblems_per_sec_device": nn / (dev / 1e3)}
-
-        try:
-            ttb = {"plain": latency("maxmass"), "learned": None, "instances": 16,
-                   "breadth_first": latency("maxmass", bucket_shift=-1),
-                   "fork_branching": latency("maxmass", branching="fork"),
-                   "plain_batch": batch_run("maxmass"),
-                   "per_graph_launches": per_graph_launches()}
-        except Exception as exc:                     # keep the bench line; report the failure
-            ttb = {"plain": f"failed: {exc}", "learned": None, "instances": 16}
-        if os.path.exists(LR.DEFAULT_MODEL) and isinstance(ttb["plain"], dict):
-            LR.set_model(ctx, LR.load())
-            ttb["learned"] = latency("learned")
-            ttb["learned_batch"] = batch_run("learned")
-        elif not os.path.exists(LR.DEFAULT_MODEL):
-            ttb["learned"] = "no model file (python -m relaibilitygpu_gb300.learned train)"
+            try:
+                configs[name] = fn()
+            except Exception as exc:                    # keep the bench line; report the failure
+                configs[name] = {"failed": f"{type(exc).__name__}: {exc}"}
+            configs[name]["bench_wall_s"] = time.perf_counter() - t0
 
     t_dev = dev_ms / 1e3
     # replicas: units add up over ranks, the slowest rank sets the time (no data-path collective)
     from relaibilitygpu_gb300 import replicas
-    red = {"nodes": float(nodes), "t_dev_max": t_dev, "wall_max": wall_s}
-    if e2e_pipe is not None:
-        red.update(pipe_nodes=float(e2e_pipe[0]), pipe_wall_max=e2e_pipe[1])
-    tot = replicas.reduce_totals(red)
-    tot_nodes, t_dev, wall_s = tot["nodes"], tot["t_dev_max"], tot["wall_max"]
+    tot = replicas.reduce_totals({"nodes": float(nodes), "t_dev_max": t_dev, "wall_max": wall_s,
+                                  "pipe_nodes": float(e2e_nodes), "pipe_wall_max": e2e_secs})
     if rank != 0:
         ctx.close()
         if dist is not None:
@@ -450,40 +610,76 @@ def main():
     peak, peak_kind = peaks()
     achieved = statistics.mean(b / (ms / 1e3) / 1e9 for ms, _, b in per_step)
     line = {
-        "metric": METRIC, "value": tot_nodes / t_dev, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": max(3, args.warmup), "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": w["name"], "l2": "flushed (512 MB write) before every step",
-                   "parallelism": f"replicas x{world}", "engine": stats["engine"], "kernel": stats["kernel"],
-                   "grid": grid0, "block": block0,
-                   "autotuned": None if tuned is None else {k: tuned[k] for k in
-                                                             ("bucket_shift", "n_buckets", "warps_per_block",
-                                                              "pages_per_warp")}},
+        "metric": METRIC, "value": tot["nodes"] / tot["t_dev_max"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": 1e3 * tot["t_dev_max"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": w["config"],
+        "time_to_bound_ms": 1e3 * t_dev / args.steps,
+        "launch": launch,
         "result": stats,
-        "time_to_bound": ttb,
+        "parity": parity,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": TRAFFIC.get(args.workload),
+                     "frac": achieved / peak, "traffic": K15_TRAFFIC,
                      "note": f"achieved = algorithmic bytes (4W+8 per queued subproblem, written once and "
                              f"read once) / kernel time; peak {peak_kind} copy bandwidth; traffic = DRAM "
-                             f"bytes read + written per launch in one ncu capture (profiles/), the queue "
-                             f"itself stays in L2"},
-        "e2e": ({"value": tot["pipe_nodes"] / tot["pipe_wall_max"], "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                 "d2h_bytes_per_step": int(d2h),
-                 "api": "nr_batch_submit / nr_batch_wait, two batches in flight; L2 flushed (192 MB write) before "
-                        "every step's upload, on its own stream, the upload ordered after it",
-                 "steps": e2e_steps, "one_call_at_a_time": tot_nodes / wall_s}
-                if e2e_pipe is not None else
-                {"value": tot_nodes / wall_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                 "d2h_bytes_per_step": int(d2h), "api": "one synchronous call per step"}),
-        "gpu_launches": args.steps * (len({(r.n_nodes, r.mask_words) for r in res}) if w["kind"] == "batch" else 1),
+                             f"bytes read + written per launch in one ncu capture (profiles/); the queue "
+                             f"stays in L2, so the binding limit is instruction issue (profiles/)"},
+        "e2e": {"value": tot["pipe_nodes"] / tot["pipe_wall_max"], "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "api": "nr_batch_submit / nr_batch_wait, two batches in flight; L2 flushed (192 MB write) before "
+                       "every step's upload, on its own stream, the upload ordered after it",
+                "steps": max(args.steps, 50), "one_call_at_a_time": tot["nodes"] / tot["wall_max"]},
+        "gpu_launches": args.steps,
         "clocks": clocks,
     }
-    if not args.no_cpu_baseline:
+    if orders is not None:
+        line["orders"] = orders
+        line["configs"] = configs
         line["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
     print(json.dumps(line), flush=True)
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def k15_orders(ctx, w, batch, tuned, flush):
+    """K15 time-to-bound under each order: single instances (in-kernel time, 16 seeds) and the
+    4096-instance batch (device time); plain max-mass is the learned order's judge."""
+    from relaibilitygpu_gb300 import learned as LR
+    cmp_opts = {k: v for k, v in tuned.items() if k not in ("order", "bucket_shift", "n_buckets")}
+
+    def latency(**kw):
+        tk, tb, nd = [], [], []
+        for s in range(16):
+            r = ctx.reliability(w["graphs"][s], 0, 14, **{**cmp_opts, **kw})
+            tk.append(r.ms)
+            tb.append(r.time_to_bound_ms)
+            nd.append(r.nodes)
+        return {"kernel_us_median": median_us(tk), "in_kernel_us_median": median_us(tb),
+                "nodes_mean": statistics.mean(nd)}
+
+    def batch_run(**kw):
+        flush()
+        rr = ctx.run_batch(batch, capacity=0, raw=True, **{**cmp_opts, **kw})
+        nn = sum(rr[i].nodes for i in range(BATCH))
+        return {"ms": rr[0].ms, "nodes": nn, "subproblems_per_sec": nn / (rr[0].ms / 1e3),
+                "kernel": __import__("relaibilitygpu_gb300").engine.KERNELS.get(rr[0].kernel, "")}
+
+    plain = dict(order="maxmass", bucket_shift=0, n_buckets=64)
+    out = {"instances_single": 16,
+           "breadth_first": {"single": latency(order="waves", n_buckets=64), "batch": batch_run(order="waves", n_buckets=64)},
+           "plain_maxmass": {"single": latency(**plain), "batch": batch_run(**plain)},
+           "fork_branching": {"single": latency(branching="fork", **plain)}}
+    if os.path.exists(LR.DEFAULT_MODEL):
+        LR.set_model(ctx, LR.load())
+        learned = dict(order="learned", bucket_shift=0, n_buckets=64)
+        out["learned"] = {"single": latency(**learned), "batch": batch_run(**learned)}
+        out["learned_over_plain_batch_time"] = out["learned"]["batch"]["ms"] / out["plain_maxmass"]["batch"]["ms"]
+    # the autotuner's own choice when the order is left to it (bucket resolution searched too)
+    best, best_ms = __import__("relaibilitygpu_gb300").autotune(ctx, batch, capacity=0, target_width=K15_TARGET)
+    out["autotune_search_all_orders"] = {"bucket_shift": best["bucket_shift"], "warps_per_block": best["warps_per_block"],
+                                         "pages_per_warp": best["pages_per_warp"], "ms": best_ms}
+    return out
 
 
 if __name__ == "__main__":

@@ -222,6 +222,7 @@ struct WarpRunCfg {
     int lane = 1;                 // one lane per subproblem where it applies
     int lane2 = 1;                // ... with several instances per warp in breadth-first waves
     int lane_slots = 2;           // instances per warp then
+    long long step_cap = 0;       // lane kernels' step bound (0: the kernels' own; tests set 1)
     const WarpDump *dump = nullptr;
     double eps, target;
     unsigned long long max_nodes;
@@ -686,6 +687,7 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
     P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
     P.fork = (o->branching == NR_BRANCH_FORK);
+    P.test_fault = (o->test_fault == 1);
 
     // root subproblem: initial mask with mass 1 (main.cu:805-809)
     std::vector<uint32_t> root(4 * W4, 0);
@@ -1198,13 +1200,16 @@ static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhausti
         w.wave_mode = 0; w.shift = -1; w.n_buckets = 32; w.escalate = 1;
         w.max_nodes = o->max_nodes ? o->max_nodes : (1ull << 21);
     } else {
-        w.wave_mode = 1; w.shift = o->bucket_shift; w.escalate = 0; w.max_nodes = o->max_nodes;
+        // NR_ORDER_WAVES: breadth-first waves, i.e. one bucket, whatever bucket_shift says
+        w.wave_mode = 1; w.shift = (o->order == NR_ORDER_WAVES) ? -1 : o->bucket_shift;
+        w.escalate = 0; w.max_nodes = o->max_nodes;
         w.learned = (o->order == NR_ORDER_LEARNED);
         int nb = o->n_buckets > 0 ? o->n_buckets : 256;
         nb = std::min(1024, (nb + 31) / 32 * 32);
         w.n_buckets = nb;
     }
     w.fork = (o->branching == NR_BRANCH_FORK);
+    w.step_cap = (o->test_fault == 2) ? 1 : 0;
     w.lane = (o->small_kernel != NR_SMALL_GROUP);
     w.lane2 = (o->small_kernel == NR_SMALL_AUTO) && w.wave_mode && w.shift < 0;
     w.lane_slots = (o->lane_slots == 4) ? 4 : 2;
@@ -1576,6 +1581,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.dump_stride = cfg.dump ? cfg.dump->stride : 0;
         P.inst_base = base;
         P.fork = cfg.fork;
+        P.step_cap = cfg.step_cap;
         const void *kfn = lanek ? (cfg.lane2 ? nr_lane2_kernel_ptr(W4, cfg.lane_slots) : nr_lane_kernel_ptr(W4))
                                 : warp_kernel(G, W4, learn, cfg.fork != 0);
         void *args[] = {&P};
@@ -1623,7 +1629,7 @@ static int warp_finish(nr_context *c, NrSlot &sl, int base, std::vector<int> *ha
     if (n_check.load()) {
         for (int i = 0; i < n; ++i)
             if (hout[i].status == NR_LANE_STATUS_CHECK) {
-                snprintf(g_internal, sizeof(g_internal), "lane kernel check %llu failed on instance %d",
+                snprintf(g_internal, sizeof(g_internal), "warp engine check %llu failed on instance %d",
                          (unsigned long long)hout[i].max_wave, base + i);
                 break;
             }
@@ -1846,20 +1852,28 @@ extern "C" int nr_autotune(nr_context *c, int n, const nr_graph *gs, const int32
     std::vector<nr_result> res(sample);
     const bool exhaustive = !(base.target_width > 0) && base.order != NR_ORDER_MAXMASS &&
                             base.order != NR_ORDER_LEARNED;
+    // The bucket resolution is searched only when the caller leaves the order to the engine:
+    // NR_ORDER_WAVES holds one bucket (breadth-first waves), NR_ORDER_MAXMASS the caller's shift.
     const int shifts_t[] = {-1, 0, 1, 2};   // -1: one bucket, i.e. breadth-first waves
-    const int shifts_e[] = {base.bucket_shift};
-    const int *shifts = exhaustive ? shifts_e : shifts_t;
-    const int n_shift = exhaustive ? 1 : 4;
-    const uint64_t pages_c[] = {64, 512};
+    const int shifts_e[] = {base.order == NR_ORDER_WAVES ? -1 : base.bucket_shift};
+    const bool held = exhaustive || base.order == NR_ORDER_WAVES || base.order == NR_ORDER_MAXMASS ||
+                      base.order == NR_ORDER_LEARNED;
+    const int *shifts = held ? shifts_e : shifts_t;
+    const int n_shift = held ? 1 : 4;
+    // pages per warp: 64 and 512 (small and medium queues), 4096 for instances whose waves
+    // outgrow 512 pages; with a capacity, candidates above it collapse onto it
+    const uint64_t pages_c[] = {64, 512, 4096};
     const int wpb_c[] = {2, 4, 8};
     double best_t = 1e300;
     nr_options pick = base;
     for (int si = 0; si < n_shift; ++si)
-        for (uint64_t pg : pages_c)
+        for (int pi = 0; pi < 3; ++pi)
             for (int wpb : wpb_c) {
+                const uint64_t pg = pages_c[pi];
+                if (pi > 0 && capacity && capacity <= pages_c[pi - 1] * NR_PAGE) continue;
                 nr_options o = base;
                 o.bucket_shift = shifts[si];
-                o.n_buckets = 64 << std::max(0, shifts[si]);
+                o.n_buckets = held && base.n_buckets > 0 ? base.n_buckets : 64 << std::max(0, shifts[si]);
                 o.warps_per_block = wpb;
                 const uint64_t cap = capacity ? std::min<uint64_t>(capacity, pg * NR_PAGE) : pg * NR_PAGE;
                 double t = 1e300;
@@ -1879,7 +1893,8 @@ extern "C" int nr_autotune(nr_context *c, int n, const nr_graph *gs, const int32
                     best_t = t;
                     pick = o;
                     pick.max_nodes = base.max_nodes;
-                    if (!capacity) pick.pages_per_warp = (int32_t)pg;
+                    // the queue size timed: pages_per_warp applies to calls with capacity 0
+                    pick.pages_per_warp = (int32_t)std::min<uint64_t>(pg, capacity ? (capacity + NR_PAGE - 1) / NR_PAGE : pg);
                 }
             }
     *best = pick;
