@@ -79,7 +79,11 @@ typedef struct og_opts {
     int32_t  branching;     /* OG_BRANCH_PATH (disjoint path children) or OG_BRANCH_FORK */
     int32_t  n_terminals;   /* K-terminal: > 0 with `terminals` below; src is terminals[0] */
     const int32_t *terminals;
+    int32_t  branch_order;  /* path branching, the order the path's UNKNOWN edges are branched in:
+                               OG_BORDER_SRC (the reference), _DST, _P_ASC, _P_DESC */
 } og_opts;
+
+enum { OG_BORDER_SRC = 0, OG_BORDER_DST = 1, OG_BORDER_P_ASC = 2, OG_BORDER_P_DESC = 3 };
 
 typedef struct og_result {
     double   R;             /* reliability found (sum of all-up leaf masses) */
@@ -122,6 +126,27 @@ double og_brute(const og_graph *g, int src, int dst);
 
 /* The same for K-terminal reliability: every node of `terminals` connected to terminals[0]. */
 double og_brute_k(const og_graph *g, const int32_t *terminals, int n_terminals);
+
+/* The ceiling of queue orders (an experiment, not the reference's method).
+ * Popping a subproblem takes its "gain" out of the width ESP + queued mass: the all-up
+ * leaf mass of a live subproblem, the whole mass of a dead end.  For a branching rule
+ * (path branching with o->branch_order; eps 0, no capacity), every order reaches
+ * width <= target only once the gains of the popped subproblems add up to >= 1 - target,
+ * so no order needs fewer pops than the smallest k for which the k largest gains of the
+ * whole decomposition tree reach 1 - target (min_pops).  Those gains are found by
+ * max-mass best-first search: a gain never exceeds its subproblem's mass and masses
+ * shrink down the tree, so once the k-th largest gain seen is >= the largest queued
+ * mass, no unseen subproblem can be among the k largest.  Breadth-first waves reach
+ * the largest gain any schedule can after h parallel steps (the first h levels of the
+ * tree hold every subproblem a height-h subtree can), so bf_waves is the fewest steps
+ * any schedule needs.  plain_pops: max-mass (heap) order; bf_pops: breadth-first.
+ * status 0, or 2 if `budget` pops ran out before min_pops was certain. */
+typedef struct og_bound {
+    uint64_t plain_pops, min_pops, bf_pops, bf_waves, explored;
+    int32_t  status;
+    int32_t  pad;
+} og_bound;
+int og_order_bound(const og_graph *g, int src, int dst, const og_opts *o, uint64_t budget, og_bound *out);
 
 /* Bucket index used by the wave schedule (shared definition with the engine). */
 int og_bucket(double mass, int shift, int n_buckets);

@@ -35,7 +35,15 @@ class OgOpts(C.Structure):
                 ("bucket_shift", C.c_int32), ("n_buckets", C.c_int32), ("threads", C.c_int32),
                 ("eps", C.c_double), ("target_width", C.c_double), ("capacity", C.c_uint64),
                 ("max_nodes", C.c_uint64), ("branching", C.c_int32), ("n_terminals", C.c_int32),
-                ("terminals", C.c_void_p)]
+                ("terminals", C.c_void_p), ("branch_order", C.c_int32)]
+
+
+BRANCH_ORDERS = {"src": 0, "dst": 1, "p_asc": 2, "p_desc": 3}
+
+
+class OgBound(C.Structure):
+    _fields_ = [("plain_pops", C.c_uint64), ("min_pops", C.c_uint64), ("bf_pops", C.c_uint64),
+                ("bf_waves", C.c_uint64), ("explored", C.c_uint64), ("status", C.c_int32), ("pad", C.c_int32)]
 
 
 class OgResult(C.Structure):
@@ -75,6 +83,9 @@ def lib():
         L.og_run_batch.argtypes = [C.c_int, C.POINTER(OgGraph), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(OgOpts), C.POINTER(OgResult), C.c_int]
         L.og_run_batch.restype = C.c_int
+        L.og_order_bound.argtypes = [C.POINTER(OgGraph), C.c_int, C.c_int, C.POINTER(OgOpts), C.c_uint64,
+                                     C.POINTER(OgBound)]
+        L.og_order_bound.restype = C.c_int
         L.og_default_opts.argtypes = [C.POINTER(OgOpts)]
         L.og_default_opts.restype = None
         _lib = L
@@ -160,7 +171,7 @@ def run_batch(batch: BatchArgs, threads: int = 1, **kw):
 def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, order: str = "waves",
         bucket_shift: int = -1, n_buckets: int = 1, threads: int = 1, eps: float = 0.0,
         target_width: float = 0.0, capacity: int = 0, max_nodes: int = 0, branching: str = "path",
-        terminals=None) -> OracleResult:
+        terminals=None, branch_order: str = "src") -> OracleResult:
     """terminals: K-terminal reliability of this node list (src and dst are then ignored;
     terminals[0] is the search root)."""
     v = _View(g)
@@ -177,6 +188,7 @@ def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, orde
     o.capacity = int(capacity)
     o.max_nodes = int(max_nodes)
     o.branching = BRANCHING[branching]
+    o.branch_order = BRANCH_ORDERS[branch_order]
     term = None
     if terminals is not None:
         term = np.ascontiguousarray(terminals, dtype=np.int32)
@@ -187,6 +199,22 @@ def run(g, src: int, dst: int, rule: str = "level", precheck: bool = False, orde
     if rc != 0:
         raise ValueError(f"oracle rejected the instance ({rc})")
     return OracleResult(**{f: getattr(r, f) for f, _ in OgResult._fields_})
+
+
+def order_bound(g, src: int, dst: int, target_width: float, branch_order: str = "src",
+                budget: int = 50_000_000) -> dict:
+    """The ceiling of queue orders for one branching rule (og_order_bound in oracle.h): max-mass
+    pops, the fewest pops any order can need, breadth-first pops and waves (the fewest parallel
+    steps any schedule can need)."""
+    v = _View(g)
+    o = OgOpts()
+    lib().og_default_opts(C.byref(o))
+    o.target_width = float(target_width)
+    o.branch_order = BRANCH_ORDERS[branch_order]
+    b = OgBound()
+    if lib().og_order_bound(C.byref(v.c), int(src), int(dst), C.byref(o), int(budget), C.byref(b)) != 0:
+        raise ValueError("oracle rejected the instance")
+    return {f: int(getattr(b, f)) for f, _ in OgBound._fields_ if f != "pad"}
 
 
 def brute_k(g, terminals) -> float:

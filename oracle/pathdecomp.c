@@ -268,7 +268,7 @@ void og_default_opts(og_opts *o)
 typedef struct {
     const og_graph *g;
     const double *q;
-    int src, dst, W, rule, precheck, branching;
+    int src, dst, W, rule, precheck, branching, border;
     int nk;                     /* K-terminal: terminals other than src (0: two-terminal) */
     uint8_t *isterm;            /* [n] */
     int32_t *order;             /* [n] BFS order of the last K-terminal search */
@@ -292,6 +292,7 @@ static void x_init(xctx *x, const og_graph *g, const double *q, int src, int dst
     x->W = (g->n_edges * 2 + 31) / 32;
     if (x->W < 1) x->W = 1;
     x->rule = o->bfs_rule; x->precheck = o->precheck; x->eps = o->eps; x->branching = o->branching;
+    x->border = o->branch_order;
     x->isterm = (uint8_t *)calloc(n, 1);
     x->order = (int32_t *)malloc((n + 1) * sizeof(int32_t));
     x->mark = (uint8_t *)calloc(n, 1);
@@ -492,9 +493,20 @@ static void x_expand(xctx *x, const uint32_t *m, double mass, sink_fn sink, void
             if (x->mark[x->order[i]]) x->path[L++] = x->par_e[x->order[i]];
     } else {
         if (!x_bfs(x, m)) { x->dead++; return; }
-        /* path hops in src -> dst order */
+        /* path hops in src -> dst order (the reference's branching order) */
         for (int v = x->dst; v != x->src; v = x->par_v[v]) x->path[L++] = x->par_e[v];
-        for (int i = 0, j = L - 1; i < j; i++, j--) { int32_t t = x->path[i]; x->path[i] = x->path[j]; x->path[j] = t; }
+        if (x->border != OG_BORDER_DST)
+            for (int i = 0, j = L - 1; i < j; i++, j--) { int32_t t = x->path[i]; x->path[i] = x->path[j]; x->path[j] = t; }
+        if (x->border == OG_BORDER_P_ASC || x->border == OG_BORDER_P_DESC) {
+            const double *pp = x->g->edge_p;      /* stable insertion sort of the hops by p */
+            const int desc = x->border == OG_BORDER_P_DESC;
+            for (int i = 1; i < L; i++) {
+                int32_t e = x->path[i];
+                int j = i - 1;
+                while (j >= 0 && (desc ? pp[x->path[j]] < pp[e] : pp[x->path[j]] > pp[e])) { x->path[j + 1] = x->path[j]; j--; }
+                x->path[j + 1] = e;
+            }
+        }
     }
     const double *p = x->g->edge_p;
     memcpy(x->work, m, x->W * sizeof(uint32_t));
@@ -909,7 +921,7 @@ static void arena_fit(og_arena *a, const og_graph *g, int src, int dst, const og
     /* point the context at this graph; scratch arrays are reused */
     xctx *x = &a->x;
     x->g = g; x->q = a->q; x->src = src; x->dst = dst; x->W = W;
-    x->rule = o->bfs_rule; x->precheck = o->precheck; x->eps = o->eps;
+    x->rule = o->bfs_rule; x->precheck = o->precheck; x->eps = o->eps; x->border = o->branch_order;
     x->gen = 0;
     memset(x->vis, 0, a->n_cap * sizeof(uint32_t));
     memset(&x->R, 0, sizeof(ksum)); memset(&x->esp_trunc, 0, sizeof(ksum)); memset(&x->esp_spill, 0, sizeof(ksum));
@@ -1185,4 +1197,87 @@ static double brute_set(const og_graph *g, int src, uint64_t want)
     free(var); free(arcs); free(arc_var); free(vindex); free(tl); free(th);
     free(vstart); free(vlist); free(fill);
     return ks_val(&R);
+}
+
+/* ------------------------------------------------------------------ */
+/* the ceiling of queue orders (og_order_bound, oracle.h)               */
+/* ------------------------------------------------------------------ */
+typedef struct { hq *h; double pushed; } gain_sink;
+
+static int gain_sink_fn(void *ud, const uint32_t *m, double mass)
+{
+    gain_sink *s = (gain_sink *)ud;
+    s->pushed += mass;
+    return hq_sink(s->h, m, mass);
+}
+
+static int cmp_desc(const void *a, const void *b)
+{
+    double x = *(const double *)a, y = *(const double *)b;
+    return (x < y) - (x > y);
+}
+
+int og_order_bound(const og_graph *g, int src, int dst, const og_opts *o_in, uint64_t budget, og_bound *out)
+{
+    memset(out, 0, sizeof(*out));
+    if (!g || g->n_nodes <= 0 || src < 0 || dst < 0 || src >= g->n_nodes || dst >= g->n_nodes) return -1;
+    og_opts o = *o_in;
+    o.eps = 0; o.capacity = 0; o.max_nodes = 0; o.threads = 1; o.precheck = 0;
+    o.branching = OG_BRANCH_PATH; o.n_terminals = 0; o.terminals = NULL;
+    if (!(o.target_width > 0)) return -1;
+    og_result r;
+    o.order = OG_ORDER_HEAP;
+    og_run(g, src, dst, &o, &r);
+    out->plain_pops = r.nodes;
+    o.order = OG_ORDER_WAVES; o.bucket_shift = -1; o.n_buckets = 1;
+    og_run(g, src, dst, &o, &r);
+    out->bf_pops = r.nodes; out->bf_waves = r.waves;
+
+    /* max-mass best-first search recording every popped subproblem's gain */
+    const int E = g->n_edges;
+    int W = (E * 2 + 31) / 32;
+    if (W < 1) W = 1;
+    double *q = (double *)malloc((size_t)(E > 0 ? E : 1) * sizeof(double));
+    uint32_t *root = (uint32_t *)calloc((size_t)W, sizeof(uint32_t));
+    for (int e = 0; e < E; e++) {
+        double p = g->edge_p[e];
+        q[e] = 1.0 - p;
+        if (p >= 1.0) root[e >> 4] |= 1u << ((e & 15) * 2);
+        else if (p > 0.0) root[e >> 4] |= 3u << ((e & 15) * 2);
+    }
+    xctx x;
+    x_init(&x, g, q, src, dst, &o);
+    hq h;
+    memset(&h, 0, sizeof(h));
+    h.W = x.W; h.heap = 1;
+    hq_sink(&h, root, 1.0);
+    uint32_t *m = (uint32_t *)malloc(x.W * sizeof(uint32_t));
+    size_t ng = 0, cg = 1024;
+    double *gains = (double *)malloc(cg * sizeof(double));
+    double *sorted = NULL;
+    const double need = 1.0 - o.target_width;
+    uint64_t next_check = 16;
+    out->status = 2;
+    while (h.n && ng < budget) {
+        double mass = hq_pop(&h, m);
+        gain_sink gs = { &h, 0.0 };
+        x_expand(&x, m, mass, gain_sink_fn, &gs);
+        if (ng == cg) { cg *= 2; gains = (double *)realloc(gains, cg * sizeof(double)); }
+        gains[ng++] = mass - gs.pushed;
+        if (ng < next_check && h.n) continue;
+        next_check = ng * 2;
+        /* the smallest k whose k largest gains reach 1 - target, and its certificate */
+        sorted = (double *)realloc(sorted, ng * sizeof(double));
+        memcpy(sorted, gains, ng * sizeof(double));
+        qsort(sorted, ng, sizeof(double), cmp_desc);
+        double s = 0.0;
+        size_t k = 0;
+        while (k < ng && s < need) s += sorted[k++];
+        const double top = h.n ? h.key[0] : 0.0;
+        if (s >= need && sorted[k - 1] >= top) { out->min_pops = k; out->status = 0; break; }
+    }
+    out->explored = ng;
+    free(sorted); free(gains); free(m); free(h.d); free(h.key); free(q); free(root);
+    x_free(&x);
+    return 0;
 }
