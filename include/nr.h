@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define NR_ABI_VERSION 1
+#define NR_ABI_VERSION 2
 
 /* status codes */
 enum {
@@ -89,6 +89,22 @@ enum {
                                :550-565, FORK_BEST_EDGE); not with NR_ORDER_LEARNED */
 };
 
+/* branch order: the order in which a path's UNKNOWN edges are branched (child k = the
+ * first k-1 of them in this order up, the k-th down).  Every order is a disjoint
+ * decomposition, so exhaustive R is the same; the tree, hence the work to a target
+ * width, is not. */
+enum {
+    NR_BORDER_SRC     = 0,  /* src side first (main.cu:114-283, seq.cpp:539-568; the default) */
+    NR_BORDER_DST     = 1,  /* dst side first */
+    NR_BORDER_P_ASC   = 2,  /* least reliable edge first (ties: path order, src side first) */
+    NR_BORDER_P_DESC  = 3,  /* most reliable edge first (ties: path order) */
+    NR_BORDER_LEARNED = 4   /* by the learned scorer (nr_context_set_model): edge e first when
+                               (1 - p_e) x (1 - r(e)) is largest, r(e) the scorer's residual
+                               reliability of the subproblem with e down -- a likely and critical
+                               failure first; ties: path order.  The warp engine (n <= 32) with a
+                               target width or a max-mass / learned order only */
+};
+
 typedef struct nr_options {
     double   truncation_eps;  /* popped mass below eps goes to ESP (main.cu:537-543); 0 = off.
                                  The reference CLI default is 1e-15. */
@@ -119,6 +135,9 @@ typedef struct nr_options {
     int32_t  lane_slots;      /* one lane per subproblem, one bucket: instances a warp carries (2 or 4;
                                  0 = the default, 2: on 4096 K15 instances 4 slots leave too few warps
                                  per SM to hide the steps' latency, 0.096 against 0.060 ms) */
+    int32_t  branch_order;    /* NR_BORDER_*: path branching only; two-terminal runs (K-terminal runs
+                                 take NR_BORDER_SRC) */
+    int32_t  reserved0;
 } nr_options;
 
 typedef struct nr_result {

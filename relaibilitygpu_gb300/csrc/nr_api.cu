@@ -223,6 +223,7 @@ struct WarpRunCfg {
     int lane2 = 1;                // ... with several instances per warp in breadth-first waves
     int lane_slots = 2;           // instances per warp then
     long long step_cap = 0;       // lane kernels' step bound (0: the kernels' own; tests set 1)
+    int border = NR_BORDER_SRC;   // branch order of the paths' UNKNOWN edges
     const WarpDump *dump = nullptr;
     double eps, target;
     unsigned long long max_nodes;
@@ -688,6 +689,7 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
     P.fork = (o->branching == NR_BRANCH_FORK);
     P.test_fault = (o->test_fault == 1);
+    P.border = o->branch_order;
 
     // root subproblem: initial mask with mass 1 (main.cu:805-809)
     std::vector<uint32_t> root(4 * W4, 0);
@@ -851,6 +853,7 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
     P.fork = (o->branching == NR_BRANCH_FORK);
+    P.border = o->branch_order;
     P.target_on = o->target_width > 0 ? 1 : 0;
     P.target_fix = nr_fix_of(o->target_width > 0 ? o->target_width : 0.0);
     P.max_nodes = o->max_nodes;
@@ -957,7 +960,7 @@ static uint64_t nr_run_fingerprint(const nr_graph *g, int src, int dst, const nr
     mix(g->edge_id, sizeof(int32_t) * g->n_arcs);
     mix(g->edge_p, sizeof(double) * g->n_edges);
     const int32_t nb = std::max(1, std::min(NR_WIDE_MAX_NB, o->n_buckets > 0 ? (int)o->n_buckets : NR_WIDE_MAX_NB));
-    const int32_t v[5] = {src, dst, o->bucket_shift, nb, o->branching};
+    const int32_t v[6] = {src, dst, o->bucket_shift, nb, o->branching, o->branch_order};
     mix(v, sizeof(v));
     const double eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
     mix(&eps, sizeof(eps));
@@ -1042,6 +1045,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     P.eps = o->truncation_eps > 0 ? o->truncation_eps : 0.0;
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
     P.fork = (o->branching == NR_BRANCH_FORK);
+    P.border = o->branch_order;
     P.target_on = o->target_width > 0 ? 1 : 0;
     P.target_fix = nr_fix_of(o->target_width > 0 ? o->target_width : 0.0);
     P.max_nodes = o->max_nodes;
@@ -1210,6 +1214,7 @@ static WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhausti
     }
     w.fork = (o->branching == NR_BRANCH_FORK);
     w.step_cap = (o->test_fault == 2) ? 1 : 0;
+    w.border = o->branch_order;
     w.lane = (o->small_kernel != NR_SMALL_GROUP);
     w.lane2 = (o->small_kernel == NR_SMALL_AUTO) && w.wave_mode && w.shift < 0;
     w.lane_slots = (o->lane_slots == 4) ? 4 : 2;
@@ -1283,7 +1288,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
                        cudaStream_t after = nullptr, bool uniform = false)
 {
     constexpr int NCLS = NR_NCLS;
-    const bool lane_ok = cfg.lane && !cfg.fork && !cfg.learned && !cfg.dump;
+    const bool lane_ok = cfg.lane && !cfg.fork && !cfg.learned && !cfg.dump && cfg.border != NR_BORDER_LEARNED;
     int rc0 = slot_ready(sl);
     if (rc0) return rc0;
     NrBatchScratch &S = sl.scratch;          // kept by the slot: no page faults on every call
@@ -1496,7 +1501,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
                              nr_lane_shm_bytes(cfgp.n_buckets, cfgp.pages)),
                     nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots)) * warps_pb > (size_t)c->smem_optin)
         cfgp.pages /= 2;
-    const bool learn = cfg.learned || cfg.dump;
+    const bool learn = cfg.learned || cfg.dump || cfg.border == NR_BORDER_LEARNED;
     int grids[NCLS] = {0};
     size_t smems[NCLS] = {0};
     size_t slab_need = 0;
@@ -1582,6 +1587,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.inst_base = base;
         P.fork = cfg.fork;
         P.step_cap = cfg.step_cap;
+        P.border = cfg.border;
         const void *kfn = lanek ? (cfg.lane2 ? nr_lane2_kernel_ptr(W4, cfg.lane_slots) : nr_lane_kernel_ptr(W4))
                                 : warp_kernel(G, W4, learn, cfg.fork != 0);
         void *args[] = {&P};
@@ -1657,9 +1663,22 @@ static int run_warp_batch(nr_context *c, int n, const nr_graph *gs, const int32_
 // Checks of a batch: shapes, CSR arrays (once per run of instances sharing them),
 // probabilities of graphs above 32 nodes (the warp engine checks its own while
 // copying them).  *n_wide = graphs above 32 nodes.
+// The branch order: a known value; the learned one needs a model and runs on the warp engine
+// only (a target width or a max-mass / learned order, path branching).
+static int branch_order_ok(const nr_context *c, const nr_options &o)
+{
+    if (o.branch_order < NR_BORDER_SRC || o.branch_order > NR_BORDER_LEARNED) return NR_ERR_INVALID;
+    if (o.branch_order != NR_BORDER_LEARNED) return NR_OK;
+    if (!c->has_model) return NR_ERR_INVALID;
+    if (o.branching != NR_BRANCH_PATH) return NR_ERR_UNSUPPORTED;
+    if (!(o.target_width > 0) && o.order != NR_ORDER_MAXMASS && o.order != NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
+    return NR_OK;
+}
+
 static int batch_options_ok(const nr_context *c, const nr_options &o)
 {
     if (o.order == NR_ORDER_LEARNED && !c->has_model) return NR_ERR_INVALID;
+    if (const int rb = branch_order_ok(c, o)) return rb;
     if (o.order == NR_ORDER_LEARNED && o.branching == NR_BRANCH_FORK) return NR_ERR_UNSUPPORTED;
     if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
     return NR_OK;
@@ -1674,7 +1693,8 @@ static int batch_validate(nr_context *c, int n, const nr_graph *gs, const int32_
         if (!rc && !(i > 0 && same_structure_arrays(&gs[i], &gs[i - 1]))) rc = validate_structure(&gs[i]);
         if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) {
             rc = validate_probabilities(&gs[i]);
-            if (!rc && o.order == NR_ORDER_LEARNED) rc = NR_ERR_UNSUPPORTED;    // learned order: n <= 32 only
+            if (!rc && (o.order == NR_ORDER_LEARNED || o.branch_order == NR_BORDER_LEARNED))
+                rc = NR_ERR_UNSUPPORTED;    // learned order and branch order: n <= 32 only
             wide.fetch_add(1);
         }
         if (rc) bad.store(rc);
@@ -2002,6 +2022,8 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     drain(c);                          // finish batches in flight: slot 0 and the model are used here
     NR_CUDA_TRY(cudaSetDevice(c->device));
     if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
+    if (const int rb = branch_order_ok(c, o)) return rb;
+    if (o.branch_order == NR_BORDER_LEARNED && g->n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
     if (o.branching == NR_BRANCH_FORK && o.order == NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
     if (g->n_nodes > NR_SMALL_MAX_N) return run_wide(c, g, src, dst, capacity, &o, res);
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {
@@ -2030,7 +2052,8 @@ extern "C" int nr_reliability_kterminal(nr_context *c, const nr_graph *g, const 
     }
     nr_options o;
     if (opt) o = *opt; else nr_options_default(&o);
-    if (o.order == NR_ORDER_LEARNED || o.branching != NR_BRANCH_PATH) return NR_ERR_UNSUPPORTED;
+    if (o.order == NR_ORDER_LEARNED || o.branching != NR_BRANCH_PATH || o.branch_order != NR_BORDER_SRC)
+        return NR_ERR_UNSUPPORTED;
     res->n_nodes = g->n_nodes;
     res->n_edges = g->n_edges;
     res->src = src;

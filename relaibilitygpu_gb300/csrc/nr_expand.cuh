@@ -120,12 +120,20 @@ __device__ __forceinline__ uint32_t nr_build_row(const NrSmemGraph &sg, const ui
     return row;
 }
 
-template <int G, int W4, bool FEAT = false>
+// No hop scorer (the default): NR_BORDER_LEARNED needs the scorer's instantiation.
+struct NrNoHopScore {
+    __device__ float operator()(bool, const float (&)[NR_FEAT]) const { return 0.f; }
+};
+
+// FEAT: the learned scorer's instantiation (child features; with hop_score, the learned branch
+// order).  hop_score(has, f) is warp-collective and returns the scorer's output for the lane's row.
+template <int G, int W4, bool FEAT = false, class HopScore = NrNoHopScore>
 __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGraph &sg,
                                           const uint32_t *my_m, bool valid, double mass, double eps,
                                           bool &has_child, uint32_t (&w)[4 * W4], double &cm,
                                           NrLaneAcc &acc, float (*feat)[NR_FEAT] = nullptr,
-                                          NrRowIO *rio = nullptr)
+                                          NrRowIO *rio = nullptr, int border = NR_BORDER_SRC,
+                                          const HopScore *hop_score = nullptr)
 {
     constexpr int NW = 4 * W4;
     const int lane = threadIdx.x & 31;
@@ -189,29 +197,77 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
         unk = ((my_m[e_h >> 4] >> ((e_h & 15) << 1)) & 3u) == 3u;
     }
 
-    // FP64 mass along the path, src side first (sequential, as the oracle); each hop lane
+    // FP64 mass along the path in branch order (sequential, as the oracle); each hop lane
     // loads its own p first, so the chain only waits on shuffles and multiplies
     const double p_h = unk ? sg.p[e_h] : 1.0;
     double P = mass;
-    for (int h = 0; h < Lmax; ++h) {
-        const double pe = __shfl_sync(NR_FULL, p_h, gbase + h);
-        const bool u = __shfl_sync(NR_FULL, unk, gbase + h);
-        if (h < L && u) {
-            if (v == h) { cm = __dmul_rn(P, __dsub_rn(1.0, p_h)); has_child = true; }
-            P = __dmul_rn(P, pe);
+    int rank = v;                                       // the hop's place in the branch order
+    if (border == NR_BORDER_SRC) {
+        for (int h = 0; h < Lmax; ++h) {
+            const double pe = __shfl_sync(NR_FULL, p_h, gbase + h);
+            const bool u = __shfl_sync(NR_FULL, unk, gbase + h);
+            if (h < L && u) {
+                if (v == h) { cm = __dmul_rn(P, __dsub_rn(1.0, p_h)); has_child = true; }
+                P = __dmul_rn(P, pe);
+            }
+        }
+    } else {
+        // rank among the group's UNKNOWN hops: dst side first, or by a key (stable in path
+        // order, the oracle's insertion sort of the src -> dst path): p, or the learned key
+        bool desc = (border == NR_BORDER_P_DESC);
+        const bool rev = (border == NR_BORDER_DST);
+        double key = p_h;
+        if constexpr (FEAT) {
+            if (hop_score && border == NR_BORDER_LEARNED) {
+                // the scorer's residual reliability r of the subproblem with hop v down (the other
+                // edges as in the parent); key (1 - p) x (1 - r): a likely, critical failure first
+                uint32_t wh[NW];
+#pragma unroll
+                for (int k = 0; k < NW; ++k) wh[k] = my_m[k];
+#pragma unroll
+                for (int k = 0; k < NW; ++k)
+                    if (unk && k == (e_h >> 4)) wh[k] &= ~(3u << ((e_h & 15) << 1));
+                const uint32_t rs = __shfl_sync(NR_FULL, row, gbase + src);
+                const uint32_t rd = __shfl_sync(NR_FULL, row, gbase + dst);
+                const int ds = __popc(rs) - ((hop_u == src || hop_v == src) ? 1 : 0);
+                const int dd = __popc(rd) - ((hop_u == dst || hop_v == dst) ? 1 : 0);
+                float hf[NR_FEAT];
+                nr_child_features<W4>(hf, wh, unk ? mass * (1.0 - p_h) : 0.0, mass, L, v, p_h, ds, dd, n, g.e);
+                const float r = (*hop_score)(unk, hf);
+                key = (double)((1.f - (float)p_h) * (1.f - r));
+                desc = true;
+            }
+        }
+        rank = 0;
+        for (int j = 0; j < Lmax; ++j) {
+            const double kj = __shfl_sync(NR_FULL, key, gbase + j);
+            const bool uj = __shfl_sync(NR_FULL, unk, gbase + j);
+            const bool before = rev ? (j > v) : desc ? (kj > key || (kj == key && j < v)) : (kj < key || (kj == key && j < v));
+            if (uj && j < L && before) ++rank;
+        }
+        for (int k = 0; k < Lmax; ++k) {
+            const unsigned b = __ballot_sync(NR_FULL, unk && rank == k);
+            const unsigned gb = (G == 32) ? b : ((b >> gbase) & ((1u << G) - 1u));
+            const int hl = gb ? __ffs(gb) - 1 : 0;
+            const double pe = __shfl_sync(NR_FULL, p_h, gbase + hl);
+            if (gb) {
+                if (v == hl) { cm = __dmul_rn(P, __dsub_rn(1.0, p_h)); has_child = true; }
+                P = __dmul_rn(P, pe);
+            }
         }
     }
     if (live && leader) { acc.leaves++; nr_fix_add_mass(acc.R, P); }
 
-    // child of hop v: parent with earlier UNKNOWN hops up and hop v down
+    // child of hop v: parent with the UNKNOWN hops before it in branch order up and hop v down
 #pragma unroll
     for (int k = 0; k < NW; ++k) w[k] = my_m[k];
     for (int j = 0; j < Lmax; ++j) {
         const int e = __shfl_sync(NR_FULL, e_h, gbase + j);
         const bool u = __shfl_sync(NR_FULL, unk, gbase + j);
-        if (has_child && u && j <= v) {
+        const int rj = __shfl_sync(NR_FULL, rank, gbase + j);
+        if (has_child && u && rj <= rank) {
             const int wi = e >> 4;
-            const uint32_t bits = (j < v ? 2u : 3u) << ((e & 15) << 1);
+            const uint32_t bits = (rj < rank ? 2u : 3u) << ((e & 15) << 1);
 #pragma unroll
             for (int k = 0; k < NW; ++k)
                 if (k == wi) w[k] &= ~bits;
@@ -225,7 +281,7 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
         if (has_child) {
             const int ds = __popc(rs) - ((hop_u == src || hop_v == src) ? 1 : 0);
             const int dd = __popc(rd) - ((hop_u == dst || hop_v == dst) ? 1 : 0);
-            nr_child_features<W4>(*feat, w, cm, mass, L, v, sg.p[e_h], ds, dd, n, g.e);
+            nr_child_features<W4>(*feat, w, cm, mass, L, rank, sg.p[e_h], ds, dd, n, g.e);
         }
     }
 }

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_kernel(NrGridParams 
             if constexpr (FORK)
                 nr_expand_fork<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
             else
-                nr_expand<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
+                nr_expand<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc, nullptr, nullptr, P.border);
 
             const unsigned cb = __ballot_sync(NR_FULL, has_child);
             if (cb) {

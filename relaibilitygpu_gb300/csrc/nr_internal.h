@@ -69,6 +69,7 @@ struct NrGridParams {
     double eps;
     long long timeout_ns;
     int fork;                         // 1: fork branching on the most reliable path edge
+    int border;                       // NR_BORDER_*: the order a path's UNKNOWN edges are branched in
     int test_fault;                   // 1 (failure-path tests only): block 0 leaves before its
                                       // first grid barrier, so the others' bounded waits run out
 };

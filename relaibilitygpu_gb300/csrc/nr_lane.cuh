@@ -160,6 +160,35 @@ __device__ __forceinline__ int nr_lane_path(const uint32_t *my_rows, uint32_t *m
     return L;
 }
 
+// Branch order of one lane's path hops my_hop[32 l], l = 0..L-1 src side first: dst side
+// first (reversed), or by p (ascending / descending, stable in path order -- the oracle's
+// insertion sort of the src -> dst path).  Known hops move too but make no child, so only
+// the UNKNOWN hops' relative order matters.
+__device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, int L, int border, const double *pt)
+{
+    if (border == NR_BORDER_DST) {
+        for (int i = 0, j = L - 1; i < j; ++i, --j) {
+            const uint32_t t = my_hop[32 * i];
+            my_hop[32 * i] = my_hop[32 * j];
+            my_hop[32 * j] = t;
+        }
+        return;
+    }
+    const bool desc = (border == NR_BORDER_P_DESC);
+    for (int i = 1; i < L; ++i) {
+        const uint32_t hp = my_hop[32 * i];
+        const double pe = pt[hp & 0xffffu];
+        int j = i - 1;
+        while (j >= 0) {
+            const double pj = pt[my_hop[32 * j] & 0xffffu];
+            if (!(desc ? pj < pe : pj > pe)) break;
+            my_hop[32 * (j + 1)] = my_hop[32 * j];
+            --j;
+        }
+        my_hop[32 * (j + 1)] = hp;
+    }
+}
+
 // Child record at slot s: the parent's mask blocks, then the one word that differs (hop edge e
 // down; this thread's later store to the same address wins); the parent's rows less the down
 // edge cu - cv; mass cm.  wv = the parent's (current) mask word of e.
@@ -377,6 +406,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                 bool live;
                 int nch, bad;
                 const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, g.e, src, dst, active, live, nch, bad);
+                if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, L, P.border, pt);
                 if (active && !live && !bad) acc.dead++;
 
                 {

@@ -272,6 +272,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         bool live;
         int nch, bad;
         const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
+        if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, L, P.border, pt);
         if (active && !live && !bad) acc.dead++;
         {
             const unsigned bm = __ballot_sync(NR_FULL, bad != 0);

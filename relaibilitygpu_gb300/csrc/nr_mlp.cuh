@@ -96,6 +96,31 @@ __device__ __forceinline__ void nr_mlp_layer(const uint32_t *in, uint32_t *out, 
     __syncwarp();
 }
 
+__device__ __forceinline__ void nr_mlp_warp_infer(const NrMlpDev &M, uint32_t *scratch, float *y);
+
+// Score one row per lane that has one (16-row tiles, the lanes' rows in lane order); returns the
+// lane's output (0 for a lane without a row).  Rows of a last, partial tile beyond the lanes'
+// keep older features: an output row depends only on its own input row, and those are not read.
+// All 32 lanes must call it.
+__device__ __forceinline__ float nr_mlp_score_lanes(const NrMlpDev &M, uint32_t *scratch, float *y, bool has,
+                                                    const float (&f)[NR_MLP_IN])
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, has);
+    const int cnt = __popc(m), rank = __popc(m & ((1u << lane) - 1u));
+    float out = 0.f;
+    for (int t = 0; t * 16 < cnt; ++t) {
+        if (has && rank / 16 == t) {
+#pragma unroll
+            for (int k = 0; k < NR_MLP_IN / 2; ++k) scratch[(rank % 16) * 8 + k] = nr_pack_bf16(f[2 * k], f[2 * k + 1]);
+        }
+        nr_mlp_warp_infer(M, scratch, y);
+        if (has && rank / 16 == t) out = y[rank % 16];
+        __syncwarp();
+    }
+    return out;
+}
+
 // Score a 16-row tile whose BF16 features are already in scratch[0..127]
 // (row r, feature k at word r*8 + k/2).  Writes sigmoid outputs to y[16]
 // (shared memory).  All 32 lanes must call it.

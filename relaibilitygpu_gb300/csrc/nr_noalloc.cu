@@ -137,6 +137,8 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     if (dev < 0 || dev >= NR_NOALLOC_MAX_DEVICES) return NR_ERR_INVALID;
 
     if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
+    if (o.branch_order < NR_BORDER_SRC || o.branch_order > NR_BORDER_LEARNED) return NR_ERR_INVALID;
+    if (o.branch_order == NR_BORDER_LEARNED) return NR_ERR_UNSUPPORTED;   // no scorer here
 
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     DeviceRestore restore;
@@ -207,6 +209,7 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     P.dump_feat = nullptr; P.dump_mask = nullptr; P.dump_mass = nullptr; P.dump_inst = nullptr;
     P.dump_count = nullptr; P.dump_cap = 0; P.dump_stride = 0; P.inst_base = 0;
     P.step_cap = 0;
+    P.border = o.branch_order;
 
     const size_t smem = nr_warp_shm_bytes(32 / G, sg.w4, P.n_buckets, pages);
     cudaStream_t s = cudaStreamPerThread;

@@ -70,6 +70,7 @@ struct NrWarpParams {
     int dump_stride;
     int inst_base;                   // index of this launch's instance 0 in the caller's batch
     int fork;                        // fork branching (informational: the FORK instantiation runs it)
+    int border;                      // NR_BORDER_*: the order a path's UNKNOWN edges are branched in
     long long step_cap;              // lane kernels: steps before the self-check ends an instance
                                      // (0: NR_LANE_STEP_CAP; the failure-path tests set 1)
 };
@@ -88,6 +89,17 @@ struct NrWarpShm {
     short *pnext;        // [pages]
     unsigned char *pcnt; // [pages]
     short *freel;        // [pages]
+};
+
+// The learned branch order's hop scorer: the MLP on the warp's scratch (learned kernels only).
+struct NrWarpHopScore {
+    NrMlpDev M;
+    uint32_t *scratch;
+    float *y;
+    __device__ float operator()(bool has, const float (&f)[NR_FEAT]) const
+    {
+        return nr_mlp_score_lanes(M, scratch, y, has, f);
+    }
 };
 
 __host__ __device__ inline size_t nr_warp_shm_bytes(int K, int W4, int n_buckets, int pages, bool learn = false)
@@ -286,8 +298,12 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
                     if constexpr (FORK)
                         nr_expand_fork<G, W4>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc);
                     else
-                        nr_expand<G, W4, LEARN>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm, acc,
-                                                LEARN ? &feat : nullptr, &rio);
+                    {
+                        const NrWarpHopScore hs{P.mlp, mlp_scratch, mlp_y};
+                        nr_expand<G, W4, LEARN, NrWarpHopScore>(g, sg, my_m, valid, mass, P.eps, has_child, w, cm,
+                                                                acc, LEARN ? &feat : nullptr, &rio, P.border,
+                                                                LEARN ? &hs : nullptr);
+                    }
                     double key = cm;
                     if constexpr (LEARN) {
                         const unsigned cbm = __ballot_sync(NR_FULL, has_child);

@@ -75,6 +75,7 @@ struct NrGridWideParams {
     NrWideShare *wpart;             // [2][gridDim.x] per-block shares, alternating slots
     int *stop_wave;                 // [0] waves run before a stop (or -1), [1] stop reason
     int fork;                       // 1: fork branching on the most reliable path edge
+    int border;                     // NR_BORDER_*: the order a path's UNKNOWN edges are branched in
 };
 
 struct NrBucketWideParams {
@@ -103,6 +104,7 @@ struct NrBucketWideParams {
     int *stop_info;                 // [0] waves run, [1] stop reason (0 empty, 1 target, 3 budget), [2] compactions
     unsigned long long *stats;      // [0] widest wave, [1] records queued at the end
     int fork;                       // 1: fork branching on the most reliable path edge
+    int border;                     // NR_BORDER_*: the order a path's UNKNOWN edges are branched in
     // resume from a checkpoint: the arena holds its queue and block 0's first lane starts from
     // its sums and counts (the stop test before the first wave sees them through the shares)
     int resume;
@@ -296,9 +298,33 @@ __device__ __forceinline__ void nr_wide_emit(const NrWideOut &O, NrWideAcc &A, c
 // in R when a path of up edges exists, else fork on the optimistic path's
 // UNKNOWN edge with the largest p (ties: nearest dst): down child, then up.
 // All 32 lanes call it; the accumulators live on lane 0.
+// Branch order of a path held dst side first in hops[0..L) (the children are made from
+// hops[L-1] down to hops[0]): rewrite hops so that walk visits the UNKNOWN edges dst side
+// first, or by p (ascending / descending, stable in path order: the oracle's insertion sort
+// over the src -> dst path).  One lane.
+__device__ __forceinline__ void nr_wide_branch_order(uint32_t *hops, int L, int border, const double *p)
+{
+    if (border == NR_BORDER_DST) {                          // walk order reversed
+        for (int i = 0, j = L - 1; i < j; ++i, --j) { const uint32_t t = hops[i]; hops[i] = hops[j]; hops[j] = t; }
+        return;
+    }
+    // s_i = hops[L-1-i] is the src -> dst path; sort it stably by p, then store it back reversed
+    const bool desc = (border == NR_BORDER_P_DESC);
+    for (int i = 1; i < L; ++i) {
+        const uint32_t e = hops[L - 1 - i];
+        const double pe = p[e];
+        int j = i - 1;
+        while (j >= 0 && (desc ? p[hops[L - 1 - j]] < pe : p[hops[L - 1 - j]] > pe)) {
+            hops[L - 1 - (j + 1)] = hops[L - 1 - j];
+            --j;
+        }
+        hops[L - 1 - (j + 1)] = e;
+    }
+}
+
 template <int W4>
 __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideView &v, double mass, double eps,
-                                             const NrWideOut &O, NrWideAcc &A, bool fork = false)
+                                             const NrWideOut &O, NrWideAcc &A, bool fork = false, int border = 0)
 {
     constexpr int NW = 4 * W4;
     const int lane = threadIdx.x & 31;
@@ -356,6 +382,7 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
                 x = (int)(pe >> 16);
             }
             L = h;
+            if (border != NR_BORDER_SRC && L > 1) nr_wide_branch_order(hops, L, border, v.p);
         }
     }
     L = __shfl_sync(NR_FULL, L, 0);
@@ -549,7 +576,7 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
             if (lane < W4) reinterpret_cast<uint4 *>(v.m)[lane] = __ldcg(in_mask + idx * W4 + lane);
             const double mass = __ldcg(in_mass + idx);
             __syncwarp();
-            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0);
+            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0, P.border);
         }
         if (P.target_on || P.max_nodes) nr_wide_write_share(P.wpart + (size_t)(wave & 1) * gridDim.x, A);
         if (!nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns)) break;
@@ -729,7 +756,7 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketW
             if (lane < W4) reinterpret_cast<uint4 *>(v.m)[lane] = __ldcg(P.mask + s * W4 + lane);
             const double mass = __ldcg(P.mass + s);
             __syncwarp();
-            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0);
+            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0, P.border);
         }
         __syncthreads();
         for (int b = threadIdx.x; b < P.nb; b += blockDim.x)

@@ -23,7 +23,7 @@ def test_exports_every_declared_symbol(engine_lib):
     for s in syms:
         assert hasattr(L, s), s
     assert set(syms) == set(engine_lib.EXPORTS)
-    assert engine_lib.lib().nr_abi_version() == 1
+    assert engine_lib.lib().nr_abi_version() == 2
 
 
 @pytest.mark.parametrize("name", ["COMP8", "COMP9", "test_simple", "test_kite", "cycle4", "gnm_3", "grid_4x4_3"])
