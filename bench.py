@@ -273,6 +273,48 @@ def pipelined_e2e(ctx, w, capacity, opts, flush_buf, steps, device):
     return nodes, secs, h2d, d2h
 
 
+def pipelined_e2e_matrix(ctx, w, opts, flush_buf, steps, device):
+    """The same loop through nr_batch_submit_matrix: the batch is one topology (K15) with a
+    [4096 x 105] probability matrix in pinned host memory, uploaded every step as it is."""
+    import ctypes
+    import numpy as np
+    import torch
+    import relaibilitygpu_gb300 as nr
+    pm = torch.from_numpy(np.stack([g.edge_p for g in w["graphs"]])).pin_memory()
+    n = pm.shape[0]
+    mbs = [nr.MatrixBatch(w["graphs"][0], pm.data_ptr(), w["srcs"], w["dsts"], n=n) for _ in range(2)]
+    fs = torch.cuda.Stream(device=f"cuda:{device}")
+    cudart = ctypes.CDLL("libcudart.so.13")
+    cudart.cudaMemsetAsync.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
+    cudart.cudaMemsetAsync.restype = ctypes.c_int
+    flush_args = (ctypes.c_void_p(flush_buf.data_ptr()), 1, ctypes.c_size_t(192 * 1024 * 1024),
+                  ctypes.c_void_p(fs.cuda_stream))
+    o = nr.make_options(**opts)
+
+    def loop(k_steps):
+        pending = None
+        for k in range(k_steps):
+            if cudart.cudaMemsetAsync(*flush_args) != 0:
+                raise RuntimeError("cudaMemsetAsync (L2 flush) failed")
+            tk = ctx.submit_matrix(mbs[k % 2], after_stream=fs.cuda_stream, options=o)
+            if pending is not None:
+                ctx.wait(pending)
+            pending = tk
+        ctx.wait(pending)
+
+    loop(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop(steps)
+    secs = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    per_batch = [sum(mb.res[i].nodes for i in range(n)) for mb in mbs]
+    nodes = sum(per_batch[k % 2] for k in range(steps))
+    h2d = sum(mbs[0].res[i].h2d_bytes for i in range(n))
+    d2h = sum(mbs[0].res[i].d2h_bytes for i in range(n))
+    return nodes, secs, h2d, d2h
+
+
 def median_us(xs):
     return 1e3 * statistics.median(xs)
 
@@ -505,7 +547,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="only the headline line (no configs, orders or CPU leg)")
+    ap.add_argument("--case", choices=["k15batch", "rgg200", "uneven"],
+                    help="profiling: run one case twice (a warm-up call, then the call to capture) and exit")
+    ap.add_argument("--budget", type=int, default=1_000_000, help="--case rgg200: subproblem budget")
+    ap.add_argument("--arena", type=int, default=22, help="--case rgg200: log2 of the arena slots")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -573,12 +622,14 @@ def main():
              "iterations": int(r0.iterations), "queued": int(r0.queued), "spilled": int(r0.spilled),
              "stop": {0: "queue empty", 1: "target width met", 3: "node budget"}.get(int(r0.stop), int(r0.stop)),
              "nodes_per_step": nodes // args.steps}
-    h2d = sum(res[i].h2d_bytes for i in range(BATCH))
-    d2h = sum(res[i].d2h_bytes for i in range(BATCH))
     checked, bad = parity_batch(res, w, list(range(0, BATCH, 64)))
     parity = {"checked": checked, "mismatches": bad, "ok": not bad,
               "what": "subproblems, waves, widest wave, queued, R and ESP bit-exact against the oracle"}
-    e2e_nodes, e2e_secs, _, _ = pipelined_e2e(ctx, w, 0, tuned, flush.buf, max(args.steps, 50), local)
+    e2e_steps = max(args.steps, 50)
+    # e2e through the matrix entry point (the workload is one topology with 4096 probability
+    # sets) and, beside it, through the per-instance entry point
+    e2e_nodes, e2e_secs, h2d, d2h = pipelined_e2e_matrix(ctx, w, tuned, flush.buf, e2e_steps, local)
+    gen_nodes, gen_secs, gen_h2d, gen_d2h = pipelined_e2e(ctx, w, 0, tuned, flush.buf, e2e_steps, local)
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
@@ -601,7 +652,8 @@ def main():
     # replicas: units add up over ranks, the slowest rank sets the time (no data-path collective)
     from relaibilitygpu_gb300 import replicas
     tot = replicas.reduce_totals({"nodes": float(nodes), "t_dev_max": t_dev, "wall_max": wall_s,
-                                  "pipe_nodes": float(e2e_nodes), "pipe_wall_max": e2e_secs})
+                                  "pipe_nodes": float(e2e_nodes), "pipe_wall_max": e2e_secs,
+                                  "gen_nodes": float(gen_nodes), "gen_wall_max": gen_secs})
     if rank != 0:
         ctx.close()
         if dist is not None:
@@ -626,9 +678,15 @@ def main():
                              f"stays in L2, so the binding limit is instruction issue (profiles/)"},
         "e2e": {"value": tot["pipe_nodes"] / tot["pipe_wall_max"], "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "api": "nr_batch_submit / nr_batch_wait, two batches in flight; L2 flushed (192 MB write) before "
-                       "every step's upload, on its own stream, the upload ordered after it",
-                "steps": max(args.steps, 50), "one_call_at_a_time": tot["nodes"] / tot["wall_max"]},
+                "api": "nr_batch_submit_matrix / nr_batch_wait (one topology, the [4096 x 105] probability "
+                       "matrix in pinned host memory uploaded every step), two batches in flight; L2 flushed "
+                       "(192 MB write) before every step's upload, on its own stream, the upload ordered after it",
+                "steps": e2e_steps,
+                "per_instance_api": {"value": tot["gen_nodes"] / tot["gen_wall_max"], "h2d_bytes_per_step": int(gen_h2d),
+                                     "d2h_bytes_per_step": int(gen_d2h),
+                                     "api": "nr_batch_submit / nr_batch_wait with 4096 nr_graph descriptions, "
+                                            "the same loop"},
+                "one_call_at_a_time": tot["nodes"] / tot["wall_max"]},
         "gpu_launches": args.steps,
         "clocks": clocks,
     }
@@ -640,6 +698,40 @@ def main():
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_case(args):
+    """One case for a profiler: the same call twice, each after an L2 flush; prints its figures."""
+    import relaibilitygpu_gb300 as nr
+    from relaibilitygpu_gb300 import build as nb
+    nb.build()
+    ctx = nr.Context(0)
+    flush = Flusher(0)
+    batch, opts = None, None
+    for k in range(2):
+        flush()
+        if args.case == "rgg200":
+            g = nr.rgg(200, 600, p_range=(0.9, 0.99), seed=7)
+            r = ctx.reliability(g, g.src, g.dst, capacity=1 << args.arena, target_width=1e-5, order="maxmass",
+                                bucket_shift=2, n_buckets=255, max_nodes=args.budget, timeout_ms=120000.0)
+            out = {"nodes": r.nodes, "waves": r.iterations, "ms": r.ms, "esp": r.esp}
+        else:
+            if batch is None:
+                if args.case == "k15batch":
+                    w = k15_workload()
+                    opts = dict(w["opts"], warps_per_block=2, pages_per_warp=64)
+                else:
+                    gs = nr.batch_instances(BATCH, seed=0)
+                    w = dict(graphs=[g for g in gs if g.n_nodes <= 32])
+                    w["srcs"] = [g.src for g in w["graphs"]]
+                    w["dsts"] = [g.dst for g in w["graphs"]]
+                    opts = dict(target_width=UNEVEN_TARGET, max_nodes=UNEVEN_BUDGET, order="waves",
+                                warps_per_block=2, pages_per_warp=512)
+                batch = nr.Batch(w["graphs"], w["srcs"], w["dsts"])
+            res = ctx.run_batch(batch, capacity=0, raw=True, **opts)
+            out = {"nodes": sum(res[i].nodes for i in range(batch.n)), "ms": res[0].ms}
+        print(json.dumps({"case": args.case, "call": k, **out}), flush=True)
+    ctx.close()
 
 
 def k15_orders(ctx, w, batch, tuned, flush):

@@ -232,6 +232,22 @@ int  nr_batch_submit(nr_context *ctx, int n_instances, const nr_graph *graphs, c
                      void *after_stream, int64_t *ticket);
 int  nr_batch_wait(nr_context *ctx, int64_t ticket);
 
+/* One topology, many probability sets (no reference counterpart: the reference runs one graph
+ * per process): instance i is `topology` with edge probabilities p_matrix[i * n_edges ..
+ * (i + 1) * n_edges) (topology->edge_p is not read) and terminals srcs[i], dsts[i]; n_nodes <=
+ * 32.  The inputs are one matrix, so the host builds no per-instance tables: the topology is
+ * checked once, the terminals per instance, and the matrix goes to the device as it is -- a
+ * plain DMA when the caller allocated it pinned (cudaHostAlloc, or a pinned torch tensor) --
+ * where a scan rejects NaN probabilities (NR_ERR_INVALID from the wait).  Results, tickets and
+ * slots as nr_batch_submit / nr_batch_wait; p_matrix must stay valid and unchanged until the
+ * wait returns. */
+int  nr_batch_submit_matrix(nr_context *ctx, const nr_graph *topology, int n_instances, const double *p_matrix,
+                            const int32_t *srcs, const int32_t *dsts, uint64_t capacity, const nr_options *opt,
+                            nr_result *results, void *after_stream, int64_t *ticket);
+int  nr_reliability_batch_matrix(nr_context *ctx, const nr_graph *topology, int n_instances,
+                                 const double *p_matrix, const int32_t *srcs, const int32_t *dsts,
+                                 uint64_t capacity, const nr_options *opt, nr_result *results);
+
 /* K-terminal reliability (the reference stubs a target set, parallel/Rel_16M.cu:43): the
  * probability that every node of terminals[0..n_terminals) is connected to terminals[0].  The
  * same disjoint decomposition runs over the BFS tree that joins every terminal to terminals[0]

@@ -253,6 +253,9 @@ struct NrSlot {
     WarpRunCfg cfgp{};
     size_t off_out = 0;
     int first_grid = 0, block = 0;
+    bool matrix = false;        // one topology, the caller's probability matrix (gs[0] for every instance)
+    const double *pmat = nullptr;
+    size_t off_flag = 0;        // matrix batches: the NaN flag the device scan sets
     // asynchronous batches: the ticket queued here and what its wait needs
     int64_t ticket = 0;
     bool pending = false;
@@ -328,6 +331,24 @@ struct nr_context {
         pool->run(n, threads - 1, std::max(1, std::min(256, n / (4 * threads))), fn);
     }
 };
+
+// Sets *flag when any of the n doubles is a NaN (integer test of the bit pattern).
+__global__ void nr_nan_scan_kernel(const unsigned long long *p, size_t n, int *flag)
+{
+    int hit = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        hit |= (p[i] & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+    if (__syncthreads_or(hit) && threadIdx.x == 0) *flag = 1;
+}
+
+static cudaError_t nr_launch_nan_scan(const double *p, size_t n, int *flag, cudaStream_t s)
+{
+    if (!n) return cudaSuccess;
+    const int block = 256;
+    const int grid = (int)std::min<size_t>((n + block - 1) / block, 1024);
+    nr_nan_scan_kernel<<<grid, block, 0, s>>>(reinterpret_cast<const unsigned long long *>(p), n, flag);
+    return cudaGetLastError();
+}
 
 static int ensure(void **buf, size_t *have, size_t need)
 {
@@ -1285,7 +1306,7 @@ static int slot_ready(NrSlot &sl)
 // is the index of gs[0] in the caller's batch (for collected children).
 static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_graph *gs, const int32_t *srcs,
                        const int32_t *dsts, const WarpRunCfg &cfg, nr_result *res, PhaseClock &pc,
-                       cudaStream_t after = nullptr, bool uniform = false)
+                       cudaStream_t after = nullptr, bool uniform = false, const double *pmat = nullptr)
 {
     constexpr int NCLS = NR_NCLS;
     const bool lane_ok = cfg.lane && !cfg.fork && !cfg.learned && !cfg.dump && cfg.border != NR_BORDER_LEARNED;
@@ -1310,6 +1331,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     int rc = NR_OK;
     const int B = std::max(1, std::min(NR_HOST_BLOCKS, n / 128));
     auto blk_begin = [&](int b) { return (int)((long long)n * b / B); };
+    size_t pm_off = 0, pm_bytes = 0;          // matrix batches: where the matrix goes, its bytes
+    if (pmat && !uniform) return NR_ERR_INVALID;
     if (uniform) {
         // one topology (the same CSR arrays) for every instance: every instance's tables have the
         // same size, so the offsets are known without a sizes pass -- instance 0's p, the shared
@@ -1327,9 +1350,13 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         const int cls = (lane_ok && gs[0].n_nodes <= NR_LANE_MAX_N && t.rows == 1 && t.w4 <= NR_LANE_MAX_W4)
                             ? NR_LANE_CLS0 + t.w4 - 1
                             : (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + t.w4 - 1;
-        size_t off = align16(sizeof(int) * NCLS);
+        size_t off = align16(sizeof(int) * (NCLS + 1));   // work counters, then a NaN flag
         const size_t tbase = off;
-        off = align16(off + (size_t)n * ib + sb);
+        // matrix batches: the structural part, then the caller's matrix as it is (row i =
+        // instance i's p; 8-byte rows suffice for the kernels' scalar loads)
+        const size_t pm_row = sizeof(double) * (size_t)gs[0].n_edges;
+        const size_t off_pm = pmat ? align16(tbase + sb) : 0;
+        off = pmat ? align16(off_pm + (size_t)n * pm_row) : align16(off + (size_t)n * ib + sb);
         class_count[cls] = n;
         for (int j = 0; j < NCLS; ++j) class_begin[j + 1] = class_begin[j] + class_count[j];
         off_desc = off; off = align16(off + sizeof(NrSmallGraph) * n);
@@ -1343,21 +1370,31 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         hb = static_cast<unsigned char *>(sl.hbuf);
         hdesc = reinterpret_cast<NrSmallGraph *>(hb + off_desc);
         hids = reinterpret_cast<int *>(hb + off_ids);
-        memset(hb + off_cnt, 0, sizeof(int) * NCLS);
-        t.struct_off = (long long)(tbase + ib);
+        memset(hb + off_cnt, 0, sizeof(int) * (NCLS + 1));
+        t.struct_off = (long long)(pmat ? tbase : tbase + ib);
         small_fill_struct(&gs[0], &t, hb + t.struct_off);
         pc.mark("sizes");
         std::atomic<int> bad(NR_OK);
+        const int n_nodes0 = gs[0].n_nodes;
         c->parallel_for(B, 1, [&](int b) {
             for (int i = blk_begin(b), e = blk_begin(b + 1); i < e; ++i) {
-                const int v = validate_shape(&gs[i], srcs[i], dsts[i]);
-                if (v) { bad.store(v); continue; }
                 NrSmallGraph d = t;
                 d.src = srcs[i];
                 d.dst = dsts[i];
-                d.blob_off = (long long)(tbase + (i == 0 ? 0 : ib + sb + (size_t)(i - 1) * ib));
-                d.blob_bytes = (int)(ib + (i == 0 ? sb : 0));
-                if (!small_fill_inst(&gs[i], &d, hb + d.blob_off)) bad.store(NR_ERR_INVALID);
+                if (pmat) {                   // terminals only: the matrix is uploaded as it is
+                    if (d.src < 0 || d.dst < 0 || d.src >= n_nodes0 || d.dst >= n_nodes0) {
+                        bad.store(NR_ERR_INVALID);
+                        continue;
+                    }
+                    d.blob_off = (long long)(off_pm + (size_t)i * pm_row);
+                    d.blob_bytes = (int)pm_row;
+                } else {
+                    const int v = validate_shape(&gs[i], srcs[i], dsts[i]);
+                    if (v) { bad.store(v); continue; }
+                    d.blob_off = (long long)(tbase + (i == 0 ? 0 : ib + sb + (size_t)(i - 1) * ib));
+                    d.blob_bytes = (int)(ib + (i == 0 ? sb : 0));
+                    if (!small_fill_inst(&gs[i], &d, hb + d.blob_off)) bad.store(NR_ERR_INVALID);
+                }
                 desc[i] = d;
                 S.cls[i] = cls;
                 hdesc[i] = d;
@@ -1365,6 +1402,9 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
             }
         });
         if (bad.load() != NR_OK) return bad.load();
+        sl.off_flag = sizeof(int) * NCLS;
+        pm_off = off_pm;
+        pm_bytes = pmat ? (size_t)n * pm_row : 0;
         pc.mark("tables");
     } else {
     // Host blocks: contiguous instance ranges, one task of the worker pool each.  Two
@@ -1544,7 +1584,17 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         NR_CUDA_TRY(cudaEventRecord(c->ev_after, after));
         NR_CUDA_TRY(cudaStreamWaitEvent(s, c->ev_after, 0));
     }
-    NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, up_bytes, cudaMemcpyHostToDevice, s));
+    if (pmat) {
+        // counters and structural part, the caller's matrix straight from its memory (a plain DMA
+        // when it is pinned), descriptors and ids; then a scan of the matrix for NaN on the device
+        NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, pm_off, cudaMemcpyHostToDevice, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(wb + pm_off, pmat, pm_bytes, cudaMemcpyHostToDevice, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(wb + off_desc, hb + off_desc, up_bytes - off_desc, cudaMemcpyHostToDevice, s));
+        NR_CUDA_TRY(nr_launch_nan_scan(reinterpret_cast<const double *>(wb + pm_off), pm_bytes / sizeof(double),
+                                       reinterpret_cast<int *>(wb + sl.off_flag), s));
+    } else {
+        NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, up_bytes, cudaMemcpyHostToDevice, s));
+    }
     NR_CUDA_TRY(cudaEventRecord(sl.ev0, s));
     int first_grid = 0;
     for (int j = 0; j < NCLS; ++j) {
@@ -1597,6 +1647,9 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     NR_CUDA_TRY(cudaEventRecord(sl.ev1, s));
     NrWarpOut *hout = reinterpret_cast<NrWarpOut *>(hb + off_out);
     NR_CUDA_TRY(cudaMemcpyAsync(hout, wb + off_out, sizeof(NrWarpOut) * n, cudaMemcpyDeviceToHost, s));
+    if (pmat) NR_CUDA_TRY(cudaMemcpyAsync(hb + sl.off_flag, wb + sl.off_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    sl.matrix = (pmat != nullptr);
+    sl.pmat = pmat;
     sl.n = n; sl.gs = gs; sl.srcs = srcs; sl.dsts = dsts; sl.res = res;
     sl.cfgp = cfgp; sl.off_out = off_out; sl.first_grid = first_grid; sl.block = block;
     pc.mark("enqueue");
@@ -1615,12 +1668,16 @@ static int warp_finish(nr_context *c, NrSlot &sl, int base, std::vector<int> *ha
     const nr_graph *gs = sl.gs;
     const NrSmallGraph *desc = sl.scratch.desc.data();
     const NrWarpOut *hout = reinterpret_cast<const NrWarpOut *>(static_cast<unsigned char *>(sl.hbuf) + sl.off_out);
+    if (sl.matrix && *reinterpret_cast<const int *>(static_cast<unsigned char *>(sl.hbuf) + sl.off_flag))
+        return NR_ERR_INVALID;                // a NaN probability in the caller's matrix
+    const int gstride = sl.matrix ? 0 : 1;    // matrix batches: one topology for every instance
     std::atomic<int> n_hand(0), n_check(0);
     c->parallel_for(n, 256, [&](int i) {
         nr_result *r = &sl.res[i];
         memset(r, 0, sizeof(*r));
-        r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = sl.srcs[i]; r->dst = sl.dsts[i];
-        r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
+        const nr_graph &gi = gs[i * gstride];
+        r->n_nodes = gi.n_nodes; r->n_edges = gi.n_edges; r->src = sl.srcs[i]; r->dst = sl.dsts[i];
+        r->mask_words = std::max(1, (2 * gi.n_edges + 31) / 32);
         if (hout[i].status == 2) { n_hand.fetch_add(1); return; }
         if (hout[i].status == NR_LANE_STATUS_CHECK) { n_check.fetch_add(1); return; }
         fill_from_warp(hout[i], sl.cfgp, desc[i].w4, r);
@@ -1713,10 +1770,13 @@ static WarpRunCfg batch_cfg(const nr_options &o, uint64_t capacity)
 // Instances the warp engine handed over (exhaustive runs that outgrew a warp's
 // budget) finish on the whole-GPU engine.
 static int run_handover(nr_context *c, const std::vector<int> &handover, const nr_graph *gs, const int32_t *srcs,
-                        const int32_t *dsts, uint64_t capacity, const nr_options &o, nr_result *res)
+                        const int32_t *dsts, uint64_t capacity, const nr_options &o, nr_result *res,
+                        const double *pmat = nullptr)
 {
     for (int i : handover) {
-        const int rc = run_grid_small(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, &res[i]);
+        nr_graph gi = pmat ? gs[0] : gs[i];      // matrix batches: the topology with row i of the matrix
+        if (pmat) gi.edge_p = pmat + (size_t)i * gi.n_edges;
+        const int rc = run_grid_small(c, &gi, srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, &res[i]);
         if (rc) return rc;
     }
     return NR_OK;
@@ -1764,7 +1824,8 @@ static int slot_finish(nr_context *c, NrSlot &sl)
     std::vector<int> handover;
     sl.pending = false;
     int rc = warp_finish(c, sl, 0, &handover, pc);
-    if (!rc) rc = run_handover(c, handover, sl.gs, sl.srcs, sl.dsts, sl.capacity, sl.opt, sl.res);
+    if (!rc) rc = run_handover(c, handover, sl.gs, sl.srcs, sl.dsts, sl.capacity, sl.opt, sl.res,
+                               sl.matrix ? sl.pmat : nullptr);
     return rc;
 }
 
@@ -1842,6 +1903,53 @@ extern "C" int nr_batch_wait(nr_context *c, int64_t ticket)
     const int rc = it->second;
     c->done_rc.erase(it);
     return rc;
+}
+
+// One topology, a matrix of probability sets (nr.h): the topology is checked once, the
+// terminals per instance, the matrix for NaN on the device; no per-instance host tables.
+extern "C" int nr_batch_submit_matrix(nr_context *c, const nr_graph *topo, int n, const double *p_matrix,
+                                      const int32_t *srcs, const int32_t *dsts, uint64_t capacity,
+                                      const nr_options *opt, nr_result *res, void *after_stream, int64_t *ticket)
+{
+    if (!c || !ticket || !topo || n < 0 || (n > 0 && (!p_matrix || !srcs || !dsts || !res))) return NR_ERR_INVALID;
+    nr_options o;
+    if (opt) o = *opt; else nr_options_default(&o);
+    std::lock_guard<std::mutex> lock(c->mu);
+    const int64_t t = c->next_ticket++;
+    *ticket = t;
+    if (n == 0) { record_done(c, t, NR_OK); return NR_OK; }
+    int rc = validate_shape(topo, srcs[0], dsts[0]);
+    if (!rc) rc = validate_structure(topo);
+    if (!rc && topo->n_nodes > NR_SMALL_MAX_N) rc = NR_ERR_UNSUPPORTED;
+    if (!rc) rc = batch_options_ok(c, o);
+    if (rc) { record_done(c, t, rc); return rc; }
+    NR_CUDA_TRY(cudaSetDevice(c->device));
+    PhaseClock pc;
+    NrSlot &sl = c->slot[(t - 1) % NR_SLOTS];
+    if (sl.pending) record_done(c, sl.ticket, slot_finish(c, sl));
+    rc = warp_submit(c, sl, 0, n, topo, srcs, dsts, batch_cfg(o, capacity), res, pc,
+                     static_cast<cudaStream_t>(after_stream), true, p_matrix);
+    if (rc) {
+        cudaStreamSynchronize(sl.stream);
+        sl.matrix = false;
+        record_done(c, t, rc);
+        return rc;
+    }
+    sl.ticket = t;
+    sl.pending = true;
+    sl.capacity = capacity;
+    sl.opt = o;
+    return NR_OK;
+}
+
+extern "C" int nr_reliability_batch_matrix(nr_context *c, const nr_graph *topo, int n, const double *p_matrix,
+                                           const int32_t *srcs, const int32_t *dsts, uint64_t capacity,
+                                           const nr_options *opt, nr_result *res)
+{
+    int64_t t = 0;
+    const int rc = nr_batch_submit_matrix(c, topo, n, p_matrix, srcs, dsts, capacity, opt, res, nullptr, &t);
+    if (rc) return rc;
+    return nr_batch_wait(c, t);
 }
 
 extern "C" int nr_reliability_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs,

@@ -80,6 +80,7 @@ EXPORTS = [
     "nr_reliability_batch", "nr_batch_submit", "nr_batch_wait", "nr_format_result", "nr_reliability_noalloc", "nr_autotune",
     "nr_mlp_param_count", "nr_mlp_init", "nr_mlp_grad", "nr_mlp_train", "nr_mlp_infer", "nr_context_set_model",
     "nr_collect_children", "nr_checkpoint_save", "nr_checkpoint_resume", "nr_reliability_kterminal",
+    "nr_batch_submit_matrix", "nr_reliability_batch_matrix",
 ]
 
 _lib_handle: Optional[C.CDLL] = None
@@ -124,6 +125,13 @@ def lib() -> C.CDLL:
     L.nr_batch_submit.restype = C.c_int
     L.nr_batch_wait.argtypes = [C.c_void_p, C.c_int64]
     L.nr_batch_wait.restype = C.c_int
+    L.nr_batch_submit_matrix.argtypes = [C.c_void_p, C.POINTER(NrGraph), C.c_int, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_uint64, C.POINTER(NrOptions), C.POINTER(NrResult),
+                                         C.c_void_p, C.POINTER(C.c_int64)]
+    L.nr_batch_submit_matrix.restype = C.c_int
+    L.nr_reliability_batch_matrix.argtypes = [C.c_void_p, C.POINTER(NrGraph), C.c_int, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_uint64, C.POINTER(NrOptions), C.POINTER(NrResult)]
+    L.nr_reliability_batch_matrix.restype = C.c_int
     L.nr_reliability_noalloc.argtypes = [C.POINTER(NrGraph), C.c_int, C.c_int, C.POINTER(NrOptions),
                                          C.POINTER(NrResult)]
     L.nr_reliability_noalloc.restype = C.c_int
@@ -365,6 +373,28 @@ class Context:
             o = self._opt_cache[key] = make_options(**opts)
         return o
 
+    def submit_matrix(self, mb: "MatrixBatch", capacity: int = 0, after_stream: int = 0,
+                      options: Optional[NrOptions] = None, **opts) -> int:
+        """Queue a MatrixBatch with nr_batch_submit_matrix and return its ticket (results in
+        mb.res after wait(ticket))."""
+        o = options if options is not None else self._options(opts)
+        t = C.c_int64()
+        _check(lib().nr_batch_submit_matrix(self.h, C.byref(mb.view.c), mb.n, C.c_void_p(mb.p_addr),
+                                            C.c_void_p(mb.s.ctypes.data), C.c_void_p(mb.d.ctypes.data),
+                                            int(capacity), C.byref(o), mb.res, C.c_void_p(after_stream or None),
+                                            C.byref(t)))
+        return t.value
+
+    def run_matrix(self, mb: "MatrixBatch", capacity: int = 0, raw: bool = False, **opts):
+        """Solve a MatrixBatch with nr_reliability_batch_matrix."""
+        o = self._options(opts)
+        _check(lib().nr_reliability_batch_matrix(self.h, C.byref(mb.view.c), mb.n, C.c_void_p(mb.p_addr),
+                                                 C.c_void_p(mb.s.ctypes.data), C.c_void_p(mb.d.ctypes.data),
+                                                 int(capacity), C.byref(o), mb.res))
+        if raw:
+            return mb.res
+        return [Result.from_raw(mb.res[i]) for i in range(mb.n)]
+
     def wait(self, ticket: int) -> None:
         """Finish a submitted batch (nr_batch_wait): its Batch.res is filled."""
         _check(lib().nr_batch_wait(self.h, int(ticket)))
@@ -388,6 +418,30 @@ def autotune(ctx: "Context", batch: "Batch", capacity: int = 0, **opts):
                              batch.d.ctypes.data_as(C.POINTER(C.c_int32)), int(capacity), C.byref(o),
                              C.byref(best), C.byref(ms)))
     return options_dict(best), ms.value
+
+
+class MatrixBatch:
+    """One topology with a matrix of probability sets (nr_batch_submit_matrix): instance i has
+    edge probabilities p[i] and terminals srcs[i], dsts[i] (scalars: the same for every one).
+
+    `p` is a float64 array [n, n_edges] (C order), or the int address of such a matrix (e.g. a
+    pinned torch tensor's data_ptr(), which makes the upload a plain DMA) with n given."""
+
+    def __init__(self, topology: Graph, p, srcs, dsts, n: Optional[int] = None):
+        self.view = _GraphView(topology)
+        if isinstance(p, int):
+            if n is None:
+                raise ValueError("n is needed with a matrix address")
+            self.p_addr, self.n, self._p = p, int(n), None
+        else:
+            self._p = np.ascontiguousarray(p, dtype=np.float64)
+            if self._p.ndim != 2 or self._p.shape[1] != topology.n_edges:
+                raise ValueError("p must be [n_instances, n_edges]")
+            self.n = self._p.shape[0]
+            self.p_addr = self._p.ctypes.data
+        self.s = np.ascontiguousarray(np.broadcast_to(np.asarray(srcs, dtype=np.int32), (self.n,)))
+        self.d = np.ascontiguousarray(np.broadcast_to(np.asarray(dsts, dtype=np.int32), (self.n,)))
+        self.res = (NrResult * self.n)()
 
 
 class Batch:
