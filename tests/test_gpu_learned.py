@@ -122,3 +122,56 @@ def test_trained_scorer_gain_over_plain_order(L, engine_lib, family, capsys):
         print(f"\n[{family}] subproblems to the bound over {len(gs)} instances: plain {n_plain}, "
               f"learned {n_learned} (ratio {n_learned / n_plain:.3f})")
     assert n_learned <= 1.5 * n_plain
+
+
+def test_learned_branch_order_is_exact_and_rigorous(L, engine_lib, oracle):
+    """The learned branch order (NR_BORDER_LEARNED: the scorer ranks a path's UNKNOWN edges) changes
+    the decomposition, never its exactness: truncated runs stop at the target and bracket the
+    brute-force value, with any parameters."""
+    import os
+    from relaibilitygpu_gb300 import graphs
+    with engine_lib.Context(0) as ctx:
+        for params in ([L.load()] if os.path.exists(L.DEFAULT_MODEL) else []) + [L.init_params(3)]:
+            L.set_model(ctx, params)
+            for g, s, t in [(graphs.grid(4, 4, p_range=(0.6, 0.95), seed=1), 0, 15),
+                            (graphs.complete(7, p_range=(0.5, 0.95), seed=2), 0, 6)]:
+                exact = oracle.brute(g, s, t)
+                for tw in (1e-3, 1e-6):
+                    for order in ("maxmass", "learned"):
+                        r = ctx.reliability(g, s, t, target_width=tw, order=order, bucket_shift=0, n_buckets=64,
+                                            branch_order="learned", capacity=1 << 16)
+                        assert r.stop == 1 and r.esp <= tw and r.spilled == 0
+                        assert r.R <= exact * (1 + 1e-12) and exact <= (r.R + r.esp) * (1 + 1e-12)
+
+
+@pytest.mark.parametrize("family", ["grid4x4_u80_99_1e-6", "k10_u50_95_1e-4", "k15_u90_99_1e-6"])
+def test_branch_order_measured(L, engine_lib, family, capsys):
+    """Subproblems to the bound with the plain max-mass queue under each branch order, summed over
+    64 held-out instances: the reference's src-side-first order, least reliable first (p_asc), and
+    the learned order.  The printed line is the measurement; the test pins rigour."""
+    import os
+    if not os.path.exists(L.DEFAULT_MODEL):
+        pytest.skip("no trained scorer")
+    from relaibilitygpu_gb300 import graphs
+    if family.startswith("grid"):
+        gs, target = [graphs.grid(4, 4, p_range=(0.8, 0.99), seed=70_000 + s) for s in range(64)], 1e-6
+    elif family.startswith("k10"):
+        gs, target = [graphs.complete(10, p_range=(0.5, 0.95), seed=60_000 + s) for s in range(64)], 1e-4
+    else:
+        gs, target = [graphs.complete(15, p_range=(0.9, 0.99), seed=50_000 + s) for s in range(64)], 1e-6
+    srcs, dsts = [0] * len(gs), [g.n_nodes - 1 for g in gs]
+    opts = dict(target_width=target, order="maxmass", bucket_shift=0, n_buckets=64, capacity=1 << 16,
+                small_kernel="group")
+    counts = {}
+    with engine_lib.Context(0) as ctx:
+        L.set_model(ctx, L.load())
+        runs = {b: ctx.reliability_batch(gs, srcs, dsts, branch_order=b, **opts) for b in ("src", "p_asc", "learned")}
+    for b, res in runs.items():
+        for r, a in zip(res, runs["src"]):
+            assert r.stop == 1 and r.esp <= target
+            assert max(a.R, r.R) <= min(a.R + a.esp, r.R + r.esp) + 1e-15
+        counts[b] = sum(r.nodes for r in res)
+    with capsys.disabled():
+        print(f"\n[{family}] subproblems to the bound over {len(gs)} instances, max-mass queue: "
+              + ", ".join(f"{b} {n}" for b, n in counts.items())
+              + f" (learned / src {counts['learned'] / counts['src']:.3f})")
