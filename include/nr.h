@@ -274,8 +274,9 @@ int  nr_checkpoint_resume(nr_context *ctx, const char *path, const nr_graph *gra
  * up to 4096 instances of the batch for each candidate setting -- bucket
  * resolution (bucket_shift -1..2, where -1 is one bucket: breadth-first waves), pages per warp (64, 512
  * or 4096, how much of the queue a warp holds; never above capacity) and warps per block (2, 4, 8) -- and
- * writes the fastest into *best (based on *opt), with its device time in
- * *best_ms.  The bucket resolution is searched only for opt->order ==
+ * writes the best into *best (based on *opt), with its device time in *best_ms:
+ * the fewest instances whose queue spilled, then the shortest time (best of three runs, and
+ * three more for the three leaders).  The bucket resolution is searched only for opt->order ==
  * NR_ORDER_AUTO with a target width: NR_ORDER_WAVES holds one bucket and
  * NR_ORDER_MAXMASS / NR_ORDER_LEARNED hold opt's bucket_shift and n_buckets.  Every candidate returns a valid result; the choice changes time
  * and, for truncated runs, where the stop falls. */
