@@ -28,6 +28,8 @@ check against the oracle (oracle/, the CPU restatement of the reference):
   k25       -- K25, p ~ U[0.9, 0.99], to ESP width <= 1e-5: plain vs learned order
   rgg200    -- random geometric graph N=200, E=600: the bucketed whole-GPU queue toward
                1e-5, the bracket at a 20M-subproblem budget
+  branch_order -- grids 4x4, K10 and K15 batches: time to the bound under the reference's
+               branch order, least reliable first, and the learned one
 (--quick skips them.)
 
 --impl reference times the reference algorithm on the host cores: the CPU
@@ -507,6 +509,40 @@ def cfg_k25(ctx, flush):
     return out
 
 
+def cfg_branch_order(ctx, flush):
+    """Time to the bound under each branch order -- the reference's (src side first), least
+    reliable first, and the learned scorer's -- with the plain max-mass queue, on families whose
+    trees have room (grids, K10) and on the metric's own (K15): batch device time and subproblems."""
+    import relaibilitygpu_gb300 as nr
+    from relaibilitygpu_gb300 import learned as LR
+    if not os.path.exists(LR.DEFAULT_MODEL):
+        return {"skipped": "no trained scorer"}
+    LR.set_model(ctx, LR.load())
+    fams = {"grid4x4_u80_99_1e-6": ([nr.grid(4, 4, p_range=(0.8, 0.99), seed=70_000 + s) for s in range(1024)], 1e-6),
+            "k10_u50_95_1e-4": ([nr.complete(10, p_range=(0.5, 0.95), seed=60_000 + s) for s in range(1024)], 1e-4),
+            "k15_u90_99_1e-6": ([nr.complete(15, p_range=(0.9, 0.99), seed=50_000 + s) for s in range(1024)], 1e-6)}
+    out = {"queue": "max-mass (one bucket per factor of two, 64 buckets)", "instances": 1024}
+    for name, (gs, tw) in fams.items():
+        b = nr.Batch(gs, [0] * len(gs), [g.n_nodes - 1 for g in gs])
+        rec = {}
+        for border in ("src", "p_asc", "learned"):
+            ms = []
+            for k in range(3):
+                flush()
+                res = ctx.run_batch(b, capacity=1 << 17, raw=True, target_width=tw, order="maxmass", bucket_shift=0,
+                                    n_buckets=64, branch_order=border)
+                if k >= 1:
+                    ms.append(res[0].ms)
+            n_b = sum(res[i].nodes for i in range(b.n))
+            rec[border] = {"batch_ms": statistics.median(ms), "subproblems": n_b,
+                           "spilled_instances": sum(1 for i in range(b.n) if res[i].spilled),
+                           "kernel": nr.engine.KERNELS.get(res[0].kernel, "")}
+        rec["learned_over_src_time"] = rec["learned"]["batch_ms"] / rec["src"]["batch_ms"]
+        rec["learned_over_src_subproblems"] = rec["learned"]["subproblems"] / rec["src"]["subproblems"]
+        out[name] = rec
+    return out
+
+
 def cfg_rgg200(ctx, flush):
     import oracle as og
     import relaibilitygpu_gb300 as nr
@@ -640,7 +676,8 @@ def main():
         configs = {}
         for name, fn in (("grid4x4", lambda: cfg_grid4x4(ctx, flush)), ("k10", lambda: cfg_k10(ctx, flush)),
                          ("uneven", lambda: cfg_uneven(ctx, flush, local)), ("k25", lambda: cfg_k25(ctx, flush)),
-                         ("rgg200", lambda: cfg_rgg200(ctx, flush))):
+                         ("rgg200", lambda: cfg_rgg200(ctx, flush)),
+                         ("branch_order", lambda: cfg_branch_order(ctx, flush))):
             t0 = time.perf_counter()
             try:
                 configs[name] = fn()
