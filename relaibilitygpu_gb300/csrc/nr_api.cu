@@ -813,7 +813,32 @@ static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg
     uint32_t *arc = reinterpret_cast<uint32_t *>(blob->data() + wg->off_arc);
     for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
     for (int u = 0; u <= n; ++u) row[u] = g->row_ptr[u];
-    for (int j = 0; j < g->n_arcs; ++j) arc[j] = ((uint32_t)g->edge_id[j] << 10) | (uint32_t)g->col_idx[j];
+    for (int j = 0; j < g->n_arcs; ++j)
+        arc[j] = ((uint32_t)g->edge_id[j] << NR_WIDE_HEAD_BITS) | (uint32_t)g->col_idx[j];
+    wg->tables_global = off > NR_WIDE_STAGE_MAX;
+}
+
+static int smem_optin(nr_context *c)
+{
+    if (!c->smem_optin) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device) != cudaSuccess) {
+            cudaGetLastError();
+            return 48 << 10;
+        }
+        c->smem_optin = v;
+    }
+    return c->smem_optin;
+}
+
+// Threads of a wide kernel's block: up to NR_WIDE_BLOCK, as many warps as the block's shared
+// memory holds (tables, unless read from global memory, and each warp's scratch); 0 if not one.
+static int wide_block(nr_context *c, const NrWideGraph &wg)
+{
+    const size_t lim = (size_t)smem_optin(c);
+    for (int w = NR_WIDE_BLOCK / 32; w >= 1; --w)
+        if (nr_wide_block_shm(wg, w) <= lim) return 32 * w;
+    return 0;
 }
 
 static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
@@ -825,11 +850,11 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     std::vector<unsigned char> blob;
     build_wide_blob(g, src, dst, &wg, &blob, terms, nt);
     const int W4 = wg.w4;
-    if (W4 > NR_WIDE_MAX_W4) return NR_ERR_UNSUPPORTED;
     const void *kfn = nr_grid_wide_kernel_ptr(W4);
     if (!kfn) return NR_ERR_UNSUPPORTED;
-    const int block = NR_WIDE_BLOCK;
-    const size_t smem = (size_t)wg.blob_bytes + (block / 32) * nr_wide_warp_shm(wg.n, W4);
+    const int block = wide_block(c, wg);
+    if (!block) return NR_ERR_UNSUPPORTED;
+    const size_t smem = nr_wide_block_shm(wg, block / 32);
     NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
     int bps = 0;
     NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
@@ -1005,11 +1030,11 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     std::vector<unsigned char> blob;
     build_wide_blob(g, src, dst, &wg, &blob, terms, nt);
     const int W4 = wg.w4;
-    if (W4 > NR_WIDE_MAX_W4) return NR_ERR_UNSUPPORTED;
     const void *kfn = nr_bucket_wide_kernel_ptr(W4);
     if (!kfn) return NR_ERR_UNSUPPORTED;
-    const int block = NR_WIDE_BLOCK;
-    const size_t smem = (size_t)wg.blob_bytes + (block / 32) * nr_wide_warp_shm(wg.n, W4);
+    const int block = wide_block(c, wg);
+    if (!block) return NR_ERR_UNSUPPORTED;
+    const size_t smem = nr_wide_block_shm(wg, block / 32);
     NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
     int bps = 0;
     NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));

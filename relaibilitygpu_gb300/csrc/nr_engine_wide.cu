@@ -1,4 +1,5 @@
-// nr_engine_wide.cu -- kernels for graphs with 33..1024 nodes (mask blocks 1..16).
+// nr_engine_wide.cu -- kernels for graphs with 33..16384 nodes: mask blocks 1..16 compiled in,
+// wider masks (up to 65535 edges) in the runtime-width instantiation W4 = 0.
 #include "nr_wide.cuh"
 
 const void *nr_grid_wide_kernel_ptr(int w4)
@@ -20,7 +21,7 @@ const void *nr_grid_wide_kernel_ptr(int w4)
     case 14: return (const void *)nr_grid_wide_kernel<14>;
     case 15: return (const void *)nr_grid_wide_kernel<15>;
     case 16: return (const void *)nr_grid_wide_kernel<16>;
-    default: return nullptr;
+    default: return w4 > NR_WIDE_MAX_W4 ? (const void *)nr_grid_wide_kernel<0> : nullptr;
     }
 }
 
@@ -43,6 +44,6 @@ const void *nr_bucket_wide_kernel_ptr(int w4)
     case 14: return (const void *)nr_bucket_wide_kernel<14>;
     case 15: return (const void *)nr_bucket_wide_kernel<15>;
     case 16: return (const void *)nr_bucket_wide_kernel<16>;
-    default: return nullptr;
+    default: return w4 > NR_WIDE_MAX_W4 ? (const void *)nr_bucket_wide_kernel<0> : nullptr;
     }
 }

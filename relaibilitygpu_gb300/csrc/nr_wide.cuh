@@ -33,19 +33,25 @@
 
 #include "nr_expand.cuh"
 
-#define NR_WIDE_MAX_N 1024
-#define NR_WIDE_MAX_W4 16
+#define NR_WIDE_MAX_N 16384     // arcs carry a 14-bit head; parents pack (node << 16 | edge)
+#define NR_WIDE_MAX_W4 16       // widest mask with a compiled width; wider masks run the
+                                // runtime-width instantiation (W4 = 0): masks up to 65535 edges
+#define NR_WIDE_HEAD_BITS 14
+#define NR_WIDE_STAGE_MAX (64u << 10)   // graph tables above this are read from global memory
 #define NR_WIDE_BLOCK 128
 #define NR_WIDE_MAX_NB 255      // bucket schedule: bucket ids fit a byte
 #define NR_WIDE_FREE 0xffu      // bucket byte of a free arena slot
 
 // Graph tables of one wide instance: p[E], q[E] (double), row_ptr[n+1] (int),
-// arcs[n_arcs] (u32 = eid << 10 | head).  Offsets from the blob start, 16-byte aligned.
+// arcs[n_arcs] (u32 = eid << 14 | head).  Offsets from the blob start, 16-byte aligned.
+// Tables up to NR_WIDE_STAGE_MAX are staged into every block's shared memory; larger ones (the
+// reference's 6301-node directed fixture: 440 KB) are read from global memory (L2).
 struct NrWideGraph {
     int n, e, w4, src, dst, n_arcs, nwd;
     int off_p, off_q, off_row, off_arc, blob_bytes;
     int nk;                     // K-terminal: terminals other than src (0: two-terminal, dst)
     int off_kmask;              // K-terminal: bitmask of the terminals, nwd words
+    int tables_global;          // 1: the tables stay in global memory
 };
 
 // A block's share of the stop test, written at the end of each wave.
@@ -112,12 +118,20 @@ struct NrBucketWideParams {
     unsigned long long init_nodes, init_leaves, init_dead, init_trunc, init_spilled;
 };
 
-// per-warp shared memory: mask words, frontier / next / visited bitmasks,
-// packed parents, frontier list, path hops.  Rounded to 16 bytes: each
-// warp's region starts with the mask, which is written with 16-byte stores.
+// per-warp shared memory: mask words, a working copy of them (runtime-width children),
+// frontier / next / visited bitmasks (nwd words each, at least 32), packed parents, frontier
+// list, path hops, K-terminal visit order.  Rounded to 16 bytes: each warp's region starts with
+// the mask, which is written with 16-byte stores.
+__host__ __device__ inline int nr_wide_nwd32(int n) { return (((n + 31) / 32 + 31) / 32) * 32; }
 __host__ __device__ inline size_t nr_wide_warp_shm(int n, int w4)
 {
-    return ((((size_t)4 * w4 + 3 * 32 + 4 * (size_t)n) * 4) + 15) & ~(size_t)15;
+    return ((((size_t)8 * w4 + 3 * (size_t)nr_wide_nwd32(n) + 4 * (size_t)n) * 4) + 15) & ~(size_t)15;
+}
+
+// shared memory of a block of `warps` warps: staged tables (unless read from global) + scratch
+__host__ __device__ inline size_t nr_wide_block_shm(const NrWideGraph &g, int warps)
+{
+    return (g.tables_global ? 0 : (size_t)g.blob_bytes) + (size_t)warps * nr_wide_warp_shm(g.n, g.w4);
 }
 
 // Where a step's children go.
@@ -143,30 +157,40 @@ struct NrWideView {
     const int *row;
     const uint32_t *arc;
     const uint32_t *kmask;           // K-terminal terminals (nullptr: two-terminal)
-    uint32_t *m, *F, *NF, *VIS, *par, *list, *hops, *order;
+    uint32_t *m, *wk, *F, *NF, *VIS, *par, *list, *hops, *order;
 };
 
-template <int W4>
-__device__ __forceinline__ NrWideView nr_wide_view(unsigned char *smem, const NrWideGraph &g)
+// tables: the staged copy in shared memory, or the blob in global memory (g.tables_global)
+__device__ __forceinline__ NrWideView nr_wide_view(unsigned char *smem, const unsigned char *blob,
+                                                   const NrWideGraph &g)
 {
-    constexpr int NW = 4 * W4;
+    const int NW = 4 * g.w4, NWD = nr_wide_nwd32(g.n);
+    const unsigned char *tb = g.tables_global ? blob : smem;
     NrWideView v;
-    v.p = reinterpret_cast<const double *>(smem + g.off_p);
-    v.q = reinterpret_cast<const double *>(smem + g.off_q);
-    v.row = reinterpret_cast<const int *>(smem + g.off_row);
-    v.arc = reinterpret_cast<const uint32_t *>(smem + g.off_arc);
+    v.p = reinterpret_cast<const double *>(tb + g.off_p);
+    v.q = reinterpret_cast<const double *>(tb + g.off_q);
+    v.row = reinterpret_cast<const int *>(tb + g.off_row);
+    v.arc = reinterpret_cast<const uint32_t *>(tb + g.off_arc);
     const int warp = threadIdx.x >> 5;
-    uint32_t *ws = reinterpret_cast<uint32_t *>(smem + g.blob_bytes + (size_t)warp * nr_wide_warp_shm(g.n, W4));
+    uint32_t *ws = reinterpret_cast<uint32_t *>(smem + (g.tables_global ? 0 : g.blob_bytes) +
+                                                (size_t)warp * nr_wide_warp_shm(g.n, g.w4));
     v.m = ws;                        // [NW] mask words of the current subproblem
-    v.F = v.m + NW;                  // [32] frontier
-    v.NF = v.F + 32;                 // [32] next frontier
-    v.VIS = v.NF + 32;               // [32] visited
-    v.par = v.VIS + 32;              // [n] (parent << 16) | edge
+    v.wk = v.m + NW;                 // [NW] working copy (runtime-width children)
+    v.F = v.wk + NW;                 // [NWD] frontier
+    v.NF = v.F + NWD;                // [NWD] next frontier
+    v.VIS = v.NF + NWD;              // [NWD] visited
+    v.par = v.VIS + NWD;             // [n] (parent << 16) | edge
     v.list = v.par + g.n;            // [n] frontier nodes
     v.hops = v.list + g.n;           // [n] path edges, dst side first
     v.order = v.hops + g.n;          // [n] K-terminal: visit order of the search
-    v.kmask = g.nk ? reinterpret_cast<const uint32_t *>(smem + g.off_kmask) : nullptr;
+    v.kmask = g.nk ? reinterpret_cast<const uint32_t *>(tb + g.off_kmask) : nullptr;
     return v;
+}
+
+// Load a record's mask (w4 16-byte blocks) into the warp's shared copy.
+__device__ __forceinline__ void nr_wide_load_mask(uint32_t *m, const uint4 *src, int w4)
+{
+    for (int k = threadIdx.x & 31; k < w4; k += 32) reinterpret_cast<uint4 *>(m)[k] = __ldcg(src + k);
 }
 
 // BFS of the warp from src over the arcs whose edge is not down (up_only:
@@ -197,30 +221,34 @@ __device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideVi
     int no = 0;
     bool found = kmode ? (g.nk == 0) : (src == dst);
     while (!found) {
-        // compact the frontier into list[]
-        const uint32_t fw = (lane < nwd) ? F[lane] : 0u;
-        const int cnt = __popc(fw);
-        int pre = cnt;
-        for (int off = 1; off < 32; off <<= 1) {
-            const int t = __shfl_up_sync(NR_FULL, pre, off);
-            if (lane >= off) pre += t;
+        // compact the frontier into list[] (and, K-terminal, append it to the visit order),
+        // 32 bitmask words at a time
+        int total = 0;
+        for (int c = 0; c < nwd; c += 32) {
+            const uint32_t fw = (c + lane < nwd) ? F[c + lane] : 0u;
+            const int cnt = __popc(fw);
+            int pre = cnt;
+            for (int off = 1; off < 32; off <<= 1) {
+                const int t = __shfl_up_sync(NR_FULL, pre, off);
+                if (lane >= off) pre += t;
+            }
+            int o = total + pre - cnt;
+            for (uint32_t b = fw; b; b &= b - 1) list[o++] = (uint32_t)((c + lane) * 32 + __ffs(b) - 1);
+            if (kmode) {
+                int oo = no + total + pre - cnt;
+                for (uint32_t b = fw; b; b &= b - 1) v.order[oo++] = (uint32_t)((c + lane) * 32 + __ffs(b) - 1);
+            }
+            total += __shfl_sync(NR_FULL, pre, 31);
         }
-        const int total = __shfl_sync(NR_FULL, pre, 31);
         if (total == 0) break;
-        int o = pre - cnt;
-        for (uint32_t b = fw; b; b &= b - 1) list[o++] = (uint32_t)(lane * 32 + __ffs(b) - 1);
-        if (kmode) {
-            int oo = no + pre - cnt;
-            for (uint32_t b = fw; b; b &= b - 1) v.order[oo++] = (uint32_t)(lane * 32 + __ffs(b) - 1);
-            no += total;
-        }
+        if (kmode) no += total;
         for (int i = lane; i < nwd; i += 32) NF[i] = 0u;
         __syncwarp();
         for (int i = lane; i < total; i += 32) {
             const uint32_t u = list[i];
             for (int j = v.row[u]; j < v.row[u + 1]; ++j) {
                 const uint32_t a = v.arc[j];
-                const uint32_t w = a & 1023u, e = a >> 10;
+                const uint32_t w = a & ((1u << NR_WIDE_HEAD_BITS) - 1u), e = a >> NR_WIDE_HEAD_BITS;
                 if (((m[e >> 4] >> ((e & 15) << 1)) & sel) == want && !((VIS[w >> 5] >> (w & 31)) & 1u)) {
                     atomicOr(&NF[w >> 5], 1u << (w & 31));
                     atomicMin(&par[w], (u << 16) | e);
@@ -247,17 +275,18 @@ __device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideVi
     }
     if (kmode && found) {
         // the last level searched: the new frontier, appended in ascending node order
-        const uint32_t fw = (lane < nwd) ? F[lane] : 0u;
-        const int cnt = __popc(fw);
-        int pre = cnt;
-        for (int off = 1; off < 32; off <<= 1) {
-            const int t = __shfl_up_sync(NR_FULL, pre, off);
-            if (lane >= off) pre += t;
+        for (int c = 0; c < nwd; c += 32) {
+            const uint32_t fw = (c + lane < nwd) ? F[c + lane] : 0u;
+            const int cnt = __popc(fw);
+            int pre = cnt;
+            for (int off = 1; off < 32; off <<= 1) {
+                const int t = __shfl_up_sync(NR_FULL, pre, off);
+                if (lane >= off) pre += t;
+            }
+            int oo = no + pre - cnt;
+            for (uint32_t b = fw; b; b &= b - 1) v.order[oo++] = (uint32_t)((c + lane) * 32 + __ffs(b) - 1);
+            no += __shfl_sync(NR_FULL, pre, 31);
         }
-        const int total = __shfl_sync(NR_FULL, pre, 31);
-        int oo = no + pre - cnt;
-        for (uint32_t b = fw; b; b &= b - 1) v.order[oo++] = (uint32_t)(lane * 32 + __ffs(b) - 1);
-        no += total;
         __syncwarp();
     }
     if (kmode) *n_order = no;
@@ -265,18 +294,15 @@ __device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideVi
 }
 
 // Write one child record (mask = m with edge e's state bits cleared by `clear`)
-// at the next slot of O and count it; lanes own mask words.
-template <int W4>
-__device__ __forceinline__ void nr_wide_emit(const NrWideOut &O, NrWideAcc &A, const uint32_t *m,
+// at the next slot of O and count it; lanes own mask words (w4: the mask's 16-byte blocks).
+__device__ __forceinline__ void nr_wide_emit(const NrWideOut &O, NrWideAcc &A, const uint32_t *m, int w4,
                                              unsigned long long slot, int e, uint32_t clear, double cm)
 {
-    constexpr int NW = 4 * W4;
     const int lane = threadIdx.x & 31;
     const int wi = e >> 4;
     if (slot < O.cap) {
-        uint32_t *dstw = reinterpret_cast<uint32_t *>(O.mask + slot * W4);
-        if (lane < NW) __stcg(dstw + lane, (lane == wi) ? (m[lane] & ~clear) : m[lane]);
-        if (lane + 32 < NW) __stcg(dstw + lane + 32, (lane + 32 == wi) ? (m[lane + 32] & ~clear) : m[lane + 32]);
+        uint32_t *dstw = reinterpret_cast<uint32_t *>(O.mask + slot * w4);
+        for (int i = lane; i < 4 * w4; i += 32) __stcg(dstw + i, (i == wi) ? (m[i] & ~clear) : m[i]);
         if (lane == 0) {
             __stcg(O.mass + slot, cm);
             nr_fix_add_mass(A.net, cm);
@@ -413,8 +439,8 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
         if (lane == 0) base = atomicAdd(O.count, 2ull);
         base = __shfl_sync(NR_FULL, base, 0);
         const int sh = (e & 15) << 1;
-        nr_wide_emit<W4>(O, A, m, base, e, 3u << sh, __dmul_rn(mass, v.q[e]));        // down
-        nr_wide_emit<W4>(O, A, m, base + 1, e, 2u << sh, __dmul_rn(mass, v.p[e]));    // up
+        nr_wide_emit(O, A, m, g.w4, base, e, 3u << sh, __dmul_rn(mass, v.q[e]));        // down
+        nr_wide_emit(O, A, m, g.w4, base + 1, e, 2u << sh, __dmul_rn(mass, v.p[e]));    // up
         __syncwarp();
         return;
     }
@@ -428,9 +454,17 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
     unsigned long long base = 0;
     if (lane == 0 && unk > 0) base = atomicAdd(O.count, (unsigned long long)unk);
     base = __shfl_sync(NR_FULL, base, 0);
-    // children in hop order, src side first; lanes own mask words
-    uint32_t w0 = (lane < NW) ? m[lane] : 0u;
-    uint32_t w1 = (lane + 32 < NW) ? m[lane + 32] : 0u;
+    // children in hop order, src side first; lanes own mask words (in registers when the width
+    // is compiled in, else in the warp's working copy wk)
+    const int w4 = W4 ? W4 : g.w4;
+    uint32_t w0 = 0u, w1 = 0u;
+    if (W4) {
+        w0 = (lane < NW) ? m[lane] : 0u;
+        w1 = (lane + 32 < NW) ? m[lane + 32] : 0u;
+    } else {
+        for (int i = lane; i < 4 * w4; i += 32) v.wk[i] = m[i];
+        __syncwarp();
+    }
     double Pm = mass;
     int k = 0;
     for (int h = L - 1; h >= 0; --h) {
@@ -441,9 +475,13 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
         const unsigned long long slot = base + (unsigned long long)k;
         const double cm = __dmul_rn(Pm, v.q[e]);
         if (slot < O.cap) {
-            uint32_t *dstw = reinterpret_cast<uint32_t *>(O.mask + slot * W4);
-            if (lane < NW) __stcg(dstw + lane, (lane == wi) ? (w0 & ~(3u << sh)) : w0);
-            if (lane + 32 < NW) __stcg(dstw + lane + 32, (lane + 32 == wi) ? (w1 & ~(3u << sh)) : w1);
+            uint32_t *dstw = reinterpret_cast<uint32_t *>(O.mask + slot * w4);
+            if (W4) {
+                if (lane < NW) __stcg(dstw + lane, (lane == wi) ? (w0 & ~(3u << sh)) : w0);
+                if (lane + 32 < NW) __stcg(dstw + lane + 32, (lane + 32 == wi) ? (w1 & ~(3u << sh)) : w1);
+            } else {
+                for (int i = lane; i < 4 * w4; i += 32) __stcg(dstw + i, (i == wi) ? (v.wk[i] & ~(3u << sh)) : v.wk[i]);
+            }
             if (lane == 0) {
                 __stcg(O.mass + slot, cm);
                 nr_fix_add_mass(A.net, cm);
@@ -457,8 +495,14 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
             A.spilled++;
             nr_fix_add_mass(A.es, cm);
         }
-        if (lane == wi) w0 &= ~(2u << sh);                  // this hop is up in later children
-        if (lane + 32 == wi) w1 &= ~(2u << sh);
+        if (W4) {                                           // this hop is up in later children
+            if (lane == wi) w0 &= ~(2u << sh);
+            if (lane + 32 == wi) w1 &= ~(2u << sh);
+        } else {
+            __syncwarp();
+            if (lane == 0) v.wk[wi] &= ~(2u << sh);
+            __syncwarp();
+        }
         Pm = __dmul_rn(Pm, v.p[e]);
         ++k;
     }
@@ -541,9 +585,10 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const NrWideGraph g = P.g;
-    nr_stage_blob(smem, P.blob, g.blob_bytes);
+    if (!g.tables_global) nr_stage_blob(smem, P.blob, g.blob_bytes);
     __syncthreads();
-    const NrWideView v = nr_wide_view<W4>(smem, g);
+    const NrWideView v = nr_wide_view(smem, P.blob, g);
+    const int w4 = W4 ? W4 : g.w4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const unsigned long long TW = (unsigned long long)gridDim.x * (blockDim.x >> 5);
@@ -573,7 +618,7 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
         O.nb = 1;
         O.hist = nullptr;
         for (unsigned long long idx = gw; idx < n_in; idx += TW) {
-            if (lane < W4) reinterpret_cast<uint4 *>(v.m)[lane] = __ldcg(in_mask + idx * W4 + lane);
+            nr_wide_load_mask(v.m, in_mask + idx * w4, w4);
             const double mass = __ldcg(in_mass + idx);
             __syncwarp();
             nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0, P.border);
@@ -670,7 +715,8 @@ __device__ __forceinline__ bool nr_bucket_compact(const NrBucketWideParams &P, u
     const unsigned long long TW = (unsigned long long)gridDim.x * nwarp;
     for (unsigned long long r = gw; r < moved; r += TW) {
         const unsigned long long d = __ldcg(hole + r), s = __ldcg(from + r);
-        if (lane < W4) __stcg(P.mask + d * W4 + lane, __ldcg(P.mask + s * W4 + lane));
+        const int w4 = W4 ? W4 : P.g.w4;
+        for (int k = lane; k < w4; k += 32) __stcg(P.mask + d * w4 + k, __ldcg(P.mask + s * w4 + k));
         if (lane == 0) {
             __stcg(P.mass + d, __ldcg(P.mass + s));
             __stcg(P.key + d, __ldcg(P.key + s));
@@ -689,9 +735,10 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketW
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_hist[NR_WIDE_MAX_NB + 1];
     const NrWideGraph g = P.g;
-    nr_stage_blob(smem, P.blob, g.blob_bytes);
+    if (!g.tables_global) nr_stage_blob(smem, P.blob, g.blob_bytes);
     __syncthreads();
-    const NrWideView v = nr_wide_view<W4>(smem, g);
+    const NrWideView v = nr_wide_view(smem, P.blob, g);
+    const int w4 = W4 ? W4 : g.w4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const unsigned long long TW = (unsigned long long)gridDim.x * (blockDim.x >> 5);
@@ -753,7 +800,7 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketW
         }
         for (unsigned long long idx = gw; idx < n_in; idx += TW) {
             const unsigned long long s = __ldcg(P.list + idx);
-            if (lane < W4) reinterpret_cast<uint4 *>(v.m)[lane] = __ldcg(P.mask + s * W4 + lane);
+            nr_wide_load_mask(v.m, P.mask + s * w4, w4);
             const double mass = __ldcg(P.mass + s);
             __syncwarp();
             nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0, P.border);

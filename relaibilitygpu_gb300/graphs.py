@@ -234,6 +234,40 @@ def gnm(n: int, m: int, p: Optional[float] = None, p_range: Optional[Tuple[float
     return g
 
 
+def random_digraph(n: int, m: int, p: Optional[float] = None, p_range: Optional[Tuple[float, float]] = None,
+                   seed: int = 0, max_out: int = 10, hops: int = 5) -> Graph:
+    """Directed graph ('D': every arc its own edge) with m distinct arcs u -> v, u != v, and
+    out-degrees of at most max_out -- the size class of a peer-to-peer overlay such as the
+    reference's directed example (6301 nodes, 20777 arcs, out-degree <= 10, p = 0.5).  src is
+    node 0, dst the smallest node `hops` arcs away from it (else the farthest reachable)."""
+    rng = np.random.default_rng(seed)
+    out = [set() for _ in range(n)]
+    arcs = 0
+    while arcs < m:
+        u = int(rng.integers(0, n))
+        v = int(rng.integers(0, n))
+        if u == v or v in out[u] or len(out[u]) >= max_out:
+            continue
+        out[u].add(v)
+        arcs += 1
+    lst = [(u, v) for u in range(n) for v in sorted(out[u])]
+    g = from_arcs(n, lst, _probs(rng, len(lst), p, p_range), name=f"digraph{n}_{m}")
+    dist = {0: 0}
+    frontier = [0]
+    while frontier:
+        nxt = []
+        for u in frontier:
+            for v in sorted(out[u]):
+                if v not in dist:
+                    dist[v] = dist[u] + 1
+                    nxt.append(v)
+        frontier = nxt
+    at = sorted(v for v, d in dist.items() if d == hops)
+    g.src = 0
+    g.dst = at[0] if at else max(dist, key=lambda v: (dist[v], -v))
+    return g
+
+
 def rgg(n: int, target_edges: int, p: Optional[float] = None, p_range: Optional[Tuple[float, float]] = None,
         seed: int = 0, max_tries: int = 1000) -> Graph:
     """Random geometric graph in the unit square with exactly ``target_edges`` edges.

@@ -296,3 +296,20 @@ def test_k_terminal_two_terminals_is_the_two_terminal_run(ctx, engine_lib):
         assert e.value.status in (-1, -4)
     with pytest.raises(engine_lib.NrError):
         ctx.reliability_kterminal(g, [0, 60])
+
+
+@pytest.mark.parametrize("shift", [2, -1])
+def test_directed_graph_beyond_1024_nodes(ctx, oracle, shift):
+    """A directed graph of the size class of the reference's directed example (workingPad's
+    6301-node, 20,777-arc peer-to-peer overlay: out-degree <= 10, p = 0.5): more than 1024 nodes
+    and a 1299-word mask, so the runtime-width kernels with the graph tables in global memory.
+    Bit for bit against the oracle at a budget, bucketed queue and breadth-first waves."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.random_digraph(6301, 20777, p=0.5, seed=1)
+    budget, nb = (3000, 255) if shift >= 0 else (500, 1)
+    r = ctx.reliability(g, g.src, g.dst, capacity=(1 << 20) if shift >= 0 else (1 << 16), target_width=1e-3,
+                        order="maxmass" if shift >= 0 else "waves", bucket_shift=shift, n_buckets=255,
+                        max_nodes=budget)
+    o = oracle.run(g, g.src, g.dst, target_width=1e-3, bucket_shift=shift, n_buckets=nb, max_nodes=budget, threads=8)
+    assert r.engine == "grid" and r.spilled == 0 and r.stop == 3
+    check(r, o)
