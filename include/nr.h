@@ -253,7 +253,7 @@ int  nr_reliability_batch_matrix(nr_context *ctx, const nr_graph *topology, int 
  * same disjoint decomposition runs over the BFS tree that joins every terminal to terminals[0]
  * (the union of their parent paths), its UNKNOWN edges in BFS order (by depth, then node
  * index); with two terminals it is the two-terminal run exactly.  Runs on the whole-GPU
- * engines for any n <= 1024 (breadth-first waves, or the bucketed max-mass queue for
+ * engines for any n <= 16384 (breadth-first waves, or the bucketed max-mass queue for
  * NR_ORDER_MAXMASS and target widths); path branching only. */
 int  nr_reliability_kterminal(nr_context *ctx, const nr_graph *graph, const int32_t *terminals, int n_terminals,
                               uint64_t capacity, const nr_options *opt, nr_result *result);

@@ -781,7 +781,7 @@ static int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, ui
 }
 
 // ---------------------------------------------------------------------------
-// whole-GPU engine for 33..1024 nodes (nr_wide.cuh)
+// whole-GPU engine for 33..16384 nodes (nr_wide.cuh)
 // ---------------------------------------------------------------------------
 static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg, std::vector<unsigned char> *blob,
                             const int32_t *terms = nullptr, int nt = 0)
@@ -1214,7 +1214,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     return NR_OK;
 }
 
-// 33..1024 nodes: the bucketed max-mass queue for the max-mass order (and for a target width
+// 33..16384 nodes: the bucketed max-mass queue for the max-mass order (and for a target width
 // in the default order) with a bucket shift >= 0, else breadth-first waves.  The learned
 // order is n <= 32 only.
 static int run_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t capacity, const nr_options *o,

@@ -1,4 +1,4 @@
-// nr_wide.cuh -- whole-GPU engine for graphs with 33..1024 nodes.
+// nr_wide.cuh -- whole-GPU engine for graphs with 33..16384 nodes.
 //
 // One warp per subproblem.  Node sets are bitmasks of ceil(n/32) words in
 // the warp's shared memory.  Each BFS level compacts the frontier into a
