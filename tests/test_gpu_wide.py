@@ -66,11 +66,21 @@ def test_wide_overflow_brackets(ctx, oracle):
     assert r.R <= exact.R + 1e-15 and exact.R + exact.esp <= r.R + r.esp + 1e-12
 
 
-def test_wide_rejects_too_many_edges(ctx, engine_lib):
+def test_wide_limits(ctx, engine_lib, oracle):
+    """Masks above 16 blocks (K47: 1081 edges, 68 words) run in the runtime-width instantiation,
+    bit for bit against the oracle; graphs above 16384 nodes are refused."""
     from relaibilitygpu_gb300 import graphs
-    g = graphs.complete(47, p=0.5)     # 1081 edges: masks above 64 words
+    g = graphs.complete(47, p=0.5)
+    for shift, nb in ((2, 255), (-1, 1)):
+        r = ctx.reliability(g, 0, 46, capacity=1 << 22, target_width=1e-2, bucket_shift=shift, n_buckets=255,
+                            order="maxmass" if shift >= 0 else "waves", max_nodes=20000)
+        o = oracle.run(g, 0, 46, target_width=1e-2, bucket_shift=shift, n_buckets=nb, max_nodes=20000, threads=8)
+        assert r.engine == "grid" and r.spilled == 0
+        check(r, o)
+    n = 16385
+    big = graphs.from_edges(n, [(i, i + 1) for i in range(n - 1)], [0.99] * (n - 1))
     with pytest.raises(engine_lib.NrError) as e:
-        ctx.reliability(g, 0, 46)
+        ctx.reliability(big, 0, n - 1)
     assert e.value.status == -4
 
 
