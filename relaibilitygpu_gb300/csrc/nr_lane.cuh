@@ -42,6 +42,7 @@ __host__ __device__ inline size_t nr_lane_shm_bytes(int n_buckets, int pages)
     size_t b = 32 * sizeof(NrLaneAcc);                       // per-lane sums and counters
     b += (size_t)NR_LANE_ROW_WORDS * 32 * 4;                 // each lane's rows, [word][lane]
     b += (size_t)NR_LANE_MAX_N * 32 * 4;                     // BFS frontiers, then path hops, [level][lane]
+    b += (size_t)NR_LANE_MAX_N * 32 * 4;                     // branch-order sort keys, [level][lane]
     b += (size_t)n_buckets * 2;
     b = (b + 3) & ~size_t(3);
     b += (size_t)(n_buckets / 32) * 4;
@@ -164,7 +165,8 @@ __device__ __forceinline__ int nr_lane_path(const uint32_t *my_rows, uint32_t *m
 // first (reversed), or by p (ascending / descending, stable in path order -- the oracle's
 // insertion sort of the src -> dst path).  Known hops move too but make no child, so only
 // the UNKNOWN hops' relative order matters.
-__device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, int L, int border, const double *pt)
+__device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, float *my_key, int L, int border,
+                                                     const double *pt)
 {
     if (border == NR_BORDER_DST) {
         for (int i = 0, j = L - 1; i < j; ++i, --j) {
@@ -174,18 +176,27 @@ __device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, int L, in
         }
         return;
     }
+    // keys: p rounded to FP32 in the lane's column (order-preserving; equal keys compare the FP64 p)
     const bool desc = (border == NR_BORDER_P_DESC);
+    for (int i = 0; i < L; ++i) my_key[32 * i] = __double2float_rn(pt[my_hop[32 * i] & 0xffffu]);
     for (int i = 1; i < L; ++i) {
         const uint32_t hp = my_hop[32 * i];
-        const double pe = pt[hp & 0xffffu];
+        const float ke = my_key[32 * i];
         int j = i - 1;
         while (j >= 0) {
-            const double pj = pt[my_hop[32 * j] & 0xffffu];
-            if (!(desc ? pj < pe : pj > pe)) break;
+            const float kj = my_key[32 * j];
+            bool after = desc ? kj < ke : kj > ke;          // j moves past i: strictly out of order
+            if (kj == ke) {
+                const double pj = pt[my_hop[32 * j] & 0xffffu], pe = pt[hp & 0xffffu];
+                after = desc ? pj < pe : pj > pe;
+            }
+            if (!after) break;
             my_hop[32 * (j + 1)] = my_hop[32 * j];
+            my_key[32 * (j + 1)] = kj;
             --j;
         }
         my_hop[32 * (j + 1)] = hp;
+        my_key[32 * (j + 1)] = ke;
     }
 }
 
@@ -235,6 +246,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
     NrWarpShm sh;
     NrLaneAcc *acc_base;
     uint32_t *my_rows, *my_hop;
+    float *my_key;
     {
         unsigned char *b = smem + (size_t)warp * nr_lane_shm_bytes(NB, NP);
         acc_base = reinterpret_cast<NrLaneAcc *>(b);
@@ -242,6 +254,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
         my_rows = reinterpret_cast<uint32_t *>(b) + lane;          // word k at my_rows[32 k]
         b += (size_t)RW * 32 * 4;
         my_hop = reinterpret_cast<uint32_t *>(b) + lane;           // level l at my_hop[32 l]
+        b += (size_t)NR_LANE_MAX_N * 32 * 4;
+        my_key = reinterpret_cast<float *>(b) + lane;              // hop l's sort key at my_key[32 l]
         b += (size_t)NR_LANE_MAX_N * 32 * 4;
         size_t o = 0;
         sh.masks = nullptr;
@@ -406,7 +420,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                 bool live;
                 int nch, bad;
                 const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, g.e, src, dst, active, live, nch, bad);
-                if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, L, P.border, pt);
+                if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, my_key, L, P.border, pt);
                 if (active && !live && !bad) acc.dead++;
 
                 {

@@ -33,7 +33,7 @@ struct NrLaneSlot {
 __host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots)
 {
     size_t b = (size_t)slots * 32 * sizeof(NrLaneAcc);       // per slot, per lane sums
-    b += (size_t)(NR_LANE_ROW_WORDS + NR_LANE_MAX_N) * 32 * 4;  // rows and hops, [word][lane]
+    b += (size_t)(NR_LANE_ROW_WORDS + 2 * NR_LANE_MAX_N) * 32 * 4;  // rows, hops, sort keys, [word][lane]
     b += (size_t)slots * sizeof(NrLaneSlot);
     b += (size_t)slots * 8 * 4;                              // the step's allocation, 8 ints a slot
     b += (size_t)pages * 2;                                  // pnext
@@ -57,8 +57,9 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     NrLaneAcc *accs = reinterpret_cast<NrLaneAcc *>(wbase);                      // [slot * 32 + lane]
     uint32_t *my_rows = reinterpret_cast<uint32_t *>(wbase + NS * 32 * sizeof(NrLaneAcc)) + lane;
     uint32_t *my_hop = my_rows + RW * 32;
+    float *my_key = reinterpret_cast<float *>(my_hop + NR_LANE_MAX_N * 32);
     NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(wbase + NS * 32 * sizeof(NrLaneAcc) +
-                                                       (size_t)(RW + NR_LANE_MAX_N) * 32 * 4);
+                                                       (size_t)(RW + 2 * NR_LANE_MAX_N) * 32 * 4);
     int *alloc = reinterpret_cast<int *>(slots + NS);
     short *pnext = reinterpret_cast<short *>(alloc + 8 * NS);
     unsigned char *pcnt = reinterpret_cast<unsigned char *>(pnext + NP);
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         bool live;
         int nch, bad;
         const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
-        if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, L, P.border, pt);
+        if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, my_key, L, P.border, pt);
         if (active && !live && !bad) acc.dead++;
         {
             const unsigned bm = __ballot_sync(NR_FULL, bad != 0);
