@@ -36,13 +36,19 @@
 #define NR_LANE_STEP_CAP (1ll << 26)   // steps (pages) per instance: 2^31 subproblems
 #define NR_LANE_STATUS_CHECK NR_WARP_STATUS_CHECK
 
-// shared memory of one warp
-__host__ __device__ inline size_t nr_lane_shm_bytes(int n_buckets, int pages)
+// the branch orders that sort a path's hops by p keep FP32 keys in a shared-memory column
+__host__ __device__ inline bool nr_lane_sort_keys(int border)
+{
+    return border == NR_BORDER_P_ASC || border == NR_BORDER_P_DESC;
+}
+
+// shared memory of one warp (keys: nr_lane_sort_keys of the run's branch order)
+__host__ __device__ inline size_t nr_lane_shm_bytes(int n_buckets, int pages, bool keys)
 {
     size_t b = 32 * sizeof(NrLaneAcc);                       // per-lane sums and counters
     b += (size_t)NR_LANE_ROW_WORDS * 32 * 4;                 // each lane's rows, [word][lane]
     b += (size_t)NR_LANE_MAX_N * 32 * 4;                     // BFS frontiers, then path hops, [level][lane]
-    b += (size_t)NR_LANE_MAX_N * 32 * 4;                     // branch-order sort keys, [level][lane]
+    if (keys) b += (size_t)NR_LANE_MAX_N * 32 * 4;           // branch-order sort keys, [level][lane]
     b += (size_t)n_buckets * 2;
     b = (b + 3) & ~size_t(3);
     b += (size_t)(n_buckets / 32) * 4;
@@ -248,7 +254,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
     uint32_t *my_rows, *my_hop;
     float *my_key;
     {
-        unsigned char *b = smem + (size_t)warp * nr_lane_shm_bytes(NB, NP);
+        const bool keys = nr_lane_sort_keys(P.border);
+        unsigned char *b = smem + (size_t)warp * nr_lane_shm_bytes(NB, NP, keys);
         acc_base = reinterpret_cast<NrLaneAcc *>(b);
         b += 32 * sizeof(NrLaneAcc);
         my_rows = reinterpret_cast<uint32_t *>(b) + lane;          // word k at my_rows[32 k]
@@ -256,7 +263,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
         my_hop = reinterpret_cast<uint32_t *>(b) + lane;           // level l at my_hop[32 l]
         b += (size_t)NR_LANE_MAX_N * 32 * 4;
         my_key = reinterpret_cast<float *>(b) + lane;              // hop l's sort key at my_key[32 l]
-        b += (size_t)NR_LANE_MAX_N * 32 * 4;
+        if (keys) b += (size_t)NR_LANE_MAX_N * 32 * 4;
         size_t o = 0;
         sh.masks = nullptr;
         sh.heads = reinterpret_cast<short *>(b + o); o += (size_t)NB * 2; o = (o + 3) & ~size_t(3);

@@ -19,21 +19,26 @@
 // warp-uniform state of one instance slot, in shared memory (written by lane 0)
 struct NrLaneSlot {
     long long t0;
-    long long blob_off, struct_off;   // the instance's tables in P.blob
     int ii;                 // instance (index into the class); -1 empty, -2 no instance left
     int n, src, dst, ge;
-    int off_p, off_eid, off_rows16, off_start, off_list;
     int head;               // the chain the current wave's children go to (the next wave)
     int cur;                // next page of the current wave; -1: the wave is done
     int waves, used;        // waves started; pages held (current wave + next wave)
     unsigned wave_items, max_wave;
-    int pad[2];
+    int pad[3];             // 64 bytes
 };
 
-__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots)
+// a slot's copy of its instance's tables: p (simple graphs on <= 16 nodes: <= 120 edges) and
+// the edge-id table (n <= 8: 8 x 8 ids, else 16 x 16)
+#define NR_LANE2_MAX_E 128
+#define NR_LANE2_TAB_BYTES (NR_LANE2_MAX_E * 8 + NR_LANE_MAX_N * NR_LANE_MAX_N * 2)
+
+__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots, bool keys)
 {
     size_t b = (size_t)slots * 32 * sizeof(NrLaneAcc);       // per slot, per lane sums
-    b += (size_t)(NR_LANE_ROW_WORDS + 2 * NR_LANE_MAX_N) * 32 * 4;  // rows, hops, sort keys, [word][lane]
+    b += (size_t)(NR_LANE_ROW_WORDS + (keys ? 2 : 1) * NR_LANE_MAX_N) * 32 * 4;  // rows, hops, sort keys, [word][lane]
+    b += (size_t)slots * 32 * 4;                             // per slot, per lane: queued-mass lower bound
+    b += (size_t)slots * NR_LANE2_TAB_BYTES;                 // per slot: p and edge ids
     b += (size_t)slots * sizeof(NrLaneSlot);
     b += (size_t)slots * 8 * 4;                              // the step's allocation, 8 ints a slot
     b += (size_t)pages * 2;                                  // pnext
@@ -53,13 +58,16 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     const int NP = P.pages;
     const int budget = max(1, NP / NS);       // pages one slot may hold
 
-    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP, NS);
+    const bool keys = nr_lane_sort_keys(P.border);
+    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP, NS, keys);
     NrLaneAcc *accs = reinterpret_cast<NrLaneAcc *>(wbase);                      // [slot * 32 + lane]
     uint32_t *my_rows = reinterpret_cast<uint32_t *>(wbase + NS * 32 * sizeof(NrLaneAcc)) + lane;
     uint32_t *my_hop = my_rows + RW * 32;
     float *my_key = reinterpret_cast<float *>(my_hop + NR_LANE_MAX_N * 32);
-    NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(wbase + NS * 32 * sizeof(NrLaneAcc) +
-                                                       (size_t)(RW + 2 * NR_LANE_MAX_N) * 32 * 4);
+    float *qlb = reinterpret_cast<float *>(wbase + NS * 32 * sizeof(NrLaneAcc) +
+                                           (size_t)(RW + (keys ? 2 : 1) * NR_LANE_MAX_N) * 32 * 4);  // [slot * 32 + lane]
+    unsigned char *tabs = reinterpret_cast<unsigned char *>(qlb + NS * 32);                       // [slot]
+    NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(tabs + NS * NR_LANE2_TAB_BYTES);
     int *alloc = reinterpret_cast<int *>(slots + NS);
     short *pnext = reinterpret_cast<short *>(alloc + 8 * NS);
     unsigned char *pcnt = reinterpret_cast<unsigned char *>(pnext + NP);
@@ -71,6 +79,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     uint4 *sl_rows = reinterpret_cast<uint4 *>(P.slab_rows) + gw * (size_t)NP * NR_PAGE * (RW / 4);
     const bool use_eps = P.eps > 0.0;
     const long long step_cap = P.step_cap > 0 ? P.step_cap : NR_LANE_STEP_CAP;
+    const float target_hi = __double2float_ru(P.target);      // >= the target
 
     for (int p = lane; p < NP; p += 32) { freel[p] = (short)(NP - 1 - p); pnext[p] = -1; pcnt[p] = 0; }
     if (lane < NS) { slots[lane].ii = -1; slots[lane].cur = -1; slots[lane].head = -1; }
@@ -128,10 +137,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 int rpg = 0;
                 if (lane == 0) {
                     S.t0 = nr_globaltimer();
-                    S.ii = ii; S.blob_off = g.blob_off; S.struct_off = g.struct_off;
+                    S.ii = ii;
                     S.n = g.n; S.src = g.src; S.dst = g.dst; S.ge = g.e;
-                    S.off_p = g.off_p; S.off_eid = g.off_eid; S.off_rows16 = g.off_rows16;
-                    S.off_start = g.off_start; S.off_list = g.off_list;
                     S.waves = 0; S.wave_items = 0; S.max_wave = 0;
                     rpg = freel[--top];                    // a slot holds <= NP/2 pages: one is free
                     pcnt[rpg] = 1;
@@ -142,39 +149,67 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 rpg = __shfl_sync(NR_FULL, rpg, 0);
                 nr_lane_root<W4>(g, gb, gs, sl_mask, sl_rows, sl_mass, rpg);
                 nr_acc_zero(accs[s * 32 + lane]);
+                {                                  // the slot's tables, for the steps' lookups
+                    double *tp = reinterpret_cast<double *>(tabs + s * NR_LANE2_TAB_BYTES);
+                    uint16_t *te = reinterpret_cast<uint16_t *>(tp + NR_LANE2_MAX_E);
+                    const double *gp = reinterpret_cast<const double *>(gb + g.off_p);
+                    const uint16_t *gi = reinterpret_cast<const uint16_t *>(gs + g.off_eid);
+                    const int es = g.n <= 8 ? 8 : 16;
+                    for (int e = lane; e < g.e; e += 32) tp[e] = gp[e];
+                    for (int k = lane; k < g.n * es; k += 32) te[k] = gi[k];
+                }
+                qlb[s * 32 + lane] = lane == 0 ? 1.0f : 0.0f;   // the root's mass is queued
                 __syncwarp();
             }
             if (S.ii < 0 || S.cur >= 0) continue;
             // slot s's wave is done (or its first not begun): the stop tests, in the one-slot
-            // kernel's order (target width, node budget, empty queue)
+            // kernel's order (target width, node budget, empty queue).  The queued mass is the
+            // next wave's chain.  Its exact sum is taken only where a test can end the run: a
+            // lower bound of it (FP32 sums rounded down, kept as the children are written) above
+            // the target already rules the width test out, as the exact test would.
             if (lane == 0 && S.wave_items > S.max_wave) S.max_wave = S.wave_items;
+            NrLaneAcc &A = accs[s * 32 + lane];
             NrFix qs = nr_fix_zero();
             long long qn = 0;
-            int pg = S.head;
-            for (int k = 0; pg >= 0 && k < NP; pg = pnext[pg], ++k)   // a chain holds <= NP pages
-                if (lane < (int)pcnt[pg]) {
-                    nr_fix_add_mass(qs, sl_mass[(size_t)pg * NR_PAGE + lane]);
-                    qn++;
-                }
-            if (pg >= 0) {                           // longer than the pool: the chain is corrupt
-                finish(s, 0, 6, nr_fix_zero(), 0);
-                continue;
-            }
-            NrLaneAcc &A = accs[s * 32 + lane];
+            bool summed = false;
+            auto chain_sum = [&]() -> bool {       // false: longer than the pool, the chain is corrupt
+                int pg = S.head;
+                for (int k = 0; pg >= 0 && k < NP; pg = pnext[pg], ++k)
+                    if (lane < (int)pcnt[pg]) {
+                        nr_fix_add_mass(qs, sl_mass[(size_t)pg * NR_PAGE + lane]);
+                        qn++;
+                    }
+                summed = true;
+                return pg < 0;
+            };
             int st = -1;
             if (P.target > 0.0) {
-                NrFix w = qs;
-                nr_fix_add(w, A.et);
-                nr_fix_add(w, A.es);
-                w = nr_fix_warp_sum(w);
-                if (nr_fix_le(w, P.target_fix)) st = 1;
+                float lb = qlb[s * 32 + lane];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) lb = __fadd_rd(lb, __shfl_xor_sync(NR_FULL, lb, off));
+                if (!(lb > target_hi)) {
+                    if (!chain_sum()) {
+                        finish(s, 0, 6, nr_fix_zero(), 0);
+                        continue;
+                    }
+                    NrFix w = qs;
+                    nr_fix_add(w, A.et);
+                    nr_fix_add(w, A.es);
+                    w = nr_fix_warp_sum(w);
+                    if (nr_fix_le(w, P.target_fix)) st = 1;
+                }
             }
             if (st < 0 && P.max_nodes && nr_warp_sum_u64(A.nodes) >= P.max_nodes) st = 3;
             if (st < 0 && S.head < 0) st = 0;
             __syncwarp();
             if (st >= 0) {
+                if (!summed && !chain_sum()) {
+                    finish(s, 0, 6, nr_fix_zero(), 0);
+                    continue;
+                }
                 finish(s, st, 0, qs, qn);
             } else {
+                qlb[s * 32 + lane] = 0.0f;          // the next wave's children start a new chain
                 if (lane == 0) { S.cur = S.head; S.head = -1; S.waves++; S.wave_items = 0; }
                 __syncwarp();
             }
@@ -187,17 +222,20 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
 #pragma unroll
         for (int t = 0; t < NS; ++t) { tpg[t] = -1; toff[t] = 0; tcnt[t] = 0; all_done = all_done && slots[t].ii == -2; }
         if (all_done) break;
+        const int t0 = (int)(steps % NS);
 #pragma unroll
-        for (int k2 = 0; k2 < NS; ++k2) {
-            const int t = (int)((steps + k2) % NS);
-            const int cp = slots[t].ii >= 0 ? slots[t].cur : -1;
-            if (cp < 0) continue;
-            const int c = pcnt[cp];
-            empty_page |= (c == 0);                 // a chain page holds >= 1 record: checked, not assumed
-            if (used_lanes + c > NR_PAGE) continue;
-            tpg[t] = cp; toff[t] = used_lanes; tcnt[t] = c;
-            used_lanes += c;
-        }
+        for (int pass = 0; pass < 2; ++pass)        // slots t0 .. NS-1, then 0 .. t0-1
+#pragma unroll
+            for (int t = 0; t < NS; ++t) {          // (t is known at compile time: no local arrays)
+                if ((t >= t0) != (pass == 0)) continue;
+                const int cp = slots[t].ii >= 0 ? slots[t].cur : -1;
+                if (cp < 0) continue;
+                const int c = pcnt[cp];
+                empty_page |= (c == 0);             // a chain page holds >= 1 record: checked, not assumed
+                if (used_lanes + c > NR_PAGE) continue;
+                tpg[t] = cp; toff[t] = used_lanes; tcnt[t] = c;
+                used_lanes += c;
+            }
         // Every pass counts toward the step bound, an idle one too, so the loop ends whatever
         // state the slots are in: past the bound (or on an empty chain page) the live slots end
         // with a check status, and the instances still to come end the same way at their first
@@ -255,9 +293,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
 
         // the lane's instance
         const NrLaneSlot &S = slots[sl];
-        const unsigned char *gs = P.blob + S.struct_off;
-        const double *pt = reinterpret_cast<const double *>(P.blob + S.blob_off + S.off_p);
-        const uint16_t *eid = reinterpret_cast<const uint16_t *>(gs + S.off_eid);
+        const double *pt = reinterpret_cast<const double *>(tabs + sl * NR_LANE2_TAB_BYTES);
+        const uint16_t *eid = reinterpret_cast<const uint16_t *>(pt + NR_LANE2_MAX_E);
         const int n = S.n, src = S.src, dst = S.dst, ge = S.ge;
         NrLaneAcc &acc = accs[sl * 32 + lane];
 
@@ -304,6 +341,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         }
         pre -= nch;
         if (lane == 0) {
+#pragma unroll
             for (int t = 0; t < NS; ++t) {
                 NrLaneSlot &T = slots[t];
                 const int want = tend[t] - tbeg[t];
@@ -339,6 +377,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         for (int t = 0; t < NS; ++t)
             if (t == sl) q -= tbeg[t];
         double Pm = mass;
+        float qadd = 0.0f;                          // lower bound of the mass this lane queues
         for (int h = 0; h < L; ++h) {
             const uint32_t hp = my_hop[32 * h];
             const int e = (int)(hp & 0xffffu);
@@ -359,6 +398,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             ++q;
             if (sc >= 0) {
                 nr_lane_write_child<W4>(sl_mask, sl_rows, sl_mass, sc, wc, rw, my_rows, e, wv, cu, cv, cm);
+                qadd = __fadd_rd(qadd, __double2float_rd(cm));
             } else {                                  // the slot's pages are full: mass to ESP
                 acc.spilled++;
                 nr_fix_add_mass(acc.es, cm);
@@ -371,6 +411,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             acc.leaves++;
             nr_fix_add_mass(acc.R, Pm);
         }
+        if (qadd > 0.0f) qlb[sl * 32 + lane] = __fadd_rd(qlb[sl * 32 + lane], qadd);
         __syncwarp();
     }
 }
