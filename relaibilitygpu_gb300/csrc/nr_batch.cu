@@ -349,11 +349,10 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     }
     // pages per warp: as asked, but no more than the block's shared memory can index
     WarpRunCfg cfgp = cfg;
-    const bool keys = nr_lane_sort_keys(cfg.border);
     while (cfgp.pages > 4 &&
            std::max(std::max(nr_warp_shm_bytes(4, NR_MAX_W4, cfgp.n_buckets, cfgp.pages, true),
-                             nr_lane_shm_bytes(cfgp.n_buckets, cfgp.pages, keys)),
-                    nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots, keys)) * warps_pb > (size_t)c->smem_optin)
+                             nr_lane_shm_bytes(cfgp.n_buckets, cfgp.pages)),
+                    nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots)) * warps_pb > (size_t)c->smem_optin)
         cfgp.pages /= 2;
     const bool learn = cfg.learned || cfg.dump || cfg.border == NR_BORDER_LEARNED;
     int grids[NCLS] = {0};
@@ -368,8 +367,8 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         const void *kfn = lanek ? (two ? nr_lane2_kernel_ptr(W4, cfg.lane_slots) : nr_lane_kernel_ptr(W4))
                                 : warp_kernel(G, W4, learn, cfg.fork != 0);
         if (!kfn) return NR_ERR_UNSUPPORTED;
-        const size_t smem = (two ? nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots, keys)
-                                 : lanek ? nr_lane_shm_bytes(cfg.n_buckets, cfgp.pages, keys)
+        const size_t smem = (two ? nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots)
+                                 : lanek ? nr_lane_shm_bytes(cfg.n_buckets, cfgp.pages)
                                          : nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn)) * warps_pb;
         auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
         int bps;

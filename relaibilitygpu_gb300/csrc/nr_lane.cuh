@@ -36,19 +36,19 @@
 #define NR_LANE_STEP_CAP (1ll << 26)   // steps (pages) per instance: 2^31 subproblems
 #define NR_LANE_STATUS_CHECK NR_WARP_STATUS_CHECK
 
-// the branch orders that sort a path's hops by p keep FP32 keys in a shared-memory column
-__host__ __device__ inline bool nr_lane_sort_keys(int border)
-{
-    return border == NR_BORDER_P_ASC || border == NR_BORDER_P_DESC;
-}
+// A path hop in a lane kernel's hop column: edge id (bits 0-6: a lane-kernel graph has <= 128
+// edges), its nodes u (bits 7-10) and x (bits 11-14); a p-ordered branch order puts the edge's
+// sort key in bits 16-31.
+#define NR_HOP_E(h) ((int)((h) & 0x7fu))
+#define NR_HOP_U(h) ((int)(((h) >> 7) & 0xfu))
+#define NR_HOP_X(h) ((int)(((h) >> 11) & 0xfu))
 
-// shared memory of one warp (keys: nr_lane_sort_keys of the run's branch order)
-__host__ __device__ inline size_t nr_lane_shm_bytes(int n_buckets, int pages, bool keys)
+// shared memory of one warp
+__host__ __device__ inline size_t nr_lane_shm_bytes(int n_buckets, int pages)
 {
     size_t b = 32 * sizeof(NrLaneAcc);                       // per-lane sums and counters
     b += (size_t)NR_LANE_ROW_WORDS * 32 * 4;                 // each lane's rows, [word][lane]
     b += (size_t)NR_LANE_MAX_N * 32 * 4;                     // BFS frontiers, then path hops, [level][lane]
-    if (keys) b += (size_t)NR_LANE_MAX_N * 32 * 4;           // branch-order sort keys, [level][lane]
     b += (size_t)n_buckets * 2;
     b = (b + 3) & ~size_t(3);
     b += (size_t)(n_buckets / 32) * 4;
@@ -159,20 +159,27 @@ __device__ __forceinline__ int nr_lane_path(const uint32_t *my_rows, uint32_t *m
         const int u = __ffs(nr_lane_row(my_rows, x) & my_hop[32 * l]) - 1;
         if (u < 0 || u >= n) { bad = 3; return 0; }
         const uint32_t e = eid[u * es + x];
-        if ((int)e >= ge) { bad = 4; return 0; }
-        my_hop[32 * l] = e | ((uint32_t)u << 16) | ((uint32_t)x << 24);
+        if ((int)e >= ge || e > 0x7fu) { bad = 4; return 0; }
+        my_hop[32 * l] = e | ((uint32_t)u << 7) | ((uint32_t)x << 11);
         nch += ((nr_pick(wc, (int)e >> 4) >> ((e & 15) << 1)) & 3u) == 3u;
         x = u;
     }
     return L;
 }
 
+// A 16-bit sort key non-decreasing in p: the top bits of p's bit pattern (positive doubles
+// order as their bit patterns do), saturated; p <= 0 gives 0.  Equal keys compare p itself.
+__device__ __forceinline__ uint32_t nr_p_key16(double p)
+{
+    const long long b = __double_as_longlong(p);
+    return b <= 0 ? 0u : (uint32_t)min((unsigned long long)b >> 38, 0xffffull);
+}
+
 // Branch order of one lane's path hops my_hop[32 l], l = 0..L-1 src side first: dst side
 // first (reversed), or by p (ascending / descending, stable in path order -- the oracle's
 // insertion sort of the src -> dst path).  Known hops move too but make no child, so only
-// the UNKNOWN hops' relative order matters.
-__device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, float *my_key, int L, int border,
-                                                     const double *pt)
+// the UNKNOWN hops' relative order matters.  The sort keys ride in the hop words' top bits.
+__device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, int L, int border, const double *pt)
 {
     if (border == NR_BORDER_DST) {
         for (int i = 0, j = L - 1; i < j; ++i, --j) {
@@ -182,27 +189,28 @@ __device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, float *my
         }
         return;
     }
-    // keys: p rounded to FP32 in the lane's column (order-preserving; equal keys compare the FP64 p)
     const bool desc = (border == NR_BORDER_P_DESC);
-    for (int i = 0; i < L; ++i) my_key[32 * i] = __double2float_rn(pt[my_hop[32 * i] & 0xffffu]);
+    for (int i = 0; i < L; ++i) {
+        const uint32_t h = my_hop[32 * i];
+        my_hop[32 * i] = (h & 0xffffu) | (nr_p_key16(pt[NR_HOP_E(h)]) << 16);
+    }
     for (int i = 1; i < L; ++i) {
         const uint32_t hp = my_hop[32 * i];
-        const float ke = my_key[32 * i];
+        const uint32_t ke = hp >> 16;
         int j = i - 1;
         while (j >= 0) {
-            const float kj = my_key[32 * j];
+            const uint32_t hj = my_hop[32 * j];
+            const uint32_t kj = hj >> 16;
             bool after = desc ? kj < ke : kj > ke;          // j moves past i: strictly out of order
             if (kj == ke) {
-                const double pj = pt[my_hop[32 * j] & 0xffffu], pe = pt[hp & 0xffffu];
+                const double pj = pt[NR_HOP_E(hj)], pe = pt[NR_HOP_E(hp)];
                 after = desc ? pj < pe : pj > pe;
             }
             if (!after) break;
-            my_hop[32 * (j + 1)] = my_hop[32 * j];
-            my_key[32 * (j + 1)] = kj;
+            my_hop[32 * (j + 1)] = hj;
             --j;
         }
         my_hop[32 * (j + 1)] = hp;
-        my_key[32 * (j + 1)] = ke;
     }
 }
 
@@ -252,18 +260,14 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
     NrWarpShm sh;
     NrLaneAcc *acc_base;
     uint32_t *my_rows, *my_hop;
-    float *my_key;
     {
-        const bool keys = nr_lane_sort_keys(P.border);
-        unsigned char *b = smem + (size_t)warp * nr_lane_shm_bytes(NB, NP, keys);
+        unsigned char *b = smem + (size_t)warp * nr_lane_shm_bytes(NB, NP);
         acc_base = reinterpret_cast<NrLaneAcc *>(b);
         b += 32 * sizeof(NrLaneAcc);
         my_rows = reinterpret_cast<uint32_t *>(b) + lane;          // word k at my_rows[32 k]
         b += (size_t)RW * 32 * 4;
         my_hop = reinterpret_cast<uint32_t *>(b) + lane;           // level l at my_hop[32 l]
         b += (size_t)NR_LANE_MAX_N * 32 * 4;
-        my_key = reinterpret_cast<float *>(b) + lane;              // hop l's sort key at my_key[32 l]
-        if (keys) b += (size_t)NR_LANE_MAX_N * 32 * 4;
         size_t o = 0;
         sh.masks = nullptr;
         sh.heads = reinterpret_cast<short *>(b + o); o += (size_t)NB * 2; o = (o + 3) & ~size_t(3);
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                 bool live;
                 int nch, bad;
                 const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, g.e, src, dst, active, live, nch, bad);
-                if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, my_key, L, P.border, pt);
+                if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, L, P.border, pt);
                 if (active && !live && !bad) acc.dead++;
 
                 {
@@ -483,11 +487,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                     int q = pre;                            // this lane's next child index
                     for (int h = 0; h < L; ++h) {
                         const uint32_t hp = my_hop[32 * h];
-                        const int e = (int)(hp & 0xffffu);
+                        const int e = NR_HOP_E(hp);
                         const int ew = e >> 4;
                         const uint32_t wv = nr_pick(wc, ew);
                         if (((wv >> ((e & 15) << 1)) & 3u) != 3u) continue;
-                        const int cu = (int)((hp >> 16) & 0xffu), cv = (int)(hp >> 24);
+                        const int cu = NR_HOP_U(hp), cv = NR_HOP_X(hp);
                         const double pe = pt[e];
                         const double cm = __dmul_rn(Pm, __dsub_rn(1.0, pe));
                         Pm = __dmul_rn(Pm, pe);
@@ -521,9 +525,9 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                     uint32_t wv = 0u;
                     if (h < L) {
                         const uint32_t hp = my_hop[32 * h];
-                        e = (int)(hp & 0xffffu);
-                        cu = (int)((hp >> 16) & 0xffu);
-                        cv = (int)(hp >> 24);
+                        e = NR_HOP_E(hp);
+                        cu = NR_HOP_U(hp);
+                        cv = NR_HOP_X(hp);
                         wv = nr_pick(wc, e >> 4);
                         if (((wv >> ((e & 15) << 1)) & 3u) == 3u) {
                             const double pe = pt[e];

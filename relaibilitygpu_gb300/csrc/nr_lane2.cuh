@@ -33,10 +33,10 @@ struct NrLaneSlot {
 #define NR_LANE2_MAX_E 128
 #define NR_LANE2_TAB_BYTES (NR_LANE2_MAX_E * 8 + NR_LANE_MAX_N * NR_LANE_MAX_N * 2)
 
-__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots, bool keys)
+__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots)
 {
     size_t b = (size_t)slots * 32 * sizeof(NrLaneAcc);       // per slot, per lane sums
-    b += (size_t)(NR_LANE_ROW_WORDS + (keys ? 2 : 1) * NR_LANE_MAX_N) * 32 * 4;  // rows, hops, sort keys, [word][lane]
+    b += (size_t)(NR_LANE_ROW_WORDS + NR_LANE_MAX_N) * 32 * 4;  // rows, hops, [word][lane]
     b += (size_t)slots * 32 * 4;                             // per slot, per lane: queued-mass lower bound
     b += (size_t)slots * NR_LANE2_TAB_BYTES;                 // per slot: p and edge ids
     b += (size_t)slots * sizeof(NrLaneSlot);
@@ -58,14 +58,12 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     const int NP = P.pages;
     const int budget = max(1, NP / NS);       // pages one slot may hold
 
-    const bool keys = nr_lane_sort_keys(P.border);
-    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP, NS, keys);
+    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP, NS);
     NrLaneAcc *accs = reinterpret_cast<NrLaneAcc *>(wbase);                      // [slot * 32 + lane]
     uint32_t *my_rows = reinterpret_cast<uint32_t *>(wbase + NS * 32 * sizeof(NrLaneAcc)) + lane;
     uint32_t *my_hop = my_rows + RW * 32;
-    float *my_key = reinterpret_cast<float *>(my_hop + NR_LANE_MAX_N * 32);
     float *qlb = reinterpret_cast<float *>(wbase + NS * 32 * sizeof(NrLaneAcc) +
-                                           (size_t)(RW + (keys ? 2 : 1) * NR_LANE_MAX_N) * 32 * 4);  // [slot * 32 + lane]
+                                           (size_t)(RW + NR_LANE_MAX_N) * 32 * 4);  // [slot * 32 + lane]
     unsigned char *tabs = reinterpret_cast<unsigned char *>(qlb + NS * 32);                       // [slot]
     NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(tabs + NS * NR_LANE2_TAB_BYTES);
     int *alloc = reinterpret_cast<int *>(slots + NS);
@@ -310,7 +308,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         bool live;
         int nch, bad;
         const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
-        if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, my_key, L, P.border, pt);
+        if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, L, P.border, pt);
         if (active && !live && !bad) acc.dead++;
         {
             const unsigned bm = __ballot_sync(NR_FULL, bad != 0);
@@ -380,11 +378,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         float qadd = 0.0f;                          // lower bound of the mass this lane queues
         for (int h = 0; h < L; ++h) {
             const uint32_t hp = my_hop[32 * h];
-            const int e = (int)(hp & 0xffffu);
+            const int e = NR_HOP_E(hp);
             const int ew = e >> 4;
             const uint32_t wv = nr_pick(wc, ew);
             if (((wv >> ((e & 15) << 1)) & 3u) != 3u) continue;
-            const int cu = (int)((hp >> 16) & 0xffu), cv = (int)(hp >> 24);
+            const int cu = NR_HOP_U(hp), cv = NR_HOP_X(hp);
             const double pe = pt[e];
             const double cm = __dmul_rn(Pm, __dsub_rn(1.0, pe));
             Pm = __dmul_rn(Pm, pe);
