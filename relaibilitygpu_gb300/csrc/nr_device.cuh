@@ -119,6 +119,23 @@ __device__ __forceinline__ NrFix nr_fix_warp_sum(NrFix a)
     return a;
 }
 
+// exact warp total of a sum that is mostly zero: one vote when every lane holds zero
+__device__ __forceinline__ NrFix nr_fix_warp_sum_sparse(const NrFix &a)
+{
+    if (!__any_sync(NR_FULL, (a.w0 | a.w1 | a.w2) != 0ull)) return nr_fix_zero();
+    return nr_fix_warp_sum(a);
+}
+
+// warp total of a 64-bit count (modulo 2^64) by three integer reductions of 21/21/22-bit limbs
+// (each limb's total stays below 2^27)
+__device__ __forceinline__ unsigned long long nr_warp_sum_u64r(unsigned long long x)
+{
+    const unsigned a = __reduce_add_sync(NR_FULL, (unsigned)(x & 0x1fffffull));
+    const unsigned b = __reduce_add_sync(NR_FULL, (unsigned)((x >> 21) & 0x1fffffull));
+    const unsigned c = __reduce_add_sync(NR_FULL, (unsigned)(x >> 42));
+    return (unsigned long long)a + ((unsigned long long)b << 21) + ((unsigned long long)c << 42);
+}
+
 __device__ __forceinline__ long long nr_globaltimer()
 {
     long long t;

@@ -37,16 +37,63 @@ __host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots)
 {
     size_t b = (size_t)slots * 32 * sizeof(NrLaneAcc);       // per slot, per lane sums
     b += (size_t)(NR_LANE_ROW_WORDS + NR_LANE_MAX_N) * 32 * 4;  // rows, hops, [word][lane]
-    b += (size_t)slots * 32 * 4;                             // per slot, per lane: queued-mass lower bound
+    b += (size_t)slots * 32 * 4;                             // per slot, per lane: queued-mass lower bound (units)
     b += (size_t)slots * NR_LANE2_TAB_BYTES;                 // per slot: p and edge ids
     b += (size_t)slots * sizeof(NrLaneSlot);
-    b += (size_t)slots * 8 * 4;                              // the step's allocation, 8 ints a slot
     b += (size_t)pages * 2;                                  // pnext
     b += (size_t)pages;                                      // pcnt
     b = (b + 1) & ~size_t(1);
     b += (size_t)pages * 2;                                  // free stack
     return (b + 15) & ~size_t(15);
 }
+
+// The root record of an instance at slot 0 of page rpg (the record nr_lane_root builds), from
+// the slot's copy of p (tp, shared memory) and the topology's rows (r16: word `lane` of the
+// table, preloaded).  Edge states come from p's bit pattern (p <= 0 down, p >= 1 up), with
+// integer compares; each 16-edge mask word is one OR reduction over half the lanes' bits.
+template <int W4>
+__device__ __forceinline__ void nr_lane2_root(const NrSmallGraph &g, const unsigned char *gs, const double *tp,
+                                              uint32_t r16, uint4 *sl_mask, uint4 *sl_rows, double *sl_mass, int rpg)
+{
+    constexpr int RW = NR_LANE_ROW_WORDS;
+    const int lane = threadIdx.x & 31;
+    uint32_t *rw = reinterpret_cast<uint32_t *>(sl_mask + (size_t)rpg * NR_PAGE * W4);
+    bool down = false;
+#pragma unroll
+    for (int e0 = 0; e0 < 64 * W4; e0 += 32) {
+        const int e = e0 + lane;
+        uint32_t v = 0u;
+        if (e < g.e) {
+            const long long b = __double_as_longlong(tp[e]);
+            const bool dn = b <= 0ll, up = b >= 0x3ff0000000000000ll;
+            down = down || dn;
+            v = (uint32_t)(dn ? NR_EDGE_DOWN : up ? NR_EDGE_UP : NR_EDGE_UNKNOWN) << ((e & 15) << 1);
+        }
+        const uint32_t lo = __reduce_or_sync(NR_FULL, lane < 16 ? v : 0u);
+        const uint32_t hi = __reduce_or_sync(NR_FULL, lane < 16 ? 0u : v);
+        if (lane == 0) { rw[e0 >> 4] = lo; rw[(e0 >> 4) + 1] = hi; }
+    }
+    uint32_t *rr = reinterpret_cast<uint32_t *>(sl_rows + (size_t)rpg * NR_PAGE * (RW / 4));
+    if (!__any_sync(NR_FULL, down)) {
+        if (lane < RW) rr[lane] = r16;
+    } else {                                   // some edge is certainly down: gather the rows
+        const int *start = reinterpret_cast<const int *>(gs + g.off_start);
+        const uint32_t *list = reinterpret_cast<const uint32_t *>(gs + g.off_list);
+        uint32_t r = 0;
+        if (lane < g.n)
+            for (int j = start[lane]; j < start[lane + 1]; ++j) {
+                const uint32_t a = list[j];
+                if (__double_as_longlong(tp[a >> 8]) > 0ll) r |= 1u << (a & 31u);
+            }
+        const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
+        if (lane < 2 * RW && !(lane & 1)) rr[lane >> 1] = r | (hi << 16);
+    }
+    if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
+}
+
+// the queued mass's lower bound is kept in units of target / 2^20, per lane and slot
+#define NR_LANE2_UNITS (1u << 20)
+#define NR_LANE2_UNIT_CAP (1u << 26)      // a lane's total saturates here: 32 lanes sum below 2^31
 
 template <int W4, int NS>
 __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpParams P)
@@ -62,12 +109,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     NrLaneAcc *accs = reinterpret_cast<NrLaneAcc *>(wbase);                      // [slot * 32 + lane]
     uint32_t *my_rows = reinterpret_cast<uint32_t *>(wbase + NS * 32 * sizeof(NrLaneAcc)) + lane;
     uint32_t *my_hop = my_rows + RW * 32;
-    float *qlb = reinterpret_cast<float *>(wbase + NS * 32 * sizeof(NrLaneAcc) +
-                                           (size_t)(RW + NR_LANE_MAX_N) * 32 * 4);  // [slot * 32 + lane]
+    unsigned *qlb = reinterpret_cast<unsigned *>(wbase + NS * 32 * sizeof(NrLaneAcc) +
+                                                 (size_t)(RW + NR_LANE_MAX_N) * 32 * 4);  // [slot * 32 + lane]
     unsigned char *tabs = reinterpret_cast<unsigned char *>(qlb + NS * 32);                       // [slot]
     NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(tabs + NS * NR_LANE2_TAB_BYTES);
-    int *alloc = reinterpret_cast<int *>(slots + NS);
-    short *pnext = reinterpret_cast<short *>(alloc + 8 * NS);
+    short *pnext = reinterpret_cast<short *>(slots + NS);
     unsigned char *pcnt = reinterpret_cast<unsigned char *>(pnext + NP);
     short *freel = reinterpret_cast<short *>(pcnt + ((NP + 1) & ~1));
 
@@ -77,7 +123,14 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     uint4 *sl_rows = reinterpret_cast<uint4 *>(P.slab_rows) + gw * (size_t)NP * NR_PAGE * (RW / 4);
     const bool use_eps = P.eps > 0.0;
     const long long step_cap = P.step_cap > 0 ? P.step_cap : NR_LANE_STEP_CAP;
-    const float target_hi = __double2float_ru(P.target);      // >= the target
+    // units: a child of mass m adds floor(m * 2^20 / target) (FP32, rounded down, <= the exact
+    // value); a sum above 2^20 units is a queued mass above the target.  Targets below 1e-30
+    // (a scale beyond FP32) take the exact test at every wave's end.
+    const bool use_units = P.target >= 1e-30;
+    const float unit_scale = use_units ? __double2float_rd(1048576.0 / P.target) : 0.0f;
+    const unsigned root_units = use_units ? min(__float2uint_rd(unit_scale), NR_LANE2_UNIT_CAP) : 0u;
+    const int nwarps = (int)(gridDim.x * (blockDim.x >> 5));
+    unsigned fresh = (1u << NS) - 1u;          // slots whose first instance is still to take
 
     for (int p = lane; p < NP; p += 32) { freel[p] = (short)(NP - 1 - p); pnext[p] = -1; pcnt[p] = 0; }
     if (lane < NS) { slots[lane].ii = -1; slots[lane].cur = -1; slots[lane].head = -1; }
@@ -88,12 +141,12 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     // end slot s's instance: its sums and counts to P.out, its pages back to the stack
     auto finish = [&](int s, int status, int check, const NrFix &qs, long long qn) {
         NrLaneAcc &A = accs[s * 32 + lane];
-        const NrFix R = nr_fix_warp_sum(A.R), et = nr_fix_warp_sum(A.et), es_ = nr_fix_warp_sum(A.es);
-        const NrFix qm = nr_fix_warp_sum(qs);
-        const unsigned long long nodes = nr_warp_sum_u64(A.nodes), leaves = nr_warp_sum_u64(A.leaves);
-        const unsigned long long dead = nr_warp_sum_u64(A.dead), trunc = nr_warp_sum_u64(A.trunc);
-        const unsigned long long spilled = nr_warp_sum_u64(A.spilled);
-        const unsigned long long queued = nr_warp_sum_u64((unsigned long long)qn);
+        const NrFix R = nr_fix_warp_sum(A.R), et = nr_fix_warp_sum_sparse(A.et), es_ = nr_fix_warp_sum_sparse(A.es);
+        const NrFix qm = nr_fix_warp_sum_sparse(qs);
+        const unsigned long long nodes = nr_warp_sum_u64r(A.nodes), leaves = nr_warp_sum_u64r(A.leaves);
+        const unsigned long long dead = nr_warp_sum_u64r(A.dead), trunc = nr_warp_sum_u64r(A.trunc);
+        const unsigned long long spilled = nr_warp_sum_u64r(A.spilled);
+        const unsigned long long queued = nr_warp_sum_u64r((unsigned long long)qn);
         NrLaneSlot &S = slots[s];
         if (lane == 0) {
             NrWarpOut o;
@@ -117,48 +170,84 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
     };
 
     for (;;) {
-        // ---- slot upkeep: take instances, end waves, stop tests ----
-        for (int s = 0; s < NS; ++s) {
-            NrLaneSlot &S = slots[s];
-            if (S.ii == -1) {
-                int ii = 0;
-                if (lane == 0) ii = atomicAdd(P.next_inst, 1);
-                ii = __shfl_sync(NR_FULL, ii, 0);
+        // ---- slot upkeep (1): empty slots take instances.  Warp gw starts with instances
+        // gw*NS .. gw*NS+NS-1 (no counter traffic as a batch starts); later ones come from the
+        // counter, past those.  New instances are set up together: one round of table loads.
+        {
+            int ii_t[NS];
+            bool any_new = false;
+#pragma unroll
+            for (int t = 0; t < NS; ++t) {
+                ii_t[t] = -1;
+                if (slots[t].ii != -1) continue;
+                int ii;
+                if (fresh & (1u << t)) {
+                    ii = (int)gw * NS + t;
+                    fresh &= ~(1u << t);
+                } else if (nwarps * NS >= P.n_inst) {
+                    ii = P.n_inst;                          // the first round took every instance
+                } else {
+                    int v = 0;
+                    if (lane == 0) v = atomicAdd(P.next_inst, 1);
+                    ii = __shfl_sync(NR_FULL, v, 0) + nwarps * NS;
+                }
                 if (ii >= P.n_inst) {
-                    if (lane == 0) S.ii = -2;
-                    __syncwarp();
+                    if (lane == 0) slots[t].ii = -2;
                     continue;
                 }
-                const NrSmallGraph g = P.inst[ii];
-                const unsigned char *gb = P.blob + g.blob_off;
-                const unsigned char *gs = P.blob + g.struct_off;
-                int rpg = 0;
-                if (lane == 0) {
-                    S.t0 = nr_globaltimer();
-                    S.ii = ii;
-                    S.n = g.n; S.src = g.src; S.dst = g.dst; S.ge = g.e;
-                    S.waves = 0; S.wave_items = 0; S.max_wave = 0;
-                    rpg = freel[--top];                    // a slot holds <= NP/2 pages: one is free
-                    pcnt[rpg] = 1;
-                    pnext[rpg] = -1;
-                    S.head = rpg; S.cur = -1; S.used = 1;
-                }
-                top = __shfl_sync(NR_FULL, top, 0);
-                rpg = __shfl_sync(NR_FULL, rpg, 0);
-                nr_lane_root<W4>(g, gb, gs, sl_mask, sl_rows, sl_mass, rpg);
-                nr_acc_zero(accs[s * 32 + lane]);
-                {                                  // the slot's tables, for the steps' lookups
-                    double *tp = reinterpret_cast<double *>(tabs + s * NR_LANE2_TAB_BYTES);
-                    uint16_t *te = reinterpret_cast<uint16_t *>(tp + NR_LANE2_MAX_E);
-                    const double *gp = reinterpret_cast<const double *>(gb + g.off_p);
-                    const uint16_t *gi = reinterpret_cast<const uint16_t *>(gs + g.off_eid);
-                    const int es = g.n <= 8 ? 8 : 16;
+                ii_t[t] = ii;
+                any_new = true;
+            }
+            if (any_new) {
+                NrSmallGraph g_t[NS];
+                uint32_t r16[NS];
+#pragma unroll
+                for (int t = 0; t < NS; ++t)
+                    if (ii_t[t] >= 0) g_t[t] = P.inst[ii_t[t]];
+#pragma unroll
+                for (int t = 0; t < NS; ++t) {          // the slots' tables, for the steps' lookups
+                    r16[t] = 0u;
+                    if (ii_t[t] < 0) continue;
+                    const NrSmallGraph &g = g_t[t];
+                    const unsigned char *gs = P.blob + g.struct_off;
+                    double *tp = reinterpret_cast<double *>(tabs + t * NR_LANE2_TAB_BYTES);
+                    uint32_t *te = reinterpret_cast<uint32_t *>(tp + NR_LANE2_MAX_E);
+                    const double *gp = reinterpret_cast<const double *>(P.blob + g.blob_off + g.off_p);
+                    const uint32_t *gi = reinterpret_cast<const uint32_t *>(gs + g.off_eid);
+                    const int ew = (g.n <= 8 ? 8 : 16) * g.n / 2;   // edge-id words
                     for (int e = lane; e < g.e; e += 32) tp[e] = gp[e];
-                    for (int k = lane; k < g.n * es; k += 32) te[k] = gi[k];
+                    for (int k = lane; k < ew; k += 32) te[k] = gi[k];
+                    if (lane < RW) r16[t] = reinterpret_cast<const uint32_t *>(gs + g.off_rows16)[lane];
                 }
-                qlb[s * 32 + lane] = lane == 0 ? 1.0f : 0.0f;   // the root's mass is queued
+                __syncwarp();
+#pragma unroll
+                for (int t = 0; t < NS; ++t) {
+                    if (ii_t[t] < 0) continue;
+                    const NrSmallGraph &g = g_t[t];
+                    NrLaneSlot &S = slots[t];
+                    const int rpg = freel[top - 1];        // a slot holds <= NP/NS pages: one is free
+                    --top;
+                    if (lane == 0) {
+                        S.t0 = nr_globaltimer();
+                        S.ii = ii_t[t];
+                        S.n = g.n; S.src = g.src; S.dst = g.dst; S.ge = g.e;
+                        S.waves = 0; S.wave_items = 0; S.max_wave = 0;
+                        pcnt[rpg] = 1;
+                        pnext[rpg] = -1;
+                        S.head = rpg; S.cur = -1; S.used = 1;
+                    }
+                    nr_lane2_root<W4>(g, P.blob + g.struct_off,
+                                      reinterpret_cast<const double *>(tabs + t * NR_LANE2_TAB_BYTES), r16[t],
+                                      sl_mask, sl_rows, sl_mass, rpg);
+                    nr_acc_zero(accs[t * 32 + lane]);
+                    qlb[t * 32 + lane] = lane == 0 ? root_units : 0u;   // the root's mass is queued
+                }
                 __syncwarp();
             }
+        }
+        // ---- slot upkeep (2): slots whose wave is done (or whose first has not begun) ----
+        for (int s = 0; s < NS; ++s) {
+            NrLaneSlot &S = slots[s];
             if (S.ii < 0 || S.cur >= 0) continue;
             // slot s's wave is done (or its first not begun): the stop tests, in the one-slot
             // kernel's order (target width, node budget, empty queue).  The queued mass is the
@@ -182,10 +271,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             };
             int st = -1;
             if (P.target > 0.0) {
-                float lb = qlb[s * 32 + lane];
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) lb = __fadd_rd(lb, __shfl_xor_sync(NR_FULL, lb, off));
-                if (!(lb > target_hi)) {
+                const unsigned units = use_units ? __reduce_add_sync(NR_FULL, qlb[s * 32 + lane]) : 0u;
+                if (units <= NR_LANE2_UNITS) {
                     if (!chain_sum()) {
                         finish(s, 0, 6, nr_fix_zero(), 0);
                         continue;
@@ -197,7 +284,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                     if (nr_fix_le(w, P.target_fix)) st = 1;
                 }
             }
-            if (st < 0 && P.max_nodes && nr_warp_sum_u64(A.nodes) >= P.max_nodes) st = 3;
+            if (st < 0 && P.max_nodes && nr_warp_sum_u64r(A.nodes) >= P.max_nodes) st = 3;
             if (st < 0 && S.head < 0) st = 0;
             __syncwarp();
             if (st >= 0) {
@@ -207,7 +294,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 }
                 finish(s, st, 0, qs, qn);
             } else {
-                qlb[s * 32 + lane] = 0.0f;          // the next wave's children start a new chain
+                qlb[s * 32 + lane] = 0u;            // the next wave's children start a new chain
                 if (lane == 0) { S.cur = S.head; S.head = -1; S.waves++; S.wave_items = 0; }
                 __syncwarp();
             }
@@ -277,16 +364,24 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
 #pragma unroll
         for (int k = 0; k < RW; ++k) my_rows[32 * k] = rw[k];
         __syncwarp();                               // every lane holds its record: the pages are free
-        if (lane == 0) {
+        {
+            // lane t < NS returns slot t's page to the stack (taken slots in slot order), one body
+            // for all of them; every lane knows the new top
+            int p0 = -1, at = top, cnt = 0;
 #pragma unroll
-            for (int t = 0; t < NS; ++t)
-                if (tpg[t] >= 0) {
-                    const int p0 = tpg[t];
-                    slots[t].cur = pnext[p0]; slots[t].wave_items += tcnt[t]; pnext[p0] = -1;
-                    freel[top++] = (short)p0; slots[t].used--;
-                }
+            for (int t = 0; t < NS; ++t) {
+                if (t == lane) { p0 = tpg[t]; cnt = tcnt[t]; }
+                if (t < lane && tpg[t] >= 0) ++at;
+            }
+            if (lane < NS && p0 >= 0) {
+                NrLaneSlot &T = slots[lane];
+                T.cur = pnext[p0]; T.wave_items += cnt; T.used--;
+                pnext[p0] = -1;
+                freel[at] = (short)p0;
+            }
+#pragma unroll
+            for (int t = 0; t < NS; ++t) top += tpg[t] >= 0;
         }
-        top = __shfl_sync(NR_FULL, top, 0);
         __syncwarp();
 
         // the lane's instance
@@ -338,44 +433,46 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             tbeg[t] = (tcnt[t] && toff[t] > 0) ? b1 : 0;
         }
         pre -= nch;
-        if (lane == 0) {
+        // Allocation, slot by slot: the head page's free records, then new pages from the free
+        // stack.  Every lane computes it (its inputs are warp-uniform) and keeps its own slot's
+        // part; lane t < NS then writes slot t's part, one body for all of them.
+        int hA = -1, cA2 = 0, nA = 0, npg = 0, top0 = 0;
+        int a_hd[NS], a_c[NS], a_n[NS], a_pg[NS], a_top[NS], a_want[NS];
 #pragma unroll
-            for (int t = 0; t < NS; ++t) {
-                NrLaneSlot &T = slots[t];
-                const int want = tend[t] - tbeg[t];
-                int hA = -1, cA2 = 0, nA = 0, npg = 0;
-                const int top0 = top;
-                if (want > 0) {
-                    const int hd = T.head;
-                    const int c = (hd >= 0) ? pcnt[hd] : NR_PAGE;
-                    nA = min(want, NR_PAGE - c);
-                    if (nA > 0) { hA = hd; cA2 = c; pcnt[hd] = (unsigned char)(c + nA); }
-                    const int rest = want - nA;
-                    npg = min(min((rest + NR_PAGE - 1) / NR_PAGE, top0), max(0, budget - T.used));
-                    int prev = hd;
-                    for (int i = 0; i < npg; ++i) {
-                        const int pgi = freel[top0 - 1 - i];
-                        pnext[pgi] = (short)prev;
-                        pcnt[pgi] = (unsigned char)min(NR_PAGE, rest - NR_PAGE * i);
-                        prev = pgi;
-                    }
-                    if (npg > 0) { T.head = prev; T.used += npg; }
-                    top = top0 - npg;
-                }
-                alloc[8 * t] = hA; alloc[8 * t + 1] = cA2; alloc[8 * t + 2] = nA; alloc[8 * t + 3] = npg;
-                alloc[8 * t + 4] = top0;
-            }
+        for (int t = 0; t < NS; ++t) {
+            const int want = tend[t] - tbeg[t];
+            const int hd = slots[t].head;
+            const int c = (want > 0 && hd >= 0) ? (int)pcnt[hd] : NR_PAGE;
+            const int na = want > 0 ? min(want, NR_PAGE - c) : 0;
+            const int rest = want - na;
+            const int np = want > 0 ? min(min((rest + NR_PAGE - 1) / NR_PAGE, top), max(0, budget - slots[t].used)) : 0;
+            a_hd[t] = hd; a_c[t] = c; a_n[t] = na; a_pg[t] = np; a_top[t] = top; a_want[t] = want;
+            top -= np;
+            if (t == sl) { hA = na > 0 ? hd : -1; cA2 = c; nA = na; npg = np; top0 = a_top[t]; }
         }
-        top = __shfl_sync(NR_FULL, top, 0);
-        __syncwarp();
-        const int hA = alloc[8 * sl], cA2 = alloc[8 * sl + 1], nA = alloc[8 * sl + 2], npg = alloc[8 * sl + 3];
-        const int top0 = alloc[8 * sl + 4];
+        __syncwarp();                               // every lane has read the slots' state
+        if (lane < NS) {
+            int hd = -1, c = 0, na = 0, np = 0, t0p = 0, want = 0;
+#pragma unroll
+            for (int t = 0; t < NS; ++t)
+                if (t == lane) { hd = a_hd[t]; c = a_c[t]; na = a_n[t]; np = a_pg[t]; t0p = a_top[t]; want = a_want[t]; }
+            if (na > 0) pcnt[hd] = (unsigned char)(c + na);
+            const int rest = want - na;
+            int prev = hd;
+            for (int i = 0; i < np; ++i) {
+                const int pgi = freel[t0p - 1 - i];
+                pnext[pgi] = (short)prev;
+                pcnt[pgi] = (unsigned char)min(NR_PAGE, rest - NR_PAGE * i);
+                prev = pgi;
+            }
+            if (np > 0) { slots[lane].head = prev; slots[lane].used += np; }
+        }
         int q = pre;                                // this lane's first child, within its slot
 #pragma unroll
         for (int t = 0; t < NS; ++t)
             if (t == sl) q -= tbeg[t];
         double Pm = mass;
-        float qadd = 0.0f;                          // lower bound of the mass this lane queues
+        unsigned qadd = 0u;                         // lower bound of the mass this lane queues, in units
         for (int h = 0; h < L; ++h) {
             const uint32_t hp = my_hop[32 * h];
             const int e = NR_HOP_E(hp);
@@ -396,7 +493,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             ++q;
             if (sc >= 0) {
                 nr_lane_write_child<W4>(sl_mask, sl_rows, sl_mass, sc, wc, rw, my_rows, e, wv, cu, cv, cm);
-                qadd = __fadd_rd(qadd, __double2float_rd(cm));
+                qadd += min(__float2uint_rd(__fmul_rd(__double2float_rd(cm), unit_scale)), NR_LANE2_UNIT_CAP);
             } else {                                  // the slot's pages are full: mass to ESP
                 acc.spilled++;
                 nr_fix_add_mass(acc.es, cm);
@@ -409,7 +506,7 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             acc.leaves++;
             nr_fix_add_mass(acc.R, Pm);
         }
-        if (qadd > 0.0f) qlb[sl * 32 + lane] = __fadd_rd(qlb[sl * 32 + lane], qadd);
+        if (qadd) qlb[sl * 32 + lane] = min(qlb[sl * 32 + lane] + min(qadd, NR_LANE2_UNIT_CAP), NR_LANE2_UNIT_CAP);
         __syncwarp();
     }
 }
