@@ -248,17 +248,18 @@ def e2e_ring_matrices(w, device):
     return [first] + [rng.uniform(0.9, 0.99, size=first.shape) for _ in range(n_ring - 1)]
 
 
-def run_pipelined(ctx, ring, submit, steps):
-    """Two batches in flight: submit ring[k % len(ring)], then wait for the one before it.  Every step
-    uploads its inputs from host memory and reads its results back."""
+def run_pipelined(ctx, ring, submit, steps, depth=3):
+    """`depth` batches in flight (the context's batch slots): submit ring[k % len(ring)], then wait for
+    the one submitted depth-1 steps before it.  Every step uploads its inputs from host memory and
+    reads its results back."""
     def loop(k_steps):
-        pending = None
+        pending = []
         for k in range(k_steps):
-            tk = submit(ring[k % len(ring)])
-            if pending is not None:
-                ctx.wait(pending)
-            pending = tk
-        ctx.wait(pending)
+            pending.append(submit(ring[k % len(ring)]))
+            if len(pending) >= depth:
+                ctx.wait(pending.pop(0))
+        for tk in pending:
+            ctx.wait(tk)
 
     import torch
     loop(3)
@@ -303,7 +304,7 @@ def pipelined_e2e_matrix(ctx, w, opts, steps, mats):
 
 
 def pipelined_e2e_flushed(ctx, w, capacity, opts, flush_buf, steps, device):
-    """Two batches in flight through nr_batch_submit / nr_batch_wait on the workload's inputs: a 192 MB
+    """Three batches in flight through nr_batch_submit / nr_batch_wait on the workload's inputs: a 192 MB
     L2 flush (1.5x the L2) runs on its own stream before each step's upload, which is ordered after it."""
     import ctypes
     import torch
@@ -321,7 +322,7 @@ def pipelined_e2e_flushed(ctx, w, capacity, opts, flush_buf, steps, device):
             raise RuntimeError("cudaMemsetAsync (L2 flush) failed")
         return ctx.submit(bb, capacity=capacity, after_stream=fs.cuda_stream, options=o)
 
-    ring = [nr.Batch(w["graphs"], w["srcs"], w["dsts"]) for _ in range(2)]
+    ring = [nr.Batch(w["graphs"], w["srcs"], w["dsts"]) for _ in range(3)]     # one per batch in flight
     return run_pipelined(ctx, ring, submit, steps)
 
 
@@ -727,7 +728,7 @@ def main():
         "e2e": {"value": tot["pipe_nodes"] / tot["pipe_wall_max"], "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "api": "nr_batch_submit_matrix / nr_batch_wait (one topology, a [4096 x 105] probability "
-                       "matrix in pinned host memory uploaded every step), two batches in flight",
+                       "matrix in pinned host memory uploaded every step), three batches in flight",
                 "l2": f"inputs larger than the L2: a ring of {len(mats)} distinct probability matrices "
                       f"({sum(m.nbytes for m in mats) / 2**20:.0f} MB; the first is the workload's, the others "
                       f"p~U[0.9,0.99] seeded), a different one every step; no flush",

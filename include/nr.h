@@ -218,10 +218,10 @@ int  nr_reliability_batch(nr_context *ctx, int n_instances, const nr_graph *grap
 /* Asynchronous batches (no reference counterpart): nr_reliability_batch in
  * two halves, so the host builds one batch's tables while the GPU runs the
  * one before.  nr_batch_submit checks the batch, builds its tables and queues
- * the upload, the kernels and the read-back on one of the context's two batch
+ * the upload, the kernels and the read-back on one of the context's three batch
  * slots, and returns a ticket; nr_batch_wait(ticket) finishes that batch and
  * fills `results` (as given to the submit) exactly as nr_reliability_batch
- * would.  Slots alternate: a submit whose slot still holds an unfinished batch
+ * would.  Slots take turns: a submit whose slot still holds an unfinished batch
  * finishes it first (a later wait on its ticket returns its status).  graphs,
  * srcs, dsts and results must stay valid and unchanged until the wait returns.
  * `after_stream` (a cudaStream_t, or NULL): the batch's upload starts after the

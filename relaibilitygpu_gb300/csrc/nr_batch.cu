@@ -114,6 +114,17 @@ static int slot_ready(NrSlot &sl)
     return NR_OK;
 }
 
+// Order the work queued next on stream s after the work already queued on the
+// caller's stream `after` (none: nothing to wait for).
+static int wait_for_caller(nr_context *c, cudaStream_t s, cudaStream_t after)
+{
+    if (!after) return NR_OK;
+    if (!c->ev_after) NR_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_after, cudaEventDisableTiming));
+    NR_CUDA_TRY(cudaEventRecord(c->ev_after, after));
+    NR_CUDA_TRY(cudaStreamWaitEvent(s, c->ev_after, 0));
+    return NR_OK;
+}
+
 // Build the tables of instances [0, n) of gs on the host and queue their
 // upload, the kernels and the read-back of the outputs on slot `sl`.  `base`
 // is the index of gs[0] in the caller's batch (for collected children).
@@ -144,7 +155,6 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     int rc = NR_OK;
     const int B = std::max(1, std::min(NR_HOST_BLOCKS, n / 128));
     auto blk_begin = [&](int b) { return (int)((long long)n * b / B); };
-    size_t pm_off = 0, pm_bytes = 0;          // matrix batches: where the matrix goes, its bytes
     if (pmat && !uniform) return NR_ERR_INVALID;
     if (uniform) {
         // one topology (the same CSR arrays) for every instance: every instance's tables have the
@@ -186,6 +196,18 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         memset(hb + off_cnt, 0, sizeof(int) * (NCLS + 1));
         t.struct_off = (long long)(pmat ? tbase : tbase + ib);
         small_fill_struct(&gs[0], &t, hb + t.struct_off);
+        if (pmat) {
+            // the matrix is the bulk of the upload: queue it, after the counters and the
+            // structural part and before the descriptors are built, so that the copy runs while
+            // the host writes them; then the scan of the matrix for NaN
+            unsigned char *wb0 = static_cast<unsigned char *>(sl.wbuf);
+            rc = wait_for_caller(c, sl.stream, after);
+            if (rc) return rc;
+            NR_CUDA_TRY(cudaMemcpyAsync(wb0, hb, off_pm, cudaMemcpyHostToDevice, sl.stream));
+            NR_CUDA_TRY(cudaMemcpyAsync(wb0 + off_pm, pmat, (size_t)n * pm_row, cudaMemcpyHostToDevice, sl.stream));
+            NR_CUDA_TRY(nr_launch_nan_scan(reinterpret_cast<const double *>(wb0 + off_pm), (size_t)n * gs[0].n_edges,
+                                           reinterpret_cast<int *>(wb0 + sizeof(int) * NCLS), sl.stream));
+        }
         pc.mark("sizes");
         std::atomic<int> bad(NR_OK);
         const int n_nodes0 = gs[0].n_nodes;
@@ -216,8 +238,6 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         });
         if (bad.load() != NR_OK) return bad.load();
         sl.off_flag = sizeof(int) * NCLS;
-        pm_off = off_pm;
-        pm_bytes = pmat ? (size_t)n * pm_row : 0;
         pc.mark("tables");
     } else {
     // Host blocks: contiguous instance ranges, one task of the worker pool each.  Two
@@ -392,20 +412,13 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     unsigned char *wb = static_cast<unsigned char *>(sl.wbuf);
     cudaStream_t s = sl.stream;
     pc.mark("geometry");
-    if (after) {                          // the upload waits for the caller's stream
-        if (!c->ev_after) NR_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_after, cudaEventDisableTiming));
-        NR_CUDA_TRY(cudaEventRecord(c->ev_after, after));
-        NR_CUDA_TRY(cudaStreamWaitEvent(s, c->ev_after, 0));
-    }
     if (pmat) {
-        // counters and structural part, the caller's matrix straight from its memory (a plain DMA
-        // when it is pinned), descriptors and ids; then a scan of the matrix for NaN on the device
-        NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, pm_off, cudaMemcpyHostToDevice, s));
-        NR_CUDA_TRY(cudaMemcpyAsync(wb + pm_off, pmat, pm_bytes, cudaMemcpyHostToDevice, s));
+        // counters, structural part and the caller's matrix (straight from its memory: a plain
+        // DMA when it is pinned) are queued already, with the NaN scan; descriptors and ids now
         NR_CUDA_TRY(cudaMemcpyAsync(wb + off_desc, hb + off_desc, up_bytes - off_desc, cudaMemcpyHostToDevice, s));
-        NR_CUDA_TRY(nr_launch_nan_scan(reinterpret_cast<const double *>(wb + pm_off), pm_bytes / sizeof(double),
-                                       reinterpret_cast<int *>(wb + sl.off_flag), s));
     } else {
+        rc = wait_for_caller(c, s, after);
+        if (rc) return rc;
         NR_CUDA_TRY(cudaMemcpyAsync(wb, hb, up_bytes, cudaMemcpyHostToDevice, s));
     }
     NR_CUDA_TRY(cudaEventRecord(sl.ev0, s));

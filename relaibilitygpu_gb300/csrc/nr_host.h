@@ -174,7 +174,7 @@ struct WarpRunCfg {
 // tables are built on the host while the batch before runs.  (Splitting one
 // batch over both slots measured slower on 4096 K15 instances: the host passes
 // are dominated by fixed costs and two concurrent launches lengthen the span.)
-#define NR_SLOTS 2
+#define NR_SLOTS 3
 struct NrSlot {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;   // around the part's kernels

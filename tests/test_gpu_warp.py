@@ -226,16 +226,16 @@ def test_batch_rejects_bad_instances(ctx, engine_lib):
 
 
 def test_async_batches_match_sync(ctx, oracle):
-    """nr_batch_submit / nr_batch_wait: three batches in flight on two slots (the third submit
+    """nr_batch_submit / nr_batch_wait: four batches in flight on three slots (the fourth submit
     finishes the first), waits in any order, results identical to the synchronous call."""
     from relaibilitygpu_gb300 import graphs
     import relaibilitygpu_gb300 as nr
-    sets = [[graphs.complete(12, p_range=(0.85, 0.99), seed=1000 * k + i) for i in range(700)] for k in range(3)]
+    sets = [[graphs.complete(12, p_range=(0.85, 0.99), seed=1000 * k + i) for i in range(700)] for k in range(4)]
     opts = dict(target_width=1e-6, bucket_shift=1, n_buckets=128)
     ref = [ctx.reliability_batch(gs, [0] * 700, [11] * 700, **opts) for gs in sets]
     batches = [nr.Batch(gs, [0] * 700, [11] * 700) for gs in sets]
     tickets = [ctx.submit(b, **opts) for b in batches]
-    for t in (tickets[2], tickets[0], tickets[1]):
+    for t in (tickets[2], tickets[0], tickets[3], tickets[1]):
         ctx.wait(t)
     for b, rr in zip(batches, ref):
         got = [nr.Result.from_raw(b.res[i]) for i in range(b.n)]
