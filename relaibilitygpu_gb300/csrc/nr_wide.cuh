@@ -145,7 +145,7 @@ struct NrWideOut {
     unsigned *hist;                  // bucket schedule: this block's new records per bucket (shared memory)
 };
 
-// Lane-0 accumulators of a warp.
+// Accumulators of a warp (its lane 0 updates them; they live in the block's shared memory).
 struct NrWideAcc {
     NrFix R, et, es;
     NrFix net;                       // mass queued minus mass popped
@@ -193,11 +193,92 @@ __device__ __forceinline__ void nr_wide_load_mask(uint32_t *m, const uint4 *src,
     for (int k = threadIdx.x & 31; k < w4; k += 32) reinterpret_cast<uint4 *>(m)[k] = __ldcg(src + k);
 }
 
+// Two-terminal BFS of the warp from src over the arcs whose edge is not down
+// (up_only: up), with the parent rule above; true if dst is reached.  The
+// frontier is a node list: the lanes take its nodes, walk their arcs two at a
+// time (independent loads), and the first discoverer of a node (the atomicOr
+// that set its bit) appends it to the next list, so no level compacts a
+// bitmask; the parent is still the atomicMin over every discovering arc of
+// the level.  v.list and v.order hold the two lists, v.F[0] the next count.
+__device__ __forceinline__ bool nr_wide_bfs_tt(const NrWideGraph &g, const NrWideView &v, bool up_only)
+{
+    const int lane = threadIdx.x & 31;
+    const int n = g.n, nwd = g.nwd, src = g.src, dst = g.dst;
+    const uint32_t *m = v.m;
+    uint32_t *NF = v.NF, *VIS = v.VIS, *par = v.par, *cnt = v.F;
+    uint32_t *cur = v.list, *nxt = v.order;
+    const uint32_t sel = up_only ? 3u : 1u;      // usable: state & sel == 01 (01 or 11; up_only: 01)
+    constexpr uint32_t HM = (1u << NR_WIDE_HEAD_BITS) - 1u;
+    for (int i = lane; i < nwd; i += 32) {
+        VIS[i] = 0u;
+        NF[i] = 0u;
+    }
+    for (int i = lane; i < n; i += 32) par[i] = 0xffffffffu;
+    __syncwarp();
+    if (lane == 0) {
+        VIS[src >> 5] = 1u << (src & 31);
+        cur[0] = (uint32_t)src;
+    }
+    int f = 1;
+    bool found = (src == dst);
+    for (int level = 0; !found && f > 0 && level < n; ++level) {
+        if (lane == 0) cnt[0] = 0u;
+        __syncwarp();
+        for (int i = lane; i < f; i += 32) {
+            const uint32_t u = cur[i];
+            const int j1 = v.row[u + 1];
+            int j = v.row[u];
+            auto visit = [&](uint32_t w, uint32_t e) {
+                const uint32_t bit = 1u << (w & 31);
+                const uint32_t old = atomicOr(&NF[w >> 5], bit);
+                atomicMin(&par[w], (u << 16) | e);
+                if (!(old & bit)) nxt[atomicAdd(cnt, 1u)] = w;
+            };
+            for (; j + 2 <= j1; j += 2) {
+                const uint32_t a0 = v.arc[j], a1 = v.arc[j + 1];
+                const uint32_t w0 = a0 & HM, e0 = a0 >> NR_WIDE_HEAD_BITS;
+                const uint32_t w1 = a1 & HM, e1 = a1 >> NR_WIDE_HEAD_BITS;
+                const uint32_t s0 = (m[e0 >> 4] >> ((e0 & 15) << 1)) & sel;
+                const uint32_t s1 = (m[e1 >> 4] >> ((e1 & 15) << 1)) & sel;
+                const uint32_t q0 = (VIS[w0 >> 5] >> (w0 & 31)) & 1u;
+                const uint32_t q1 = (VIS[w1 >> 5] >> (w1 & 31)) & 1u;
+                if (s0 == 1u && !q0) visit(w0, e0);
+                if (s1 == 1u && !q1) visit(w1, e1);
+            }
+            if (j < j1) {
+                const uint32_t a0 = v.arc[j];
+                const uint32_t w0 = a0 & HM, e0 = a0 >> NR_WIDE_HEAD_BITS;
+                if (((m[e0 >> 4] >> ((e0 & 15) << 1)) & sel) == 1u && !((VIS[w0 >> 5] >> (w0 & 31)) & 1u))
+                    visit(w0, e0);
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < nwd; i += 32) {
+            const uint32_t nf = NF[i];
+            if (nf) {
+                VIS[i] |= nf;
+                NF[i] = 0u;
+            }
+        }
+        __syncwarp();
+        f = (int)cnt[0];
+        found = (VIS[dst >> 5] >> (dst & 31)) & 1u;
+        uint32_t *t = cur;
+        cur = nxt;
+        nxt = t;
+        __syncwarp();
+    }
+    return found;
+}
+
 // BFS of the warp from src over the arcs whose edge is not down (up_only:
 // up), with the parent rule above; true if dst is reached.  All 32 lanes call it.
+// K-terminal (n_order given) keeps the bitmask frontier, whose compaction
+// yields the visit order; two-terminal searches take nr_wide_bfs_tt.
 __device__ __forceinline__ bool nr_wide_bfs(const NrWideGraph &g, const NrWideView &v, bool up_only,
                                             int *n_order = nullptr)
 {
+    if (n_order == nullptr) return nr_wide_bfs_tt(g, v, up_only);
     const int lane = threadIdx.x & 31;
     const int n = g.n, nwd = g.nwd, src = g.src, dst = g.dst;
     const uint32_t *m = v.m;
@@ -518,6 +599,15 @@ __device__ __forceinline__ void nr_wide_acc_init(NrWideAcc &A)
     A.nodes = A.leaves = A.dead = A.trunc = A.spilled = 0;
 }
 
+// The block's partial sums from its warps' accumulators (lane 0 of each warp holds them).
+__device__ __forceinline__ void nr_wide_block_partial(NrPartial *out, const NrWideAcc &A)
+{
+    NrWideAcc F;
+    if ((threadIdx.x & 31) == 0) F = A;
+    else nr_wide_acc_init(F);                                // zeros off thread 0
+    nr_block_partial(out, F.R, F.et, F.es, F.net, F.nodes, F.leaves, F.dead, F.trunc, F.spilled);
+}
+
 // Sum over the block of a per-thread count, on every thread.
 __device__ __forceinline__ unsigned long long nr_block_u64_sum(unsigned long long x)
 {
@@ -581,7 +671,7 @@ __device__ __forceinline__ int nr_wide_stop_test(const NrWideShare *slot, bool f
 }
 
 template <int W4>
-__global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideParams P)
+__global__ void __launch_bounds__(NR_WIDE_BLOCK, 6) nr_grid_wide_kernel(NrGridWideParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const NrWideGraph g = P.g;
@@ -593,8 +683,11 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
     const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const unsigned long long TW = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long cap = P.capacity;
-    NrWideAcc A;
-    nr_wide_acc_init(A);
+    // the warp's accumulators: shared memory, written by its lane 0 only (registers for the step)
+    __shared__ NrWideAcc s_acc[NR_WIDE_BLOCK / 32];
+    NrWideAcc &A = s_acc[warp];
+    if (lane == 0) nr_wide_acc_init(A);
+    __syncwarp();
 
     for (int wave = 0; wave < P.max_waves; ++wave) {
         unsigned long long n_in = *(volatile unsigned long long *)&P.wave_count[wave];
@@ -629,8 +722,7 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_grid_wide_kernel(NrGridWideP
             *(volatile unsigned long long *)&P.wave_count[wave + 1] != 0)
             atomicOr(P.status, NR_DEV_ERR_WAVES);
     }
-    nr_block_partial(P.partials + blockIdx.x, A.R, A.et, A.es, A.net, A.nodes, A.leaves, A.dead, A.trunc,
-                     A.spilled);
+    nr_wide_block_partial(P.partials + blockIdx.x, A);
 }
 
 // Records queued in all buckets and the highest non-empty bucket (every block
@@ -730,7 +822,7 @@ __device__ __forceinline__ bool nr_bucket_compact(const NrBucketWideParams &P, u
 }
 
 template <int W4>
-__global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketWideParams P)
+__global__ void __launch_bounds__(NR_WIDE_BLOCK, 6) nr_bucket_wide_kernel(NrBucketWideParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_hist[NR_WIDE_MAX_NB + 1];
@@ -743,13 +835,15 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketW
     const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const unsigned long long TW = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long cap = P.capacity;
-    NrWideAcc A;
-    nr_wide_acc_init(A);
+    __shared__ NrWideAcc s_acc[NR_WIDE_BLOCK / 32];          // as in nr_grid_wide_kernel
+    NrWideAcc &A = s_acc[warp];
+    if (lane == 0) nr_wide_acc_init(A);
     if (P.resume && blockIdx.x == 0 && threadIdx.x == 0) {
         A.R = P.init_R; A.et = P.init_et; A.es = P.init_es; A.net = P.init_net;
         A.nodes = P.init_nodes; A.leaves = P.init_leaves; A.dead = P.init_dead; A.trunc = P.init_trunc;
         A.spilled = P.init_spilled;
     }
+    __syncwarp();
     NrWideOut O;
     O.mask = P.mask;
     O.mass = P.mass;
@@ -817,6 +911,5 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK) nr_bucket_wide_kernel(NrBucketW
         P.stop_info[1] = stop;
         P.stats[1] = live;
     }
-    nr_block_partial(P.partials + blockIdx.x, A.R, A.et, A.es, A.net, A.nodes, A.leaves, A.dead, A.trunc,
-                     A.spilled);
+    nr_wide_block_partial(P.partials + blockIdx.x, A);
 }
