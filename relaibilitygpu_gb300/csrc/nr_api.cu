@@ -503,10 +503,32 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
 // ---------------------------------------------------------------------------
 // whole-GPU engine for 33..16384 nodes (nr_wide.cuh)
 // ---------------------------------------------------------------------------
-static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg, std::vector<unsigned char> *blob,
-                            const int32_t *terms = nullptr, int nt = 0)
+// The bitset search's conditions: at most NR_WIDE_BITS_MAX_N nodes, no self-loop, no two arcs
+// with the same tail and head, no edge id on more than two arcs.
+static bool wide_bits_ok(const nr_graph *g)
 {
     const int n = g->n_nodes, E = g->n_edges;
+    if (n > NR_WIDE_BITS_MAX_N) return false;
+    std::vector<unsigned char> uses(std::max(E, 1), 0);
+    uint32_t seen[NR_WIDE_BITS_MAX_N / 32];
+    for (int u = 0; u < n; ++u) {
+        memset(seen, 0, sizeof(seen));
+        for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
+            const int w = g->col_idx[j], e = g->edge_id[j];
+            if (w == u || ((seen[w >> 5] >> (w & 31)) & 1u) || ++uses[e] > 2) return false;
+            seen[w >> 5] |= 1u << (w & 31);
+        }
+    }
+    return true;
+}
+
+static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg, std::vector<unsigned char> *blob,
+                            const int32_t *terms = nullptr, int nt = 0, bool fork = false)
+{
+    const int n = g->n_nodes, E = g->n_edges;
+    // the bitset search serves two-terminal path branching (the fork's up-only search and the
+    // K-terminal visit order walk the out-arcs)
+    wg->bitset = (!fork && nt == 0 && wide_bits_ok(g)) ? 1 : 0;
     const int W = std::max(1, (2 * E + 31) / 32);
     wg->n = n; wg->e = E; wg->w4 = (W + 3) / 4; wg->src = src; wg->dst = dst; wg->n_arcs = g->n_arcs;
     wg->nwd = (n + 31) / 32;
@@ -516,6 +538,11 @@ static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg
     wg->off_row = (int)off; off = align16(off + sizeof(int) * (n + 1));
     wg->off_arc = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
     wg->off_kmask = (int)off; off = align16(off + sizeof(uint32_t) * wg->nwd);
+    wg->off_rows = wg->off_ehead = 0;
+    if (wg->bitset) {
+        wg->off_rows = (int)off; off = align16(off + sizeof(uint32_t) * (size_t)n * wg->nwd);
+        wg->off_ehead = (int)off; off = align16(off + sizeof(uint32_t) * std::max(E, 1));
+    }
     wg->blob_bytes = (int)off;
     blob->assign(off, 0);
     // K-terminal: the terminals other than src
@@ -532,9 +559,27 @@ static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg
     int *row = reinterpret_cast<int *>(blob->data() + wg->off_row);
     uint32_t *arc = reinterpret_cast<uint32_t *>(blob->data() + wg->off_arc);
     for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
-    for (int u = 0; u <= n; ++u) row[u] = g->row_ptr[u];
-    for (int j = 0; j < g->n_arcs; ++j)
-        arc[j] = ((uint32_t)g->edge_id[j] << NR_WIDE_HEAD_BITS) | (uint32_t)g->col_idx[j];
+    if (wg->bitset) {
+        // in-arcs (eid << 14 | tail) grouped by head, out-neighbour rows, heads of each edge
+        uint32_t *rows = reinterpret_cast<uint32_t *>(blob->data() + wg->off_rows);
+        uint32_t *eh = reinterpret_cast<uint32_t *>(blob->data() + wg->off_ehead);
+        for (int e = 0; e < E; ++e) eh[e] = 0xffffffffu;
+        std::vector<int> fill(n + 1, 0);
+        for (int j = 0; j < g->n_arcs; ++j) fill[g->col_idx[j] + 1]++;
+        for (int w = 0; w < n; ++w) fill[w + 1] += fill[w];
+        for (int w = 0; w <= n; ++w) row[w] = fill[w];
+        for (int u = 0; u < n; ++u)
+            for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
+                const int w = g->col_idx[j], e = g->edge_id[j];
+                arc[fill[w]++] = ((uint32_t)e << NR_WIDE_HEAD_BITS) | (uint32_t)u;
+                rows[(size_t)u * wg->nwd + (w >> 5)] |= 1u << (w & 31);
+                eh[e] = ((eh[e] & 0xffffu) == 0xffffu) ? (0xffff0000u | (uint32_t)w) : ((eh[e] & 0xffffu) | ((uint32_t)w << 16));
+            }
+    } else {
+        for (int u = 0; u <= n; ++u) row[u] = g->row_ptr[u];
+        for (int j = 0; j < g->n_arcs; ++j)
+            arc[j] = ((uint32_t)g->edge_id[j] << NR_WIDE_HEAD_BITS) | (uint32_t)g->col_idx[j];
+    }
     wg->tables_global = off > NR_WIDE_STAGE_MAX;
 }
 
@@ -568,7 +613,7 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
     if (g->n_nodes > NR_WIDE_MAX_N || g->n_edges > 65535) return NR_ERR_UNSUPPORTED;
     NrWideGraph wg;
     std::vector<unsigned char> blob;
-    build_wide_blob(g, src, dst, &wg, &blob, terms, nt);
+    build_wide_blob(g, src, dst, &wg, &blob, terms, nt, o->branching == NR_BRANCH_FORK);
     const int W4 = wg.w4;
     const void *kfn = nr_grid_wide_kernel_ptr(W4);
     if (!kfn) return NR_ERR_UNSUPPORTED;
@@ -748,7 +793,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     const int nb = std::max(1, std::min(NR_WIDE_MAX_NB, o->n_buckets > 0 ? (int)o->n_buckets : NR_WIDE_MAX_NB));
     NrWideGraph wg;
     std::vector<unsigned char> blob;
-    build_wide_blob(g, src, dst, &wg, &blob, terms, nt);
+    build_wide_blob(g, src, dst, &wg, &blob, terms, nt, o->branching == NR_BRANCH_FORK);
     const int W4 = wg.w4;
     const void *kfn = nr_bucket_wide_kernel_ptr(W4);
     if (!kfn) return NR_ERR_UNSUPPORTED;

@@ -46,13 +46,20 @@
 // arcs[n_arcs] (u32 = eid << 14 | head).  Offsets from the blob start, 16-byte aligned.
 // Tables up to NR_WIDE_STAGE_MAX are staged into every block's shared memory; larger ones (the
 // reference's 6301-node directed fixture: 440 KB) are read from global memory (L2).
+// Bitset tables (bitset = 1; two-terminal path branching on graphs of <= NR_WIDE_BITS_MAX_N nodes
+// without self-loops or parallel arcs): row/arc then hold the IN-arcs (u32 = eid << 14 | tail),
+// rows[n][nwd] each node's out-neighbour bitmask, ehead[E] the heads of an edge's arcs (low and
+// high 16 bits; 0xffff: none).
 struct NrWideGraph {
     int n, e, w4, src, dst, n_arcs, nwd;
     int off_p, off_q, off_row, off_arc, blob_bytes;
     int nk;                     // K-terminal: terminals other than src (0: two-terminal, dst)
     int off_kmask;              // K-terminal: bitmask of the terminals, nwd words
     int tables_global;          // 1: the tables stay in global memory
+    int bitset;                 // 1: the bitset search (nr_wide_bfs_bits) and its tables
+    int off_rows, off_ehead;
 };
+#define NR_WIDE_BITS_MAX_N 256  // bitset search: nwd <= 8 words, levels fit a byte
 
 // A block's share of the stop test, written at the end of each wave.
 struct NrWideShare {
@@ -156,6 +163,7 @@ struct NrWideView {
     const double *p, *q;
     const int *row;
     const uint32_t *arc;
+    const uint32_t *rows, *ehead;    // bitset tables (g.bitset)
     const uint32_t *kmask;           // K-terminal terminals (nullptr: two-terminal)
     uint32_t *m, *wk, *F, *NF, *VIS, *par, *list, *hops, *order;
 };
@@ -171,6 +179,8 @@ __device__ __forceinline__ NrWideView nr_wide_view(unsigned char *smem, const un
     v.q = reinterpret_cast<const double *>(tb + g.off_q);
     v.row = reinterpret_cast<const int *>(tb + g.off_row);
     v.arc = reinterpret_cast<const uint32_t *>(tb + g.off_arc);
+    v.rows = g.bitset ? reinterpret_cast<const uint32_t *>(tb + g.off_rows) : nullptr;
+    v.ehead = g.bitset ? reinterpret_cast<const uint32_t *>(tb + g.off_ehead) : nullptr;
     const int warp = threadIdx.x >> 5;
     uint32_t *ws = reinterpret_cast<uint32_t *>(smem + (g.tables_global ? 0 : g.blob_bytes) +
                                                 (size_t)warp * nr_wide_warp_shm(g.n, g.w4));
@@ -269,6 +279,129 @@ __device__ __forceinline__ bool nr_wide_bfs_tt(const NrWideGraph &g, const NrWid
         __syncwarp();
     }
     return found;
+}
+
+// Two-terminal BFS on node bitsets (g.bitset).  The next level is the union of
+// the frontier's out-neighbour rows less the visited set; a new node that is
+// the head of a down arc (the set H, from the mask's 00 states) stays only if
+// one of its in-arcs from the frontier has a not-down edge, so the levels are
+// those of the search over not-down arcs.  Word k of a union is OR-ed by the
+// lanes k, k + nwp, ... (nwp: nwd rounded up to a power of two) and combined
+// by shuffles; no atomics on the search's state.  Levels go to lvl[] (the
+// bytes of v.par), the frontier lists to v.list / v.order in ascending node
+// order; the parents follow on the path only (nr_wide_path_bits).
+__device__ __forceinline__ bool nr_wide_bfs_bits(const NrWideGraph &g, const NrWideView &v)
+{
+    constexpr uint32_t HM = (1u << NR_WIDE_HEAD_BITS) - 1u;
+    const int lane = threadIdx.x & 31;
+    const int n = g.n, nwd = g.nwd, src = g.src, dst = g.dst, E = g.e;
+    const uint32_t *m = v.m;
+    uint32_t *F = v.F, *VIS = v.VIS, *H = v.NF;
+    uint8_t *lvl = reinterpret_cast<uint8_t *>(v.par);
+    uint32_t *cur = v.list, *nxt = v.order;
+    if (lane < nwd) { H[lane] = 0u; VIS[lane] = 0u; F[lane] = 0u; }
+    __syncwarp();
+    // H: heads of the arcs of the down edges (00 states; mask bits past edge E-1 are padding)
+    for (int k = lane; k < 4 * g.w4 && 16 * k < E; k += 32) {
+        const uint32_t w = m[k];
+        for (uint32_t dn = ~w & ~(w >> 1) & 0x55555555u; dn; dn &= dn - 1) {
+            const int e = 16 * k + ((__ffs(dn) - 1) >> 1);
+            if (e >= E) break;
+            const uint32_t hh = v.ehead[e];
+            atomicOr(&H[(hh & 0xffffu) >> 5], 1u << (hh & 31u));
+            if ((hh >> 16) != 0xffffu) atomicOr(&H[(hh >> 16) >> 5], 1u << ((hh >> 16) & 31u));
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        VIS[src >> 5] = 1u << (src & 31);
+        F[src >> 5] = 1u << (src & 31);
+        cur[0] = (uint32_t)src;
+        lvl[src] = 0;
+    }
+    __syncwarp();
+    const int nwp = nwd <= 1 ? 1 : nwd <= 2 ? 2 : nwd <= 4 ? 4 : 8;
+    const int k = lane & (nwp - 1), part = lane / nwp, parts = 32 / nwp;
+    int f = 1;
+    bool found = (src == dst);
+    for (int level = 0; !found && f > 0 && level < n; ++level) {
+        uint32_t acc = 0u;
+        if (k < nwd)
+            for (int i = part; i < f; i += parts) acc |= v.rows[cur[i] * nwd + k];
+        for (int off = nwp; off < 32; off <<= 1) acc |= __shfl_xor_sync(NR_FULL, acc, off);
+        uint32_t nw = 0u;
+        if (lane < nwd) {
+            nw = acc & ~VIS[lane];
+            for (uint32_t dn = nw & H[lane]; dn; dn &= dn - 1) {
+                const int b = __ffs(dn) - 1;
+                const int w = 32 * lane + b;
+                bool ok = false;
+                for (int j = v.row[w]; j < v.row[w + 1] && !ok; ++j) {
+                    const uint32_t a = v.arc[j];
+                    const uint32_t u = a & HM, e = a >> NR_WIDE_HEAD_BITS;
+                    ok = ((F[u >> 5] >> (u & 31)) & 1u) && ((m[e >> 4] >> ((e & 15) << 1)) & 1u);
+                }
+                if (!ok) nw &= ~(1u << b);
+            }
+        }
+        __syncwarp();                               // the checks above read F
+        if (lane < nwd) {
+            VIS[lane] |= nw;
+            F[lane] = nw;
+        }
+        const int c = __popc(nw);                   // 0 on lanes >= nwd
+        int pre = c;
+#pragma unroll
+        for (int off = 1; off < 8; off <<= 1) {
+            const int t = __shfl_up_sync(NR_FULL, pre, off);
+            if (lane >= off) pre += t;
+        }
+        f = __shfl_sync(NR_FULL, pre, 7);
+        if (lane < nwd) {
+            int o = pre - c;
+            for (uint32_t b = nw; b; b &= b - 1) {
+                const int w = 32 * lane + __ffs(b) - 1;
+                nxt[o++] = (uint32_t)w;
+                lvl[w] = (uint8_t)(level + 1);
+            }
+        }
+        found = (__shfl_sync(NR_FULL, nw, dst >> 5) >> (dst & 31)) & 1u;
+        uint32_t *t = cur;
+        cur = nxt;
+        nxt = t;
+        __syncwarp();
+    }
+    return found;
+}
+
+// Path of a bitset search, dst back to src: the parent of x is the smallest
+// (u << 16 | edge) over x's in-arcs from level lvl[x] - 1 whose edge is not
+// down -- the parent rule of the other searches, evaluated on the path only.
+// Writes hops[0..L) dst side first and returns L on every lane.
+__device__ __forceinline__ int nr_wide_path_bits(const NrWideGraph &g, const NrWideView &v, uint32_t *hops)
+{
+    constexpr uint32_t HM = (1u << NR_WIDE_HEAD_BITS) - 1u;
+    const int lane = threadIdx.x & 31;
+    const uint8_t *lvl = reinterpret_cast<const uint8_t *>(v.par);
+    const uint32_t *VIS = v.VIS, *m = v.m;
+    int x = g.dst, h = 0;
+    while (x != g.src && h < g.n) {
+        const int want = (int)lvl[x] - 1;
+        uint32_t best = 0xffffffffu;
+        for (int j = v.row[x] + lane; j < v.row[x + 1]; j += 32) {
+            const uint32_t a = v.arc[j];
+            const uint32_t u = a & HM, e = a >> NR_WIDE_HEAD_BITS;
+            if (((VIS[u >> 5] >> (u & 31)) & 1u) && (int)lvl[u] == want && ((m[e >> 4] >> ((e & 15) << 1)) & 1u))
+                best = min(best, (u << 16) | e);
+        }
+        best = __reduce_min_sync(NR_FULL, best);
+        if (best == 0xffffffffu) break;             // not reached: x came from level lvl[x] - 1
+        if (lane == 0) hops[h] = best & 0xffffu;
+        ++h;
+        x = (int)(best >> 16);
+    }
+    __syncwarp();
+    return h;
 }
 
 // BFS of the warp from src over the arcs whose edge is not down (up_only:
@@ -453,14 +586,17 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
         return;
     }
     int no = 0;
-    const bool found = nr_wide_bfs(g, v, false, g.nk ? &no : nullptr);
+    const bool found = g.bitset ? nr_wide_bfs_bits(g, v) : nr_wide_bfs(g, v, false, g.nk ? &no : nullptr);
     int L = 0;
     if (!found) {
         if (lane == 0) A.dead++;
         __syncwarp();
         return;
     }
-    if (lane == 0) {
+    if (g.bitset) {
+        L = nr_wide_path_bits(g, v, hops);
+        if (lane == 0 && border != NR_BORDER_SRC && L > 1) nr_wide_branch_order(hops, L, border, v.p);
+    } else if (lane == 0) {
         if (g.nk) {
             // K-terminal: the tree of the terminals' parent paths to src (marked in NF), its
             // edges in visit order, stored last first as the path hops are (dst side first)
