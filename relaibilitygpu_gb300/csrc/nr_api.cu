@@ -180,7 +180,7 @@ size_t small_inst_layout(const nr_graph *g, int src, int dst, NrSmallGraph *sg)
     sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst;
     sg->n_in = g->n_arcs;
     sg->rows = 0;
-    sg->off_rows16 = 0;
+    sg->off_root_rows = 0;
     size_t off = 0;
     sg->off_p = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
     return off;
@@ -194,7 +194,7 @@ size_t small_struct_layout(const nr_graph *g, NrSmallGraph *sg, size_t at)
     sg->off_eid = (int)off; off = align16(off + sizeof(uint16_t) * G * G);
     sg->off_start = (int)off; off = align16(off + sizeof(int) * (n + 1));
     sg->off_list = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
-    sg->off_rows16 = (int)off; off = align16(off + sizeof(uint32_t) * 8);
+    sg->off_root_rows = (int)off; off = align16(off + sizeof(uint32_t) * 32);
     return off - at;
 }
 
@@ -229,15 +229,16 @@ void small_fill_struct(const nr_graph *g, const NrSmallGraph *sg, unsigned char 
             list[start[v] + fill[v]++] = ((uint32_t)e << 8) | (uint32_t)u;
             if (eid[u * G + v] == 0xffff) eid[u * G + v] = (uint16_t)e;   // first arc u->v in CSR order
         }
-    // n <= 16: the rows of the lane kernel's root when no edge is certainly down
-    uint32_t *rows16 = reinterpret_cast<uint32_t *>(b + sg->off_rows16);
-    for (int k = 0; k < 8; ++k) rows16[k] = 0u;
-    if (n <= 16)
-        for (int u = 0; u < n; ++u)
-            for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
-                const int v = g->col_idx[j];
-                rows16[v >> 1] |= 1u << (u + ((v & 1) << 4));
-            }
+    // the rows of a lane kernel's root when no edge is certainly down: n <= 16, 16-bit rows two
+    // to a word; n <= 32, one 32-bit row a word
+    uint32_t *rr = reinterpret_cast<uint32_t *>(b + sg->off_root_rows);
+    for (int k = 0; k < 32; ++k) rr[k] = 0u;
+    for (int u = 0; u < n && n <= 32; ++u)
+        for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
+            const int v = g->col_idx[j];
+            if (n <= 16) rr[v >> 1] |= 1u << (u + ((v & 1) << 4));
+            else rr[v] |= 1u << u;
+        }
 }
 
 // Both parts in one blob (whole-GPU engine): struct_off == blob_off.
@@ -534,7 +535,6 @@ static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg
     wg->nwd = (n + 31) / 32;
     size_t off = 0;
     wg->off_p = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
-    wg->off_q = (int)off; off = align16(off + sizeof(double) * std::max(E, 1));
     wg->off_row = (int)off; off = align16(off + sizeof(int) * (n + 1));
     wg->off_arc = (int)off; off = align16(off + sizeof(uint32_t) * std::max(g->n_arcs, 1));
     wg->off_kmask = (int)off; off = align16(off + sizeof(uint32_t) * wg->nwd);
@@ -555,10 +555,9 @@ static void build_wide_blob(const nr_graph *g, int src, int dst, NrWideGraph *wg
         wg->nk++;
     }
     double *p = reinterpret_cast<double *>(blob->data() + wg->off_p);
-    double *q = reinterpret_cast<double *>(blob->data() + wg->off_q);
     int *row = reinterpret_cast<int *>(blob->data() + wg->off_row);
     uint32_t *arc = reinterpret_cast<uint32_t *>(blob->data() + wg->off_arc);
-    for (int e = 0; e < E; ++e) { p[e] = g->edge_p[e]; q[e] = 1.0 - g->edge_p[e]; }
+    for (int e = 0; e < E; ++e) p[e] = g->edge_p[e];
     if (wg->bitset) {
         // in-arcs (eid << 14 | tail) grouped by head, out-neighbour rows, heads of each edge
         uint32_t *rows = reinterpret_cast<uint32_t *>(blob->data() + wg->off_rows);

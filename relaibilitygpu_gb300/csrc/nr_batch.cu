@@ -125,6 +125,18 @@ static int wait_for_caller(nr_context *c, cudaStream_t s, cudaStream_t after)
     return NR_OK;
 }
 
+// Kernel class of an instance: one lane per subproblem on undirected simple graphs (rows mode
+// 1) of <= 16 nodes, and of <= 32 nodes in the two-slot kernel for breadth-first waves; else
+// the lane-group kernel of its group width (8, 16, 32).  Each class is x the mask blocks.
+static int small_class(const WarpRunCfg &cfg, bool lane_ok, int n, int rows, int w4)
+{
+    if (lane_ok && rows == 1 && n <= NR_LANE_MAX_N && w4 <= NR_LANE_MAX_W4) return NR_LANE_CLS0 + w4 - 1;
+    if (lane_ok && rows == 1 && cfg.lane2 && cfg.lane_slots == 2 && n <= 32 && w4 <= NR_LANE32_MAX_W4)
+        return NR_LANE32_CLS0 + w4 - 1;
+    const int G = group_width(n);
+    return (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + w4 - 1;
+}
+
 // Build the tables of instances [0, n) of gs on the host and queue their
 // upload, the kernels and the read-back of the outputs on slot `sl`.  `base`
 // is the index of gs[0] in the caller's batch (for collected children).
@@ -169,10 +181,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         const size_t sb = small_struct_layout(&gs[0], &t, 0);
         t.rows = rows_mode_of(&gs[0]);
         if (t.w4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
-        const int G = group_width(gs[0].n_nodes);
-        const int cls = (lane_ok && gs[0].n_nodes <= NR_LANE_MAX_N && t.rows == 1 && t.w4 <= NR_LANE_MAX_W4)
-                            ? NR_LANE_CLS0 + t.w4 - 1
-                            : (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + t.w4 - 1;
+        const int cls = small_class(cfg, lane_ok, gs[0].n_nodes, t.rows, t.w4);
         size_t off = align16(sizeof(int) * (NCLS + 1));   // work counters, then a NaN flag
         const size_t tbase = off;
         // matrix batches: the structural part, then the caller's matrix as it is (row i =
@@ -266,7 +275,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
             size_t sb = 0;                    // offsets relative to struct_off
             if (same && i > i0) {
                 desc[i].off_eid = desc[i - 1].off_eid; desc[i].off_start = desc[i - 1].off_start;
-                desc[i].off_list = desc[i - 1].off_list; desc[i].off_rows16 = desc[i - 1].off_rows16;
+                desc[i].off_list = desc[i - 1].off_list; desc[i].off_root_rows = desc[i - 1].off_root_rows;
             } else {
                 sb = small_struct_layout(&gs[i], &desc[i], 0);
             }
@@ -284,11 +293,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
                 cur_rows = rows_mode_of(&gs[i]);   // its owner is in an earlier block
             }
             if (desc[i].w4 > NR_MAX_W4) { too_wide.store(1); S.cls[i] = 0; continue; }
-            const int G = group_width(gs[i].n_nodes);
-            if (lane_ok && gs[i].n_nodes <= NR_LANE_MAX_N && cur_rows == 1 && desc[i].w4 <= NR_LANE_MAX_W4)
-                S.cls[i] = NR_LANE_CLS0 + desc[i].w4 - 1;
-            else
-                S.cls[i] = (G == 8 ? 0 : G == 16 ? 1 : 2) * NR_MAX_W4 + desc[i].w4 - 1;
+            S.cls[i] = small_class(cfg, lane_ok, gs[i].n_nodes, cur_rows, desc[i].w4);
             k.cnt[S.cls[i]]++;
         }
         k.bytes = rel;
@@ -375,36 +380,47 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
                     nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots)) * warps_pb > (size_t)c->smem_optin)
         cfgp.pages /= 2;
     const bool learn = cfg.learned || cfg.dump || cfg.border == NR_BORDER_LEARNED;
-    int grids[NCLS] = {0};
+    int grids[NCLS] = {0}, wpbs[NCLS] = {0}, nps[NCLS] = {0};
     size_t smems[NCLS] = {0};
     size_t slab_need = 0;
     for (int j = 0; j < NCLS; ++j) {
         if (!class_count[j]) continue;
-        const bool lanek = j >= NR_LANE_CLS0;
+        const bool lanek = j >= NR_LANE_CLS0, lane32 = j >= NR_LANE32_CLS0;
         const int G = lanek ? 0 : 8 << (j / NR_MAX_W4);
-        const int W4 = lanek ? j - NR_LANE_CLS0 + 1 : j % NR_MAX_W4 + 1;
+        const int W4 = lane32 ? j - NR_LANE32_CLS0 + 1 : lanek ? j - NR_LANE_CLS0 + 1 : j % NR_MAX_W4 + 1;
         const bool two = lanek && cfg.lane2;
-        const void *kfn = lanek ? (two ? nr_lane2_kernel_ptr(W4, cfg.lane_slots) : nr_lane_kernel_ptr(W4))
+        const int slots = lane32 ? 2 : cfg.lane_slots, rb = lane32 ? 32 : 16;
+        // the 32-bit-row kernel's warps hold a pool of two slots' worth: each slot (instance) gets
+        // the pages one instance has in the lane-group kernel it stands in for; its blocks have as
+        // many of the asked warps as their shared memory holds
+        int np = lane32 ? 2 * cfgp.pages : cfgp.pages, wpb = warps_pb;
+        if (lane32) {
+            while (wpb > 1 && nr_lane2_shm_bytes(np, 2, 32) * wpb > (size_t)c->smem_optin) --wpb;
+            while (np > 8 && nr_lane2_shm_bytes(np, 2, 32) > (size_t)c->smem_optin) np /= 2;
+        }
+        const void *kfn = lanek ? (two ? nr_lane2_kernel_ptr(W4, slots, rb) : nr_lane_kernel_ptr(W4))
                                 : warp_kernel(G, W4, learn, cfg.fork != 0);
         if (!kfn) return NR_ERR_UNSUPPORTED;
-        const size_t smem = (two ? nr_lane2_shm_bytes(cfgp.pages, cfg.lane_slots)
+        const size_t smem = (two ? nr_lane2_shm_bytes(np, slots, rb)
                                  : lanek ? nr_lane_shm_bytes(cfg.n_buckets, cfgp.pages)
-                                         : nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn)) * warps_pb;
-        auto it = c->occupancy.find({kfn, smem * 64 + warps_pb});
+                                         : nr_warp_shm_bytes(32 / G, W4, cfg.n_buckets, cfgp.pages, learn)) * wpb;
+        auto it = c->occupancy.find({kfn, smem * 64 + wpb});
         int bps;
         if (it == c->occupancy.end()) {
             NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
-            NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
-            c->occupancy[{kfn, smem * 64 + warps_pb}] = bps;
+            NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, 32 * wpb, smem));
+            c->occupancy[{kfn, smem * 64 + wpb}] = bps;
         } else {
             bps = it->second;
         }
         if (bps < 1) return NR_ERR_UNSUPPORTED;
-        const int per_block = warps_pb * (two ? cfg.lane_slots : 1);   // instances a block starts with
+        const int per_block = wpb * (two ? slots : 1);   // instances a block starts with
         grids[j] = std::max(1, std::min(bps * c->sms, (class_count[j] + per_block - 1) / per_block));
         smems[j] = smem;
-        const size_t row_bytes = lanek ? 4 * (size_t)NR_LANE_ROW_WORDS : 4 * (size_t)G;
-        slab_need = std::max(slab_need, (size_t)grids[j] * warps_pb * cfgp.pages * NR_PAGE *
+        wpbs[j] = wpb;
+        nps[j] = np;
+        const size_t row_bytes = lane32 ? 128 : lanek ? 4 * (size_t)NR_LANE_ROW_WORDS : 4 * (size_t)G;
+        slab_need = std::max(slab_need, (size_t)grids[j] * wpb * np * NR_PAGE *
                                             (16 * (size_t)W4 + 8 + row_bytes));
     }
     rc = ensure(&sl.wslab, &sl.wslab_bytes, slab_need);
@@ -425,10 +441,11 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     int first_grid = 0;
     for (int j = 0; j < NCLS; ++j) {
         if (!class_count[j]) continue;
-        const bool lanek = j >= NR_LANE_CLS0;
+        const bool lanek = j >= NR_LANE_CLS0, lane32 = j >= NR_LANE32_CLS0;
         const int G = lanek ? 0 : 8 << (j / NR_MAX_W4);
-        const int W4 = lanek ? j - NR_LANE_CLS0 + 1 : j % NR_MAX_W4 + 1;
+        const int W4 = lane32 ? j - NR_LANE32_CLS0 + 1 : lanek ? j - NR_LANE_CLS0 + 1 : j % NR_MAX_W4 + 1;
         if (!first_grid) first_grid = grids[j];
+        const int np = nps[j], wpb = wpbs[j];     // pages a warp holds, warps a block (see above)
         NrWarpParams P;
         P.blob = wb;
         P.inst = reinterpret_cast<const NrSmallGraph *>(wb + off_desc) + class_begin[j];
@@ -436,12 +453,12 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.n_inst = class_count[j];
         P.next_inst = reinterpret_cast<int *>(wb + off_cnt) + j;
         P.slab_mask = static_cast<uint4 *>(sl.wslab);
-        const size_t warps = (size_t)grids[j] * warps_pb;
+        const size_t warps = (size_t)grids[j] * wpb;
         P.slab_mass = reinterpret_cast<double *>(static_cast<unsigned char *>(sl.wslab) +
-                                                 warps * cfgp.pages * NR_PAGE * 16 * (size_t)W4);
+                                                 warps * np * NR_PAGE * 16 * (size_t)W4);
         P.slab_rows = reinterpret_cast<uint32_t *>(static_cast<unsigned char *>(sl.wslab) +
-                                                   warps * cfgp.pages * NR_PAGE * (16 * (size_t)W4 + 8));
-        P.pages = cfgp.pages;
+                                                   warps * np * NR_PAGE * (16 * (size_t)W4 + 8));
+        P.pages = np;
         P.n_buckets = cfg.n_buckets;
         P.shift = cfg.shift;
         P.wave_mode = cfg.wave_mode;
@@ -464,11 +481,12 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.fork = cfg.fork;
         P.step_cap = cfg.step_cap;
         P.border = cfg.border;
-        const void *kfn = lanek ? (cfg.lane2 ? nr_lane2_kernel_ptr(W4, cfg.lane_slots) : nr_lane_kernel_ptr(W4))
+        const void *kfn = lanek ? (cfg.lane2 ? nr_lane2_kernel_ptr(W4, lane32 ? 2 : cfg.lane_slots, lane32 ? 32 : 16)
+                                             : nr_lane_kernel_ptr(W4))
                                 : warp_kernel(G, W4, learn, cfg.fork != 0);
         void *args[] = {&P};
         NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smems[j]));
-        NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[j]), dim3(block), args, smems[j], s));
+        NR_CUDA_TRY(cudaLaunchKernel(kfn, dim3(grids[j]), dim3(32 * wpb), args, smems[j], s));
     }
     NR_CUDA_TRY(cudaEventRecord(sl.ev1, s));
     NrWarpOut *hout = reinterpret_cast<NrWarpOut *>(hb + off_out);

@@ -48,7 +48,7 @@ const void *nr_warp_fork_kernel_ptr_g32(int w4);
 const void *nr_warp_learn_kernel_ptr_g16(int w4);
 const void *nr_warp_learn_kernel_ptr_g32(int w4);
 const void *nr_lane_kernel_ptr(int w4);
-const void *nr_lane2_kernel_ptr(int w4, int slots);
+const void *nr_lane2_kernel_ptr(int w4, int slots, int row_bits = 16);
 int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
 
 #define NR_CUDA_TRY(call)                                                     \
@@ -132,7 +132,10 @@ struct PhaseClock {
 // warp-engine kernel classes: lane-group width (8, 16, 32) x mask blocks, then the
 // one-lane-per-subproblem kernel x mask blocks
 #define NR_LANE_CLS0 (3 * NR_MAX_W4)
-#define NR_NCLS (NR_LANE_CLS0 + NR_LANE_MAX_W4)
+// then the two-slot lane kernel with 32-bit rows (17..32 nodes) x mask blocks
+#define NR_LANE32_MAX_W4 8      // a simple graph on <= 32 nodes has <= 496 edges: 31 mask words
+#define NR_LANE32_CLS0 (NR_LANE_CLS0 + NR_LANE_MAX_W4)
+#define NR_NCLS (NR_LANE32_CLS0 + NR_LANE32_MAX_W4)
 struct NrHostBlock {
     size_t bytes;               // tables of the block's instances (16-byte multiples)
     long long last_owner_rel;   // offset in the block of its last structural part, -1 if none

@@ -48,8 +48,9 @@ struct NrSmallGraph {
     int off_p, off_eid, off_start, off_list, blob_bytes;
     int rows;                   // rows carried in queue records: 0 no (rebuilt from the mask),
                                 // 1 undirected simple graph, 2 directed simple graph
-    int off_rows16;             // n <= 16: every node's in-neighbour row (all arcs), 16 bits each,
-                                // two to a word (structural part; 0 when absent)
+    int off_root_rows;          // every node's in-neighbour row (all arcs) for the lane kernels'
+                                // roots: n <= 16, 16 bits each, two to a word; n <= 32, one a
+                                // word (32 words; structural part; 0 when absent)
     long long blob_off;
     long long struct_off;
 };

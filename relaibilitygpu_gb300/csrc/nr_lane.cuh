@@ -36,12 +36,30 @@
 #define NR_LANE_STEP_CAP (1ll << 26)   // steps (pages) per instance: 2^31 subproblems
 #define NR_LANE_STATUS_CHECK NR_WARP_STATUS_CHECK
 
-// A path hop in a lane kernel's hop column: edge id (bits 0-6: a lane-kernel graph has <= 128
-// edges), its nodes u (bits 7-10) and x (bits 11-14); a p-ordered branch order puts the edge's
-// sort key in bits 16-31.
-#define NR_HOP_E(h) ((int)((h) & 0x7fu))
-#define NR_HOP_U(h) ((int)(((h) >> 7) & 0xfu))
-#define NR_HOP_X(h) ((int)(((h) >> 11) & 0xfu))
+// A path hop in a lane kernel's hop column.  Rows of RB bits (RB = 16: graphs of <= 16 nodes,
+// <= 120 edges; RB = 32: <= 32 nodes, <= 496 edges): edge id (EB bits), its nodes u and x (NB
+// bits each), and above bit KS a p-ordered branch order's sort key (16 or 13 bits).
+template <int RB> struct NrHop;
+template <> struct NrHop<16> { static constexpr int EB = 7, NB = 4, KS = 16; };
+template <> struct NrHop<32> { static constexpr int EB = 9, NB = 5, KS = 19; };
+template <int RB> __device__ __forceinline__ int nr_hop_e(uint32_t h) { return (int)(h & ((1u << NrHop<RB>::EB) - 1u)); }
+template <int RB> __device__ __forceinline__ int nr_hop_u(uint32_t h)
+{
+    return (int)((h >> NrHop<RB>::EB) & ((1u << NrHop<RB>::NB) - 1u));
+}
+template <int RB> __device__ __forceinline__ int nr_hop_x(uint32_t h)
+{
+    return (int)((h >> (NrHop<RB>::EB + NrHop<RB>::NB)) & ((1u << NrHop<RB>::NB) - 1u));
+}
+template <int RB> __device__ __forceinline__ uint32_t nr_hop_make(uint32_t e, uint32_t u, uint32_t x)
+{
+    return e | (u << NrHop<RB>::EB) | (x << (NrHop<RB>::EB + NrHop<RB>::NB));
+}
+#define NR_HOP_E(h) nr_hop_e<16>(h)
+#define NR_HOP_U(h) nr_hop_u<16>(h)
+#define NR_HOP_X(h) nr_hop_x<16>(h)
+// row words of a lane's rows: 16-bit rows two to a word, 32-bit rows one a word
+template <int RB> __host__ __device__ constexpr int nr_lane_rw() { return RB == 16 ? 8 : 32; }
 
 // shared memory of one warp
 __host__ __device__ inline size_t nr_lane_shm_bytes(int n_buckets, int pages)
@@ -59,10 +77,12 @@ __host__ __device__ inline size_t nr_lane_shm_bytes(int n_buckets, int pages)
     return (b + 15) & ~size_t(15);
 }
 
-// row of node u (its not-down neighbours) from the lane's packed rows in shared memory
+// row of node u (its not-down neighbours) from the lane's rows in shared memory
+template <int RB = 16>
 __device__ __forceinline__ uint32_t nr_lane_row(const uint32_t *my_rows, int u)
 {
-    return (my_rows[(u >> 1) * 32] >> ((u & 1) << 4)) & 0xffffu;
+    if constexpr (RB == 16) return (my_rows[(u >> 1) * 32] >> ((u & 1) << 4)) & 0xffffu;
+    else return my_rows[u * 32];
 }
 
 template <int N>
@@ -106,7 +126,7 @@ __device__ __forceinline__ void nr_lane_root(const NrSmallGraph &g, const unsign
     }
     uint32_t *rr = reinterpret_cast<uint32_t *>(sl_rows + (size_t)rpg * NR_PAGE * (RW / 4));
     if (!__any_sync(NR_FULL, down)) {
-        if (lane < RW) rr[lane] = reinterpret_cast<const uint32_t *>(gs + g.off_rows16)[lane];
+        if (lane < RW) rr[lane] = reinterpret_cast<const uint32_t *>(gs + g.off_root_rows)[lane];
     } else {
         const int *start = reinterpret_cast<const int *>(gs + g.off_start);
         const uint32_t *list = reinterpret_cast<const uint32_t *>(gs + g.off_list);
@@ -128,26 +148,26 @@ __device__ __forceinline__ void nr_lane_root(const NrSmallGraph &g, const unsign
 // of frontier l adjacent to it; hop l = (u, x) with its edge id replaces frontier l).  Returns
 // the hops L (0 for a dead end or an inactive lane); live = dst reached; nch = the UNKNOWN hops,
 // i.e. the lane's children; bad = a failed internal check (2 levels, 3 parent, 4 edge id).
-template <int NW>
+template <int NW, int RB = 16>
 __device__ __forceinline__ int nr_lane_path(const uint32_t *my_rows, uint32_t *my_hop, const uint32_t (&wc)[NW],
                                             const uint16_t *eid, int n, int ge, int src, int dst, bool active,
                                             bool &live, int &nch, int &bad)
 {
-    const int es = n <= 8 ? 8 : 16;                 // edge-id table stride (the host's group width)
+    const int es = n <= 8 ? 8 : n <= 16 ? 16 : 32;  // edge-id table stride (the host's group width)
     int L = 0;
     live = false;
     nch = 0;
     bad = 0;
     if (!active) return 0;
     if (src == dst) { live = true; return 0; }
-    const uint32_t rd = nr_lane_row(my_rows, dst);
+    const uint32_t rd = nr_lane_row<RB>(my_rows, dst);
     uint32_t F = 1u << src, vis = F;
     for (;;) {                                      // every level adds a node: at most n - 1 levels
-        if (L >= NR_LANE_MAX_N) { bad = 2; return 0; }
+        if (L >= RB) { bad = 2; return 0; }
         my_hop[32 * L] = F;
         if (rd & F) { ++L; live = true; break; }    // dst is on the next level
         uint32_t nf = 0u;
-        for (uint32_t t = F; t; t &= t - 1u) nf |= nr_lane_row(my_rows, __ffs(t) - 1);
+        for (uint32_t t = F; t; t &= t - 1u) nf |= nr_lane_row<RB>(my_rows, __ffs(t) - 1);
         nf &= ~vis;
         if (!nf) return 0;                          // a dead end has no path: no hops, no children
         vis |= nf;
@@ -156,31 +176,36 @@ __device__ __forceinline__ int nr_lane_path(const uint32_t *my_rows, uint32_t *m
     }
     int x = dst;
     for (int l = L - 1; l >= 0; --l) {
-        const int u = __ffs(nr_lane_row(my_rows, x) & my_hop[32 * l]) - 1;
+        const int u = __ffs(nr_lane_row<RB>(my_rows, x) & my_hop[32 * l]) - 1;
         if (u < 0 || u >= n) { bad = 3; return 0; }
         const uint32_t e = eid[u * es + x];
-        if ((int)e >= ge || e > 0x7fu) { bad = 4; return 0; }
-        my_hop[32 * l] = e | ((uint32_t)u << 7) | ((uint32_t)x << 11);
+        if ((int)e >= ge || e >= (1u << NrHop<RB>::EB)) { bad = 4; return 0; }
+        my_hop[32 * l] = nr_hop_make<RB>(e, (uint32_t)u, (uint32_t)x);
         nch += ((nr_pick(wc, (int)e >> 4) >> ((e & 15) << 1)) & 3u) == 3u;
         x = u;
     }
     return L;
 }
 
-// A 16-bit sort key non-decreasing in p: the top bits of p's bit pattern (positive doubles
-// order as their bit patterns do), saturated; p <= 0 gives 0.  Equal keys compare p itself.
-__device__ __forceinline__ uint32_t nr_p_key16(double p)
+// A sort key non-decreasing in p, in the hop word's key bits (16 or 13): the top bits of p's bit
+// pattern (positive doubles order as their bit patterns do), saturated; p <= 0 gives 0.  Equal
+// keys compare p itself.
+template <int RB = 16>
+__device__ __forceinline__ uint32_t nr_p_key(double p)
 {
+    constexpr int KB = 32 - NrHop<RB>::KS;
     const long long b = __double_as_longlong(p);
-    return b <= 0 ? 0u : (uint32_t)min((unsigned long long)b >> 38, 0xffffull);
+    return b <= 0 ? 0u : (uint32_t)min((unsigned long long)b >> (54 - KB), (1ull << KB) - 1ull);
 }
 
 // Branch order of one lane's path hops my_hop[32 l], l = 0..L-1 src side first: dst side
 // first (reversed), or by p (ascending / descending, stable in path order -- the oracle's
 // insertion sort of the src -> dst path).  Known hops move too but make no child, so only
 // the UNKNOWN hops' relative order matters.  The sort keys ride in the hop words' top bits.
+template <int RB = 16>
 __device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, int L, int border, const double *pt)
 {
+    constexpr int KS = NrHop<RB>::KS;
     if (border == NR_BORDER_DST) {
         for (int i = 0, j = L - 1; i < j; ++i, --j) {
             const uint32_t t = my_hop[32 * i];
@@ -192,18 +217,18 @@ __device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, int L, in
     const bool desc = (border == NR_BORDER_P_DESC);
     for (int i = 0; i < L; ++i) {
         const uint32_t h = my_hop[32 * i];
-        my_hop[32 * i] = (h & 0xffffu) | (nr_p_key16(pt[NR_HOP_E(h)]) << 16);
+        my_hop[32 * i] = (h & ((1u << KS) - 1u)) | (nr_p_key<RB>(pt[nr_hop_e<RB>(h)]) << KS);
     }
     for (int i = 1; i < L; ++i) {
         const uint32_t hp = my_hop[32 * i];
-        const uint32_t ke = hp >> 16;
+        const uint32_t ke = hp >> KS;
         int j = i - 1;
         while (j >= 0) {
             const uint32_t hj = my_hop[32 * j];
-            const uint32_t kj = hj >> 16;
+            const uint32_t kj = hj >> KS;
             bool after = desc ? kj < ke : kj > ke;          // j moves past i: strictly out of order
             if (kj == ke) {
-                const double pj = pt[NR_HOP_E(hj)], pe = pt[NR_HOP_E(hp)];
+                const double pj = pt[nr_hop_e<RB>(hj)], pe = pt[nr_hop_e<RB>(hp)];
                 after = desc ? pj < pe : pj > pe;
             }
             if (!after) break;
@@ -216,7 +241,32 @@ __device__ __forceinline__ void nr_lane_branch_order(uint32_t *my_hop, int L, in
 
 // Child record at slot s: the parent's mask blocks, then the one word that differs (hop edge e
 // down; this thread's later store to the same address wins); the parent's rows less the down
-// edge cu - cv; mass cm.  wv = the parent's (current) mask word of e.
+// edge cu - cv; mass cm.  wv = the parent's (current) mask word of e.  32-bit rows
+// (nr_lane_write_child32) are copied from the lane's shared-memory column, not registers.
+template <int W4>
+__device__ __forceinline__ void nr_lane_write_child32(uint4 *sl_mask, uint4 *sl_rows, double *sl_mass, int s,
+                                                      const uint32_t (&wc)[4 * W4], const uint32_t *my_rows, int e,
+                                                      uint32_t wv, int cu, int cv, double cm)
+{
+    uint4 *d = sl_mask + (size_t)s * W4;
+#pragma unroll
+    for (int kk = 0; kk < W4; ++kk)
+        d[kk] = make_uint4(wc[4 * kk], wc[4 * kk + 1], wc[4 * kk + 2], wc[4 * kk + 3]);
+    reinterpret_cast<uint32_t *>(d)[e >> 4] = wv & ~(3u << ((e & 15) << 1));
+    uint4 *dr = sl_rows + (size_t)s * 8;
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+        uint32_t r[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int u = 4 * kk + i;
+            r[i] = my_rows[32 * u] & ~(u == cu ? 1u << cv : 0u) & ~(u == cv ? 1u << cu : 0u);
+        }
+        dr[kk] = make_uint4(r[0], r[1], r[2], r[3]);
+    }
+    sl_mass[s] = cm;
+}
+
 template <int W4>
 __device__ __forceinline__ void nr_lane_write_child(uint4 *sl_mask, uint4 *sl_rows, double *sl_mass, int s,
                                                     const uint32_t (&wc)[4 * W4],

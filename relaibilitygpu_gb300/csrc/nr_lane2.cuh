@@ -1,5 +1,7 @@
 // nr_lane2.cuh -- the lane kernel with several instances per warp (NS = 2 or 4), for
-// breadth-first waves (one bucket) on undirected simple graphs of up to 16 nodes.
+// breadth-first waves (one bucket) on undirected simple graphs of up to 16 nodes (16-bit
+// rows, RB = 16), or up to 32 nodes with 32-bit rows (RB = 32: 128 B of rows a record, two
+// slots a warp).
 //
 // nr_lane_kernel gives a warp one instance, and the first waves of an instance hold
 // 1, 1, 2, 4, ... records: most lanes idle while every step pays its full fixed work,
@@ -28,17 +30,17 @@ struct NrLaneSlot {
     int pad[3];             // 64 bytes
 };
 
-// a slot's copy of its instance's tables: p (simple graphs on <= 16 nodes: <= 120 edges) and
-// the edge-id table (n <= 8: 8 x 8 ids, else 16 x 16)
-#define NR_LANE2_MAX_E 128
-#define NR_LANE2_TAB_BYTES (NR_LANE2_MAX_E * 8 + NR_LANE_MAX_N * NR_LANE_MAX_N * 2)
+// a slot's copy of its instance's tables: p (simple graphs on <= 16 nodes: <= 120 edges; on
+// <= 32 nodes: <= 496) and the edge-id table (n <= 8: 8 x 8 ids, n <= 16: 16 x 16, else 32 x 32)
+__host__ __device__ constexpr int nr_lane2_max_e(int rb) { return rb == 16 ? 128 : 512; }
+__host__ __device__ constexpr int nr_lane2_tab_bytes(int rb) { return nr_lane2_max_e(rb) * 8 + rb * rb * 2; }
 
-__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots)
+__host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots, int rb = 16)
 {
     size_t b = (size_t)slots * 32 * sizeof(NrLaneAcc);       // per slot, per lane sums
-    b += (size_t)(NR_LANE_ROW_WORDS + NR_LANE_MAX_N) * 32 * 4;  // rows, hops, [word][lane]
+    b += (size_t)((rb == 16 ? 8 : 32) + rb) * 32 * 4;        // rows, hops, [word][lane]
     b += (size_t)slots * 32 * 4;                             // per slot, per lane: queued-mass lower bound (units)
-    b += (size_t)slots * NR_LANE2_TAB_BYTES;                 // per slot: p and edge ids
+    b += (size_t)slots * nr_lane2_tab_bytes(rb);             // per slot: p and edge ids
     b += (size_t)slots * sizeof(NrLaneSlot);
     b += (size_t)pages * 2;                                  // pnext
     b += (size_t)pages;                                      // pcnt
@@ -51,11 +53,11 @@ __host__ __device__ inline size_t nr_lane2_shm_bytes(int pages, int slots)
 // the slot's copy of p (tp, shared memory) and the topology's rows (r16: word `lane` of the
 // table, preloaded).  Edge states come from p's bit pattern (p <= 0 down, p >= 1 up), with
 // integer compares; each 16-edge mask word is one OR reduction over half the lanes' bits.
-template <int W4>
+template <int W4, int RB = 16>
 __device__ __forceinline__ void nr_lane2_root(const NrSmallGraph &g, const unsigned char *gs, const double *tp,
                                               uint32_t r16, uint4 *sl_mask, uint4 *sl_rows, double *sl_mass, int rpg)
 {
-    constexpr int RW = NR_LANE_ROW_WORDS;
+    constexpr int RW = nr_lane_rw<RB>();
     const int lane = threadIdx.x & 31;
     uint32_t *rw = reinterpret_cast<uint32_t *>(sl_mask + (size_t)rpg * NR_PAGE * W4);
     bool down = false;
@@ -85,8 +87,12 @@ __device__ __forceinline__ void nr_lane2_root(const NrSmallGraph &g, const unsig
                 const uint32_t a = list[j];
                 if (__double_as_longlong(tp[a >> 8]) > 0ll) r |= 1u << (a & 31u);
             }
-        const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
-        if (lane < 2 * RW && !(lane & 1)) rr[lane >> 1] = r | (hi << 16);
+        if constexpr (RB == 16) {
+            const uint32_t hi = __shfl_down_sync(NR_FULL, r, 1);
+            if (lane < 2 * RW && !(lane & 1)) rr[lane >> 1] = r | (hi << 16);
+        } else {
+            rr[lane] = r;                     // row `lane`; 0 past the nodes
+        }
     }
     if (lane == 0) sl_mass[(size_t)rpg * NR_PAGE] = 1.0;
 }
@@ -95,24 +101,25 @@ __device__ __forceinline__ void nr_lane2_root(const NrSmallGraph &g, const unsig
 #define NR_LANE2_UNITS (1u << 20)
 #define NR_LANE2_UNIT_CAP (1u << 26)      // a lane's total saturates here: 32 lanes sum below 2^31
 
-template <int W4, int NS>
+template <int W4, int NS, int RB = 16>
 __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpParams P)
 {
     constexpr int NW = 4 * W4;
-    constexpr int RW = NR_LANE_ROW_WORDS;
+    constexpr int RW = nr_lane_rw<RB>();
+    constexpr int TAB = nr_lane2_tab_bytes(RB), MAXE = nr_lane2_max_e(RB);
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int NP = P.pages;
     const int budget = max(1, NP / NS);       // pages one slot may hold
 
-    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP, NS);
+    unsigned char *wbase = smem + (size_t)warp * nr_lane2_shm_bytes(NP, NS, RB);
     NrLaneAcc *accs = reinterpret_cast<NrLaneAcc *>(wbase);                      // [slot * 32 + lane]
     uint32_t *my_rows = reinterpret_cast<uint32_t *>(wbase + NS * 32 * sizeof(NrLaneAcc)) + lane;
     uint32_t *my_hop = my_rows + RW * 32;
     unsigned *qlb = reinterpret_cast<unsigned *>(wbase + NS * 32 * sizeof(NrLaneAcc) +
-                                                 (size_t)(RW + NR_LANE_MAX_N) * 32 * 4);  // [slot * 32 + lane]
+                                                 (size_t)(RW + RB) * 32 * 4);  // [slot * 32 + lane]
     unsigned char *tabs = reinterpret_cast<unsigned char *>(qlb + NS * 32);                       // [slot]
-    NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(tabs + NS * NR_LANE2_TAB_BYTES);
+    NrLaneSlot *slots = reinterpret_cast<NrLaneSlot *>(tabs + NS * TAB);
     short *pnext = reinterpret_cast<short *>(slots + NS);
     unsigned char *pcnt = reinterpret_cast<unsigned char *>(pnext + NP);
     short *freel = reinterpret_cast<short *>(pcnt + ((NP + 1) & ~1));
@@ -210,14 +217,14 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                     if (ii_t[t] < 0) continue;
                     const NrSmallGraph &g = g_t[t];
                     const unsigned char *gs = P.blob + g.struct_off;
-                    double *tp = reinterpret_cast<double *>(tabs + t * NR_LANE2_TAB_BYTES);
-                    uint32_t *te = reinterpret_cast<uint32_t *>(tp + NR_LANE2_MAX_E);
+                    double *tp = reinterpret_cast<double *>(tabs + t * TAB);
+                    uint32_t *te = reinterpret_cast<uint32_t *>(tp + MAXE);
                     const double *gp = reinterpret_cast<const double *>(P.blob + g.blob_off + g.off_p);
                     const uint32_t *gi = reinterpret_cast<const uint32_t *>(gs + g.off_eid);
-                    const int ew = (g.n <= 8 ? 8 : 16) * g.n / 2;   // edge-id words
+                    const int ew = (g.n <= 8 ? 8 : g.n <= 16 ? 16 : 32) * g.n / 2;   // edge-id words
                     for (int e = lane; e < g.e; e += 32) tp[e] = gp[e];
                     for (int k = lane; k < ew; k += 32) te[k] = gi[k];
-                    if (lane < RW) r16[t] = reinterpret_cast<const uint32_t *>(gs + g.off_rows16)[lane];
+                    if (lane < RW) r16[t] = reinterpret_cast<const uint32_t *>(gs + g.off_root_rows)[lane];
                 }
                 __syncwarp();
 #pragma unroll
@@ -236,8 +243,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                         pnext[rpg] = -1;
                         S.head = rpg; S.cur = -1; S.used = 1;
                     }
-                    nr_lane2_root<W4>(g, P.blob + g.struct_off,
-                                      reinterpret_cast<const double *>(tabs + t * NR_LANE2_TAB_BYTES), r16[t],
+                    nr_lane2_root<W4, RB>(g, P.blob + g.struct_off,
+                                          reinterpret_cast<const double *>(tabs + t * TAB), r16[t],
                                       sl_mask, sl_rows, sl_mass, rpg);
                     nr_acc_zero(accs[t * 32 + lane]);
                     qlb[t * 32 + lane] = lane == 0 ? root_units : 0u;   // the root's mass is queued
@@ -341,7 +348,10 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         const bool valid = s >= 0;
         const int sl = valid ? s : 0;
         const size_t slot = (size_t)(valid ? pg : 0) * NR_PAGE + idx;
-        uint32_t wc[NW], rw[RW];
+        // 16-bit rows stay in registers too (the child writes copy them); 32-bit rows go
+        // straight to the lane's shared-memory column
+        constexpr int RWR = RB == 16 ? RW : 1;
+        uint32_t wc[NW], rw[RWR];
         double mass = 0.0;
         if (valid) {
 #pragma unroll
@@ -352,17 +362,28 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
 #pragma unroll
             for (int k = 0; k < RW / 4; ++k) {
                 const uint4 q = sl_rows[slot * (RW / 4) + k];
-                rw[4 * k] = q.x; rw[4 * k + 1] = q.y; rw[4 * k + 2] = q.z; rw[4 * k + 3] = q.w;
+                if constexpr (RB == 16) {
+                    rw[4 * k] = q.x; rw[4 * k + 1] = q.y; rw[4 * k + 2] = q.z; rw[4 * k + 3] = q.w;
+                } else {
+                    my_rows[32 * (4 * k)] = q.x; my_rows[32 * (4 * k + 1)] = q.y;
+                    my_rows[32 * (4 * k + 2)] = q.z; my_rows[32 * (4 * k + 3)] = q.w;
+                }
             }
             mass = sl_mass[slot];
         } else {
 #pragma unroll
             for (int k = 0; k < NW; ++k) wc[k] = 0u;
 #pragma unroll
-            for (int k = 0; k < RW; ++k) rw[k] = 0u;
-        }
+            for (int k = 0; k < RWR; ++k) rw[k] = 0u;
+            if constexpr (RB == 32) {
 #pragma unroll
-        for (int k = 0; k < RW; ++k) my_rows[32 * k] = rw[k];
+                for (int k = 0; k < RW; ++k) my_rows[32 * k] = 0u;
+            }
+        }
+        if constexpr (RB == 16) {
+#pragma unroll
+            for (int k = 0; k < RW; ++k) my_rows[32 * k] = rw[k];
+        }
         __syncwarp();                               // every lane holds its record: the pages are free
         {
             // lane t < NS returns slot t's page to the stack (taken slots in slot order), one body
@@ -386,8 +407,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
 
         // the lane's instance
         const NrLaneSlot &S = slots[sl];
-        const double *pt = reinterpret_cast<const double *>(tabs + sl * NR_LANE2_TAB_BYTES);
-        const uint16_t *eid = reinterpret_cast<const uint16_t *>(pt + NR_LANE2_MAX_E);
+        const double *pt = reinterpret_cast<const double *>(tabs + sl * TAB);
+        const uint16_t *eid = reinterpret_cast<const uint16_t *>(pt + MAXE);
         const int n = S.n, src = S.src, dst = S.dst, ge = S.ge;
         NrLaneAcc &acc = accs[sl * 32 + lane];
 
@@ -402,8 +423,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         }
         bool live;
         int nch, bad;
-        const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
-        if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order(my_hop, L, P.border, pt);
+        const int L = nr_lane_path<NW, RB>(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
+        if (P.border != NR_BORDER_SRC && L > 1) nr_lane_branch_order<RB>(my_hop, L, P.border, pt);
         if (active && !live && !bad) acc.dead++;
         {
             const unsigned bm = __ballot_sync(NR_FULL, bad != 0);
@@ -475,11 +496,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         unsigned qadd = 0u;                         // lower bound of the mass this lane queues, in units
         for (int h = 0; h < L; ++h) {
             const uint32_t hp = my_hop[32 * h];
-            const int e = NR_HOP_E(hp);
+            const int e = nr_hop_e<RB>(hp);
             const int ew = e >> 4;
             const uint32_t wv = nr_pick(wc, ew);
             if (((wv >> ((e & 15) << 1)) & 3u) != 3u) continue;
-            const int cu = NR_HOP_U(hp), cv = NR_HOP_X(hp);
+            const int cu = nr_hop_u<RB>(hp), cv = nr_hop_x<RB>(hp);
             const double pe = pt[e];
             const double cm = __dmul_rn(Pm, __dsub_rn(1.0, pe));
             Pm = __dmul_rn(Pm, pe);
@@ -492,7 +513,10 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             }
             ++q;
             if (sc >= 0) {
-                nr_lane_write_child<W4>(sl_mask, sl_rows, sl_mass, sc, wc, rw, my_rows, e, wv, cu, cv, cm);
+                if constexpr (RB == 16)
+                    nr_lane_write_child<W4>(sl_mask, sl_rows, sl_mass, sc, wc, rw, my_rows, e, wv, cu, cv, cm);
+                else
+                    nr_lane_write_child32<W4>(sl_mask, sl_rows, sl_mass, sc, wc, my_rows, e, wv, cu, cv, cm);
                 qadd += min(__float2uint_rd(__fmul_rd(__double2float_rd(cm), unit_scale)), NR_LANE2_UNIT_CAP);
             } else {                                  // the slot's pages are full: mass to ESP
                 acc.spilled++;

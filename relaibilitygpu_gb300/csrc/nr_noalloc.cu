@@ -79,7 +79,7 @@ size_t noalloc_tables(const nr_graph *g, int src, int dst, int G, NrSmallGraph *
     const int n = g->n_nodes, E = g->n_edges;
     const int W = std::max(1, (2 * E + 31) / 32);
     sg->n = n; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst; sg->n_in = g->n_arcs;
-    sg->rows = 0; sg->off_rows16 = 0;
+    sg->rows = 0; sg->off_root_rows = 0;
     size_t off = 0;
     sg->off_p = (int)off; off = a16(off + sizeof(double) * std::max(E, 1));
     sg->off_eid = (int)off; off = a16(off + sizeof(uint16_t) * G * G);

@@ -42,7 +42,7 @@
 #define NR_WIDE_MAX_NB 255      // bucket schedule: bucket ids fit a byte
 #define NR_WIDE_FREE 0xffu      // bucket byte of a free arena slot
 
-// Graph tables of one wide instance: p[E], q[E] (double), row_ptr[n+1] (int),
+// Graph tables of one wide instance: p[E] (double), row_ptr[n+1] (int),
 // arcs[n_arcs] (u32 = eid << 14 | head).  Offsets from the blob start, 16-byte aligned.
 // Tables up to NR_WIDE_STAGE_MAX are staged into every block's shared memory; larger ones (the
 // reference's 6301-node directed fixture: 440 KB) are read from global memory (L2).
@@ -52,7 +52,7 @@
 // high 16 bits; 0xffff: none).
 struct NrWideGraph {
     int n, e, w4, src, dst, n_arcs, nwd;
-    int off_p, off_q, off_row, off_arc, blob_bytes;
+    int off_p, off_row, off_arc, blob_bytes;
     int nk;                     // K-terminal: terminals other than src (0: two-terminal, dst)
     int off_kmask;              // K-terminal: bitmask of the terminals, nwd words
     int tables_global;          // 1: the tables stay in global memory
@@ -160,7 +160,7 @@ struct NrWideAcc {
 };
 
 struct NrWideView {
-    const double *p, *q;
+    const double *p;                 // q = 1 - p is computed (__dsub_rn: the host's rounding)
     const int *row;
     const uint32_t *arc;
     const uint32_t *rows, *ehead;    // bitset tables (g.bitset)
@@ -176,7 +176,6 @@ __device__ __forceinline__ NrWideView nr_wide_view(unsigned char *smem, const un
     const unsigned char *tb = g.tables_global ? blob : smem;
     NrWideView v;
     v.p = reinterpret_cast<const double *>(tb + g.off_p);
-    v.q = reinterpret_cast<const double *>(tb + g.off_q);
     v.row = reinterpret_cast<const int *>(tb + g.off_row);
     v.arc = reinterpret_cast<const uint32_t *>(tb + g.off_arc);
     v.rows = g.bitset ? reinterpret_cast<const uint32_t *>(tb + g.off_rows) : nullptr;
@@ -656,7 +655,7 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
         if (lane == 0) base = atomicAdd(O.count, 2ull);
         base = __shfl_sync(NR_FULL, base, 0);
         const int sh = (e & 15) << 1;
-        nr_wide_emit(O, A, m, g.w4, base, e, 3u << sh, __dmul_rn(mass, v.q[e]));        // down
+        nr_wide_emit(O, A, m, g.w4, base, e, 3u << sh, __dmul_rn(mass, __dsub_rn(1.0, v.p[e])));   // down
         nr_wide_emit(O, A, m, g.w4, base + 1, e, 2u << sh, __dmul_rn(mass, v.p[e]));    // up
         __syncwarp();
         return;
@@ -690,7 +689,7 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
         const int wi = (int)(e >> 4);
         if (((m[wi] >> sh) & 3u) != 3u) continue;          // only UNKNOWN hops branch
         const unsigned long long slot = base + (unsigned long long)k;
-        const double cm = __dmul_rn(Pm, v.q[e]);
+        const double cm = __dmul_rn(Pm, __dsub_rn(1.0, v.p[e]));
         if (slot < O.cap) {
             uint32_t *dstw = reinterpret_cast<uint32_t *>(O.mask + slot * w4);
             if (W4) {

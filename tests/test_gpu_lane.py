@@ -48,11 +48,12 @@ def mixed_batch():
     return gs, [s for s, _ in st], [t for _, t in st]
 
 
-def lane_expected(g):
-    """n <= 16 and an undirected simple graph: every edge id on exactly the two arcs u -> v and
-    v -> u, no self-loop, no ordered pair twice."""
+def lane_expected(g, max_n=16):
+    """n <= max_n and an undirected simple graph: every edge id on exactly the two arcs u -> v and
+    v -> u, no self-loop, no ordered pair twice.  (The one-slot lane kernel takes up to 16 nodes,
+    the two-slot kernel of breadth-first waves up to 32.)"""
     import numpy as np
-    if g.n_nodes > 16:
+    if g.n_nodes > max_n:
         return False
     tails = np.repeat(np.arange(g.n_nodes), np.diff(g.row_ptr))
     arcs = list(zip(tails.tolist(), g.col_idx.tolist(), g.edge_id.tolist()))
@@ -82,13 +83,13 @@ def test_lane_kernel_wave_schedule(ctx, oracle, target, shift):
     if shift < 0:                                 # four instances a warp instead of the default two
         two = ctx.reliability_batch(gs, srcs, dsts, target_width=target, bucket_shift=shift, n_buckets=nb,
                                     capacity=1 << 16, lane_slots=4)
-        for i, (a, d) in enumerate(zip(lane, two)):
-            assert a.kernel == d.kernel, i
+        for i, (g, a, d) in enumerate(zip(gs, lane, two)):
+            assert d.kernel == ("lane2" if lane_expected(g) else "group"), i   # 17..32 nodes: two slots only
             for f in FIELDS:
                 assert getattr(a, f) == getattr(d, f), (i, f)
     for i, (g, a, b, c) in enumerate(zip(gs, lane, group, one)):
         assert a.engine == "warp" and b.engine == "warp" and a.spilled == 0
-        assert a.kernel == (lane_name if lane_expected(g) else "group"), i
+        assert a.kernel == (lane_name if lane_expected(g, 32 if shift < 0 else 16) else "group"), i
         assert b.kernel == "group" and c.kernel == ("lane" if lane_expected(g) else "group")
         for f in FIELDS:
             assert getattr(a, f) == getattr(b, f), (i, f, getattr(a, f), getattr(b, f))
@@ -170,3 +171,68 @@ def test_two_slot_kernel_budget_spills_and_uneven_batches(ctx, oracle):
             assert rr.kernel == "lane2" and rr.spilled == 0
             assert (rr.nodes, rr.iterations, rr.max_queue_items, rr.queued) == (o.nodes, o.waves, o.max_wave, o.queued)
             assert rr.R == o.R and rr.esp == o.esp
+
+
+def lane32_batch():
+    """Undirected simple graphs of 17..32 nodes (32-bit rows in the two-slot kernel), mask widths
+    1..8 blocks, and edge cases: certain edges (p = 0 and 1: the root's rows are gathered), src ==
+    dst, an unreachable dst, a two-node path inside a large node set."""
+    from relaibilitygpu_gb300 import graphs
+    gs, st = [], []
+    for s in range(6):
+        for r, c in ((4, 5), (5, 5), (5, 6), (6, 5), (4, 8)):
+            g = graphs.grid(r, c, p_range=(0.8, 0.99), seed=900 + 10 * s + r * c)
+            gs.append(g); st.append((0, g.n_nodes - 1))
+        g = graphs.gnm(20, 60, p_range=(0.8, 0.99), seed=950 + s); gs.append(g); st.append((g.src, g.dst))
+        g = graphs.gnm(28, 84, p_range=(0.85, 0.99), seed=960 + s); gs.append(g); st.append((g.src, g.dst))
+        gs.append(graphs.complete(20, p_range=(0.9, 0.99), seed=970 + s)); st.append((0, 19))
+    gs.append(graphs.complete(25, p_range=(0.9, 0.99), seed=980)); st.append((0, 24))
+    gs.append(graphs.complete(32, p_range=(0.95, 0.99), seed=981)); st.append((3, 30))
+    g = graphs.grid(5, 5, p_range=(0.8, 0.99), seed=982)
+    p = g.edge_p.copy(); p[3] = 0.0; p[7] = 1.0; p[11] = 0.0
+    gs.append(graphs.from_edges(25, g.edge_list(), p)); st.append((0, 24))
+    gs.append(graphs.grid(4, 5, p_range=(0.8, 0.99), seed=983)); st.append((7, 7))
+    gs.append(graphs.from_edges(20, [(i, i + 1) for i in range(18)] + [(0, 5)], [0.9] * 19)); st.append((0, 19))
+    gs.append(graphs.from_edges(30, [(0, 29)] + [(i, i + 1) for i in range(1, 28)], [0.8] * 28)); st.append((0, 29))
+    return gs, [a for a, _ in st], [b for _, b in st]
+
+
+@pytest.mark.parametrize("target,budget,border", [(1e-6, 0, "src"), (1e-9, 4000, "src"), (1e-7, 0, "p_asc"),
+                                                  (1e-5, 0, "dst")])
+def test_two_slot_kernel_32_bit_rows(ctx, oracle, target, budget, border):
+    """Graphs of 17..32 nodes in breadth-first waves run in the two-slot lane kernel with 32-bit
+    rows; every field equals the lane-group kernel's and the oracle's (waves, widest wave, counts,
+    queue, exact sums), with budgets and branch orders.  Runs whose queue filled (each slot has
+    the lane-group kernel's pages, but the kernels choose different children to spill) are
+    brackets of the same value."""
+    gs, srcs, dsts = lane32_batch()
+    opts = dict(target_width=target, bucket_shift=-1, n_buckets=64, capacity=1 << 18, max_nodes=budget,
+                branch_order=border)
+    lane = ctx.reliability_batch(gs, srcs, dsts, **opts)
+    group = ctx.reliability_batch(gs, srcs, dsts, small_kernel="group", **opts)
+    compared = 0
+    for i, (g, a, b) in enumerate(zip(gs, lane, group)):
+        assert a.kernel == ("lane2" if lane_expected(g, 32) else "group") and b.kernel == "group", i
+        if a.spilled or b.spilled:            # a full queue (the large grids at 1e-6): brackets of
+            assert max(a.R, b.R) <= min(a.R + a.esp, b.R + b.esp) + 1e-15, i   # the same value
+            continue
+        for f in FIELDS:
+            assert getattr(a, f) == getattr(b, f), (i, f, getattr(a, f), getattr(b, f))
+        if i % 3 == 0 or i >= len(gs) - 6:
+            o = oracle.run(g, srcs[i], dsts[i], target_width=target, max_nodes=budget, branch_order=border)
+            assert (a.nodes, a.leaves, a.dead_ends, a.iterations, a.max_queue_items, a.queued) == \
+                (o.nodes, o.leaves, o.dead, o.waves, o.max_wave, o.queued), i
+            assert a.R == o.R and a.esp == o.esp, i
+            compared += 1
+    assert compared >= 12
+
+
+def test_two_slot_kernel_32_bit_rows_spills(ctx, oracle):
+    """A 32-bit-row instance whose half of the warp's pages fills spills into ESP; the bracket
+    holds (exact R of a 4 x 5 grid by the oracle)."""
+    from relaibilitygpu_gb300 import graphs
+    g = graphs.grid(4, 5, p_range=(0.6, 0.95), seed=3)
+    exact = oracle.run(g, 0, 19, threads=8)
+    r = ctx.reliability(g, 0, 19, target_width=1e-15, bucket_shift=-1, n_buckets=64, capacity=256)
+    assert r.kernel == "lane2" and r.spilled > 0
+    assert r.R <= exact.R + 1e-15 and exact.R <= r.R + r.esp + 1e-12
