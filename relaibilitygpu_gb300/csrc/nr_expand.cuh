@@ -45,6 +45,39 @@ __device__ __forceinline__ void nr_acc_zero(NrLaneAcc &a)
     a.nodes = a.leaves = a.dead = a.trunc = a.spilled = 0;
 }
 
+// Level-synchronous BFS of every group of the warp over the in-neighbour rows
+// `row` (lane v: the nodes u with a usable arc u -> v); one ballot per level.
+// Returns whether dst was reached; par = the smallest frontier node with a
+// usable arc to v (lane v), level = hops of the shortest path.  All 32 lanes
+// call it; groups with search == false take part without searching.
+template <int G>
+__device__ __forceinline__ bool nr_group_bfs(uint32_t row, bool search, int n, int src, int dst, int &par, int &level)
+{
+    const int lane = threadIdx.x & 31;
+    const int v = lane & (G - 1);
+    const int gbase = lane & ~(G - 1);
+    uint32_t F = 1u << src, vis = F;
+    par = -1;
+    level = 0;
+    bool found = search && (src == dst);
+    bool searching = search && !found;
+    while (__any_sync(NR_FULL, searching)) {
+        const uint32_t t = row & F;
+        const bool hit = searching && (v < n) && (t != 0u) && !((vis >> v) & 1u);
+        if (hit) par = __ffs(t) - 1;
+        const uint32_t b = __ballot_sync(NR_FULL, hit);
+        const uint32_t nf = (G == 32) ? b : ((b >> gbase) & ((1u << G) - 1u));
+        if (searching) {
+            vis |= nf;
+            F = nf;
+            ++level;
+            if ((vis >> dst) & 1u) { found = true; searching = false; }
+            else if (nf == 0u) searching = false;
+        }
+    }
+    return found;
+}
+
 // Expand the group's subproblem (mask words in smem at my_m, mass `mass`).
 // Every lane of the warp must call this (it uses full-warp shuffles/ballots).
 // On return, a lane with has_child holds one child: words w[] and mass cm.
@@ -157,24 +190,8 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
     else if (active && v < n) row = nr_build_row(sg, my_m, v);
 
     // level-synchronous BFS, one ballot per level for all groups of the warp
-    uint32_t F = 1u << src, vis = F;
     int par = -1, level = 0;
-    bool found = active && (src == dst);
-    bool searching = active && !found;
-    while (__any_sync(NR_FULL, searching)) {
-        const uint32_t t = row & F;
-        const bool hit = searching && (v < n) && (t != 0u) && !((vis >> v) & 1u);
-        if (hit) par = __ffs(t) - 1;
-        const uint32_t b = __ballot_sync(NR_FULL, hit);
-        const uint32_t nf = (G == 32) ? b : ((b >> gbase) & ((1u << G) - 1u));
-        if (searching) {
-            vis |= nf;
-            F = nf;
-            ++level;
-            if ((vis >> dst) & 1u) { found = true; searching = false; }
-            else if (nf == 0u) searching = false;
-        }
-    }
+    const bool found = nr_group_bfs<G>(row, active, n, src, dst, par, level);
     if (active && !found && leader) acc.dead++;
     const bool live = active && found;
     const int L = live ? level : 0;                     // hops on the path
@@ -286,38 +303,6 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
     }
 }
 
-// Level-synchronous BFS of every group of the warp over the in-neighbour rows
-// `row` (lane v: the nodes u with a usable arc u -> v); one ballot per level.
-// Returns whether dst was reached; par = the smallest frontier node with a
-// usable arc to v (lane v), level = hops of the shortest path.  All 32 lanes
-// call it; groups with search == false take part without searching.
-template <int G>
-__device__ __forceinline__ bool nr_group_bfs(uint32_t row, bool search, int n, int src, int dst, int &par, int &level)
-{
-    const int lane = threadIdx.x & 31;
-    const int v = lane & (G - 1);
-    const int gbase = lane & ~(G - 1);
-    uint32_t F = 1u << src, vis = F;
-    par = -1;
-    level = 0;
-    bool found = search && (src == dst);
-    bool searching = search && !found;
-    while (__any_sync(NR_FULL, searching)) {
-        const uint32_t t = row & F;
-        const bool hit = searching && (v < n) && (t != 0u) && !((vis >> v) & 1u);
-        if (hit) par = __ffs(t) - 1;
-        const uint32_t b = __ballot_sync(NR_FULL, hit);
-        const uint32_t nf = (G == 32) ? b : ((b >> gbase) & ((1u << G) - 1u));
-        if (searching) {
-            vis |= nf;
-            F = nf;
-            ++level;
-            if ((vis >> dst) & 1u) { found = true; searching = false; }
-            else if (nf == 0u) searching = false;
-        }
-    }
-    return found;
-}
 
 // Fork branching (workingPad/main.cu:303-430 with :550-565, FORK_BEST_EDGE):
 // a path of up edges means the subproblem is connected, so its whole mass goes

@@ -8,7 +8,7 @@ rank sets the job's time), and exact mass sums are added in integer space.
 """
 from __future__ import annotations
 
-from typing import Dict, Sequence, Tuple
+from typing import Dict, Tuple
 
 
 def shard(n: int, rank: int, world: int) -> Tuple[int, int]:
@@ -43,12 +43,3 @@ def reduce_totals(local: Dict[str, float], group=None) -> Dict[str, float]:
         else:
             out[k] = float(sums[i]); i += 1
     return out
-
-
-def exact_sum_words(words: Sequence[Sequence[int]]) -> Tuple[int, int, int]:
-    """Add 192-bit fixed-point mass sums given as (w0, w1, w2) 64-bit words (exact, any order)."""
-    total = 0
-    for w0, w1, w2 in words:
-        total += int(w0) | (int(w1) << 64) | (int(w2) << 128)
-    total &= (1 << 192) - 1
-    return total & (2**64 - 1), (total >> 64) & (2**64 - 1), total >> 128

@@ -41,13 +41,6 @@ def test_shard_covers_everything():
             assert max(sizes) - min(sizes) <= 1
 
 
-def test_exact_sum_words():
-    from relaibilitygpu_gb300 import replicas
-    a = (2**64 - 1, 5, 0)
-    b = (1, 0, 1)
-    assert replicas.exact_sum_words([a, b]) == (0, 6, 1)
-
-
 def test_two_gloo_ranks_match_single_process():
     import multiprocessing as mp
     import socket
