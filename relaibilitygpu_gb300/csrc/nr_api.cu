@@ -379,12 +379,18 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     const int G = group_width(g->n_nodes);
     const int W4 = sg.w4;
     if (W4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
-    const void *kfn = grid_kernel(G, W4, o->branching == NR_BRANCH_FORK);
+    // one lane per subproblem (nr_grid_lane.cuh) on undirected simple graphs of <= 16 nodes with
+    // path branching, unless the lane groups are asked for
+    const bool lane = o->branching != NR_BRANCH_FORK && o->small_kernel != NR_SMALL_GROUP &&
+                      g->n_nodes <= NR_LANE_MAX_N && W4 <= NR_LANE_MAX_W4 && rows_mode_of(g) == 1 &&
+                      cap <= 0x7fffffffull;
+    const void *kfn = lane ? nr_grid_lane_kernel_ptr(W4) : grid_kernel(G, W4, o->branching == NR_BRANCH_FORK);
     if (!kfn) return NR_ERR_UNSUPPORTED;
 
     const int block = NR_BLOCK_THREADS;
     const int warps = block / 32;
-    const size_t smem = (size_t)sg.blob_bytes + (size_t)warps * (32 / G) * 4 * W4 * sizeof(uint32_t);
+    const size_t smem = lane ? nr_grid_lane_shm_bytes(sg.blob_bytes, warps)
+                             : (size_t)sg.blob_bytes + (size_t)warps * (32 / G) * 4 * W4 * sizeof(uint32_t);
     NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
     int bps = 0;
     NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
@@ -392,10 +398,12 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     if (o->blocks_per_sm > 0 && o->blocks_per_sm < bps) bps = o->blocks_per_sm;
     const int grid = bps * c->sms;
 
-    const size_t item_bytes = (size_t)W4 * 16 + sizeof(double);
+    const size_t row_bytes = lane ? 4 * (size_t)NR_LANE_ROW_WORDS : 0;    // rows carried in the records
+    const size_t item_bytes = (size_t)W4 * 16 + sizeof(double) + row_bytes;
     const size_t mask_bytes = align16((size_t)cap * W4 * 16);
     const size_t mass_bytes = align16((size_t)cap * sizeof(double));
-    const size_t qneed = 2 * (mask_bytes + mass_bytes);
+    const size_t rows_bytes = align16((size_t)cap * row_bytes);
+    const size_t qneed = 2 * (mask_bytes + mass_bytes + rows_bytes);
     size_t free_b = 0, total_b = 0;
     NR_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
     if (qneed > c->qbytes && qneed > free_b + c->qbytes) return NR_ERR_NOMEM;
@@ -420,6 +428,8 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     P.mass[0] = reinterpret_cast<double *>(qb + mask_bytes);
     P.mask[1] = reinterpret_cast<uint4 *>(qb + mask_bytes + mass_bytes);
     P.mass[1] = reinterpret_cast<double *>(qb + 2 * mask_bytes + mass_bytes);
+    P.rows[0] = lane ? reinterpret_cast<uint4 *>(qb + 2 * (mask_bytes + mass_bytes)) : nullptr;
+    P.rows[1] = lane ? reinterpret_cast<uint4 *>(qb + 2 * (mask_bytes + mass_bytes) + rows_bytes) : nullptr;
     P.capacity = cap;
     P.wave_count = reinterpret_cast<unsigned long long *>(sb + off_wc);
     P.max_waves = max_waves;
@@ -444,6 +454,18 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     NR_CUDA_TRY(cudaMemcpyAsync(P.wave_count, &one_u, sizeof(one_u), cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaMemcpyAsync(P.mask[0], root.data(), 16 * W4, cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaMemcpyAsync(P.mass[0], &one, sizeof(one), cudaMemcpyHostToDevice, s));
+    // the root's not-down rows (lane kernel): node v's in-neighbours over edges with p > 0, two
+    // 16-bit rows a word
+    uint32_t root_rows[NR_LANE_ROW_WORDS] = {0};
+    if (lane) {
+        for (int u = 0; u < g->n_nodes; ++u)
+            for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j)
+                if (g->edge_p[g->edge_id[j]] > 0.0) {
+                    const int v = g->col_idx[j];
+                    root_rows[v >> 1] |= 1u << (u + ((v & 1) << 4));
+                }
+        NR_CUDA_TRY(cudaMemcpyAsync(P.rows[0], root_rows, sizeof(root_rows), cudaMemcpyHostToDevice, s));
+    }
 
     void *args[] = {&P};
     NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
@@ -491,10 +513,11 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     r->ms = ms;
     r->time_to_bound_ms = 0;
     r->engine = NR_ENGINE_GRID;
+    r->kernel = lane ? NR_KERNEL_LANE : 0;
     r->grid_blocks = grid;
     r->block_threads = block;
     r->capacity = cap;
-    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one);
+    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one) + (lane ? sizeof(root_rows) : 0);
     r->d2h_bytes = sizeof(unsigned long long) * wc.size() + sizeof(NrPartial) * grid + sizeof(int);
     if (status & NR_DEV_ERR_TIMEOUT) return NR_ERR_TIMEOUT;
     if (status) return NR_ERR_INTERNAL;

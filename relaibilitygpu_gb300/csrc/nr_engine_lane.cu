@@ -2,12 +2,22 @@
 // graphs of up to 16 nodes (nr_lane.cuh, nr_lane2.cuh), one per mask width, and the
 // two-slot kernel with 32-bit rows for 17..32 nodes.
 #include "nr_lane2.cuh"
+#include "nr_grid_lane.cuh"
 
 const void *nr_lane_kernel_ptr(int w4)
 {
     switch (w4) {
     case 1: return (const void *)nr_lane_kernel<1>;
     case 2: return (const void *)nr_lane_kernel<2>;
+    default: return nullptr;
+    }
+}
+
+const void *nr_grid_lane_kernel_ptr(int w4)
+{
+    switch (w4) {
+    case 1: return (const void *)nr_grid_lane_kernel<1>;
+    case 2: return (const void *)nr_grid_lane_kernel<2>;
     default: return nullptr;
     }
 }

@@ -27,6 +27,7 @@
 #include "nr_device.cuh"
 #include "nr_warp.cuh"
 #include "nr_lane2.cuh"
+#include "nr_grid_lane.cuh"
 #include "nr_wide.cuh"
 #include "nr_mlp.cuh"
 
@@ -48,6 +49,7 @@ const void *nr_warp_fork_kernel_ptr_g32(int w4);
 const void *nr_warp_learn_kernel_ptr_g16(int w4);
 const void *nr_warp_learn_kernel_ptr_g32(int w4);
 const void *nr_lane_kernel_ptr(int w4);
+const void *nr_grid_lane_kernel_ptr(int w4);
 const void *nr_lane2_kernel_ptr(int w4, int slots, int row_bits = 16);
 int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
 

@@ -60,6 +60,7 @@ struct NrGridParams {
     const unsigned char *blob;        // graph tables in global memory
     uint4 *mask[2];                   // ping-pong wave buffers: [capacity][w4] 16-byte blocks
     double *mass[2];                  // [capacity]
+    uint4 *rows[2];                   // one lane a subproblem: [capacity][2] not-down rows (else nullptr)
     unsigned long long capacity;
     unsigned long long *wave_count;   // [max_waves + 1]; wave_count[0] = 1 (the root)
     int max_waves;

@@ -236,3 +236,38 @@ def test_two_slot_kernel_32_bit_rows_spills(ctx, oracle):
     r = ctx.reliability(g, 0, 19, target_width=1e-15, bucket_shift=-1, n_buckets=64, capacity=256)
     assert r.kernel == "lane2" and r.spilled > 0
     assert r.R <= exact.R + 1e-15 and exact.R <= r.R + r.esp + 1e-12
+
+
+def test_whole_gpu_lane_kernel(ctx, oracle):
+    """Single exhaustive (and eps-truncated) runs of undirected simple graphs of <= 16 nodes take
+    the whole-GPU wave engine with one lane per subproblem; counts, waves, widest wave and exact
+    sums equal the lane-group version's (small_kernel="group") and the oracle's, with branch
+    orders; a capacity overflow spills into a bracket."""
+    from relaibilitygpu_gb300 import graphs
+    cases = [(graphs.complete(8, p=0.5), 0, 7), (graphs.complete(9, p_range=(0.5, 0.95), seed=3), 0, 8),
+             (graphs.grid(3, 4, p_range=(0.6, 0.97), seed=4), 0, 11), (graphs.grid(4, 4, p=0.9), 0, 15),
+             (graphs.gnm(14, 30, p_range=(0.7, 0.99), seed=5), 2, 11),
+             (graphs.from_edges(6, [(0, 1), (1, 5), (0, 2), (2, 5), (1, 2), (0, 5)], [1.0, 0.9, 0.0, 0.8, 1.0, 0.5]), 0, 5),
+             (graphs.complete(6, p=0.7), 3, 3),
+             (graphs.from_edges(5, [(0, 1), (1, 2), (2, 0), (3, 1)], [0.9, 0.8, 0.7, 0.6]), 0, 4)]
+    for g, s, t in cases:
+        for eps, border in ((0.0, "src"), (1e-6, "src"), (0.0, "p_asc"), (1e-7, "dst")):
+            a = ctx.reliability(g, s, t, capacity=1 << 22, eps=eps, branch_order=border)
+            b = ctx.reliability(g, s, t, capacity=1 << 22, eps=eps, branch_order=border, small_kernel="group")
+            assert a.engine == "grid" and b.engine == "grid" and a.kernel == "lane" and b.kernel == ""
+            for f in ("R", "esp", "nodes", "leaves", "dead_ends", "truncated", "spilled", "paths", "iterations",
+                      "max_queue_items"):
+                assert getattr(a, f) == getattr(b, f), (g.n_nodes, eps, border, f)
+            o = oracle.run(g, s, t, eps=eps, branch_order=border)
+            assert (a.nodes, a.leaves, a.dead_ends, a.truncated, a.iterations, a.max_queue_items) == \
+                (o.nodes, o.leaves, o.dead, o.truncated, o.waves, o.max_wave)
+            assert a.R == o.R and a.esp == o.esp
+    # the reference's published K10 p=0.5 run: 14,866,064 subproblems in 38 waves, widest 1,596,000
+    k10 = graphs.complete(10, p=0.5)
+    r = ctx.reliability(k10, 0, 9, capacity=1 << 22)
+    assert r.kernel == "lane" and (r.nodes, r.iterations, r.max_queue_items) == (14866064, 38, 1596000)
+    g = graphs.complete(9, p_range=(0.6, 0.97), seed=5)
+    exact = oracle.run(g, 0, 8)
+    r = ctx.reliability(g, 0, 8, capacity=2000)
+    assert r.kernel == "lane" and r.spilled > 0
+    assert r.R <= exact.R + 1e-15 and exact.R <= r.R + r.esp + 1e-12
