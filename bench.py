@@ -594,7 +594,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="only the headline line (no configs, orders or CPU leg)")
-    ap.add_argument("--case", choices=["k15batch", "rgg200", "uneven"],
+    ap.add_argument("--case", choices=["k15batch", "rgg200", "uneven", "k10"],
                     help="profiling: run one case twice (a warm-up call, then the call to capture) and exit")
     ap.add_argument("--budget", type=int, default=1_000_000, help="--case rgg200: subproblem budget")
     ap.add_argument("--arena", type=int, default=22, help="--case rgg200: log2 of the arena slots")
@@ -761,7 +761,11 @@ def run_case(args):
     batch, opts = None, None
     for k in range(2):
         flush()
-        if args.case == "rgg200":
+        if args.case == "k10":
+            g = nr.complete(10, p_range=(0.5, 0.95), seed=2)
+            r = ctx.reliability(g, 0, 9, capacity=1 << 22)
+            out = {"nodes": r.nodes, "waves": r.iterations, "ms": r.ms, "kernel": r.kernel}
+        elif args.case == "rgg200":
             g = nr.rgg(200, 600, p_range=(0.9, 0.99), seed=7)
             r = ctx.reliability(g, g.src, g.dst, capacity=1 << args.arena, target_width=1e-5, order="maxmass",
                                 bucket_shift=2, n_buckets=255, max_nodes=args.budget, timeout_ms=120000.0)

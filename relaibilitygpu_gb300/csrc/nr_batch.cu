@@ -655,7 +655,16 @@ static int run_mixed_batch(nr_context *c, int n, const nr_graph *gs, const int32
         memset(r, 0, sizeof(*r));
         r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
-        rc = run_wide(c, &gs[i], srcs[i], dsts[i], std::max<uint64_t>(capacity, 1u << 22), &o, r);
+    }
+    const uint64_t wcap = std::max<uint64_t>(capacity, 1u << 22);
+    // breadth-first waves with path branching (run_wide's whole-GPU wave engine): the graphs run
+    // side by side, each on its own group of blocks; else one at a time
+    const bool buckets = o.bucket_shift >= 0 &&
+                         (o.order == NR_ORDER_MAXMASS || (o.order == NR_ORDER_AUTO && o.target_width > 0));
+    if (wide_idx.size() > 1 && !buckets && o.order != NR_ORDER_LEARNED && o.branching == NR_BRANCH_PATH)
+        return run_grid_wide_multi(c, wide_idx, gs, srcs, dsts, wcap, &o, res);
+    for (int i : wide_idx) {
+        rc = run_wide(c, &gs[i], srcs[i], dsts[i], wcap, &o, &res[i]);
         if (rc) return rc;
     }
     return NR_OK;

@@ -147,9 +147,12 @@ __device__ __forceinline__ long long nr_globaltimer()
 // that sees no other block arrive for timeout_ns (or sees another block's
 // error) gives up, sets NR_DEV_ERR_TIMEOUT and returns false, and the caller
 // leaves its loop so the kernel still ends.
+// nblocks: the blocks that meet at this barrier (all of the grid, or one instance's group of
+// blocks in a launch that runs several instances).
 __device__ __forceinline__ bool nr_grid_sync(unsigned *count, unsigned *gen, int *status,
-                                             long long timeout_ns)
+                                             long long timeout_ns, unsigned nblocks = 0)
 {
+    if (nblocks == 0) nblocks = gridDim.x;
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -160,7 +163,7 @@ __device__ __forceinline__ bool nr_grid_sync(unsigned *count, unsigned *gen, int
         __threadfence();
         unsigned prev = atomicAdd(count, 1u);
         int ok = 1;
-        if (prev == gridDim.x - 1) {
+        if (prev == nblocks - 1) {
             *vcount = 0;
             __threadfence();
             atomicAdd(gen, 1u);

@@ -757,8 +757,9 @@ __device__ __forceinline__ unsigned long long nr_block_u64_sum(unsigned long lon
 }
 
 // This block's share of the stop test after a wave (all threads call it).
-__device__ __forceinline__ void nr_wide_write_share(NrWideShare *slot, const NrWideAcc &A)
+__device__ __forceinline__ void nr_wide_write_share(NrWideShare *slot, const NrWideAcc &A, int bid = -1)
 {
+    if (bid < 0) bid = (int)blockIdx.x;
     NrFix w = nr_fix_zero();
     unsigned long long nodes = 0;
     if ((threadIdx.x & 31) == 0) {
@@ -770,7 +771,7 @@ __device__ __forceinline__ void nr_wide_write_share(NrWideShare *slot, const NrW
     w = nr_block_fix_sum(w);
     nodes = nr_block_u64_sum(nodes);
     if (threadIdx.x == 0) {
-        NrWideShare *d = slot + blockIdx.x;
+        NrWideShare *d = slot + bid;
         __stcg(&d->width.w0, w.w0);
         __stcg(&d->width.w1, w.w1);
         __stcg(&d->width.w2, w.w2);
@@ -781,15 +782,17 @@ __device__ __forceinline__ void nr_wide_write_share(NrWideShare *slot, const NrW
 // Stop test before a wave from the shares of the last one (every block gets
 // the same answer): 0 go on, 1 target width met, 3 node budget reached.
 __device__ __forceinline__ int nr_wide_stop_test(const NrWideShare *slot, bool first, int target_on,
-                                                 const NrFix &target_fix, unsigned long long max_nodes)
+                                                 const NrFix &target_fix, unsigned long long max_nodes,
+                                                 unsigned nblk = 0)
 {
+    if (nblk == 0) nblk = gridDim.x;
     if (!target_on && !max_nodes) return 0;
     NrFix width = nr_fix_zero();
     unsigned long long nodes = 0;
     if (first) {
         if (threadIdx.x == 0) width = nr_fix_of(1.0);      // the root alone is queued
     } else {
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+        for (unsigned b = threadIdx.x; b < nblk; b += blockDim.x) {
             NrFix v;                                       // written by other blocks: read from L2
             v.w0 = __ldcg(&slot[b].width.w0);
             v.w1 = __ldcg(&slot[b].width.w1);
@@ -856,6 +859,115 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK, 6) nr_grid_wide_kernel(NrGridWi
         if (wave + 1 == P.max_waves && threadIdx.x == 0 && blockIdx.x == 0 &&
             *(volatile unsigned long long *)&P.wave_count[wave + 1] != 0)
             atomicOr(P.status, NR_DEV_ERR_WAVES);
+    }
+    nr_wide_block_partial(P.partials + blockIdx.x, A);
+}
+
+// Several instances in one cooperative launch, breadth-first waves: instance i owns the
+// blocks [i * bpi, (i + 1) * bpi) and runs nr_grid_wide_kernel's loop on them -- its own
+// ping-pong buffers, wave counters, barrier, stop-test shares and stop record -- so every
+// instance follows the one-instance schedule exactly, and the instances of a batch of large
+// graphs run side by side instead of one launch each.
+struct NrGridWideMultiParams {
+    const NrWideGraph *g;            // [m] in global memory
+    const unsigned char *blob;       // the instances' tables, instance i at blob_off[i]
+    const long long *blob_off;       // [m]
+    const uint4 *root;               // [m][w4]: the instances' root masks
+    uint4 *mask;                     // [m][2][mask_half]: an instance's two wave buffers
+    double *mass;                    // [m][2][mass_half]
+    unsigned long long mask_half;    // 16-byte blocks of one wave buffer (capacity x the widest mask)
+    unsigned long long mass_half;    // masses of one wave buffer (capacity, rounded up)
+    unsigned long long capacity;
+    unsigned long long *wave_count;  // [m][max_waves + 1]
+    int max_waves;
+    unsigned *bar;                   // [m][4]: barrier count, generation, status
+    NrPartial *partials;             // [gridDim.x]
+    NrWideShare *wpart;              // [m][2][bpi]
+    int *stop_wave;                  // [m][2]: waves run before a stop (or -1), stop reason
+    int m, bpi;
+    double eps;
+    long long timeout_ns;
+    int target_on;
+    NrFix target_fix;
+    unsigned long long max_nodes;
+    int border;
+};
+
+template <int W4>
+__global__ void __launch_bounds__(NR_WIDE_BLOCK, 6) nr_grid_wide_multi_kernel(NrGridWideMultiParams P)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int inst = (int)blockIdx.x / P.bpi, lb = (int)blockIdx.x % P.bpi;
+    const NrWideGraph g = P.g[inst];
+    const unsigned char *blob = P.blob + P.blob_off[inst];
+    if (!g.tables_global) nr_stage_blob(smem, blob, g.blob_bytes);
+    __syncthreads();
+    const NrWideView v = nr_wide_view(smem, blob, g);
+    const int w4 = W4 ? W4 : g.w4;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned long long gw = (unsigned long long)lb * (blockDim.x >> 5) + warp;
+    const unsigned long long TW = (unsigned long long)P.bpi * (blockDim.x >> 5);
+    const unsigned long long cap = P.capacity;
+    uint4 *mask0 = P.mask + (size_t)inst * 2 * P.mask_half;
+    double *mass0 = P.mass + (size_t)inst * 2 * P.mass_half;
+    unsigned long long *wave_count = P.wave_count + (size_t)inst * (P.max_waves + 1);
+    unsigned *bar = P.bar + (size_t)inst * 4;
+    int *status = reinterpret_cast<int *>(bar + 2);
+    NrWideShare *wpart = P.wpart + (size_t)inst * 2 * P.bpi;
+    int *stop_wave = P.stop_wave + (size_t)inst * 2;
+    __shared__ NrWideAcc s_acc[NR_WIDE_BLOCK / 32];        // as in nr_grid_wide_kernel
+    NrWideAcc &A = s_acc[warp];
+    if (lane == 0) {
+        nr_wide_acc_init(A);
+        // the root is queued before the first wave: the instance's first block holds its mass
+        A.net = (lb == 0 && threadIdx.x == 0) ? nr_fix_of(1.0) : nr_fix_zero();
+    }
+    __syncwarp();
+    // the instance's first block queues its root (mass 1) and clears its stop record; the group
+    // meets once before the first wave
+    if (lb == 0 && warp == 0) {
+        for (int k = lane; k < w4; k += 32) mask0[k] = P.root[(size_t)inst * w4 + k];
+        if (lane == 0) {
+            mass0[0] = 1.0;
+            wave_count[0] = 1ull;
+            stop_wave[0] = -1;
+            stop_wave[1] = 0;
+        }
+    }
+    bool ok = nr_grid_sync(bar, bar + 1, status, P.timeout_ns, (unsigned)P.bpi);
+
+    for (int wave = 0; ok && wave < P.max_waves; ++wave) {
+        unsigned long long n_in = *(volatile unsigned long long *)&wave_count[wave];
+        if (n_in > cap) n_in = cap;
+        if (n_in == 0) break;
+        const int stop = nr_wide_stop_test(wpart + (size_t)((wave + 1) & 1) * P.bpi, wave == 0, P.target_on,
+                                           P.target_fix, P.max_nodes, (unsigned)P.bpi);
+        if (stop) {
+            if (threadIdx.x == 0 && lb == 0) { stop_wave[0] = wave; stop_wave[1] = stop; }
+            break;
+        }
+        const uint4 *in_mask = mask0 + (size_t)(wave & 1) * P.mask_half;
+        const double *in_mass = mass0 + (size_t)(wave & 1) * P.mass_half;
+        NrWideOut O;
+        O.mask = mask0 + (size_t)((wave + 1) & 1) * P.mask_half;
+        O.mass = mass0 + (size_t)((wave + 1) & 1) * P.mass_half;
+        O.key = nullptr;
+        O.count = &wave_count[wave + 1];
+        O.cap = cap;
+        O.shift = 0;
+        O.nb = 1;
+        O.hist = nullptr;
+        for (unsigned long long idx = gw; idx < n_in; idx += TW) {
+            nr_wide_load_mask(v.m, in_mask + idx * w4, w4);
+            const double mass = __ldcg(in_mass + idx);
+            __syncwarp();
+            nr_wide_step<W4>(g, v, mass, P.eps, O, A, false, P.border);
+        }
+        if (P.target_on || P.max_nodes) nr_wide_write_share(wpart + (size_t)(wave & 1) * P.bpi, A, lb);
+        if (!nr_grid_sync(bar, bar + 1, status, P.timeout_ns, (unsigned)P.bpi)) break;
+        if (wave + 1 == P.max_waves && threadIdx.x == 0 && lb == 0 &&
+            *(volatile unsigned long long *)&wave_count[wave + 1] != 0)
+            atomicOr(status, NR_DEV_ERR_WAVES);
     }
     nr_wide_block_partial(P.partials + blockIdx.x, A);
 }

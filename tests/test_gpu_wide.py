@@ -113,7 +113,7 @@ def test_wide_target_width_matches_oracle(ctx, oracle, name, make, target):
 
 
 def test_batch_routes_large_graphs_to_wide_engine(ctx, oracle):
-    """Batches mix graphs above 32 nodes (whole-GPU engine, one at a time) with small ones
+    """Batches mix graphs above 32 nodes (whole-GPU engine, side by side) with small ones
     (warp engine, all together); with one bucket both follow the oracle's wave schedule."""
     from relaibilitygpu_gb300 import graphs
     gs = []
@@ -132,6 +132,39 @@ def test_batch_routes_large_graphs_to_wide_engine(ctx, oracle):
         assert (r.n_nodes, r.src, r.dst) == (g.n_nodes, g.src, g.dst)
         check(r, o)
         assert r.queued == o.queued
+
+
+def test_batch_runs_large_graphs_side_by_side(ctx, oracle):
+    """A batch's graphs above 32 nodes (breadth-first waves) share cooperative launches, each on
+    its own group of blocks with its own waves, barrier and stop tests: every field equals the
+    one-at-a-time run's, for compiled and runtime mask widths, budgets and eps truncation."""
+    from relaibilitygpu_gb300 import graphs
+    gs = ([graphs.grid(6, 6, p_range=(0.8, 0.99), seed=80 + s) for s in range(4)] +
+          [graphs.grid(6, 7, p_range=(0.85, 0.99), seed=85), graphs.rgg(60, 150, p_range=(0.9, 0.99), seed=86),
+           graphs.rgg(60, 150, p_range=(0.9, 0.99), seed=87), graphs.rgg(100, 300, p_range=(0.9, 0.99), seed=88),
+           graphs.complete(40, p_range=(0.9, 0.99), seed=89), graphs.complete(50, p_range=(0.95, 0.99), seed=90)])
+    srcs = [g.src if g.n_nodes not in (40, 50) else 0 for g in gs]
+    dsts = [g.dst if g.n_nodes not in (40, 50) else g.n_nodes - 1 for g in gs]
+    fields = ("R", "esp", "nodes", "leaves", "dead_ends", "truncated", "spilled", "paths", "iterations",
+              "max_queue_items", "queued", "stop")
+    compared = 0
+    for opts in (dict(target_width=1e-3), dict(target_width=1e-7, max_nodes=20000), dict(eps=1e-9, target_width=1e-3)):
+        res = ctx.reliability_batch(gs, srcs, dsts, capacity=1 << 22, bucket_shift=-1, **opts)
+        for k, (g, s, t, r) in enumerate(zip(gs, srcs, dsts, res)):
+            one = ctx.reliability(g, s, t, capacity=1 << 22, bucket_shift=-1, **opts)
+            assert r.engine == "grid" and one.engine == "grid"
+            if r.spilled or one.spilled:      # which records a full buffer spills depends on the
+                assert max(r.R, one.R) <= min(r.R + r.esp, one.R + one.esp) + 1e-15   # launch: brackets
+                continue
+            compared += 1
+            for f in fields:
+                assert getattr(r, f) == getattr(one, f), (k, opts, f, getattr(r, f), getattr(one, f))
+            if k % 3 == 0:
+                o = oracle.run(g, s, t, target_width=opts["target_width"], max_nodes=opts.get("max_nodes", 0),
+                               eps=opts.get("eps", 0.0), threads=4)
+                check(r, o)
+                assert r.queued == o.queued
+    assert compared >= 24
 
 
 def test_batch_large_graph_learned_order_unsupported(ctx, engine_lib):
