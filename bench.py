@@ -579,6 +579,18 @@ def cfg_rgg200(ctx, flush):
     exact = (r1.nodes, r1.leaves, r1.dead_ends, r1.iterations, r1.queued) == \
         (o.nodes, o.leaves, o.dead, o.waves, o.queued) and r1.R == o.R and r1.esp == o.esp
     dev_s = statistics.median(ms) / 1e3
+    # branch orders at the same budget: the bracket each leaves (ESP) and its device time
+    orders = {}
+    from relaibilitygpu_gb300 import learned as LR
+    for border in ("src", "p_asc", "learned"):
+        if border == "learned":
+            if not os.path.exists(LR.DEFAULT_MODEL):
+                continue
+            LR.set_model(ctx, LR.load())
+        flush()
+        rb = ctx.reliability(g, g.src, g.dst, capacity=1 << 28, max_nodes=budget, branch_order=border, **kw)
+        orders[border] = {"R": rb.R, "esp": rb.esp, "ms": rb.ms, "nodes": int(rb.nodes)}
+    dev_s = statistics.median(ms) / 1e3
     return {"workload": f"RGG N=200 E={g.n_edges} (unit square, seed 7) src={g.src} dst={g.dst} (farthest pair) "
                         f"p~U[0.9,0.99], bucketed max-mass queue (4 buckets per octave) toward ESP width<=1e-5, "
                         f"stopped at {budget:,} subproblems; 2^28-slot arena",
@@ -586,6 +598,7 @@ def cfg_rgg200(ctx, flush):
             "waves": int(r.iterations), "stop": int(r.stop), "gpu_ms_median": 1e3 * dev_s,
             "subproblems_per_sec": r.nodes / dev_s,
             "cpu": {"threads": threads, "budget": small, "seconds": cpu_s, "subproblems_per_sec": o.nodes / cpu_s},
+            "branch_orders_at_budget": orders,
             "parity": {"budget": small, "bit_exact_vs_oracle": exact, "ok": exact}}
 
 

@@ -105,7 +105,8 @@ enum {
                                (1 - p_e) x (1 - r(e)) is largest, r(e) the scorer's residual
                                reliability of the subproblem with e down -- a likely and critical
                                failure first; ties: path order.  The warp engine (n <= 32) with a
-                               target width or a max-mass / learned order only */
+                               target width or a max-mass / learned order, and the bucketed
+                               whole-GPU queue (n > 32, max-mass order), only */
 };
 
 typedef struct nr_options {

@@ -631,6 +631,7 @@ static int wide_block(nr_context *c, const NrWideGraph &wg)
 static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
                          nr_result *r, const int32_t *terms = nullptr, int nt = 0)
 {
+    if (o->branch_order == NR_BORDER_LEARNED) return NR_ERR_UNSUPPORTED;   // the bucketed queue only
     c->ckpt.valid = false;                 // the arena is about to be reused
     if (g->n_nodes > NR_WIDE_MAX_N || g->n_edges > 65535) return NR_ERR_UNSUPPORTED;
     NrWideGraph wg;
@@ -773,6 +774,7 @@ static int run_grid_wide(nr_context *c, const nr_graph *g, int src, int dst, uin
 int run_grid_wide_multi(nr_context *c, const std::vector<int> &idx, const nr_graph *gs, const int32_t *srcs,
                         const int32_t *dsts, uint64_t cap, const nr_options *o, nr_result *res)
 {
+    if (o->branch_order == NR_BORDER_LEARNED) return NR_ERR_UNSUPPORTED;   // the bucketed queue only
     c->ckpt.valid = false;                 // the arena is about to be reused
     struct Inst { int i; NrWideGraph wg; std::vector<unsigned char> blob; };
     std::vector<Inst> all;
@@ -1010,11 +1012,18 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     std::vector<unsigned char> blob;
     build_wide_blob(g, src, dst, &wg, &blob, terms, nt, o->branching == NR_BRANCH_FORK);
     const int W4 = wg.w4;
-    const void *kfn = nr_bucket_wide_kernel_ptr(W4);
+    // the learned branch order: the scorer's kernel, its weights and scratch (two-terminal path
+    // branching)
+    const bool learn = o->branch_order == NR_BORDER_LEARNED;
+    if (learn && (!c->has_model || nt > 0 || o->branching != NR_BRANCH_PATH)) return NR_ERR_UNSUPPORTED;
+    const void *kfn = learn ? nr_bucket_wide_learn_kernel_ptr(W4) : nr_bucket_wide_kernel_ptr(W4);
     if (!kfn) return NR_ERR_UNSUPPORTED;
-    const int block = wide_block(c, wg);
+    const size_t learn_warp = learn ? (size_t)NR_WIDE_LEARN_WORDS * 4 : 0;
+    int block = 0;
+    for (int w = NR_WIDE_BLOCK / 32; w >= 1 && !block; --w)
+        if (nr_wide_block_shm(wg, w) + w * learn_warp <= (size_t)smem_optin(c)) block = 32 * w;
     if (!block) return NR_ERR_UNSUPPORTED;
-    const size_t smem = nr_wide_block_shm(wg, block / 32);
+    const size_t smem = nr_wide_block_shm(wg, block / 32) + (block / 32) * learn_warp;
     NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
     int bps = 0;
     NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, block, smem));
@@ -1072,6 +1081,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     P.timeout_ns = (long long)((o->timeout_ms > 0 ? o->timeout_ms : 60000.0) * 1e6);
     P.fork = (o->branching == NR_BRANCH_FORK);
     P.border = o->branch_order;
+    P.mlp = c->mlp;                       // used by the learned instantiation only
     P.target_on = o->target_width > 0 ? 1 : 0;
     P.target_fix = nr_fix_of(o->target_width > 0 ? o->target_width : 0.0);
     P.max_nodes = o->max_nodes;
@@ -1226,7 +1236,10 @@ extern "C" int nr_reliability_ctx(nr_context *c, const nr_graph *g, int src, int
     NR_CUDA_TRY(cudaSetDevice(c->device));
     if (o.branching != NR_BRANCH_PATH && o.branching != NR_BRANCH_FORK) return NR_ERR_INVALID;
     if (const int rb = branch_order_ok(c, o)) return rb;
-    if (o.branch_order == NR_BORDER_LEARNED && g->n_nodes > NR_SMALL_MAX_N) return NR_ERR_UNSUPPORTED;
+    // graphs above 32 nodes take the learned branch order in the bucketed whole-GPU queue only
+    if (o.branch_order == NR_BORDER_LEARNED && g->n_nodes > NR_SMALL_MAX_N &&
+        !(o.bucket_shift >= 0 && (o.order == NR_ORDER_MAXMASS || (o.order == NR_ORDER_AUTO && o.target_width > 0))))
+        return NR_ERR_UNSUPPORTED;
     if (o.branching == NR_BRANCH_FORK && o.order == NR_ORDER_LEARNED) return NR_ERR_UNSUPPORTED;
     if (g->n_nodes > NR_SMALL_MAX_N) return run_wide(c, g, src, dst, capacity, &o, res);
     if (o.target_width > 0 || o.order == NR_ORDER_MAXMASS || o.order == NR_ORDER_LEARNED) {

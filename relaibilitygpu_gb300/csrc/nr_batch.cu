@@ -594,8 +594,12 @@ static int batch_validate(nr_context *c, int n, const nr_graph *gs, const int32_
         if (!rc && !(i > 0 && same_structure_arrays(&gs[i], &gs[i - 1]))) rc = validate_structure(&gs[i]);
         if (!rc && gs[i].n_nodes > NR_SMALL_MAX_N) {
             rc = validate_probabilities(&gs[i]);
-            if (!rc && (o.order == NR_ORDER_LEARNED || o.branch_order == NR_BORDER_LEARNED))
-                rc = NR_ERR_UNSUPPORTED;    // learned order and branch order: n <= 32 only
+            // the learned queue order: n <= 32 only; the learned branch order: in the bucketed
+            // whole-GPU queue (max-mass order) only
+            const bool buckets = o.bucket_shift >= 0 &&
+                                 (o.order == NR_ORDER_MAXMASS || (o.order == NR_ORDER_AUTO && o.target_width > 0));
+            if (!rc && (o.order == NR_ORDER_LEARNED || (o.branch_order == NR_BORDER_LEARNED && !buckets)))
+                rc = NR_ERR_UNSUPPORTED;
             wide.fetch_add(1);
         }
         if (rc) bad.store(rc);

@@ -32,6 +32,7 @@
 #pragma once
 
 #include "nr_expand.cuh"
+#include "nr_mlp.cuh"
 
 #define NR_WIDE_MAX_N 16384     // arcs carry a 14-bit head; parents pack (node << 16 | edge)
 #define NR_WIDE_MAX_W4 16       // widest mask with a compiled width; wider masks run the
@@ -118,6 +119,7 @@ struct NrBucketWideParams {
     unsigned long long *stats;      // [0] widest wave, [1] records queued at the end
     int fork;                       // 1: fork branching on the most reliable path edge
     int border;                     // NR_BORDER_*: the order a path's UNKNOWN edges are branched in
+    NrMlpDev mlp;                   // the learned branch order's scorer (the LEARN instantiation)
     // resume from a checkpoint: the arena holds its queue and block 0's first lane starts from
     // its sums and counts (the stop test before the first wave sees them through the shares)
     int resume;
@@ -561,9 +563,106 @@ __device__ __forceinline__ void nr_wide_branch_order(uint32_t *hops, int L, int 
     }
 }
 
+// The learned branch order's scorer in a whole-GPU kernel: the weights, and the warp's scratch
+// (nr_mlp_score_lanes: BF16 tiles, 16 outputs) in shared memory.
+struct NrWideLearn {
+    NrMlpDev M;
+    uint32_t *scratch;
+    float *y;
+};
+
+// Learned branch order of a path held dst side first in hops[0..L) (all lanes): the scorer
+// estimates the residual reliability r of the subproblem with each UNKNOWN hop down (the
+// features of the lane-group kernel's learned order: that child's edge-state fractions, the path
+// length and the hop's place on it, p, the not-down degrees of src and dst less the hop, the
+// masses, n and E), and the hops are branched largest (1 - p) x (1 - r) first -- a likely and
+// critical failure first; ties keep path order (src side first); known hops go last (they make
+// no child).  Keys go to v.order and the reordered hops through v.list (free after the search).
+__device__ __forceinline__ void nr_wide_learned_order(const NrWideGraph &g, const NrWideView &v, uint32_t *hops,
+                                                      int L, double mass, const NrWideLearn &W)
+{
+    constexpr uint32_t HM = (1u << NR_WIDE_HEAD_BITS) - 1u;
+    const int lane = threadIdx.x & 31;
+    const int n = g.n, E = g.e, src = g.src, dst = g.dst;
+    const uint32_t *m = v.m;
+    // the parent's UNKNOWN and up edges (mask bits past edge E-1 are padding)
+    int unk = 0, up = 0;
+    for (int k = lane; k < 4 * g.w4 && 16 * k < E; k += 32) {
+        const int valid = min(16, E - 16 * k);
+        const uint32_t vm = valid >= 16 ? 0x55555555u : ((1u << (2 * valid)) - 1u) & 0x55555555u;
+        const uint32_t w = m[k], lo = w & vm, hi = (w >> 1) & vm;
+        unk += __popc(lo & hi);
+        up += __popc(lo & ~hi);
+    }
+    unk = __reduce_add_sync(NR_FULL, unk);
+    up = __reduce_add_sync(NR_FULL, up);
+    // not-down degrees of src and dst (their arc lists: in- or out-arcs, the same on undirected graphs)
+    int ds = 0, dd = 0;
+    for (int j = v.row[src] + lane; j < v.row[src + 1]; j += 32) {
+        const uint32_t e = v.arc[j] >> NR_WIDE_HEAD_BITS;
+        ds += (m[e >> 4] >> ((e & 15) << 1)) & 1u;
+    }
+    for (int j = v.row[dst] + lane; j < v.row[dst + 1]; j += 32) {
+        const uint32_t e = v.arc[j] >> NR_WIDE_HEAD_BITS;
+        dd += (m[e >> 4] >> ((e & 15) << 1)) & 1u;
+    }
+    ds = __reduce_add_sync(NR_FULL, ds);
+    dd = __reduce_add_sync(NR_FULL, dd);
+    (void)HM;
+    float *key = reinterpret_cast<float *>(v.order);
+    const float inv_e = E > 0 ? 1.f / (float)E : 0.f, inv_n1 = n > 1 ? 1.f / (float)(n - 1) : 0.f;
+    for (int c = 0; c < L; c += 32) {
+        const int k = c + lane;
+        const uint32_t e = k < L ? hops[k] : 0u;
+        const bool has = k < L && ((m[e >> 4] >> ((e & 15) << 1)) & 3u) == 3u;
+        float f[NR_MLP_IN];
+        const double pe = has ? v.p[e] : 0.0;
+        const int pos = L - 1 - k;                          // place on the path, src side first
+        {
+            const double cm = mass * (1.0 - pe);
+            const int dsx = ds - (pos == 0 ? 1 : 0), ddx = dd - (pos == L - 1 ? 1 : 0);
+            f[0] = cm > 0.0 ? log2f((float)cm) * (1.f / 64.f) : -16.f;
+            f[1] = (unk - 1) * inv_e;
+            f[2] = up * inv_e;
+            f[3] = (E - unk - up + 1) * inv_e;
+            f[4] = (float)L / (float)n;
+            f[5] = (float)(pos + 1) / (float)L;
+            f[6] = (float)pe;
+            f[7] = dsx * inv_n1;
+            f[8] = ddx * inv_n1;
+            f[9] = min(dsx, ddx) * inv_n1;
+            f[10] = mass > 0.0 ? log2f((float)mass) * (1.f / 64.f) : -16.f;
+            f[11] = n * (1.f / 64.f);
+            f[12] = E * (1.f / 512.f);
+            f[13] = 0.f;
+            f[14] = 0.f;
+            f[15] = 1.f;
+        }
+        const float r = nr_mlp_score_lanes(W.M, W.scratch, W.y, has, f);
+        if (k < L) key[k] = has ? (1.f - (float)pe) * (1.f - r) : -1.f;
+    }
+    __syncwarp();
+    // rank of hop k: the hops with a larger key, or an equal key nearer src, go first; the walk
+    // branches hops[L-1] first, so rank r goes to hops[L-1-r]
+    uint32_t *nh = v.list;
+    for (int k = lane; k < L; k += 32) {
+        const float kk = key[k];
+        int r = 0;
+        for (int j = 0; j < L; ++j) {
+            const float kj = key[j];
+            r += (kj > kk || (kj == kk && j > k)) ? 1 : 0;  // j > k: nearer src
+        }
+        nh[L - 1 - r] = hops[k];
+    }
+    __syncwarp();
+    for (int k = lane; k < L; k += 32) hops[k] = nh[k];
+    __syncwarp();
+}
+
 template <int W4>
 __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideView &v, double mass, double eps,
-                                             const NrWideOut &O, NrWideAcc &A, bool fork = false, int border = 0)
+                                             const NrWideOut &O, NrWideAcc &A, bool fork = false, int border = 0,
+                                             const NrWideLearn *learn = nullptr)
 {
     constexpr int NW = 4 * W4;
     const int lane = threadIdx.x & 31;
@@ -594,7 +693,8 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
     }
     if (g.bitset) {
         L = nr_wide_path_bits(g, v, hops);
-        if (lane == 0 && border != NR_BORDER_SRC && L > 1) nr_wide_branch_order(hops, L, border, v.p);
+        if (lane == 0 && border != NR_BORDER_SRC && border != NR_BORDER_LEARNED && L > 1)
+            nr_wide_branch_order(hops, L, border, v.p);
     } else if (lane == 0) {
         if (g.nk) {
             // K-terminal: the tree of the terminals' parent paths to src (marked in NF), its
@@ -624,11 +724,13 @@ __device__ __forceinline__ void nr_wide_step(const NrWideGraph &g, const NrWideV
                 x = (int)(pe >> 16);
             }
             L = h;
-            if (border != NR_BORDER_SRC && L > 1) nr_wide_branch_order(hops, L, border, v.p);
+            if (border != NR_BORDER_SRC && border != NR_BORDER_LEARNED && L > 1)
+                nr_wide_branch_order(hops, L, border, v.p);
         }
     }
     L = __shfl_sync(NR_FULL, L, 0);
     __syncwarp();
+    if (learn && border == NR_BORDER_LEARNED && L > 1 && !g.nk) nr_wide_learned_order(g, v, hops, L, mass, *learn);
     if (fork) {
         // the pivot: largest p among the UNKNOWN hops, the nearest dst (lowest index) on ties
         double bp = -1.0;
@@ -1068,8 +1170,12 @@ __device__ __forceinline__ bool nr_bucket_compact(const NrBucketWideParams &P, u
     return nr_grid_sync(P.bar_count, P.bar_gen, P.status, P.timeout_ns);
 }
 
-template <int W4>
-__global__ void __launch_bounds__(NR_WIDE_BLOCK, 6) nr_bucket_wide_kernel(NrBucketWideParams P)
+// per warp, after the block's search scratch: the scorer's tiles and outputs (LEARN)
+#define NR_WIDE_LEARN_WORDS (NR_MLP_WARP_WORDS + 16)
+
+// LEARN: the learned branch order (NR_BORDER_LEARNED), with the scorer's scratch per warp.
+template <int W4, bool LEARN = false>
+__global__ void __launch_bounds__(NR_WIDE_BLOCK, LEARN ? 3 : 6) nr_bucket_wide_kernel(NrBucketWideParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_hist[NR_WIDE_MAX_NB + 1];
@@ -1077,6 +1183,14 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK, 6) nr_bucket_wide_kernel(NrBuck
     if (!g.tables_global) nr_stage_blob(smem, P.blob, g.blob_bytes);
     __syncthreads();
     const NrWideView v = nr_wide_view(smem, P.blob, g);
+    NrWideLearn W;
+    if constexpr (LEARN) {
+        uint32_t *ls = reinterpret_cast<uint32_t *>(smem + nr_wide_block_shm(g, (int)(blockDim.x >> 5))) +
+                       (size_t)(threadIdx.x >> 5) * NR_WIDE_LEARN_WORDS;
+        W.M = P.mlp;
+        W.scratch = ls;
+        W.y = reinterpret_cast<float *>(ls + NR_MLP_WARP_WORDS);
+    }
     const int w4 = W4 ? W4 : g.w4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -1144,7 +1258,7 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK, 6) nr_bucket_wide_kernel(NrBuck
             nr_wide_load_mask(v.m, P.mask + s * w4, w4);
             const double mass = __ldcg(P.mass + s);
             __syncwarp();
-            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0, P.border);
+            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0, P.border, LEARN ? &W : nullptr);
         }
         __syncthreads();
         for (int b = threadIdx.x; b < P.nb; b += blockDim.x)

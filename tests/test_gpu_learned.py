@@ -175,3 +175,32 @@ def test_branch_order_measured(L, engine_lib, family, capsys):
         print(f"\n[{family}] subproblems to the bound over {len(gs)} instances, max-mass queue: "
               + ", ".join(f"{b} {n}" for b, n in counts.items())
               + f" (learned / src {counts['learned'] / counts['src']:.3f})")
+
+
+def test_learned_branch_order_on_large_graphs(L, engine_lib):
+    """Graphs above 32 nodes take the learned branch order in the bucketed whole-GPU queue: each
+    run stops at its target or budget, and its bracket contains the value a tight plain run
+    brackets, with the trained and with random parameters; a batch of them gives the same
+    results; breadth-first waves refuse it (NR_ERR_UNSUPPORTED)."""
+    import os
+    from relaibilitygpu_gb300 import graphs
+    cases = [graphs.rgg(40, 80, p_range=(0.85, 0.99), seed=11), graphs.rgg(60, 150, p_range=(0.9, 0.99), seed=12),
+             graphs.grid(6, 6, p_range=(0.8, 0.99), seed=13), graphs.complete(40, p_range=(0.9, 0.99), seed=14)]
+    ends = [(g.src, g.dst) if g.n_nodes != 40 or g.n_edges == 80 else (0, 39) for g in cases]
+    kw = dict(order="maxmass", bucket_shift=2, n_buckets=255, capacity=1 << 22)
+    with engine_lib.Context(0) as ctx:
+        tight = [ctx.reliability(g, s, t, target_width=1e-9, max_nodes=3_000_000, **kw) for g, (s, t) in zip(cases, ends)]
+        for params in ([L.load()] if os.path.exists(L.DEFAULT_MODEL) else []) + [L.init_params(4)]:
+            L.set_model(ctx, params)
+            one = []
+            for g, (s, t), ref in zip(cases, ends, tight):
+                r = ctx.reliability(g, s, t, target_width=1e-5, max_nodes=500_000, branch_order="learned", **kw)
+                assert r.engine == "grid" and r.stop in (1, 3) and (r.esp <= 1e-5 or r.stop == 3)
+                assert max(r.R, ref.R) <= min(r.R + r.esp, ref.R + ref.esp) + 1e-15
+                one.append(r)
+            res = ctx.reliability_batch(cases, [s for s, _ in ends], [t for _, t in ends], target_width=1e-5,
+                                        max_nodes=500_000, branch_order="learned", **kw)
+            for a, b in zip(res, one):
+                assert (a.R, a.esp, a.nodes, a.iterations, a.queued) == (b.R, b.esp, b.nodes, b.iterations, b.queued)
+        with pytest.raises(engine_lib.NrError):
+            ctx.reliability(cases[0], ends[0][0], ends[0][1], target_width=1e-5, order="waves", branch_order="learned")
