@@ -103,7 +103,7 @@ __device__ __forceinline__ void nr_child_features(float (&f)[NR_FEAT], const uin
         up += __popc(lo & ~hi);
     }
     const float inv_e = E > 0 ? 1.f / (float)E : 0.f, inv_n1 = n > 1 ? 1.f / (float)(n - 1) : 0.f;
-    f[0] = cm > 0.0 ? log2f((float)cm) * (1.f / 64.f) : -16.f;
+    f[0] = cm > 0.0 ? fmaxf(log2f((float)cm) * (1.f / 64.f), -16.f) : -16.f;   // below FLT_MIN: -16
     f[1] = unk * inv_e;
     f[2] = up * inv_e;
     f[3] = (E - unk - up) * inv_e;
@@ -113,7 +113,7 @@ __device__ __forceinline__ void nr_child_features(float (&f)[NR_FEAT], const uin
     f[7] = deg_s * inv_n1;
     f[8] = deg_d * inv_n1;
     f[9] = min(deg_s, deg_d) * inv_n1;
-    f[10] = mass > 0.0 ? log2f((float)mass) * (1.f / 64.f) : -16.f;
+    f[10] = mass > 0.0 ? fmaxf(log2f((float)mass) * (1.f / 64.f), -16.f) : -16.f;
     f[11] = n * (1.f / 64.f);
     f[12] = E * (1.f / 512.f);
     f[13] = 0.f;
@@ -250,7 +250,8 @@ __device__ __forceinline__ void nr_expand(const NrSmallGraph &g, const NrSmemGra
                 const int dd = __popc(rd) - ((hop_u == dst || hop_v == dst) ? 1 : 0);
                 float hf[NR_FEAT];
                 nr_child_features<W4>(hf, wh, unk ? mass * (1.0 - p_h) : 0.0, mass, L, v, p_h, ds, dd, n, g.e);
-                const float r = (*hop_score)(unk, hf);
+                float r = (*hop_score)(unk, hf);
+                r = (r >= 0.f) ? fminf(r, 1.f) : 0.f;  // a NaN estimate must not break the ranking
                 key = (double)((1.f - (float)p_h) * (1.f - r));
                 desc = true;
             }

@@ -621,7 +621,7 @@ __device__ __forceinline__ void nr_wide_learned_order(const NrWideGraph &g, cons
         {
             const double cm = mass * (1.0 - pe);
             const int dsx = ds - (pos == 0 ? 1 : 0), ddx = dd - (pos == L - 1 ? 1 : 0);
-            f[0] = cm > 0.0 ? log2f((float)cm) * (1.f / 64.f) : -16.f;
+            f[0] = cm > 0.0 ? fmaxf(log2f((float)cm) * (1.f / 64.f), -16.f) : -16.f;   // below FLT_MIN: -16
             f[1] = (unk - 1) * inv_e;
             f[2] = up * inv_e;
             f[3] = (E - unk - up + 1) * inv_e;
@@ -631,14 +631,15 @@ __device__ __forceinline__ void nr_wide_learned_order(const NrWideGraph &g, cons
             f[7] = dsx * inv_n1;
             f[8] = ddx * inv_n1;
             f[9] = min(dsx, ddx) * inv_n1;
-            f[10] = mass > 0.0 ? log2f((float)mass) * (1.f / 64.f) : -16.f;
+            f[10] = mass > 0.0 ? fmaxf(log2f((float)mass) * (1.f / 64.f), -16.f) : -16.f;
             f[11] = n * (1.f / 64.f);
             f[12] = E * (1.f / 512.f);
             f[13] = 0.f;
             f[14] = 0.f;
             f[15] = 1.f;
         }
-        const float r = nr_mlp_score_lanes(W.M, W.scratch, W.y, has, f);
+        float r = nr_mlp_score_lanes(W.M, W.scratch, W.y, has, f);
+        r = (r >= 0.f) ? fminf(r, 1.f) : 0.f;            // a NaN estimate must not break the ranking
         if (k < L) key[k] = has ? (1.f - (float)pe) * (1.f - r) : -1.f;
     }
     __syncwarp();
