@@ -76,7 +76,7 @@ enum {
     NR_SMALL_AUTO = 0,      /* one lane per subproblem where it applies (undirected simple graphs of
                                <= 16 nodes, path branching, plain order; <= 32 nodes in breadth-first
                                waves with two instances a warp; and the whole-GPU wave engine for
-                               <= 16 nodes), lane groups elsewhere */
+                               <= 32 nodes), lane groups elsewhere */
     NR_SMALL_GROUP = 1,     /* a lane group (one lane per node) per subproblem for every instance,
                                in the warp engine and in the whole-GPU engine for <= 32 nodes */
     NR_SMALL_LANE1 = 2      /* where one lane per subproblem applies, one instance per warp (with one
@@ -174,7 +174,7 @@ typedef struct nr_result {
     uint64_t d2h_bytes;         /* device -> host bytes copied by this call */
     int32_t  stop;              /* 0 queue empty, 1 target width met, 3 pop budget reached */
     int32_t  kernel;            /* warp engine: NR_KERNEL_GROUP, NR_KERNEL_LANE or NR_KERNEL_LANE2;
-                                   whole-GPU engine for <= 16 nodes: NR_KERNEL_LANE when one lane
+                                   whole-GPU engine for <= 32 nodes: NR_KERNEL_LANE when one lane
                                    per subproblem ran; 0 otherwise */
     int32_t  reserved[2];
 } nr_result;

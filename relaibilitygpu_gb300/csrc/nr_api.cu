@@ -379,17 +379,19 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     const int G = group_width(g->n_nodes);
     const int W4 = sg.w4;
     if (W4 > NR_MAX_W4) return NR_ERR_UNSUPPORTED;
-    // one lane per subproblem (nr_grid_lane.cuh) on undirected simple graphs of <= 16 nodes with
-    // path branching, unless the lane groups are asked for
+    // one lane per subproblem (nr_grid_lane.cuh) on undirected simple graphs with path branching,
+    // unless the lane groups are asked for: graphs of <= 16 nodes
+    // (16-bit rows), or of <= 32 nodes (32-bit rows)
+    const int rb = g->n_nodes <= NR_LANE_MAX_N ? 16 : 32;
     const bool lane = o->branching != NR_BRANCH_FORK && o->small_kernel != NR_SMALL_GROUP &&
-                      g->n_nodes <= NR_LANE_MAX_N && W4 <= NR_LANE_MAX_W4 && rows_mode_of(g) == 1 &&
+                      W4 <= (rb == 16 ? NR_LANE_MAX_W4 : NR_LANE32_MAX_W4) && rows_mode_of(g) == 1 &&
                       cap <= 0x7fffffffull;
-    const void *kfn = lane ? nr_grid_lane_kernel_ptr(W4) : grid_kernel(G, W4, o->branching == NR_BRANCH_FORK);
+    const void *kfn = lane ? nr_grid_lane_kernel_ptr(W4, rb) : grid_kernel(G, W4, o->branching == NR_BRANCH_FORK);
     if (!kfn) return NR_ERR_UNSUPPORTED;
 
     const int block = NR_BLOCK_THREADS;
     const int warps = block / 32;
-    const size_t smem = lane ? nr_grid_lane_shm_bytes(sg.blob_bytes, warps)
+    const size_t smem = lane ? nr_grid_lane_shm_bytes(sg.blob_bytes, warps, rb)
                              : (size_t)sg.blob_bytes + (size_t)warps * (32 / G) * 4 * W4 * sizeof(uint32_t);
     NR_CUDA_TRY(nr_smem_limit(c->device, kfn, smem));
     int bps = 0;
@@ -398,7 +400,7 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     if (o->blocks_per_sm > 0 && o->blocks_per_sm < bps) bps = o->blocks_per_sm;
     const int grid = bps * c->sms;
 
-    const size_t row_bytes = lane ? 4 * (size_t)NR_LANE_ROW_WORDS : 0;    // rows carried in the records
+    const size_t row_bytes = lane ? (rb == 16 ? 4 * (size_t)NR_LANE_ROW_WORDS : 128) : 0;   // rows in the records
     const size_t item_bytes = (size_t)W4 * 16 + sizeof(double) + row_bytes;
     const size_t mask_bytes = align16((size_t)cap * W4 * 16);
     const size_t mass_bytes = align16((size_t)cap * sizeof(double));
@@ -455,16 +457,17 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     NR_CUDA_TRY(cudaMemcpyAsync(P.mask[0], root.data(), 16 * W4, cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaMemcpyAsync(P.mass[0], &one, sizeof(one), cudaMemcpyHostToDevice, s));
     // the root's not-down rows (lane kernel): node v's in-neighbours over edges with p > 0, two
-    // 16-bit rows a word
-    uint32_t root_rows[NR_LANE_ROW_WORDS] = {0};
+    // 16-bit rows a word, or one 32-bit row a word
+    uint32_t root_rows[32] = {0};
     if (lane) {
         for (int u = 0; u < g->n_nodes; ++u)
             for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j)
                 if (g->edge_p[g->edge_id[j]] > 0.0) {
                     const int v = g->col_idx[j];
-                    root_rows[v >> 1] |= 1u << (u + ((v & 1) << 4));
+                    if (rb == 16) root_rows[v >> 1] |= 1u << (u + ((v & 1) << 4));
+                    else root_rows[v] |= 1u << u;
                 }
-        NR_CUDA_TRY(cudaMemcpyAsync(P.rows[0], root_rows, sizeof(root_rows), cudaMemcpyHostToDevice, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(P.rows[0], root_rows, row_bytes, cudaMemcpyHostToDevice, s));
     }
 
     void *args[] = {&P};
@@ -517,7 +520,7 @@ int run_grid_small(nr_context *c, const nr_graph *g, int src, int dst, uint64_t 
     r->grid_blocks = grid;
     r->block_threads = block;
     r->capacity = cap;
-    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one) + (lane ? sizeof(root_rows) : 0);
+    r->h2d_bytes = blob.size() + sizeof(one_u) + 16 * W4 + sizeof(one) + row_bytes;
     r->d2h_bytes = sizeof(unsigned long long) * wc.size() + sizeof(NrPartial) * grid + sizeof(int);
     if (status & NR_DEV_ERR_TIMEOUT) return NR_ERR_TIMEOUT;
     if (status) return NR_ERR_INTERNAL;

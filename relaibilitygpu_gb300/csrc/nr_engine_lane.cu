@@ -13,8 +13,21 @@ const void *nr_lane_kernel_ptr(int w4)
     }
 }
 
-const void *nr_grid_lane_kernel_ptr(int w4)
+const void *nr_grid_lane_kernel_ptr(int w4, int row_bits)
 {
+    if (row_bits == 32) {
+        switch (w4) {
+        case 1: return (const void *)nr_grid_lane_kernel<1, 32>;
+        case 2: return (const void *)nr_grid_lane_kernel<2, 32>;
+        case 3: return (const void *)nr_grid_lane_kernel<3, 32>;
+        case 4: return (const void *)nr_grid_lane_kernel<4, 32>;
+        case 5: return (const void *)nr_grid_lane_kernel<5, 32>;
+        case 6: return (const void *)nr_grid_lane_kernel<6, 32>;
+        case 7: return (const void *)nr_grid_lane_kernel<7, 32>;
+        case 8: return (const void *)nr_grid_lane_kernel<8, 32>;
+        default: return nullptr;
+        }
+    }
     switch (w4) {
     case 1: return (const void *)nr_grid_lane_kernel<1>;
     case 2: return (const void *)nr_grid_lane_kernel<2>;

@@ -1,5 +1,6 @@
 // nr_grid_lane.cuh -- whole-GPU wave engine with one lane per subproblem, for one
-// undirected simple graph of up to 16 nodes (path branching).
+// undirected simple graph of up to 16 nodes (16-bit rows, RB = 16) or up to 32 nodes (32-bit
+// rows, RB = 32: 128 B of rows a record), path branching.
 //
 // nr_grid_kernel spreads a subproblem over a lane group (a lane per node: the
 // not-down rows rebuilt from the mask, one ballot per BFS level), two K10
@@ -21,18 +22,18 @@
 
 #include "nr_lane.cuh"
 
-// shared memory: the staged graph tables, then per warp the lanes' rows [8][32] and hops [16][32]
-__host__ __device__ inline size_t nr_grid_lane_shm_bytes(int blob_bytes, int warps)
+// shared memory: the staged graph tables, then per warp the lanes' rows [RW][32] and hops [RB][32]
+__host__ __device__ inline size_t nr_grid_lane_shm_bytes(int blob_bytes, int warps, int rb = 16)
 {
     return (((size_t)blob_bytes + 15) & ~size_t(15)) +
-           (size_t)warps * (NR_LANE_ROW_WORDS + NR_LANE_MAX_N) * 32 * sizeof(uint32_t);
+           (size_t)warps * ((rb == 16 ? 8 : 32) + rb) * 32 * sizeof(uint32_t);
 }
 
-template <int W4>
+template <int W4, int RB = 16>
 __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_lane_kernel(NrGridParams P)
 {
     constexpr int NW = 4 * W4;
-    constexpr int RW = NR_LANE_ROW_WORDS;
+    constexpr int RW = nr_lane_rw<RB>();
     extern __shared__ __align__(16) unsigned char smem[];
     const NrSmallGraph g = P.g;
     nr_stage_blob(smem, P.blob, g.blob_bytes);
@@ -42,7 +43,7 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_lane_kernel(NrGridPa
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t *my_rows = reinterpret_cast<uint32_t *>(smem + ((g.blob_bytes + 15) & ~15)) +
-                        (size_t)warp * (RW + NR_LANE_MAX_N) * 32 + lane;     // word k at my_rows[32 k]
+                        (size_t)warp * (RW + RB) * 32 + lane;                // word k at my_rows[32 k]
     uint32_t *my_hop = my_rows + RW * 32;                                      // level l at my_hop[32 l]
     const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const unsigned long long TW = (unsigned long long)gridDim.x * (blockDim.x >> 5);
@@ -69,7 +70,10 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_lane_kernel(NrGridPa
         for (unsigned long long base = gw * 32; base < n_in; base += TW * 32) {
             const unsigned long long idx = base + lane;
             const bool valid = idx < n_in;
-            uint32_t wc[NW], rw[RW];
+            // 16-bit rows stay in registers too (the child writes copy them); 32-bit rows go
+            // straight to the lane's shared-memory column
+            constexpr int RWR = RB == 16 ? RW : 1;
+            uint32_t wc[NW], rw[RWR];
             double mass = 0.0;
             if (valid) {
 #pragma unroll
@@ -80,17 +84,28 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_lane_kernel(NrGridPa
 #pragma unroll
                 for (int k = 0; k < RW / 4; ++k) {
                     const uint4 q = __ldcg(in_rows + idx * (RW / 4) + k);
-                    rw[4 * k] = q.x; rw[4 * k + 1] = q.y; rw[4 * k + 2] = q.z; rw[4 * k + 3] = q.w;
+                    if constexpr (RB == 16) {
+                        rw[4 * k] = q.x; rw[4 * k + 1] = q.y; rw[4 * k + 2] = q.z; rw[4 * k + 3] = q.w;
+                    } else {
+                        my_rows[32 * (4 * k)] = q.x; my_rows[32 * (4 * k + 1)] = q.y;
+                        my_rows[32 * (4 * k + 2)] = q.z; my_rows[32 * (4 * k + 3)] = q.w;
+                    }
                 }
                 mass = __ldcg(in_mass + idx);
             } else {
 #pragma unroll
                 for (int k = 0; k < NW; ++k) wc[k] = 0u;
 #pragma unroll
-                for (int k = 0; k < RW; ++k) rw[k] = 0u;
-            }
+                for (int k = 0; k < RWR; ++k) rw[k] = 0u;
+                if constexpr (RB == 32) {
 #pragma unroll
-            for (int k = 0; k < RW; ++k) my_rows[32 * k] = rw[k];
+                    for (int k = 0; k < RW; ++k) my_rows[32 * k] = 0u;
+                }
+            }
+            if constexpr (RB == 16) {
+#pragma unroll
+                for (int k = 0; k < RW; ++k) my_rows[32 * k] = rw[k];
+            }
             __syncwarp();
 
             bool active = valid;
@@ -104,13 +119,13 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_lane_kernel(NrGridPa
             }
             bool live;
             int nch, bad;
-            const int L = nr_lane_path(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
+            const int L = nr_lane_path<NW, RB>(my_rows, my_hop, wc, eid, n, ge, src, dst, active, live, nch, bad);
             if (bad) {                                      // an internal check failed: no children
                 atomicOr(P.status, NR_DEV_ERR_BOUNDS);
                 nch = 0;
                 live = false;
             }
-            if (P.border != NR_BORDER_SRC && L > 1 && !bad) nr_lane_branch_order(my_hop, L, P.border, pt);
+            if (P.border != NR_BORDER_SRC && L > 1 && !bad) nr_lane_branch_order<RB>(my_hop, L, P.border, pt);
             if (active && !live && !bad) acc.dead++;
 
             // the warp's children take one range of the next wave's slots
@@ -128,7 +143,7 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_lane_kernel(NrGridPa
             double Pm = mass;
             for (int h = 0; h < L && !bad; ++h) {
                 const uint32_t hp = my_hop[32 * h];
-                const int e = NR_HOP_E(hp);
+                const int e = nr_hop_e<RB>(hp);
                 const int ew = e >> 4;
                 const uint32_t wv = nr_pick(wc, ew);
                 if (((wv >> ((e & 15) << 1)) & 3u) != 3u) continue;     // only UNKNOWN hops branch
@@ -136,8 +151,12 @@ __global__ void __launch_bounds__(NR_BLOCK_THREADS) nr_grid_lane_kernel(NrGridPa
                 const double cm = __dmul_rn(Pm, __dsub_rn(1.0, pe));
                 Pm = __dmul_rn(Pm, pe);
                 if (q < cap) {
-                    nr_lane_write_child<W4>(out_mask, out_rows, out_mass, (int)q, wc, rw, my_rows, e, wv,
-                                            NR_HOP_U(hp), NR_HOP_X(hp), cm);
+                    if constexpr (RB == 16)
+                        nr_lane_write_child<W4>(out_mask, out_rows, out_mass, (int)q, wc, rw, my_rows, e, wv,
+                                                nr_hop_u<RB>(hp), nr_hop_x<RB>(hp), cm);
+                    else
+                        nr_lane_write_child32<W4>(out_mask, out_rows, out_mass, (int)q, wc, my_rows, e, wv,
+                                                  nr_hop_u<RB>(hp), nr_hop_x<RB>(hp), cm);
                 } else {                                    // queue full: mass to ESP (main.cu:245-252)
                     acc.spilled++;
                     nr_fix_add_mass(acc.es, cm);

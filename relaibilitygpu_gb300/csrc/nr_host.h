@@ -49,7 +49,7 @@ const void *nr_warp_fork_kernel_ptr_g32(int w4);
 const void *nr_warp_learn_kernel_ptr_g16(int w4);
 const void *nr_warp_learn_kernel_ptr_g32(int w4);
 const void *nr_lane_kernel_ptr(int w4);
-const void *nr_grid_lane_kernel_ptr(int w4);
+const void *nr_grid_lane_kernel_ptr(int w4, int row_bits = 16);
 const void *nr_grid_wide_multi_kernel_ptr(int w4);
 const void *nr_bucket_wide_learn_kernel_ptr(int w4);
 int run_grid_wide_multi(nr_context *c, const std::vector<int> &idx, const nr_graph *gs, const int32_t *srcs,

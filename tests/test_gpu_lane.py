@@ -271,3 +271,31 @@ def test_whole_gpu_lane_kernel(ctx, oracle):
     r = ctx.reliability(g, 0, 8, capacity=2000)
     assert r.kernel == "lane" and r.spilled > 0
     assert r.R <= exact.R + 1e-15 and exact.R <= r.R + r.esp + 1e-12
+
+
+def test_whole_gpu_lane_kernel_32_bit_rows(ctx, oracle):
+    """17..32-node undirected simple graphs in the whole-GPU wave engine take one lane per
+    subproblem with 32-bit rows: exhaustive and eps-truncated runs, branch orders, certain edges;
+    every count, wave and exact sum equals the lane-group version's and the oracle's."""
+    from relaibilitygpu_gb300 import graphs
+    g5 = graphs.grid(4, 5, p_range=(0.8, 0.99), seed=21)
+    p = g5.edge_p.copy(); p[2] = 0.0; p[9] = 1.0
+    cases = [(graphs.grid(4, 5, p=0.9), 0, 19), (graphs.grid(3, 6, p_range=(0.7, 0.99), seed=22), 0, 17),
+             (graphs.gnm(20, 34, p_range=(0.8, 0.99), seed=1), None, None),
+             (graphs.from_edges(20, g5.edge_list(), p), 0, 19),
+             (graphs.complete(20, p_range=(0.3, 0.7), seed=23), 0, 19)]
+    for g, s, t in cases:
+        s = g.src if s is None else s
+        t = g.dst if t is None else t
+        runs = ((0.0, "src"), (1e-7, "p_asc")) if g.n_edges < 100 else ((1e-9, "src"), (1e-8, "dst"))
+        for eps, border in runs:
+            a = ctx.reliability(g, s, t, capacity=1 << 22, eps=eps, branch_order=border)
+            b = ctx.reliability(g, s, t, capacity=1 << 22, eps=eps, branch_order=border, small_kernel="group")
+            assert a.engine == "grid" and a.kernel == "lane" and b.kernel == ""
+            for f in ("R", "esp", "nodes", "leaves", "dead_ends", "truncated", "spilled", "paths", "iterations",
+                      "max_queue_items"):
+                assert getattr(a, f) == getattr(b, f), (g.n_nodes, eps, border, f)
+            o = oracle.run(g, s, t, eps=eps, branch_order=border, threads=8)
+            assert (a.nodes, a.leaves, a.dead_ends, a.truncated, a.iterations, a.max_queue_items) == \
+                (o.nodes, o.leaves, o.dead, o.truncated, o.waves, o.max_wave)
+            assert a.R == o.R and a.esp == o.esp
