@@ -835,7 +835,6 @@ int run_grid_wide_multi(nr_context *c, const std::vector<int> &idx, const nr_gra
             size_t off = 0;
             std::vector<long long> boff(m);
             for (int k = 0; k < m; ++k) { boff[k] = (long long)off; off = align16(off + all[c0 + k].blob.size()); }
-            const size_t blob_total = off;
             const size_t off_g = off; off = align16(off + sizeof(NrWideGraph) * m);
             const size_t off_bo = off; off = align16(off + sizeof(long long) * m);
             const size_t off_root = off; off = align16(off + (size_t)16 * maxw4 * m);
