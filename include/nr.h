@@ -82,7 +82,8 @@ enum {
     NR_SMALL_LANE1 = 2      /* where one lane per subproblem applies, one instance per warp (with one
                                bucket the default gives a warp two instances, interleaving their steps) */
 };
-enum { NR_KERNEL_GROUP = 1, NR_KERNEL_LANE = 2, NR_KERNEL_LANE2 = 3 };
+enum { NR_KERNEL_GROUP = 1, NR_KERNEL_LANE = 2, NR_KERNEL_LANE2 = 3,
+       NR_KERNEL_BLOCK = 4 /* handed over by the two-slot kernel: one instance a block */ };
 
 /* branching of a subproblem whose optimistic BFS finds a path */
 enum {
@@ -141,7 +142,10 @@ typedef struct nr_options {
                                  per SM to hide the steps' latency, 0.096 against 0.060 ms) */
     int32_t  branch_order;    /* NR_BORDER_*: path branching only; two-terminal runs (K-terminal runs
                                  take NR_BORDER_SRC) */
-    int32_t  reserved0;
+    int32_t  handover_pages;  /* breadth-first waves, two instances a warp: an instance whose next wave
+                                 holds more than this many pages of 32 subproblems runs again from its
+                                 root on a block of warps (the block kernel), with the same schedule and
+                                 results; 0 = the default (32 pages), -1 = never */
 } nr_options;
 
 typedef struct nr_result {
@@ -173,7 +177,8 @@ typedef struct nr_result {
     uint64_t h2d_bytes;         /* host -> device bytes copied by this call */
     uint64_t d2h_bytes;         /* device -> host bytes copied by this call */
     int32_t  stop;              /* 0 queue empty, 1 target width met, 3 pop budget reached */
-    int32_t  kernel;            /* warp engine: NR_KERNEL_GROUP, NR_KERNEL_LANE or NR_KERNEL_LANE2;
+    int32_t  kernel;            /* warp engine: NR_KERNEL_GROUP, NR_KERNEL_LANE, NR_KERNEL_LANE2 or
+                                   NR_KERNEL_BLOCK;
                                    whole-GPU engine for <= 32 nodes: NR_KERNEL_LANE when one lane
                                    per subproblem ran; 0 otherwise */
     int32_t  reserved[2];

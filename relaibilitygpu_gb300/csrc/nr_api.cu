@@ -357,6 +357,8 @@ extern "C" void nr_context_destroy(nr_context *c)
         if (sl.wslab) cudaFree(sl.wslab);
         if (sl.wbuf) cudaFree(sl.wbuf);
         if (sl.hbuf) cudaFreeHost(sl.hbuf);
+        if (sl.hv_dev) cudaFree(sl.hv_dev);
+        if (sl.hv_host) cudaFreeHost(sl.hv_host);
         if (sl.ev0) cudaEventDestroy(sl.ev0);
         if (sl.ev1) cudaEventDestroy(sl.ev1);
         if (sl.stream) cudaStreamDestroy(sl.stream);

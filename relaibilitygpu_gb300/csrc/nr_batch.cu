@@ -49,6 +49,7 @@ WarpRunCfg warp_cfg(const nr_options *o, uint64_t capacity, bool exhaustive)
     w.fork = (o->branching == NR_BRANCH_FORK);
     w.step_cap = (o->test_fault == 2) ? 1 : 0;
     w.border = o->branch_order;
+    w.handover_pages = o->handover_pages < 0 ? 0 : o->handover_pages > 0 ? o->handover_pages : NR_HANDOVER_PAGES;
     w.lane = (o->small_kernel != NR_SMALL_GROUP);
     w.lane2 = (o->small_kernel == NR_SMALL_AUTO) && w.wave_mode && w.shift < 0;
     w.lane_slots = (o->lane_slots == 4) ? 4 : 2;
@@ -481,6 +482,7 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
         P.fork = cfg.fork;
         P.step_cap = cfg.step_cap;
         P.border = cfg.border;
+        P.handover_pages = (lanek && cfg.lane2) ? cfg.handover_pages : 0;
         const void *kfn = lanek ? (cfg.lane2 ? nr_lane2_kernel_ptr(W4, lane32 ? 2 : cfg.lane_slots, lane32 ? 32 : 16)
                                              : nr_lane_kernel_ptr(W4))
                                 : warp_kernel(G, W4, learn, cfg.fork != 0);
@@ -496,7 +498,124 @@ static int warp_submit(nr_context *c, NrSlot &sl, int base, int n, const nr_grap
     sl.pmat = pmat;
     sl.n = n; sl.gs = gs; sl.srcs = srcs; sl.dsts = dsts; sl.res = res;
     sl.cfgp = cfgp; sl.off_out = off_out; sl.first_grid = first_grid; sl.block = block;
+    for (int j = 0; j < NCLS; ++j) sl.nps[j] = nps[j];
     pc.mark("enqueue");
+    return NR_OK;
+}
+
+// Instances the two-slot lane kernel handed over (status 2 in breadth-first waves: a next wave
+// above cfg.handover_pages pages) run again from their roots on the block kernel, a block each,
+// from the slot's tables (still on the device); each gets wave buffers of the pages its slot
+// could hold.  ids: the part's indices.  Fills their results; *ms = the launches' device time.
+static int block_handover(nr_context *c, NrSlot &sl, const std::vector<int> &ids, float *ms)
+{
+    const NrSmallGraph *desc = sl.scratch.desc.data();
+    const std::vector<int> &cls = sl.scratch.cls;
+    const int k = (int)ids.size();
+    std::vector<int> order(ids);             // grouped by kernel class
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cls[a] < cls[b]; });
+    // staging: [work counters | descriptors | ids] then [outputs]
+    const size_t off_desc = align16(sizeof(int) * NR_NCLS);
+    const size_t off_ids = align16(off_desc + sizeof(NrSmallGraph) * k);
+    const size_t off_out = align16(off_ids + sizeof(int) * k);
+    const size_t bytes = align16(off_out + sizeof(NrWarpOut) * k);
+    int rc = ensure_host(&sl.hv_host, &sl.hv_host_bytes, bytes);
+    if (!rc) rc = ensure(&sl.hv_dev, &sl.hv_dev_bytes, bytes);
+    if (rc) return rc;
+    unsigned char *hb = static_cast<unsigned char *>(sl.hv_host), *db = static_cast<unsigned char *>(sl.hv_dev);
+    memset(hb, 0, off_desc);
+    NrSmallGraph *hd = reinterpret_cast<NrSmallGraph *>(hb + off_desc);
+    int *hid = reinterpret_cast<int *>(hb + off_ids);
+    for (int j = 0; j < k; ++j) { hd[j] = desc[order[j]]; hid[j] = j; }
+    const WarpRunCfg &cfg = sl.cfgp;
+    // launch geometry per class, and the largest slab any of them needs (one allocation, made
+    // before the first launch)
+    struct Grp { int j0, j1, w4, rb, grid, budget; const void *kfn; size_t smem; };
+    std::vector<Grp> grps;
+    size_t slab_need = 0;
+    for (int j0 = 0; j0 < k;) {
+        const int cj = cls[order[j0]];
+        int j1 = j0;
+        while (j1 < k && cls[order[j1]] == cj) ++j1;
+        if (cj < NR_LANE_CLS0) return NR_ERR_INTERNAL;       // only lane kernels hand over here
+        const bool lane32 = cj >= NR_LANE32_CLS0;
+        Grp gr;
+        gr.j0 = j0; gr.j1 = j1;
+        gr.w4 = lane32 ? cj - NR_LANE32_CLS0 + 1 : cj - NR_LANE_CLS0 + 1;
+        gr.rb = lane32 ? 32 : 16;
+        gr.kfn = nr_block_lane_kernel_ptr(gr.w4, gr.rb);
+        if (!gr.kfn) return NR_ERR_INTERNAL;
+        gr.smem = nr_block_lane_shm_bytes(gr.rb);
+        auto it = c->occupancy.find({gr.kfn, gr.smem * 64 + NR_BLOCK_LANE_WARPS});
+        int bps;
+        if (it == c->occupancy.end()) {
+            NR_CUDA_TRY(nr_smem_limit(c->device, gr.kfn, gr.smem));
+            NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gr.kfn, NR_BLOCK_LANE_THREADS, gr.smem));
+            c->occupancy[{gr.kfn, gr.smem * 64 + NR_BLOCK_LANE_WARPS}] = bps;
+        } else {
+            bps = it->second;
+        }
+        if (bps < 1) return NR_ERR_UNSUPPORTED;
+        gr.grid = std::max(1, std::min(j1 - j0, bps * c->sms));
+        gr.budget = std::max(1, sl.nps[cj] / (lane32 ? 2 : cfg.lane_slots));   // pages one slot may hold
+        slab_need = std::max(slab_need, (size_t)gr.grid * 2 * gr.budget * NR_PAGE * nr_block_lane_rec_bytes(gr.w4, gr.rb));
+        grps.push_back(gr);
+        j0 = j1;
+    }
+    rc = ensure(&sl.wslab, &sl.wslab_bytes, slab_need);
+    if (rc) return rc;
+    cudaStream_t s = sl.stream;
+    NR_CUDA_TRY(cudaMemcpyAsync(db, hb, off_out, cudaMemcpyHostToDevice, s));
+    NR_CUDA_TRY(cudaEventRecord(sl.ev0, s));
+    for (const Grp &gr : grps) {
+        const size_t cap = (size_t)gr.budget * NR_PAGE;
+        unsigned char *slab = static_cast<unsigned char *>(sl.wslab);
+        NrWarpParams P{};
+        P.blob = static_cast<const unsigned char *>(sl.wbuf);
+        P.inst = reinterpret_cast<const NrSmallGraph *>(db + off_desc) + gr.j0;
+        P.inst_id = reinterpret_cast<const int *>(db + off_ids) + gr.j0;
+        P.n_inst = gr.j1 - gr.j0;
+        P.next_inst = reinterpret_cast<int *>(db) + cls[order[gr.j0]];
+        P.slab_mask = reinterpret_cast<uint4 *>(slab);
+        P.slab_mass = reinterpret_cast<double *>(slab + (size_t)gr.grid * 2 * cap * 16 * gr.w4);
+        P.slab_rows = reinterpret_cast<uint32_t *>(slab + (size_t)gr.grid * 2 * cap * (16 * gr.w4 + 8));
+        P.pages = gr.budget;
+        P.n_buckets = cfg.n_buckets;
+        P.shift = -1;
+        P.wave_mode = 1;
+        P.eps = cfg.eps;
+        P.target = cfg.target;
+        P.target_fix = nr_fix_of(cfg.target);
+        P.max_nodes = cfg.max_nodes;
+        P.out = reinterpret_cast<NrWarpOut *>(db + off_out);
+        P.step_cap = cfg.step_cap;
+        P.border = cfg.border;
+        void *args[] = {&P};
+        NR_CUDA_TRY(nr_smem_limit(c->device, gr.kfn, gr.smem));
+        NR_CUDA_TRY(cudaLaunchKernel(gr.kfn, dim3(gr.grid), dim3(NR_BLOCK_LANE_THREADS), args, gr.smem, s));
+    }
+    NR_CUDA_TRY(cudaEventRecord(sl.ev1, s));
+    const NrWarpOut *hout = reinterpret_cast<const NrWarpOut *>(hb + off_out);
+    NR_CUDA_TRY(cudaMemcpyAsync(hb + off_out, db + off_out, sizeof(NrWarpOut) * k, cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    NR_CUDA_TRY(cudaEventElapsedTime(ms, sl.ev0, sl.ev1));
+    for (const Grp &gr : grps)
+        for (int j = gr.j0; j < gr.j1; ++j) {
+            const int i = order[j];
+            if (hout[j].status == NR_LANE_STATUS_CHECK) {
+                snprintf(g_internal, sizeof(g_internal), "block kernel check %llu failed on instance %d",
+                         (unsigned long long)hout[j].max_wave, i);
+                return NR_ERR_INTERNAL;
+            }
+            nr_result *r = &sl.res[i];
+            fill_from_warp(hout[j], cfg, desc[i].w4, r);
+            r->kernel = NR_KERNEL_BLOCK;
+            r->capacity = (uint64_t)gr.budget * NR_PAGE;
+            r->grid_blocks = gr.grid;
+            r->block_threads = NR_BLOCK_LANE_THREADS;
+            r->h2d_bytes = desc[i].blob_bytes + 2 * sizeof(NrSmallGraph) + 2 * sizeof(int);
+            r->d2h_bytes = 2 * sizeof(NrWarpOut);
+        }
     return NR_OK;
 }
 
@@ -542,9 +661,22 @@ static int warp_finish(nr_context *c, NrSlot &sl, int base, std::vector<int> *ha
             }
         return NR_ERR_INTERNAL;
     }
-    if (n_hand.load())
+    if (n_hand.load()) {
+        // breadth-first waves: the two-slot lane kernel's hand-overs run on the block kernel now;
+        // the others (exhaustive runs past a warp's budget) on the whole-GPU engine after the part
+        std::vector<int> blk;
         for (int i = 0; i < n; ++i)
-            if (hout[i].status == 2) handover->push_back(base + i);
+            if (hout[i].status == 2) {
+                if (sl.cfgp.wave_mode && sl.cfgp.lane2 && sl.scratch.cls[i] >= NR_LANE_CLS0) blk.push_back(i);
+                else handover->push_back(base + i);
+            }
+        if (!blk.empty()) {
+            float ms2 = 0.f;
+            const int rc = block_handover(c, sl, blk, &ms2);
+            if (rc) return rc;
+            for (int i = 0; i < n; ++i) sl.res[i].ms = ms + ms2;   // the part's device time
+        }
+    }
     pc.mark("results");
     return NR_OK;
 }

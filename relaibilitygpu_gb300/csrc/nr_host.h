@@ -28,6 +28,7 @@
 #include "nr_warp.cuh"
 #include "nr_lane2.cuh"
 #include "nr_grid_lane.cuh"
+#include "nr_block_lane.cuh"
 #include "nr_wide.cuh"
 #include "nr_mlp.cuh"
 
@@ -55,6 +56,7 @@ const void *nr_bucket_wide_learn_kernel_ptr(int w4);
 int run_grid_wide_multi(nr_context *c, const std::vector<int> &idx, const nr_graph *gs, const int32_t *srcs,
                         const int32_t *dsts, uint64_t cap, const nr_options *o, nr_result *res);
 const void *nr_lane2_kernel_ptr(int w4, int slots, int row_bits = 16);
+const void *nr_block_lane_kernel_ptr(int w4, int row_bits);
 int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
 
 #define NR_CUDA_TRY(call)                                                     \
@@ -142,6 +144,9 @@ struct PhaseClock {
 #define NR_LANE32_MAX_W4 8      // a simple graph on <= 32 nodes has <= 496 edges: 31 mask words
 #define NR_LANE32_CLS0 (NR_LANE_CLS0 + NR_LANE_MAX_W4)
 #define NR_NCLS (NR_LANE32_CLS0 + NR_LANE32_MAX_W4)
+// the two-slot lane kernel hands an instance to the block kernel once its next wave holds more
+// than this many pages (1024 subproblems: four block steps)
+#define NR_HANDOVER_PAGES 32
 struct NrHostBlock {
     size_t bytes;               // tables of the block's instances (16-byte multiples)
     long long last_owner_rel;   // offset in the block of its last structural part, -1 if none
@@ -173,13 +178,14 @@ struct WarpRunCfg {
     int lane_slots = 2;           // instances per warp then
     long long step_cap = 0;       // lane kernels' step bound (0: the kernels' own; tests set 1)
     int border = NR_BORDER_SRC;   // branch order of the paths' UNKNOWN edges
+    int handover_pages = 0;       // two-slot lane kernel: hand-over to the block kernel (0 = never)
     const WarpDump *dump = nullptr;
     double eps, target;
     unsigned long long max_nodes;
 };
 
 // A warp-engine batch in flight: its stream, staging, device tables and page
-// slabs.  A context has two, used in turn by nr_batch_submit, so one batch's
+// slabs.  A context has NR_SLOTS, used in turn by nr_batch_submit, so one batch's
 // tables are built on the host while the batch before runs.  (Splitting one
 // batch over both slots measured slower on 4096 K15 instances: the host passes
 // are dominated by fixed costs and two concurrent launches lengthen the span.)
@@ -194,6 +200,10 @@ struct NrSlot {
     void *wslab = nullptr;      // device: per-warp page slabs
     size_t wslab_bytes = 0;
     NrBatchScratch scratch;     // per-instance host tables (reused from call to call)
+    void *hv_host = nullptr;    // instances handed to the block kernel: pinned staging ...
+    size_t hv_host_bytes = 0;
+    void *hv_dev = nullptr;     // ... and device copies of their descriptors, ids and outputs
+    size_t hv_dev_bytes = 0;
     // the part queued by warp_submit, for warp_finish
     int n = 0;
     const nr_graph *gs = nullptr;
@@ -202,6 +212,7 @@ struct NrSlot {
     WarpRunCfg cfgp{};
     size_t off_out = 0;
     int first_grid = 0, block = 0;
+    int nps[NR_NCLS] = {0};     // pages a warp held, per kernel class
     bool matrix = false;        // one topology, the caller's probability matrix (gs[0] for every instance)
     const double *pmat = nullptr;
     size_t off_flag = 0;        // matrix batches: the NaN flag the device scan sets

@@ -294,6 +294,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             if (st < 0 && P.max_nodes && nr_warp_sum_u64r(A.nodes) >= P.max_nodes) st = 3;
             if (st < 0 && S.head < 0) st = 0;
             __syncwarp();
+            if (st < 0 && P.handover_pages > 0 && S.used > P.handover_pages) {
+                // the next wave outgrows the warp: the block kernel runs the instance again
+                finish(s, 2, 0, nr_fix_zero(), 0);
+                continue;
+            }
             if (st >= 0) {
                 if (!summed && !chain_sum()) {
                     finish(s, 0, 6, nr_fix_zero(), 0);

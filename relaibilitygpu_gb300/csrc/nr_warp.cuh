@@ -73,6 +73,9 @@ struct NrWarpParams {
     int border;                      // NR_BORDER_*: the order a path's UNKNOWN edges are branched in
     long long step_cap;              // lane kernels: steps before the self-check ends an instance
                                      // (0: NR_LANE_STEP_CAP; the failure-path tests set 1)
+    int handover_pages;              // two-slot lane kernel: an instance whose next wave holds more
+                                     // pages than this is handed over (status 2) to the block
+                                     // kernel (nr_block_lane.cuh); 0 = never
 };
 
 __device__ __forceinline__ unsigned long long nr_warp_sum_u64(unsigned long long x)

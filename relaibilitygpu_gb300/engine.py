@@ -29,7 +29,7 @@ ORDERS = {"auto": 0, "waves": 1, "maxmass": 2, "learned": 3}
 BRANCHING = {"path": 0, "fork": 1}
 BRANCH_ORDERS = {"src": 0, "dst": 1, "p_asc": 2, "p_desc": 3, "learned": 4}
 ENGINES = {1: "grid", 2: "warp"}
-KERNELS = {0: "", 1: "group", 2: "lane", 3: "lane2"}     # the warp engine's kernel
+KERNELS = {0: "", 1: "group", 2: "lane", 3: "lane2", 4: "block"}     # the warp engine's kernel
 SMALL_KERNELS = {"auto": 0, "group": 1, "lane1": 2}
 
 
@@ -54,7 +54,7 @@ class NrOptions(C.Structure):
         ("blocks_per_sm", C.c_int32), ("warps_per_block", C.c_int32), ("timeout_ms", C.c_double),
         ("verbose", C.c_int32), ("test_fault", C.c_int32), ("max_nodes", C.c_uint64),
         ("pages_per_warp", C.c_int32), ("branching", C.c_int32), ("small_kernel", C.c_int32),
-        ("lane_slots", C.c_int32), ("branch_order", C.c_int32), ("reserved0", C.c_int32),
+        ("lane_slots", C.c_int32), ("branch_order", C.c_int32), ("handover_pages", C.c_int32),
     ]
 
 
@@ -245,7 +245,7 @@ def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto
                  n_buckets: int = 256, device: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0,
                  timeout_ms: float = 60000.0, max_nodes: int = 0, pages_per_warp: int = 0, branching: str = "path",
                  small_kernel: str = "auto", lane_slots: int = 0, test_fault: int = 0,
-                 branch_order: str = "src") -> NrOptions:
+                 branch_order: str = "src", handover_pages: int = 0) -> NrOptions:
     o = NrOptions()
     lib().nr_options_default(C.byref(o))
     o.truncation_eps = float(eps)
@@ -264,6 +264,7 @@ def make_options(eps: float = 0.0, target_width: float = 0.0, order: str = "auto
     o.lane_slots = int(lane_slots)
     o.test_fault = int(test_fault)
     o.branch_order = BRANCH_ORDERS[branch_order] if isinstance(branch_order, str) else int(branch_order)
+    o.handover_pages = int(handover_pages)
     return o
 
 
@@ -277,7 +278,8 @@ def options_dict(o: NrOptions) -> dict:
                 branching={v: k for k, v in BRANCHING.items()}.get(o.branching, "path"),
                 small_kernel={v: k for k, v in SMALL_KERNELS.items()}.get(o.small_kernel, "auto"),
                 lane_slots=o.lane_slots, test_fault=o.test_fault,
-                branch_order={v: k for k, v in BRANCH_ORDERS.items()}.get(o.branch_order, "src"))
+                branch_order={v: k for k, v in BRANCH_ORDERS.items()}.get(o.branch_order, "src"),
+                handover_pages=o.handover_pages)
 
 
 def _check(rc: int) -> None:
