@@ -614,6 +614,8 @@ def main():
                     help="profiling: run one case twice (a warm-up call, then the call to capture) and exit")
     ap.add_argument("--budget", type=int, default=1_000_000, help="--case rgg200: subproblem budget")
     ap.add_argument("--arena", type=int, default=22, help="--case rgg200: log2 of the arena slots")
+    ap.add_argument("--instances", type=int, default=BATCH, help="--case uneven: instances generated")
+    ap.add_argument("--pages", type=int, default=4096, help="--case uneven: pages per warp")
     args = ap.parse_args()
     if args.case:
         run_case(args)
@@ -792,15 +794,20 @@ def run_case(args):
                     w = k15_workload()
                     opts = dict(w["opts"], warps_per_block=2, pages_per_warp=64)
                 else:
-                    gs = nr.batch_instances(BATCH, seed=0)
+                    gs = nr.batch_instances(args.instances, seed=0)
                     w = dict(graphs=[g for g in gs if g.n_nodes <= 32])
                     w["srcs"] = [g.src for g in w["graphs"]]
                     w["dsts"] = [g.dst for g in w["graphs"]]
                     opts = dict(target_width=UNEVEN_TARGET, max_nodes=UNEVEN_BUDGET, order="waves",
-                                warps_per_block=2, pages_per_warp=512)
+                                warps_per_block=4, pages_per_warp=args.pages)
                 batch = nr.Batch(w["graphs"], w["srcs"], w["dsts"])
             res = ctx.run_batch(batch, capacity=0, raw=True, **opts)
-            out = {"nodes": sum(res[i].nodes for i in range(batch.n)), "ms": res[0].ms}
+            kinds = {}
+            for i in range(batch.n):
+                kk = nr.engine.KERNELS.get(res[i].kernel, "")
+                kinds[kk] = kinds.get(kk, 0) + 1
+            out = {"nodes": sum(res[i].nodes for i in range(batch.n)), "ms": res[0].ms, "kernels": kinds,
+                   "spilled": sum(1 for i in range(batch.n) if res[i].spilled)}
         print(json.dumps({"case": args.case, "call": k, **out}), flush=True)
     ctx.close()
 

@@ -145,7 +145,7 @@ typedef struct nr_options {
     int32_t  handover_pages;  /* breadth-first waves, two instances a warp: an instance whose next wave
                                  holds more than this many pages of 32 subproblems runs again from its
                                  root on a block of warps (the block kernel), with the same schedule and
-                                 results; 0 = the default (32 pages), -1 = never */
+                                 results; 0 = the default (8 pages), -1 = never */
 } nr_options;
 
 typedef struct nr_result {

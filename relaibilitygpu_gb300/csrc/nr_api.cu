@@ -359,6 +359,11 @@ extern "C" void nr_context_destroy(nr_context *c)
         if (sl.hbuf) cudaFreeHost(sl.hbuf);
         if (sl.hv_dev) cudaFree(sl.hv_dev);
         if (sl.hv_host) cudaFreeHost(sl.hv_host);
+        for (int k = 0; k < NR_HV_STREAMS; ++k) {
+            if (sl.hv_side[k]) cudaStreamDestroy(sl.hv_side[k]);
+            if (sl.hv_join[k]) cudaEventDestroy(sl.hv_join[k]);
+        }
+        if (sl.hv_fork) cudaEventDestroy(sl.hv_fork);
         if (sl.ev0) cudaEventDestroy(sl.ev0);
         if (sl.ev1) cudaEventDestroy(sl.ev1);
         if (sl.stream) cudaStreamDestroy(sl.stream);

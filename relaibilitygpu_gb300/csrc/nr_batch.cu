@@ -512,8 +512,13 @@ static int block_handover(nr_context *c, NrSlot &sl, const std::vector<int> &ids
     const NrSmallGraph *desc = sl.scratch.desc.data();
     const std::vector<int> &cls = sl.scratch.cls;
     const int k = (int)ids.size();
-    std::vector<int> order(ids);             // grouped by kernel class
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cls[a] < cls[b]; });
+    // grouped by kernel class; in a class the largest next wave at the hand-over first, so the
+    // largest instances do not start last and leave the launch with a tail
+    const NrWarpOut *lout = reinterpret_cast<const NrWarpOut *>(static_cast<unsigned char *>(sl.hbuf) + sl.off_out);
+    std::vector<int> order(ids);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return cls[a] != cls[b] ? cls[a] < cls[b] : lout[a].queued > lout[b].queued;
+    });
     // staging: [work counters | descriptors | ids] then [outputs]
     const size_t off_desc = align16(sizeof(int) * NR_NCLS);
     const size_t off_ids = align16(off_desc + sizeof(NrSmallGraph) * k);
@@ -528,9 +533,9 @@ static int block_handover(nr_context *c, NrSlot &sl, const std::vector<int> &ids
     int *hid = reinterpret_cast<int *>(hb + off_ids);
     for (int j = 0; j < k; ++j) { hd[j] = desc[order[j]]; hid[j] = j; }
     const WarpRunCfg &cfg = sl.cfgp;
-    // launch geometry per class, and the largest slab any of them needs (one allocation, made
-    // before the first launch)
-    struct Grp { int j0, j1, w4, rb, grid, budget; const void *kfn; size_t smem; };
+    // launch geometry per class; the classes run side by side (up to NR_HV_STREAMS streams, the
+    // most work first), each in its own part of the slab, so a small class fills the large one's tail
+    struct Grp { int j0, j1, w4, rb, grid, budget; const void *kfn; size_t smem, slab_off, work; };
     std::vector<Grp> grps;
     size_t slab_need = 0;
     for (int j0 = 0; j0 < k;) {
@@ -558,18 +563,36 @@ static int block_handover(nr_context *c, NrSlot &sl, const std::vector<int> &ids
         if (bps < 1) return NR_ERR_UNSUPPORTED;
         gr.grid = std::max(1, std::min(j1 - j0, bps * c->sms));
         gr.budget = std::max(1, sl.nps[cj] / (lane32 ? 2 : cfg.lane_slots));   // pages one slot may hold
-        slab_need = std::max(slab_need, (size_t)gr.grid * 2 * gr.budget * NR_PAGE * nr_block_lane_rec_bytes(gr.w4, gr.rb));
+        gr.slab_off = slab_need;
+        slab_need += align16((size_t)gr.grid * 2 * gr.budget * NR_PAGE * nr_block_lane_rec_bytes(gr.w4, gr.rb));
+        gr.work = 0;
+        for (int j = j0; j < j1; ++j) gr.work += lout[order[j]].queued;
         grps.push_back(gr);
         j0 = j1;
     }
+    std::stable_sort(grps.begin(), grps.end(), [](const Grp &a, const Grp &b) { return a.work > b.work; });
     rc = ensure(&sl.wslab, &sl.wslab_bytes, slab_need);
     if (rc) return rc;
     cudaStream_t s = sl.stream;
+    const int nside = std::min<int>(NR_HV_STREAMS, (int)grps.size());
+    if (nside > 1) {
+        if (!sl.hv_fork) NR_CUDA_TRY(cudaEventCreateWithFlags(&sl.hv_fork, cudaEventDisableTiming));
+        for (int q = 0; q < nside; ++q) {
+            if (!sl.hv_side[q]) NR_CUDA_TRY(cudaStreamCreateWithFlags(&sl.hv_side[q], cudaStreamNonBlocking));
+            if (!sl.hv_join[q]) NR_CUDA_TRY(cudaEventCreateWithFlags(&sl.hv_join[q], cudaEventDisableTiming));
+        }
+    }
     NR_CUDA_TRY(cudaMemcpyAsync(db, hb, off_out, cudaMemcpyHostToDevice, s));
     NR_CUDA_TRY(cudaEventRecord(sl.ev0, s));
-    for (const Grp &gr : grps) {
+    if (nside > 1) {
+        NR_CUDA_TRY(cudaEventRecord(sl.hv_fork, s));
+        for (int q = 0; q < nside; ++q) NR_CUDA_TRY(cudaStreamWaitEvent(sl.hv_side[q], sl.hv_fork, 0));
+    }
+    for (size_t gi = 0; gi < grps.size(); ++gi) {
+        const Grp &gr = grps[gi];
         const size_t cap = (size_t)gr.budget * NR_PAGE;
-        unsigned char *slab = static_cast<unsigned char *>(sl.wslab);
+        unsigned char *slab = static_cast<unsigned char *>(sl.wslab) + gr.slab_off;
+        cudaStream_t gs_ = nside > 1 ? sl.hv_side[gi % nside] : s;
         NrWarpParams P{};
         P.blob = static_cast<const unsigned char *>(sl.wbuf);
         P.inst = reinterpret_cast<const NrSmallGraph *>(db + off_desc) + gr.j0;
@@ -592,8 +615,13 @@ static int block_handover(nr_context *c, NrSlot &sl, const std::vector<int> &ids
         P.border = cfg.border;
         void *args[] = {&P};
         NR_CUDA_TRY(nr_smem_limit(c->device, gr.kfn, gr.smem));
-        NR_CUDA_TRY(cudaLaunchKernel(gr.kfn, dim3(gr.grid), dim3(NR_BLOCK_LANE_THREADS), args, gr.smem, s));
+        NR_CUDA_TRY(cudaLaunchKernel(gr.kfn, dim3(gr.grid), dim3(NR_BLOCK_LANE_THREADS), args, gr.smem, gs_));
     }
+    if (nside > 1)
+        for (int q = 0; q < nside; ++q) {
+            NR_CUDA_TRY(cudaEventRecord(sl.hv_join[q], sl.hv_side[q]));
+            NR_CUDA_TRY(cudaStreamWaitEvent(s, sl.hv_join[q], 0));
+        }
     NR_CUDA_TRY(cudaEventRecord(sl.ev1, s));
     const NrWarpOut *hout = reinterpret_cast<const NrWarpOut *>(hb + off_out);
     NR_CUDA_TRY(cudaMemcpyAsync(hb + off_out, db + off_out, sizeof(NrWarpOut) * k, cudaMemcpyDeviceToHost, s));

@@ -145,8 +145,10 @@ struct PhaseClock {
 #define NR_LANE32_CLS0 (NR_LANE_CLS0 + NR_LANE_MAX_W4)
 #define NR_NCLS (NR_LANE32_CLS0 + NR_LANE32_MAX_W4)
 // the two-slot lane kernel hands an instance to the block kernel once its next wave holds more
-// than this many pages (1024 subproblems: four block steps)
-#define NR_HANDOVER_PAGES 32
+// than this many pages (256 subproblems: one step of the block's 256 lanes).  On the uneven
+// batch's 3,959 graphs of <= 32 nodes: 8 pages 13.0 ms, 16 13.6-14.0, 32 15.7, 64 17.6-18.6, 128
+// 22.9-24.7, never 59-72 ms; 4,096 K15 or 1,024 K25 instances never reach it (widest waves 32).
+#define NR_HANDOVER_PAGES 8
 struct NrHostBlock {
     size_t bytes;               // tables of the block's instances (16-byte multiples)
     long long last_owner_rel;   // offset in the block of its last structural part, -1 if none
@@ -190,6 +192,7 @@ struct WarpRunCfg {
 // batch over both slots measured slower on 4096 K15 instances: the host passes
 // are dominated by fixed costs and two concurrent launches lengthen the span.)
 #define NR_SLOTS 3
+#define NR_HV_STREAMS 4
 struct NrSlot {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;   // around the part's kernels
@@ -204,6 +207,8 @@ struct NrSlot {
     size_t hv_host_bytes = 0;
     void *hv_dev = nullptr;     // ... and device copies of their descriptors, ids and outputs
     size_t hv_dev_bytes = 0;
+    cudaStream_t hv_side[NR_HV_STREAMS] = {};   // their launches, one class a stream, side by side
+    cudaEvent_t hv_fork = nullptr, hv_join[NR_HV_STREAMS] = {};
     // the part queued by warp_submit, for warp_finish
     int n = 0;
     const nr_graph *gs = nullptr;

@@ -296,7 +296,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
             __syncwarp();
             if (st < 0 && P.handover_pages > 0 && S.used > P.handover_pages) {
                 // the next wave outgrows the warp: the block kernel runs the instance again
-                finish(s, 2, 0, nr_fix_zero(), 0);
+                // (queued reports the next wave's pages x 32, the host's largest-first order)
+                finish(s, 2, 0, nr_fix_zero(), lane == 0 ? (long long)S.used * NR_PAGE : 0ll);
                 continue;
             }
             if (st >= 0) {

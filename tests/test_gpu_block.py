@@ -42,7 +42,7 @@ def same_or_bracket(a, b, i):
 
 def test_handover_matches_two_slot_group_and_oracle(ctx, oracle):
     """The uneven mix to ESP width <= 1e-6 or 16,384 subproblems (checked between waves): the
-    instances whose waves outgrow 32 pages run on the block kernel; every field equals the
+    instances whose waves outgrow 8 pages (the default) run on the block kernel; every field equals the
     two-slot kernel's run without hand-over and the lane-group kernel's; a sample of the
     handed-over instances equals the oracle."""
     gs, srcs, dsts = uneven_small(384, seed=11)
