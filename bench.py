@@ -24,8 +24,8 @@ check against the oracle (oracle/, the CPU restatement of the reference):
   k10       -- K10, p ~ U[0.5, 0.95], exhaustive; against the single-thread oracle
   uneven    -- 4096 uneven instances (G(n,m) n~U{8..20}, grids 3x3..6x6), p ~ U[0.8, 0.99],
                each to ESP width <= 1e-6 or 16,384 subproblems; autotuned batched launch
-               against per-graph launches, device and e2e (the graphs above 32 nodes side by
-               side on the whole GPU)
+               against per-graph launches, device and e2e (the 6x6 grids, 36 nodes, one block
+               each on the 64-bit-row block kernel)
   k25       -- K25, p ~ U[0.9, 0.99], to ESP width <= 1e-5: plain vs learned order
   rgg200    -- random geometric graph N=200, E=600: the bucketed whole-GPU queue toward
                1e-5, the bracket at a 20M-subproblem budget
@@ -399,8 +399,8 @@ def cfg_uneven(ctx, flush, device):
     # breadth-first waves (the schedule with the fewest waves, hence the fewest grid barriers for the
     # graphs above 32 nodes); the autotuner picks pages per warp and warps per block
     base = dict(target_width=UNEVEN_TARGET, max_nodes=UNEVEN_BUDGET, order="waves", n_buckets=64)
-    # graphs above 32 nodes (the 6x6 grids) run one at a time on the whole-GPU engine after the
-    # batched launch; the autotuner times the batched launch on the others
+    # graphs above 32 nodes (the 6x6 grids) run after the batched launch, one block each on the
+    # 64-bit-row block kernel; the autotuner times the batched launch on the others
     small = [i for i in range(BATCH) if gs[i].n_nodes <= 32]
     wide = [i for i in range(BATCH) if gs[i].n_nodes > 32]
     tb = nr.Batch([gs[i] for i in small], [w["srcs"][i] for i in small], [w["dsts"][i] for i in small])
@@ -415,9 +415,9 @@ def cfg_uneven(ctx, flush, device):
         flush()
         res = ctx.run_batch(batch, capacity=0, raw=True, **tuned)
         if k >= 2:
-            # the batched launch's time (shared by its instances) plus each whole-GPU run's
+            # the batched launch's time (shared by its instances) plus the larger graphs' launches'
             mb = res[small[0]].ms
-            # graphs above 32 nodes share whole-GPU launches (a launch's instances report its time)
+            # graphs above 32 nodes share launches (a launch's instances report its time)
             mw = sum({res[i].ms for i in wide})
             ms_batched.append(mb)
             ms_wide.append(mw)
@@ -469,8 +469,10 @@ def cfg_uneven(ctx, flush, device):
             "batched_launch": {"instances": len(small), "ms_median": statistics.median(ms_batched),
                                "subproblems": n_small,
                                "subproblems_per_sec": n_small / (statistics.median(ms_batched) / 1e3)},
-            "whole_gpu": {"instances": len(wide), "launches": len({res[i].ms for i in wide}),
-                          "ms_median_sum": statistics.median(ms_wide)},
+            "above_32_nodes": {"instances": len(wide), "launches": len({res[i].ms for i in wide}),
+                               "kernels": sorted({nr.engine.KERNELS.get(res[i].kernel, "") or
+                                                  nr.engine.ENGINES.get(res[i].engine, "?") for i in wide}),
+                               "ms_median_sum": statistics.median(ms_wide)},
             "e2e": {"subproblems_per_sec": e_nodes / e_secs, "steps": 10, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "over_device": (e_nodes / e_secs) / (n_step / dev_s)},
             "per_graph_launches": {"instances": "the first 256 of at most 32 nodes", "batched_launch_ms": b_ms, "wall_ms": 1e3 * wall,

@@ -790,6 +790,208 @@ static int run_handover(nr_context *c, const std::vector<int> &handover, const n
     return NR_OK;
 }
 
+// ---------------------------------------------------------------------------
+// graphs of 33..64 nodes on the 64-bit-row block kernel (nr_block64.cuh)
+// ---------------------------------------------------------------------------
+
+// An undirected simple graph of 33..64 nodes and <= 256 edges: every edge id on exactly the
+// arcs u -> v and v -> u, no self-loop, no ordered pair twice.
+static bool mid_ok(const nr_graph &g)
+{
+    const int n = g.n_nodes, E = g.n_edges;
+    if (n <= NR_SMALL_MAX_N || n > NR_MID_MAX_N || E > NR_MID_MAX_E || g.n_arcs != 2 * E) return false;
+    static thread_local int pid[NR_MID_MAX_N][NR_MID_MAX_N];
+    for (int u = 0; u < n; ++u)
+        for (int v = 0; v < n; ++v) pid[u][v] = -1;
+    std::vector<int> cnt(std::max(E, 1), 0);
+    for (int u = 0; u < n; ++u)
+        for (int j = g.row_ptr[u]; j < g.row_ptr[u + 1]; ++j) {
+            const int v = g.col_idx[j], e = g.edge_id[j];
+            if (v == u || pid[u][v] != -1) return false;
+            pid[u][v] = e;
+            cnt[e]++;
+        }
+    for (int e = 0; e < E; ++e)
+        if (cnt[e] != 2) return false;
+    for (int u = 0; u < n; ++u)
+        for (int j = g.row_ptr[u]; j < g.row_ptr[u + 1]; ++j)
+            if (pid[g.col_idx[j]][u] != g.edge_id[j]) return false;
+    return true;
+}
+
+// One instance's tables: [p: E doubles][endpoints: E x u16, u | v << 8][edge ids: 64 x 64 u16].
+static size_t mid_layout(const nr_graph &g, int src, int dst, NrSmallGraph *sg)
+{
+    memset(sg, 0, sizeof(*sg));
+    const int E = g.n_edges, W = std::max(1, (2 * E + 31) / 32);
+    sg->n = g.n_nodes; sg->e = E; sg->w4 = (W + 3) / 4; sg->src = src; sg->dst = dst;
+    sg->n_in = g.n_arcs;
+    sg->rows = 1;
+    size_t off = 0;
+    sg->off_p = 0; off = align16(sizeof(double) * std::max(E, 1));
+    sg->off_list = (int)off; off = align16(off + sizeof(uint16_t) * std::max(E, 1));
+    sg->off_eid = (int)off; off = align16(off + sizeof(uint16_t) * NR_MID_MAX_N * NR_MID_MAX_N);
+    sg->blob_bytes = (int)off;
+    return off;
+}
+
+static void mid_fill(const nr_graph &g, const NrSmallGraph &sg, unsigned char *b)
+{
+    memcpy(b + sg.off_p, g.edge_p, sizeof(double) * g.n_edges);
+    uint16_t *ends = reinterpret_cast<uint16_t *>(b + sg.off_list);
+    uint16_t *eid = reinterpret_cast<uint16_t *>(b + sg.off_eid);
+    for (int i = 0; i < NR_MID_MAX_N * NR_MID_MAX_N; ++i) eid[i] = 0xffff;
+    for (int u = 0; u < g.n_nodes; ++u)
+        for (int j = g.row_ptr[u]; j < g.row_ptr[u + 1]; ++j) {
+            const int v = g.col_idx[j], e = g.edge_id[j];
+            eid[u * NR_MID_MAX_N + v] = (uint16_t)e;
+            if (u < v) ends[e] = (uint16_t)(u | (v << 8));
+        }
+}
+
+// The graphs idx (mid_ok) in breadth-first waves, one block each: tables to the control buffer,
+// wave buffers of `cap` records per block in the arena, one launch per mask width.
+static int run_block64(nr_context *c, const std::vector<int> &idx, const nr_graph *gs, const int32_t *srcs,
+                       const int32_t *dsts, uint64_t cap, const WarpRunCfg &cfg, nr_result *res)
+{
+    c->ckpt.valid = false;                 // the arena is about to be reused
+    const int k = (int)idx.size();
+    std::vector<NrSmallGraph> d(k);
+    size_t blob = 0;
+    for (int j = 0; j < k; ++j) {
+        const int i = idx[j];
+        const size_t b = mid_layout(gs[i], srcs[i], dsts[i], &d[j]);
+        d[j].blob_off = d[j].struct_off = (long long)blob;
+        blob += b;
+        if (d[j].w4 > NR_MID_MAX_W4) return NR_ERR_INTERNAL;
+    }
+    // one launch per mask width; inside it the largest graphs first
+    std::vector<int> order(k);
+    for (int j = 0; j < k; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return d[a].w4 != d[b].w4 ? d[a].w4 < d[b].w4 : d[a].e > d[b].e;
+    });
+    const size_t off_blob = 16;
+    const size_t off_desc = align16(off_blob + blob);
+    const size_t off_ids = align16(off_desc + sizeof(NrSmallGraph) * k);
+    const size_t off_out = align16(off_ids + sizeof(int) * k);
+    const size_t total = align16(off_out + sizeof(NrWarpOut) * k);
+    int rc = ensure(&c->sbuf, &c->sbytes, total);
+    if (rc) return rc;
+    std::vector<unsigned char> up(off_out, 0);
+    NrSmallGraph *hd = reinterpret_cast<NrSmallGraph *>(up.data() + off_desc);
+    int *hid = reinterpret_cast<int *>(up.data() + off_ids);
+    for (int j = 0; j < k; ++j) {
+        NrSmallGraph t = d[order[j]];
+        mid_fill(gs[idx[order[j]]], t, up.data() + off_blob + t.blob_off);
+        t.blob_off += (long long)off_blob;
+        t.struct_off = t.blob_off;
+        hd[j] = t;
+        hid[j] = j;
+    }
+    unsigned char *sb = static_cast<unsigned char *>(c->sbuf);
+    cudaStream_t s = c->stream;
+    NR_CUDA_TRY(cudaMemcpyAsync(sb, up.data(), off_out, cudaMemcpyHostToDevice, s));
+    const int optin = smem_optin(c);
+    const int pages = (int)std::max<uint64_t>(1, std::min<uint64_t>(cap / NR_PAGE, 1u << 30));
+    const size_t capr = (size_t)pages * NR_PAGE;
+    struct Grp { int j0, j1, w4, warps, grid; size_t smem; int row_words; const void *kfn; };
+    std::vector<Grp> grps;
+    size_t slab_need = 0;
+    size_t free_b = 0, total_b = 0;
+    NR_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    for (int j0 = 0; j0 < k;) {
+        Grp gr;
+        gr.j0 = j0;
+        gr.w4 = hd[j0].w4;
+        int j1 = j0, nmax = 1;
+        while (j1 < k && hd[j1].w4 == gr.w4) nmax = std::max(nmax, hd[j1++].n);
+        gr.j1 = j1;
+        gr.row_words = 2 * nmax;
+        gr.kfn = nr_block64_kernel_ptr(gr.w4);
+        if (!gr.kfn) return NR_ERR_INTERNAL;
+        const size_t per_warp = nr_mid_shm_bytes(nmax, 1) - (size_t)nr_mid_tab_bytes();
+        gr.warps = (int)std::max<size_t>(1, std::min<size_t>(NR_MID_MAX_WARPS,
+                                                             ((size_t)optin - nr_mid_tab_bytes() - 1024) / per_warp));
+        gr.smem = nr_mid_shm_bytes(nmax, gr.warps);
+        auto it = c->occupancy.find({gr.kfn, gr.smem * 64 + gr.warps});
+        int bps;
+        if (it == c->occupancy.end()) {
+            NR_CUDA_TRY(nr_smem_limit(c->device, gr.kfn, gr.smem));
+            NR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gr.kfn, 32 * gr.warps, gr.smem));
+            c->occupancy[{gr.kfn, gr.smem * 64 + gr.warps}] = bps;
+        } else {
+            bps = it->second;
+        }
+        if (bps < 1) return NR_ERR_UNSUPPORTED;
+        // a block's two wave buffers; no more blocks than half the free memory holds
+        const size_t per_block = 2 * capr * (16 * (size_t)gr.w4 + 8);
+        const size_t budget = std::max(per_block, (free_b + c->qbytes) / 2);
+        gr.grid = (int)std::max<size_t>(1, std::min<size_t>({(size_t)(j1 - j0), (size_t)bps * c->sms, budget / per_block}));
+        slab_need = std::max(slab_need, (size_t)gr.grid * per_block);
+        grps.push_back(gr);
+        j0 = j1;
+    }
+    rc = ensure(&c->qbuf, &c->qbytes, slab_need);
+    if (rc) return rc;
+    NR_CUDA_TRY(cudaEventRecord(c->ev0, s));
+    for (const Grp &gr : grps) {
+        unsigned char *qb = static_cast<unsigned char *>(c->qbuf);
+        NrWarpParams P{};
+        P.blob = sb;
+        P.inst = reinterpret_cast<const NrSmallGraph *>(sb + off_desc) + gr.j0;
+        P.inst_id = reinterpret_cast<const int *>(sb + off_ids) + gr.j0;
+        P.n_inst = gr.j1 - gr.j0;
+        P.next_inst = reinterpret_cast<int *>(sb);
+        P.slab_mask = reinterpret_cast<uint4 *>(qb);
+        P.slab_mass = reinterpret_cast<double *>(qb + (size_t)gr.grid * 2 * capr * 16 * gr.w4);
+        P.pages = pages;
+        P.n_buckets = cfg.n_buckets;
+        P.shift = -1;
+        P.wave_mode = 1;
+        P.eps = cfg.eps;
+        P.target = cfg.target;
+        P.target_fix = nr_fix_of(cfg.target);
+        P.max_nodes = cfg.max_nodes;
+        P.out = reinterpret_cast<NrWarpOut *>(sb + off_out);
+        P.step_cap = cfg.step_cap;
+        P.border = cfg.border;
+        P.row_words = gr.row_words;
+        NR_CUDA_TRY(cudaMemsetAsync(sb, 0, sizeof(int), s));            // the launch's work counter
+        void *args[] = {&P};
+        NR_CUDA_TRY(nr_smem_limit(c->device, gr.kfn, gr.smem));
+        NR_CUDA_TRY(cudaLaunchKernel(gr.kfn, dim3(gr.grid), dim3(32 * gr.warps), args, gr.smem, s));
+    }
+    NR_CUDA_TRY(cudaEventRecord(c->ev1, s));
+    std::vector<NrWarpOut> hout(k);
+    NR_CUDA_TRY(cudaMemcpyAsync(hout.data(), sb + off_out, sizeof(NrWarpOut) * k, cudaMemcpyDeviceToHost, s));
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    NR_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    for (const Grp &gr : grps)
+        for (int j = gr.j0; j < gr.j1; ++j) {
+            const int i = idx[order[j]];
+            if (hout[j].status == NR_LANE_STATUS_CHECK) {
+                snprintf(g_internal, sizeof(g_internal), "block kernel check %llu failed on instance %d",
+                         (unsigned long long)hout[j].max_wave, i);
+                return NR_ERR_INTERNAL;
+            }
+            nr_result *r = &res[i];
+            memset(r, 0, sizeof(*r));
+            r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
+            r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
+            fill_from_warp(hout[j], cfg, hd[j].w4, r);
+            r->kernel = NR_KERNEL_BLOCK;
+            r->capacity = capr;
+            r->ms = ms;
+            r->grid_blocks = gr.grid;
+            r->block_threads = 32 * gr.warps;
+            r->h2d_bytes = hd[j].blob_bytes + sizeof(NrSmallGraph) + sizeof(int);
+            r->d2h_bytes = sizeof(NrWarpOut);
+        }
+    return NR_OK;
+}
+
 // A batch with graphs above 32 nodes, start to end: graphs of up to 32 nodes run
 // together on the warp engine, larger ones one at a time on the whole-GPU engine.
 static int run_mixed_batch(nr_context *c, int n, const nr_graph *gs, const int32_t *srcs, const int32_t *dsts,
@@ -814,13 +1016,28 @@ static int run_mixed_batch(nr_context *c, int n, const nr_graph *gs, const int32
     }
     rc = run_handover(c, handover, gs, srcs, dsts, capacity, o, res);
     if (rc) return rc;
+    const uint64_t wcap = std::max<uint64_t>(capacity, 1u << 22);
+    // graphs of 33..64 nodes: the 64-bit-row block kernel, one block each, when the run is the lane
+    // kernels' kind (breadth-first waves, path branching, plain order) and there are at least a
+    // quarter as many of them as SMs (fewer leave most of the GPU to a few blocks: the whole-GPU
+    // engine then)
+    const WarpRunCfg bcfg = batch_cfg(o, capacity);
+    if (bcfg.lane && bcfg.lane2 && !bcfg.fork && !bcfg.learned && bcfg.border != NR_BORDER_LEARNED) {
+        std::vector<int> mid_idx, rest;
+        for (int i : wide_idx) (mid_ok(gs[i]) ? mid_idx : rest).push_back(i);
+        if ((int)mid_idx.size() >= std::max(2, c->sms / 4)) {
+            rc = run_block64(c, mid_idx, gs, srcs, dsts, wcap, bcfg, res);
+            if (rc) return rc;
+            wide_idx.swap(rest);
+        }
+    }
     for (int i : wide_idx) {
         nr_result *r = &res[i];
         memset(r, 0, sizeof(*r));
         r->n_nodes = gs[i].n_nodes; r->n_edges = gs[i].n_edges; r->src = srcs[i]; r->dst = dsts[i];
         r->mask_words = std::max(1, (2 * gs[i].n_edges + 31) / 32);
     }
-    const uint64_t wcap = std::max<uint64_t>(capacity, 1u << 22);
+    if (wide_idx.empty()) return NR_OK;
     // breadth-first waves with path branching (run_wide's whole-GPU wave engine): the graphs run
     // side by side, each on its own group of blocks; else one at a time
     const bool buckets = o.bucket_shift >= 0 &&

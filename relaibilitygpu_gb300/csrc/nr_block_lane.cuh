@@ -10,8 +10,8 @@
 // block: each warp takes 32 records of the current wave at a time, the children go to the
 // block's next-wave buffer (one shared-memory atomicAdd per warp step places a warp's
 // children), and the block meets at the end of every wave for the stop tests.  Waves, stop
-// tests (in the lane kernels' order: target width, node budget, empty queue), parent rule,
-// path, children and FP64 products are the lane kernels', so every count and exact sum is
+// tests (in the oracle's order: empty queue, target width, node budget), parent rule, path,
+// children and FP64 products are the lane kernels', so every count and exact sum is
 // what the two-slot kernel (and the oracle) reports; only the order of the children inside a
 // wave is new, and nothing depends on it but which children spill when a wave outgrows the
 // buffer.
@@ -127,13 +127,13 @@ __global__ void __launch_bounds__(NR_BLOCK_LANE_THREADS, 2) nr_block_lane_kernel
         for (int wave = 0;; ++wave) {
             const int cur = wave & 1;
             const double *in_mass = mass_b + (size_t)cur * cap;
-            // ---- stop tests between waves, in the lane kernels' order ----
+            // ---- stop tests between waves, in the oracle's order: empty queue, target width, budget ----
             const unsigned long long units = nr_u64_block_sum(use_units ? qunits : 0u, s_u64);
             const unsigned long long nodes = nr_u64_block_sum(acc.nodes, s_u64);
-            int st = -1;
+            int st = !check && n_in == 0 ? 0 : -1;         // an empty queue first, as in the oracle
             NrFix qs = nr_fix_zero();                   // this thread's share of the queued mass
             bool summed = false;
-            if (!check && P.target > 0.0 && units <= NR_LANE2_UNITS) {
+            if (!check && st < 0 && P.target > 0.0 && units <= NR_LANE2_UNITS) {
                 for (unsigned long long r = threadIdx.x; r < n_in; r += blockDim.x)
                     nr_fix_add_mass(qs, __ldcg(in_mass + r));
                 summed = true;
@@ -143,7 +143,6 @@ __global__ void __launch_bounds__(NR_BLOCK_LANE_THREADS, 2) nr_block_lane_kernel
                 if (nr_fix_le(nr_fix_block_sum(w, s_fix), P.target_fix)) st = 1;
             }
             if (!check && st < 0 && P.max_nodes && nodes >= P.max_nodes) st = 3;
-            if (!check && st < 0 && n_in == 0) st = 0;
             // self-checks: a failed internal check; more waves than a path decomposition can have
             // (every child has one more edge down than its parent)
             if (!check && st < 0 && (waves > ge + 1 || (P.step_cap > 0 && waves >= P.step_cap))) check = 1;

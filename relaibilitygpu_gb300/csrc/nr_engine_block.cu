@@ -1,6 +1,7 @@
-// nr_engine_block.cu -- the block kernel (nr_block_lane.cuh), one instantiation per row width and
-// mask width: the instances the two-slot lane kernel hands over.
-#include "nr_block_lane.cuh"
+// nr_engine_block.cu -- the block kernels, one instantiation per row width and mask width: the
+// instances the two-slot lane kernel hands over (nr_block_lane.cuh), and a batch's graphs of
+// 33..64 nodes (nr_block64.cuh).
+#include "nr_block64.cuh"
 
 const void *nr_block_lane_kernel_ptr(int w4, int row_bits)
 {
@@ -20,6 +21,17 @@ const void *nr_block_lane_kernel_ptr(int w4, int row_bits)
     switch (w4) {
     case 1: return (const void *)nr_block_lane_kernel<1, 16>;
     case 2: return (const void *)nr_block_lane_kernel<2, 16>;
+    default: return nullptr;
+    }
+}
+
+const void *nr_block64_kernel_ptr(int w4)
+{
+    switch (w4) {
+    case 1: return (const void *)nr_block64_kernel<1>;
+    case 2: return (const void *)nr_block64_kernel<2>;
+    case 3: return (const void *)nr_block64_kernel<3>;
+    case 4: return (const void *)nr_block64_kernel<4>;
     default: return nullptr;
     }
 }

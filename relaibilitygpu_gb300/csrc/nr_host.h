@@ -28,7 +28,7 @@
 #include "nr_warp.cuh"
 #include "nr_lane2.cuh"
 #include "nr_grid_lane.cuh"
-#include "nr_block_lane.cuh"
+#include "nr_block64.cuh"
 #include "nr_wide.cuh"
 #include "nr_mlp.cuh"
 
@@ -57,6 +57,7 @@ int run_grid_wide_multi(nr_context *c, const std::vector<int> &idx, const nr_gra
                         const int32_t *dsts, uint64_t cap, const nr_options *o, nr_result *res);
 const void *nr_lane2_kernel_ptr(int w4, int slots, int row_bits = 16);
 const void *nr_block_lane_kernel_ptr(int w4, int row_bits);
+const void *nr_block64_kernel_ptr(int w4);
 int nr_mlp_upload(const float *params, void **storage, NrMlpDev *out, cudaStream_t s);
 
 #define NR_CUDA_TRY(call)                                                     \

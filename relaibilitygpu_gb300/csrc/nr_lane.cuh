@@ -393,6 +393,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
         long long steps = 0;
 
         for (;;) {
+            // fullest (lowest-index) non-empty bucket; an empty queue ends the run before the other
+            // tests, as in the oracle's wave loop (pathdecomp.c: empty, target width, budget)
+            const uint32_t wbm = (lane < NB / 32) ? sh.bitmap[lane] : 0u;
+            const unsigned nz = __ballot_sync(NR_FULL, wbm != 0u);
+            if (!nz) break;
             if (P.wave_mode && P.target > 0.0) {     // exact: ESP + queued mass <= target
                 chain_sum();
                 if (check) { status = NR_LANE_STATUS_CHECK; max_wave = (unsigned long long)check; break; }
@@ -406,10 +411,6 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane_kernel(NrWarpPar
                 if (P.wave_mode) { status = 3; } else { status = 2; abandon = true; }
                 break;
             }
-            // fullest (lowest-index) non-empty bucket
-            const uint32_t wbm = (lane < NB / 32) ? sh.bitmap[lane] : 0u;
-            const unsigned nz = __ballot_sync(NR_FULL, wbm != 0u);
-            if (!nz) break;
             const int wi = __ffs(nz) - 1;
             const int bk = wi * 32 + __ffs(__shfl_sync(NR_FULL, wbm, wi)) - 1;
             int chain = 0;

@@ -256,8 +256,8 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
         for (int s = 0; s < NS; ++s) {
             NrLaneSlot &S = slots[s];
             if (S.ii < 0 || S.cur >= 0) continue;
-            // slot s's wave is done (or its first not begun): the stop tests, in the one-slot
-            // kernel's order (target width, node budget, empty queue).  The queued mass is the
+            // slot s's wave is done (or its first not begun): the stop tests, in the oracle's and
+            // the one-slot kernel's order (empty queue, target width, node budget).  The queued mass is the
             // next wave's chain.  Its exact sum is taken only where a test can end the run: a
             // lower bound of it (FP32 sums rounded down, kept as the children are written) above
             // the target already rules the width test out, as the exact test would.
@@ -276,8 +276,9 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 summed = true;
                 return pg < 0;
             };
-            int st = -1;
-            if (P.target > 0.0) {
+            // an empty queue first, as in the oracle's wave loop
+            int st = S.head < 0 ? 0 : -1;
+            if (st < 0 && P.target > 0.0) {
                 const unsigned units = use_units ? __reduce_add_sync(NR_FULL, qlb[s * 32 + lane]) : 0u;
                 if (units <= NR_LANE2_UNITS) {
                     if (!chain_sum()) {
@@ -292,7 +293,6 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, 2) nr_lane2_kernel(NrWarpPa
                 }
             }
             if (st < 0 && P.max_nodes && nr_warp_sum_u64r(A.nodes) >= P.max_nodes) st = 3;
-            if (st < 0 && S.head < 0) st = 0;
             __syncwarp();
             if (st < 0 && P.handover_pages > 0 && S.used > P.handover_pages) {
                 // the next wave outgrows the warp: the block kernel runs the instance again

@@ -211,6 +211,7 @@ extern "C" int nr_reliability_noalloc(const nr_graph *g, int src, int dst, const
     P.step_cap = 0;
     P.border = o.branch_order;
     P.handover_pages = 0;
+    P.row_words = 0;
 
     const size_t smem = nr_warp_shm_bytes(32 / G, sg.w4, P.n_buckets, pages);
     cudaStream_t s = cudaStreamPerThread;

@@ -76,6 +76,8 @@ struct NrWarpParams {
     int handover_pages;              // two-slot lane kernel: an instance whose next wave holds more
                                      // pages than this is handed over (status 2) to the block
                                      // kernel (nr_block_lane.cuh); 0 = never
+    int row_words;                   // 64-bit-row block kernel (nr_block64.cuh): shared-memory words
+                                     // a lane's rows take (and its BFS levels): 2 x the largest n
 };
 
 __device__ __forceinline__ unsigned long long nr_warp_sum_u64(unsigned long long x)
@@ -242,6 +244,11 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
         long long t_stop = 0;
 
         for (;;) {
+            // fullest (lowest-index) non-empty bucket; an empty queue ends the run before the other
+            // tests, as in the oracle's wave loop (pathdecomp.c: empty, target width, budget)
+            const uint32_t wb = (lane < NB / 32) ? sh.bitmap[lane] : 0u;
+            const unsigned nz = __ballot_sync(NR_FULL, wb != 0u);
+            if (!nz) break;
             if (P.wave_mode && P.target > 0.0) {     // exact: ESP + queued mass <= target
                 NrFix w = qacc;
                 nr_fix_add(w, acc.et);
@@ -253,10 +260,6 @@ __global__ void __launch_bounds__(NR_WARP_BLOCK_MAX, LEARN ? 1 : (W4 <= 4 ? NR_W
                 if (P.wave_mode) { status = 3; } else { status = 2; abandon = true; }
                 break;
             }
-            // fullest (lowest-index) non-empty bucket
-            const uint32_t wb = (lane < NB / 32) ? sh.bitmap[lane] : 0u;
-            const unsigned nz = __ballot_sync(NR_FULL, wb != 0u);
-            if (!nz) break;
             const int wi = __ffs(nz) - 1;
             const int bk = wi * 32 + __ffs(__shfl_sync(NR_FULL, wb, wi)) - 1;
             int chain = 0;

@@ -115,3 +115,49 @@ def test_single_instance_handover_and_block_spill(ctx, oracle):
     s = ctx.reliability(k9, 0, 8, target_width=1e-14, order="waves", n_buckets=64, capacity=256, handover_pages=1)
     assert s.kernel == "block" and s.spilled > 0
     assert s.R <= exact.R + 1e-15 and exact.R <= s.R + s.esp + 1e-12
+
+
+def mid_batch():
+    """Undirected simple graphs of 33..64 nodes (mask widths 1..4 blocks) for the 64-bit-row block
+    kernel, and edge cases: src == dst, certain edges (p = 0 and 1 in the root's mask), a 64-node
+    path (63 BFS levels)."""
+    from relaibilitygpu_gb300 import graphs
+    gs, st = [], []
+    for s in range(16):
+        gs.append(graphs.grid(6, 6, p_range=(0.8, 0.99), seed=1300 + s)); st.append((0, 35))
+    for s in range(8):
+        gs.append(graphs.grid(7, 7, p_range=(0.85, 0.99), seed=1320 + s)); st.append((0, 48))
+        g = graphs.gnm(40, 100, p_range=(0.8, 0.99), seed=1330 + s); gs.append(g); st.append((g.src, g.dst))
+        g = graphs.gnm(60, 180, p_range=(0.85, 0.99), seed=1340 + s); gs.append(g); st.append((g.src, g.dst))
+    for s in range(4):
+        g = graphs.gnm(64, 250, p_range=(0.9, 0.99), seed=1350 + s); gs.append(g); st.append((g.src, g.dst))
+    g = graphs.grid(6, 6, p_range=(0.8, 0.99), seed=1360)
+    p = g.edge_p.copy(); p[2] = 0.0; p[5] = 1.0; p[17] = 0.0
+    gs.append(graphs.from_edges(36, g.edge_list(), p)); st.append((0, 35))
+    gs.append(graphs.grid(6, 6, p_range=(0.8, 0.99), seed=1361)); st.append((14, 14))
+    gs.append(graphs.from_edges(64, [(i, i + 1) for i in range(63)], [0.99] * 63)); st.append((0, 63))
+    return gs, [a for a, _ in st], [b for _, b in st]
+
+
+@pytest.mark.parametrize("target,budget,border", [(1e-6, 20000, "src"), (1e-5, 100000, "p_asc"), (1e-6, 5000, "dst")])
+def test_mid_graphs_block_kernel(ctx, oracle, target, budget, border):
+    """A batch's graphs of 33..64 nodes in breadth-first waves run one block each with 64-bit rows
+    rebuilt from the mask; every field equals the whole-GPU wide engine's (small_kernel="group"
+    keeps them there) and the oracle's."""
+    gs, srcs, dsts = mid_batch()
+    opts = dict(target_width=target, max_nodes=budget, order="waves", n_buckets=64, branch_order=border)
+    a = ctx.reliability_batch(gs, srcs, dsts, **opts)
+    b = ctx.reliability_batch(gs, srcs, dsts, small_kernel="group", **opts)
+    assert {r.kernel for r in a} == {"block"} and {r.engine for r in b} == {"grid"}
+    checked = 0
+    for i, (g, x, y) in enumerate(zip(gs, a, b)):
+        assert x.spilled == 0 and y.spilled == 0, i
+        same_or_bracket(x, y, i)
+        if i % 3 == 0 or i >= len(gs) - 3:
+            o = oracle.run(g, srcs[i], dsts[i], target_width=target, max_nodes=budget, branch_order=border)
+            assert (x.nodes, x.leaves, x.dead_ends, x.iterations, x.max_queue_items, x.queued) == \
+                (o.nodes, o.leaves, o.dead, o.waves, o.max_wave, o.queued), i
+            assert x.R == o.R and x.esp == o.esp, i
+            assert x.stop == {0: 0, 1: 1, 2: 3}[o.status], i      # (the oracle's 2 is the budget)
+            checked += 1
+    assert checked >= 16
