@@ -612,11 +612,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="only the headline line (no configs, orders or CPU leg)")
-    ap.add_argument("--case", choices=["k15batch", "rgg200", "uneven", "k10"],
+    ap.add_argument("--case", choices=["k15batch", "rgg200", "uneven", "k10", "mid"],
                     help="profiling: run one case twice (a warm-up call, then the call to capture) and exit")
     ap.add_argument("--budget", type=int, default=1_000_000, help="--case rgg200: subproblem budget")
     ap.add_argument("--arena", type=int, default=22, help="--case rgg200: log2 of the arena slots")
-    ap.add_argument("--instances", type=int, default=BATCH, help="--case uneven: instances generated")
+    ap.add_argument("--instances", type=int, default=BATCH,
+                    help="--case uneven: instances generated; --case mid: 6x6 grids taken (at most 137)")
     ap.add_argument("--pages", type=int, default=4096, help="--case uneven: pages per warp")
     args = ap.parse_args()
     if args.case:
@@ -785,6 +786,15 @@ def run_case(args):
             g = nr.complete(10, p_range=(0.5, 0.95), seed=2)
             r = ctx.reliability(g, 0, 9, capacity=1 << 22)
             out = {"nodes": r.nodes, "waves": r.iterations, "ms": r.ms, "kernel": r.kernel}
+        elif args.case == "mid":
+            # the uneven batch's 6x6 grids (36 nodes): the 64-bit-row block kernel, one block each
+            if batch is None:
+                gs = [g for g in nr.batch_instances(BATCH, seed=0) if g.n_nodes > 32][:args.instances]
+                batch = nr.Batch(gs, [g.src for g in gs], [g.dst for g in gs])
+            res = ctx.run_batch(batch, capacity=0, raw=True, target_width=UNEVEN_TARGET, max_nodes=UNEVEN_BUDGET,
+                                order="waves", n_buckets=64)
+            out = {"instances": batch.n, "nodes": sum(res[i].nodes for i in range(batch.n)), "ms": res[0].ms,
+                   "kernel": nr.engine.KERNELS.get(res[0].kernel, "")}
         elif args.case == "rgg200":
             g = nr.rgg(200, 600, p_range=(0.9, 0.99), seed=7)
             r = ctx.reliability(g, g.src, g.dst, capacity=1 << args.arena, target_width=1e-5, order="maxmass",

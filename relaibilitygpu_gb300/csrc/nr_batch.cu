@@ -1026,7 +1026,9 @@ static int run_mixed_batch(nr_context *c, int n, const nr_graph *gs, const int32
         std::vector<int> mid_idx, rest;
         for (int i : wide_idx) (mid_ok(gs[i]) ? mid_idx : rest).push_back(i);
         if ((int)mid_idx.size() >= std::max(2, c->sms / 4)) {
-            rc = run_block64(c, mid_idx, gs, srcs, dsts, wcap, bcfg, res);
+            // wave buffers of 2^20 records a block at least (48-80 MB a block; the wide engine's
+            // 2^22 a graph would be 200-330 MB for each of up to 152 blocks)
+            rc = run_block64(c, mid_idx, gs, srcs, dsts, std::max<uint64_t>(capacity, 1u << 20), bcfg, res);
             if (rc) return rc;
             wide_idx.swap(rest);
         }

@@ -143,9 +143,11 @@ def mid_batch():
 def test_mid_graphs_block_kernel(ctx, oracle, target, budget, border):
     """A batch's graphs of 33..64 nodes in breadth-first waves run one block each with 64-bit rows
     rebuilt from the mask; every field equals the whole-GPU wide engine's (small_kernel="group"
-    keeps them there) and the oracle's."""
+    keeps them there) and the oracle's.  A 2^22-record capacity holds every wave (the widest, the
+    children of the last wave before a 100 K budget, exceed the default 2^20 a block)."""
     gs, srcs, dsts = mid_batch()
-    opts = dict(target_width=target, max_nodes=budget, order="waves", n_buckets=64, branch_order=border)
+    opts = dict(target_width=target, max_nodes=budget, order="waves", n_buckets=64, branch_order=border,
+                capacity=1 << 22)
     a = ctx.reliability_batch(gs, srcs, dsts, **opts)
     b = ctx.reliability_batch(gs, srcs, dsts, small_kernel="group", **opts)
     assert {r.kernel for r in a} == {"block"} and {r.engine for r in b} == {"grid"}
