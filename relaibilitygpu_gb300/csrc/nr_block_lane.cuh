@@ -23,7 +23,9 @@
 
 #include "nr_lane2.cuh"
 
-#define NR_BLOCK_LANE_THREADS 256
+// 16 warps an instance, one block per SM (128 registers): the largest instances' chains of waves
+// are the launch's tail, and 8-warp blocks two per SM took 3-7 % longer on the uneven batch
+#define NR_BLOCK_LANE_THREADS 512
 #define NR_BLOCK_LANE_WARPS (NR_BLOCK_LANE_THREADS / 32)
 
 // dynamic shared memory: the instance's p and edge-id tables, then per warp the lanes' rows
@@ -64,7 +66,7 @@ __device__ __forceinline__ unsigned long long nr_u64_block_sum(unsigned long lon
 }
 
 template <int W4, int RB>
-__global__ void __launch_bounds__(NR_BLOCK_LANE_THREADS, 2) nr_block_lane_kernel(NrWarpParams P)
+__global__ void __launch_bounds__(NR_BLOCK_LANE_THREADS, 1) nr_block_lane_kernel(NrWarpParams P)
 {
     constexpr int NW = 4 * W4;
     constexpr int RW = nr_lane_rw<RB>();
