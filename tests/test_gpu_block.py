@@ -163,3 +163,33 @@ def test_mid_graphs_block_kernel(ctx, oracle, target, budget, border):
             assert x.stop == {0: 0, 1: 1, 2: 3}[o.status], i      # (the oracle's 2 is the budget)
             checked += 1
     assert checked >= 16
+
+
+def test_matrix_batches_hand_over(ctx, engine_lib, oracle):
+    """One 5 x 5 grid topology with 256 probability rows through the matrix entry points
+    (synchronous and submitted): the instances whose waves outgrow the warp run on the block
+    kernel from their own row; every field equals the per-instance batch's, the run without
+    hand-over and (a sample) the oracle's."""
+    import numpy as np
+    from relaibilitygpu_gb300 import graphs
+    gs = [graphs.grid(5, 5, p_range=(0.8, 0.99), seed=1400 + s) for s in range(256)]
+    pm = np.stack([g.edge_p for g in gs])
+    opts = dict(target_width=1e-6, max_nodes=16384, order="waves", n_buckets=64, pages_per_warp=4096)
+    mb = engine_lib.MatrixBatch(gs[0], pm, 0, 24)
+    a = ctx.run_matrix(mb, **opts)
+    b = ctx.run_matrix(mb, handover_pages=-1, **opts)
+    c = ctx.reliability_batch(gs, [0] * len(gs), [24] * len(gs), **opts)
+    t = ctx.submit_matrix(mb, **opts)
+    ctx.wait(t)
+    d = [engine_lib.Result.from_raw(mb.res[i]) for i in range(len(gs))]
+    assert sum(r.kernel == "block" for r in a) >= 32 and {r.kernel for r in b} == {"lane2"}
+    for i in range(len(gs)):
+        same_or_bracket(a[i], b[i], i)
+        same_or_bracket(a[i], c[i], i)
+        same_or_bracket(a[i], d[i], i)
+        assert a[i].kernel == c[i].kernel == d[i].kernel, i
+        if i % 16 == 0 and not a[i].spilled:
+            o = oracle.run(gs[i], 0, 24, target_width=1e-6, max_nodes=16384)
+            assert (a[i].nodes, a[i].iterations, a[i].max_queue_items, a[i].queued) == \
+                (o.nodes, o.waves, o.max_wave, o.queued), i
+            assert a[i].R == o.R and a[i].esp == o.esp, i
