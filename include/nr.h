@@ -179,8 +179,9 @@ typedef struct nr_result {
     int32_t  stop;              /* 0 queue empty, 1 target width met, 3 pop budget reached */
     int32_t  kernel;            /* warp engine: NR_KERNEL_GROUP, NR_KERNEL_LANE, NR_KERNEL_LANE2 or
                                    NR_KERNEL_BLOCK;
-                                   whole-GPU engine for <= 32 nodes: NR_KERNEL_LANE when one lane
-                                   per subproblem ran; 0 otherwise */
+                                   whole-GPU engines: NR_KERNEL_LANE when one lane per subproblem
+                                   ran (waves on <= 32 nodes; the bucketed queue on undirected
+                                   simple graphs of <= 250 nodes); 0 otherwise */
     int32_t  reserved[2];
 } nr_result;
 

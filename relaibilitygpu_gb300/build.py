@@ -25,7 +25,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
               "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["nr_api.cu", "nr_engine_g8.cu", "nr_engine_g16.cu", "nr_engine_g32.cu", "nr_engine_wide.cu",
-              "nr_engine_wide_learn.cu", "nr_engine_wide_multi.cu",
+              "nr_engine_wide_learn.cu", "nr_engine_wide_multi.cu", "nr_engine_wide_lanes.cu",
               "nr_engine_lane.cu", "nr_engine_block.cu", "nr_mlp.cu", "nr_noalloc.cu", "nr_io.cu", "nr_batch.cu"]
 
 

@@ -1004,6 +1004,28 @@ static uint64_t nr_run_fingerprint(const nr_graph *g, int src, int dst, const nr
     return h;
 }
 
+// Every edge id on exactly the two arcs u -> v and v -> u, no self-loop, no ordered pair twice.
+static bool undirected_simple(const nr_graph *g)
+{
+    const int n = g->n_nodes, E = g->n_edges;
+    if (g->n_arcs != 2 * E) return false;
+    std::vector<int> cnt(std::max(E, 1), 0), tail(std::max(E, 1), -1), head(std::max(E, 1), -1);
+    std::vector<std::pair<int, int>> pairs;
+    pairs.reserve(g->n_arcs);
+    for (int u = 0; u < n; ++u)
+        for (int j = g->row_ptr[u]; j < g->row_ptr[u + 1]; ++j) {
+            const int v = g->col_idx[j], e = g->edge_id[j];
+            if (v == u || e < 0 || e >= E) return false;
+            if (cnt[e]++ == 0) { tail[e] = u; head[e] = v; }
+            else if (tail[e] != v || head[e] != u) return false;   // the second arc is v -> u
+            pairs.push_back({u, v});
+        }
+    for (int e = 0; e < E; ++e)
+        if (cnt[e] != 2) return false;
+    std::sort(pairs.begin(), pairs.end());
+    return std::adjacent_find(pairs.begin(), pairs.end()) == pairs.end();
+}
+
 // Whole-GPU bucketed max-mass queue (nr_bucket_wide_kernel) over an arena of
 // `cap` slots: 2^shift buckets per factor of two in mass, nb buckets.
 static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, uint64_t cap, const nr_options *o,
@@ -1025,9 +1047,16 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     // branching)
     const bool learn = o->branch_order == NR_BORDER_LEARNED;
     if (learn && (!c->has_model || nt > 0 || o->branching != NR_BRANCH_PATH)) return NR_ERR_UNSUPPORTED;
-    const void *kfn = learn ? nr_bucket_wide_learn_kernel_ptr(W4) : nr_bucket_wide_kernel_ptr(W4);
+    // one lane per subproblem: undirected simple graphs of <= 250 nodes with the bit-set tables,
+    // two-terminal path branching, the src-side-first branch order (small_kernel = group keeps a
+    // warp per subproblem)
+    const bool lanes = !learn && wg.bitset && nt == 0 && o->branching == NR_BRANCH_PATH &&
+                       o->branch_order == NR_BORDER_SRC && o->small_kernel != NR_SMALL_GROUP &&
+                       wg.n <= NR_WIDE_LANES_MAX_N && W4 >= 1 && W4 <= NR_WIDE_MAX_W4 && undirected_simple(g);
+    const void *kfn = learn ? nr_bucket_wide_learn_kernel_ptr(W4)
+                            : lanes ? nr_bucket_wide_lanes_kernel_ptr(W4) : nr_bucket_wide_kernel_ptr(W4);
     if (!kfn) return NR_ERR_UNSUPPORTED;
-    const size_t learn_warp = learn ? (size_t)NR_WIDE_LEARN_WORDS * 4 : 0;
+    const size_t learn_warp = learn ? (size_t)NR_WIDE_LEARN_WORDS * 4 : lanes ? nr_wide_lane_shm(wg.n, W4) : 0;
     int block = 0;
     for (int w = NR_WIDE_BLOCK / 32; w >= 1 && !block; --w)
         if (nr_wide_block_shm(wg, w) + w * learn_warp <= (size_t)smem_optin(c)) block = 32 * w;
@@ -1098,6 +1127,8 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     P.stop_info = reinterpret_cast<int *>(sb + off_info);
     P.stats = reinterpret_cast<unsigned long long *>(sb + off_stats);
     P.resume = rin ? 1 : 0;
+    // one lane a record from waves of NR_WIDE_LANE_MIN_PER_WARP records a warp up
+    P.lane_min_wave = (unsigned long long)NR_WIDE_LANE_MIN_PER_WARP * grid * (block / 32);
     P.init_R = P.init_et = P.init_es = P.init_net = nr_fix_zero();
     P.init_nodes = P.init_leaves = P.init_dead = P.init_trunc = P.init_spilled = 0;
     cudaStream_t s = c->stream;
@@ -1202,6 +1233,7 @@ static int run_bucket_wide(nr_context *c, const nr_graph *g, int src, int dst, u
     r->ms = ms;
     if (info[1] == 1) r->time_to_bound_ms = ms;
     r->engine = NR_ENGINE_GRID;
+    r->kernel = lanes ? NR_KERNEL_LANE : 0;
     r->grid_blocks = grid;
     r->block_threads = block;
     r->capacity = cap;

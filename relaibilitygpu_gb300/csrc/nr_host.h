@@ -53,6 +53,7 @@ const void *nr_lane_kernel_ptr(int w4);
 const void *nr_grid_lane_kernel_ptr(int w4, int row_bits = 16);
 const void *nr_grid_wide_multi_kernel_ptr(int w4);
 const void *nr_bucket_wide_learn_kernel_ptr(int w4);
+const void *nr_bucket_wide_lanes_kernel_ptr(int w4);
 int run_grid_wide_multi(nr_context *c, const std::vector<int> &idx, const nr_graph *gs, const int32_t *srcs,
                         const int32_t *dsts, uint64_t cap, const nr_options *o, nr_result *res);
 const void *nr_lane2_kernel_ptr(int w4, int slots, int row_bits = 16);

@@ -125,6 +125,7 @@ struct NrBucketWideParams {
     int resume;
     NrFix init_R, init_et, init_es, init_net;
     unsigned long long init_nodes, init_leaves, init_dead, init_trunc, init_spilled;
+    unsigned long long lane_min_wave;   // LANES: the smallest wave run one lane a record
 };
 
 // per-warp shared memory: mask words, a working copy of them (runtime-width children),
@@ -1174,9 +1175,189 @@ __device__ __forceinline__ bool nr_bucket_compact(const NrBucketWideParams &P, u
 // per warp, after the block's search scratch: the scorer's tiles and outputs (LEARN)
 #define NR_WIDE_LEARN_WORDS (NR_MLP_WARP_WORDS + 16)
 
+// ---- one lane per subproblem (the bucketed queue's LANES instantiation) ----
+// Undirected simple graphs of <= 250 nodes with the bit-set tables (whose in-arc lists are then
+// every node's neighbours), two-terminal path branching, the src-side-first branch order.  A warp
+// step expands 32 records of the wave, one a lane, where nr_wide_step gives each record the whole
+// warp.  A lane's scratch, in shared memory as [row][lane] columns after the block's search
+// scratch: the record's mask words, each node's BFS level (a byte; 0xff unseen) and the BFS
+// queue (node bytes), whose first L + 1 bytes then hold the path's nodes, src first.
+#define NR_WIDE_LANES_MAX_N 250
+// A wave runs one lane a record from this many records a warp up, else a warp a record.  RGG
+// N=200 (bucketed queue, 1 M / 20 M subproblems): 1, 4, 8, 16, 32, never: 19.5 / 186.5, 17.9 /
+// 185.1, 17.1 / 184.3, 17.3 / 184.8, 19.3 / 186.9, 29.2 / 521 ms; the warp-per-subproblem
+// kernel, whose registers and shared memory allow three times the blocks: 18.2 / 255 ms.
+#define NR_WIDE_LANE_MIN_PER_WARP 8
+__host__ __device__ inline size_t nr_wide_lane_shm(int n, int w4)
+{
+    return (size_t)(4 * w4 + 2 * ((n + 3) / 4)) * 32 * 4;
+}
+
+struct NrWideLaneAcc {
+    NrFix R, et, es, net;
+    unsigned long long nodes, leaves, dead, trunc, spilled;
+};
+
+__device__ __forceinline__ void nr_wide_lane_acc_zero(NrWideLaneAcc &a)
+{
+    a.R = a.et = a.es = a.net = nr_fix_zero();
+    a.nodes = a.leaves = a.dead = a.trunc = a.spilled = 0;
+}
+
+// The lanes' sums and counts into the warp's accumulators (all lanes call; lane 0 adds).
+__device__ __forceinline__ void nr_wide_lane_fold(NrWideLaneAcc &a, NrWideAcc &A)
+{
+    const NrFix R = nr_fix_warp_sum(a.R), net = nr_fix_warp_sum(a.net);
+    const NrFix et = nr_fix_warp_sum_sparse(a.et), es = nr_fix_warp_sum_sparse(a.es);
+    const unsigned long long nodes = nr_warp_sum_u64r(a.nodes), leaves = nr_warp_sum_u64r(a.leaves);
+    const unsigned long long dead = nr_warp_sum_u64r(a.dead), trunc = nr_warp_sum_u64r(a.trunc);
+    const unsigned long long spilled = nr_warp_sum_u64r(a.spilled);
+    if ((threadIdx.x & 31) == 0) {
+        nr_fix_add(A.R, R); nr_fix_add(A.et, et); nr_fix_add(A.es, es); nr_fix_add(A.net, net);
+        A.nodes += nodes; A.leaves += leaves; A.dead += dead; A.trunc += trunc; A.spilled += spilled;
+    }
+    __syncwarp();
+    nr_wide_lane_acc_zero(a);
+}
+
+// One lane's record (all lanes call: the children's slots are one warp-wide allocation).  mc:
+// the lane's mask column (word k at mc[32 k]); dq: its level and queue columns (byte i at
+// dq[32 i] and dq[32 (4 DB + i)]).  The search, path, children and products are nr_wide_step's
+// for these graphs: a level BFS over the not-down edges, the parent of a node on level l + 1 the
+// smallest node of level l adjacent to it, one child per UNKNOWN path edge src side first.
+template <int W4>
+__device__ __forceinline__ void nr_wide_lane_step(const NrWideGraph &g, const NrWideView &v, uint32_t *mc,
+                                                  unsigned char *dq, bool valid, double mass, double eps,
+                                                  const NrWideOut &O, NrWideLaneAcc &A, int *status)
+{
+    constexpr uint32_t HM = (1u << NR_WIDE_HEAD_BITS) - 1u;
+    const int lane = threadIdx.x & 31;
+    const int n = g.n, src = g.src, dst = g.dst;
+    unsigned char *lev = dq;
+    unsigned char *que = dq + (size_t)((n + 3) / 4) * 4 * 32;
+    auto state = [&](int e) -> uint32_t { return (mc[32 * (e >> 4)] >> ((e & 15) << 1)) & 3u; };
+    bool active = valid;
+    if (valid) {
+        A.nodes++;
+        nr_fix_sub(A.net, nr_fix_of(mass));
+        if (eps > 0.0 && mass < eps) {                      // main.cu:537-543
+            A.trunc++;
+            nr_fix_add_mass(A.et, mass);
+            active = false;
+        }
+    }
+    int L = -1, nch = 0;                                    // L < 0: no path
+    bool bad = false;
+    if (active) {
+        for (int i = 0; i < n; ++i) lev[32 * i] = 0xff;
+        if (src == dst) {
+            L = 0;
+        } else {
+            lev[32 * src] = 0;
+            que[0] = (unsigned char)src;
+            int head = 0, tail = 1;
+            bool found = false;
+            while (!found && head < tail) {                 // each node is queued once: <= n pops
+                const int u = que[32 * head++];
+                const int du = lev[32 * u];
+                for (int j = v.row[u], je = v.row[u + 1]; j < je; ++j) {
+                    const uint32_t a = v.arc[j];
+                    const int e = (int)(a >> NR_WIDE_HEAD_BITS), w = (int)(a & HM);
+                    if (state(e) == NR_EDGE_DOWN || lev[32 * w] != 0xff) continue;
+                    lev[32 * w] = (unsigned char)(du + 1);
+                    que[32 * tail++] = (unsigned char)w;
+                    if (w == dst) { found = true; break; }
+                }
+            }
+            if (found) {
+                L = lev[32 * dst];
+                que[32 * L] = (unsigned char)dst;           // the path's nodes, src first
+                int x = dst;
+                for (int l = L - 1; l >= 0 && !bad; --l) {
+                    int best = n, be = -1;
+                    for (int j = v.row[x], je = v.row[x + 1]; j < je; ++j) {
+                        const uint32_t a = v.arc[j];
+                        const int e = (int)(a >> NR_WIDE_HEAD_BITS), w = (int)(a & HM);
+                        if (lev[32 * w] != l || state(e) == NR_EDGE_DOWN) continue;
+                        if (w < best) { best = w; be = e; }
+                    }
+                    if (be < 0) { bad = true; break; }
+                    nch += state(be) == NR_EDGE_UNKNOWN;
+                    que[32 * l] = (unsigned char)best;
+                    x = best;
+                }
+                if (!bad && x != src) bad = true;
+            }
+        }
+    }
+    if (bad) {                                              // an internal check failed: no children
+        atomicOr(status, NR_DEV_ERR_BOUNDS);
+        nch = 0;
+        L = -1;
+        active = false;
+    }
+    // the warp's children take one range of slots
+    int pre = nch;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int t = __shfl_up_sync(NR_FULL, pre, off);
+        if (lane >= off) pre += t;
+    }
+    const int total = __shfl_sync(NR_FULL, pre, 31);
+    unsigned long long base = 0;
+    if (lane == 0 && total > 0) base = atomicAdd(O.count, (unsigned long long)total);
+    base = __shfl_sync(NR_FULL, base, 0);
+    unsigned long long q = base + (unsigned long long)(pre - nch);
+    if (L < 0) {
+        if (active) A.dead++;
+        return;
+    }
+    double Pm = mass;
+    for (int h = 0; h < L; ++h) {
+        const int u = que[32 * h], x = que[32 * (h + 1)];
+        int e = 0;
+        for (int j = v.row[x], je = v.row[x + 1]; j < je; ++j)
+            if ((int)(v.arc[j] & HM) == u) { e = (int)(v.arc[j] >> NR_WIDE_HEAD_BITS); break; }
+        const int wi = e >> 4, sh = (e & 15) << 1;
+        const uint32_t wv = mc[32 * wi];
+        if (((wv >> sh) & 3u) != 3u) continue;              // only UNKNOWN hops branch
+        const double pe = v.p[e];
+        const double cm = __dmul_rn(Pm, __dsub_rn(1.0, pe));
+        Pm = __dmul_rn(Pm, pe);
+        if (q < O.cap) {
+            uint4 *d = O.mask + q * W4;
+#pragma unroll
+            for (int kk = 0; kk < W4; ++kk) {
+                uint32_t r[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int k = 4 * kk + i;
+                    r[i] = (k == wi) ? (wv & ~(3u << sh)) : mc[32 * k];
+                }
+                __stcg(d + kk, make_uint4(r[0], r[1], r[2], r[3]));
+            }
+            __stcg(O.mass + q, cm);
+            nr_fix_add_mass(A.net, cm);
+            if (O.key) {
+                const int b = nr_bucket(cm, O.shift, O.nb);
+                __stcg(O.key + q, (unsigned char)b);
+                atomicAdd(&O.hist[b], 1u);
+            }
+        } else {                                            // queue full (main.cu:245-252)
+            A.spilled++;
+            nr_fix_add_mass(A.es, cm);
+        }
+        mc[32 * wi] = wv & ~(2u << sh);                     // this hop is up in later children
+        ++q;
+    }
+    A.leaves++;
+    nr_fix_add_mass(A.R, Pm);
+}
+
 // LEARN: the learned branch order (NR_BORDER_LEARNED), with the scorer's scratch per warp.
-template <int W4, bool LEARN = false>
-__global__ void __launch_bounds__(NR_WIDE_BLOCK, LEARN ? 3 : 6) nr_bucket_wide_kernel(NrBucketWideParams P)
+// LANES: one lane per subproblem (nr_wide_lane_step), with its scratch per warp.
+template <int W4, bool LEARN = false, bool LANES = false>
+__global__ void __launch_bounds__(NR_WIDE_BLOCK, LEARN ? 3 : LANES ? 2 : 6) nr_bucket_wide_kernel(NrBucketWideParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_hist[NR_WIDE_MAX_NB + 1];
@@ -1197,6 +1378,17 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK, LEARN ? 3 : 6) nr_bucket_wide_k
     const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const unsigned long long TW = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long cap = P.capacity;
+    // LANES: the lane's mask, level and queue columns, and its sums
+    uint32_t *lmc = nullptr;
+    unsigned char *ldq = nullptr;
+    NrWideLaneAcc LA;
+    if constexpr (LANES) {
+        unsigned char *lb = smem + nr_wide_block_shm(g, (int)(blockDim.x >> 5)) +
+                            (size_t)warp * nr_wide_lane_shm(g.n, W4);
+        lmc = reinterpret_cast<uint32_t *>(lb) + lane;
+        ldq = lb + (size_t)4 * W4 * 32 * 4 + lane;
+        nr_wide_lane_acc_zero(LA);
+    }
     __shared__ NrWideAcc s_acc[NR_WIDE_BLOCK / 32];          // as in nr_grid_wide_kernel
     NrWideAcc &A = s_acc[warp];
     if (lane == 0) nr_wide_acc_init(A);
@@ -1254,12 +1446,40 @@ __global__ void __launch_bounds__(NR_WIDE_BLOCK, LEARN ? 3 : 6) nr_bucket_wide_k
             P.wave_len[(wave + 1) & 1] = 0;
             if (n_in > P.stats[0]) P.stats[0] = n_in;
         }
-        for (unsigned long long idx = gw; idx < n_in; idx += TW) {
-            const unsigned long long s = __ldcg(P.list + idx);
-            nr_wide_load_mask(v.m, P.mask + s * w4, w4);
-            const double mass = __ldcg(P.mass + s);
-            __syncwarp();
-            nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0, P.border, LEARN ? &W : nullptr);
+        // LANES: a wave of at least lane_min_wave records takes one lane a record; a smaller one
+        // the whole warp a record (a lane's search is a long serial chain: in a wave that leaves
+        // most lanes idle the warp's parallel search ends sooner)
+        bool lane_wave = false;
+        if constexpr (LANES) lane_wave = n_in >= P.lane_min_wave;
+        if (lane_wave) {
+            if constexpr (LANES) {
+                for (unsigned long long b0 = gw * 32; b0 < n_in; b0 += TW * 32) {
+                    const unsigned long long idx = b0 + lane;
+                    const bool valid = idx < n_in;
+                    double mass = 0.0;
+                    if (valid) {
+                        const unsigned long long s = __ldcg(P.list + idx);
+#pragma unroll
+                        for (int k = 0; k < W4; ++k) {
+                            const uint4 q = __ldcg(P.mask + s * W4 + k);
+                            lmc[32 * (4 * k)] = q.x; lmc[32 * (4 * k + 1)] = q.y;
+                            lmc[32 * (4 * k + 2)] = q.z; lmc[32 * (4 * k + 3)] = q.w;
+                        }
+                        mass = __ldcg(P.mass + s);
+                    }
+                    nr_wide_lane_step<W4>(g, v, lmc, ldq, valid, mass, P.eps, O, LA, P.status);
+                    __syncwarp();
+                }
+                nr_wide_lane_fold(LA, A);
+            }
+        } else {
+            for (unsigned long long idx = gw; idx < n_in; idx += TW) {
+                const unsigned long long s = __ldcg(P.list + idx);
+                nr_wide_load_mask(v.m, P.mask + s * w4, w4);
+                const double mass = __ldcg(P.mass + s);
+                __syncwarp();
+                nr_wide_step<W4>(g, v, mass, P.eps, O, A, P.fork != 0, P.border, LEARN ? &W : nullptr);
+            }
         }
         __syncthreads();
         for (int b = threadIdx.x; b < P.nb; b += blockDim.x)
