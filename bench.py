@@ -828,7 +828,7 @@ def run_case(args):
 
 def k15_orders(ctx, w, batch, tuned, flush):
     """K15 time-to-bound under each order: single instances (in-kernel time, 16 seeds) and the
-    4096-instance batch (device time); plain max-mass is the learned order's judge."""
+    4096-instance batch (device time); plain max-mass is what the learned order is compared with."""
     from relaibilitygpu_gb300 import learned as LR
     cmp_opts = {k: v for k, v in tuned.items() if k not in ("order", "bucket_shift", "n_buckets")}
 
